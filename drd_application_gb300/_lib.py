@@ -1,0 +1,66 @@
+"""Loads libdrd_gb300.so and declares its C-ABI for ctypes.
+
+There is no fallback: if the library is missing or fails to load, every entry point of
+this package raises.  Build it with drd_application_gb300.build.build().
+"""
+import ctypes as C
+import os
+
+from . import abi
+from .build import lib_path
+
+_LIB = None
+
+# Every symbol include/drd_gb300.h declares, with its ctypes signature.
+_dp = C.POINTER(C.c_double)
+_ctx = C.c_void_p
+_st = C.POINTER(abi.drd_status)
+SIGNATURES = {
+    "drd_abi_version": (C.c_int, []),
+    "drd_create": (C.c_int, [C.POINTER(abi.drd_params), C.POINTER(C.c_void_p)]),
+    "drd_destroy": (C.c_int, [_ctx]),
+    "drd_set_params": (C.c_int, [_ctx, C.POINTER(abi.drd_params)]),
+    "drd_last_error": (C.c_char_p, [_ctx]),
+    "drd_set_coefs": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "drd_set_tp_fields": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
+    "drd_interpolate_coef": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
+    "drd_phsolve": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp, _st]),
+    "drd_ph_mu_solve": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp, _dp, _dp, _st]),
+    "drd_velosolve_combined": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp, _dp, _dp, _dp,
+                                         _dp, _st]),
+    "drd_velosolve_2_combined": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double,
+                                           _dp, _dp, _dp, _dp, _dp, _dp, _st]),
+    "drd_presolve_2": (C.c_int, [_ctx, _dp, _dp, C.c_double, _dp, _st]),
+    "drd_mass": (C.c_int, [_ctx, _dp, _dp]),
+    "drd_state_upload": (C.c_int, [_ctx, C.c_int, _dp]),
+    "drd_state_download": (C.c_int, [_ctx, C.c_int, _dp]),
+    "drd_state_device_ptr": (C.c_int, [_ctx, C.c_int, C.POINTER(_dp)]),
+    "drd_step": (C.c_int, [_ctx, C.c_int, C.c_double, C.POINTER(abi.drd_step_stats)]),
+    "drd_steps_async": (C.c_int, [_ctx, C.c_int, C.c_double, C.c_int]),
+    "drd_synchronize": (C.c_int, [_ctx]),
+    "drd_op_apply": (C.c_int, [_ctx, C.c_int, C.c_int, C.c_int, _dp, _dp]),
+    "drd_op_length": (C.c_long, [_ctx, C.c_int]),
+    "drd_kernel_launches": (C.c_int64, [_ctx]),
+    "drd_stream": (C.c_void_p, [_ctx]),
+}
+
+
+def load(path=None):
+    """Load (once) and return the CUDA library with its signatures declared."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    path = path or lib_path()
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build the CUDA library first "
+                           "(python -m drd_application_gb300.build); there is no CPU fallback")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.drd_abi_version() != abi.DRD_ABI_VERSION:
+        raise RuntimeError("libdrd_gb300.so ABI version does not match drd_application_gb300.abi")
+    if path == lib_path():
+        _LIB = lib
+    return lib

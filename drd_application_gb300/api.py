@@ -1,0 +1,214 @@
+"""Python mirror of the reference's per-step subroutine interface over the C-ABI.
+
+Method names and argument order follow the Fortran subroutines
+(microfluidics_complex_domain/PhSolve.f90:1, VeloSolve_combined.f90:5,
+VeloSolve_2_combined.f90:4, PreSolve_2.f90:1, two_phase_flow_complex_domain/ph_mu_solve.f90:3);
+the module-global inputs those subroutines read are set once with set_coefs /
+set_tp_fields or passed explicitly.  Arrays are numpy float64 with the Fortran ghosted
+shapes of drd_application_gb300.layout.  Every call runs the CUDA library; a missing
+library raises.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi, _lib
+from .layout import cell_shape, ptr, u_shape, v_shape
+
+
+class DRDError(RuntimeError):
+    pass
+
+
+def _check_shape(a, shape, name):
+    if a is None:
+        return None
+    if not isinstance(a, np.ndarray) or a.shape != shape or a.dtype != np.float64:
+        raise ValueError(f"{name}: expected float64 array of shape {shape}")
+    return np.ascontiguousarray(a)
+
+
+class DRDContext:
+    """One GPU context for an nr x nz grid (drd_create / drd_destroy)."""
+
+    def __init__(self, params, lib=None):
+        self.L = lib or _lib.load()
+        self.P = params.copy()
+        h = C.c_void_p()
+        rc = self.L.drd_create(C.byref(self.P), C.byref(h))
+        if rc != 0:
+            raise DRDError(f"drd_create failed with {rc}")
+        self.h = h
+        self.nr, self.nz = params.nr, params.nz
+        self.cs, self.us, self.vs = cell_shape(self.nr, self.nz), u_shape(self.nr, self.nz), v_shape(self.nr, self.nz)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.drd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -------------------------------------------------------------------------------------
+    def _rc(self, rc, what, allow_info=True):
+        if rc == 0:
+            return rc
+        if allow_info and (rc > 0 or rc in (-10, -11)):
+            return rc  # BiCGSTAB INFO: the reference prints it and continues
+        msg = self.L.drd_last_error(self.h)
+        raise DRDError(f"{what} failed with {rc}: {msg.decode() if msg else ''}")
+
+    def set_params(self, params):
+        self.P = params.copy()
+        self._rc(self.L.drd_set_params(self.h, C.byref(self.P)), "drd_set_params", False)
+
+    def set_coefs(self, rho=None, eta=None, bdr_ph=None, bdr_ph_grad=None, ph_M_0=None, ph_M_inner=None):
+        a = [_check_shape(x, self.cs, n) for x, n in ((rho, "rho"), (eta, "eta"), (bdr_ph, "bdr_ph"),
+                                                        (bdr_ph_grad, "bdr_ph_grad"), (ph_M_0, "ph_M_0"),
+                                                        (ph_M_inner, "ph_M_inner"))]
+        self._rc(self.L.drd_set_coefs(self.h, *[ptr(x) for x in a]), "drd_set_coefs", False)
+
+    def set_tp_fields(self, bdr_ph_used=None, bdr_ph_penalty=None, angleB=None, angleT=None):
+        a = [_check_shape(bdr_ph_used, self.cs, "bdr_ph_used"), _check_shape(bdr_ph_penalty, self.cs, "bdr_ph_penalty")]
+        ang = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (angleB, angleT)]
+        for x in ang:
+            if x is not None and x.shape != (self.nr + 1,):
+                raise ValueError("angle arrays have nr+1 entries")
+        self._rc(self.L.drd_set_tp_fields(self.h, ptr(a[0]), ptr(a[1]), ptr(ang[0]), ptr(ang[1])),
+                 "drd_set_tp_fields", False)
+
+    def set_case(self, case):
+        """Load the coefficient fields of a workloads.Case."""
+        k = case.coefs
+        self.set_coefs(k["rho"], k["eta"], k["bdr_ph"], k["bdr_ph_grad"], k["M0"], k["Mi"])
+        if self.P.variant == abi.DRD_VARIANT_TP:
+            self.set_tp_fields(k["bdr_used"], k["bdr_pen"])
+
+    # ---- the reference subroutines --------------------------------------------------------
+    def interpolate_coef(self, dist):
+        dist = np.ascontiguousarray(dist, dtype=np.float64)
+        if dist.shape != (self.nz, self.nr):
+            raise ValueError("dist has shape (nz, nr)")
+        fpd, rho, eta = (np.zeros(self.cs) for _ in range(3))
+        self._rc(self.L.drd_interpolate_coef(self.h, ptr(dist), ptr(fpd), ptr(rho), ptr(eta)), "interpolate_coef", False)
+        return fpd, rho, eta
+
+    def PhSolve(self, u, v, ph, rmu, t):
+        """PhSolve(rmu_after, ph_after, t) -> (rmu_after, ph_after, status)."""
+        u, v = _check_shape(u, self.us, "u"), _check_shape(v, self.vs, "v")
+        ph, rmu = _check_shape(ph, self.cs, "ph"), _check_shape(rmu, self.cs, "rmu")
+        rmu_after, ph_after = np.zeros(self.cs), np.zeros(self.cs)
+        st = abi.drd_status()
+        self._rc(self.L.drd_phsolve(self.h, ptr(u), ptr(v), ptr(ph), ptr(rmu), t, ptr(rmu_after), ptr(ph_after),
+                                    C.byref(st)), "PhSolve")
+        return rmu_after, ph_after, st
+
+    def ph_mu_solve(self, u, v, ph, rmu, t):
+        """ph_mu_solve(ph_after, rmu_after, t) -> (ph_after, rmu_after, ph_M_0, (coef_bot, coef_top), status)."""
+        u, v = _check_shape(u, self.us, "u"), _check_shape(v, self.vs, "v")
+        ph, rmu = _check_shape(ph, self.cs, "ph"), _check_shape(rmu, self.cs, "rmu")
+        ph_after, rmu_after, M0 = np.zeros(self.cs), np.zeros(self.cs), np.zeros(self.cs)
+        cbt = np.zeros(2)
+        st = abi.drd_status()
+        self._rc(self.L.drd_ph_mu_solve(self.h, ptr(u), ptr(v), ptr(ph), ptr(rmu), t, ptr(ph_after), ptr(rmu_after),
+                                        ptr(M0), ptr(cbt), C.byref(st)), "ph_mu_solve")
+        return ph_after, rmu_after, M0, tuple(cbt), st
+
+    def VeloSolve_combined(self, psi, u, v, p, rmu_after, ph_after, t, particle_force1=None, particle_force2=None):
+        """VeloSolve_combined(psi, u_after, v_after, rmu_after, ph_after, t, pf1, pf2)
+        -> (u_after, v_after, uL, uR, status)."""
+        args = [_check_shape(x, s, n) for x, s, n in ((u, self.us, "u"), (v, self.vs, "v"), (p, self.cs, "p"),
+                                                       (rmu_after, self.cs, "rmu_after"), (ph_after, self.cs, "ph_after"))]
+        pf = [_check_shape(x, self.cs, "particle_force") for x in (particle_force1, particle_force2)]
+        u_after, v_after = np.zeros(self.us), np.zeros(self.vs)
+        uL, uR = np.zeros(self.nz + 1), np.zeros(self.nz + 1)
+        st = abi.drd_status()
+        self._rc(self.L.drd_velosolve_combined(self.h, ptr(_check_shape(psi, self.cs, "psi")), *[ptr(x) for x in args],
+                                               t, ptr(pf[0]), ptr(pf[1]), ptr(u_after), ptr(v_after), ptr(uL), ptr(uR),
+                                               C.byref(st)), "VeloSolve_combined")
+        return u_after, v_after, uL, uR, st
+
+    def VeloSolve_2_combined(self, psi1, psi2, u_pre, u, v_pre, v, p, ph_pre, ph_after, rmu_pre, rmu_after, t,
+                             particle_force1=None, particle_force2=None):
+        """VeloSolve_2_combined(psi1, psi2, u_pre, u_after, v_pre, v_after, ph_pre, ph_after, rmu_pre,
+        rmu_after, t, pf1, pf2) -> (u_after, v_after, uL, uR, status)."""
+        cs, us, vs = self.cs, self.us, self.vs
+        a = [_check_shape(x, s, n) for x, s, n in (
+            (psi1, cs, "psi1"), (psi2, cs, "psi2"), (u_pre, us, "u_pre"), (u, us, "u"), (v_pre, vs, "v_pre"),
+            (v, vs, "v"), (p, cs, "p"), (ph_pre, cs, "ph_pre"), (ph_after, cs, "ph_after"), (rmu_pre, cs, "rmu_pre"),
+            (rmu_after, cs, "rmu_after"))]
+        pf = [_check_shape(x, cs, "particle_force") for x in (particle_force1, particle_force2)]
+        u_after, v_after = np.zeros(us), np.zeros(vs)
+        uL, uR = np.zeros(self.nz + 1), np.zeros(self.nz + 1)
+        st = abi.drd_status()
+        self._rc(self.L.drd_velosolve_2_combined(self.h, *[ptr(x) for x in a], t, ptr(pf[0]), ptr(pf[1]),
+                                                 ptr(u_after), ptr(v_after), ptr(uL), ptr(uR), C.byref(st)),
+                 "VeloSolve_2_combined")
+        return u_after, v_after, uL, uR, st
+
+    def PreSolve_2(self, u, v, coef):
+        """PreSolve_2(plan, plan_back, psi, coef) -> psi (the FFTW plans live in the context)."""
+        u, v = _check_shape(u, self.us, "u"), _check_shape(v, self.vs, "v")
+        psi = np.zeros(self.cs)
+        st = abi.drd_status()
+        self._rc(self.L.drd_presolve_2(self.h, ptr(u), ptr(v), coef, ptr(psi), C.byref(st)), "PreSolve_2", False)
+        return psi
+
+    def mass(self, ph):
+        ph = _check_shape(ph, self.cs, "ph")
+        m = C.c_double()
+        self._rc(self.L.drd_mass(self.h, ptr(ph), C.byref(m)), "mass", False)
+        return m.value
+
+    # ---- resident state --------------------------------------------------------------------
+    def upload_state(self, state):
+        for fid, arr in state.items():
+            shape = {"u": self.us, "v": self.vs, "cell": self.cs}[abi.FIELD_KIND[fid]]
+            self._rc(self.L.drd_state_upload(self.h, fid, ptr(_check_shape(arr, shape, f"field {fid}"))),
+                     "state_upload", False)
+
+    def download_state(self, fields=None):
+        out = {}
+        for fid in (fields if fields is not None else range(abi.F_COUNT)):
+            shape = {"u": self.us, "v": self.vs, "cell": self.cs}[abi.FIELD_KIND[fid]]
+            a = np.zeros(shape)
+            self._rc(self.L.drd_state_download(self.h, fid, ptr(a)), "state_download", False)
+            out[fid] = a
+        return out
+
+    def step(self, first, t, stats=True):
+        st = abi.drd_step_stats() if stats else None
+        self._rc(self.L.drd_step(self.h, int(first), t, C.byref(st) if st is not None else None), "drd_step", False)
+        return st
+
+    def steps_async(self, first, t, n):
+        self._rc(self.L.drd_steps_async(self.h, int(first), t, int(n)), "drd_steps_async", False)
+
+    def synchronize(self):
+        self._rc(self.L.drd_synchronize(self.h), "drd_synchronize", False)
+
+    def op_apply(self, op, x, bdf=2, precision=abi.DRD_PREC_FP64):
+        """y = op(x) for one of the DRD_OP_* operators (verification access)."""
+        n = self.L.drd_op_length(self.h, op)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.shape != (n,):
+            raise ValueError(f"operator {op} acts on vectors of length {n}")
+        y = np.zeros(n)
+        self._rc(self.L.drd_op_apply(self.h, op, bdf, precision, ptr(x), ptr(y)), "drd_op_apply", False)
+        return y
+
+    def kernel_launches(self):
+        return int(self.L.drd_kernel_launches(self.h))
+
+    def stream(self):
+        return self.L.drd_stream(self.h)

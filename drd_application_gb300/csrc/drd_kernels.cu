@@ -1,0 +1,1357 @@
+// drd_kernels.cu — sm_103a kernels of the DRD-Micro per-time-step solver core.
+//
+// Every kernel is written against the reference line it replaces (cited at the kernel).
+// Floating-point expressions keep the reference's left-to-right evaluation order so that
+// the FP64 path agrees with the FP64 CPU restatement to rounding (FMA contraction aside).
+// Kernels that take a Krylov state `ks` and a gate return immediately when the solve has
+// left the state they belong to, so a fixed launch sequence (a captured CUDA graph) can
+// express BiCGSTAB's early exits.
+#include <math.h>
+
+#include "drd_kernels.cuh"
+
+namespace drd {
+
+static __device__ __forceinline__ bool gate_closed(const KState* ks, int gate) {
+    if (gate == G_ALWAYS || ks == nullptr) return false;
+    const int ph = *((volatile const int*)&ks->phase);
+    if (gate == G_RUNNING) return ph != PH_RUNNING;
+    if (gate == G_XNZ) return ph != PH_RUNNING || ks->x_nonzero == 0;
+    if (gate == G_EARLY_OR_RUNNING) return ph == PH_DONE;
+    return false;
+}
+
+static inline int grid_for(long n, int per_thread = 2) {
+    long b = (n + (long)DRD_TPB * per_thread - 1) / ((long)DRD_TPB * per_thread);
+    if (b < 1) b = 1;
+    if (b > 4096) b = 4096;
+    return (int)b;
+}
+
+// ======================================================================================
+// op_double_gradient_Neum (microfluidics_complex_domain/matrix_tool.f90:178-219) at (i,k):
+// variable-coefficient 5-point operator with face mobility (M_i + M_nb)/2 and zero flux
+// through the domain faces.  Reads interior values only.
+// ======================================================================================
+template <typename T, class XA, class MA>
+__device__ __forceinline__ T op_dgn(int i, int k, int nr, int nz, T idx2, T idz2, const XA& x, const MA& mo) {
+    const T h = T(0.5);
+    T acc = T(0);
+    const T m0 = mo(i, k), x0 = x(i, k);
+    T moL, moR;
+    if (i == 0) {
+        moL = (m0 + m0) * h;
+        moR = (m0 + mo(i + 1, k)) * h;
+        acc = acc + idx2 * (moL * x0 + moR * x(i + 1, k) - (moL + moR) * x0);
+    } else if (i == nr - 1) {
+        moL = (mo(i - 1, k) + m0) * h;
+        moR = (m0 + m0) * h;
+        acc = acc + idx2 * (moL * x(i - 1, k) + moR * x0 - (moL + moR) * x0);
+    } else {
+        moL = (mo(i - 1, k) + m0) * h;
+        moR = (m0 + mo(i + 1, k)) * h;
+        acc = acc + idx2 * (moL * x(i - 1, k) + moR * x(i + 1, k) - (moL + moR) * x0);
+    }
+    if (k == 0) {
+        moL = (m0 + m0) * h;
+        moR = (m0 + mo(i, k + 1)) * h;
+        acc = acc + idz2 * (moL * x0 + moR * x(i, k + 1) - (moL + moR) * x0);
+    } else if (k == nz - 1) {
+        moL = (mo(i, k - 1) + m0) * h;
+        moR = (m0 + m0) * h;
+        acc = acc + idz2 * (moL * x(i, k - 1) + moR * x0 - (moL + moR) * x0);
+    } else {
+        moL = (mo(i, k - 1) + m0) * h;
+        moR = (m0 + mo(i, k + 1)) * h;
+        acc = acc + idz2 * (moL * x(i, k - 1) + moR * x(i, k + 1) - (moL + moR) * x0);
+    }
+    return acc;
+}
+
+template <typename T>
+struct PackedA {
+    const T* p; int nr;
+    __device__ __forceinline__ T operator()(int i, int k) const { return p[i + (long)nr * k]; }
+};
+template <typename T>
+struct CellA {
+    const T* p; int nr;
+    __device__ __forceinline__ T operator()(int i, int k) const { return p[cidx(nr, i, k)]; }
+};
+
+// Block-level accumulation of up to two dot products into the partials buffer.
+template <int NT>
+__device__ __forceinline__ void emit_partials(double a1, double a2, int n1, int n2, const Dots& d, int slot1) {
+    __shared__ double sm[32];
+    if (n1) {
+        double r = block_sum<NT>(a1, sm);
+        if (threadIdx.x == 0) d.part[slot1 * DRD_MAXB + blockIdx.x] = r;
+    }
+    if (n2) {
+        double r = block_sum<NT>(a2, sm);
+        if (threadIdx.x == 0) d.part[(slot1 + 1) * DRD_MAXB + blockIdx.x] = r;
+    }
+}
+
+// ======================================================================================
+// CH (microfluidics_complex_domain/PhSolve.f90)
+// ======================================================================================
+
+// f2 = ph - dt u.grad(ph) (:26-34) on the whole CELL array (ghosts keep ph).
+__global__ void k_ch_f2(DevParams P, const double* __restrict__ u, const double* __restrict__ v,
+                        const double* __restrict__ ph, double* __restrict__ f2, ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz;
+    const long cs = (long)(nr + 2) * (nz + 2);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < cs; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % (nr + 2)) - 1, k = (int)(q / (nr + 2)) - 1;
+        double val = ph[q];
+        if (i >= 0 && i < nr && k >= 0 && k < nz) {
+            val = val - P.dt * (u[uidx(nr, i + 1, k)] + u[uidx(nr, i, k)]) / 2.0 *
+                            (ph[cidx(nr, i + 1, k)] - ph[cidx(nr, i - 1, k)]) / 2.0 / P.dr -
+                  P.dt * (v[vidx(nr, i, k + 1)] + v[vidx(nr, i, k)]) / 2.0 *
+                      (ph[cidx(nr, i, k + 1)] - ph[cidx(nr, i, k - 1)]) / 2.0 / P.dz;
+        }
+        f2[q] = val;
+    }
+}
+
+// ch_bulk_energy (microfluidics_complex_domain/ch_bulk_energy.f90:20-22).
+__device__ __forceinline__ double bulk_mf(double phi, double psi) {
+    double aa = (phi * phi) * ((1.0 - phi) * (1.0 - phi));
+    aa = 1.0 - sqrt(aa / (aa + 1.0E-2)) * psi;
+    return 0.5 * phi * (1.0 - phi) * (1.0 - 2.0 * phi) * aa;
+}
+
+// rhs = -f1 + s f2/eps - eps L_Mi(f2) (:37-48) packed by Atob; x0 = Atob(rmu) (:62-63).
+__global__ void k_ch_rhs(DevParams P, const double* __restrict__ ph, const double* __restrict__ rmu,
+                         const double* __restrict__ bdr, const double* __restrict__ grad,
+                         const double* __restrict__ Mi, const double* __restrict__ f2, double* __restrict__ b,
+                         double* __restrict__ x, ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz;
+    const long n = (long)nr * nz;
+    CellA<double> F{f2, nr}, M{Mi, nr};
+    const double sq2 = sqrt(2.0);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        const long c = cidx(nr, i, k);
+        const double p0 = ph[c];
+        double f1 = P.s * p0 / P.eps - bulk_mf(p0, bdr[c]) / P.eps - p0 * (p0 - 1.0) * grad[c] * P.cang / sq2;
+        const double ff = op_dgn<double>(i, k, nr, nz, P.idr2, P.idz2, F, M);
+        b[q] = -f1 + P.s * f2[c] / P.eps - P.eps * ff;
+        x[q] = rmu[c];
+    }
+}
+
+// MATRIX_VECTOR_CG (:240-292), first half: ff1 = -(dt xld) L_M0(x).
+template <typename T>
+__global__ void k_ch_mv1(OpScal<T> o, const T* __restrict__ M0, const T* __restrict__ x, T* __restrict__ ff1,
+                         const KState* ks, int gate, ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, gate)) return;
+    const int nr = o.nr, nz = o.nz;
+    const long n = (long)nr * nz;
+    PackedA<T> X{x, nr};
+    CellA<T> M{M0, nr};
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        ff1[q] = -(o.dtxld * op_dgn<T>(i, k, nr, nz, o.idr2, o.idz2, X, M));
+    }
+}
+
+// Second half: y = alpha (x + s ff1/eps - eps L_Mi(ff1)) + beta y, with optional partial dots.
+template <typename T>
+__global__ void k_ch_mv2(OpScal<T> o, const T* __restrict__ Mi, const T* __restrict__ x, const T* __restrict__ ff1,
+                         T alpha, T beta, T* y, const T* dot1, int self2, Dots d, int slot1, const KState* ks,
+                         int gate, ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, gate)) return;
+    const int nr = o.nr, nz = o.nz;
+    const long n = (long)nr * nz;
+    PackedA<T> F{ff1, nr};
+    CellA<T> M{Mi, nr};
+    double a1 = 0.0, a2 = 0.0;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        const T f = ff1[q];
+        const T a = o.s * f / o.eps - o.eps * op_dgn<T>(i, k, nr, nz, o.idr2, o.idz2, F, M);
+        const T av = x[q] + a;
+        const T yn = (beta == T(0)) ? alpha * av : alpha * av + beta * y[q];
+        y[q] = yn;
+        if (dot1) a1 += (double)dot1[q] * (double)yn;
+        if (self2) a2 += (double)yn * (double)yn;
+    }
+    if (dot1 != nullptr || self2) emit_partials<DRD_TPB>(a1, a2, dot1 != nullptr, self2, d, slot1);
+}
+
+// rmu_after interior (:85) and ph_after = f2 + dt xld L_M0(rmu_after) interior (:100-101).
+__global__ void k_ch_fin(DevParams P, const double* __restrict__ x, const double* __restrict__ f2,
+                         const double* __restrict__ M0, double* __restrict__ rmu_after, double* __restrict__ ph_after,
+                         ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz;
+    const long n = (long)nr * nz;
+    PackedA<double> X{x, nr};
+    CellA<double> M{M0, nr};
+    const double dtxld = P.dt * P.xld;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        const long c = cidx(nr, i, k);
+        rmu_after[c] = x[q];
+        ph_after[c] = f2[c] + dtxld * op_dgn<double>(i, k, nr, nz, P.idr2, P.idz2, X, M);
+    }
+}
+
+// Neumann ghost copies of CELL fields: the ghost takes the nearest interior value, which is
+// the net effect of the reference's two loops (e.g. PhSolve.f90:88-96, dct_fftw.f90:175-183).
+__global__ void k_fill_neumann(int nr, int nz, double* a, double* b, ull* ctr) {
+    count_launch(ctr);
+    const long ng = 2L * (nr + 2) + 2L * nz;
+    for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < ng; g += (long)gridDim.x * blockDim.x) {
+        int i, k;
+        if (g < nr + 2) { i = (int)g - 1; k = -1; }
+        else if (g < 2L * (nr + 2)) { i = (int)(g - (nr + 2)) - 1; k = nz; }
+        else {
+            const long h = g - 2L * (nr + 2);
+            k = (int)(h >> 1);
+            i = (h & 1) ? nr : -1;
+        }
+        const int si = i < 0 ? 0 : (i > nr - 1 ? nr - 1 : i);
+        const int sk = k < 0 ? 0 : (k > nz - 1 ? nz - 1 : k);
+        const long dst = cidx(nr, i, k), src = cidx(nr, si, sk);
+        a[dst] = a[src];
+        if (b) b[dst] = b[src];
+    }
+}
+
+// ======================================================================================
+// Coupled CH (two_phase_flow_complex_domain/ph_mu_solve.f90)
+// ======================================================================================
+
+// M0 = (1-bdr) W(ph) (:31-35) and f2 = ph (used + adjust) - dt u.grad(ph used) (:40-51).
+__global__ void k_phmu_prep(DevParams P, const double* __restrict__ u, const double* __restrict__ v,
+                            const double* __restrict__ ph, const double* __restrict__ bdr,
+                            const double* __restrict__ used, double* __restrict__ M0, double* __restrict__ f2,
+                            ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz;
+    const long cs = (long)(nr + 2) * (nz + 2);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < cs; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % (nr + 2)) - 1, k = (int)(q / (nr + 2)) - 1;
+        const double p0 = ph[q];
+        if (P.phi_mode == 1) M0[q] = (1.0 - bdr[q]) * (p0 * p0) * ((p0 - 1.0) * (p0 - 1.0));
+        else M0[q] = (1.0 - bdr[q]) * ((p0 * p0 - 1.0) * (p0 * p0 - 1.0));
+        double val = p0 * (used[q] + P.adjust);
+        if (i >= 0 && i < nr && k >= 0 && k < nz) {
+            val = val -
+                  P.dt * (u[uidx(nr, i + 1, k)] + u[uidx(nr, i, k)]) / 2.0 *
+                      (ph[cidx(nr, i + 1, k)] * used[cidx(nr, i + 1, k)] - ph[cidx(nr, i - 1, k)] * used[cidx(nr, i - 1, k)]) /
+                      2.0 / P.dr -
+                  P.dt * (v[vidx(nr, i, k + 1)] + v[vidx(nr, i, k)]) / 2.0 *
+                      (ph[cidx(nr, i, k + 1)] * used[cidx(nr, i, k + 1)] - ph[cidx(nr, i, k - 1)] * used[cidx(nr, i, k - 1)]) /
+                      2.0 / P.dz;
+        }
+        f2[q] = val;
+    }
+}
+
+// ch_bulk_energy (two_phase_flow_complex_domain/ch_bulk_energy.f90:39-58).
+__device__ __forceinline__ double bulk_tp(double phi, double psi, int mode) {
+    if (mode == 1) return 0.5 * phi * (1.0 - phi) * (1.0 - 2.0 * phi) * (1 - psi);
+    return (phi * phi * phi - phi) * (1 - psi);
+}
+
+// rhs [f1; f2] (:55-153) with the wall terms of ch_bdr_condition (:108-149); cfB/cfT hold
+// cos(angle pi/180)/sqrt(2) per column.
+__global__ void k_phmu_rhs(DevParams P, const double* __restrict__ ph, const double* __restrict__ rmu,
+                           const double* __restrict__ bdr, const double* __restrict__ grad,
+                           const double* __restrict__ f2, const double* __restrict__ cfB,
+                           const double* __restrict__ cfT, double* __restrict__ b, double* __restrict__ x,
+                           double* __restrict__ pnb, double* __restrict__ pnt, ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz, mode = P.phi_mode;
+    const long n = (long)nr * nz;
+    const double sq2 = sqrt(2.0);
+    const double tmp = P.eps / P.dz;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        const long c = cidx(nr, i, k);
+        const double p0 = ph[c];
+        const double wet = (mode == 1) ? p0 * (p0 - 1.0) : (p0 * p0 - 1.0);
+        double f1 = P.s * p0 / P.eps - bulk_tp(p0, bdr[c], mode) / P.eps - wet * grad[c] * P.cang / sq2;
+        if (k == 0) {
+            const double pb = (ph[cidx(nr, i, -1)] + ph[cidx(nr, i, 0)]) / 2.0;
+            double val = (mode == 1) ? cfB[i] * (1.0 - pb) * pb : cfB[i] * (1.0 - pb * pb);
+            val = val / tmp;
+            pnb[i] = val;
+            f1 = f1 + val * P.eps / P.dz2;
+        }
+        if (k == nz - 1) {
+            const double pt = (ph[cidx(nr, i, nz - 1)] + ph[cidx(nr, i, nz)]) / 2.0;
+            double val = (mode == 1) ? cfT[i] * (1.0 - pt) * pt : cfT[i] * (1.0 - pt * pt);
+            val = val / tmp;
+            pnt[i] = val;
+            f1 = f1 + val * P.eps / P.dz2;
+        }
+        b[q] = f1;
+        b[q + n] = f2[c];
+        x[q] = p0;
+        x[q + n] = rmu[c];
+    }
+}
+
+// MATRIX_VECTOR_PH_MU_CG (:203-299).  The ghost rows of phi are the Neumann copies of
+// btoA_ph_mu (matrix_tool.f90:120-126).
+template <typename T>
+__global__ void k_phmu_mv(OpScal<T> o, const T* __restrict__ M0, const T* __restrict__ Mi,
+                          const T* __restrict__ used, const T* __restrict__ x, T alpha, T beta, T* y, const T* dot1,
+                          int self2, Dots d, int slot1, const KState* ks, int gate, ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, gate)) return;
+    const int nr = o.nr, nz = o.nz;
+    const long n = (long)nr * nz;
+    PackedA<T> F1{x, nr}, F2{x + n, nr};
+    CellA<T> MI{Mi, nr}, MO{M0, nr};
+    const T epsdz2 = o.eps / o.dz2;
+    double a1 = 0.0, a2 = 0.0;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < 2 * n; q += (long)gridDim.x * blockDim.x) {
+        const long qq = q < n ? q : q - n;
+        const int i = (int)(qq % nr), k = (int)(qq / nr);
+        const long c = cidx(nr, i, k);
+        T val;
+        if (q < n) {
+            const T f1 = x[qq];
+            val = o.s * f1 / o.eps - o.eps * op_dgn<T>(i, k, nr, nz, o.idr2, o.idz2, F1, MI) - x[qq + n] * used[c];
+            if (k == 0) val = val + epsdz2 * (f1 - o.cb * f1);
+            if (k == nz - 1) val = val + epsdz2 * (f1 - o.ct * f1);
+        } else {
+            val = x[qq] * (used[c] + o.adjust) - o.dtxld * op_dgn<T>(i, k, nr, nz, o.idr2, o.idz2, F2, MO);
+        }
+        const T yn = (beta == T(0)) ? alpha * val : alpha * val + beta * y[q];
+        y[q] = yn;
+        if (dot1) a1 += (double)dot1[q] * (double)yn;
+        if (self2) a2 += (double)yn * (double)yn;
+    }
+    if (dot1 != nullptr || self2) emit_partials<DRD_TPB>(a1, a2, dot1 != nullptr, self2, d, slot1);
+}
+
+// Diagonal of PSolve_PH_MU_CG (:321-353) with its index tests exactly as written there.
+template <typename T>
+__global__ void k_phmu_diag(OpScal<T> o, T* __restrict__ diag, ull* ctr) {
+    count_launch(ctr);
+    const int nr = o.nr, nz = o.nz;
+    const long n = (long)nr * nz;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nr), j = (int)(q / nr);
+        const T tmpx = (i == 0 || j == nr - 1) ? T(1) / o.dr2 : T(2) / o.dr2;
+        const T tmpz = (i == 0 || j == nz - 1) ? T(1) / o.dz2 : T(2) / o.dz2;
+        diag[q] = (tmpx + tmpz) * o.eps + o.s / o.eps;
+        diag[q + n] = o.dtxld * (tmpx + tmpz);
+    }
+}
+
+// btoA_ph_mu + ghost rows of phi (:173-177).
+__global__ void k_phmu_fin(DevParams P, const double* __restrict__ x, const double* __restrict__ pnb,
+                           const double* __restrict__ pnt, double cb, double ct, double* __restrict__ ph_after,
+                           double* __restrict__ rmu_after, ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz;
+    const long n = (long)nr * nz;
+    const long cs = (long)(nr + 2) * (nz + 2);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < cs; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % (nr + 2)) - 1, k = (int)(q / (nr + 2)) - 1;
+        const int si = i < 0 ? 0 : (i > nr - 1 ? nr - 1 : i);
+        const int sk = k < 0 ? 0 : (k > nz - 1 ? nz - 1 : k);
+        const long s = si + (long)nr * sk;
+        double pv = x[s];
+        if (i >= 0 && i < nr && k == -1) pv = x[i] * cb + pnb[i];
+        if (i >= 0 && i < nr && k == nz) pv = x[i + (long)nr * (nz - 1)] * ct + pnt[i];
+        ph_after[q] = pv;
+        rmu_after[q] = x[s + n];
+    }
+}
+
+// ======================================================================================
+// Momentum (microfluidics_complex_domain/VeloSolve_2_combined.f90, VeloSolve_combined.f90,
+// two_phase_flow_complex_domain/VeloSolve_2_combined.f90)
+// ======================================================================================
+
+// RHS fu/fv (:62-295, :377-385) packed by Atob_uv (:388-389); x0 = Atob_uv(u, v).
+__global__ void k_uv_rhs(DevParams P, int bdf, const CallArgs* __restrict__ ca, const double* __restrict__ psi1,
+                         const double* __restrict__ psi2, const double* __restrict__ u_pre,
+                         const double* __restrict__ u, const double* __restrict__ v_pre,
+                         const double* __restrict__ v, const double* __restrict__ p, const double* __restrict__ rho,
+                         const double* __restrict__ eta, const double* __restrict__ bdr,
+                         const double* __restrict__ used, const double* __restrict__ ph,
+                         const double* __restrict__ rmu, const double* __restrict__ pf1,
+                         const double* __restrict__ pf2, double* __restrict__ b, double* __restrict__ x,
+                         double* __restrict__ uL, ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz;
+    const long mn = (long)(nr + 1) * nz, N = mn + (long)nr * (nz - 1);
+    const bool tp = P.variant == DRD_VARIANT_TP;
+    const bool dirichlet = !(tp && P.lr_neumann);
+    const double dr = P.dr, dz = P.dz, dt = P.dt, re = P.re, ca_ = P.ca;
+    const double cf = ca->cf;
+#define UT(i, k) (bdf == 2 ? 2.0 * u[uidx(nr, i, k)] - u_pre[uidx(nr, i, k)] : u[uidx(nr, i, k)])
+#define VT(i, k) (bdf == 2 ? 2.0 * v[vidx(nr, i, k)] - v_pre[vidx(nr, i, k)] : v[vidx(nr, i, k)])
+#define TPR(i, k) (bdf == 2 ? p[cidx(nr, i, k)] + 4 * psi2[cidx(nr, i, k)] / 3.0 - psi1[cidx(nr, i, k)] / 3.0 : p[cidx(nr, i, k)])
+#define C_(a, i, k) a[cidx(nr, i, k)]
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < N; q += (long)gridDim.x * blockDim.x) {
+        if (q < mn) {
+            const int i = (int)(q % (nr + 1)), k = (int)(q / (nr + 1));
+            double fu;
+            if (!tp)
+                fu = ca_ * (C_(rmu, i, k) + C_(rmu, i - 1, k)) / 2.0 * (C_(ph, i, k) - C_(ph, i - 1, k)) / dr *
+                     (1.0 - (C_(bdr, i, k) + C_(bdr, i - 1, k)) / 2.0);
+            else
+                fu = ca_ * (C_(rmu, i, k) + C_(rmu, i - 1, k)) / 2.0 *
+                     (C_(ph, i, k) * C_(used, i, k) - C_(ph, i - 1, k) * C_(used, i - 1, k)) / dr;
+            fu = fu - re * (C_(rho, i, k) + C_(rho, i - 1, k)) / 2.0 *
+                          (UT(i, k) * (UT(i + 1, k) - UT(i - 1, k)) / 2.0 / dr +
+                           (VT(i, k) + VT(i - 1, k) + VT(i, k + 1) + VT(i - 1, k + 1)) / 4.0 * (UT(i, k + 1) - UT(i, k - 1)) / 2.0 / dz);
+            const double g = (tp && bdf == 2) ? (C_(ph, i, k) + C_(ph, i - 1, k)) / 2.0 * P.ggx : P.ggx;
+            const double uu = u[uidx(nr, i, k)];
+            const double mass = (bdf == 2) ? 2.0 * uu * re / dt - u_pre[uidx(nr, i, k)] * re / 2.0 / dt + g : uu * re / dt + g;
+            fu = fu - (TPR(i, k) - TPR(i - 1, k)) / dr + (C_(rho, i, k) + C_(rho, i - 1, k)) / 2.0 * mass;
+            fu = fu + (C_(pf1, i, k) + C_(pf1, i - 1, k)) / 2.0;
+            fu = fu * dt;
+            if (dirichlet && (i == 0 || i == nr)) {
+                const double hig = P.bdr_upp - P.bdr_low;
+                const double z = (k + 0.5) * dz;
+                double ul = 0.0;
+                if (z > P.bdr_low && z < P.bdr_upp) {
+                    const double dd = z - P.bdr_low - hig / 2;
+                    ul = P.UU * (-(dd * dd) / hig / hig * 4 + 1) * cf;
+                }
+                if (i == 0 && uL != nullptr) uL[k] = ul;
+                fu = fu + 2.0 * ul * C_(eta, i, k) * 2.0 * dt / P.dr2;
+            }
+            if (k == 0) {
+                const double etay = (C_(eta, i, k) + C_(eta, i - 1, k) + C_(eta, i, k - 1) + C_(eta, i - 1, k - 1)) / 4.0;
+                fu = fu + dt * (2.0 * P.uwB / P.dz2 * etay);
+            }
+            if (k == nz - 1) {
+                const double etay = (C_(eta, i, k + 1) + C_(eta, i - 1, k + 1) + C_(eta, i, k) + C_(eta, i - 1, k)) / 4.0;
+                fu = fu + dt * (2.0 * P.uwT / P.dz2 * etay);
+            }
+            b[q] = fu;
+            x[q] = uu;
+        } else {
+            const long qv = q - mn;
+            const int i = (int)(qv % nr), k = (int)(qv / nr) + 1;
+            double fv;
+            if (!tp)
+                fv = ca_ * (C_(rmu, i, k) + C_(rmu, i, k - 1)) / 2.0 * (C_(ph, i, k) - C_(ph, i, k - 1)) / dz *
+                     (1.0 - (C_(bdr, i, k) + C_(bdr, i, k - 1)) / 2.0);
+            else
+                fv = ca_ * (C_(rmu, i, k) + C_(rmu, i, k - 1)) / 2.0 *
+                     (C_(ph, i, k) * C_(used, i, k) - C_(ph, i, k - 1) * C_(used, i, k - 1)) / dz;
+            fv = fv - re * (C_(rho, i, k) + C_(rho, i, k - 1)) / 2.0 *
+                          ((UT(i, k) + UT(i + 1, k) + UT(i, k - 1) + UT(i + 1, k - 1)) / 4.0 * (VT(i + 1, k) - VT(i - 1, k)) / 2.0 / dr +
+                           VT(i, k) * (VT(i, k + 1) - VT(i, k - 1)) / 2.0 / dz);
+            const double g = (tp && bdf == 2) ? (C_(ph, i, k) + C_(ph, i - 1, k)) / 2.0 * P.ggz : P.ggz;
+            const double vv = v[vidx(nr, i, k)];
+            const double mass = (bdf == 2) ? 2.0 * vv * re / dt - v_pre[vidx(nr, i, k)] * re / 2.0 / dt + g : vv * re / dt + g;
+            fv = fv - (TPR(i, k) - TPR(i, k - 1)) / dz + (C_(rho, i, k) + C_(rho, i, k - 1)) / 2.0 * mass;
+            fv = fv + (C_(pf2, i, k) + C_(pf2, i, k - 1)) / 2.0;
+            fv = fv * dt;
+            b[q] = fv;
+            x[q] = vv;
+        }
+    }
+#undef UT
+#undef VT
+#undef TPR
+#undef C_
+}
+
+// Values of the unknown fields at any index the operator reads, with the ghost values
+// MatrixVector_uv_2_CG assigns (:533-553; TP lr_bd_type 'n': copies instead of reflections).
+template <typename T>
+struct UVFetch {
+    const T* x; int nr, nz; long mn; int neumann;
+    __device__ __forceinline__ T U(int i, int k) const {
+        if (k < 0) return -Uc(i, 0);
+        if (k > nz - 1) return -Uc(i, nz - 1);
+        return Uc(i, k);
+    }
+    __device__ __forceinline__ T Uc(int i, int k) const {  // k in [0, nz-1]
+        if (i < 0) return neumann ? x[1 + (long)(nr + 1) * k] : -x[1 + (long)(nr + 1) * k];
+        if (i > nr) return neumann ? x[(nr - 1) + (long)(nr + 1) * k] : -x[(nr - 1) + (long)(nr + 1) * k];
+        return x[i + (long)(nr + 1) * k];
+    }
+    __device__ __forceinline__ T V(int i, int k) const {
+        if (k <= 0 || k >= nz) return T(0);
+        const int ii = i < 0 ? 0 : (i > nr - 1 ? nr - 1 : i);
+        return x[mn + ii + (long)nr * (k - 1)];
+    }
+};
+
+// MatrixVector_uv_2_CG (:515-646) / MatrixVector_uv_CG: y = alpha A x + beta y.
+template <typename T>
+__global__ void k_uv_mv(OpScal<T> o, const T* __restrict__ rho, const T* __restrict__ eta,
+                        const T* __restrict__ pen, const T* __restrict__ x, T alpha, T beta, T* y, const T* dot1,
+                        int self2, Dots d, int slot1, const KState* ks, int gate, ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, gate)) return;
+    const int nr = o.nr, nz = o.nz;
+    const long mn = (long)(nr + 1) * nz, N = mn + (long)nr * (nz - 1);
+    UVFetch<T> F{x, nr, nz, mn, o.lr_neumann};
+    const T h = T(0.5), q4 = T(0.25);
+    const T mcoef = (o.bdf == 2) ? T(1.5) * o.re : o.re;
+    double a1 = 0.0, a2 = 0.0;
+#define E_(i, k) eta[cidx(nr, i, k)]
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < N; q += (long)gridDim.x * blockDim.x) {
+        T val;
+        if (q < mn) {
+            const int i = (int)(q % (nr + 1)), k = (int)(q / (nr + 1));
+            const T f1 = x[q];
+            if (o.bdf == 2)
+                val = f1 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i - 1, k)]) * h +
+                      f1 * o.pk * (pen[cidx(nr, i, k)] + pen[cidx(nr, i - 1, k)]) * h * o.dt;
+            else
+                val = f1 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i - 1, k)]) * h;
+            T cr = E_(i, k), cl = E_(i - 1, k);
+            val = val - T(2) * o.dt * (cr * F.Uc(i + 1, k) + cl * F.Uc(i - 1, k) - (cl + cr) * f1) / o.dr2;
+            cr = (E_(i, k + 1) + E_(i - 1, k + 1) + E_(i, k) + E_(i - 1, k)) * q4;
+            cl = (E_(i, k) + E_(i - 1, k) + E_(i, k - 1) + E_(i - 1, k - 1)) * q4;
+            val = val - o.dt * (cr * F.U(i, k + 1) + cl * F.U(i, k - 1) - (cl + cr) * f1) / o.dz2;
+            val = val - o.dt * (cr * (F.V(i, k + 1) - F.V(i - 1, k + 1)) - cl * (F.V(i, k) - F.V(i - 1, k))) / o.dr / o.dz;
+        } else {
+            const long qv = q - mn;
+            const int i = (int)(qv % nr), k = (int)(qv / nr) + 1;
+            const T f2 = x[q];
+            if (o.bdf == 2)
+                val = f2 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i, k - 1)]) * h +
+                      f2 * o.pk * (pen[cidx(nr, i, k)] + pen[cidx(nr, i, k - 1)]) * h * o.dt;
+            else
+                val = f2 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i, k - 1)]) * h;
+            T cr = E_(i, k), cl = E_(i, k - 1);
+            val = val - T(2) * o.dt * (cr * F.V(i, k + 1) + cl * F.V(i, k - 1) - (cl + cr) * f2) / o.dz2;
+            cr = (E_(i + 1, k) + E_(i, k) + E_(i + 1, k - 1) + E_(i, k - 1)) * q4;
+            cl = (E_(i, k) + E_(i - 1, k) + E_(i, k - 1) + E_(i - 1, k - 1)) * q4;
+            val = val - o.dt * (cr * F.V(i + 1, k) + cl * F.V(i - 1, k) - (cl + cr) * f2) / o.dr2;
+            val = val - o.dt * (cr * (F.Uc(i + 1, k) - F.Uc(i + 1, k - 1)) - cl * (F.Uc(i, k) - F.Uc(i, k - 1))) / o.dr / o.dz;
+        }
+        const T yn = (beta == T(0)) ? alpha * val : alpha * val + beta * y[q];
+        y[q] = yn;
+        if (dot1) a1 += (double)dot1[q] * (double)yn;
+        if (self2) a2 += (double)yn * (double)yn;
+    }
+#undef E_
+    if (dot1 != nullptr || self2) emit_partials<DRD_TPB>(a1, a2, dot1 != nullptr, self2, d, slot1);
+}
+
+// Jacobi diagonal of PSolve_uv_2_CG (:662-709) / PSolve_uv_CG, including rho(i-1,j) in the
+// v block as written at :690.
+template <typename T>
+__global__ void k_uv_diag(OpScal<T> o, const T* __restrict__ rho, const T* __restrict__ eta, T* __restrict__ diag,
+                          ull* ctr) {
+    count_launch(ctr);
+    const int nr = o.nr, nz = o.nz;
+    const long mn = (long)(nr + 1) * nz, N = mn + (long)nr * (nz - 1);
+    const T mcoef = (o.bdf == 2) ? T(1.5) * o.re : o.re;
+    const T h = T(0.5), q4 = T(0.25);
+#define E_(i, k) eta[cidx(nr, i, k)]
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < N; q += (long)gridDim.x * blockDim.x) {
+        T tmp;
+        if (q < mn) {
+            const int i = (int)(q % (nr + 1)), j = (int)(q / (nr + 1));
+            tmp = mcoef * (rho[cidx(nr, i, j)] + rho[cidx(nr, i - 1, j)]) * h;
+            T cr = E_(i, j), cl = E_(i - 1, j);
+            tmp = tmp + T(2) * o.dt * (cl + cr) / o.dr2;
+            cr = (E_(i, j + 1) + E_(i - 1, j + 1) + E_(i, j) + E_(i - 1, j)) * q4;
+            cl = (E_(i, j) + E_(i - 1, j) + E_(i, j - 1) + E_(i - 1, j - 1)) * q4;
+            if (j == 0) tmp = tmp + o.dt * (cl + (cl + cr)) / o.dz2;
+            else if (j == nz - 1) tmp = tmp + o.dt * (cr + (cl + cr)) / o.dz2;
+            else tmp = tmp + o.dt * (cl + cr) / o.dz2;
+        } else {
+            const long qv = q - mn;
+            const int i = (int)(qv % nr), j = (int)(qv / nr) + 1;
+            tmp = mcoef * (rho[cidx(nr, i, j)] + rho[cidx(nr, i - 1, j)]) * h;
+            T cr = E_(i, j), cl = E_(i, j - 1);
+            tmp = tmp + T(2) * o.dt * (cl + cr) / o.dz2;
+            cr = (E_(i + 1, j) + E_(i, j) + E_(i + 1, j - 1) + E_(i, j - 1)) * q4;
+            cl = (E_(i, j) + E_(i - 1, j) + E_(i, j - 1) + E_(i - 1, j - 1)) * q4;
+            if (i == 0) tmp = tmp + o.dt * cr / o.dr2;
+            else if (i == nr - 1) tmp = tmp + o.dt * cl / o.dr2;
+            else tmp = tmp + o.dt * (cl + cr) / o.dr2;
+        }
+        diag[q] = tmp;
+    }
+#undef E_
+}
+
+// btoA_uv (matrix_tool.f90:32-75) followed by the ghost assignments of :411-436 (TP :428-441).
+__global__ void k_uv_fin(DevParams P, const double* __restrict__ x, const double* __restrict__ uL,
+                         double* __restrict__ u_after, double* __restrict__ v_after, ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz;
+    const long mn = (long)(nr + 1) * nz;
+    const bool dirichlet = !(P.variant == DRD_VARIANT_TP && P.lr_neumann);
+    const long us = (long)(nr + 3) * (nz + 2), vs = (long)(nr + 2) * (nz + 1);
+    auto xu = [&](int i, int k) { return x[i + (long)(nr + 1) * k]; };
+    auto ucol = [&](int i, int k) -> double {  // value at column i (-1..nr+1), row k (0..nz-1)
+        if (i < 0) return dirichlet ? 2.0 * uL[k] - xu(1, k) : xu(1, k);
+        if (i > nr) return dirichlet ? 2.0 * uL[k] - xu(nr - 1, k) : xu(nr - 1, k);
+        return xu(i, k);
+    };
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < us + vs; q += (long)gridDim.x * blockDim.x) {
+        if (q < us) {
+            const int i = (int)(q % (nr + 3)) - 1, k = (int)(q / (nr + 3)) - 1;
+            double val;
+            if (k == -1) val = P.uwB * 2.0 - ucol(i, 0);
+            else if (k == nz) val = P.uwT * 2.0 - ucol(i, nz - 1);
+            else val = ucol(i, k);
+            u_after[q] = val;
+        } else {
+            const long qv = q - us;
+            const int i = (int)(qv % (nr + 2)) - 1, k = (int)(qv / (nr + 2));
+            double val = 0.0;
+            if (k > 0 && k < nz) {
+                const int ii = i < 0 ? 0 : (i > nr - 1 ? nr - 1 : i);
+                val = x[mn + ii + (long)nr * (k - 1)];
+            }
+            v_after[qv] = val;
+        }
+    }
+}
+
+// ======================================================================================
+// Pressure (microfluidics_complex_domain/PreSolve_2.f90:16-21), interpolate_coef, mass
+// ======================================================================================
+__global__ void k_pre_div(DevParams P, const double* __restrict__ u, const double* __restrict__ v,
+                          double* __restrict__ w, ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz;
+    const long n = (long)nr * nz;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        w[q] = (u[uidx(nr, i + 1, k)] - u[uidx(nr, i, k)]) / P.dr + (v[vidx(nr, i, k + 1)] - v[vidx(nr, i, k)]) / P.dz;
+    }
+}
+
+__global__ void k_cell_add(long n, const double* __restrict__ x, double* __restrict__ y, ull* ctr) {
+    count_launch(ctr);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        y[q] = x[q] + y[q];
+}
+
+// interpolate_coef (interpolate_coef.f90:55-89): fpd = (tanh(-d/(sqrt2 eps))+1)/2 + bdr,
+// Neumann ghosts, rho/eta linear in fpd.
+__global__ void k_interp_coef(DevParams P, const double* __restrict__ dist, const double* __restrict__ bdr,
+                              double* __restrict__ fpd, double* __restrict__ rho, double* __restrict__ eta, ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz;
+    const long cs = (long)(nr + 2) * (nz + 2);
+    const double sq2 = sqrt(2.0);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < cs; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % (nr + 2)) - 1, k = (int)(q / (nr + 2)) - 1;
+        const int si = i < 0 ? 0 : (i > nr - 1 ? nr - 1 : i);
+        const int sk = k < 0 ? 0 : (k > nz - 1 ? nz - 1 : k);
+        double f = tanh(-1.0 * dist[si + (long)nr * sk] / sq2 / P.eps);
+        f = (f + 1.0) / 2.0;
+        f = f + bdr[cidx(nr, si, sk)];
+        fpd[q] = f;
+        rho[q] = 1.0 + (P.lambda_rho - 1.0) * f;
+        eta[q] = 1.0 + (P.lambda_eta - 1.0) * f;
+    }
+}
+
+__global__ void k_mass_partial(int nr, int nz, const double* __restrict__ ph, Dots d, int slot, ull* ctr) {
+    count_launch(ctr);
+    const long n = (long)nr * nz;
+    double a = 0.0;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        a += ph[cidx(nr, i, k)];
+    }
+    __shared__ double sm[32];
+    double r = block_sum<DRD_TPB>(a, sm);
+    if (threadIdx.x == 0) d.part[slot * DRD_MAXB + blockIdx.x] = r;
+}
+
+__global__ void k_mass_final(Dots d, int slot, double drdz, double* out, ull* ctr) {
+    count_launch(ctr);
+    __shared__ double sm[32];
+    double r = reduce_partials<DRD_TPB>(d.part + slot * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) *out = r * drdz;
+}
+
+// ======================================================================================
+// Transforms as GEMMs: C = A B (row-major), the 2-D DCT-I / DCT-II / DCT-III of the
+// preconditioner and the pressure solve applied one axis at a time.  Tiles BM x BN x BK,
+// each thread TM x TN outputs strided by the thread grid (coalesced loads and stores).
+// ======================================================================================
+template <typename T, int BM, int BN, int BK, int TM, int TN, int EPI>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm(GemmArgs<T> a) {
+    constexpr int NT = (BM / TM) * (BN / TN);
+    constexpr int TX = BN / TN, TY = BM / TM;
+    __shared__ T As[BK][BM + 1];
+    __shared__ T Bs[BK][BN];
+    count_launch(a.ctr);
+    if (gate_closed(a.ks, a.gate)) return;
+    const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    T acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+    for (int k0 = 0; k0 < a.K; k0 += BK) {
+#pragma unroll
+        for (int e = tid; e < BM * BK; e += NT) {
+            const int r = e / BK, c = e % BK;
+            const int gm = m0 + r, gk = k0 + c;
+            As[c][r] = (gm < a.M && gk < a.K) ? a.A[(long)gm * a.lda + gk] : T(0);
+        }
+#pragma unroll
+        for (int e = tid; e < BK * BN; e += NT) {
+            const int r = e / BN, c = e % BN;
+            const int gk = k0 + r, gn = n0 + c;
+            Bs[r][c] = (gk < a.K && gn < a.N) ? a.B[(long)gk * a.ldb + gn] : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            T av[TM], bv[TN];
+#pragma unroll
+            for (int i = 0; i < TM; ++i) av[i] = As[kk][ty + i * TY];
+#pragma unroll
+            for (int j = 0; j < TN; ++j) bv[j] = Bs[kk][tx + j * TX];
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TN; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+    const double coef = (EPI == EPI_PRE_FINAL) ? a.ca->coef : 0.0;
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+        const int gm = m0 + ty + i * TY;
+        if (gm >= a.M) continue;
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            const int gn = n0 + tx + j * TX;
+            if (gn >= a.N) continue;
+            const T v = acc[i][j];
+            if (EPI == EPI_STORE) a.C[(long)gm * a.ldc + gn] = v;
+            else if (EPI == EPI_DIV_TAB) a.C[(long)gm * a.ldc + gn] = v / a.tab[(long)gm * a.ldt + gn];
+            else if (EPI == EPI_SCALE) a.C[(long)gm * a.ldc + gn] = v * (T)a.scale;
+            else a.C[cidx(a.nr, gn, gm)] = (T)(((double)v / a.scale) * coef);
+        }
+    }
+}
+
+struct GemmCfg { const char* name; };
+static const GemmCfg kGemmCfgs[] = {{"64x64x16/4x4"}, {"32x64x16/2x4"}, {"32x32x16/2x2"}, {"16x32x16/1x2"}};
+
+int gemm_config_count() { return 4; }
+const char* gemm_config_name(int cfg) { return kGemmCfgs[cfg].name; }
+
+template <typename T, int BM, int BN, int TM, int TN>
+static void gemm_dispatch_epi(int epi, const GemmArgs<T>& a, cudaStream_t s) {
+    dim3 grid((a.N + BN - 1) / BN, (a.M + BM - 1) / BM);
+    constexpr int NT = (BM / TM) * (BN / TN);
+    switch (epi) {
+        case EPI_STORE: k_gemm<T, BM, BN, 16, TM, TN, EPI_STORE><<<grid, NT, 0, s>>>(a); break;
+        case EPI_DIV_TAB: k_gemm<T, BM, BN, 16, TM, TN, EPI_DIV_TAB><<<grid, NT, 0, s>>>(a); break;
+        case EPI_SCALE: k_gemm<T, BM, BN, 16, TM, TN, EPI_SCALE><<<grid, NT, 0, s>>>(a); break;
+        default: k_gemm<T, BM, BN, 16, TM, TN, EPI_PRE_FINAL><<<grid, NT, 0, s>>>(a); break;
+    }
+}
+
+template <typename T>
+void launch_gemm(int cfg, int epi, const GemmArgs<T>& a, cudaStream_t s) {
+    switch (cfg) {
+        case 0: gemm_dispatch_epi<T, 64, 64, 4, 4>(epi, a, s); break;
+        case 1: gemm_dispatch_epi<T, 32, 64, 2, 4>(epi, a, s); break;
+        case 2: gemm_dispatch_epi<T, 32, 32, 2, 2>(epi, a, s); break;
+        default: gemm_dispatch_epi<T, 16, 32, 1, 2>(epi, a, s); break;
+    }
+}
+template void launch_gemm<double>(int, int, const GemmArgs<double>&, cudaStream_t);
+template void launch_gemm<float>(int, int, const GemmArgs<float>&, cudaStream_t);
+
+// ======================================================================================
+// BiCGSTAB (lib/BiCGSTABREVCOM.f:150-418, lib/STOPTEST2.f:281-290) as element-wise kernels
+// with fused partial dot products and one-block scalar kernels.  Dot products are summed in
+// FP64 in a fixed order (deterministic for a fixed grid).
+// Partials slots: 0 = ||.||^2 / (rtld,v), 1 = (rtld,r) or (t,s), 2 = (t,t), 3 = ||b||^2.
+// ======================================================================================
+static __device__ const double kBreakTol = 1.2325951644078309e-32;  // DLAMCH('E')**2 (getbreak.f)
+
+template <typename T>
+__global__ void k_bi_init1(long n, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r, Dots d,
+                           ull* ctr) {
+    count_launch(ctr);
+    double ax = 0.0, ab = 0.0;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const T bv = b[q], xv = x[q];
+        r[q] = bv;
+        ax += (double)xv * (double)xv;
+        ab += (double)bv * (double)bv;
+    }
+    __shared__ double sm[32];
+    double r1 = block_sum<DRD_TPB>(ax, sm);
+    if (threadIdx.x == 0) d.part[0 * DRD_MAXB + blockIdx.x] = r1;
+    double r2 = block_sum<DRD_TPB>(ab, sm);
+    if (threadIdx.x == 0) d.part[3 * DRD_MAXB + blockIdx.x] = r2;
+}
+
+// Start of BICGSTABREVCOM (:153-255) up to the x0 test.
+__global__ void k_bi_init2(KState* ks, Dots d, double tol, int maxit, const KState* parent, ull* ctr) {
+    count_launch(ctr);
+    __shared__ double sm[32];
+    const double xx = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
+    const double bb = reduce_partials<DRD_TPB>(d.part + 3 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) {
+        ks->tol = tol;
+        ks->maxit = maxit;
+        ks->info = 0;
+        ks->flags = 0u;
+        ks->iter = maxit;   // ITER keeps MAXIT if the x0 test ends the solve (:248)
+        ks->resid = tol;    // RESID keeps TOL in that case
+        ks->xnorm = sqrt(xx);
+        ks->x_nonzero = (ks->xnorm != 0.0);
+        ks->bnorm_raw = sqrt(bb);
+        ks->bnrm2 = (ks->bnorm_raw == 0.0) ? 1.0 : ks->bnorm_raw;
+        ks->rho = ks->rho1 = ks->alpha = ks->omega = ks->beta = 0.0;
+        ks->phase = (maxit <= 0) ? PH_DONE : PH_RUNNING;
+        if (maxit <= 0) ks->info = -3;
+        if (parent != nullptr && parent->phase != PH_RUNNING) ks->phase = PH_DONE;
+    }
+}
+
+// The x0 test (:248) after r = b - A x0 (gated matvec wrote ||r||^2 into slot 0).
+__global__ void k_bi_init3(KState* ks, Dots d, ull* ctr) {
+    count_launch(ctr);
+    __shared__ double sm[32];
+    const int run = (ks->phase == PH_RUNNING);
+    const int xnz = ks->x_nonzero;
+    double rr = 0.0;
+    if (run && xnz) rr = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0 && run) {
+        if (xnz && sqrt(rr) <= ks->tol) {
+            ks->phase = PH_DONE;
+            ks->info = 0;
+            ks->flags |= DRD_FLAG_EARLY_X0;
+        } else {
+            ks->iter = 0;
+        }
+    }
+}
+
+// rtld = r and the first rho partials (rtld, r) into slot 1.
+template <typename T>
+__global__ void k_bi_init4(long n, const T* __restrict__ r, T* __restrict__ rtld, Dots d, const KState* ks,
+                           ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, G_RUNNING)) return;
+    double a = 0.0;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const T rv = r[q];
+        rtld[q] = rv;
+        a += (double)rv * (double)rv;
+    }
+    __shared__ double sm[32];
+    double s = block_sum<DRD_TPB>(a, sm);
+    if (threadIdx.x == 0) d.part[1 * DRD_MAXB + blockIdx.x] = s;
+}
+
+// ITER = ITER + 1; RHO = (rtld, r); breakdown test; BETA (:261-269).
+__global__ void k_bi_rho(KState* ks, Dots d, ull* ctr) {
+    count_launch(ctr);
+    if (ks->phase != PH_RUNNING) return;
+    __shared__ double sm[32];
+    const double rho = reduce_partials<DRD_TPB>(d.part + 1 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) {
+        ks->iter = ks->iter + 1;
+        ks->rho = rho;
+        if (fabs(rho) < kBreakTol) {
+            ks->info = -10;
+            ks->phase = PH_DONE;
+        } else if (ks->iter > 1) {
+            ks->beta = (rho / ks->rho1) * (ks->alpha / ks->omega);
+        }
+    }
+}
+
+// P = R (first iteration) or P = beta (P - omega V) + R (:268-275), fused with the
+// preconditioner when it is diagonal (Jacobi) or the identity.
+template <typename T>
+__global__ void k_bi_p(long n, const T* __restrict__ r, const T* __restrict__ v, T* __restrict__ p,
+                       T* __restrict__ phat, const T* __restrict__ diag, int ident, const KState* ks, ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, G_RUNNING)) return;
+    const bool first = ks->iter == 1;
+    const T beta = (T)ks->beta, nomega = (T)(-ks->omega);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        T pv;
+        if (first) pv = r[q];
+        else {
+            pv = p[q] + nomega * v[q];
+            pv = beta * pv;
+            pv = pv + r[q];
+        }
+        p[q] = pv;
+        if (diag) phat[q] = pv / diag[q];
+        else if (ident) phat[q] = pv;
+    }
+}
+
+// ALPHA = RHO / (rtld, v) (:307).
+__global__ void k_bi_alpha(KState* ks, Dots d, ull* ctr) {
+    count_launch(ctr);
+    if (ks->phase != PH_RUNNING) return;
+    __shared__ double sm[32];
+    const double rv = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) ks->alpha = ks->rho / rv;
+}
+
+// S = R - ALPHA V (:311-312, S aliases R) with ||S||^2 partials.
+template <typename T>
+__global__ void k_bi_s(long n, const T* __restrict__ v, T* __restrict__ r, Dots d, const KState* ks, ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, G_RUNNING)) return;
+    const T na = (T)(-ks->alpha);
+    double a = 0.0;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const T s = r[q] + na * v[q];
+        r[q] = s;
+        a += (double)s * (double)s;
+    }
+    __shared__ double sm[32];
+    double t = block_sum<DRD_TPB>(a, sm);
+    if (threadIdx.x == 0) d.part[0 * DRD_MAXB + blockIdx.x] = t;
+}
+
+// Early absolute test ||S|| <= TOL (:313-316).
+__global__ void k_bi_snorm(KState* ks, Dots d, ull* ctr) {
+    count_launch(ctr);
+    if (ks->phase != PH_RUNNING) return;
+    __shared__ double sm[32];
+    const double ss = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) {
+        ks->snorm = sqrt(ss);
+        if (ks->snorm <= ks->tol) {
+            ks->phase = PH_EARLY;
+            ks->resid = ks->snorm / ks->bnrm2;
+            ks->info = 0;
+            ks->flags |= DRD_FLAG_EARLY_S;
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_bi_diag_apply(long n, const T* __restrict__ x, const T* __restrict__ diag, int ident,
+                                T* __restrict__ y, const KState* ks, int gate, ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, gate)) return;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        y[q] = ident ? x[q] : x[q] / diag[q];
+}
+
+// OMEGA = (t, s) / (t, t) (:349-350).
+__global__ void k_bi_omega(KState* ks, Dots d, ull* ctr) {
+    count_launch(ctr);
+    if (ks->phase != PH_RUNNING) return;
+    __shared__ double sm[32];
+    const double ts = reduce_partials<DRD_TPB>(d.part + 1 * DRD_MAXB, d.G, sm);
+    const double tt = reduce_partials<DRD_TPB>(d.part + 2 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) ks->omega = ts / tt;
+}
+
+// X = X + ALPHA PHAT (+ OMEGA SHAT); R = R - OMEGA T (:314, :354-359) with ||R||^2 and
+// (rtld, R) partials for STOPTEST2 and the next RHO.
+template <typename T>
+__global__ void k_bi_xr(long n, const T* __restrict__ phat, const T* __restrict__ shat, const T* __restrict__ t,
+                        const T* __restrict__ rtld, T* __restrict__ x, T* __restrict__ r, Dots d, const KState* ks,
+                        ull* ctr) {
+    count_launch(ctr);
+    const int ph = ks->phase;
+    if (ph == PH_DONE) return;
+    const T al = (T)ks->alpha;
+    if (ph == PH_EARLY) {
+        for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+            x[q] = x[q] + al * phat[q];
+        return;
+    }
+    const T om = (T)ks->omega, nom = (T)(-ks->omega);
+    double a0 = 0.0, a1 = 0.0;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        T xv = x[q] + al * phat[q];
+        xv = xv + om * shat[q];
+        x[q] = xv;
+        const T rv = r[q] + nom * t[q];
+        r[q] = rv;
+        a0 += (double)rv * (double)rv;
+        a1 += (double)rtld[q] * (double)rv;
+    }
+    __shared__ double sm[32];
+    double s0 = block_sum<DRD_TPB>(a0, sm);
+    if (threadIdx.x == 0) d.part[0 * DRD_MAXB + blockIdx.x] = s0;
+    double s1 = block_sum<DRD_TPB>(a1, sm);
+    if (threadIdx.x == 0) d.part[1 * DRD_MAXB + blockIdx.x] = s1;
+}
+
+// STOPTEST2 (:361-362 via lib/STOPTEST2.f:286-290), MAXIT test (:376-379), OMEGA breakdown
+// (:383-388); sets the WHILE condition of the captured loop.  Iterations with a non-finite
+// residual end the solve with DRD_ERR_NONFINITE instead of running on to MAXIT.
+__global__ void k_bi_end(KState* ks, Dots d, cudaGraphConditionalHandle h, int use_graph, ull* ctr) {
+    count_launch(ctr);
+    __shared__ double sm[32];
+    const int ph = ks->phase;
+    double rr = 0.0;
+    if (ph == PH_RUNNING) rr = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) {
+        if (ph == PH_EARLY) {
+            ks->phase = PH_DONE;
+        } else if (ph == PH_RUNNING) {
+            const double resid = sqrt(rr) / ks->bnrm2;
+            ks->resid = resid;
+            if (!isfinite(resid)) {
+                ks->info = DRD_ERR_NONFINITE;
+                ks->phase = PH_DONE;
+            } else if (resid <= ks->tol) {
+                ks->info = 0;
+                ks->phase = PH_DONE;
+            } else if (ks->iter >= ks->maxit) {
+                ks->info = 1;
+                ks->phase = PH_DONE;
+            } else if (fabs(ks->omega) < kBreakTol) {
+                ks->info = (fabs(ks->rho) < kBreakTol) ? -10 : -11;
+                ks->phase = PH_DONE;
+            } else {
+                ks->rho1 = ks->rho;
+            }
+        }
+        if (use_graph) cudaGraphSetConditional(h, ks->phase == PH_RUNNING ? 1u : 0u);
+    }
+}
+
+// ||b - A x|| / ||b|| from slot 0 (the residual's partials) and the stored ||b||.
+__global__ void k_bi_true_resid(KState* ks, Dots d, ull* ctr) {
+    count_launch(ctr);
+    __shared__ double sm[32];
+    const double rr = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) ks->true_resid = sqrt(rr) / (ks->bnorm_raw == 0.0 ? 1.0 : ks->bnorm_raw);
+}
+
+template <typename T>
+__global__ void k_copy(long n, const T* __restrict__ x, T* __restrict__ y, ull* ctr) {
+    count_launch(ctr);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) y[q] = x[q];
+}
+
+template <typename TO, typename TI>
+__global__ void k_convert(long n, const TI* __restrict__ x, double scale, TO* __restrict__ y, ull* ctr) {
+    count_launch(ctr);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        y[q] = (TO)(scale * (double)x[q]);
+}
+
+template <typename T>
+__global__ void k_norm2_partial(long n, const T* __restrict__ x, Dots d, int slot, ull* ctr) {
+    count_launch(ctr);
+    double a = 0.0;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        a += (double)x[q] * (double)x[q];
+    __shared__ double sm[32];
+    double r = block_sum<DRD_TPB>(a, sm);
+    if (threadIdx.x == 0) d.part[slot * DRD_MAXB + blockIdx.x] = r;
+}
+
+// ---- mixed-precision refinement ----------------------------------------------------------
+// outer->snorm holds ||r64||; the FP32 system is solved for r64/||r64|| from a zero guess.
+__global__ void k_mx_init(KState* o, Dots d, double tol, int max_refine, ull* ctr) {
+    count_launch(ctr);
+    __shared__ double sm[32];
+    const double rr = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
+    const double bb = reduce_partials<DRD_TPB>(d.part + 3 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) {
+        o->tol = tol;
+        o->maxit = max_refine;
+        o->bnorm_raw = sqrt(bb);
+        o->bnrm2 = (o->bnorm_raw == 0.0) ? 1.0 : o->bnorm_raw;
+        o->snorm = sqrt(rr);
+        o->resid = o->snorm / o->bnrm2;
+        o->outer = 0;
+        o->inner_total = 0;
+        o->iter = 0;
+        o->flags = DRD_FLAG_REFINED;
+        o->info = 0;
+        o->phase = (o->resid <= tol || o->snorm == 0.0) ? PH_DONE : PH_RUNNING;
+        if (!isfinite(o->resid)) { o->info = DRD_ERR_NONFINITE; o->phase = PH_DONE; }
+        o->true_resid = o->resid;
+    }
+}
+
+template <typename TO>
+__global__ void k_mx_scale_from_state(long n, const double* __restrict__ r, const KState* o, TO* __restrict__ y,
+                                      TO* __restrict__ zero, ull* ctr) {
+    count_launch(ctr);
+    if (o->phase != PH_RUNNING) return;
+    const double sc = 1.0 / o->snorm;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        y[q] = (TO)(r[q] * sc);
+        zero[q] = TO(0);
+    }
+}
+
+__global__ void k_mx_inner_setup(KState* in, const KState* o, double inner_tol, int inner_maxit, ull* ctr) {
+    count_launch(ctr);
+    if (threadIdx.x == 0) {
+        const bool run = o->phase == PH_RUNNING;
+        in->tol = inner_tol;
+        in->maxit = inner_maxit;
+        in->info = 0;
+        in->flags = 0u;
+        in->iter = 0;
+        in->resid = 1.0;
+        in->x_nonzero = 0;
+        in->bnorm_raw = 1.0;
+        in->bnrm2 = 1.0;
+        in->rho = in->rho1 = in->alpha = in->omega = in->beta = 0.0;
+        in->phase = run ? PH_RUNNING : PH_DONE;
+    }
+}
+
+// x64 += ||r64|| d32
+__global__ void k_axpy_f2d(long n, const KState* o, const float* __restrict__ d, double* __restrict__ x, ull* ctr) {
+    count_launch(ctr);
+    if (o->phase != PH_RUNNING) return;
+    const double sc = o->snorm;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        x[q] = x[q] + sc * (double)d[q];
+}
+
+// True FP64 residual of the refined iterate (slot 0), refinement bookkeeping, WHILE condition.
+__global__ void k_mx_check(KState* o, const KState* in, Dots d, cudaGraphConditionalHandle h, int use_graph,
+                           ull* ctr) {
+    count_launch(ctr);
+    __shared__ double sm[32];
+    const int run = o->phase == PH_RUNNING;
+    double rr = 0.0;
+    if (run) rr = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) {
+        if (run) {
+            const double prev = o->resid;
+            o->snorm = sqrt(rr);
+            o->resid = o->snorm / o->bnrm2;
+            o->true_resid = o->resid;
+            o->outer += 1;
+            o->inner_total += in->iter;
+            o->iter = o->inner_total;
+            if (!isfinite(o->resid)) { o->info = DRD_ERR_NONFINITE; o->phase = PH_DONE; }
+            else if (o->resid <= o->tol) { o->info = 0; o->phase = PH_DONE; }
+            else if (o->outer >= o->maxit) { o->info = 1; o->phase = PH_DONE; }
+            else if (o->resid > 0.9 * prev) { o->info = 1; o->phase = PH_DONE; }  // stalled refinement
+        }
+        if (use_graph) cudaGraphSetConditional(h, o->phase == PH_RUNNING ? 1u : 0u);
+    }
+}
+
+// ======================================================================================
+// Host launchers
+// ======================================================================================
+#define GRID(n) grid_for(n), DRD_TPB, 0, s
+
+void launch_ch_f2(const DevParams& P, const double* u, const double* v, const double* ph, double* f2, ull* ctr,
+                  cudaStream_t s) {
+    k_ch_f2<<<GRID((long)(P.nr + 2) * (P.nz + 2))>>>(P, u, v, ph, f2, ctr);
+}
+void launch_ch_rhs(const DevParams& P, const double* ph, const double* rmu, const double* bdr, const double* grad,
+                   const double* Mi, const double* f2, double* b, double* x, ull* ctr, cudaStream_t s) {
+    k_ch_rhs<<<GRID((long)P.nr * P.nz)>>>(P, ph, rmu, bdr, grad, Mi, f2, b, x, ctr);
+}
+template <typename T>
+void launch_ch_matvec(const OpScal<T>& o, const T* M0, const T* Mi, T alpha, const T* x, T beta, T* y, T* ff1,
+                      const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,
+                      cudaStream_t s) {
+    const long n = (long)o.nr * o.nz;
+    k_ch_mv1<T><<<GRID(n)>>>(o, M0, x, ff1, ks, gate, ctr);
+    const int g = (dot1 || self2) ? d.G : grid_for(n);
+    k_ch_mv2<T><<<g, DRD_TPB, 0, s>>>(o, Mi, x, ff1, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);
+}
+void launch_ch_fin(const DevParams& P, const double* x, const double* f2, const double* M0, double* rmu_after,
+                   double* ph_after, ull* ctr, cudaStream_t s) {
+    k_ch_fin<<<GRID((long)P.nr * P.nz)>>>(P, x, f2, M0, rmu_after, ph_after, ctr);
+    launch_fill_neumann(P.nr, P.nz, rmu_after, ph_after, ctr, s);
+}
+void launch_fill_neumann(int nr, int nz, double* a, double* b, ull* ctr, cudaStream_t s) {
+    k_fill_neumann<<<GRID(2L * (nr + 2) + 2L * nz)>>>(nr, nz, a, b, ctr);
+}
+
+void launch_phmu_prep(const DevParams& P, const double* u, const double* v, const double* ph, const double* bdr,
+                      const double* used, double* M0, double* f2, ull* ctr, cudaStream_t s) {
+    k_phmu_prep<<<GRID((long)(P.nr + 2) * (P.nz + 2))>>>(P, u, v, ph, bdr, used, M0, f2, ctr);
+}
+void launch_phmu_rhs(const DevParams& P, const double* ph, const double* rmu, const double* bdr, const double* grad,
+                     const double* f2, const double* cfB, const double* cfT, double* b, double* x, double* pnb,
+                     double* pnt, ull* ctr, cudaStream_t s) {
+    k_phmu_rhs<<<GRID((long)P.nr * P.nz)>>>(P, ph, rmu, bdr, grad, f2, cfB, cfT, b, x, pnb, pnt, ctr);
+}
+template <typename T>
+void launch_phmu_matvec(const OpScal<T>& o, const T* M0, const T* Mi, const T* used, T alpha, const T* x, T beta, T* y,
+                        const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,
+                        cudaStream_t s) {
+    const long n = 2L * o.nr * o.nz;
+    const int g = (dot1 || self2) ? d.G : grid_for(n);
+    k_phmu_mv<T><<<g, DRD_TPB, 0, s>>>(o, M0, Mi, used, x, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);
+}
+template <typename T>
+void launch_phmu_diag(const OpScal<T>& o, T* diag, ull* ctr, cudaStream_t s) {
+    k_phmu_diag<T><<<GRID((long)o.nr * o.nz)>>>(o, diag, ctr);
+}
+void launch_phmu_fin(const DevParams& P, const double* x, const double* pnb, const double* pnt, double cb, double ct,
+                     double* ph_after, double* rmu_after, ull* ctr, cudaStream_t s) {
+    k_phmu_fin<<<GRID((long)(P.nr + 2) * (P.nz + 2))>>>(P, x, pnb, pnt, cb, ct, ph_after, rmu_after, ctr);
+}
+
+void launch_uv_rhs(const DevParams& P, int bdf, const CallArgs* ca, const double* psi1, const double* psi2,
+                   const double* u_pre, const double* u, const double* v_pre, const double* v, const double* p,
+                   const double* rho, const double* eta, const double* bdr, const double* used, const double* ph_after,
+                   const double* rmu_after, const double* pf1, const double* pf2, double* b, double* x, double* uL,
+                   ull* ctr, cudaStream_t s) {
+    const long N = (long)(P.nr + 1) * P.nz + (long)P.nr * (P.nz - 1);
+    k_uv_rhs<<<GRID(N)>>>(P, bdf, ca, psi1, psi2, u_pre, u, v_pre, v, p, rho, eta, bdr, used, ph_after, rmu_after, pf1,
+                          pf2, b, x, uL, ctr);
+}
+template <typename T>
+void launch_uv_matvec(const OpScal<T>& o, const T* rho, const T* eta, const T* pen, T alpha, const T* x, T beta, T* y,
+                      const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,
+                      cudaStream_t s) {
+    const long N = (long)(o.nr + 1) * o.nz + (long)o.nr * (o.nz - 1);
+    const int g = (dot1 || self2) ? d.G : grid_for(N);
+    k_uv_mv<T><<<g, DRD_TPB, 0, s>>>(o, rho, eta, pen, x, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);
+}
+template <typename T>
+void launch_uv_diag(const OpScal<T>& o, const T* rho, const T* eta, T* diag, ull* ctr, cudaStream_t s) {
+    const long N = (long)(o.nr + 1) * o.nz + (long)o.nr * (o.nz - 1);
+    k_uv_diag<T><<<GRID(N)>>>(o, rho, eta, diag, ctr);
+}
+void launch_uv_fin(const DevParams& P, const double* x, const double* uL, double* u_after, double* v_after, ull* ctr,
+                   cudaStream_t s) {
+    const long n = (long)(P.nr + 3) * (P.nz + 2) + (long)(P.nr + 2) * (P.nz + 1);
+    k_uv_fin<<<GRID(n)>>>(P, x, uL, u_after, v_after, ctr);
+}
+
+void launch_pre_div(const DevParams& P, const double* u, const double* v, double* w, ull* ctr, cudaStream_t s) {
+    k_pre_div<<<GRID((long)P.nr * P.nz)>>>(P, u, v, w, ctr);
+}
+void launch_cell_add(long n, const double* x, double* y, ull* ctr, cudaStream_t s) {
+    k_cell_add<<<GRID(n)>>>(n, x, y, ctr);
+}
+void launch_interp_coef(const DevParams& P, const double* dist, const double* bdr, double* fpd, double* rho, double* eta,
+                        ull* ctr, cudaStream_t s) {
+    k_interp_coef<<<GRID((long)(P.nr + 2) * (P.nz + 2))>>>(P, dist, bdr, fpd, rho, eta, ctr);
+}
+void launch_mass_partial(int nr, int nz, const double* ph, const Dots& d, int slot, ull* ctr, cudaStream_t s) {
+    k_mass_partial<<<d.G, DRD_TPB, 0, s>>>(nr, nz, ph, d, slot, ctr);
+}
+void launch_mass_final(const Dots& d, int slot, double drdz, double* out, ull* ctr, cudaStream_t s) {
+    k_mass_final<<<1, DRD_TPB, 0, s>>>(d, slot, drdz, out, ctr);
+}
+
+template <typename T>
+void launch_bi_init1(long n, const T* b, const T* x, T* r, const Dots& d, ull* ctr, cudaStream_t s) {
+    k_bi_init1<T><<<d.G, DRD_TPB, 0, s>>>(n, b, x, r, d, ctr);
+}
+void launch_bi_init2(KState* ks, const Dots& d, double tol, int maxit, const KState* parent, ull* ctr, cudaStream_t s) {
+    k_bi_init2<<<1, DRD_TPB, 0, s>>>(ks, d, tol, maxit, parent, ctr);
+}
+void launch_bi_init3(KState* ks, const Dots& d, ull* ctr, cudaStream_t s) { k_bi_init3<<<1, DRD_TPB, 0, s>>>(ks, d, ctr); }
+template <typename T>
+void launch_bi_init4(long n, const T* r, T* rtld, const Dots& d, const KState* ks, ull* ctr, cudaStream_t s) {
+    k_bi_init4<T><<<d.G, DRD_TPB, 0, s>>>(n, r, rtld, d, ks, ctr);
+}
+void launch_bi_rho(KState* ks, const Dots& d, ull* ctr, cudaStream_t s) { k_bi_rho<<<1, DRD_TPB, 0, s>>>(ks, d, ctr); }
+template <typename T>
+void launch_bi_p(long n, const T* r, const T* v, T* p, T* phat, const T* diag, int ident, const KState* ks, ull* ctr,
+                 cudaStream_t s) {
+    k_bi_p<T><<<GRID(n)>>>(n, r, v, p, phat, diag, ident, ks, ctr);
+}
+void launch_bi_alpha(KState* ks, const Dots& d, ull* ctr, cudaStream_t s) { k_bi_alpha<<<1, DRD_TPB, 0, s>>>(ks, d, ctr); }
+template <typename T>
+void launch_bi_s(long n, const T* v, T* r, const Dots& d, const KState* ks, ull* ctr, cudaStream_t s) {
+    k_bi_s<T><<<d.G, DRD_TPB, 0, s>>>(n, v, r, d, ks, ctr);
+}
+void launch_bi_snorm(KState* ks, const Dots& d, ull* ctr, cudaStream_t s) { k_bi_snorm<<<1, DRD_TPB, 0, s>>>(ks, d, ctr); }
+template <typename T>
+void launch_bi_diag_apply(long n, const T* x, const T* diag, int ident, T* y, const KState* ks, int gate, ull* ctr,
+                          cudaStream_t s) {
+    k_bi_diag_apply<T><<<GRID(n)>>>(n, x, diag, ident, y, ks, gate, ctr);
+}
+void launch_bi_omega(KState* ks, const Dots& d, ull* ctr, cudaStream_t s) { k_bi_omega<<<1, DRD_TPB, 0, s>>>(ks, d, ctr); }
+template <typename T>
+void launch_bi_xr(long n, const T* phat, const T* shat, const T* t, const T* rtld, T* x, T* r, const Dots& d,
+                  const KState* ks, ull* ctr, cudaStream_t s) {
+    k_bi_xr<T><<<d.G, DRD_TPB, 0, s>>>(n, phat, shat, t, rtld, x, r, d, ks, ctr);
+}
+void launch_bi_end(KState* ks, const Dots& d, cudaGraphConditionalHandle h, int use_graph, ull* ctr, cudaStream_t s) {
+    k_bi_end<<<1, DRD_TPB, 0, s>>>(ks, d, h, use_graph, ctr);
+}
+void launch_bi_true_resid(KState* ks, const Dots& d, ull* ctr, cudaStream_t s) {
+    k_bi_true_resid<<<1, DRD_TPB, 0, s>>>(ks, d, ctr);
+}
+template <typename T>
+void launch_copy(long n, const T* x, T* y, ull* ctr, cudaStream_t s) { k_copy<T><<<GRID(n)>>>(n, x, y, ctr); }
+template <typename T>
+void launch_norm2_partial(long n, const T* x, const Dots& d, int slot, ull* ctr, cudaStream_t s) {
+    k_norm2_partial<T><<<d.G, DRD_TPB, 0, s>>>(n, x, d, slot, ctr);
+}
+template <typename TO, typename TI>
+void launch_convert_scale(long n, const TI* x, double scale, TO* y, ull* ctr, cudaStream_t s) {
+    k_convert<TO, TI><<<GRID(n)>>>(n, x, scale, y, ctr);
+}
+template void launch_convert_scale<float, double>(long, const double*, double, float*, ull*, cudaStream_t);
+template void launch_convert_scale<double, float>(long, const float*, double, double*, ull*, cudaStream_t);
+template void launch_convert_scale<double, double>(long, const double*, double, double*, ull*, cudaStream_t);
+
+void launch_axpy_f2d(long n, const KState* ks, const float* d, double* x, ull* ctr, cudaStream_t s) {
+    k_axpy_f2d<<<GRID(n)>>>(n, ks, d, x, ctr);
+}
+void launch_mx_init(KState* outer, const Dots& d, double tol, int max_refine, ull* ctr, cudaStream_t s) {
+    k_mx_init<<<1, DRD_TPB, 0, s>>>(outer, d, tol, max_refine, ctr);
+}
+void launch_mx_inner_setup(KState* inner, const KState* outer, double inner_tol, int inner_maxit, ull* ctr,
+                           cudaStream_t s) {
+    k_mx_inner_setup<<<1, 32, 0, s>>>(inner, outer, inner_tol, inner_maxit, ctr);
+}
+void launch_mx_check(KState* outer, const KState* inner, const Dots& d, cudaGraphConditionalHandle h, int use_graph,
+                     ull* ctr, cudaStream_t s) {
+    k_mx_check<<<1, DRD_TPB, 0, s>>>(outer, inner, d, h, use_graph, ctr);
+}
+template <typename TO>
+void launch_mx_scale(long n, const double* r, const KState* o, TO* y, TO* zero, ull* ctr, cudaStream_t s) {
+    k_mx_scale_from_state<TO><<<GRID(n)>>>(n, r, o, y, zero, ctr);
+}
+template void launch_mx_scale<float>(long, const double*, const KState*, float*, float*, ull*, cudaStream_t);
+
+#define INST(T)                                                                                                        \
+    template void launch_ch_matvec<T>(const OpScal<T>&, const T*, const T*, T, const T*, T, T*, T*, const T*, int,     \
+                                      const Dots&, int, const KState*, int, ull*, cudaStream_t);                      \
+    template void launch_phmu_matvec<T>(const OpScal<T>&, const T*, const T*, const T*, T, const T*, T, T*, const T*,  \
+                                        int, const Dots&, int, const KState*, int, ull*, cudaStream_t);               \
+    template void launch_phmu_diag<T>(const OpScal<T>&, T*, ull*, cudaStream_t);                                      \
+    template void launch_uv_matvec<T>(const OpScal<T>&, const T*, const T*, const T*, T, const T*, T, T*, const T*,    \
+                                      int, const Dots&, int, const KState*, int, ull*, cudaStream_t);                 \
+    template void launch_uv_diag<T>(const OpScal<T>&, const T*, const T*, T*, ull*, cudaStream_t);                    \
+    template void launch_bi_init1<T>(long, const T*, const T*, T*, const Dots&, ull*, cudaStream_t);                  \
+    template void launch_bi_init4<T>(long, const T*, T*, const Dots&, const KState*, ull*, cudaStream_t);             \
+    template void launch_bi_p<T>(long, const T*, const T*, T*, T*, const T*, int, const KState*, ull*, cudaStream_t); \
+    template void launch_bi_s<T>(long, const T*, T*, const Dots&, const KState*, ull*, cudaStream_t);                 \
+    template void launch_bi_diag_apply<T>(long, const T*, const T*, int, T*, const KState*, int, ull*, cudaStream_t); \
+    template void launch_bi_xr<T>(long, const T*, const T*, const T*, const T*, T*, T*, const Dots&, const KState*,   \
+                                  ull*, cudaStream_t);                                                                \
+    template void launch_copy<T>(long, const T*, T*, ull*, cudaStream_t);                                            \
+    template void launch_norm2_partial<T>(long, const T*, const Dots&, int, ull*, cudaStream_t);
+INST(double)
+INST(float)
+#undef INST
+
+}  // namespace drd

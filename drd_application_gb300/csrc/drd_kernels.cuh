@@ -1,0 +1,143 @@
+// drd_kernels.cuh — host launchers of the solver-core kernels (defined in drd_kernels.cu).
+#pragma once
+
+#include "drd_common.cuh"
+
+namespace drd {
+
+typedef unsigned long long ull;
+
+// Gate of a kernel on the Krylov state: always run, run while the solve is running, or run
+// while running and the initial guess is nonzero (the ||x0|| != 0 branch of
+// lib/BiCGSTABREVCOM.f:230).
+enum Gate : int { G_ALWAYS = 0, G_RUNNING = 1, G_XNZ = 2, G_EARLY_OR_RUNNING = 3 };
+
+// Scalars of the operators in the precision T of the Krylov vectors.
+template <typename T>
+struct OpScal {
+    T dt, xld, eps, s, idr2, idz2, dtxld, re, pk, dr, dz, dr2, dz2, adjust;
+    T cb, ct;  // ph_mu_solve coef_bot / coef_top
+    int nr, nz, variant, lr_neumann, bdf, phi_mode;
+};
+
+struct Dots {
+    double* part;      // partials buffer, slot s at part + s*DRD_MAXB
+    int G;             // blocks of the reduction grid
+};
+
+// ---- transforms (GEMM form) -----------------------------------------------------------
+enum Epi : int { EPI_STORE = 0, EPI_DIV_TAB = 1, EPI_PRE_FINAL = 2, EPI_SCALE = 3 };
+template <typename T>
+struct GemmArgs {
+    int M, N, K;
+    const T* A; long lda;   // row-major M x K
+    const T* B; long ldb;   // row-major K x N
+    T* C; long ldc;         // row-major M x N (EPI_PRE_FINAL: CELL field, ldc ignored)
+    const T* tab; long ldt; // EPI_DIV_TAB: C = acc / tab[m*ldt + n]
+    const CallArgs* ca;     // EPI_PRE_FINAL: coef
+    double scale;           // EPI_PRE_FINAL: divisor 4 nr nz; EPI_SCALE: multiplier
+    int nr;
+    const KState* ks; int gate;
+    ull* ctr;
+};
+int gemm_config_count();
+const char* gemm_config_name(int cfg);
+template <typename T>
+void launch_gemm(int cfg, int epi, const GemmArgs<T>& a, cudaStream_t s);
+
+// ---- CH (microfluidics_complex_domain/PhSolve.f90) -------------------------------------
+void launch_ch_f2(const DevParams& P, const double* u, const double* v, const double* ph, double* f2, ull* ctr, cudaStream_t s);
+void launch_ch_rhs(const DevParams& P, const double* ph, const double* rmu, const double* bdr, const double* grad,
+                   const double* Mi, const double* f2, double* b, double* x, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_ch_matvec(const OpScal<T>& o, const T* M0, const T* Mi, T alpha, const T* x, T beta, T* y, T* ff1,
+                      const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,
+                      cudaStream_t s);
+void launch_ch_fin(const DevParams& P, const double* x, const double* f2, const double* M0, double* rmu_after,
+                   double* ph_after, ull* ctr, cudaStream_t s);
+
+// ---- coupled CH (two_phase_flow_complex_domain/ph_mu_solve.f90) -----------------------
+void launch_phmu_prep(const DevParams& P, const double* u, const double* v, const double* ph, const double* bdr,
+                      const double* used, double* M0, double* f2, ull* ctr, cudaStream_t s);
+void launch_phmu_rhs(const DevParams& P, const double* ph, const double* rmu, const double* bdr, const double* grad,
+                     const double* f2, const double* cfB, const double* cfT, double* b, double* x, double* pnb,
+                     double* pnt, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_phmu_matvec(const OpScal<T>& o, const T* M0, const T* Mi, const T* used, T alpha, const T* x, T beta, T* y,
+                        const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,
+                        cudaStream_t s);
+template <typename T>
+void launch_phmu_diag(const OpScal<T>& o, T* diag, ull* ctr, cudaStream_t s);
+void launch_phmu_fin(const DevParams& P, const double* x, const double* pnb, const double* pnt, double cb, double ct,
+                     double* ph_after, double* rmu_after, ull* ctr, cudaStream_t s);
+
+// ---- momentum (microfluidics_complex_domain/VeloSolve_2_combined.f90) -----------------
+void launch_uv_rhs(const DevParams& P, int bdf, const CallArgs* ca, const double* psi1, const double* psi2,
+                   const double* u_pre, const double* u, const double* v_pre, const double* v, const double* p,
+                   const double* rho, const double* eta, const double* bdr, const double* used, const double* ph_after,
+                   const double* rmu_after, const double* pf1, const double* pf2, double* b, double* x, double* uL,
+                   ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_uv_matvec(const OpScal<T>& o, const T* rho, const T* eta, const T* pen, T alpha, const T* x, T beta, T* y,
+                      const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,
+                      cudaStream_t s);
+template <typename T>
+void launch_uv_diag(const OpScal<T>& o, const T* rho, const T* eta, T* diag, ull* ctr, cudaStream_t s);
+void launch_uv_fin(const DevParams& P, const double* x, const double* uL, double* u_after, double* v_after, ull* ctr,
+                   cudaStream_t s);
+
+// ---- pressure (microfluidics_complex_domain/PreSolve_2.f90) -----------------------------
+void launch_pre_div(const DevParams& P, const double* u, const double* v, double* w, ull* ctr, cudaStream_t s);
+void launch_fill_neumann(int nr, int nz, double* a, double* b, ull* ctr, cudaStream_t s);
+void launch_cell_add(long n, const double* x, double* y, ull* ctr, cudaStream_t s);  // y = x + y
+
+// ---- interpolate_coef / mass ----------------------------------------------------------
+void launch_interp_coef(const DevParams& P, const double* dist, const double* bdr, double* fpd, double* rho, double* eta,
+                        ull* ctr, cudaStream_t s);
+void launch_mass_partial(int nr, int nz, const double* ph, const Dots& d, int slot, ull* ctr, cudaStream_t s);
+void launch_mass_final(const Dots& d, int slot, double drdz, double* out, ull* ctr, cudaStream_t s);
+
+// ---- BiCGSTAB (lib/BiCGSTABREVCOM.f) ----------------------------------------------------
+template <typename T>
+void launch_bi_init1(long n, const T* b, const T* x, T* r, const Dots& d, ull* ctr, cudaStream_t s);
+void launch_bi_init2(KState* ks, const Dots& d, double tol, int maxit, const KState* parent, ull* ctr, cudaStream_t s);
+void launch_bi_init3(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_bi_init4(long n, const T* r, T* rtld, const Dots& d, const KState* ks, ull* ctr, cudaStream_t s);
+void launch_bi_rho(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_bi_p(long n, const T* r, const T* v, T* p, T* phat, const T* diag, int ident, const KState* ks, ull* ctr,
+                 cudaStream_t s);
+void launch_bi_alpha(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_bi_s(long n, const T* v, T* r, const Dots& d, const KState* ks, ull* ctr, cudaStream_t s);
+void launch_bi_snorm(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_bi_diag_apply(long n, const T* x, const T* diag, int ident, T* y, const KState* ks, int gate, ull* ctr,
+                          cudaStream_t s);
+void launch_bi_omega(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_bi_xr(long n, const T* phat, const T* shat, const T* t, const T* rtld, T* x, T* r, const Dots& d,
+                  const KState* ks, ull* ctr, cudaStream_t s);
+void launch_bi_end(KState* ks, const Dots& d, cudaGraphConditionalHandle h, int use_graph, ull* ctr, cudaStream_t s);
+void launch_bi_true_resid(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
+
+// ---- vectors ---------------------------------------------------------------------------
+template <typename T>
+void launch_copy(long n, const T* x, T* y, ull* ctr, cudaStream_t s);
+template <typename TO, typename TI>
+void launch_convert_scale(long n, const TI* x, double scale, TO* y, ull* ctr, cudaStream_t s);  // y = scale * x
+void launch_axpy_f2d(long n, const KState* ks, const float* d, double* x, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_norm2_partial(long n, const T* x, const Dots& d, int slot, ull* ctr, cudaStream_t s);
+
+// ---- mixed-precision refinement control -------------------------------------------------
+void launch_mx_init(KState* outer, const Dots& d, double tol, int max_refine, ull* ctr, cudaStream_t s);
+void launch_mx_inner_setup(KState* inner, const KState* outer, double inner_tol, int inner_maxit, ull* ctr,
+                           cudaStream_t s);
+void launch_mx_check(KState* outer, const KState* inner, const Dots& d, cudaGraphConditionalHandle h, int use_graph,
+                     ull* ctr, cudaStream_t s);
+template <typename TO>
+void launch_mx_scale(long n, const double* r, const KState* o, TO* y, TO* zero, ull* ctr, cudaStream_t s);
+
+}  // namespace drd

@@ -1,0 +1,1119 @@
+// drd_solver.cu — context, solve sequences, CUDA-graph capture and the extern "C" entry
+// points of include/drd_gb300.h.
+//
+// Each reference subroutine becomes one captured CUDA graph: its RHS kernels, a BiCGSTAB
+// whose iteration loop is a device-side WHILE conditional node (the loop never returns to
+// the host; the last kernel of each iteration decides whether another one runs), and the
+// finalisation kernels.  A full time step (drd_step) is one graph holding all three solves.
+// In mixed precision the FP32 BiCGSTAB is nested in a second WHILE loop of FP64 iterative
+// refinement (true residual b - A x recomputed in FP64 at every restart).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "drd_kernels.cuh"
+
+using namespace drd;
+
+namespace {
+
+enum SysKind { SYS_CH = 0, SYS_UV = 1, SYS_PHMU = 2 };
+enum { KS_CH = 0, KS_UV = 1, KS_PHMU = 2, KS_INNER = 3, KS_PRE = 4, KS_MASS = 5, KS_COUNT = 6 };
+
+template <typename T>
+struct KVecs {
+    T *x, *b, *r, *rtld, *p, *v, *t, *phat, *shat, *tmp, *diag, *ff1;
+};
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+constexpr double kPimach = 3.14159265358979;  // lib/vfftpack.f:294
+
+}  // namespace
+
+struct drd_ctx {
+    drd_params P;
+    DevParams dp;
+    int nr = 0, nz = 0;
+    long cs = 0, us = 0, vs = 0, nc = 0, nuv = 0, nphmu = 0, nmax = 0;
+    cudaStream_t s = nullptr, s2 = nullptr, s3 = nullptr;
+    int device = 0;
+    char* arena = nullptr;
+    size_t arena_bytes = 0, arena_used = 0;
+    // coefficients (CELL)
+    double *rho, *eta, *bdr, *grad, *M0, *Mi, *pen, *used;
+    float *rho32, *eta32, *pen32, *M032, *Mi32, *used32;
+    // tables and transform matrices
+    double *ph_lcc, *pre_lcc;
+    float* ph_lcc32;
+    double *m1xT, *m1z, *m2xT, *m2z, *m3xT, *m3z;
+    float *m1xT32, *m1z32;
+    double *cfB, *cfT;
+    // resident state and scratch
+    double* fld[DRD_F_COUNT];
+    double *u_after, *v_after, *ph_after, *rmu_after, *f2, *uL, *pnb, *pnt, *dist, *fpd, *w, *t1, *t2;
+    float *t1f, *t2f;
+    KVecs<double> k64;
+    KVecs<float> k32;
+    double* part;
+    KState* ks;      // device, KS_COUNT entries
+    CallArgs* ca;    // device
+    double* d_mass;  // device
+    KState* h_ks;    // pinned
+    CallArgs* h_ca;  // pinned
+    double* h_mass;  // pinned
+    unsigned long long* ctr;
+    int G = 1;
+    int gcfg[2][2] = {{-1, -1}, {-1, -1}};  // [fp32?][z-pass?]
+    std::map<long, cudaGraphExec_t> graphs;
+    std::string err;
+    int use_graph = 1;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+#define CK(call)                                                                   \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess) {                                                   \
+            c->err = std::string(#call) + ": " + cudaGetErrorString(e_);           \
+            return DRD_ERR_CUDA;                                                   \
+        }                                                                          \
+    } while (0)
+
+template <typename T>
+T* carve(drd_ctx* c, long n) {
+    size_t bytes = ((size_t)(n > 0 ? n : 1) * sizeof(T) + 255) & ~(size_t)255;
+    T* p = (T*)(c->arena + c->arena_used);
+    c->arena_used += bytes;
+    return p;
+}
+
+size_t arena_need(long cs, long us, long vs, long nc, long nr, long nz, long nmax) {
+    size_t b = 0;
+    auto add = [&](size_t n, size_t sz) { b += ((n > 0 ? n : 1) * sz + 255) & ~(size_t)255; };
+    for (int i = 0; i < 8; ++i) add(cs, 8);      // coefficients
+    for (int i = 0; i < 6; ++i) add(cs, 4);      // FP32 coefficients
+    add(nc, 8); add((nr + 1) * (nz + 1), 8); add(nc, 4);
+    add(nr * nr, 8); add(nz * nz, 8); add(nr * nr, 8); add(nz * nz, 8); add(nr * nr, 8); add(nz * nz, 8);
+    add(nr * nr, 4); add(nz * nz, 4);
+    add(nr + 1, 8); add(nr + 1, 8);
+    for (int f = 0; f < DRD_F_COUNT; ++f) add(std::max(us, cs), 8);
+    add(us, 8); add(vs, 8); add(cs, 8); add(cs, 8); add(cs, 8); add(nz + 1, 8); add(nr, 8); add(nr, 8);
+    add(nc, 8); add(cs, 8); add(nc, 8); add(nc, 8); add(nc, 8); add(nc, 4); add(nc, 4);
+    for (int i = 0; i < 12; ++i) add(nmax, 8);
+    for (int i = 0; i < 12; ++i) add(nmax, 4);
+    add(DRD_NDOT * DRD_MAXB, 8);
+    add(KS_COUNT * sizeof(KState), 1); add(sizeof(CallArgs), 1); add(1, 8); add(1, 8);
+    return b + 4096;
+}
+
+DevParams make_dev_params(const drd_params& P) {
+    DevParams d{};
+    d.nr = P.nr; d.nz = P.nz; d.variant = P.variant; d.phi_mode = P.phi_mode;
+    d.lr_neumann = (P.variant == DRD_VARIANT_TP && P.lr_bd_type == 'n');
+    d.dr = P.dr; d.dz = P.dz; d.dr2 = P.dr * P.dr; d.dz2 = P.dz * P.dz;
+    d.idr2 = 1.0 / d.dr2; d.idz2 = 1.0 / d.dz2;
+    d.dt = P.dt; d.xld = P.xld; d.re = P.re; d.ca = P.ca; d.eps = P.I_thickness; d.s = P.s_implicit;
+    d.ggx = P.ggx; d.ggz = P.ggz; d.uwT = P.uwT; d.uwB = P.uwB; d.UU = P.UU; d.twall = P.twall;
+    d.bdr_upp = P.bdr_upp; d.bdr_low = P.bdr_low;
+    d.cang = std::cos(P.angle * kPi / 180);
+    d.penalty_k = P.penalty_k; d.lambda_rho = P.lambda_rho; d.lambda_eta = P.lambda_eta;
+    d.adjust = P.bdr_ph_used_adjust;
+    return d;
+}
+
+template <typename T>
+OpScal<T> make_op(const drd_ctx* c, int bdf) {
+    const DevParams& d = c->dp;
+    OpScal<T> o{};
+    o.dt = (T)d.dt; o.xld = (T)d.xld; o.eps = (T)d.eps; o.s = (T)d.s; o.idr2 = (T)d.idr2; o.idz2 = (T)d.idz2;
+    o.dtxld = (T)(d.dt * d.xld); o.re = (T)d.re; o.pk = (T)d.penalty_k; o.dr = (T)d.dr; o.dz = (T)d.dz;
+    o.dr2 = (T)d.dr2; o.dz2 = (T)d.dz2; o.adjust = (T)d.adjust;
+    const double tmp = d.eps / d.dz;
+    o.cb = (T)((d.eps / d.dz) / tmp);  // coef_bot = (I/dz)/tmp (ph_mu_solve.f90:123)
+    o.ct = o.cb;
+    o.nr = d.nr; o.nz = d.nz; o.variant = d.variant; o.lr_neumann = d.lr_neumann; o.bdf = bdf; o.phi_mode = d.phi_mode;
+    return o;
+}
+
+// setup() tables (microfluidics_complex_domain/setup.f90:106-155), FP64 on the host.
+void host_tables(const drd_params& P, std::vector<double>& ph_lcc, std::vector<double>& pre_lcc) {
+    const int nr = P.nr, nz = P.nz;
+    const double dr2 = P.dr * P.dr, dz2 = P.dz * P.dz;
+    pre_lcc.assign((size_t)(nr + 1) * (nz + 1), 0.0);
+    ph_lcc.assign((size_t)nr * nz, 0.0);
+    for (int j = 0; j <= nz; ++j) {
+        double t1 = kPi * j / 2.0 / nz, fmy = 4.0 * (std::sin(t1) * std::sin(t1)) / dz2;
+        for (int i = 0; i <= nr; ++i) {
+            double t0 = kPi * i / 2.0 / nr, fmx = 4.0 * (std::sin(t0) * std::sin(t0)) / dr2;
+            pre_lcc[i + (size_t)j * (nr + 1)] = -(fmx + fmy);
+        }
+    }
+    pre_lcc[0] = -1.0;
+    for (int j = 0; j < nz; ++j) {
+        double t1 = kPi * j / 2.0 / (nz - 1), fmy = 4.0 * (std::sin(t1) * std::sin(t1)) / dz2;
+        for (int i = 0; i < nr; ++i) {
+            double t0 = kPi * i / 2.0 / (nr - 1), fmx = 4.0 * (std::sin(t0) * std::sin(t0)) / dr2;
+            double temp = fmx + fmy;
+            ph_lcc[i + (size_t)j * nr] =
+                1. + P.xld * P.dt * P.s_implicit * temp / P.I_thickness + P.xld * P.I_thickness * P.dt * (temp * temp);
+        }
+    }
+}
+
+// Transform matrices.  D1[o][j]: VCOST of length n (lib/vfftpack.f:689-704, pi = PIMACH);
+// D2[o][j]: REDFT10; D3[o][j]: REDFT01 (FFTW manual).  Entries use an exact periodic table.
+void host_dct_mats(int n, std::vector<double>& d1, std::vector<double>& d2, std::vector<double>& d3) {
+    d1.assign((size_t)n * n, 0.0);
+    d2.assign((size_t)n * n, 0.0);
+    d3.assign((size_t)n * n, 0.0);
+    if (n >= 2) {
+        const long per = 2L * (n - 1);
+        std::vector<double> tab(per);
+        for (long q = 0; q < per; ++q) tab[q] = std::cos((double)q * kPimach / (double)(n - 1));
+        const double sc = std::sqrt(2.0 * (n - 1));
+        for (int o = 0; o < n; ++o)
+            for (int j = 0; j < n; ++j) {
+                double w = (j == 0) ? 1.0 : (j == n - 1 ? ((o & 1) ? -1.0 : 1.0) : 2.0 * tab[((long)o * j) % per]);
+                d1[(size_t)o * n + j] = w / sc;
+            }
+    }
+    const long per4 = 4L * n;
+    std::vector<double> t4(per4);
+    for (long q = 0; q < per4; ++q) t4[q] = std::cos(kPi * (double)q / (2.0 * n));
+    for (int o = 0; o < n; ++o)
+        for (int j = 0; j < n; ++j) {
+            d2[(size_t)o * n + j] = 2.0 * t4[((long)(2 * j + 1) * o) % per4];
+            d3[(size_t)o * n + j] = (j == 0) ? 1.0 : 2.0 * t4[((long)j * (2 * o + 1)) % per4];
+        }
+}
+
+std::vector<double> transpose(const std::vector<double>& a, int n) {
+    std::vector<double> t(a.size());
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) t[(size_t)j * n + i] = a[(size_t)i * n + j];
+    return t;
+}
+
+template <typename T>
+KVecs<T> carve_vecs(drd_ctx* c) {
+    KVecs<T> k;
+    T** f[] = {&k.x, &k.b, &k.r, &k.rtld, &k.p, &k.v, &k.t, &k.phat, &k.shat, &k.tmp, &k.diag, &k.ff1};
+    for (auto* pp : f) *pp = carve<T>(c, c->nmax);
+    return k;
+}
+
+Dots dots(drd_ctx* c) { return Dots{c->part, c->G}; }
+KVecs<double>& vecs(drd_ctx* c, double*) { return c->k64; }
+KVecs<float>& vecs(drd_ctx* c, float*) { return c->k32; }
+
+// ---- transforms --------------------------------------------------------------------------
+template <typename T>
+const T* mat(const drd_ctx* c, int which);
+template <>
+const double* mat<double>(const drd_ctx* c, int which) { return which == 0 ? c->m1xT : c->m1z; }
+template <>
+const float* mat<float>(const drd_ctx* c, int which) { return which == 0 ? c->m1xT32 : c->m1z32; }
+
+template <typename T>
+T* tmp1(drd_ctx* c);
+template <>
+double* tmp1<double>(drd_ctx* c) { return c->t1; }
+template <>
+float* tmp1<float>(drd_ctx* c) { return c->t1f; }
+template <typename T>
+T* tmp2(drd_ctx* c);
+template <>
+double* tmp2<double>(drd_ctx* c) { return c->t2; }
+template <>
+float* tmp2<float>(drd_ctx* c) { return c->t2f; }
+
+template <typename T>
+GemmArgs<T> gargs(drd_ctx* c, int M, int N, int K, const T* A, long lda, const T* B, long ldb, T* C, long ldc,
+                  const KState* ks, int gate) {
+    GemmArgs<T> a{};
+    a.M = M; a.N = N; a.K = K; a.A = A; a.lda = lda; a.B = B; a.ldb = ldb; a.C = C; a.ldc = ldc;
+    a.nr = c->nr; a.ks = ks; a.gate = gate; a.ctr = c->ctr; a.ca = c->ca; a.scale = 1.0;
+    return a;
+}
+
+template <typename T>
+int gcfg(drd_ctx* c, int zpass) { return c->gcfg[sizeof(T) == 4][zpass]; }
+
+// PSolve_CG (microfluidics_complex_domain/PhSolve.f90:296-313): y = C (C x ./ Ph_Lcc) with the
+// separable 2-D DCT-I C = VCOST_x VCOST_z, as four GEMM passes (x, z, x, z).
+template <typename T>
+void enq_ch_psolve(drd_ctx* c, const T* x, T* y, const KState* ks, int gate, cudaStream_t s) {
+    const int nr = c->nr, nz = c->nz;
+    T* t1 = tmp1<T>(c);
+    T* t2 = tmp2<T>(c);
+    const T* mx = mat<T>(c, 0);
+    const T* mz = mat<T>(c, 1);
+    const T* tab = (sizeof(T) == 8) ? (const T*)c->ph_lcc : (const T*)c->ph_lcc32;
+    launch_gemm<T>(gcfg<T>(c, 0), EPI_STORE, gargs<T>(c, nz, nr, nr, x, nr, mx, nr, t1, nr, ks, gate), s);
+    auto a2 = gargs<T>(c, nz, nr, nz, mz, nz, t1, nr, t2, nr, ks, gate);
+    a2.tab = tab; a2.ldt = nr;
+    launch_gemm<T>(gcfg<T>(c, 1), EPI_DIV_TAB, a2, s);
+    launch_gemm<T>(gcfg<T>(c, 0), EPI_STORE, gargs<T>(c, nz, nr, nr, t2, nr, mx, nr, t1, nr, ks, gate), s);
+    launch_gemm<T>(gcfg<T>(c, 1), EPI_STORE, gargs<T>(c, nz, nr, nz, mz, nz, t1, nr, y, nr, ks, gate), s);
+}
+
+// ---- generic system operations -------------------------------------------------------------
+struct Sys {
+    int kind;
+    int bdf;
+    long n;
+    int jacobi;  // diagonal preconditioner in k.diag
+    int ident;   // identity preconditioner
+};
+
+template <typename T>
+const T* coef(drd_ctx* c, int which);  // 0 rho 1 eta 2 pen 3 M0 4 Mi 5 used
+template <>
+const double* coef<double>(drd_ctx* c, int w) {
+    const double* a[] = {c->rho, c->eta, c->pen, c->M0, c->Mi, c->used};
+    return a[w];
+}
+template <>
+const float* coef<float>(drd_ctx* c, int w) {
+    const float* a[] = {c->rho32, c->eta32, c->pen32, c->M032, c->Mi32, c->used32};
+    return a[w];
+}
+
+template <typename T>
+void enq_matvec(drd_ctx* c, const Sys& S, T alpha, const T* x, T beta, T* y, const T* dot1, int self2, int slot1,
+                const KState* ks, int gate, cudaStream_t s) {
+    Dots d = dots(c);
+    KVecs<T>& k = vecs(c, (T*)nullptr);
+    if (S.kind == SYS_CH) {
+        launch_ch_matvec<T>(make_op<T>(c, 0), coef<T>(c, 3), coef<T>(c, 4), alpha, x, beta, y, k.ff1, dot1, self2, d,
+                            slot1, ks, gate, c->ctr, s);
+    } else if (S.kind == SYS_UV) {
+        launch_uv_matvec<T>(make_op<T>(c, S.bdf), coef<T>(c, 0), coef<T>(c, 1), coef<T>(c, 2), alpha, x, beta, y,
+                            dot1, self2, d, slot1, ks, gate, c->ctr, s);
+    } else {
+        launch_phmu_matvec<T>(make_op<T>(c, 0), coef<T>(c, 3), coef<T>(c, 4), coef<T>(c, 5), alpha, x, beta, y, dot1,
+                              self2, d, slot1, ks, gate, c->ctr, s);
+    }
+}
+
+template <typename T>
+void enq_psolve(drd_ctx* c, const Sys& S, const T* x, T* y, const KState* ks, int gate, cudaStream_t s) {
+    KVecs<T>& k = vecs(c, (T*)nullptr);
+    if (S.kind == SYS_CH) enq_ch_psolve<T>(c, x, y, ks, gate, s);
+    else launch_bi_diag_apply<T>(S.n, x, S.jacobi ? k.diag : nullptr, S.ident, y, ks, gate, c->ctr, s);
+}
+
+// Preconditioner diagonal for the systems that use one (set up once per solve).
+template <typename T>
+void enq_sys_setup(drd_ctx* c, const Sys& S, cudaStream_t s) {
+    KVecs<T>& k = vecs(c, (T*)nullptr);
+    if (S.kind == SYS_UV && S.jacobi) launch_uv_diag<T>(make_op<T>(c, S.bdf), coef<T>(c, 0), coef<T>(c, 1), k.diag, c->ctr, s);
+    if (S.kind == SYS_PHMU) launch_phmu_diag<T>(make_op<T>(c, 0), k.diag, c->ctr, s);
+}
+
+// One BiCGSTAB iteration (lib/BiCGSTABREVCOM.f:257-388).
+template <typename T>
+void enq_bicg_iter(drd_ctx* c, const Sys& S, KVecs<T>& k, KState* ks, cudaGraphConditionalHandle h, int use_graph,
+                   cudaStream_t s) {
+    Dots d = dots(c);
+    const long n = S.n;
+    launch_bi_rho(ks, d, c->ctr, s);
+    if (S.kind == SYS_CH) {
+        launch_bi_p<T>(n, k.r, k.v, k.p, k.phat, nullptr, 0, ks, c->ctr, s);
+        enq_psolve<T>(c, S, k.p, k.phat, ks, G_RUNNING, s);
+    } else {
+        launch_bi_p<T>(n, k.r, k.v, k.p, k.phat, S.jacobi ? k.diag : nullptr, S.ident || !S.jacobi, ks, c->ctr, s);
+    }
+    enq_matvec<T>(c, S, T(1), k.phat, T(0), k.v, k.rtld, 0, 0, ks, G_RUNNING, s);
+    launch_bi_alpha(ks, d, c->ctr, s);
+    launch_bi_s<T>(n, k.v, k.r, d, ks, c->ctr, s);
+    launch_bi_snorm(ks, d, c->ctr, s);
+    enq_psolve<T>(c, S, k.r, k.shat, ks, G_RUNNING, s);
+    enq_matvec<T>(c, S, T(1), k.shat, T(0), k.t, k.r, 1, 1, ks, G_RUNNING, s);
+    launch_bi_omega(ks, d, c->ctr, s);
+    launch_bi_xr<T>(n, k.phat, k.shat, k.t, k.rtld, k.x, k.r, d, ks, c->ctr, s);
+    launch_bi_end(ks, d, h, use_graph, c->ctr, s);
+}
+
+// Start of the solve with the guess already in k.x (:229-255).
+template <typename T>
+void enq_bicg_setup(drd_ctx* c, const Sys& S, KVecs<T>& k, KState* ks, double tol, int maxit, const KState* parent,
+                    cudaStream_t s) {
+    Dots d = dots(c);
+    launch_bi_init1<T>(S.n, k.b, k.x, k.r, d, c->ctr, s);
+    launch_bi_init2(ks, d, tol, maxit, parent, c->ctr, s);
+    enq_matvec<T>(c, S, T(-1), k.x, T(1), k.r, nullptr, 1, -1, ks, G_XNZ, s);
+    launch_bi_init3(ks, d, c->ctr, s);
+    launch_bi_init4<T>(S.n, k.r, k.rtld, d, ks, c->ctr, s);
+}
+
+// Appends a WHILE conditional node to the graph being captured on `s` and captures
+// body(stream, handle) into its body graph on `sb`.
+int capture_while(drd_ctx* c, cudaStream_t s, cudaStream_t sb,
+                  const std::function<void(cudaStream_t, cudaGraphConditionalHandle)>& body) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
+    if (st != cudaStreamCaptureStatusActive) { c->err = "capture_while: stream not capturing"; return DRD_ERR_CUDA; }
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams p{};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+    CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraph_t bg = p.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(sb, bg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    body(sb, h);
+    cudaGraph_t out;
+    CK(cudaStreamEndCapture(sb, &out));
+    return DRD_OK;
+}
+
+// A whole Krylov solve of system S for k64.b with guess k64.x (FP64 result in k64.x).
+// FP64 mode: the reference's BiCGSTAB.  Mixed mode: FP64 iterative refinement around an FP32
+// BiCGSTAB with the same preconditioner.  `ks_slot` receives the status.
+int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int mixed, cudaStream_t s) {
+    KState* ks = c->ks + ks_slot;
+    KVecs<double>& k = c->k64;
+    Dots d = dots(c);
+    int rc = DRD_OK;
+    if (!mixed) {
+        enq_sys_setup<double>(c, S, s);
+        enq_bicg_setup<double>(c, S, k, ks, tol, maxit, nullptr, s);
+        rc = capture_while(c, s, c->s2, [&](cudaStream_t sb, cudaGraphConditionalHandle h) {
+            enq_bicg_iter<double>(c, S, k, ks, h, 1, sb);
+        });
+        if (rc) return rc;
+    } else {
+        KVecs<float>& f = c->k32;
+        KState* in = c->ks + KS_INNER;
+        enq_sys_setup<float>(c, S, s);
+        launch_copy<double>(S.n, k.b, k.r, c->ctr, s);
+        enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.r, nullptr, 1, -1, nullptr, G_ALWAYS, s);
+        launch_norm2_partial<double>(S.n, k.b, d, 3, c->ctr, s);
+        launch_mx_init(ks, d, tol, c->P.mixed_max_refine, c->ctr, s);
+        const double itol = c->P.mixed_inner_tol;
+        const int imax = maxit;
+        rc = capture_while(c, s, c->s2, [&](cudaStream_t sb, cudaGraphConditionalHandle ho) {
+            launch_mx_scale<float>(S.n, k.r, ks, f.b, f.x, c->ctr, sb);
+            enq_bicg_setup<float>(c, S, f, in, itol, imax, ks, sb);
+            int rc2 = capture_while(c, sb, c->s3, [&](cudaStream_t si, cudaGraphConditionalHandle hi) {
+                enq_bicg_iter<float>(c, S, f, in, hi, 1, si);
+            });
+            if (rc2) rc = rc2;
+            launch_axpy_f2d(S.n, ks, f.x, k.x, c->ctr, sb);
+            launch_copy<double>(S.n, k.b, k.r, c->ctr, sb);
+            enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.r, nullptr, 1, -1, nullptr, G_ALWAYS, sb);
+            launch_mx_check(ks, in, d, ho, 1, c->ctr, sb);
+        });
+        if (rc) return rc;
+    }
+    // true FP64 residual of the returned x
+    launch_copy<double>(S.n, k.b, k.tmp, c->ctr, s);
+    enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.tmp, nullptr, 1, -1, nullptr, G_ALWAYS, s);
+    launch_bi_true_resid(ks, d, c->ctr, s);
+    return DRD_OK;
+}
+
+// ---- the per-step routines as graph segments ------------------------------------------------
+Sys sys_of(drd_ctx* c, int kind, int bdf) {
+    Sys S{};
+    S.kind = kind;
+    S.bdf = bdf;
+    if (kind == SYS_CH) S.n = c->nc;
+    else if (kind == SYS_PHMU) { S.n = c->nphmu; S.jacobi = 1; }
+    else {
+        S.n = c->nuv;
+        const bool tp_ident = (c->P.variant == DRD_VARIANT_TP && bdf == 2);
+        S.jacobi = !tp_ident;
+        S.ident = tp_ident;
+    }
+    return S;
+}
+
+int mixed_of(drd_ctx* c) { return c->P.precision == DRD_PREC_MIXED; }
+
+// PhSolve (microfluidics_complex_domain/PhSolve.f90:1-126) on fld[U,V,PH,RMU] -> rmu_after, ph_after.
+int enq_ch(drd_ctx* c, cudaStream_t s) {
+    const DevParams& P = c->dp;
+    launch_ch_f2(P, c->fld[DRD_F_U], c->fld[DRD_F_V], c->fld[DRD_F_PH], c->f2, c->ctr, s);
+    launch_ch_rhs(P, c->fld[DRD_F_PH], c->fld[DRD_F_RMU], c->bdr, c->grad, c->Mi, c->f2, c->k64.b, c->k64.x, c->ctr, s);
+    int rc = enq_solve(c, sys_of(c, SYS_CH, 0), KS_CH, c->P.tol, c->P.ch_maxit, mixed_of(c), s);
+    if (rc) return rc;
+    launch_ch_fin(P, c->k64.x, c->f2, c->M0, c->rmu_after, c->ph_after, c->ctr, s);
+    return DRD_OK;
+}
+
+// ph_mu_solve (two_phase_flow_complex_domain/ph_mu_solve.f90:3-197).
+int enq_phmu(drd_ctx* c, cudaStream_t s) {
+    const DevParams& P = c->dp;
+    launch_phmu_prep(P, c->fld[DRD_F_U], c->fld[DRD_F_V], c->fld[DRD_F_PH], c->bdr, c->used, c->M0, c->f2, c->ctr, s);
+    launch_convert_scale<float, double>(c->cs, c->M0, 1.0, c->M032, c->ctr, s);
+    launch_phmu_rhs(P, c->fld[DRD_F_PH], c->fld[DRD_F_RMU], c->bdr, c->grad, c->f2, c->cfB, c->cfT, c->k64.b, c->k64.x,
+                    c->pnb, c->pnt, c->ctr, s);
+    int rc = enq_solve(c, sys_of(c, SYS_PHMU, 0), KS_PHMU, c->P.tol, c->P.phmu_maxit, mixed_of(c), s);
+    if (rc) return rc;
+    OpScal<double> o = make_op<double>(c, 0);
+    launch_phmu_fin(P, c->k64.x, c->pnb, c->pnt, o.cb, o.ct, c->ph_after, c->rmu_after, c->ctr, s);
+    return DRD_OK;
+}
+
+// VeloSolve_combined (bdf 1) / VeloSolve_2_combined (bdf 2) -> u_after, v_after.
+int enq_uv(drd_ctx* c, int bdf, cudaStream_t s) {
+    const DevParams& P = c->dp;
+    double** f = c->fld;
+    launch_uv_rhs(P, bdf, c->ca, f[DRD_F_PSI1], f[DRD_F_PSI2], f[DRD_F_U_PRE], f[DRD_F_U], f[DRD_F_V_PRE], f[DRD_F_V],
+                  f[DRD_F_P], c->rho, c->eta, c->bdr, c->used, c->ph_after, c->rmu_after, f[DRD_F_PF1], f[DRD_F_PF2],
+                  c->k64.b, c->k64.x, c->uL, c->ctr, s);
+    int rc = enq_solve(c, sys_of(c, SYS_UV, bdf), KS_UV, c->P.tol, c->P.uv_maxit, mixed_of(c), s);
+    if (rc) return rc;
+    launch_uv_fin(P, c->k64.x, c->uL, c->u_after, c->v_after, c->ctr, s);
+    return DRD_OK;
+}
+
+// PreSolve_2 + dct_fftw (microfluidics_complex_domain/PreSolve_2.f90:1-186) on fld[U,V] -> out.
+void enq_pre(drd_ctx* c, double* out, cudaStream_t s) {
+    const int nr = c->nr, nz = c->nz;
+    launch_pre_div(c->dp, c->fld[DRD_F_U], c->fld[DRD_F_V], c->w, c->ctr, s);
+    launch_gemm<double>(gcfg<double>(c, 0), EPI_STORE, gargs<double>(c, nz, nr, nr, c->w, nr, c->m2xT, nr, c->t1, nr, nullptr, G_ALWAYS), s);
+    auto a2 = gargs<double>(c, nz, nr, nz, c->m2z, nz, c->t1, nr, c->t2, nr, nullptr, G_ALWAYS);
+    a2.tab = c->pre_lcc; a2.ldt = nr + 1;
+    launch_gemm<double>(gcfg<double>(c, 1), EPI_DIV_TAB, a2, s);
+    launch_gemm<double>(gcfg<double>(c, 0), EPI_STORE, gargs<double>(c, nz, nr, nr, c->t2, nr, c->m3xT, nr, c->t1, nr, nullptr, G_ALWAYS), s);
+    auto a4 = gargs<double>(c, nz, nr, nz, c->m3z, nz, c->t1, nr, out, 0, nullptr, G_ALWAYS);
+    a4.scale = 4.0 * nr * nz;
+    launch_gemm<double>(gcfg<double>(c, 1), EPI_PRE_FINAL, a4, s);
+    launch_fill_neumann(nr, nz, out, nullptr, c->ctr, s);
+}
+
+void enq_mass(drd_ctx* c, const double* ph, cudaStream_t s) {
+    Dots d = dots(c);
+    launch_mass_partial(c->nr, c->nz, ph, d, 0, c->ctr, s);
+    launch_mass_final(d, 0, c->P.dr * c->P.dz, c->d_mass, c->ctr, s);
+}
+
+// The mcl6 step (microfluidics_complex_domain/mcl6.f90:239-306 first, :378-486 loop).
+int enq_step(drd_ctx* c, int first, cudaStream_t s) {
+    double** f = c->fld;
+    const size_t cb = sizeof(double) * c->cs, ub = sizeof(double) * c->us, vb = sizeof(double) * c->vs;
+    int rc = (c->P.variant == DRD_VARIANT_TP) ? enq_phmu(c, s) : enq_ch(c, s);
+    if (rc) return rc;
+    rc = enq_uv(c, first ? 1 : 2, s);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(f[DRD_F_U_PRE], f[DRD_F_U], ub, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(f[DRD_F_V_PRE], f[DRD_F_V], vb, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(f[DRD_F_U], c->u_after, ub, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(f[DRD_F_V], c->v_after, vb, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(f[DRD_F_PH_PRE], f[DRD_F_PH], cb, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(f[DRD_F_RMU_PRE], f[DRD_F_RMU], cb, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(f[DRD_F_PH], c->ph_after, cb, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(f[DRD_F_RMU], c->rmu_after, cb, cudaMemcpyDeviceToDevice, s));
+    if (!first) CK(cudaMemcpyAsync(f[DRD_F_PSI1], f[DRD_F_PSI2], cb, cudaMemcpyDeviceToDevice, s));
+    enq_pre(c, f[DRD_F_PSI2], s);
+    launch_cell_add(c->cs, f[DRD_F_PSI2], f[DRD_F_P], c->ctr, s);
+    enq_mass(c, f[DRD_F_PH], s);
+    return DRD_OK;
+}
+
+// Graph keys
+enum GraphKind { GK_CH = 1, GK_UV = 2, GK_PHMU = 3, GK_PRE = 4, GK_STEP = 5 };
+long gkey(int kind, int a, int b) { return (long)kind * 100 + a * 10 + b; }
+
+int get_graph(drd_ctx* c, long key, const std::function<int(cudaStream_t)>& build, cudaGraphExec_t* out) {
+    auto it = c->graphs.find(key);
+    if (it != c->graphs.end()) { *out = it->second; return DRD_OK; }
+    CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
+    int rc = build(c->s);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->s, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) { c->err = std::string("capture: ") + cudaGetErrorString(e); return DRD_ERR_CUDA; }
+    cudaGraphExec_t ex;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { c->err = std::string("instantiate: ") + cudaGetErrorString(e); return DRD_ERR_CUDA; }
+    c->graphs[key] = ex;
+    *out = ex;
+    return DRD_OK;
+}
+
+void clear_graphs(drd_ctx* c) {
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();
+}
+
+// ---- GEMM tile autotuner: times each tile configuration on the context's transform shapes --
+template <typename T>
+int tune_pass(drd_ctx* c, int zpass) {
+    const int nr = c->nr, nz = c->nz;
+    const char* env = std::getenv("DRD_GEMM_CFG");
+    if (env) { int v = std::atoi(env); if (v >= 0 && v < gemm_config_count()) return v; }
+    int best = 0;
+    float best_ms = 1e30f;
+    T* t1 = tmp1<T>(c);
+    T* t2 = tmp2<T>(c);
+    const T* mx = mat<T>(c, 0);
+    const T* mz = mat<T>(c, 1);
+    for (int cfg = 0; cfg < gemm_config_count(); ++cfg) {
+        auto a = zpass ? gargs<T>(c, nz, nr, nz, mz, nz, t1, nr, t2, nr, nullptr, G_ALWAYS)
+                       : gargs<T>(c, nz, nr, nr, t1, nr, mx, nr, t2, nr, nullptr, G_ALWAYS);
+        a.ctr = nullptr;
+        launch_gemm<T>(cfg, EPI_STORE, a, c->s);  // warm-up
+        cudaEventRecord(c->ev0, c->s);
+        for (int r = 0; r < 5; ++r) launch_gemm<T>(cfg, EPI_STORE, a, c->s);
+        cudaEventRecord(c->ev1, c->s);
+        cudaEventSynchronize(c->ev1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        if (cudaGetLastError() != cudaSuccess) continue;
+        if (ms < best_ms) { best_ms = ms; best = cfg; }
+    }
+    return best;
+}
+
+int ensure_tuned(drd_ctx* c) {
+    if (c->gcfg[0][0] >= 0) return DRD_OK;
+    CK(cudaMemsetAsync(c->t1, 0, sizeof(double) * c->nc, c->s));
+    CK(cudaMemsetAsync(c->t1f, 0, sizeof(float) * c->nc, c->s));
+    c->gcfg[0][0] = tune_pass<double>(c, 0);
+    c->gcfg[0][1] = tune_pass<double>(c, 1);
+    c->gcfg[1][0] = tune_pass<float>(c, 0);
+    c->gcfg[1][1] = tune_pass<float>(c, 1);
+    CK(cudaStreamSynchronize(c->s));
+    return DRD_OK;
+}
+
+int run_graph(drd_ctx* c, long key, const std::function<int(cudaStream_t)>& build, double t, double coef) {
+    int rc = ensure_tuned(c);
+    if (rc) return rc;
+    cudaGraphExec_t ex;
+    rc = get_graph(c, key, build, &ex);
+    if (rc) return rc;
+    c->h_ca->t = t;
+    c->h_ca->cf = 1.0 - std::exp(-t / c->P.twall);
+    c->h_ca->coef = coef;
+    CK(cudaMemcpyAsync(c->ca, c->h_ca, sizeof(CallArgs), cudaMemcpyHostToDevice, c->s));
+    CK(cudaGraphLaunch(ex, c->s));
+    return DRD_OK;
+}
+
+void fill_status(const KState& k, drd_status* st, int mixed, double secs) {
+    if (!st) return;
+    st->info = k.info;
+    st->iter = mixed ? k.inner_total : k.iter;
+    st->resid = k.resid;
+    st->true_resid = k.true_resid;
+    st->refinements = mixed ? k.outer : 0;
+    st->flags = k.flags;
+    st->seconds = secs;
+}
+
+int check_ctx(drd_ctx* c) { return c ? DRD_OK : DRD_ERR_BADARG; }
+
+int up(drd_ctx* c, double* dst, const double* src, long n) {
+    if (!src) return DRD_OK;
+    CK(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
+    return DRD_OK;
+}
+int down(drd_ctx* c, double* dst, const double* src, long n) {
+    if (!dst) return DRD_OK;
+    CK(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+    return DRD_OK;
+}
+
+int refresh_fp32(drd_ctx* c) {
+    launch_convert_scale<float, double>(c->cs, c->rho, 1.0, c->rho32, nullptr, c->s);
+    launch_convert_scale<float, double>(c->cs, c->eta, 1.0, c->eta32, nullptr, c->s);
+    launch_convert_scale<float, double>(c->cs, c->pen, 1.0, c->pen32, nullptr, c->s);
+    launch_convert_scale<float, double>(c->cs, c->M0, 1.0, c->M032, nullptr, c->s);
+    launch_convert_scale<float, double>(c->cs, c->Mi, 1.0, c->Mi32, nullptr, c->s);
+    launch_convert_scale<float, double>(c->cs, c->used, 1.0, c->used32, nullptr, c->s);
+    CK(cudaGetLastError());
+    return DRD_OK;
+}
+
+int upload_tables(drd_ctx* c) {
+    std::vector<double> ph, pre;
+    host_tables(c->P, ph, pre);
+    CK(cudaMemcpy(c->ph_lcc, ph.data(), sizeof(double) * ph.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->pre_lcc, pre.data(), sizeof(double) * pre.size(), cudaMemcpyHostToDevice));
+    launch_convert_scale<float, double>(c->nc, c->ph_lcc, 1.0, c->ph_lcc32, nullptr, c->s);
+    CK(cudaStreamSynchronize(c->s));
+    return DRD_OK;
+}
+
+int setup_context(drd_ctx* c) {
+    const int nr = c->nr, nz = c->nz;
+    CK(cudaGetDevice(&c->device));
+    CK(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->s3, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&c->ev0));
+    CK(cudaEventCreate(&c->ev1));
+    c->arena_bytes = arena_need(c->cs, c->us, c->vs, c->nc, nr, nz, c->nmax);
+    CK(cudaMalloc(&c->arena, c->arena_bytes));
+    CK(cudaMemset(c->arena, 0, c->arena_bytes));
+    double** cf[] = {&c->rho, &c->eta, &c->bdr, &c->grad, &c->M0, &c->Mi, &c->pen, &c->used};
+    for (auto* pp : cf) *pp = carve<double>(c, c->cs);
+    float** cf32[] = {&c->rho32, &c->eta32, &c->pen32, &c->M032, &c->Mi32, &c->used32};
+    for (auto* pp : cf32) *pp = carve<float>(c, c->cs);
+    c->ph_lcc = carve<double>(c, c->nc);
+    c->pre_lcc = carve<double>(c, (long)(nr + 1) * (nz + 1));
+    c->ph_lcc32 = carve<float>(c, c->nc);
+    c->m1xT = carve<double>(c, (long)nr * nr); c->m1z = carve<double>(c, (long)nz * nz);
+    c->m2xT = carve<double>(c, (long)nr * nr); c->m2z = carve<double>(c, (long)nz * nz);
+    c->m3xT = carve<double>(c, (long)nr * nr); c->m3z = carve<double>(c, (long)nz * nz);
+    c->m1xT32 = carve<float>(c, (long)nr * nr); c->m1z32 = carve<float>(c, (long)nz * nz);
+    c->cfB = carve<double>(c, nr + 1); c->cfT = carve<double>(c, nr + 1);
+    for (int f = 0; f < DRD_F_COUNT; ++f) c->fld[f] = carve<double>(c, std::max(c->us, c->cs));
+    c->u_after = carve<double>(c, c->us); c->v_after = carve<double>(c, c->vs);
+    c->ph_after = carve<double>(c, c->cs); c->rmu_after = carve<double>(c, c->cs); c->f2 = carve<double>(c, c->cs);
+    c->uL = carve<double>(c, nz + 1); c->pnb = carve<double>(c, nr); c->pnt = carve<double>(c, nr);
+    c->dist = carve<double>(c, c->nc); c->fpd = carve<double>(c, c->cs); c->w = carve<double>(c, c->nc);
+    c->t1 = carve<double>(c, c->nc); c->t2 = carve<double>(c, c->nc);
+    c->t1f = carve<float>(c, c->nc); c->t2f = carve<float>(c, c->nc);
+    c->k64 = carve_vecs<double>(c);
+    c->k32 = carve_vecs<float>(c);
+    c->part = carve<double>(c, DRD_NDOT * DRD_MAXB);
+    c->ks = (KState*)carve<char>(c, KS_COUNT * sizeof(KState));
+    c->ca = (CallArgs*)carve<char>(c, sizeof(CallArgs));
+    c->d_mass = carve<double>(c, 1);
+    c->ctr = (unsigned long long*)carve<double>(c, 1);
+    if (c->arena_used > c->arena_bytes) { c->err = "arena overflow"; return DRD_ERR_NOMEM; }
+    CK(cudaMallocHost(&c->h_ks, KS_COUNT * sizeof(KState)));
+    CK(cudaMallocHost(&c->h_ca, sizeof(CallArgs)));
+    CK(cudaMallocHost(&c->h_mass, sizeof(double)));
+    memset(c->h_ks, 0, KS_COUNT * sizeof(KState));
+    memset(c->h_ca, 0, sizeof(CallArgs));
+    // default coefficients: no solid, unit density / viscosity / mobility
+    std::vector<double> ones(c->cs, 1.0), zeros(c->cs, 0.0);
+    CK(cudaMemcpy(c->rho, ones.data(), sizeof(double) * c->cs, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->eta, ones.data(), sizeof(double) * c->cs, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->M0, ones.data(), sizeof(double) * c->cs, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->Mi, ones.data(), sizeof(double) * c->cs, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->used, ones.data(), sizeof(double) * c->cs, cudaMemcpyHostToDevice));
+    // transform matrices: x-pass operands transposed (B[j][o] = D[o][j]), z-pass as is
+    std::vector<double> d1, d2, d3, e1, e2, e3;
+    host_dct_mats(nr, d1, d2, d3);
+    host_dct_mats(nz, e1, e2, e3);
+    auto put = [&](double* dst, const std::vector<double>& v) {
+        return cudaMemcpy(dst, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice);
+    };
+    CK(put(c->m1xT, transpose(d1, nr)));
+    CK(put(c->m2xT, transpose(d2, nr)));
+    CK(put(c->m3xT, transpose(d3, nr)));
+    CK(put(c->m1z, e1));
+    CK(put(c->m2z, e2));
+    CK(put(c->m3z, e3));
+    launch_convert_scale<float, double>((long)nr * nr, c->m1xT, 1.0, c->m1xT32, nullptr, c->s);
+    launch_convert_scale<float, double>((long)nz * nz, c->m1z, 1.0, c->m1z32, nullptr, c->s);
+    std::vector<double> cfa(nr + 1, std::cos(c->P.angle * kPi / 180.0) / std::sqrt(2.0));
+    CK(put(c->cfB, cfa));
+    CK(put(c->cfT, cfa));
+    int rc = upload_tables(c);
+    if (rc) return rc;
+    rc = refresh_fp32(c);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->s));
+    const char* g = std::getenv("DRD_NO_GRAPH");
+    c->use_graph = !(g && g[0] == '1');
+    return DRD_OK;
+}
+
+int validate(const drd_params* p, std::string& why) {
+    if (!p) { why = "params is NULL"; return DRD_ERR_BADARG; }
+    if (p->nr < 3 || p->nz < 3) { why = "nr and nz must be >= 3"; return DRD_ERR_BADARG; }
+    if ((long)p->nr * p->nz > (1L << 26)) { why = "grid too large"; return DRD_ERR_BADARG; }
+    if (!(p->dr > 0) || !(p->dz > 0) || !(p->dt > 0)) { why = "dr, dz, dt must be positive"; return DRD_ERR_BADARG; }
+    if (!(p->I_thickness > 0)) { why = "I_thickness must be positive"; return DRD_ERR_BADARG; }
+    if (p->variant != DRD_VARIANT_MF && p->variant != DRD_VARIANT_TP) { why = "unknown variant"; return DRD_ERR_BADARG; }
+    if (p->precision != DRD_PREC_FP64 && p->precision != DRD_PREC_MIXED) { why = "unknown precision"; return DRD_ERR_BADARG; }
+    if (p->variant == DRD_VARIANT_TP && p->phi_mode != 1 && p->phi_mode != 2) { why = "phi_mode must be 1 or 2"; return DRD_ERR_BADARG; }
+    if (p->ch_maxit <= 0 || p->uv_maxit <= 0 || p->phmu_maxit <= 0) { why = "maxit must be positive"; return DRD_ERR_BADARG; }
+    if (p->xlsB >= 1.e-8) { why = "slip walls (xlsB >= 1e-8) have no solve in the reference"; return DRD_ERR_UNSUPPORTED; }
+    if (p->precision == DRD_PREC_MIXED && (!(p->mixed_inner_tol > 0) || p->mixed_max_refine <= 0)) {
+        why = "mixed precision needs mixed_inner_tol > 0 and mixed_max_refine > 0";
+        return DRD_ERR_BADARG;
+    }
+    return DRD_OK;
+}
+
+int finish_call(drd_ctx* c, int slot, drd_status* st, bool has_solve) {
+    if (has_solve) CK(cudaMemcpyAsync(c->h_ks + slot, c->ks + slot, sizeof(KState), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaEventRecord(c->ev1, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    CK(cudaGetLastError());
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    if (has_solve) {
+        fill_status(c->h_ks[slot], st, mixed_of(c), ms * 1e-3);
+        return c->h_ks[slot].info;
+    }
+    if (st) { memset(st, 0, sizeof(*st)); st->seconds = ms * 1e-3; }
+    return DRD_OK;
+}
+
+}  // namespace
+
+// ============================================================================================
+// extern "C"
+// ============================================================================================
+extern "C" {
+
+int drd_abi_version(void) { return DRD_ABI_VERSION; }
+
+int drd_create(const drd_params* params, drd_ctx** out) {
+    if (!out) return DRD_ERR_BADARG;
+    *out = nullptr;
+    std::string why;
+    int rc = validate(params, why);
+    if (rc) { std::fprintf(stderr, "drd_create: %s\n", why.c_str()); return rc; }
+    drd_ctx* c = new drd_ctx();
+    c->P = *params;
+    c->dp = make_dev_params(c->P);
+    c->nr = params->nr;
+    c->nz = params->nz;
+    c->cs = (long)(c->nr + 2) * (c->nz + 2);
+    c->us = (long)(c->nr + 3) * (c->nz + 2);
+    c->vs = (long)(c->nr + 2) * (c->nz + 1);
+    c->nc = (long)c->nr * c->nz;
+    c->nuv = (long)(c->nr + 1) * c->nz + (long)c->nr * (c->nz - 1);
+    c->nphmu = 2 * c->nc;
+    c->nmax = std::max(c->nuv, c->nphmu);
+    long g = (c->nmax + 2L * DRD_TPB - 1) / (2L * DRD_TPB);
+    c->G = (int)std::max(1L, std::min<long>(DRD_MAXB, g));
+    rc = setup_context(c);
+    if (rc) {
+        std::fprintf(stderr, "drd_create: %s\n", c->err.c_str());
+        drd_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return DRD_OK;
+}
+
+int drd_destroy(drd_ctx* c) {
+    if (!c) return DRD_ERR_BADARG;
+    if (c->s) cudaStreamSynchronize(c->s);
+    clear_graphs(c);
+    if (c->arena) cudaFree(c->arena);
+    if (c->h_ks) cudaFreeHost(c->h_ks);
+    if (c->h_ca) cudaFreeHost(c->h_ca);
+    if (c->h_mass) cudaFreeHost(c->h_mass);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->s) cudaStreamDestroy(c->s);
+    if (c->s2) cudaStreamDestroy(c->s2);
+    if (c->s3) cudaStreamDestroy(c->s3);
+    delete c;
+    return DRD_OK;
+}
+
+const char* drd_last_error(drd_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int drd_set_params(drd_ctx* c, const drd_params* p) {
+    if (!c) return DRD_ERR_BADARG;
+    std::string why;
+    int rc = validate(p, why);
+    if (rc) { c->err = why; return rc; }
+    if (p->nr != c->nr || p->nz != c->nz) { c->err = "grid size cannot change"; return DRD_ERR_BADARG; }
+    CK(cudaStreamSynchronize(c->s));
+    c->P = *p;
+    c->dp = make_dev_params(c->P);
+    clear_graphs(c);
+    rc = upload_tables(c);
+    if (rc) return rc;
+    std::vector<double> cfa(c->nr + 1, std::cos(c->P.angle * kPi / 180.0) / std::sqrt(2.0));
+    CK(cudaMemcpy(c->cfB, cfa.data(), sizeof(double) * cfa.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->cfT, cfa.data(), sizeof(double) * cfa.size(), cudaMemcpyHostToDevice));
+    return DRD_OK;
+}
+
+int drd_set_coefs(drd_ctx* c, const double* rho, const double* eta, const double* bdr_ph, const double* bdr_ph_grad,
+                  const double* ph_M_0, const double* ph_M_inner) {
+    if (!c) return DRD_ERR_BADARG;
+    int rc = 0;
+    rc |= up(c, c->rho, rho, c->cs);
+    rc |= up(c, c->eta, eta, c->cs);
+    rc |= up(c, c->bdr, bdr_ph, c->cs);
+    rc |= up(c, c->grad, bdr_ph_grad, c->cs);
+    rc |= up(c, c->M0, ph_M_0, c->cs);
+    rc |= up(c, c->Mi, ph_M_inner, c->cs);
+    if (rc) return DRD_ERR_CUDA;
+    // MF penalises with bdr_ph itself (VeloSolve_2_combined.f90:580); TP keeps its own mask
+    if (bdr_ph && c->P.variant == DRD_VARIANT_MF)
+        CK(cudaMemcpyAsync(c->pen, c->bdr, sizeof(double) * c->cs, cudaMemcpyDeviceToDevice, c->s));
+    rc = refresh_fp32(c);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->s));
+    return DRD_OK;
+}
+
+int drd_set_tp_fields(drd_ctx* c, const double* bdr_ph_used, const double* bdr_ph_penalty, const double* angleB,
+                      const double* angleT) {
+    if (!c) return DRD_ERR_BADARG;
+    int rc = 0;
+    rc |= up(c, c->used, bdr_ph_used, c->cs);
+    rc |= up(c, c->pen, bdr_ph_penalty, c->cs);
+    if (rc) return DRD_ERR_CUDA;
+    auto cf = [&](double* dst, const double* ang) -> int {
+        if (!ang) return DRD_OK;
+        std::vector<double> v(c->nr + 1);
+        for (int i = 0; i <= c->nr; ++i) v[i] = std::cos(ang[i] * kPi / 180.0) / std::sqrt(2.0);
+        CK(cudaMemcpy(dst, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice));
+        return DRD_OK;
+    };
+    rc = cf(c->cfB, angleB);
+    if (rc) return rc;
+    rc = cf(c->cfT, angleT);
+    if (rc) return rc;
+    rc = refresh_fp32(c);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->s));
+    return DRD_OK;
+}
+
+int drd_interpolate_coef(drd_ctx* c, const double* dist, double* fpd_ph, double* rho, double* eta) {
+    if (!c || !dist) return DRD_ERR_BADARG;
+    CK(cudaEventRecord(c->ev0, c->s));
+    if (up(c, c->dist, dist, c->nc)) return DRD_ERR_CUDA;
+    launch_interp_coef(c->dp, c->dist, c->bdr, c->fpd, c->rho, c->eta, c->ctr, c->s);
+    int rc = refresh_fp32(c);
+    if (rc) return rc;
+    rc = down(c, fpd_ph, c->fpd, c->cs) | down(c, rho, c->rho, c->cs) | down(c, eta, c->eta, c->cs);
+    if (rc) return DRD_ERR_CUDA;
+    return finish_call(c, 0, nullptr, false);
+}
+
+int drd_phsolve(drd_ctx* c, const double* u, const double* v, const double* ph, const double* rmu, double t,
+                double* rmu_after, double* ph_after, drd_status* st) {
+    if (!c || !u || !v || !ph || !rmu || !rmu_after || !ph_after) return DRD_ERR_BADARG;
+    if (c->P.variant != DRD_VARIANT_MF) { c->err = "PhSolve belongs to the MF variant"; return DRD_ERR_BADARG; }
+    CK(cudaEventRecord(c->ev0, c->s));
+    int rc = up(c, c->fld[DRD_F_U], u, c->us) | up(c, c->fld[DRD_F_V], v, c->vs) | up(c, c->fld[DRD_F_PH], ph, c->cs) |
+             up(c, c->fld[DRD_F_RMU], rmu, c->cs);
+    if (rc) return DRD_ERR_CUDA;
+    rc = run_graph(c, gkey(GK_CH, mixed_of(c), 0), [&](cudaStream_t s) { return enq_ch(c, s); }, t, 0.0);
+    if (rc) return rc;
+    rc = down(c, rmu_after, c->rmu_after, c->cs) | down(c, ph_after, c->ph_after, c->cs);
+    if (rc) return DRD_ERR_CUDA;
+    return finish_call(c, KS_CH, st, true);
+}
+
+int drd_ph_mu_solve(drd_ctx* c, const double* u, const double* v, const double* ph, const double* rmu, double t,
+                    double* ph_after, double* rmu_after, double* ph_M_0_out, double* coef_bot_top, drd_status* st) {
+    if (!c || !u || !v || !ph || !rmu || !rmu_after || !ph_after) return DRD_ERR_BADARG;
+    if (c->P.variant != DRD_VARIANT_TP) { c->err = "ph_mu_solve belongs to the TP variant"; return DRD_ERR_BADARG; }
+    CK(cudaEventRecord(c->ev0, c->s));
+    int rc = up(c, c->fld[DRD_F_U], u, c->us) | up(c, c->fld[DRD_F_V], v, c->vs) | up(c, c->fld[DRD_F_PH], ph, c->cs) |
+             up(c, c->fld[DRD_F_RMU], rmu, c->cs);
+    if (rc) return DRD_ERR_CUDA;
+    rc = run_graph(c, gkey(GK_PHMU, mixed_of(c), 0), [&](cudaStream_t s) { return enq_phmu(c, s); }, t, 0.0);
+    if (rc) return rc;
+    rc = down(c, ph_after, c->ph_after, c->cs) | down(c, rmu_after, c->rmu_after, c->cs) |
+         down(c, ph_M_0_out, c->M0, c->cs);
+    if (rc) return DRD_ERR_CUDA;
+    if (coef_bot_top) {
+        OpScal<double> o = make_op<double>(c, 0);
+        coef_bot_top[0] = o.cb;
+        coef_bot_top[1] = o.ct;
+    }
+    return finish_call(c, KS_PHMU, st, true);
+}
+
+static int velo_common(drd_ctx* c, int bdf, const double* psi1, const double* psi2, const double* u_pre,
+                       const double* u, const double* v_pre, const double* v, const double* p, const double* ph_after,
+                       const double* rmu_after, double t, const double* pf1, const double* pf2, double* u_after,
+                       double* v_after, double* uL, double* uR, drd_status* st) {
+    if (!c || !u || !v || !p || !ph_after || !rmu_after || !u_after || !v_after) return DRD_ERR_BADARG;
+    if (bdf == 2 && (!psi1 || !psi2 || !u_pre || !v_pre)) return DRD_ERR_BADARG;
+    CK(cudaEventRecord(c->ev0, c->s));
+    int rc = up(c, c->fld[DRD_F_U], u, c->us) | up(c, c->fld[DRD_F_V], v, c->vs) | up(c, c->fld[DRD_F_P], p, c->cs) |
+             up(c, c->ph_after, ph_after, c->cs) | up(c, c->rmu_after, rmu_after, c->cs);
+    if (bdf == 2)
+        rc |= up(c, c->fld[DRD_F_PSI1], psi1, c->cs) | up(c, c->fld[DRD_F_PSI2], psi2, c->cs) |
+              up(c, c->fld[DRD_F_U_PRE], u_pre, c->us) | up(c, c->fld[DRD_F_V_PRE], v_pre, c->vs);
+    if (pf1) rc |= up(c, c->fld[DRD_F_PF1], pf1, c->cs);
+    else CK(cudaMemsetAsync(c->fld[DRD_F_PF1], 0, sizeof(double) * c->cs, c->s));
+    if (pf2) rc |= up(c, c->fld[DRD_F_PF2], pf2, c->cs);
+    else CK(cudaMemsetAsync(c->fld[DRD_F_PF2], 0, sizeof(double) * c->cs, c->s));
+    if (rc) return DRD_ERR_CUDA;
+    rc = run_graph(c, gkey(GK_UV, mixed_of(c), bdf), [&](cudaStream_t s) { return enq_uv(c, bdf, s); }, t, 0.0);
+    if (rc) return rc;
+    rc = down(c, u_after, c->u_after, c->us) | down(c, v_after, c->v_after, c->vs);
+    const bool dirichlet = !(c->P.variant == DRD_VARIANT_TP && c->P.lr_bd_type == 'n');
+    if (dirichlet) rc |= down(c, uL, c->uL, c->nz) | down(c, uR, c->uL, c->nz);
+    if (rc) return DRD_ERR_CUDA;
+    return finish_call(c, KS_UV, st, true);
+}
+
+int drd_velosolve_combined(drd_ctx* c, const double* psi, const double* u, const double* v, const double* p,
+                           const double* rmu_after, const double* ph_after, double t, const double* pf1,
+                           const double* pf2, double* u_after, double* v_after, double* uL, double* uR, drd_status* st) {
+    (void)psi;  // VeloSolve_combined ignores psi (temp_p = p, VeloSolve_combined.f90:182)
+    return velo_common(c, 1, nullptr, nullptr, nullptr, u, nullptr, v, p, ph_after, rmu_after, t, pf1, pf2, u_after,
+                       v_after, uL, uR, st);
+}
+
+int drd_velosolve_2_combined(drd_ctx* c, const double* psi1, const double* psi2, const double* u_pre,
+                             const double* u, const double* v_pre, const double* v, const double* p,
+                             const double* ph_pre, const double* ph_after, const double* rmu_pre,
+                             const double* rmu_after, double t, const double* pf1, const double* pf2, double* u_after,
+                             double* v_after, double* uL, double* uR, drd_status* st) {
+    (void)ph_pre;
+    (void)rmu_pre;
+    return velo_common(c, 2, psi1, psi2, u_pre, u, v_pre, v, p, ph_after, rmu_after, t, pf1, pf2, u_after, v_after,
+                       uL, uR, st);
+}
+
+int drd_presolve_2(drd_ctx* c, const double* u, const double* v, double coef, double* psi, drd_status* st) {
+    if (!c || !u || !v || !psi) return DRD_ERR_BADARG;
+    CK(cudaEventRecord(c->ev0, c->s));
+    int rc = up(c, c->fld[DRD_F_U], u, c->us) | up(c, c->fld[DRD_F_V], v, c->vs);
+    if (rc) return DRD_ERR_CUDA;
+    rc = run_graph(c, gkey(GK_PRE, 0, 0), [&](cudaStream_t s) { enq_pre(c, c->fld[DRD_F_PSI2], s); return DRD_OK; },
+                   0.0, coef);
+    if (rc) return rc;
+    if (down(c, psi, c->fld[DRD_F_PSI2], c->cs)) return DRD_ERR_CUDA;
+    return finish_call(c, 0, st, false);
+}
+
+int drd_mass(drd_ctx* c, const double* ph, double* mass) {
+    if (!c || !ph || !mass) return DRD_ERR_BADARG;
+    CK(cudaEventRecord(c->ev0, c->s));
+    if (up(c, c->ph_after, ph, c->cs)) return DRD_ERR_CUDA;
+    enq_mass(c, c->ph_after, c->s);
+    CK(cudaMemcpyAsync(c->h_mass, c->d_mass, sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    int rc = finish_call(c, 0, nullptr, false);
+    *mass = *c->h_mass;
+    return rc;
+}
+
+int drd_state_upload(drd_ctx* c, int field, const double* host) {
+    if (!c || field < 0 || field >= DRD_F_COUNT || !host) return DRD_ERR_BADARG;
+    const long n = (field == DRD_F_U || field == DRD_F_U_PRE) ? c->us : (field == DRD_F_V || field == DRD_F_V_PRE) ? c->vs : c->cs;
+    CK(cudaMemcpyAsync(c->fld[field], host, sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    return DRD_OK;
+}
+
+int drd_state_download(drd_ctx* c, int field, double* host) {
+    if (!c || field < 0 || field >= DRD_F_COUNT || !host) return DRD_ERR_BADARG;
+    const long n = (field == DRD_F_U || field == DRD_F_U_PRE) ? c->us : (field == DRD_F_V || field == DRD_F_V_PRE) ? c->vs : c->cs;
+    CK(cudaMemcpyAsync(host, c->fld[field], sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    return DRD_OK;
+}
+
+int drd_state_device_ptr(drd_ctx* c, int field, double** dptr) {
+    if (!c || field < 0 || field >= DRD_F_COUNT || !dptr) return DRD_ERR_BADARG;
+    *dptr = c->fld[field];
+    return DRD_OK;
+}
+
+int drd_steps_async(drd_ctx* c, int first, double t, int nsteps) {
+    if (!c || nsteps < 0) return DRD_ERR_BADARG;
+    for (int k = 0; k < nsteps; ++k) {
+        const int fst = (first && k == 0);
+        const double gamma1 = std::min(1.0, c->P.lambda_rho);
+        const double coef = fst ? c->P.re * gamma1 / c->P.dt : 3 * c->P.re * gamma1 / 2. / c->P.dt;
+        const double tt = t + k * c->P.dt + c->P.dt;
+        int rc = run_graph(c, gkey(GK_STEP, mixed_of(c), fst), [&](cudaStream_t s) { return enq_step(c, fst, s); }, tt,
+                           coef);
+        if (rc) return rc;
+    }
+    return DRD_OK;
+}
+
+int drd_step(drd_ctx* c, int first, double t, drd_step_stats* stats) {
+    if (!c) return DRD_ERR_BADARG;
+    CK(cudaEventRecord(c->ev0, c->s));
+    int rc = drd_steps_async(c, first, t, 1);
+    if (rc) return rc;
+    if (!stats) return DRD_OK;
+    CK(cudaMemcpyAsync(c->h_ks, c->ks, KS_COUNT * sizeof(KState), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaMemcpyAsync(c->h_mass, c->d_mass, sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaEventRecord(c->ev1, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    CK(cudaGetLastError());
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    const int mixed = mixed_of(c);
+    fill_status(c->h_ks[c->P.variant == DRD_VARIANT_TP ? KS_PHMU : KS_CH], &stats->ch, mixed, ms * 1e-3);
+    fill_status(c->h_ks[KS_UV], &stats->uv, mixed, ms * 1e-3);
+    memset(&stats->pre, 0, sizeof(stats->pre));
+    stats->mass = *c->h_mass;
+    stats->t = t + c->P.dt;
+    return DRD_OK;
+}
+
+int drd_synchronize(drd_ctx* c) {
+    if (!c) return DRD_ERR_BADARG;
+    CK(cudaStreamSynchronize(c->s));
+    CK(cudaGetLastError());
+    return DRD_OK;
+}
+
+long drd_op_length(drd_ctx* c, int op) {
+    if (!c) return -1;
+    if (op == DRD_OP_CH_MATVEC || op == DRD_OP_CH_PSOLVE) return c->nc;
+    if (op == DRD_OP_UV_MATVEC || op == DRD_OP_UV_PSOLVE) return c->nuv;
+    if (op == DRD_OP_PHMU_MATVEC || op == DRD_OP_PHMU_PSOLVE) return c->nphmu;
+    return -1;
+}
+
+int drd_op_apply(drd_ctx* c, int op, int bdf, int precision, const double* x, double* y) {
+    if (!c || !x || !y) return DRD_ERR_BADARG;
+    const long n = drd_op_length(c, op);
+    if (n < 0 || (bdf != 1 && bdf != 2)) return DRD_ERR_BADARG;
+    int rc = ensure_tuned(c);
+    if (rc) return rc;
+    const int kind = (op <= DRD_OP_CH_PSOLVE) ? SYS_CH : (op <= DRD_OP_UV_PSOLVE) ? SYS_UV : SYS_PHMU;
+    const bool mv = (op % 2) == 0;
+    Sys S = sys_of(c, kind, bdf);
+    KVecs<double>& k = c->k64;
+    CK(cudaMemcpyAsync(k.tmp, x, sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
+    if (precision == DRD_PREC_FP64) {
+        enq_sys_setup<double>(c, S, c->s);
+        if (mv) enq_matvec<double>(c, S, 1.0, k.tmp, 0.0, k.v, nullptr, 0, 0, nullptr, G_ALWAYS, c->s);
+        else enq_psolve<double>(c, S, k.tmp, k.v, nullptr, G_ALWAYS, c->s);
+    } else {
+        KVecs<float>& f = c->k32;
+        enq_sys_setup<float>(c, S, c->s);
+        launch_convert_scale<float, double>(n, k.tmp, 1.0, f.tmp, c->ctr, c->s);
+        if (mv) enq_matvec<float>(c, S, 1.0f, f.tmp, 0.0f, f.v, nullptr, 0, 0, nullptr, G_ALWAYS, c->s);
+        else enq_psolve<float>(c, S, f.tmp, f.v, nullptr, G_ALWAYS, c->s);
+        launch_convert_scale<double, float>(n, f.v, 1.0, k.v, c->ctr, c->s);
+    }
+    CK(cudaMemcpyAsync(y, k.v, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    CK(cudaGetLastError());
+    return DRD_OK;
+}
+
+int64_t drd_kernel_launches(drd_ctx* c) {
+    if (!c) return -1;
+    unsigned long long v = 0;
+    cudaStreamSynchronize(c->s);
+    cudaMemcpy(&v, c->ctr, sizeof(v), cudaMemcpyDeviceToHost);
+    return (int64_t)v;
+}
+
+void* drd_stream(drd_ctx* c) { return c ? (void*)c->s : nullptr; }
+
+}  // extern "C"

@@ -1,0 +1,200 @@
+"""Seeded synthetic workloads with the reference's shapes and field construction.
+
+No reference output data exists, so every workload is built here from a seed, the way
+microfluidics_complex_domain/finit.f90 builds its fields:
+
+* bdr_ph: the solid indicator in [0, 1] (1 in solid), Neumann ghosts;
+* bdr_ph_grad = |grad bdr_ph| by central differences on the interior, 0 on ghosts
+  (finit.f90:346-352); ph_M_0 = ph_M_inner = 1 - bdr_ph (finit.f90:358-359);
+* phi in [0, 1] from tanh profiles, clipped by 1 - bdr_ph (finit.f90:274-288);
+* rmu = -eps lap(phi) - phi/eps + phi^3/eps with Neumann ghosts (finit.f90:315-329);
+* fpd_ph / rho / eta from interpolate_coef (interpolate_coef.f90:55-89) with the particle
+  distance field of rigid rectangular fibers.
+
+Workloads:
+  "c1"  128x64 channel, one drop, no solid (lambda ratios 1), tol 1e-10, dt 1e-3.
+  "c2"  420x180 serpentine channel (seeded sinusoidal walls, amplitude 30, period 140 cells,
+        half-width 45 cells), resistance penalty 1e4, walls smoothed by tanh(d / 2 cells),
+        3 rigid fibers of 40x4 cells at seeded poses, two drops of radius 15 cells,
+        viscosity ratio 5, Re 0.5, Ca 0.05.
+  "tp"  the two_phase_flow_complex_domain variant (phi in [-1,1], ph_mu_solve, sharp penalty).
+Any workload can be built at another grid size; geometry lengths scale with the grid.
+"""
+import math
+
+import numpy as np
+
+from . import abi
+from .layout import cell_shape, neumann_ghosts_cell, u_shape, v_shape
+
+
+def _grad_mag(b, dr, dz):
+    g = np.zeros_like(b)
+    g[1:-1, 1:-1] = np.sqrt(((b[1:-1, 2:] - b[1:-1, :-2]) / 2.0 / dr) ** 2.0 +
+                            ((b[2:, 1:-1] - b[:-2, 1:-1]) / 2.0 / dz) ** 2.0)
+    return g
+
+
+def _rmu_init(ph, eps, dr, dz):
+    r = np.zeros_like(ph)
+    p = ph
+    r[1:-1, 1:-1] = (-eps * ((p[1:-1, 2:] + p[1:-1, :-2] - 2 * p[1:-1, 1:-1]) / dr ** 2 +
+                             (p[2:, 1:-1] + p[:-2, 1:-1] - 2 * p[1:-1, 1:-1]) / dz ** 2)
+                     - p[1:-1, 1:-1] / eps + p[1:-1, 1:-1] ** 3 / eps)
+    return neumann_ghosts_cell(r)
+
+
+def _rect_sdf(x, y, cx, cy, half_l, half_w, ang):
+    """Signed distance to a rotated rectangle (negative inside)."""
+    c, s = math.cos(ang), math.sin(ang)
+    lx = (x - cx) * c + (y - cy) * s
+    ly = -(x - cx) * s + (y - cy) * c
+    qx = np.abs(lx) - half_l
+    qy = np.abs(ly) - half_w
+    outside = np.sqrt(np.maximum(qx, 0.0) ** 2 + np.maximum(qy, 0.0) ** 2)
+    inside = np.minimum(np.maximum(qx, qy), 0.0)
+    return outside + inside
+
+
+def interpolate_coef_host(params, dist, bdr_ph):
+    """numpy form of interpolate_coef (interpolate_coef.f90:55-89) used to prepare inputs."""
+    eps = params.I_thickness
+    fpd = np.zeros_like(bdr_ph)
+    fpd[1:-1, 1:-1] = np.tanh(-1.0 * dist / math.sqrt(2.0) / eps)
+    fpd = (fpd + 1.0) / 2.0 + bdr_ph
+    neumann_ghosts_cell(fpd)
+    rho = 1.0 + (params.lambda_rho - 1.0) * fpd
+    eta = 1.0 + (params.lambda_eta - 1.0) * fpd
+    return fpd, rho, eta
+
+
+class Case:
+    """A workload: parameters, resident-state fields and coefficient fields."""
+
+    def __init__(self, name, params, state, coefs, dist, meta):
+        self.name, self.params, self.state, self.coefs, self.dist, self.meta = name, params, state, coefs, dist, meta
+
+    @property
+    def nr(self):
+        return self.params.nr
+
+    @property
+    def nz(self):
+        return self.params.nz
+
+    def copy_state(self):
+        return {k: v.copy() for k, v in self.state.items()}
+
+
+def _empty_state(nr, nz):
+    st = {}
+    for fid, kind in abi.FIELD_KIND.items():
+        shape = {"u": u_shape, "v": v_shape, "cell": cell_shape}[kind](nr, nz)
+        st[fid] = np.zeros(shape)
+    return st
+
+
+def make_case(name="c2", seed=0, nr=None, nz=None, precision=abi.DRD_PREC_FP64, **overrides):
+    rng = np.random.default_rng(seed)
+    name = name.lower()
+    if name == "c1":
+        nr = nr or 128
+        nz = nz or 64
+        slen, shig = 2.0, 1.0
+        p = abi.default_params(nr, nz, xld=0.01, re=1.0, ca=0.1, I_thickness=0.02, s_implicit=1.5, tol=1e-10,
+                               lambda_rho=1.0, lambda_eta=1.0, penalty_k=1.0e5, ggx=1.0, UU=1.0)
+        p.dr, p.dz = slen / nr, shig / nz
+        p.dt = 1.0e-3
+        p.bdr_low, p.bdr_upp = 0.0, shig
+    elif name in ("c2", "tp"):
+        nr = nr or (420 if name == "c2" else 128)
+        nz = nz or (180 if name == "c2" else 128)
+        slen, shig = 3.5, 1.5
+        p = abi.default_params(nr, nz, re=0.5, ca=0.05, lambda_rho=1.0, lambda_eta=5.0, penalty_k=1.0e4)
+        p.dr, p.dz = slen / nr, shig / nz
+        p.dt = min(p.dr, p.dz) * 0.1
+    else:
+        raise ValueError(f"unknown workload {name!r}")
+    p.precision = precision
+    for k, v in overrides.items():
+        setattr(p, k, ord(v) if k == "lr_bd_type" and isinstance(v, str) else v)
+    dr, dz, eps = p.dr, p.dz, p.I_thickness
+    # cell-centre coordinates r(i,k) = (i+0.5) dr, z(i,k) = (k+0.5) dz (finit.f90:34-35)
+    xi = (np.arange(nr) + 0.5)
+    zk = (np.arange(nz) + 0.5)
+    X, Z = np.meshgrid(xi * dr, zk * dz)  # [k, i]
+    bdr = np.zeros(cell_shape(nr, nz))
+    dist = np.full((nz, nr), 10.0)  # no particles: far away
+    meta = {"seed": seed, "nr": nr, "nz": nz}
+    sx, sz = nr / 420.0, nz / 180.0
+    if name in ("c2", "tp"):
+        phase = rng.uniform(0, 2 * math.pi)
+        amp, period, half = 30.0 * sz, 140.0 * sx, 45.0 * sz
+        yc = nz / 2.0 + amp * np.sin(2 * math.pi * xi / period + phase)  # cells, per column
+        slope = amp * 2 * math.pi / period * np.cos(2 * math.pi * xi / period + phase)
+        d_cells = (half - np.abs(zk[:, None] - yc[None, :])) / np.sqrt(1.0 + slope[None, :] ** 2)
+        smooth = max(2.0 * min(sx, sz), 0.75)
+        bdr[1:-1, 1:-1] = 0.5 * (1.0 - np.tanh(d_cells / smooth))
+        neumann_ghosts_cell(bdr)
+        p.bdr_low = (yc[0] - half) * dz
+        p.bdr_upp = (yc[0] + half) * dz
+        meta.update(phase=phase, amp=amp, period=period, half=half)
+        # rigid fibers 40 x 4 cells at seeded poses inside the channel
+        fibers = []
+        sdf = np.full((nz, nr), np.inf)
+        for f in range(3):
+            cxc = (f + 0.5) * nr / 3.0 + rng.uniform(-0.1, 0.1) * nr / 3.0
+            ic = int(min(max(round(cxc - 0.5), 0), nr - 1))
+            czc = yc[ic] + rng.uniform(-0.25, 0.25) * half
+            ang = rng.uniform(0, math.pi)
+            fibers.append((cxc, czc, ang))
+            sdf = np.minimum(sdf, _rect_sdf(X / dr, Z / dz, cxc, czc, 20.0 * sx, 2.0 * sz, ang))
+        dist = sdf * min(dr, dz)
+        meta["fibers"] = fibers
+    fpd, rho, eta = interpolate_coef_host(p, dist, bdr)
+    # phase field: drops (phi = 1 inside), clipped by the solid (finit.f90:288)
+    ph = np.zeros(cell_shape(nr, nz))
+    if name == "c1":
+        R = 12.0 * sz
+        cx = nr / 2.0 + rng.uniform(-2, 2)
+        cz = nz / 2.0 + rng.uniform(-2, 2)
+        d = np.sqrt((X / dr - cx) ** 2 + (Z / dz - cz) ** 2) * dr
+        ph[1:-1, 1:-1] = 0.5 * (1.0 + np.tanh((R * dr - d) / (math.sqrt(2.0) * eps)))
+        meta["drops"] = [(cx, cz, R)]
+    else:
+        R = 15.0 * sz
+        drops = []
+        ymid = meta["phase"]
+        for j in range(2):
+            cxd = (j + 0.5) * nr / 2.0 + rng.uniform(-0.05, 0.05) * nr
+            ic = int(min(max(round(cxd), 0), nr - 1))
+            czd = yc[ic] + rng.uniform(-0.2, 0.2) * half
+            drops.append((cxd, czd, R))
+            d = np.sqrt((X / dr - cxd) ** 2 + (Z / dz - czd) ** 2) * min(dr, dz)
+            ph[1:-1, 1:-1] = np.maximum(ph[1:-1, 1:-1],
+                                        0.5 * (1.0 + np.tanh((R * min(dr, dz) - d) / (math.sqrt(2.0) * eps))))
+        del ymid
+        meta["drops"] = drops
+    ph = np.minimum(1.0 - bdr, ph)
+    neumann_ghosts_cell(ph)
+    if name == "tp":
+        # two_phase_flow_complex_domain: phi in [-1, 1], bdr_ph_used = 1 - bdr_ph, sharp penalty mask
+        p.variant = abi.DRD_VARIANT_TP
+        p.phi_mode = 2
+        p.lr_bd_type = ord("d")
+        p.uv_maxit = 2000
+        p.penalty_k = 1.0e8
+        ph = 2.0 * ph - 1.0
+        neumann_ghosts_cell(ph)
+    state = _empty_state(nr, nz)
+    state[abi.F_PH] = ph
+    state[abi.F_RMU] = _rmu_init(ph, eps, dr, dz)
+    M = 1.0 - bdr
+    coefs = {
+        "rho": rho, "eta": eta, "fpd": fpd, "bdr_ph": bdr, "bdr_ph_grad": _grad_mag(bdr, dr, dz),
+        "M0": M.copy(), "Mi": M.copy(), "bdr_pen": bdr.copy(), "bdr_used": 1.0 - bdr,
+    }
+    if name == "tp":
+        coefs["bdr_pen"] = (bdr > 0.5).astype(np.float64)
+        coefs["M0"] = (1.0 - bdr) * (ph ** 2 - 1.0) ** 2
+    return Case(name, p, state, coefs, dist, meta)

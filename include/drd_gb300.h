@@ -1,0 +1,256 @@
+/*
+ * drd_gb300.h — C-ABI of the GB300 (sm_103a) per-time-step solver core of DRD-Micro.
+ *
+ * The reference is a serial Fortran program whose per-step solver subroutines
+ * take explicit-shape REAL(8) arrays by reference and read everything else from
+ * `module global` (microfluidics_complex_domain/global.f90:1-129).  This header
+ * is what a Fortran `iso_c_binding` interface (or ctypes) binds instead: every
+ * hidden module input becomes an explicit argument or a field of drd_params,
+ * every array keeps its Fortran ghosted shape and column-major order, so the
+ * Fortran side passes its arrays unchanged.
+ *
+ * Array shapes (Fortran bounds, i fastest, no padding):
+ *   CELL  (-1:nr, -1:nz)     element (i,k) at [(i+1) + (k+1)*(nr+2)], (nr+2)*(nz+2) doubles
+ *   UFACE (-1:nr+1, -1:nz)   element (i,k) at [(i+1) + (k+1)*(nr+3)], (nr+3)*(nz+2) doubles
+ *   VFACE (-1:nr, 0:nz)      element (i,k) at [(i+1) +  k   *(nr+2)], (nr+2)*(nz+1) doubles
+ *   DIST  (0:nr-1, 0:nz-1)   element (i,k) at [i + k*nr],             nr*nz doubles
+ *   ZLINE (0:nz)             uL / uR inlet profiles, nz+1 doubles (entries 0..nz-1 written)
+ *   XLINE (0:nr)             angleB / angleT contact angles (TP), nr+1 doubles
+ *
+ * Host pointers are caller-owned and only read/written during the call.
+ * Device buffers are owned by the context.  One context per host thread; a
+ * context owns one CUDA stream and its CUDA graphs.
+ *
+ * Return codes: DRD_OK, a BiCGSTAB INFO value (>0 not converged, -10/-11
+ * breakdown, exactly as lib/BiCGSTABREVCOM.f:64-90 defines them), or a
+ * negative DRD_ERR_* code for argument, CUDA or timeout errors.  The reference
+ * prints INFO and continues (microfluidics_complex_domain/PhSolve.f90:75-79);
+ * callers of this library may do the same: outputs are always written.
+ */
+#ifndef DRD_GB300_H
+#define DRD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DRD_ABI_VERSION 1
+
+/* Which application's copy of the solver routines to follow. */
+#define DRD_VARIANT_MF 0 /* microfluidics_complex_domain/ (README example, headline)   */
+#define DRD_VARIANT_TP 1 /* two_phase_flow_complex_domain/ (ph_mu_solve, sharp penalty) */
+
+/* Arithmetic of the Krylov solves. */
+#define DRD_PREC_FP64 0  /* every operator in FP64: the reference's arithmetic           */
+#define DRD_PREC_MIXED 1 /* FP32 operators and preconditioners inside FP64 iterative
+                            refinement; FP64 inner products and true-residual recompute  */
+
+/* Return codes besides BiCGSTAB INFO values. */
+#define DRD_OK 0
+#define DRD_ERR_BADARG (-100)
+#define DRD_ERR_CUDA (-101)
+#define DRD_ERR_TIMEOUT (-102)
+#define DRD_ERR_UNSUPPORTED (-103)
+#define DRD_ERR_NONFINITE (-104)
+#define DRD_ERR_NOMEM (-105)
+
+/* Status flags. */
+#define DRD_FLAG_EARLY_S 1u      /* stopped at the absolute ||s|| <= tol test (BiCGSTABREVCOM.f:313) */
+#define DRD_FLAG_EARLY_X0 2u     /* stopped at the absolute ||b - A x0|| <= tol test (:248)          */
+#define DRD_FLAG_REFINED 4u      /* mixed mode: result produced by FP64 iterative refinement         */
+#define DRD_FLAG_FALLBACK64 8u   /* mixed mode: refinement stalled; finished with the FP64 solver   */
+
+/*
+ * Scalars that the reference keeps in `module global` and the input deck
+ * (microfluidics_complex_domain/mcl6.f90:68-101, global.f90:30-91).
+ */
+typedef struct drd_params {
+    int32_t nr, nz;        /* cells in x (r) and y (z); global.f90:18-19                          */
+    int32_t variant;       /* DRD_VARIANT_*                                                        */
+    int32_t precision;     /* DRD_PREC_*                                                           */
+    int32_t phi_mode;      /* TP: 1 = phi in [0,1], 2 = phi in [-1,1] (TP/mcl6.f90:156)            */
+    int32_t lr_bd_type;    /* TP: 'd' Dirichlet inlet or 'n' Neumann sides (TP/VeloSolve_2:272)   */
+    int32_t ch_maxit;      /* PhSolve ITER, 500 (PhSolve.f90:72)                                   */
+    int32_t uv_maxit;      /* VeloSolve ITER, 800 MF (VeloSolve_2_combined.f90:398), 2000 TP       */
+    int32_t phmu_maxit;    /* ph_mu_solve ITER, 5000 (TP/ph_mu_solve.f90:156)                      */
+    int32_t reserved0;
+    double dr, dz, dt;     /* grid spacing and time step (finit.f90:25-28,397)                    */
+    double xld, re, ca;    /* 1/Pe, Reynolds, capillary number (input deck lines 1-3)             */
+    double I_thickness;    /* interface thickness epsilon (deck line 18)                           */
+    double s_implicit;     /* stabilisation s (deck line 19)                                       */
+    double tol;            /* BiCGSTAB tolerance (deck line 20)                                    */
+    double ggx, ggz;       /* body force (deck lines 21-22)                                        */
+    double uwT, uwB;       /* wall speeds (deck lines 9-10)                                        */
+    double UU, twall;      /* inlet amplitude (deck line 26), ramp time 0.1 (mcl6.f90:151)         */
+    double bdr_upp, bdr_low; /* inlet extent (finit.f90:106-107)                                   */
+    double angle;          /* contact angle in degrees (deck line 13)                              */
+    double xlsB;           /* bottom slip length; only the no-slip branch (< 1e-8) is on the path  */
+    double penalty_k;      /* DRD resistance coefficient (global.f90:91, 1e5)                      */
+    double lambda_rho, lambda_eta; /* density / viscosity ratios (deck lines 24-25)                */
+    double bdr_ph_used_adjust;     /* TP: 1e-6 (TP/finit.f90:572)                                  */
+    double mixed_inner_tol;        /* mixed mode: relative residual reduction per FP32 inner solve */
+    int32_t mixed_max_refine;      /* mixed mode: maximum FP64 refinement sweeps                   */
+    int32_t reserved1;
+} drd_params;
+
+typedef struct drd_status {
+    int32_t info;        /* BiCGSTAB INFO on exit (lib/BiCGSTAB.f:99-124)                         */
+    int32_t iter;        /* ITER on exit: iterations performed (FP32 iterations summed in mixed)  */
+    double resid;        /* RESID on exit                                                          */
+    double true_resid;   /* ||b - A x||_2 / ||b||_2 recomputed in FP64 from the returned x         */
+    int32_t refinements; /* mixed mode: FP64 refinement sweeps                                     */
+    uint32_t flags;      /* DRD_FLAG_*                                                             */
+    double seconds;      /* device time of the call (CUDA events)                                  */
+} drd_status;
+
+typedef struct drd_ctx drd_ctx;
+
+/* ---- life cycle ------------------------------------------------------------------------ */
+
+/* Replaces setup() (microfluidics_complex_domain/setup.f90:106-155: Ph_Lcc, Pre_Lcc tables)
+ * and PreSolve_init() (microfluidics_complex_domain/PreSolve_init.f90:1-16: the FFTW
+ * REDFT10/REDFT01 plans).  Allocates all device memory for an nr x nz grid. */
+int drd_create(const drd_params* params, drd_ctx** ctx_out);
+int drd_destroy(drd_ctx* ctx);
+/* Re-derives the dt-dependent tables after dt changes (setup() is re-run in mcl6.f90:201). */
+int drd_set_params(drd_ctx* ctx, const drd_params* params);
+const char* drd_last_error(drd_ctx* ctx);
+int drd_abi_version(void);
+
+/* ---- hidden module inputs --------------------------------------------------------------- */
+
+/* rho, eta, bdr_ph, bdr_ph_grad, ph_M_0, ph_M_inner: CELL arrays of module global
+ * (microfluidics_complex_domain/global.f90:47,81-85).  Any pointer may be NULL to keep the
+ * value on the device. */
+int drd_set_coefs(drd_ctx* ctx, const double* rho, const double* eta, const double* bdr_ph,
+                  const double* bdr_ph_grad, const double* ph_M_0, const double* ph_M_inner);
+/* TP-only module inputs: bdr_ph_used, bdr_ph_penalty (CELL), angleB, angleT (XLINE)
+ * (two_phase_flow_complex_domain/global.f90:44,95-98). */
+int drd_set_tp_fields(drd_ctx* ctx, const double* bdr_ph_used, const double* bdr_ph_penalty,
+                      const double* angleB, const double* angleT);
+
+/* ---- the per-step solver core (drop-in for the reference subroutines) ------------------ */
+
+/* interpolate_coef (microfluidics_complex_domain/interpolate_coef.f90:4-92).  `dist` is the
+ * particle distance dist(r(i,k), z(i,k)) of every interior cell (DIST shape); fpd_ph, rho,
+ * eta (CELL) are written and rho/eta also replace the context's coefficients. */
+int drd_interpolate_coef(drd_ctx* ctx, const double* dist, double* fpd_ph, double* rho, double* eta);
+
+/* PhSolve(rmu_after, ph_after, t) (microfluidics_complex_domain/PhSolve.f90:1-126).
+ * Inputs u (UFACE), v (VFACE), ph, rmu (CELL) are the module globals it reads. */
+int drd_phsolve(drd_ctx* ctx, const double* u, const double* v, const double* ph, const double* rmu,
+                double t, double* rmu_after, double* ph_after, drd_status* st);
+
+/* ph_mu_solve(ph_after, rmu_after, t) (two_phase_flow_complex_domain/ph_mu_solve.f90:3-197).
+ * ph_M_0 is recomputed inside the reference (:31-35) and written back (CELL, may be NULL);
+ * coef_bot_top[2] receives the global side outputs coef_bot, coef_top (may be NULL). */
+int drd_ph_mu_solve(drd_ctx* ctx, const double* u, const double* v, const double* ph, const double* rmu,
+                    double t, double* ph_after, double* rmu_after, double* ph_M_0_out,
+                    double* coef_bot_top, drd_status* st);
+
+/* VeloSolve_combined(psi, u_after, v_after, rmu_after, ph_after, t, pf1, pf2)
+ * (microfluidics_complex_domain/VeloSolve_combined.f90:5-511): first-step backward Euler.
+ * u, v (module globals), p (CELL), psi (unused by the reference, may be NULL).  uL, uR
+ * (ZLINE) receive the global inlet profiles (may be NULL). */
+int drd_velosolve_combined(drd_ctx* ctx, const double* psi, const double* u, const double* v,
+                           const double* p, const double* rmu_after, const double* ph_after, double t,
+                           const double* particle_force1, const double* particle_force2,
+                           double* u_after, double* v_after, double* uL, double* uR, drd_status* st);
+
+/* VeloSolve_2_combined(psi1, psi2, u_pre, u_after, v_pre, v_after, ph_pre, ph_after,
+ * rmu_pre, rmu_after, t, pf1, pf2) (microfluidics_complex_domain/VeloSolve_2_combined.f90:4-510
+ * and two_phase_flow_complex_domain/VeloSolve_2_combined.f90): BDF2 momentum with the DRD
+ * penalty.  ph_pre and rmu_pre are unused by the reference (may be NULL). */
+int drd_velosolve_2_combined(drd_ctx* ctx, const double* psi1, const double* psi2,
+                             const double* u_pre, const double* u, const double* v_pre, const double* v,
+                             const double* p, const double* ph_pre, const double* ph_after,
+                             const double* rmu_pre, const double* rmu_after, double t,
+                             const double* particle_force1, const double* particle_force2,
+                             double* u_after, double* v_after, double* uL, double* uR, drd_status* st);
+
+/* PreSolve_2(plan, plan_back, psi, coef) (microfluidics_complex_domain/PreSolve_2.f90:1-130 with
+ * dct_fftw :135-186): div u -> DCT-II -> / Pre_Lcc -> DCT-III -> / (4 nr nz) -> Neumann ghosts
+ * -> * coef.  u (UFACE), v (VFACE) are the module globals it reads; psi is CELL. */
+int drd_presolve_2(drd_ctx* ctx, const double* u, const double* v, double coef, double* psi,
+                   drd_status* st);
+
+/* Mass sum of dissipation() (microfluidics_complex_domain/dissipation.f90:116-122), FP64. */
+int drd_mass(drd_ctx* ctx, const double* ph, double* mass);
+
+/* ---- resident-state time stepping (the mcl6 step sequence on device) ------------------- */
+
+/* Fields of the resident state; the same arrays mcl6 keeps (mcl6.f90:22-31, global.f90:42-47). */
+#define DRD_F_U 0        /* UFACE */
+#define DRD_F_V 1        /* VFACE */
+#define DRD_F_U_PRE 2    /* UFACE */
+#define DRD_F_V_PRE 3    /* VFACE */
+#define DRD_F_PH 4       /* CELL  */
+#define DRD_F_RMU 5      /* CELL  */
+#define DRD_F_PH_PRE 6   /* CELL  */
+#define DRD_F_RMU_PRE 7  /* CELL  */
+#define DRD_F_P 8        /* CELL  */
+#define DRD_F_PSI1 9     /* CELL  */
+#define DRD_F_PSI2 10    /* CELL  */
+#define DRD_F_PF1 11     /* CELL  particle_force1 */
+#define DRD_F_PF2 12     /* CELL  particle_force2 */
+#define DRD_F_COUNT 13
+
+int drd_state_upload(drd_ctx* ctx, int field, const double* host);
+int drd_state_download(drd_ctx* ctx, int field, double* host);
+/* Device pointer of a resident field (for callers that keep data on the GPU). */
+int drd_state_device_ptr(drd_ctx* ctx, int field, double** dptr);
+
+typedef struct drd_step_stats {
+    drd_status ch;   /* PhSolve or ph_mu_solve */
+    drd_status uv;   /* VeloSolve(_2)_combined  */
+    drd_status pre;  /* PreSolve_2              */
+    double mass;     /* sum(ph) dr dz after the step (FP64)  */
+    double t;        /* time after the step     */
+} drd_step_stats;
+
+/* One pass of the mcl6 time loop body (microfluidics_complex_domain/mcl6.f90:378-486, the
+ * first step :239-306 when `first` != 0): CH solve -> momentum -> swaps -> pressure ->
+ * p += psi2, on the resident state, with particles held fixed (coefficients as last set).
+ * t is the time before the step; solves see t + dt as in the reference.  `stats` may be NULL;
+ * when non-NULL the call waits for the step and fills it. */
+int drd_step(drd_ctx* ctx, int first, double t, drd_step_stats* stats);
+/* Enqueue `nsteps` steps without host synchronisation (stats are not collected). */
+int drd_steps_async(drd_ctx* ctx, int first, double t, int nsteps);
+int drd_synchronize(drd_ctx* ctx);
+
+/* ---- operator access (verification) ---------------------------------------------------- */
+
+/* Operators of the three Krylov systems on packed vectors (the reference's Atob orders):
+ *   DRD_OP_CH_MATVEC   MATRIX_VECTOR_CG (microfluidics_complex_domain/PhSolve.f90:240-292)
+ *   DRD_OP_CH_PSOLVE   PSolve_CG -> DCT (PhSolve.f90:296-313, DCT.f90:1-57)
+ *   DRD_OP_UV_MATVEC   MatrixVector_uv_2_CG / MatrixVector_uv_CG (bdf 2 / 1)
+ *   DRD_OP_UV_PSOLVE   PSolve_uv_2_CG / PSolve_uv_CG Jacobi (identity for TP bdf 2)
+ *   DRD_OP_PHMU_MATVEC MATRIX_VECTOR_PH_MU_CG (two_phase_flow_complex_domain/ph_mu_solve.f90:203-299)
+ *   DRD_OP_PHMU_PSOLVE PSolve_PH_MU_CG (:304-380)
+ * y = op(x) with the context's current coefficients, in FP64 (precision DRD_PREC_FP64) or
+ * with the FP32 operators of the mixed mode (DRD_PREC_MIXED; x and y stay FP64 arrays). */
+#define DRD_OP_CH_MATVEC 0
+#define DRD_OP_CH_PSOLVE 1
+#define DRD_OP_UV_MATVEC 2
+#define DRD_OP_UV_PSOLVE 3
+#define DRD_OP_PHMU_MATVEC 4
+#define DRD_OP_PHMU_PSOLVE 5
+int drd_op_apply(drd_ctx* ctx, int op, int bdf, int precision, const double* x, double* y);
+/* Length of the packed vector of operator `op`. */
+long drd_op_length(drd_ctx* ctx, int op);
+
+/* ---- performance instrumentation ------------------------------------------------------- */
+
+/* Number of kernels this library has launched on the context (graph nodes counted per
+ * execution), cumulative. */
+int64_t drd_kernel_launches(drd_ctx* ctx);
+/* Raw CUDA stream of the context (cudaStream_t), for callers timing with events. */
+void* drd_stream(drd_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DRD_GB300_H */

@@ -1,0 +1,1026 @@
+/*
+ * drd_oracle.c — FP64 CPU restatement of the DRD-Micro per-time-step solver core.
+ *
+ * TEST INFRASTRUCTURE ONLY: this file is the checker for the CUDA library.  Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline legs load it; nothing in the
+ * product path calls it.  Parity is "unpinned" against reference-run outputs (none exist
+ * and the Fortran reference cannot be built); see drd_oracle.h for the pins used instead.
+ *
+ * Each routine cites the reference lines it restates.  Arithmetic follows the Fortran
+ * left-to-right evaluation order of those lines so that a faithful build of the
+ * reference would agree to rounding.  Transforms are evaluated by direct summation of
+ * their published definitions (vfftpack VCOST prologue, FFTW REDFT10/REDFT01).
+ */
+#include "drd_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define CI(i, k) ((long)((i) + 1) + (long)((k) + 1) * (nr + 2)) /* CELL  (-1:nr,  -1:nz) */
+#define UI(i, k) ((long)((i) + 1) + (long)((k) + 1) * (nr + 3)) /* UFACE (-1:nr+1,-1:nz) */
+#define VI(i, k) ((long)((i) + 1) + (long)(k) * (nr + 2))       /* VFACE (-1:nr,   0:nz) */
+
+static const double kPi = 3.14159265358979323846264338327950288; /* global.f90:27 */
+static const double kPimach = 3.14159265358979;                  /* lib/vfftpack.f:294 PIMACH */
+static const double kBreakTol = 1.2325951644078309e-32;           /* GETBREAK = DLAMCH('E')**2 */
+
+static long cell_size(int nr, int nz) { return (long)(nr + 2) * (nz + 2); }
+static long u_size(int nr, int nz) { return (long)(nr + 3) * (nz + 2); }
+static long v_size(int nr, int nz) { return (long)(nr + 2) * (nz + 1); }
+static long uv_len(int nr, int nz) { return (long)(nr + 1) * nz + (long)nr * (nz - 1); }
+
+static double* dalloc(long n) { return (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double)); }
+
+/* ---------------------------------------------------------------------------------------
+ * BLAS-1 (the MKL routines BiCGSTABREVCOM calls), sequential order.
+ * ------------------------------------------------------------------------------------- */
+static double ddot(long n, const double* x, const double* y) {
+    double s = 0.0;
+    for (long i = 0; i < n; ++i) s += x[i] * y[i];
+    return s;
+}
+static double dnrm2(long n, const double* x) { return sqrt(ddot(n, x, x)); }
+static void daxpy(long n, double a, const double* x, double* y) {
+    for (long i = 0; i < n; ++i) y[i] += a * x[i];
+}
+
+/* ---------------------------------------------------------------------------------------
+ * setup() tables: microfluidics_complex_domain/setup.f90:106-155.
+ * ------------------------------------------------------------------------------------- */
+void orc_setup_tables(const drd_params* P, double* ph_lcc, double* pre_lcc) {
+    const int nr = P->nr, nz = P->nz;
+    const double dr2 = P->dr * P->dr, dz2 = P->dz * P->dz;
+    /* Pre_Lcc(0:nr,0:nz) = -(fmx(i)+fmy(j)), fmx(i) = 4 sin^2(pi i/(2 nr))/dr2; Pre_Lcc(0,0) = -1 */
+    for (int j = 0; j <= nz; ++j) {
+        double t1 = kPi * j / 2.0 / nz;
+        double fmy = 4.0 * (sin(t1) * sin(t1)) / dz2;
+        for (int i = 0; i <= nr; ++i) {
+            double t0 = kPi * i / 2.0 / nr;
+            double fmx = 4.0 * (sin(t0) * sin(t0)) / dr2;
+            pre_lcc[i + (long)j * (nr + 1)] = -(fmx + fmy);
+        }
+    }
+    pre_lcc[0] = -1.0; /* setup.f90:131 */
+    /* Ph_Lcc(0:nr-1,0:nz-1) with the eigenvalues of the (nr-1, nz-1)-interval grid (:134-155) */
+    for (int j = 0; j < nz; ++j) {
+        double t1 = kPi * j / 2.0 / (nz - 1);
+        double fmy = 4.0 * (sin(t1) * sin(t1)) / dz2;
+        for (int i = 0; i < nr; ++i) {
+            double t0 = kPi * i / 2.0 / (nr - 1);
+            double fmx = 4.0 * (sin(t0) * sin(t0)) / dr2;
+            double temp = fmx + fmy;
+            ph_lcc[i + (long)j * nr] = 1. + P->xld * P->dt * P->s_implicit * temp / P->I_thickness +
+                                       P->xld * P->I_thickness * P->dt * (temp * temp);
+        }
+    }
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Transforms by direct summation of their definitions.
+ * ------------------------------------------------------------------------------------- */
+
+/* VCOST (lib/vfftpack.f:689-704):
+ *   X_i = ( x_1 + (-1)^(i-1) x_N + sum_{k=2}^{N-1} 2 x_k cos((k-1)(i-1) pi/(N-1)) ) / sqrt(2(N-1))
+ * with pi = PIMACH.  Self-inverse. */
+void orc_vcost(int n, int m, double* x, long seq_stride, long elem_stride) {
+    if (n < 2 || m <= 0) return;
+    const long period = 2L * (n - 1);
+    double* tab = dalloc(period);
+    double* in = dalloc(n);
+    for (long q = 0; q < period; ++q) tab[q] = cos((double)q * kPimach / (double)(n - 1));
+    const double scale = sqrt(2.0 * (n - 1));
+    for (int s = 0; s < m; ++s) {
+        double* xs = x + (long)s * seq_stride;
+        for (int j = 0; j < n; ++j) in[j] = xs[j * elem_stride];
+        for (int i = 0; i < n; ++i) {
+            double acc = in[0] + ((i & 1) ? -in[n - 1] : in[n - 1]);
+            long idx = 0;
+            for (int k = 1; k < n - 1; ++k) {
+                idx += i;
+                if (idx >= period) idx -= period * (idx / period);
+                acc += 2.0 * in[k] * tab[idx];
+            }
+            xs[i * elem_stride] = acc / scale;
+        }
+    }
+    free(tab);
+    free(in);
+}
+
+/* REDFT10 (DCT-II, FFTW manual): Y_k = 2 sum_{j=0}^{n-1} X_j cos(pi (j+1/2) k / n). */
+void orc_redft10(int n, int m, double* x, long seq_stride, long elem_stride) {
+    if (n < 1 || m <= 0) return;
+    const long period = 4L * n;
+    double* tab = dalloc(period);
+    double* in = dalloc(n);
+    for (long q = 0; q < period; ++q) tab[q] = cos(kPi * (double)q / (2.0 * n));
+    for (int s = 0; s < m; ++s) {
+        double* xs = x + (long)s * seq_stride;
+        for (int j = 0; j < n; ++j) in[j] = xs[j * elem_stride];
+        for (int k = 0; k < n; ++k) {
+            double acc = 0.0;
+            for (int j = 0; j < n; ++j) acc += in[j] * tab[((long)(2 * j + 1) * k) % period];
+            xs[k * elem_stride] = 2.0 * acc;
+        }
+    }
+    free(tab);
+    free(in);
+}
+
+/* REDFT01 (DCT-III, FFTW manual): Y_k = X_0 + 2 sum_{j=1}^{n-1} X_j cos(pi j (k+1/2) / n). */
+void orc_redft01(int n, int m, double* x, long seq_stride, long elem_stride) {
+    if (n < 1 || m <= 0) return;
+    const long period = 4L * n;
+    double* tab = dalloc(period);
+    double* in = dalloc(n);
+    for (long q = 0; q < period; ++q) tab[q] = cos(kPi * (double)q / (2.0 * n));
+    for (int s = 0; s < m; ++s) {
+        double* xs = x + (long)s * seq_stride;
+        for (int j = 0; j < n; ++j) in[j] = xs[j * elem_stride];
+        for (int k = 0; k < n; ++k) {
+            double acc = 0.0;
+            for (int j = 1; j < n; ++j) acc += in[j] * tab[((long)j * (2 * k + 1)) % period];
+            xs[k * elem_stride] = in[0] + 2.0 * acc;
+        }
+    }
+    free(tab);
+    free(in);
+}
+
+/* ---------------------------------------------------------------------------------------
+ * op_double_gradient_Neum: microfluidics_complex_domain/matrix_tool.f90:178-219.
+ * out = 0 everywhere, then the variable-coefficient 5-point operator on the interior with
+ * zero flux through the domain faces.  Reads no ghost values.
+ * ------------------------------------------------------------------------------------- */
+void orc_op_double_gradient_neum(int nr, int nz, double dx2, double dy2, const double* x,
+                                 const double* mo, double* out) {
+    memset(out, 0, sizeof(double) * cell_size(nr, nz));
+    for (int j = 0; j < nz; ++j) {
+        for (int i = 0; i < nr; ++i) {
+            double moL, moR, acc = 0.0;
+            if (i == 0) {
+                moL = (mo[CI(i, j)] + mo[CI(i, j)]) / 2.0;
+                moR = (mo[CI(i, j)] + mo[CI(i + 1, j)]) / 2.0;
+                acc = acc + 1.0 / dx2 * (moL * x[CI(i, j)] + moR * x[CI(i + 1, j)] - (moL + moR) * x[CI(i, j)]);
+            } else if (i == nr - 1) {
+                moL = (mo[CI(i - 1, j)] + mo[CI(i, j)]) / 2.0;
+                moR = (mo[CI(i, j)] + mo[CI(i, j)]) / 2.0;
+                acc = acc + 1.0 / dx2 * (moL * x[CI(i - 1, j)] + moR * x[CI(i, j)] - (moL + moR) * x[CI(i, j)]);
+            } else {
+                moL = (mo[CI(i - 1, j)] + mo[CI(i, j)]) / 2.0;
+                moR = (mo[CI(i, j)] + mo[CI(i + 1, j)]) / 2.0;
+                acc = acc + 1.0 / dx2 * (moL * x[CI(i - 1, j)] + moR * x[CI(i + 1, j)] - (moL + moR) * x[CI(i, j)]);
+            }
+            if (j == 0) {
+                moL = (mo[CI(i, j)] + mo[CI(i, j)]) / 2.0;
+                moR = (mo[CI(i, j)] + mo[CI(i, j + 1)]) / 2.0;
+                acc = acc + 1.0 / dy2 * (moL * x[CI(i, j)] + moR * x[CI(i, j + 1)] - (moL + moR) * x[CI(i, j)]);
+            } else if (j == nz - 1) {
+                moL = (mo[CI(i, j - 1)] + mo[CI(i, j)]) / 2.0;
+                moR = (mo[CI(i, j)] + mo[CI(i, j)]) / 2.0;
+                acc = acc + 1.0 / dy2 * (moL * x[CI(i, j - 1)] + moR * x[CI(i, j)] - (moL + moR) * x[CI(i, j)]);
+            } else {
+                moL = (mo[CI(i, j - 1)] + mo[CI(i, j)]) / 2.0;
+                moR = (mo[CI(i, j)] + mo[CI(i, j + 1)]) / 2.0;
+                acc = acc + 1.0 / dy2 * (moL * x[CI(i, j - 1)] + moR * x[CI(i, j + 1)] - (moL + moR) * x[CI(i, j)]);
+            }
+            out[CI(i, j)] = acc;
+        }
+    }
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Pack / unpack: microfluidics_complex_domain/matrix_tool.f90:5-173.
+ * ------------------------------------------------------------------------------------- */
+static void atob_cell(int nr, int nz, const double* f, double* b) { /* Atob(nr-1,nz-1,...) :142-155 */
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i < nr; ++i) b[i + (long)nr * j] = f[CI(i, j)];
+}
+static void btoa_cell(int nr, int nz, double* f, const double* b) { /* btoA(nr-1,nz-1,...) :160-173 */
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i < nr; ++i) f[CI(i, j)] = b[i + (long)nr * j];
+}
+static void atob_uv(int nr, int nz, const double* f1, const double* f2, double* b) { /* :5-26 */
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i <= nr; ++i) b[i + (long)(nr + 1) * j] = f1[UI(i, j)];
+    const long mn = (long)(nr + 1) * nz;
+    for (int j = 1; j < nz; ++j)
+        for (int i = 0; i < nr; ++i) b[i + (long)nr * (j - 1) + mn] = f2[VI(i, j)];
+}
+static void btoa_uv(int nr, int nz, double* f1, double* f2, const double* b) { /* :32-75 */
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i <= nr; ++i) f1[UI(i, j)] = b[i + (long)(nr + 1) * j];
+    const long mn = (long)(nr + 1) * nz;
+    for (int j = 1; j < nz; ++j)
+        for (int i = 0; i < nr; ++i) f2[VI(i, j)] = b[i + (long)nr * (j - 1) + mn];
+    for (int i = 0; i <= nr; ++i) {
+        f1[UI(i, -1)] = -f1[UI(i, 0)];
+        f1[UI(i, nz)] = -f1[UI(i, nz - 1)];
+    }
+    for (int j = -1; j <= nz; ++j) {
+        f1[UI(-1, j)] = f1[UI(1, j)];
+        f1[UI(nr + 1, j)] = f1[UI(nr - 1, j)];
+    }
+    for (int i = 0; i < nr; ++i) {
+        f2[VI(i, 0)] = 0;
+        f2[VI(i, nz)] = 0;
+    }
+    for (int j = 0; j <= nz; ++j) {
+        f2[VI(-1, j)] = f2[VI(0, j)];
+        f2[VI(nr, j)] = f2[VI(nr - 1, j)];
+    }
+}
+static void atob_ph_mu(int nr, int nz, const double* f1, const double* f2, double* b) { /* :82-98 */
+    const long mn = (long)nr * nz;
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i < nr; ++i) {
+            b[i + (long)nr * j] = f1[CI(i, j)];
+            b[i + (long)nr * j + mn] = f2[CI(i, j)];
+        }
+}
+static void btoa_ph_mu(int nr, int nz, double* f1, double* f2, const double* b) { /* :104-136 */
+    const long mn = (long)nr * nz;
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i < nr; ++i) {
+            f1[CI(i, j)] = b[i + (long)nr * j];
+            f2[CI(i, j)] = b[i + (long)nr * j + mn];
+        }
+    for (int i = 0; i < nr; ++i) {
+        f1[CI(i, -1)] = f1[CI(i, 0)];
+        f1[CI(i, nz)] = f1[CI(i, nz - 1)];
+        f2[CI(i, -1)] = f2[CI(i, 0)];
+        f2[CI(i, nz)] = f2[CI(i, nz - 1)];
+    }
+    for (int j = -1; j <= nz; ++j) {
+        f1[CI(-1, j)] = f1[CI(0, j)];
+        f1[CI(nr, j)] = f1[CI(nr - 1, j)];
+        f2[CI(-1, j)] = f2[CI(0, j)];
+        f2[CI(nr, j)] = f2[CI(nr - 1, j)];
+    }
+}
+
+/* ---------------------------------------------------------------------------------------
+ * BiCGSTAB: lib/BiCGSTAB.f:153-217 driving lib/BiCGSTABREVCOM.f:150-418 with
+ * lib/STOPTEST2.f:281-290.  Right preconditioning, absolute early tests at :248 and
+ * :313, relative final test in STOPTEST2, breakdown at |rho|,|omega| < eps^2.
+ * ------------------------------------------------------------------------------------- */
+int orc_bicgstab(long n, const double* b, double* x, int maxit, double tol, orc_matvec_fn mv,
+                 orc_psolve_fn ps, void* ctx, drd_status* st) {
+    drd_status local;
+    if (!st) st = &local;
+    memset(st, 0, sizeof(*st));
+    if (n < 0) { st->info = -1; return -1; }
+    if (maxit <= 0) { st->info = -3; return -3; }
+    double* r = dalloc(n);
+    double* rtld = dalloc(n);
+    double* p = dalloc(n);
+    double* v = dalloc(n);
+    double* t = dalloc(n);
+    double* phat = dalloc(n);
+    double* shat = dalloc(n);
+    int info = 0, iter = maxit;
+    double resid = tol, rho = 0.0, rho1 = 0.0, alpha = 0.0, omega = 0.0, bnrm2;
+
+    memcpy(r, b, sizeof(double) * n);
+    if (dnrm2(n, x) != 0.0) {
+        mv(ctx, -1.0, x, 1.0, r);
+        if (dnrm2(n, r) <= tol) { st->flags |= DRD_FLAG_EARLY_X0; goto done; }
+    }
+    memcpy(rtld, r, sizeof(double) * n);
+    bnrm2 = dnrm2(n, b);
+    if (bnrm2 == 0.0) bnrm2 = 1.0;
+    iter = 0;
+    for (;;) {
+        iter = iter + 1;
+        rho = ddot(n, rtld, r);
+        if (fabs(rho) < kBreakTol) { info = -10; goto done; }
+        if (iter > 1) {
+            double beta = (rho / rho1) * (alpha / omega);
+            daxpy(n, -omega, v, p);
+            for (long q = 0; q < n; ++q) p[q] = beta * p[q];
+            daxpy(n, 1.0, r, p);
+        } else {
+            memcpy(p, r, sizeof(double) * n);
+        }
+        ps(ctx, p, phat);
+        mv(ctx, 1.0, phat, 0.0, v);
+        alpha = rho / ddot(n, rtld, v);
+        daxpy(n, -alpha, v, r); /* s = r - alpha v, s aliases r */
+        if (dnrm2(n, r) <= tol) {
+            daxpy(n, alpha, phat, x);
+            resid = dnrm2(n, r) / bnrm2;
+            st->flags |= DRD_FLAG_EARLY_S;
+            info = 0;
+            goto done;
+        }
+        ps(ctx, r, shat);
+        mv(ctx, 1.0, shat, 0.0, t);
+        omega = ddot(n, t, r) / ddot(n, t, t);
+        daxpy(n, alpha, phat, x);
+        daxpy(n, omega, shat, x);
+        daxpy(n, -omega, t, r);
+        resid = dnrm2(n, r) / bnrm2; /* STOPTEST2 */
+        if (resid <= tol) { info = 0; goto done; }
+        if (iter == maxit) { info = 1; goto done; }
+        if (fabs(omega) < kBreakTol) { info = (fabs(rho) < kBreakTol) ? -10 : -11; goto done; }
+        rho1 = rho;
+    }
+done:
+    st->info = info;
+    st->iter = iter;
+    st->resid = resid;
+    /* true residual of the returned x (not part of the reference; reported alongside) */
+    {
+        memcpy(t, b, sizeof(double) * n);
+        mv(ctx, -1.0, x, 1.0, t);
+        double bn = dnrm2(n, b);
+        st->true_resid = dnrm2(n, t) / (bn == 0.0 ? 1.0 : bn);
+    }
+    free(r); free(rtld); free(p); free(v); free(t); free(phat); free(shat);
+    return info;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * CH operators: microfluidics_complex_domain/PhSolve.f90:240-313.
+ * ------------------------------------------------------------------------------------- */
+void orc_ch_matvec(const drd_params* P, const double* M0, const double* Mi, double alpha,
+                   const double* x, double beta, double* y) {
+    const int nr = P->nr, nz = P->nz;
+    const double dr2 = P->dr * P->dr, dz2 = P->dz * P->dz;
+    const long cs = cell_size(nr, nz);
+    double* f1 = dalloc(cs);
+    double* ff1 = dalloc(cs);
+    double* ff2 = dalloc(cs);
+    btoa_cell(nr, nz, f1, x);
+    orc_op_double_gradient_neum(nr, nz, dr2, dz2, f1, M0, ff1);
+    for (long q = 0; q < cs; ++q) ff1[q] = -(P->dt * P->xld * ff1[q]);
+    orc_op_double_gradient_neum(nr, nz, dr2, dz2, ff1, Mi, ff2);
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i < nr; ++i) {
+            long c = CI(i, j), q = i + (long)nr * j;
+            double a = P->s_implicit * ff1[c] / P->I_thickness - P->I_thickness * ff2[c];
+            double av = f1[c] + a;
+            y[q] = (beta == 0.0) ? alpha * av : alpha * av + beta * y[q];
+        }
+    free(f1); free(ff1); free(ff2);
+}
+
+/* PSolve_CG -> DCT(nr-1, nz-1, f1, f2, Ph_Lcc, ...) (microfluidics_complex_domain/DCT.f90:1-57):
+ * VCOST along z, VCOST along x, divide by Ph_Lcc, VCOST along z, VCOST along x. */
+void orc_ch_psolve(const drd_params* P, const double* ph_lcc, const double* x, double* y) {
+    const int nr = P->nr, nz = P->nz;
+    const long n = (long)nr * nz;
+    double* w = dalloc(n);
+    memcpy(w, x, sizeof(double) * n);
+    orc_vcost(nz, nr, w, 1, nr); /* sequences along z: one per i */
+    orc_vcost(nr, nz, w, nr, 1); /* sequences along x: one per k */
+    for (long q = 0; q < n; ++q) w[q] = w[q] / ph_lcc[q];
+    orc_vcost(nz, nr, w, 1, nr);
+    orc_vcost(nr, nz, w, nr, 1);
+    memcpy(y, w, sizeof(double) * n);
+    free(w);
+}
+
+typedef struct { const drd_params* P; const double* M0; const double* Mi; const double* lcc; } ch_ctx;
+static void ch_mv_cb(void* c, double a, const double* x, double b, double* y) {
+    ch_ctx* C = (ch_ctx*)c;
+    orc_ch_matvec(C->P, C->M0, C->Mi, a, x, b, y);
+}
+static void ch_ps_cb(void* c, const double* x, double* y) {
+    ch_ctx* C = (ch_ctx*)c;
+    orc_ch_psolve(C->P, C->lcc, x, y);
+}
+
+/* ch_bulk_energy: microfluidics_complex_domain/ch_bulk_energy.f90:4-28 (localised double well). */
+static double bulk_mf(double phi, double psi) {
+    double aa = (phi * phi) * ((1.0 - phi) * (1.0 - phi));
+    aa = 1.0 - sqrt(aa / (aa + 1.0E-2)) * psi;
+    return 0.5 * phi * (1.0 - phi) * (1.0 - 2.0 * phi) * aa;
+}
+
+/* PhSolve: microfluidics_complex_domain/PhSolve.f90:1-126. */
+int orc_phsolve(const drd_params* P, const double* ph_lcc, const double* u, const double* v,
+                const double* ph, const double* rmu, const double* bdr_ph, const double* bdr_ph_grad,
+                const double* M0, const double* Mi, double* rmu_after, double* ph_after, drd_status* st) {
+    const int nr = P->nr, nz = P->nz;
+    const double dr = P->dr, dz = P->dz, dt = P->dt, eps = P->I_thickness, s = P->s_implicit;
+    const double dr2 = dr * dr, dz2 = dz * dz;
+    const long cs = cell_size(nr, nz), n = (long)nr * nz;
+    double* f1 = dalloc(cs);
+    double* f2 = dalloc(cs);
+    double* ff = dalloc(cs);
+    double* rhs = dalloc(n);
+    double* x = dalloc(n);
+    memcpy(f2, ph, sizeof(double) * cs); /* :26 */
+    for (int k = 0; k < nz; ++k)        /* :29-34 */
+        for (int i = 0; i < nr; ++i)
+            f2[CI(i, k)] = f2[CI(i, k)] -
+                           dt * (u[UI(i + 1, k)] + u[UI(i, k)]) / 2.0 * (ph[CI(i + 1, k)] - ph[CI(i - 1, k)]) / 2.0 / dr -
+                           dt * (v[VI(i, k + 1)] + v[VI(i, k)]) / 2.0 * (ph[CI(i, k + 1)] - ph[CI(i, k - 1)]) / 2.0 / dz;
+    const double cang = cos(P->angle * kPi / 180);
+    for (int k = 0; k < nz; ++k) /* :37-42 */
+        for (int i = 0; i < nr; ++i) {
+            double p0 = ph[CI(i, k)];
+            f1[CI(i, k)] = s * p0 / eps - bulk_mf(p0, bdr_ph[CI(i, k)]) / eps -
+                           p0 * (p0 - 1.0) * bdr_ph_grad[CI(i, k)] * cang / sqrt(2.0);
+        }
+    orc_op_double_gradient_neum(nr, nz, dr2, dz2, f2, Mi, ff); /* :47 */
+    for (int k = 0; k < nz; ++k)                               /* :48 (interior is what Atob reads) */
+        for (int i = 0; i < nr; ++i) {
+            long c = CI(i, k);
+            f1[c] = -f1[c] + s * f2[c] / eps - eps * ff[c];
+        }
+    atob_cell(nr, nz, f1, rhs); /* :62-63 */
+    atob_cell(nr, nz, rmu, x);
+    ch_ctx C = {P, M0, Mi, ph_lcc};
+    int info = orc_bicgstab(n, rhs, x, P->ch_maxit, P->tol, ch_mv_cb, ch_ps_cb, &C, st); /* :72-74 */
+    memcpy(rmu_after, rmu, sizeof(double) * cs);
+    btoa_cell(nr, nz, rmu_after, x); /* :85 */
+    for (int i = 0; i < nr; ++i) {   /* :88-96 */
+        rmu_after[CI(i, -1)] = rmu_after[CI(i, 0)];
+        rmu_after[CI(i, nz)] = rmu_after[CI(i, nz - 1)];
+    }
+    for (int k = -1; k <= nz; ++k) {
+        rmu_after[CI(-1, k)] = rmu_after[CI(0, k)];
+        rmu_after[CI(nr, k)] = rmu_after[CI(nr - 1, k)];
+    }
+    orc_op_double_gradient_neum(nr, nz, dr2, dz2, rmu_after, M0, ff); /* :100-101 */
+    for (long q = 0; q < cs; ++q) ph_after[q] = f2[q] + dt * P->xld * ff[q];
+    for (int i = 0; i < nr; ++i) { /* :111-124 */
+        ph_after[CI(i, -1)] = ph_after[CI(i, 0)];
+        ph_after[CI(i, nz)] = ph_after[CI(i, nz - 1)];
+    }
+    for (int k = -1; k <= nz; ++k) {
+        ph_after[CI(-1, k)] = ph_after[CI(0, k)];
+        ph_after[CI(nr, k)] = ph_after[CI(nr - 1, k)];
+    }
+    free(f1); free(f2); free(ff); free(rhs); free(x);
+    return info;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Coupled CH: two_phase_flow_complex_domain/ph_mu_solve.f90:3-380, ch_bulk_energy.f90:32-67,
+ * ch_bdr_condition.f90:3-27.
+ * ------------------------------------------------------------------------------------- */
+static double bulk_tp(double phi, double psi, int mode) {
+    if (mode == 1) return 0.5 * phi * (1.0 - phi) * (1.0 - 2.0 * phi) * (1 - psi);
+    return (phi * phi * phi - phi) * (1 - psi);
+}
+static double bdr_cond_tp(double angle, double phi, int mode) {
+    double cf = cos(angle * kPi / 180.0) / sqrt(2.0);
+    if (mode == 1) return cf * (1.0 - phi) * phi;
+    return cf * (1.0 - phi * phi);
+}
+
+void orc_phmu_matvec(const drd_params* P, const double* M0, const double* Mi, const double* bdr_used,
+                     double coef_bot, double coef_top, double alpha, const double* x, double beta,
+                     double* y) {
+    const int nr = P->nr, nz = P->nz;
+    const double dr2 = P->dr * P->dr, dz2 = P->dz * P->dz, eps = P->I_thickness;
+    const long cs = cell_size(nr, nz), mn = (long)nr * nz;
+    double* f1 = dalloc(cs);
+    double* f2 = dalloc(cs);
+    double* ff1 = dalloc(cs);
+    double* ff2 = dalloc(cs);
+    btoa_ph_mu(nr, nz, f1, f2, x);
+    orc_op_double_gradient_neum(nr, nz, dr2, dz2, f1, Mi, ff1); /* :214 */
+    for (int j = 0; j < nz; ++j)                                  /* :216-224 */
+        for (int i = 0; i < nr; ++i) {
+            long c = CI(i, j);
+            ff1[c] = P->s_implicit * f1[c] / eps - eps * ff1[c] - f2[c] * bdr_used[c];
+        }
+    for (int i = 0; i < nr; ++i) { /* :227-233 */
+        ff1[CI(i, 0)] = ff1[CI(i, 0)] + eps / dz2 * (f1[CI(i, -1)] - coef_bot * f1[CI(i, 0)]);
+        ff1[CI(i, nz - 1)] = ff1[CI(i, nz - 1)] + eps / dz2 * (f1[CI(i, nz)] - coef_top * f1[CI(i, nz - 1)]);
+    }
+    orc_op_double_gradient_neum(nr, nz, dr2, dz2, f2, M0, ff2); /* :245 */
+    for (int j = 0; j < nz; ++j)                                  /* :247-253 */
+        for (int i = 0; i < nr; ++i) {
+            long c = CI(i, j);
+            ff2[c] = f1[c] * (bdr_used[c] + P->bdr_ph_used_adjust) - P->dt * P->xld * ff2[c];
+        }
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i < nr; ++i) {
+            long c = CI(i, j), q = i + (long)nr * j;
+            y[q] = (beta == 0.0) ? alpha * ff1[c] : alpha * ff1[c] + beta * y[q];
+            y[q + mn] = (beta == 0.0) ? alpha * ff2[c] : alpha * ff2[c] + beta * y[q + mn];
+        }
+    free(f1); free(f2); free(ff1); free(ff2);
+}
+
+/* PSolve_PH_MU_CG Jacobi (:304-356), including `j == nr-1` in the x test and `i == 0` in the
+ * z test exactly as written there. */
+void orc_phmu_psolve(const drd_params* P, const double* x, double* y) {
+    const int nr = P->nr, nz = P->nz;
+    const double dr2 = P->dr * P->dr, dz2 = P->dz * P->dz, eps = P->I_thickness;
+    const long mn = (long)nr * nz;
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i < nr; ++i) {
+            double tmpx = (i == 0 || j == nr - 1) ? 1.0 / dr2 : 2.0 / dr2;
+            double tmpz = (i == 0 || j == nz - 1) ? 1.0 / dz2 : 2.0 / dz2;
+            long q = i + (long)nr * j;
+            y[q] = x[q] / ((tmpx + tmpz) * eps + P->s_implicit / eps);
+            y[q + mn] = x[q + mn] / (P->dt * P->xld * (tmpx + tmpz));
+        }
+}
+
+typedef struct {
+    const drd_params* P; const double* M0; const double* Mi; const double* used; double cb, ct;
+} phmu_ctx;
+static void phmu_mv_cb(void* c, double a, const double* x, double b, double* y) {
+    phmu_ctx* C = (phmu_ctx*)c;
+    orc_phmu_matvec(C->P, C->M0, C->Mi, C->used, C->cb, C->ct, a, x, b, y);
+}
+static void phmu_ps_cb(void* c, const double* x, double* y) {
+    phmu_ctx* C = (phmu_ctx*)c;
+    orc_phmu_psolve(C->P, x, y);
+}
+
+int orc_ph_mu_solve(const drd_params* P, const double* u, const double* v, const double* ph,
+                    const double* rmu, const double* bdr_ph, const double* bdr_ph_used,
+                    const double* bdr_ph_grad, const double* Mi, const double* angleB,
+                    const double* angleT, double* M0, double* ph_after, double* rmu_after,
+                    double* coef_bot_top, drd_status* st) {
+    const int nr = P->nr, nz = P->nz, mode = P->phi_mode;
+    const double dr = P->dr, dz = P->dz, dt = P->dt, eps = P->I_thickness, s = P->s_implicit;
+    const double dz2 = dz * dz;
+    const long cs = cell_size(nr, nz), n = 2L * nr * nz;
+    double* f1 = dalloc(cs);
+    double* f2 = dalloc(cs);
+    double* rhs = dalloc(n);
+    double* x = dalloc(n);
+    double* pnb = dalloc(nr);
+    double* pnt = dalloc(nr);
+    for (long q = 0; q < cs; ++q) { /* :31-35 */
+        double p0 = ph[q];
+        if (mode == 1) M0[q] = (1.0 - bdr_ph[q]) * (p0 * p0) * ((p0 - 1.0) * (p0 - 1.0));
+        else M0[q] = (1.0 - bdr_ph[q]) * ((p0 * p0 - 1.0) * (p0 * p0 - 1.0));
+    }
+    for (long q = 0; q < cs; ++q) f2[q] = ph[q] * (bdr_ph_used[q] + P->bdr_ph_used_adjust); /* :40 */
+    for (int k = 0; k < nz; ++k) /* :43-51 */
+        for (int i = 0; i < nr; ++i)
+            f2[CI(i, k)] = f2[CI(i, k)] -
+                           dt * (u[UI(i + 1, k)] + u[UI(i, k)]) / 2.0 *
+                               (ph[CI(i + 1, k)] * bdr_ph_used[CI(i + 1, k)] - ph[CI(i - 1, k)] * bdr_ph_used[CI(i - 1, k)]) / 2.0 / dr -
+                           dt * (v[VI(i, k + 1)] + v[VI(i, k)]) / 2.0 *
+                               (ph[CI(i, k + 1)] * bdr_ph_used[CI(i, k + 1)] - ph[CI(i, k - 1)] * bdr_ph_used[CI(i, k - 1)]) / 2.0 / dz;
+    const double cang = cos(P->angle * kPi / 180);
+    for (int k = 0; k < nz; ++k) /* :55-77 */
+        for (int i = 0; i < nr; ++i) {
+            double p0 = ph[CI(i, k)];
+            double wet = (mode == 1) ? p0 * (p0 - 1.0) : (p0 * p0 - 1.0);
+            f1[CI(i, k)] = s * p0 / eps - bulk_tp(p0, bdr_ph[CI(i, k)], mode) / eps -
+                           wet * bdr_ph_grad[CI(i, k)] * cang / sqrt(2.0);
+        }
+    double coef_bot = 1.0, coef_top = 1.0;
+    for (int i = 0; i < nr; ++i) { /* :109-127 */
+        double tmp = (ph[CI(i, -1)] + ph[CI(i, 0)]) / 2.0;
+        pnb[i] = bdr_cond_tp(angleB[i], tmp, mode);
+    }
+    for (int i = 0; i < nr; ++i) {
+        double tmp = eps / dz;
+        coef_bot = (eps / dz) / tmp;
+        pnb[i] = pnb[i] / tmp;
+        f1[CI(i, 0)] = f1[CI(i, 0)] + pnb[i] * eps / dz2;
+    }
+    for (int i = 0; i < nr; ++i) { /* :130-149 */
+        double tmp = (ph[CI(i, nz - 1)] + ph[CI(i, nz)]) / 2.0;
+        pnt[i] = bdr_cond_tp(angleT[i], tmp, mode);
+    }
+    for (int i = 0; i < nr; ++i) {
+        double tmp = eps / dz;
+        coef_top = (eps / dz) / tmp;
+        pnt[i] = pnt[i] / tmp;
+        f1[CI(i, nz - 1)] = f1[CI(i, nz - 1)] + pnt[i] * eps / dz2;
+    }
+    atob_ph_mu(nr, nz, f1, f2, rhs); /* :152-153 */
+    atob_ph_mu(nr, nz, ph, rmu, x);
+    phmu_ctx C = {P, M0, Mi, bdr_ph_used, coef_bot, coef_top};
+    int info = orc_bicgstab(n, rhs, x, P->phmu_maxit, P->tol, phmu_mv_cb, phmu_ps_cb, &C, st);
+    memcpy(ph_after, ph, sizeof(double) * cs);
+    memcpy(rmu_after, rmu, sizeof(double) * cs);
+    btoa_ph_mu(nr, nz, ph_after, rmu_after, x); /* :173-177 */
+    for (int i = 0; i < nr; ++i) {
+        ph_after[CI(i, -1)] = ph_after[CI(i, 0)] * coef_bot + pnb[i];
+        ph_after[CI(i, nz)] = ph_after[CI(i, nz - 1)] * coef_top + pnt[i];
+    }
+    if (coef_bot_top) { coef_bot_top[0] = coef_bot; coef_bot_top[1] = coef_top; }
+    free(f1); free(f2); free(rhs); free(x); free(pnb); free(pnt);
+    return info;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Momentum operators: microfluidics_complex_domain/VeloSolve_2_combined.f90:515-711 (bdf 2),
+ * VeloSolve_combined.f90:516-760 (bdf 1), two_phase_flow_complex_domain/VeloSolve_2_combined.f90
+ * (TP: penalty field bdr_ph_penalty, lr_bd_type, identity preconditioner).
+ * ------------------------------------------------------------------------------------- */
+static void uv_unpack_for_matvec(const drd_params* P, const double* x, double* f1, double* f2) {
+    const int nr = P->nr, nz = P->nz;
+    btoa_uv(nr, nz, f1, f2, x);
+    const int tp_neumann = (P->variant == DRD_VARIANT_TP && P->lr_bd_type == 'n');
+    if (!tp_neumann) {
+        for (int k = 0; k < nz; ++k) { /* :536-539 */
+            f1[UI(-1, k)] = -f1[UI(1, k)];
+            f1[UI(nr + 1, k)] = -f1[UI(nr - 1, k)];
+        }
+    } else {
+        for (int k = -1; k <= nz; ++k) {
+            f1[UI(-1, k)] = f1[UI(1, k)];
+            f1[UI(nr + 1, k)] = f1[UI(nr - 1, k)];
+        }
+    }
+    for (int k = 0; k <= nz; ++k) { /* :540-543 */
+        f2[VI(-1, k)] = f2[VI(0, k)];
+        f2[VI(nr, k)] = f2[VI(nr - 1, k)];
+    }
+    for (int i = -1; i <= nr + 1; ++i) { /* :545-548 */
+        f1[UI(i, -1)] = -f1[UI(i, 0)];
+        f1[UI(i, nz)] = -f1[UI(i, nz - 1)];
+    }
+    for (int i = -1; i <= nr; ++i) { /* :550-553 */
+        f2[VI(i, 0)] = 0.0;
+        f2[VI(i, nz)] = 0.0;
+    }
+}
+
+void orc_uv_matvec(const drd_params* P, int bdf, const double* rho, const double* eta,
+                   const double* bdr_pen, double alpha, const double* x, double beta, double* y) {
+    const int nr = P->nr, nz = P->nz;
+    const double dr = P->dr, dz = P->dz, dt = P->dt, re = P->re, pk = P->penalty_k;
+    const double dr2 = dr * dr, dz2 = dz * dz;
+    double* f1 = dalloc(u_size(nr, nz));
+    double* f2 = dalloc(v_size(nr, nz));
+    double* f11 = dalloc(u_size(nr, nz));
+    double* f22 = dalloc(v_size(nr, nz));
+    const long N = uv_len(nr, nz);
+    double* zz = dalloc(N);
+    uv_unpack_for_matvec(P, x, f1, f2);
+    for (int k = 0; k < nz; ++k) /* u: :577-584 */
+        for (int i = 0; i <= nr; ++i) {
+            if (bdf == 2)
+                f11[UI(i, k)] = f1[UI(i, k)] * 1.5 * re * (rho[CI(i, k)] + rho[CI(i - 1, k)]) / 2.0 +
+                                f1[UI(i, k)] * pk * (bdr_pen[CI(i, k)] + bdr_pen[CI(i - 1, k)]) / 2.0 * dt;
+            else
+                f11[UI(i, k)] = f1[UI(i, k)] * re * (rho[CI(i, k)] + rho[CI(i - 1, k)]) / 2.0;
+        }
+    for (int k = 0; k < nz; ++k) /* :587-594 */
+        for (int i = 0; i <= nr; ++i) {
+            double cr = eta[CI(i, k)], cl = eta[CI(i - 1, k)];
+            f11[UI(i, k)] = f11[UI(i, k)] -
+                            2.0 * dt * (cr * f1[UI(i + 1, k)] + cl * f1[UI(i - 1, k)] - (cl + cr) * f1[UI(i, k)]) / dr2;
+        }
+    for (int k = 0; k < nz; ++k) /* :597-607 */
+        for (int i = 0; i <= nr; ++i) {
+            double cr = (eta[CI(i, k + 1)] + eta[CI(i - 1, k + 1)] + eta[CI(i, k)] + eta[CI(i - 1, k)]) / 4.0;
+            double cl = (eta[CI(i, k)] + eta[CI(i - 1, k)] + eta[CI(i, k - 1)] + eta[CI(i - 1, k - 1)]) / 4.0;
+            f11[UI(i, k)] = f11[UI(i, k)] - dt * (cr * f1[UI(i, k + 1)] + cl * f1[UI(i, k - 1)] - (cl + cr) * f1[UI(i, k)]) / dz2;
+            f11[UI(i, k)] = f11[UI(i, k)] -
+                            dt * (cr * (f2[VI(i, k + 1)] - f2[VI(i - 1, k + 1)]) - cl * (f2[VI(i, k)] - f2[VI(i - 1, k)])) / dr / dz;
+        }
+    for (int k = 1; k < nz; ++k) /* v: :610-617 */
+        for (int i = 0; i < nr; ++i) {
+            if (bdf == 2)
+                f22[VI(i, k)] = f2[VI(i, k)] * 1.5 * re * (rho[CI(i, k)] + rho[CI(i, k - 1)]) / 2.0 +
+                                f2[VI(i, k)] * pk * (bdr_pen[CI(i, k)] + bdr_pen[CI(i, k - 1)]) / 2.0 * dt;
+            else
+                f22[VI(i, k)] = f2[VI(i, k)] * re * (rho[CI(i, k)] + rho[CI(i, k - 1)]) / 2.0;
+        }
+    for (int k = 1; k < nz; ++k) /* :620-627 */
+        for (int i = 0; i < nr; ++i) {
+            double cr = eta[CI(i, k)], cl = eta[CI(i, k - 1)];
+            f22[VI(i, k)] = f22[VI(i, k)] -
+                            2.0 * dt * (cr * f2[VI(i, k + 1)] + cl * f2[VI(i, k - 1)] - (cl + cr) * f2[VI(i, k)]) / dz2;
+        }
+    for (int k = 1; k < nz; ++k) /* :630-640 */
+        for (int i = 0; i < nr; ++i) {
+            double cr = (eta[CI(i + 1, k)] + eta[CI(i, k)] + eta[CI(i + 1, k - 1)] + eta[CI(i, k - 1)]) / 4.0;
+            double cl = (eta[CI(i, k)] + eta[CI(i - 1, k)] + eta[CI(i, k - 1)] + eta[CI(i - 1, k - 1)]) / 4.0;
+            f22[VI(i, k)] = f22[VI(i, k)] - dt * (cr * f2[VI(i + 1, k)] + cl * f2[VI(i - 1, k)] - (cl + cr) * f2[VI(i, k)]) / dr2;
+            f22[VI(i, k)] = f22[VI(i, k)] -
+                            dt * (cr * (f1[UI(i + 1, k)] - f1[UI(i + 1, k - 1)]) - cl * (f1[UI(i, k)] - f1[UI(i, k - 1)])) / dr / dz;
+        }
+    atob_uv(nr, nz, f11, f22, zz); /* :644-645 */
+    for (long q = 0; q < N; ++q) y[q] = (beta == 0.0) ? alpha * zz[q] : alpha * zz[q] + beta * y[q];
+    free(f1); free(f2); free(f11); free(f22); free(zz);
+}
+
+/* Jacobi of PSolve_uv_2_CG (:649-711) / PSolve_uv_CG; identity for TP (TP :779-780). */
+void orc_uv_psolve(const drd_params* P, int bdf, const double* rho, const double* eta,
+                   const double* x, double* y) {
+    const int nr = P->nr, nz = P->nz;
+    const double dt = P->dt, re = P->re, dr2 = P->dr * P->dr, dz2 = P->dz * P->dz;
+    const long N = uv_len(nr, nz), mn = (long)(nr + 1) * nz;
+    if (P->variant == DRD_VARIANT_TP && bdf == 2) { /* the first-step TP solve keeps Jacobi */
+        memcpy(y, x, sizeof(double) * N);
+        return;
+    }
+    const double m = (bdf == 2) ? 1.5 * re : re;
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i <= nr; ++i) {
+            double tmp = m * (rho[CI(i, j)] + rho[CI(i - 1, j)]) / 2.0;
+            double cr = eta[CI(i, j)], cl = eta[CI(i - 1, j)];
+            tmp = tmp + 2.0 * dt * (cl + cr) / dr2;
+            cr = (eta[CI(i, j + 1)] + eta[CI(i - 1, j + 1)] + eta[CI(i, j)] + eta[CI(i - 1, j)]) / 4.0;
+            cl = (eta[CI(i, j)] + eta[CI(i - 1, j)] + eta[CI(i, j - 1)] + eta[CI(i - 1, j - 1)]) / 4.0;
+            if (j == 0) tmp = tmp + dt * (cl + (cl + cr)) / dz2;
+            else if (j == nz - 1) tmp = tmp + dt * (cr + (cl + cr)) / dz2;
+            else tmp = tmp + dt * (cl + cr) / dz2;
+            long q = i + (long)(nr + 1) * j;
+            y[q] = x[q] / tmp;
+        }
+    for (int j = 1; j < nz; ++j)
+        for (int i = 0; i < nr; ++i) {
+            double tmp = m * (rho[CI(i, j)] + rho[CI(i - 1, j)]) / 2.0; /* rho(i-1,j) as written (:690) */
+            double cr = eta[CI(i, j)], cl = eta[CI(i, j - 1)];
+            tmp = tmp + 2.0 * dt * (cl + cr) / dz2;
+            cr = (eta[CI(i + 1, j)] + eta[CI(i, j)] + eta[CI(i + 1, j - 1)] + eta[CI(i, j - 1)]) / 4.0;
+            cl = (eta[CI(i, j)] + eta[CI(i - 1, j)] + eta[CI(i, j - 1)] + eta[CI(i - 1, j - 1)]) / 4.0;
+            if (i == 0) tmp = tmp + dt * cr / dr2;
+            else if (i == nr - 1) tmp = tmp + dt * cl / dr2;
+            else tmp = tmp + dt * (cl + cr) / dr2;
+            long q = i + (long)nr * (j - 1) + mn;
+            y[q] = x[q] / tmp;
+        }
+}
+
+typedef struct {
+    const drd_params* P; int bdf; const double* rho; const double* eta; const double* pen;
+} uv_ctx;
+static void uv_mv_cb(void* c, double a, const double* x, double b, double* y) {
+    uv_ctx* C = (uv_ctx*)c;
+    orc_uv_matvec(C->P, C->bdf, C->rho, C->eta, C->pen, a, x, b, y);
+}
+static void uv_ps_cb(void* c, const double* x, double* y) {
+    uv_ctx* C = (uv_ctx*)c;
+    orc_uv_psolve(C->P, C->bdf, C->rho, C->eta, x, y);
+}
+
+/* VeloSolve_combined (bdf 1) / VeloSolve_2_combined (bdf 2). */
+int orc_velosolve(const drd_params* P, int bdf, const double* psi1, const double* psi2,
+                  const double* u_pre, const double* u, const double* v_pre, const double* v,
+                  const double* p, const double* rho, const double* eta, const double* bdr_ph,
+                  const double* bdr_pen, const double* bdr_used, const double* ph_after,
+                  const double* rmu_after, double t, const double* pf1, const double* pf2,
+                  double* u_after, double* v_after, double* uL, double* uR, drd_status* st) {
+    const int nr = P->nr, nz = P->nz;
+    const double dr = P->dr, dz = P->dz, dt = P->dt, re = P->re, ca = P->ca;
+    const double dr2 = dr * dr, dz2 = dz * dz;
+    const int tp = (P->variant == DRD_VARIANT_TP);
+    const int dirichlet = !tp || P->lr_bd_type != 'n';
+    if (P->xlsB >= 1.E-8) return DRD_ERR_UNSUPPORTED; /* the slip branch is commented out (:299-369) */
+    const long us = u_size(nr, nz), vs = v_size(nr, nz), cs = cell_size(nr, nz), N = uv_len(nr, nz);
+    double* fu = dalloc(us);
+    double* fv = dalloc(vs);
+    double* ut = dalloc(us);
+    double* vt = dalloc(vs);
+    double* tp_ = dalloc(cs);
+    double* rhs = dalloc(N);
+    double* x = dalloc(N);
+    /* surface tension ca*mu*grad(phi) (:62-86; TP :64-90) */
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i <= nr; ++i) {
+            if (!tp)
+                fu[UI(i, k)] = ca * (rmu_after[CI(i, k)] + rmu_after[CI(i - 1, k)]) / 2.0 *
+                               (ph_after[CI(i, k)] - ph_after[CI(i - 1, k)]) / dr *
+                               (1.0 - (bdr_ph[CI(i, k)] + bdr_ph[CI(i - 1, k)]) / 2.0);
+            else
+                fu[UI(i, k)] = ca * (rmu_after[CI(i, k)] + rmu_after[CI(i - 1, k)]) / 2.0 *
+                               (ph_after[CI(i, k)] * bdr_used[CI(i, k)] - ph_after[CI(i - 1, k)] * bdr_used[CI(i - 1, k)]) / dr;
+        }
+    for (int k = 1; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) {
+            if (!tp)
+                fv[VI(i, k)] = ca * (rmu_after[CI(i, k)] + rmu_after[CI(i, k - 1)]) / 2.0 *
+                               (ph_after[CI(i, k)] - ph_after[CI(i, k - 1)]) / dz *
+                               (1.0 - (bdr_ph[CI(i, k)] + bdr_ph[CI(i, k - 1)]) / 2.0);
+            else
+                fv[VI(i, k)] = ca * (rmu_after[CI(i, k)] + rmu_after[CI(i, k - 1)]) / 2.0 *
+                               (ph_after[CI(i, k)] * bdr_used[CI(i, k)] - ph_after[CI(i, k - 1)] * bdr_used[CI(i, k - 1)]) / dz;
+        }
+    /* advection with u~ = 2u - u_pre (bdf 2, :98-113) or u (bdf 1) */
+    for (long q = 0; q < us; ++q) ut[q] = (bdf == 2) ? 2.0 * u[q] - u_pre[q] : u[q];
+    for (long q = 0; q < vs; ++q) vt[q] = (bdf == 2) ? 2.0 * v[q] - v_pre[q] : v[q];
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i <= nr; ++i)
+            fu[UI(i, k)] = fu[UI(i, k)] -
+                           re * (rho[CI(i, k)] + rho[CI(i - 1, k)]) / 2.0 *
+                               (ut[UI(i, k)] * (ut[UI(i + 1, k)] - ut[UI(i - 1, k)]) / 2.0 / dr +
+                                (vt[VI(i, k)] + vt[VI(i - 1, k)] + vt[VI(i, k + 1)] + vt[VI(i - 1, k + 1)]) / 4.0 *
+                                    (ut[UI(i, k + 1)] - ut[UI(i, k - 1)]) / 2.0 / dz);
+    for (int k = 1; k < nz; ++k)
+        for (int i = 0; i < nr; ++i)
+            fv[VI(i, k)] = fv[VI(i, k)] -
+                           re * (rho[CI(i, k)] + rho[CI(i, k - 1)]) / 2.0 *
+                               ((ut[UI(i, k)] + ut[UI(i + 1, k)] + ut[UI(i, k - 1)] + ut[UI(i + 1, k - 1)]) / 4.0 *
+                                    (vt[VI(i + 1, k)] - vt[VI(i - 1, k)]) / 2.0 / dr +
+                                vt[VI(i, k)] * (vt[VI(i, k + 1)] - vt[VI(i, k - 1)]) / 2.0 / dz);
+    /* pressure gradient, mass and body force (:187-210) */
+    for (long q = 0; q < cs; ++q) tp_[q] = (bdf == 2) ? p[q] + 4 * psi2[q] / 3.0 - psi1[q] / 3.0 : p[q];
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i <= nr; ++i) {
+            double g = (tp && bdf == 2) ? (ph_after[CI(i, k)] + ph_after[CI(i - 1, k)]) / 2.0 * P->ggx : P->ggx;
+            double mass = (bdf == 2) ? 2.0 * u[UI(i, k)] * re / dt - u_pre[UI(i, k)] * re / 2.0 / dt + g
+                                     : u[UI(i, k)] * re / dt + g;
+            fu[UI(i, k)] = fu[UI(i, k)] - (tp_[CI(i, k)] - tp_[CI(i - 1, k)]) / dr +
+                           (rho[CI(i, k)] + rho[CI(i - 1, k)]) / 2.0 * mass;
+        }
+    for (int k = 1; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) {
+            /* TP weights ggz with (ph(i,k)+ph(i-1,k))/2 as written (TP :219) */
+            double g = (tp && bdf == 2) ? (ph_after[CI(i, k)] + ph_after[CI(i - 1, k)]) / 2.0 * P->ggz : P->ggz;
+            double mass = (bdf == 2) ? 2.0 * v[VI(i, k)] * re / dt - v_pre[VI(i, k)] * re / 2.0 / dt + g
+                                     : v[VI(i, k)] * re / dt + g;
+            fv[VI(i, k)] = fv[VI(i, k)] - (tp_[CI(i, k)] - tp_[CI(i, k - 1)]) / dz +
+                           (rho[CI(i, k)] + rho[CI(i, k - 1)]) / 2.0 * mass;
+        }
+    /* particle force (:229-239) and the dt scaling (:242-252) */
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i <= nr; ++i) fu[UI(i, k)] = fu[UI(i, k)] + (pf1[CI(i, k)] + pf1[CI(i - 1, k)]) / 2.0;
+    for (int k = 1; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) fv[VI(i, k)] = fv[VI(i, k)] + (pf2[CI(i, k)] + pf2[CI(i, k - 1)]) / 2.0;
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i <= nr; ++i) fu[UI(i, k)] = fu[UI(i, k)] * dt;
+    for (int k = 1; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) fv[VI(i, k)] = fv[VI(i, k)] * dt;
+    /* inlet / outlet Dirichlet profiles (:262-295) */
+    double* uLl = dalloc(nz + 1);
+    double* uRl = dalloc(nz + 1);
+    if (dirichlet) {
+        double cf = 1.0 - exp(-t / P->twall);
+        double hig = P->bdr_upp - P->bdr_low;
+        for (int k = 0; k < nz; ++k) {
+            double z = (k + 0.5) * dz;
+            if (z > P->bdr_low && z < P->bdr_upp) {
+                double d = z - P->bdr_low - hig / 2;
+                uLl[k] = P->UU * (-(d * d) / hig / hig * 4 + 1) * cf;
+            } else {
+                uLl[k] = 0.0;
+            }
+            fu[UI(0, k)] = fu[UI(0, k)] + 2.0 * uLl[k] * eta[CI(0, k)] * 2.0 * dt / dr2;
+        }
+        for (int k = 0; k < nz; ++k) {
+            uRl[k] = uLl[k];
+            fu[UI(nr, k)] = fu[UI(nr, k)] + 2.0 * uRl[k] * eta[CI(nr, k)] * 2.0 * dt / dr2;
+        }
+    }
+    /* no-slip wall terms (:377-385) */
+    for (int i = 0; i <= nr; ++i) {
+        int k = 0;
+        double etay = (eta[CI(i, k)] + eta[CI(i - 1, k)] + eta[CI(i, k - 1)] + eta[CI(i - 1, k - 1)]) / 4.0;
+        fu[UI(i, k)] = fu[UI(i, k)] + dt * (2.0 * P->uwB / dz2 * etay);
+        k = nz - 1;
+        etay = (eta[CI(i, k + 1)] + eta[CI(i - 1, k + 1)] + eta[CI(i, k)] + eta[CI(i - 1, k)]) / 4.0;
+        fu[UI(i, k)] = fu[UI(i, k)] + dt * (2.0 * P->uwT / dz2 * etay);
+    }
+    atob_uv(nr, nz, fu, fv, rhs); /* :388-389 */
+    atob_uv(nr, nz, u, v, x);
+    uv_ctx C = {P, bdf, rho, eta, bdr_pen};
+    int info = orc_bicgstab(N, rhs, x, P->uv_maxit, P->tol, uv_mv_cb, uv_ps_cb, &C, st); /* :398-401 */
+    btoa_uv(nr, nz, u_after, v_after, x); /* :411 */
+    if (dirichlet) {
+        for (int k = 0; k < nz; ++k) u_after[UI(-1, k)] = 2.0 * uLl[k] - u_after[UI(1, k)];
+        for (int k = 0; k < nz; ++k) u_after[UI(nr + 1, k)] = 2.0 * uRl[k] - u_after[UI(nr - 1, k)];
+    } else {
+        for (int k = 0; k <= nz; ++k) { /* TP :437-440 */
+            u_after[UI(-1, k)] = u_after[UI(1, k)];
+            u_after[UI(nr + 1, k)] = u_after[UI(nr - 1, k)];
+        }
+    }
+    for (int i = -1; i <= nr + 1; ++i) {
+        u_after[UI(i, -1)] = P->uwB * 2.0 - u_after[UI(i, 0)];
+        u_after[UI(i, nz)] = P->uwT * 2.0 - u_after[UI(i, nz - 1)];
+    }
+    for (int i = -1; i <= nr; ++i) {
+        v_after[VI(i, 0)] = 0.0;
+        v_after[VI(i, nz)] = 0.0;
+    }
+    for (int k = 1; k < nz; ++k) {
+        v_after[VI(-1, k)] = v_after[VI(0, k)];
+        v_after[VI(nr, k)] = v_after[VI(nr - 1, k)];
+    }
+    if (dirichlet) {
+        if (uL) memcpy(uL, uLl, sizeof(double) * nz);
+        if (uR) memcpy(uR, uRl, sizeof(double) * nz);
+    }
+    free(fu); free(fv); free(ut); free(vt); free(tp_); free(rhs); free(x); free(uLl); free(uRl);
+    return info;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * PreSolve_2 + dct_fftw: microfluidics_complex_domain/PreSolve_2.f90:1-130,135-186.
+ * ------------------------------------------------------------------------------------- */
+void orc_presolve(const drd_params* P, const double* pre_lcc, const double* u, const double* v,
+                  double coef, double* psi) {
+    const int nr = P->nr, nz = P->nz;
+    const long n = (long)nr * nz, cs = cell_size(nr, nz);
+    double* w = dalloc(n);
+    for (int k = 0; k < nz; ++k) /* :16-21 */
+        for (int i = 0; i < nr; ++i)
+            w[i + (long)nr * k] = (u[UI(i + 1, k)] - u[UI(i, k)]) / P->dr + (v[VI(i, k + 1)] - v[VI(i, k)]) / P->dz;
+    orc_redft10(nr, nz, w, nr, 1); /* dfftw_execute_r2r(plan): REDFT10 in both dimensions */
+    orc_redft10(nz, nr, w, 1, nr);
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) w[i + (long)nr * k] = w[i + (long)nr * k] / pre_lcc[i + (long)(nr + 1) * k];
+    orc_redft01(nr, nz, w, nr, 1); /* plan_back: REDFT01 in both dimensions */
+    orc_redft01(nz, nr, w, 1, nr);
+    const double scale = 4.0 * nr * nz; /* :47 */
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) psi[CI(i, k)] = w[i + (long)nr * k] / scale;
+    for (int k = 0; k < nz; ++k) { /* :175-183 */
+        psi[CI(-1, k)] = psi[CI(0, k)];
+        psi[CI(nr, k)] = psi[CI(nr - 1, k)];
+    }
+    for (int i = -1; i <= nr; ++i) {
+        psi[CI(i, -1)] = psi[CI(i, 0)];
+        psi[CI(i, nz)] = psi[CI(i, nz - 1)];
+    }
+    for (long q = 0; q < cs; ++q) psi[q] = psi[q] * coef; /* :125 */
+    free(w);
+}
+
+/* interpolate_coef: microfluidics_complex_domain/interpolate_coef.f90:55-89. */
+void orc_interpolate_coef(const drd_params* P, const double* dist, const double* bdr_ph,
+                          double* fpd_ph, double* rho, double* eta) {
+    const int nr = P->nr, nz = P->nz;
+    const long cs = cell_size(nr, nz);
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nr; ++i)
+            fpd_ph[CI(i, k)] = tanh(-1.0 * dist[i + (long)nr * k] / sqrt(2.0) / P->I_thickness);
+    for (long q = 0; q < cs; ++q) fpd_ph[q] = (fpd_ph[q] + 1.0) / 2.0;
+    for (long q = 0; q < cs; ++q) fpd_ph[q] = fpd_ph[q] + bdr_ph[q];
+    for (int k = 0; k < nz; ++k) {
+        fpd_ph[CI(-1, k)] = fpd_ph[CI(0, k)];
+        fpd_ph[CI(nr, k)] = fpd_ph[CI(nr - 1, k)];
+    }
+    for (int i = -1; i <= nr; ++i) {
+        fpd_ph[CI(i, -1)] = fpd_ph[CI(i, 0)];
+        fpd_ph[CI(i, nz)] = fpd_ph[CI(i, nz - 1)];
+    }
+    for (long q = 0; q < cs; ++q) {
+        rho[q] = 1.0 + (P->lambda_rho - 1.0) * fpd_ph[q];
+        eta[q] = 1.0 + (P->lambda_eta - 1.0) * fpd_ph[q];
+    }
+}
+
+/* Mass sum of dissipation(): microfluidics_complex_domain/dissipation.f90:116-122. */
+double orc_mass(const drd_params* P, const double* ph) {
+    const int nr = P->nr, nz = P->nz;
+    double e4 = 0.0;
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) e4 = e4 + ph[CI(i, k)];
+    return e4 * P->dr * P->dz;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * The mcl6 step: microfluidics_complex_domain/mcl6.f90:239-306 (first) and :378-486 (loop).
+ * ------------------------------------------------------------------------------------- */
+int orc_step(const drd_params* P, const double* ph_lcc, const double* pre_lcc, orc_state* S,
+             int first, double t, drd_status* st2) {
+    const int nr = P->nr, nz = P->nz;
+    const long cs = cell_size(nr, nz), us = u_size(nr, nz), vs = v_size(nr, nz);
+    double** f = S->f;
+    double* rmu_after = dalloc(cs);
+    double* ph_after = dalloc(cs);
+    double* u_after = dalloc(us);
+    double* v_after = dalloc(vs);
+    drd_status st[2];
+    memset(st, 0, sizeof(st));
+    const double gamma1 = fmin(1.0, P->lambda_rho);
+    int rc = 0;
+    if (P->variant == DRD_VARIANT_TP) {
+        /* TP step: the angle arrays are uniform (TP/finit.f90:581) */
+        double* ang = dalloc(nr + 1);
+        for (int i = 0; i <= nr; ++i) ang[i] = P->angle;
+        rc = orc_ph_mu_solve(P, f[DRD_F_U], f[DRD_F_V], f[DRD_F_PH], f[DRD_F_RMU], S->bdr_ph, S->bdr_used,
+                             S->bdr_ph_grad, S->Mi, ang, ang, S->M0, ph_after, rmu_after, NULL, &st[0]);
+        free(ang);
+    } else {
+        rc = orc_phsolve(P, ph_lcc, f[DRD_F_U], f[DRD_F_V], f[DRD_F_PH], f[DRD_F_RMU], S->bdr_ph, S->bdr_ph_grad,
+                         S->M0, S->Mi, rmu_after, ph_after, &st[0]);
+    }
+    (void)rc;
+    orc_velosolve(P, first ? 1 : 2, f[DRD_F_PSI1], f[DRD_F_PSI2], f[DRD_F_U_PRE], f[DRD_F_U], f[DRD_F_V_PRE],
+                  f[DRD_F_V], f[DRD_F_P], S->rho, S->eta, S->bdr_ph, S->bdr_pen, S->bdr_used, ph_after,
+                  rmu_after, t + P->dt, f[DRD_F_PF1], f[DRD_F_PF2], u_after, v_after, NULL, NULL, &st[1]);
+    memcpy(f[DRD_F_U_PRE], f[DRD_F_U], sizeof(double) * us);
+    memcpy(f[DRD_F_V_PRE], f[DRD_F_V], sizeof(double) * vs);
+    memcpy(f[DRD_F_U], u_after, sizeof(double) * us);
+    memcpy(f[DRD_F_V], v_after, sizeof(double) * vs);
+    memcpy(f[DRD_F_PH_PRE], f[DRD_F_PH], sizeof(double) * cs);
+    memcpy(f[DRD_F_RMU_PRE], f[DRD_F_RMU], sizeof(double) * cs);
+    memcpy(f[DRD_F_PH], ph_after, sizeof(double) * cs);
+    memcpy(f[DRD_F_RMU], rmu_after, sizeof(double) * cs);
+    double coef;
+    if (first) {
+        coef = P->re * gamma1 / P->dt;
+    } else {
+        memcpy(f[DRD_F_PSI1], f[DRD_F_PSI2], sizeof(double) * cs);
+        coef = 3 * P->re * gamma1 / 2. / P->dt;
+    }
+    orc_presolve(P, pre_lcc, f[DRD_F_U], f[DRD_F_V], coef, f[DRD_F_PSI2]);
+    for (long q = 0; q < cs; ++q) f[DRD_F_P][q] = f[DRD_F_PSI2][q] + f[DRD_F_P][q];
+    if (st2) { st2[0] = st[0]; st2[1] = st[1]; }
+    free(rmu_after); free(ph_after); free(u_after); free(v_after);
+    return 0;
+}

@@ -1,0 +1,209 @@
+"""ctypes binding of the FP64 CPU oracle (oracle/drd_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline legs as the checker.  The product library never loads it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from drd_application_gb300 import abi
+from drd_application_gb300.layout import ptr
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "build")
+LIB = os.path.join(BUILD, "liboracle.so")
+LIB_OMP = os.path.join(BUILD, "liboracle_omp.so")
+SRC = os.path.join(HERE, "drd_oracle.c")
+HDR = os.path.join(HERE, "drd_oracle.h")
+
+
+def build(force=False):
+    """Compile the oracle with gcc: a serial library (the checker and the single-thread CPU
+    baseline, like the reference's serial build) and an OpenMP one for all-core timing."""
+    os.makedirs(BUILD, exist_ok=True)
+    deps = [SRC, HDR, os.path.join(HERE, "..", "include", "drd_gb300.h")]
+    newest = max(os.path.getmtime(d) for d in deps)
+    for out, extra in ((LIB, []), (LIB_OMP, ["-fopenmp", "-DORC_OPENMP"])):
+        if force or not os.path.exists(out) or os.path.getmtime(out) < newest:
+            cmd = ["gcc", "-O3", "-std=c11", "-fPIC", "-shared", *extra, "-o", out + ".tmp", SRC, "-lm"]
+            subprocess.run(cmd, check=True)
+            os.replace(out + ".tmp", out)
+    return LIB
+
+
+_libs = {}
+
+
+def lib(openmp=False):
+    path = LIB_OMP if openmp else LIB
+    if path not in _libs:
+        build()
+        L = C.CDLL(path)
+        dp = C.POINTER(C.c_double)
+        P = C.POINTER(abi.drd_params)
+        S = C.POINTER(abi.drd_status)
+        L.orc_setup_tables.argtypes = [P, dp, dp]
+        for f in ("orc_vcost", "orc_redft10", "orc_redft01"):
+            getattr(L, f).argtypes = [C.c_int, C.c_int, dp, C.c_long, C.c_long]
+        L.orc_op_double_gradient_neum.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, dp, dp, dp]
+        L.orc_ch_matvec.argtypes = [P, dp, dp, C.c_double, dp, C.c_double, dp]
+        L.orc_ch_psolve.argtypes = [P, dp, dp, dp]
+        L.orc_uv_matvec.argtypes = [P, C.c_int, dp, dp, dp, C.c_double, dp, C.c_double, dp]
+        L.orc_uv_psolve.argtypes = [P, C.c_int, dp, dp, dp, dp]
+        L.orc_phmu_matvec.argtypes = [P, dp, dp, dp, C.c_double, C.c_double, C.c_double, dp, C.c_double, dp]
+        L.orc_phmu_psolve.argtypes = [P, dp, dp]
+        L.orc_phsolve.argtypes = [P, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, S]
+        L.orc_phsolve.restype = C.c_int
+        L.orc_ph_mu_solve.argtypes = [P, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, S]
+        L.orc_ph_mu_solve.restype = C.c_int
+        L.orc_velosolve.argtypes = [P, C.c_int] + [dp] * 14 + [C.c_double, dp, dp, dp, dp, dp, dp, S]
+        L.orc_velosolve.restype = C.c_int
+        L.orc_presolve.argtypes = [P, dp, dp, dp, C.c_double, dp]
+        L.orc_interpolate_coef.argtypes = [P, dp, dp, dp, dp, dp]
+        L.orc_mass.argtypes = [P, dp]
+        L.orc_mass.restype = C.c_double
+        _libs[path] = L
+    return _libs[path]
+
+
+class OrcState(C.Structure):
+    _fields_ = [("f", C.POINTER(C.c_double) * abi.F_COUNT)] + [
+        (n, C.POINTER(C.c_double)) for n in ("rho", "eta", "bdr_ph", "bdr_ph_grad", "M0", "Mi", "bdr_pen", "bdr_used")
+    ]
+
+
+class Oracle:
+    """FP64 CPU restatement bound to one drd_params."""
+
+    def __init__(self, params, openmp=False):
+        self.P = params.copy()
+        self.L = lib(openmp)
+        nr, nz = self.P.nr, self.P.nz
+        self.ph_lcc = np.zeros(nr * nz)
+        self.pre_lcc = np.zeros((nr + 1) * (nz + 1))
+        self.L.orc_setup_tables(C.byref(self.P), ptr(self.ph_lcc), ptr(self.pre_lcc))
+        self.L.orc_step.argtypes = [C.POINTER(abi.drd_params), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                    C.POINTER(OrcState), C.c_int, C.c_double, C.POINTER(abi.drd_status)]
+
+    # -- transforms on arrays of sequences --------------------------------------------------
+    def vcost(self, x, axis=-1):
+        return self._transform(self.L.orc_vcost, x, axis)
+
+    def redft10(self, x, axis=-1):
+        return self._transform(self.L.orc_redft10, x, axis)
+
+    def redft01(self, x, axis=-1):
+        return self._transform(self.L.orc_redft01, x, axis)
+
+    @staticmethod
+    def _transform(fn, x, axis):
+        y = np.ascontiguousarray(np.moveaxis(np.array(x, dtype=np.float64), axis, -1))
+        n = y.shape[-1]
+        m = y.size // n
+        fn(n, m, ptr(y), n, 1)
+        return np.moveaxis(y, -1, axis)
+
+    # -- operators ---------------------------------------------------------------------------
+    def op_double_gradient_neum(self, x, mo):
+        out = np.zeros_like(x)
+        self.L.orc_op_double_gradient_neum(self.P.nr, self.P.nz, self.P.dr ** 2, self.P.dz ** 2,
+                                           ptr(np.ascontiguousarray(x)), ptr(np.ascontiguousarray(mo)), ptr(out))
+        return out
+
+    def ch_matvec(self, M0, Mi, x, alpha=1.0, beta=0.0, y=None):
+        y = np.zeros_like(x) if y is None else np.array(y, dtype=np.float64)
+        self.L.orc_ch_matvec(C.byref(self.P), ptr(M0), ptr(Mi), alpha, ptr(np.ascontiguousarray(x)), beta, ptr(y))
+        return y
+
+    def ch_psolve(self, x):
+        y = np.zeros_like(x)
+        self.L.orc_ch_psolve(C.byref(self.P), ptr(self.ph_lcc), ptr(np.ascontiguousarray(x)), ptr(y))
+        return y
+
+    def uv_matvec(self, bdf, rho, eta, pen, x, alpha=1.0, beta=0.0, y=None):
+        y = np.zeros_like(x) if y is None else np.array(y, dtype=np.float64)
+        self.L.orc_uv_matvec(C.byref(self.P), bdf, ptr(rho), ptr(eta), ptr(pen), alpha,
+                             ptr(np.ascontiguousarray(x)), beta, ptr(y))
+        return y
+
+    def uv_psolve(self, bdf, rho, eta, x):
+        y = np.zeros_like(x)
+        self.L.orc_uv_psolve(C.byref(self.P), bdf, ptr(rho), ptr(eta), ptr(np.ascontiguousarray(x)), ptr(y))
+        return y
+
+    def phmu_matvec(self, M0, Mi, used, x, coef_bot=1.0, coef_top=1.0, alpha=1.0, beta=0.0, y=None):
+        y = np.zeros_like(x) if y is None else np.array(y, dtype=np.float64)
+        self.L.orc_phmu_matvec(C.byref(self.P), ptr(M0), ptr(Mi), ptr(used), coef_bot, coef_top, alpha,
+                               ptr(np.ascontiguousarray(x)), beta, ptr(y))
+        return y
+
+    def phmu_psolve(self, x):
+        y = np.zeros_like(x)
+        self.L.orc_phmu_psolve(C.byref(self.P), ptr(np.ascontiguousarray(x)), ptr(y))
+        return y
+
+    # -- per-step routines -------------------------------------------------------------------
+    def phsolve(self, u, v, ph, rmu, bdr_ph, bdr_ph_grad, M0, Mi):
+        rmu_after = np.zeros_like(ph)
+        ph_after = np.zeros_like(ph)
+        st = abi.drd_status()
+        self.L.orc_phsolve(C.byref(self.P), ptr(self.ph_lcc), ptr(u), ptr(v), ptr(ph), ptr(rmu), ptr(bdr_ph),
+                           ptr(bdr_ph_grad), ptr(M0), ptr(Mi), ptr(rmu_after), ptr(ph_after), C.byref(st))
+        return rmu_after, ph_after, st
+
+    def ph_mu_solve(self, u, v, ph, rmu, bdr_ph, bdr_used, bdr_grad, Mi, angleB, angleT):
+        M0 = np.zeros_like(ph)
+        ph_after = np.zeros_like(ph)
+        rmu_after = np.zeros_like(ph)
+        cbt = np.zeros(2)
+        st = abi.drd_status()
+        self.L.orc_ph_mu_solve(C.byref(self.P), ptr(u), ptr(v), ptr(ph), ptr(rmu), ptr(bdr_ph), ptr(bdr_used),
+                               ptr(bdr_grad), ptr(Mi), ptr(angleB), ptr(angleT), ptr(M0), ptr(ph_after),
+                               ptr(rmu_after), ptr(cbt), C.byref(st))
+        return ph_after, rmu_after, M0, cbt, st
+
+    def velosolve(self, bdf, psi1, psi2, u_pre, u, v_pre, v, p, rho, eta, bdr_ph, bdr_pen, bdr_used,
+                  ph_after, rmu_after, t, pf1, pf2):
+        u_after = np.zeros_like(u)
+        v_after = np.zeros_like(v)
+        nz = self.P.nz
+        uL = np.zeros(nz + 1)
+        uR = np.zeros(nz + 1)
+        st = abi.drd_status()
+        rc = self.L.orc_velosolve(C.byref(self.P), bdf, ptr(psi1), ptr(psi2), ptr(u_pre), ptr(u), ptr(v_pre),
+                                  ptr(v), ptr(p), ptr(rho), ptr(eta), ptr(bdr_ph), ptr(bdr_pen), ptr(bdr_used),
+                                  ptr(ph_after), ptr(rmu_after), t, ptr(pf1), ptr(pf2), ptr(u_after),
+                                  ptr(v_after), ptr(uL), ptr(uR), C.byref(st))
+        if rc == abi.DRD_ERR_UNSUPPORTED:
+            raise ValueError("slip walls (xlsB >= 1e-8) have no solve in the reference")
+        return u_after, v_after, uL, uR, st
+
+    def presolve(self, u, v, coef):
+        psi = np.zeros(((self.P.nz + 2), (self.P.nr + 2)))
+        self.L.orc_presolve(C.byref(self.P), ptr(self.pre_lcc), ptr(u), ptr(v), coef, ptr(psi))
+        return psi
+
+    def interpolate_coef(self, dist, bdr_ph):
+        fpd = np.zeros_like(bdr_ph)
+        rho = np.zeros_like(bdr_ph)
+        eta = np.zeros_like(bdr_ph)
+        self.L.orc_interpolate_coef(C.byref(self.P), ptr(np.ascontiguousarray(dist)), ptr(bdr_ph), ptr(fpd),
+                                    ptr(rho), ptr(eta))
+        return fpd, rho, eta
+
+    def mass(self, ph):
+        return self.L.orc_mass(C.byref(self.P), ptr(ph))
+
+    def step(self, state, coefs, first, t):
+        """state: dict field-id -> array (updated in place); coefs: dict of coefficient arrays."""
+        S = OrcState()
+        for fid in range(abi.F_COUNT):
+            S.f[fid] = ptr(state[fid])
+        for name in ("rho", "eta", "bdr_ph", "bdr_ph_grad", "M0", "Mi", "bdr_pen", "bdr_used"):
+            setattr(S, name, ptr(coefs[name]))
+        st = (abi.drd_status * 2)()
+        self.L.orc_step(C.byref(self.P), ptr(self.ph_lcc), ptr(self.pre_lcc), C.byref(S), int(first), t, st)
+        return st[0], st[1]
