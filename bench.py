@@ -1,0 +1,405 @@
+"""Benchmark of the GB300 per-time-step solver core.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload: 420x180 complex-domain two-phase flow -- a seeded serpentine channel (sinusoidal
+walls, amplitude 30 and period 140 cells, resistance penalty 1e4, walls smoothed by tanh over
+2 cells), three rigid 40x4-cell fibers at seeded poses, two drops of radius 15 cells,
+viscosity ratio 5, Re 0.5, Ca 0.05.  A step is one pass of the reference's time loop body
+(CH solve -> momentum solve -> pressure solve -> p += psi), every Krylov solve to the deck
+tolerance 1e-8 (relative FP64 residual).  Inputs are synthetic (seeded), as no dataset exists.
+
+value: time-steps/s of the mixed path (FP32 Krylov solves inside FP64 iterative refinement)
+with the state resident in HBM, device-timed with CUDA events per step, L2 flushed between
+steps.  The plain FP64 path is timed the same way and reported beside it.  e2e: the same
+metric through the drop-in C-ABI routines with host arrays (PhSolve, VeloSolve_2_combined,
+PreSolve_2 each step, host<->device copies inside the timed region).
+
+Multi-GPU: the path does not shard a grid; N ranks run N independent replicas (weak scaling)
+and value = steps of all ranks / max elapsed over ranks.
+
+--impl reference times the reference's algorithm on the host cores: the FP64 CPU
+restatement (oracle/, OpenMP over transform lines), since the Fortran reference cannot be
+built without a Fortran compiler, MKL and the prebuilt FFTW.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time-steps/s and solves/s to FP64 resid 1e-8: learned+FP32 vs plain FP64, 1 GB300"
+WORKLOAD = ("420x180 serpentine channel (amp 30, period 140 cells, penalty 1e4), 3 rigid fibers 40x4, "
+            "2 drops R=15, lambda_eta 5, Re 0.5, Ca 0.05; CH + momentum + pressure per step, tol 1e-8")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=None, help="timed steps of the plain FP64 path")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--nr", type=int, default=420)
+    ap.add_argument("--nz", type=int, default=180)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------ distributed
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws, local):
+    if ws <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+
+    dist.init_process_group("nccl", device_id=torch.device("cuda", 0))
+    return dist
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ------------------------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples (clocks and throttle reasons) while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu, self.rows, self.proc = gpu, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[0]) for r in self.rows if r and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for j, nm in enumerate(names):
+                if len(r) > 4 + j and r[4 + j].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------ CPU baseline
+def cpu_baseline(steps, budget_s=40.0, nr=420, nz=180):
+    """The FP64 CPU restatement (OpenMP over transform lines) on the host cores, on a bounded
+    sample of the same workload: the first `steps` steps or as many as fit in budget_s."""
+    from oracle.oracle import Oracle
+    from drd_application_gb300.workloads import make_case
+
+    case = make_case("c2", seed=0, nr=nr, nz=nz)
+    orc = Oracle(case.params, openmp=True)
+    st = case.copy_state()
+    t, done, elapsed = 0.0, 0, 0.0
+    t0 = time.perf_counter()
+    for s in range(steps):
+        orc.step(st, case.coefs, s == 0, t)
+        t += case.params.dt
+        done += 1
+        elapsed = time.perf_counter() - t0
+        if elapsed > budget_s:
+            break
+    cores = os.cpu_count()
+    return {"value": done / elapsed, "unit": "time-steps/s", "cores": cores, "kind": "port",
+            "sample": f"first {done} steps of the same {nr}x{nz} workload, FP64 oracle (oracle/drd_oracle.c, "
+                      f"OpenMP over transform lines, {cores} threads), {elapsed:.1f} s"}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    from oracle import oracle
+
+    oracle.build()
+    w = min(args.warmup, 1)
+    from drd_application_gb300.workloads import make_case
+    from oracle.oracle import Oracle
+
+    case = make_case("c2", seed=0, nr=args.nr, nz=args.nz)
+    orc = Oracle(case.params, openmp=True)
+    st = case.copy_state()
+    t = 0.0
+    for s in range(w):
+        orc.step(st, case.coefs, s == 0, t)
+        t += case.params.dt
+    timed, elapsed = 0, 0.0
+    budget = 150.0
+    for s in range(args.steps):
+        t0 = time.perf_counter()
+        orc.step(st, case.coefs, (w + s) == 0, t)
+        elapsed += time.perf_counter() - t0
+        t += case.params.dt
+        timed += 1
+        if elapsed > budget:
+            break
+    v = timed / elapsed
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "time-steps/s", "n_gpus": args.gpus,
+        "steps": timed, "warmup": w, "ms_per_step": 1e3 * elapsed / timed, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "reference_code": "FP64 CPU restatement of the reference routines "
+                                                            "(Fortran reference not buildable: no Fortran compiler)"},
+        "cpu_baseline": {"value": v, "unit": "time-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{timed} timed steps after {w} warm-up, OpenMP over transform lines, {cores} threads"},
+        "e2e": {"value": v, "unit": "time-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------------- GPU arm
+def time_resident(ctx, case, warmup, steps, flush_bytes):
+    """Per-step device time (CUDA events inside drd_step) with the state resident in HBM."""
+    from drd_application_gb300 import abi
+
+    ctx.upload_state(case.state)
+    dt = case.params.dt
+    t = 0.0
+    for s in range(warmup):
+        ctx.step(s == 0, t)
+        t += dt
+    ctx.synchronize()
+    launches0 = ctx.kernel_launches()
+    per, ch_it, uv_it, refine, resid, ok = [], [], [], [], [], 0
+    for s in range(steps):
+        ctx.flush_l2(flush_bytes)
+        ctx.synchronize()
+        st = ctx.step(False, t)
+        t += dt
+        per.append(st.ch.seconds)
+        ch_it.append(st.ch.iter)
+        uv_it.append(st.uv.iter)
+        refine.append(st.ch.refinements + st.uv.refinements)
+        resid.append(max(st.ch.true_resid, st.uv.true_resid))
+        ok += int(st.ch.info == 0 and st.ch.true_resid <= case.params.tol * 1.0001) + \
+            int(st.uv.info == 0 and st.uv.true_resid <= case.params.tol * 1.0001)
+    launches = ctx.kernel_launches() - launches0
+    del abi
+    return {"seconds": sum(per), "per_step_ms": [1e3 * x for x in per], "ch_iters": ch_it, "uv_iters": uv_it,
+            "refinements": refine, "max_true_resid": max(resid), "solves_ok": ok, "solves": 2 * steps,
+            "launches": launches, "t_end": t}
+
+
+def time_e2e(ctx, case, warmup, steps, flush_bytes):
+    """The drop-in path: per-routine C-ABI calls with host arrays, mcl6 swaps on the host."""
+    import numpy as np
+
+    from drd_application_gb300 import abi
+
+    P = case.params
+    st = {k: v.copy() for k, v in case.state.items()}
+    F = abi
+    gamma1 = min(1.0, P.lambda_rho)
+    t = 0.0
+    nb_cell = st[F.F_PH].nbytes
+    nb_u = st[F.F_U].nbytes
+    nb_v = st[F.F_V].nbytes
+    h2d = (nb_u + nb_v + 2 * nb_cell) + (5 * nb_cell + 2 * nb_u + 2 * nb_v) + (nb_u + nb_v)
+    d2h = (2 * nb_cell) + (nb_u + nb_v + 2 * 8 * (P.nz + 1)) + nb_cell
+
+    def one(first, t):
+        rmu_after, ph_after, s1 = ctx.PhSolve(st[F.F_U], st[F.F_V], st[F.F_PH], st[F.F_RMU], t + P.dt)
+        if first:
+            u_after, v_after, _, _, s2 = ctx.VeloSolve_combined(None, st[F.F_U], st[F.F_V], st[F.F_P], rmu_after,
+                                                                ph_after, t + P.dt)
+        else:
+            u_after, v_after, _, _, s2 = ctx.VeloSolve_2_combined(st[F.F_PSI1], st[F.F_PSI2], st[F.F_U_PRE],
+                                                                  st[F.F_U], st[F.F_V_PRE], st[F.F_V], st[F.F_P],
+                                                                  st[F.F_PH_PRE], ph_after, st[F.F_RMU_PRE],
+                                                                  rmu_after, t + P.dt)
+        st[F.F_U_PRE], st[F.F_V_PRE] = st[F.F_U], st[F.F_V]
+        st[F.F_U], st[F.F_V] = u_after, v_after
+        st[F.F_PH_PRE], st[F.F_RMU_PRE] = st[F.F_PH], st[F.F_RMU]
+        st[F.F_PH], st[F.F_RMU] = ph_after, rmu_after
+        if first:
+            coef = P.re * gamma1 / P.dt
+        else:
+            st[F.F_PSI1] = st[F.F_PSI2]
+            coef = 3 * P.re * gamma1 / 2.0 / P.dt
+        st[F.F_PSI2] = ctx.PreSolve_2(st[F.F_U], st[F.F_V], coef)
+        st[F.F_P] = st[F.F_PSI2] + st[F.F_P]
+        return s1, s2
+
+    for s in range(warmup):
+        one(s == 0, t)
+        t += P.dt
+    total = 0.0
+    for s in range(steps):
+        ctx.flush_l2(flush_bytes)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        one(False, t)
+        total += time.perf_counter() - t0
+        t += P.dt
+    del np
+    return {"seconds": total, "h2d": h2d, "d2h": d2h}
+
+
+def run_gpu(args, ws, rank, local):
+    if ws > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    import __graft_entry__
+
+    __graft_entry__.build()
+    dist = dist_init(ws, local)
+    from drd_application_gb300 import abi
+    from drd_application_gb300.api import DRDContext
+    from drd_application_gb300.workloads import make_case
+
+    flush = 512 << 20  # > 129 MB L2
+    K, W = args.steps, max(3, args.warmup)
+    K64 = args.fp64_steps if args.fp64_steps is not None else max(3, K // 4)
+    case = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED)
+
+    # mixed (headline) path, resident state
+    ctx = DRDContext(case.params)
+    ctx.set_case(case)
+    clocks = ClockSampler(int(local) if ws == 1 else 0)
+    barrier(dist)
+    clocks.start()
+    wall0 = time.perf_counter()
+    mx = time_resident(ctx, case, W, K, flush)
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    sec = max_over_ranks(dist, mx["seconds"])
+    barrier(dist)
+
+    # roofline of the dominant kernel, timed live (CUDA events, back-to-back launches)
+    kb = {}
+    for kid in (abi.DRD_KB_DCT_X_FP32, abi.DRD_KB_DCT_Z_FP32, abi.DRD_KB_UV_MATVEC_FP32, abi.DRD_KB_CH_MATVEC_FP32,
+                abi.DRD_KB_DCT_X_FP64, abi.DRD_KB_UV_MATVEC_FP64):
+        us, by, fl = ctx.kernel_bench(kid, reps=200)
+        kb[kid] = (us, by, fl)
+
+    # e2e through the drop-in C-ABI routines (host arrays)
+    e2e = time_e2e(ctx, case, 1, max(3, K // 4), flush)
+    e2e_sec = max_over_ranks(dist, e2e["seconds"])
+    e2e_steps = max(3, K // 4)
+    ctx.close()
+
+    # plain FP64 path, resident state
+    case64 = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_FP64)
+    ctx64 = DRDContext(case64.params)
+    ctx64.set_case(case64)
+    f64 = time_resident(ctx64, case64, W, K64, flush)
+    f64_sec = max_over_ranks(dist, f64["seconds"])
+    ctx64.close()
+
+    if rank != 0:
+        return 0
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    dom = abi.DRD_KB_DCT_X_FP32
+    us, by, fl = kb[dom]
+    achieved = by / (us * 1e-6) / 1e9
+    steps_total = K * ws
+    value = steps_total / sec
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "time-steps/s",
+        "n_gpus": ws,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": 1e3 * sec / K,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64",
+        "data": "synthetic (seeded geometry, fibers and drops per rank)",
+        "config": {
+            "workload": WORKLOAD, "nr": args.nr, "nz": args.nz, "path": "mixed: FP32 BiCGSTAB in FP64 refinement",
+            "parallelism": f"replicas x{ws}", "l2": "flushed between timed steps (512 MiB write)",
+            "solves_per_s": 2 * steps_total / sec,
+            "solves_to_fp64_1e-8": f"{mx['solves_ok']}/{mx['solves']}",
+            "max_true_resid": mx["max_true_resid"],
+            "ch_iters_mean": statistics.mean(mx["ch_iters"]), "uv_iters_mean": statistics.mean(mx["uv_iters"]),
+            "refinements_mean": statistics.mean(mx["refinements"]),
+            "wall_s_timed_region": wall,
+            "fp64": {"steps_per_s": K64 * ws / f64_sec, "ms_per_step": 1e3 * f64_sec / K64, "steps": K64,
+                     "ch_iters_mean": statistics.mean(f64["ch_iters"]), "uv_iters_mean": statistics.mean(f64["uv_iters"]),
+                     "solves_to_fp64_1e-8": f"{f64['solves_ok']}/{f64['solves']}"},
+            "mixed_over_fp64": (value / (K64 * ws / f64_sec)),
+            "kernels_us": {abi.KB_NAMES[k]: round(v[0], 3) for k, v in kb.items()},
+        },
+        "roofline": {"bound": "hbm", "kernel": abi.KB_NAMES[dom], "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                     "flops_per_launch": fl, "bytes_per_launch": by, "us_per_launch": us,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst)" if peaks else "fallback 6800 GB/s"},
+        "e2e": {"value": e2e_steps * ws / e2e_sec, "unit": "time-steps/s", "h2d_bytes_per_step": e2e["h2d"],
+                "d2h_bytes_per_step": e2e["d2h"]},
+        "clocks": clk,
+        "gpu_launches": mx["launches"],
+    }
+    if not args.no_cpu and ws == 1:
+        line["cpu_baseline"] = cpu_baseline(steps=3, nr=args.nr, nz=args.nz)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    return run_gpu(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -27,6 +27,18 @@ DRD_FLAG_FALLBACK64 = 8
 
 DRD_OP_CH_MATVEC, DRD_OP_CH_PSOLVE, DRD_OP_UV_MATVEC, DRD_OP_UV_PSOLVE, DRD_OP_PHMU_MATVEC, DRD_OP_PHMU_PSOLVE = range(6)
 
+(DRD_KB_UV_MATVEC_FP64, DRD_KB_UV_MATVEC_FP32, DRD_KB_DCT_X_FP64, DRD_KB_DCT_X_FP32, DRD_KB_DCT_Z_FP64,
+ DRD_KB_DCT_Z_FP32, DRD_KB_CH_MATVEC_FP32) = range(7)
+KB_NAMES = {
+    DRD_KB_UV_MATVEC_FP64: "k_uv_mv<double> (momentum stencil)",
+    DRD_KB_UV_MATVEC_FP32: "k_uv_mv<float> (momentum stencil)",
+    DRD_KB_DCT_X_FP64: "k_gemm<double> DCT-I x pass",
+    DRD_KB_DCT_X_FP32: "k_gemm<float> DCT-I x pass",
+    DRD_KB_DCT_Z_FP64: "k_gemm<double> DCT-I z pass",
+    DRD_KB_DCT_Z_FP32: "k_gemm<float> DCT-I z pass",
+    DRD_KB_CH_MATVEC_FP32: "k_ch_mv2<float> (CH stencil)",
+}
+
 # resident-state fields (DRD_F_*)
 F_U, F_V, F_U_PRE, F_V_PRE, F_PH, F_RMU, F_PH_PRE, F_RMU_PRE, F_P, F_PSI1, F_PSI2, F_PF1, F_PF2 = range(13)
 F_COUNT = 13

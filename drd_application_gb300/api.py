@@ -207,6 +207,16 @@ class DRDContext:
         self._rc(self.L.drd_op_apply(self.h, op, bdf, precision, ptr(x), ptr(y)), "drd_op_apply", False)
         return y
 
+    def kernel_bench(self, which, reps=200):
+        """(us per launch, algorithmic bytes per launch, flops per launch) of kernel `which`."""
+        us, by, fl = C.c_double(), C.c_double(), C.c_double()
+        self._rc(self.L.drd_kernel_bench(self.h, which, reps, C.byref(us), C.byref(by), C.byref(fl)),
+                 "drd_kernel_bench", False)
+        return us.value, by.value, fl.value
+
+    def flush_l2(self, nbytes=512 << 20):
+        self._rc(self.L.drd_flush_l2(self.h, int(nbytes)), "drd_flush_l2", False)
+
     def kernel_launches(self):
         return int(self.L.drd_kernel_launches(self.h))
 

@@ -15,7 +15,7 @@
 
 #define DRD_TPB 256        // threads per block of the element-wise / stencil kernels
 #define DRD_MAXB 1024      // maximum blocks of a reduction grid (= partials per dot product)
-#define DRD_NDOT 4         // dot-product slots in the partials buffer
+#define DRD_NDOT 8         // dot-product slots in the partials buffer
 
 namespace drd {
 
@@ -51,8 +51,13 @@ struct KState {
     int iter, maxit, info, phase;
     unsigned flags;
     int x_nonzero;
-    int outer;         // mixed mode: refinement sweeps so far
+    int outer;         // mixed mode: reliable updates (FP64 residual recomputes) so far
     int inner_total;   // mixed mode: FP32 iterations summed
+    double rmax;       // mixed mode: ||r|| at the last reliable update
+    int first_next;    // the next iteration starts a fresh Krylov sequence (P = R)
+    int do_update;     // mixed mode: this iteration ends with a reliable update
+    int mixed;         // mixed mode: no absolute ||s|| exit; convergence on the FP64 residual only
+    int restart;       // mixed mode: the update also restarts the Krylov sequence (breakdown)
 };
 
 __host__ __device__ __forceinline__ long cidx(int nr, int i, int k) { return (long)(i + 1) + (long)(k + 1) * (nr + 2); }

@@ -6,9 +6,12 @@
 // Kernels that take a Krylov state `ks` and a gate return immediately when the solve has
 // left the state they belong to, so a fixed launch sequence (a captured CUDA graph) can
 // express BiCGSTAB's early exits.
+#include <cooperative_groups.h>
 #include <math.h>
 
 #include "drd_kernels.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace drd {
 
@@ -33,11 +36,25 @@ static inline int grid_for(long n, int per_thread = 2) {
 // variable-coefficient 5-point operator with face mobility (M_i + M_nb)/2 and zero flux
 // through the domain faces.  Reads interior values only.
 // ======================================================================================
+//
+// FP64 keeps the reference's form moL*x(i-1) + moR*x(i+1) - (moL+moR)*x(i).  FP32 (the inner
+// operators of the mixed mode) evaluates the same sum as moR*(x(i+1)-x(i)) - moL*(x(i)-x(i-1)):
+// for smooth fields the neighbour differences are exact in FP32 while the reference form
+// cancels, and iterative refinement only converges if the FP32 operator stays close to the
+// FP64 one on those fields.
 template <typename T, class XA, class MA>
 __device__ __forceinline__ T op_dgn(int i, int k, int nr, int nz, T idx2, T idz2, const XA& x, const MA& mo) {
     const T h = T(0.5);
     T acc = T(0);
     const T m0 = mo(i, k), x0 = x(i, k);
+    if constexpr (sizeof(T) == 4) {
+        T sx = T(0), sz = T(0);
+        if (i > 0) sx -= (mo(i - 1, k) + m0) * h * (x0 - x(i - 1, k));
+        if (i < nr - 1) sx += (m0 + mo(i + 1, k)) * h * (x(i + 1, k) - x0);
+        if (k > 0) sz -= (mo(i, k - 1) + m0) * h * (x0 - x(i, k - 1));
+        if (k < nz - 1) sz += (m0 + mo(i, k + 1)) * h * (x(i, k + 1) - x0);
+        return idx2 * sx + idz2 * sz;
+    }
     T moL, moR;
     if (i == 0) {
         moL = (m0 + m0) * h;
@@ -514,10 +531,16 @@ __global__ void k_uv_mv(OpScal<T> o, const T* __restrict__ rho, const T* __restr
             else
                 val = f1 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i - 1, k)]) * h;
             T cr = E_(i, k), cl = E_(i - 1, k);
-            val = val - T(2) * o.dt * (cr * F.Uc(i + 1, k) + cl * F.Uc(i - 1, k) - (cl + cr) * f1) / o.dr2;
+            if constexpr (sizeof(T) == 4)
+                val = val - T(2) * o.dt * (cr * (F.Uc(i + 1, k) - f1) + cl * (F.Uc(i - 1, k) - f1)) / o.dr2;
+            else
+                val = val - T(2) * o.dt * (cr * F.Uc(i + 1, k) + cl * F.Uc(i - 1, k) - (cl + cr) * f1) / o.dr2;
             cr = (E_(i, k + 1) + E_(i - 1, k + 1) + E_(i, k) + E_(i - 1, k)) * q4;
             cl = (E_(i, k) + E_(i - 1, k) + E_(i, k - 1) + E_(i - 1, k - 1)) * q4;
-            val = val - o.dt * (cr * F.U(i, k + 1) + cl * F.U(i, k - 1) - (cl + cr) * f1) / o.dz2;
+            if constexpr (sizeof(T) == 4)
+                val = val - o.dt * (cr * (F.U(i, k + 1) - f1) + cl * (F.U(i, k - 1) - f1)) / o.dz2;
+            else
+                val = val - o.dt * (cr * F.U(i, k + 1) + cl * F.U(i, k - 1) - (cl + cr) * f1) / o.dz2;
             val = val - o.dt * (cr * (F.V(i, k + 1) - F.V(i - 1, k + 1)) - cl * (F.V(i, k) - F.V(i - 1, k))) / o.dr / o.dz;
         } else {
             const long qv = q - mn;
@@ -529,10 +552,16 @@ __global__ void k_uv_mv(OpScal<T> o, const T* __restrict__ rho, const T* __restr
             else
                 val = f2 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i, k - 1)]) * h;
             T cr = E_(i, k), cl = E_(i, k - 1);
-            val = val - T(2) * o.dt * (cr * F.V(i, k + 1) + cl * F.V(i, k - 1) - (cl + cr) * f2) / o.dz2;
+            if constexpr (sizeof(T) == 4)
+                val = val - T(2) * o.dt * (cr * (F.V(i, k + 1) - f2) + cl * (F.V(i, k - 1) - f2)) / o.dz2;
+            else
+                val = val - T(2) * o.dt * (cr * F.V(i, k + 1) + cl * F.V(i, k - 1) - (cl + cr) * f2) / o.dz2;
             cr = (E_(i + 1, k) + E_(i, k) + E_(i + 1, k - 1) + E_(i, k - 1)) * q4;
             cl = (E_(i, k) + E_(i - 1, k) + E_(i, k - 1) + E_(i - 1, k - 1)) * q4;
-            val = val - o.dt * (cr * F.V(i + 1, k) + cl * F.V(i - 1, k) - (cl + cr) * f2) / o.dr2;
+            if constexpr (sizeof(T) == 4)
+                val = val - o.dt * (cr * (F.V(i + 1, k) - f2) + cl * (F.V(i - 1, k) - f2)) / o.dr2;
+            else
+                val = val - o.dt * (cr * F.V(i + 1, k) + cl * F.V(i - 1, k) - (cl + cr) * f2) / o.dr2;
             val = val - o.dt * (cr * (F.Uc(i + 1, k) - F.Uc(i + 1, k - 1)) - cl * (F.Uc(i, k) - F.Uc(i, k - 1))) / o.dr / o.dz;
         }
         const T yn = (beta == T(0)) ? alpha * val : alpha * val + beta * y[q];
@@ -746,11 +775,136 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm(GemmArgs<T> a) {
     }
 }
 
-struct GemmCfg { const char* name; };
-static const GemmCfg kGemmCfgs[] = {{"64x64x16/4x4"}, {"32x64x16/2x4"}, {"32x32x16/2x2"}, {"16x32x16/1x2"}};
+// Split-K variant: the KS CTAs of a thread-block cluster (cluster dims 1 x 1 x KS) each
+// accumulate one slice of K for the same output tile; the partial tiles are then summed
+// through distributed shared memory in a fixed rank order (deterministic, no atomics), each
+// CTA reducing and storing BM/KS of the tile's rows.  Small-M transforms get KS times more
+// CTAs this way, enough to occupy all SMs.
+template <typename T, int BM, int BN, int BK, int TM, int TN, int KS, int EPI>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm_sk(GemmArgs<T> a) {
+    constexpr int NT = (BM / TM) * (BN / TN);
+    constexpr int TX = BN / TN, TY = BM / TM;
+    static_assert(BM % KS == 0, "rows split over the cluster");
+    __shared__ T As[BK][BM + 1];
+    __shared__ T Bs[BK][BN];
+    __shared__ T Cs[BM][BN + 1];
+    count_launch(a.ctr);
+    if (gate_closed(a.ks, a.gate)) return;  // uniform over the cluster: the state is not written here
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int kchunk = ((a.K + KS * BK - 1) / (KS * BK)) * BK;
+    const int kbeg = rank * kchunk, kend = min(a.K, kbeg + kchunk);
+    T acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+    constexpr int LA = (BM * BK + NT - 1) / NT, LB = (BK * BN + NT - 1) / NT;
+    T ra[LA], rb[LB];
+    auto gload = [&](int k0) {
+#pragma unroll
+        for (int l = 0; l < LA; ++l) {
+            const int e = tid + l * NT;
+            const int r = e / BK, c = e % BK;
+            const int gm = m0 + r, gk = k0 + c;
+            ra[l] = (e < BM * BK && gm < a.M && gk < kend) ? a.A[(long)gm * a.lda + gk] : T(0);
+        }
+#pragma unroll
+        for (int l = 0; l < LB; ++l) {
+            const int e = tid + l * NT;
+            const int r = e / BN, c = e % BN;
+            const int gk = k0 + r, gn = n0 + c;
+            rb[l] = (e < BK * BN && gk < kend && gn < a.N) ? a.B[(long)gk * a.ldb + gn] : T(0);
+        }
+    };
+    if (kbeg < kend) gload(kbeg);
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
+#pragma unroll
+        for (int l = 0; l < LA; ++l) {
+            const int e = tid + l * NT;
+            if (e < BM * BK) As[e % BK][e / BK] = ra[l];
+        }
+#pragma unroll
+        for (int l = 0; l < LB; ++l) {
+            const int e = tid + l * NT;
+            if (e < BK * BN) Bs[e / BN][e % BN] = rb[l];
+        }
+        __syncthreads();
+        if (k0 + BK < kend) gload(k0 + BK);  // prefetch the next slice while computing this one
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            T av[TM], bv[TN];
+#pragma unroll
+            for (int i = 0; i < TM; ++i) av[i] = As[kk][ty + i * TY];
+#pragma unroll
+            for (int j = 0; j < TN; ++j) bv[j] = Bs[kk][tx + j * TX];
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TN; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) Cs[ty + i * TY][tx + j * TX] = acc[i][j];
+    cluster.sync();
+    const double coef = (EPI == EPI_PRE_FINAL) ? a.ca->coef : 0.0;
+    constexpr int RB = BM / KS;
+    for (int e = tid; e < RB * BN; e += NT) {
+        const int r = rank * RB + e / BN, c = e % BN;
+        const int gm = m0 + r, gn = n0 + c;
+        T v = T(0);
+#pragma unroll
+        for (int q = 0; q < KS; ++q) v += cluster.map_shared_rank(&Cs[0][0], q)[r * (BN + 1) + c];
+        if (gm < a.M && gn < a.N) {
+            if (EPI == EPI_STORE) a.C[(long)gm * a.ldc + gn] = v;
+            else if (EPI == EPI_DIV_TAB) a.C[(long)gm * a.ldc + gn] = v / a.tab[(long)gm * a.ldt + gn];
+            else if (EPI == EPI_SCALE) a.C[(long)gm * a.ldc + gn] = v * (T)a.scale;
+            else a.C[cidx(a.nr, gn, gm)] = (T)(((double)v / a.scale) * coef);
+        }
+    }
+    cluster.sync();  // keep every CTA's partial tile alive until all readers are done
+}
 
-int gemm_config_count() { return 4; }
+struct GemmCfg { const char* name; };
+static const GemmCfg kGemmCfgs[] = {{"64x64x16/4x4"},         {"32x64x16/2x4"},         {"32x32x16/2x2"},
+                                    {"16x32x16/1x2"},         {"sk4 32x64x16/4x4"},     {"sk4 32x32x16/4x4"},
+                                    {"sk4 16x64x16/2x4"},     {"sk8 32x32x16/2x2"},     {"sk2 32x64x16/4x4"}};
+
+int gemm_config_count() { return 9; }
 const char* gemm_config_name(int cfg) { return kGemmCfgs[cfg].name; }
+
+template <typename T, int BM, int BN, int TM, int TN, int KS, int EPI>
+static void gemm_sk_launch(const GemmArgs<T>& a, cudaStream_t s) {
+    constexpr int NT = (BM / TM) * (BN / TN);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((a.N + BN - 1) / BN, (a.M + BM - 1) / BM, KS);
+    cfg.blockDim = dim3(NT, 1, 1);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 1;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = KS;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_gemm_sk<T, BM, BN, 16, TM, TN, KS, EPI>, a);
+}
+
+template <typename T, int BM, int BN, int TM, int TN, int KS>
+static void gemm_sk_dispatch(int epi, const GemmArgs<T>& a, cudaStream_t s) {
+    switch (epi) {
+        case EPI_STORE: gemm_sk_launch<T, BM, BN, TM, TN, KS, EPI_STORE>(a, s); break;
+        case EPI_DIV_TAB: gemm_sk_launch<T, BM, BN, TM, TN, KS, EPI_DIV_TAB>(a, s); break;
+        case EPI_SCALE: gemm_sk_launch<T, BM, BN, TM, TN, KS, EPI_SCALE>(a, s); break;
+        default: gemm_sk_launch<T, BM, BN, TM, TN, KS, EPI_PRE_FINAL>(a, s); break;
+    }
+}
 
 template <typename T, int BM, int BN, int TM, int TN>
 static void gemm_dispatch_epi(int epi, const GemmArgs<T>& a, cudaStream_t s) {
@@ -770,7 +924,12 @@ void launch_gemm(int cfg, int epi, const GemmArgs<T>& a, cudaStream_t s) {
         case 0: gemm_dispatch_epi<T, 64, 64, 4, 4>(epi, a, s); break;
         case 1: gemm_dispatch_epi<T, 32, 64, 2, 4>(epi, a, s); break;
         case 2: gemm_dispatch_epi<T, 32, 32, 2, 2>(epi, a, s); break;
-        default: gemm_dispatch_epi<T, 16, 32, 1, 2>(epi, a, s); break;
+        case 3: gemm_dispatch_epi<T, 16, 32, 1, 2>(epi, a, s); break;
+        case 4: gemm_sk_dispatch<T, 32, 64, 4, 4, 4>(epi, a, s); break;
+        case 5: gemm_sk_dispatch<T, 32, 32, 4, 4, 4>(epi, a, s); break;
+        case 6: gemm_sk_dispatch<T, 16, 64, 2, 4, 4>(epi, a, s); break;
+        case 7: gemm_sk_dispatch<T, 32, 32, 2, 2, 8>(epi, a, s); break;
+        default: gemm_sk_dispatch<T, 32, 64, 4, 4, 2>(epi, a, s); break;
     }
 }
 template void launch_gemm<double>(int, int, const GemmArgs<double>&, cudaStream_t);
@@ -780,7 +939,11 @@ template void launch_gemm<float>(int, int, const GemmArgs<float>&, cudaStream_t)
 // BiCGSTAB (lib/BiCGSTABREVCOM.f:150-418, lib/STOPTEST2.f:281-290) as element-wise kernels
 // with fused partial dot products and one-block scalar kernels.  Dot products are summed in
 // FP64 in a fixed order (deterministic for a fixed grid).
-// Partials slots: 0 = ||.||^2 / (rtld,v), 1 = (rtld,r) or (t,s), 2 = (t,t), 3 = ||b||^2.
+// Partials slots (a kernel never reads a slot it writes, since other blocks may still be
+// reading it): 0 = ||r||^2 (and init/residual norms), 1 = (rtld, r), 3 = ||b||^2,
+// 4 = (rtld, v), 5 = ||s||^2, 6 = (t, s), 7 = (t, t).  RHO, ALPHA and OMEGA are computed
+// redundantly by every block of the vector kernel that needs them, from the partials in a
+// fixed order, so all blocks agree and no one-block scalar kernel is launched for them.
 // ======================================================================================
 static __device__ const double kBreakTol = 1.2325951644078309e-32;  // DLAMCH('E')**2 (getbreak.f)
 
@@ -820,6 +983,10 @@ __global__ void k_bi_init2(KState* ks, Dots d, double tol, int maxit, const KSta
         ks->bnorm_raw = sqrt(bb);
         ks->bnrm2 = (ks->bnorm_raw == 0.0) ? 1.0 : ks->bnorm_raw;
         ks->rho = ks->rho1 = ks->alpha = ks->omega = ks->beta = 0.0;
+        ks->first_next = 1;
+        ks->mixed = 0;
+        ks->do_update = 0;
+        ks->restart = 0;
         ks->phase = (maxit <= 0) ? PH_DONE : PH_RUNNING;
         if (maxit <= 0) ks->info = -3;
         if (parent != nullptr && parent->phase != PH_RUNNING) ks->phase = PH_DONE;
@@ -862,33 +1029,38 @@ __global__ void k_bi_init4(long n, const T* __restrict__ r, T* __restrict__ rtld
     if (threadIdx.x == 0) d.part[1 * DRD_MAXB + blockIdx.x] = s;
 }
 
-// ITER = ITER + 1; RHO = (rtld, r); breakdown test; BETA (:261-269).
-__global__ void k_bi_rho(KState* ks, Dots d, ull* ctr) {
+// ITER = ITER + 1; RHO = (rtld, r); breakdown test; BETA (:261-269); then P = R (first
+// iteration) or P = beta (P - omega V) + R (:268-275), fused with the preconditioner when it
+// is diagonal (Jacobi) or the identity.
+template <typename T>
+__global__ void k_bi_p(long n, const T* __restrict__ r, const T* __restrict__ v, T* __restrict__ p,
+                       T* __restrict__ phat, const T* __restrict__ diag, int ident, KState* ks, Dots d, ull* ctr) {
     count_launch(ctr);
     if (ks->phase != PH_RUNNING) return;
     __shared__ double sm[32];
-    const double rho = reduce_partials<DRD_TPB>(d.part + 1 * DRD_MAXB, d.G, sm);
-    if (threadIdx.x == 0) {
-        ks->iter = ks->iter + 1;
-        ks->rho = rho;
-        if (fabs(rho) < kBreakTol) {
+    __shared__ double s_rho;
+    const double rr = reduce_partials<DRD_TPB>(d.part + 1 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) s_rho = rr;
+    __syncthreads();
+    const double rho = s_rho;
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    if (fabs(rho) < kBreakTol) {
+        if (lead) {
+            ks->iter = ks->iter + 1;
+            ks->rho = rho;
             ks->info = -10;
             ks->phase = PH_DONE;
-        } else if (ks->iter > 1) {
-            ks->beta = (rho / ks->rho1) * (ks->alpha / ks->omega);
         }
+        return;
     }
-}
-
-// P = R (first iteration) or P = beta (P - omega V) + R (:268-275), fused with the
-// preconditioner when it is diagonal (Jacobi) or the identity.
-template <typename T>
-__global__ void k_bi_p(long n, const T* __restrict__ r, const T* __restrict__ v, T* __restrict__ p,
-                       T* __restrict__ phat, const T* __restrict__ diag, int ident, const KState* ks, ull* ctr) {
-    count_launch(ctr);
-    if (gate_closed(ks, G_RUNNING)) return;
-    const bool first = ks->iter == 1;
-    const T beta = (T)ks->beta, nomega = (T)(-ks->omega);
+    const bool first = ks->first_next != 0;
+    const double beta_d = first ? 0.0 : (rho / ks->rho1) * (ks->alpha / ks->omega);
+    if (lead) {
+        ks->iter = ks->iter + 1;
+        ks->rho = rho;
+        ks->beta = beta_d;
+    }
+    const T beta = (T)beta_d, nomega = (T)(-ks->omega);
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
         T pv;
         if (first) pv = r[q];
@@ -903,41 +1075,59 @@ __global__ void k_bi_p(long n, const T* __restrict__ r, const T* __restrict__ v,
     }
 }
 
-// ALPHA = RHO / (rtld, v) (:307).
-__global__ void k_bi_alpha(KState* ks, Dots d, ull* ctr) {
+// ALPHA = RHO / (rtld, v) (:307) from slot 4, then S = R - ALPHA V (:311-312, S aliases R)
+// with ||S||^2 partials (slot 5).
+template <typename T>
+__global__ void k_bi_s(long n, const T* __restrict__ v, T* __restrict__ r, KState* ks, Dots d, ull* ctr) {
     count_launch(ctr);
     if (ks->phase != PH_RUNNING) return;
     __shared__ double sm[32];
-    const double rv = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
-    if (threadIdx.x == 0) ks->alpha = ks->rho / rv;
-}
-
-// S = R - ALPHA V (:311-312, S aliases R) with ||S||^2 partials.
-template <typename T>
-__global__ void k_bi_s(long n, const T* __restrict__ v, T* __restrict__ r, Dots d, const KState* ks, ull* ctr) {
-    count_launch(ctr);
-    if (gate_closed(ks, G_RUNNING)) return;
-    const T na = (T)(-ks->alpha);
+    __shared__ double s_rv;
+    const double rv0 = reduce_partials<DRD_TPB>(d.part + 4 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) s_rv = rv0;
+    __syncthreads();
+    const double rv = s_rv;
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    if (ks->mixed && !(fabs(rv) > 0.0)) {  // mixed: fold and restart instead of dividing by zero
+        if (lead) {
+            ks->alpha = 0.0;
+            ks->phase = PH_EARLY;
+            ks->first_next = 0;
+        }
+        return;
+    }
+    const double alpha = ks->rho / rv;
+    if (lead) {
+        ks->alpha = alpha;
+        ks->first_next = 0;  // every block of k_bi_p has read it
+    }
+    const T na = (T)(-alpha);
     double a = 0.0;
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
-        const T s = r[q] + na * v[q];
-        r[q] = s;
-        a += (double)s * (double)s;
+        const T sv = r[q] + na * v[q];
+        r[q] = sv;
+        a += (double)sv * (double)sv;
     }
-    __shared__ double sm[32];
     double t = block_sum<DRD_TPB>(a, sm);
-    if (threadIdx.x == 0) d.part[0 * DRD_MAXB + blockIdx.x] = t;
+    if (threadIdx.x == 0) d.part[5 * DRD_MAXB + blockIdx.x] = t;
 }
 
 // Early absolute test ||S|| <= TOL (:313-316).
+// In mixed mode the test is relative (||s|| <= tol ||b|| / 10, or s == 0): the iteration then
+// stops after the ALPHA half-step, and a reliable update decides on the FP64 residual.
 __global__ void k_bi_snorm(KState* ks, Dots d, ull* ctr) {
     count_launch(ctr);
     if (ks->phase != PH_RUNNING) return;
     __shared__ double sm[32];
-    const double ss = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
+    const double ss = reduce_partials<DRD_TPB>(d.part + 5 * DRD_MAXB, d.G, sm);
     if (threadIdx.x == 0) {
         ks->snorm = sqrt(ss);
-        if (ks->snorm <= ks->tol) {
+        if (ks->mixed) {
+            if (ks->snorm == 0.0 || ks->snorm <= 0.1 * ks->tol * ks->bnrm2 || !isfinite(ks->snorm)) {
+                ks->phase = PH_EARLY;
+                ks->flags |= DRD_FLAG_EARLY_S;
+            }
+        } else if (ks->snorm <= ks->tol) {
             ks->phase = PH_EARLY;
             ks->resid = ks->snorm / ks->bnrm2;
             ks->info = 0;
@@ -955,21 +1145,12 @@ __global__ void k_bi_diag_apply(long n, const T* __restrict__ x, const T* __rest
         y[q] = ident ? x[q] : x[q] / diag[q];
 }
 
-// OMEGA = (t, s) / (t, t) (:349-350).
-__global__ void k_bi_omega(KState* ks, Dots d, ull* ctr) {
-    count_launch(ctr);
-    if (ks->phase != PH_RUNNING) return;
-    __shared__ double sm[32];
-    const double ts = reduce_partials<DRD_TPB>(d.part + 1 * DRD_MAXB, d.G, sm);
-    const double tt = reduce_partials<DRD_TPB>(d.part + 2 * DRD_MAXB, d.G, sm);
-    if (threadIdx.x == 0) ks->omega = ts / tt;
-}
-
-// X = X + ALPHA PHAT (+ OMEGA SHAT); R = R - OMEGA T (:314, :354-359) with ||R||^2 and
-// (rtld, R) partials for STOPTEST2 and the next RHO.
+// OMEGA = (t, s) / (t, t) (:349-350) from slots 6/7, then X = X + ALPHA PHAT (+ OMEGA SHAT);
+// R = R - OMEGA T (:314, :354-359) with ||R||^2 (slot 0) and (rtld, R) (slot 1) partials for
+// STOPTEST2 and the next RHO.
 template <typename T>
 __global__ void k_bi_xr(long n, const T* __restrict__ phat, const T* __restrict__ shat, const T* __restrict__ t,
-                        const T* __restrict__ rtld, T* __restrict__ x, T* __restrict__ r, Dots d, const KState* ks,
+                        const T* __restrict__ rtld, T* __restrict__ x, T* __restrict__ r, KState* ks, Dots d,
                         ull* ctr) {
     count_launch(ctr);
     const int ph = ks->phase;
@@ -980,7 +1161,15 @@ __global__ void k_bi_xr(long n, const T* __restrict__ phat, const T* __restrict_
             x[q] = x[q] + al * phat[q];
         return;
     }
-    const T om = (T)ks->omega, nom = (T)(-ks->omega);
+    __shared__ double sm[32];
+    __shared__ double s_om;
+    const double ts = reduce_partials<DRD_TPB>(d.part + 6 * DRD_MAXB, d.G, sm);
+    const double tt = reduce_partials<DRD_TPB>(d.part + 7 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) s_om = (ks->mixed && !(tt > 0.0)) ? 0.0 : ts / tt;  // mixed: restart on omega = 0
+    __syncthreads();
+    const double omega = s_om;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ks->omega = omega;
+    const T om = (T)omega, nom = (T)(-omega);
     double a0 = 0.0, a1 = 0.0;
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
         T xv = x[q] + al * phat[q];
@@ -991,7 +1180,6 @@ __global__ void k_bi_xr(long n, const T* __restrict__ phat, const T* __restrict_
         a0 += (double)rv * (double)rv;
         a1 += (double)rtld[q] * (double)rv;
     }
-    __shared__ double sm[32];
     double s0 = block_sum<DRD_TPB>(a0, sm);
     if (threadIdx.x == 0) d.part[0 * DRD_MAXB + blockIdx.x] = s0;
     double s1 = block_sum<DRD_TPB>(a1, sm);
@@ -1033,6 +1221,14 @@ __global__ void k_bi_end(KState* ks, Dots d, cudaGraphConditionalHandle h, int u
     }
 }
 
+// Sets a WHILE node's condition from the state it loops on.  Runs right before the node: a
+// handle's default value is only applied when the top-level graph launches, so a loop nested
+// in another loop's body must be re-armed each time the outer body runs.
+__global__ void k_arm_while(const KState* ks, cudaGraphConditionalHandle h, ull* ctr) {
+    count_launch(ctr);
+    if (threadIdx.x == 0) cudaGraphSetConditional(h, ks->phase == PH_RUNNING ? 1u : 0u);
+}
+
 // ||b - A x|| / ||b|| from slot 0 (the residual's partials) and the stored ||b||.
 __global__ void k_bi_true_resid(KState* ks, Dots d, ull* ctr) {
     count_launch(ctr);
@@ -1063,6 +1259,129 @@ __global__ void k_norm2_partial(long n, const T* __restrict__ x, Dots d, int slo
     __shared__ double sm[32];
     double r = block_sum<DRD_TPB>(a, sm);
     if (threadIdx.x == 0) d.part[slot * DRD_MAXB + blockIdx.x] = r;
+}
+
+// ---- mixed precision: FP32 BiCGSTAB with FP64 reliable updates ---------------------------
+// One FP32 BiCGSTAB runs on; whenever its recursive residual fell a decade below the last true
+// residual (or claims convergence, or the iteration cap is hit), the FP32 increment is folded
+// into the FP64 solution, b - A x is recomputed with the FP64 operator and replaces the
+// recursive residual.  Convergence is decided on that FP64 residual only.
+
+// After r64 = b - A x64 (slot 0) and ||b||^2 (slot 3).
+__global__ void k_mr_init(KState* ks, Dots d, double tol, int maxit, ull* ctr) {
+    count_launch(ctr);
+    __shared__ double sm[32];
+    const double rr = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
+    const double bb = reduce_partials<DRD_TPB>(d.part + 3 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) {
+        ks->tol = tol;
+        ks->maxit = maxit;
+        ks->bnorm_raw = sqrt(bb);
+        ks->bnrm2 = (ks->bnorm_raw == 0.0) ? 1.0 : ks->bnorm_raw;
+        ks->rmax = sqrt(rr);
+        ks->resid = ks->rmax / ks->bnrm2;
+        ks->true_resid = ks->resid;
+        ks->iter = 0;
+        ks->inner_total = 0;
+        ks->outer = 0;
+        ks->info = 0;
+        ks->flags = DRD_FLAG_REFINED;
+        ks->rho = ks->rho1 = ks->alpha = ks->omega = ks->beta = 0.0;
+        ks->first_next = 1;
+        ks->mixed = 1;
+        ks->do_update = 0;
+        ks->restart = 0;
+        ks->x_nonzero = 0;
+        ks->phase = (ks->resid <= tol || ks->rmax == 0.0) ? PH_DONE : PH_RUNNING;
+        if (!isfinite(ks->resid)) { ks->info = DRD_ERR_NONFINITE; ks->phase = PH_DONE; }
+    }
+}
+
+// r32 = r64 (a fresh sequence also takes rtld = r32), and the (rtld, r) partials for the next RHO.
+template <typename T>
+__global__ void k_mr_reset(long n, const double* __restrict__ r64, T* __restrict__ r, T* __restrict__ rtld,
+                           Dots d, const KState* ks, ull* ctr) {
+    count_launch(ctr);
+    if (ks->phase != PH_RUNNING) return;
+    const bool fresh = ks->first_next != 0;
+    double a = 0.0;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const T rv = (T)r64[q];
+        r[q] = rv;
+        T tv;
+        if (fresh) { rtld[q] = rv; tv = rv; }
+        else tv = rtld[q];
+        a += (double)tv * (double)rv;
+    }
+    __shared__ double sm[32];
+    double s1 = block_sum<DRD_TPB>(a, sm);
+    if (threadIdx.x == 0) d.part[1 * DRD_MAXB + blockIdx.x] = s1;
+}
+
+// End of an FP32 iteration: decides on a reliable update (IF node) and the loop condition.
+__global__ void k_mr_end(KState* ks, Dots d, cudaGraphConditionalHandle hw, cudaGraphConditionalHandle hif,
+                         ull* ctr) {
+    count_launch(ctr);
+    __shared__ double sm[32];
+    const int ph = ks->phase;
+    double rr = 0.0;
+    if (ph == PH_RUNNING) rr = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) {
+        int upd = 0;
+        if (ph == PH_EARLY) {
+            // the half-step ended the iteration: fold, recompute in FP64, restart the sequence
+            upd = 1;
+            ks->restart = 1;
+            ks->phase = PH_RUNNING;
+            ks->inner_total = ks->iter;
+            ks->rho1 = ks->rho;
+        } else if (ph == PH_RUNNING) {
+            const double rn = sqrt(rr);
+            ks->snorm = rn;
+            ks->inner_total = ks->iter;
+            if (!isfinite(rn)) upd = 1;
+            else if (rn <= 0.1 * ks->rmax || rn / ks->bnrm2 <= ks->tol || ks->iter >= ks->maxit) upd = 1;
+            else if (fabs(ks->omega) < kBreakTol) { upd = 1; ks->restart = 1; }
+            ks->rho1 = ks->rho;
+        } else if (ph == PH_DONE) {
+            upd = 1;  // RHO breakdown this iteration: fold the FP32 increment in before stopping
+        }
+        ks->do_update = upd;
+        cudaGraphSetConditional(hif, upd ? 1u : 0u);
+        cudaGraphSetConditional(hw, (ks->phase == PH_RUNNING) ? 1u : 0u);
+    }
+}
+
+// x64 += x32; x32 = 0
+template <typename T>
+__global__ void k_mr_fold(long n, T* __restrict__ x32, double* __restrict__ x64, ull* ctr) {
+    count_launch(ctr);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        x64[q] = x64[q] + (double)x32[q];
+        x32[q] = T(0);
+    }
+}
+
+// After r64 = b - A x64 (slot 0): the FP64 convergence test and the loop condition.
+__global__ void k_mr_check(KState* ks, Dots d, cudaGraphConditionalHandle hw, ull* ctr) {
+    count_launch(ctr);
+    __shared__ double sm[32];
+    const double rr = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
+    if (threadIdx.x == 0) {
+        const double rn = sqrt(rr);
+        const double tr = rn / ks->bnrm2;
+        ks->outer += 1;
+        ks->rmax = rn;
+        ks->resid = tr;
+        ks->true_resid = tr;
+        if (!isfinite(tr)) { ks->info = DRD_ERR_NONFINITE; ks->phase = PH_DONE; }
+        else if (tr <= ks->tol) { ks->info = 0; ks->phase = PH_DONE; }
+        else if (ks->phase == PH_DONE) { /* breakdown: keep its INFO */ }
+        else if (ks->iter >= ks->maxit) { ks->info = 1; ks->phase = PH_DONE; }
+        else if (ks->restart) { ks->first_next = 1; ks->restart = 0; }
+        ks->do_update = 0;
+        cudaGraphSetConditional(hw, (ks->phase == PH_RUNNING) ? 1u : 0u);
+    }
 }
 
 // ---- mixed-precision refinement ----------------------------------------------------------
@@ -1269,16 +1588,14 @@ template <typename T>
 void launch_bi_init4(long n, const T* r, T* rtld, const Dots& d, const KState* ks, ull* ctr, cudaStream_t s) {
     k_bi_init4<T><<<d.G, DRD_TPB, 0, s>>>(n, r, rtld, d, ks, ctr);
 }
-void launch_bi_rho(KState* ks, const Dots& d, ull* ctr, cudaStream_t s) { k_bi_rho<<<1, DRD_TPB, 0, s>>>(ks, d, ctr); }
 template <typename T>
-void launch_bi_p(long n, const T* r, const T* v, T* p, T* phat, const T* diag, int ident, const KState* ks, ull* ctr,
-                 cudaStream_t s) {
-    k_bi_p<T><<<GRID(n)>>>(n, r, v, p, phat, diag, ident, ks, ctr);
+void launch_bi_p(long n, const T* r, const T* v, T* p, T* phat, const T* diag, int ident, KState* ks, const Dots& d,
+                 ull* ctr, cudaStream_t s) {
+    k_bi_p<T><<<d.G, DRD_TPB, 0, s>>>(n, r, v, p, phat, diag, ident, ks, d, ctr);
 }
-void launch_bi_alpha(KState* ks, const Dots& d, ull* ctr, cudaStream_t s) { k_bi_alpha<<<1, DRD_TPB, 0, s>>>(ks, d, ctr); }
 template <typename T>
-void launch_bi_s(long n, const T* v, T* r, const Dots& d, const KState* ks, ull* ctr, cudaStream_t s) {
-    k_bi_s<T><<<d.G, DRD_TPB, 0, s>>>(n, v, r, d, ks, ctr);
+void launch_bi_s(long n, const T* v, T* r, KState* ks, const Dots& d, ull* ctr, cudaStream_t s) {
+    k_bi_s<T><<<d.G, DRD_TPB, 0, s>>>(n, v, r, ks, d, ctr);
 }
 void launch_bi_snorm(KState* ks, const Dots& d, ull* ctr, cudaStream_t s) { k_bi_snorm<<<1, DRD_TPB, 0, s>>>(ks, d, ctr); }
 template <typename T>
@@ -1286,14 +1603,38 @@ void launch_bi_diag_apply(long n, const T* x, const T* diag, int ident, T* y, co
                           cudaStream_t s) {
     k_bi_diag_apply<T><<<GRID(n)>>>(n, x, diag, ident, y, ks, gate, ctr);
 }
-void launch_bi_omega(KState* ks, const Dots& d, ull* ctr, cudaStream_t s) { k_bi_omega<<<1, DRD_TPB, 0, s>>>(ks, d, ctr); }
 template <typename T>
-void launch_bi_xr(long n, const T* phat, const T* shat, const T* t, const T* rtld, T* x, T* r, const Dots& d,
-                  const KState* ks, ull* ctr, cudaStream_t s) {
-    k_bi_xr<T><<<d.G, DRD_TPB, 0, s>>>(n, phat, shat, t, rtld, x, r, d, ks, ctr);
+void launch_bi_xr(long n, const T* phat, const T* shat, const T* t, const T* rtld, T* x, T* r, KState* ks,
+                  const Dots& d, ull* ctr, cudaStream_t s) {
+    k_bi_xr<T><<<d.G, DRD_TPB, 0, s>>>(n, phat, shat, t, rtld, x, r, ks, d, ctr);
 }
 void launch_bi_end(KState* ks, const Dots& d, cudaGraphConditionalHandle h, int use_graph, ull* ctr, cudaStream_t s) {
     k_bi_end<<<1, DRD_TPB, 0, s>>>(ks, d, h, use_graph, ctr);
+}
+void launch_mr_init(KState* ks, const Dots& d, double tol, int maxit, ull* ctr, cudaStream_t s) {
+    k_mr_init<<<1, DRD_TPB, 0, s>>>(ks, d, tol, maxit, ctr);
+}
+template <typename T>
+void launch_mr_reset(long n, const double* r64, T* r, T* rtld, const Dots& d, const KState* ks, ull* ctr,
+                     cudaStream_t s) {
+    k_mr_reset<T><<<d.G, DRD_TPB, 0, s>>>(n, r64, r, rtld, d, ks, ctr);
+}
+template void launch_mr_reset<float>(long, const double*, float*, float*, const Dots&, const KState*, ull*, cudaStream_t);
+void launch_mr_end(KState* ks, const Dots& d, cudaGraphConditionalHandle hw, cudaGraphConditionalHandle hif, ull* ctr,
+                   cudaStream_t s) {
+    k_mr_end<<<1, DRD_TPB, 0, s>>>(ks, d, hw, hif, ctr);
+}
+template <typename T>
+void launch_mr_fold(long n, T* x32, double* x64, ull* ctr, cudaStream_t s) {
+    k_mr_fold<T><<<GRID(n)>>>(n, x32, x64, ctr);
+}
+template void launch_mr_fold<float>(long, float*, double*, ull*, cudaStream_t);
+void launch_mr_check(KState* ks, const Dots& d, cudaGraphConditionalHandle hw, ull* ctr, cudaStream_t s) {
+    k_mr_check<<<1, DRD_TPB, 0, s>>>(ks, d, hw, ctr);
+}
+
+void launch_arm_while(const KState* ks, cudaGraphConditionalHandle h, ull* ctr, cudaStream_t s) {
+    k_arm_while<<<1, 32, 0, s>>>(ks, h, ctr);
 }
 void launch_bi_true_resid(KState* ks, const Dots& d, ull* ctr, cudaStream_t s) {
     k_bi_true_resid<<<1, DRD_TPB, 0, s>>>(ks, d, ctr);
@@ -1343,11 +1684,12 @@ template void launch_mx_scale<float>(long, const double*, const KState*, float*,
     template void launch_uv_diag<T>(const OpScal<T>&, const T*, const T*, T*, ull*, cudaStream_t);                    \
     template void launch_bi_init1<T>(long, const T*, const T*, T*, const Dots&, ull*, cudaStream_t);                  \
     template void launch_bi_init4<T>(long, const T*, T*, const Dots&, const KState*, ull*, cudaStream_t);             \
-    template void launch_bi_p<T>(long, const T*, const T*, T*, T*, const T*, int, const KState*, ull*, cudaStream_t); \
-    template void launch_bi_s<T>(long, const T*, T*, const Dots&, const KState*, ull*, cudaStream_t);                 \
+    template void launch_bi_p<T>(long, const T*, const T*, T*, T*, const T*, int, KState*, const Dots&, ull*,          \
+                                 cudaStream_t);                                                                       \
+    template void launch_bi_s<T>(long, const T*, T*, KState*, const Dots&, ull*, cudaStream_t);                       \
     template void launch_bi_diag_apply<T>(long, const T*, const T*, int, T*, const KState*, int, ull*, cudaStream_t); \
-    template void launch_bi_xr<T>(long, const T*, const T*, const T*, const T*, T*, T*, const Dots&, const KState*,   \
-                                  ull*, cudaStream_t);                                                                \
+    template void launch_bi_xr<T>(long, const T*, const T*, const T*, const T*, T*, T*, KState*, const Dots&, ull*,   \
+                                  cudaStream_t);                                                                      \
     template void launch_copy<T>(long, const T*, T*, ull*, cudaStream_t);                                            \
     template void launch_norm2_partial<T>(long, const T*, const Dots&, int, ull*, cudaStream_t);
 INST(double)

@@ -104,23 +104,32 @@ void launch_bi_init2(KState* ks, const Dots& d, double tol, int maxit, const KSt
 void launch_bi_init3(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
 template <typename T>
 void launch_bi_init4(long n, const T* r, T* rtld, const Dots& d, const KState* ks, ull* ctr, cudaStream_t s);
-void launch_bi_rho(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
 template <typename T>
-void launch_bi_p(long n, const T* r, const T* v, T* p, T* phat, const T* diag, int ident, const KState* ks, ull* ctr,
-                 cudaStream_t s);
-void launch_bi_alpha(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
+void launch_bi_p(long n, const T* r, const T* v, T* p, T* phat, const T* diag, int ident, KState* ks, const Dots& d,
+                 ull* ctr, cudaStream_t s);
 template <typename T>
-void launch_bi_s(long n, const T* v, T* r, const Dots& d, const KState* ks, ull* ctr, cudaStream_t s);
+void launch_bi_s(long n, const T* v, T* r, KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
 void launch_bi_snorm(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
 template <typename T>
 void launch_bi_diag_apply(long n, const T* x, const T* diag, int ident, T* y, const KState* ks, int gate, ull* ctr,
                           cudaStream_t s);
-void launch_bi_omega(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
 template <typename T>
-void launch_bi_xr(long n, const T* phat, const T* shat, const T* t, const T* rtld, T* x, T* r, const Dots& d,
-                  const KState* ks, ull* ctr, cudaStream_t s);
+void launch_bi_xr(long n, const T* phat, const T* shat, const T* t, const T* rtld, T* x, T* r, KState* ks,
+                  const Dots& d, ull* ctr, cudaStream_t s);
 void launch_bi_end(KState* ks, const Dots& d, cudaGraphConditionalHandle h, int use_graph, ull* ctr, cudaStream_t s);
 void launch_bi_true_resid(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
+void launch_arm_while(const KState* ks, cudaGraphConditionalHandle h, ull* ctr, cudaStream_t s);
+
+// ---- mixed precision: FP32 BiCGSTAB with FP64 reliable updates ---------------------------
+void launch_mr_init(KState* ks, const Dots& d, double tol, int maxit, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_mr_reset(long n, const double* r64, T* r, T* rtld, const Dots& d, const KState* ks, ull* ctr,
+                     cudaStream_t s);
+void launch_mr_end(KState* ks, const Dots& d, cudaGraphConditionalHandle hw, cudaGraphConditionalHandle hif, ull* ctr,
+                   cudaStream_t s);
+template <typename T>
+void launch_mr_fold(long n, T* x32, double* x64, ull* ctr, cudaStream_t s);
+void launch_mr_check(KState* ks, const Dots& d, cudaGraphConditionalHandle hw, ull* ctr, cudaStream_t s);
 
 // ---- vectors ---------------------------------------------------------------------------
 template <typename T>

@@ -75,6 +75,7 @@ struct drd_ctx {
     std::string err;
     int use_graph = 1;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t tev0 = nullptr, tev1 = nullptr;  // autotuner timing
 };
 
 namespace {
@@ -320,28 +321,30 @@ void enq_sys_setup(drd_ctx* c, const Sys& S, cudaStream_t s) {
     if (S.kind == SYS_PHMU) launch_phmu_diag<T>(make_op<T>(c, 0), k.diag, c->ctr, s);
 }
 
-// One BiCGSTAB iteration (lib/BiCGSTABREVCOM.f:257-388).
+// One BiCGSTAB iteration (lib/BiCGSTABREVCOM.f:257-388) up to the X/R update.
+template <typename T>
+void enq_bicg_body(drd_ctx* c, const Sys& S, KVecs<T>& k, KState* ks, cudaStream_t s) {
+    Dots d = dots(c);
+    const long n = S.n;
+    if (S.kind == SYS_CH) {
+        launch_bi_p<T>(n, k.r, k.v, k.p, k.phat, nullptr, 0, ks, d, c->ctr, s);
+        enq_psolve<T>(c, S, k.p, k.phat, ks, G_RUNNING, s);
+    } else {
+        launch_bi_p<T>(n, k.r, k.v, k.p, k.phat, S.jacobi ? k.diag : nullptr, S.ident || !S.jacobi, ks, d, c->ctr, s);
+    }
+    enq_matvec<T>(c, S, T(1), k.phat, T(0), k.v, k.rtld, 0, 4, ks, G_RUNNING, s);
+    launch_bi_s<T>(n, k.v, k.r, ks, d, c->ctr, s);
+    launch_bi_snorm(ks, d, c->ctr, s);
+    enq_psolve<T>(c, S, k.r, k.shat, ks, G_RUNNING, s);
+    enq_matvec<T>(c, S, T(1), k.shat, T(0), k.t, k.r, 1, 6, ks, G_RUNNING, s);
+    launch_bi_xr<T>(n, k.phat, k.shat, k.t, k.rtld, k.x, k.r, ks, d, c->ctr, s);
+}
+
 template <typename T>
 void enq_bicg_iter(drd_ctx* c, const Sys& S, KVecs<T>& k, KState* ks, cudaGraphConditionalHandle h, int use_graph,
                    cudaStream_t s) {
-    Dots d = dots(c);
-    const long n = S.n;
-    launch_bi_rho(ks, d, c->ctr, s);
-    if (S.kind == SYS_CH) {
-        launch_bi_p<T>(n, k.r, k.v, k.p, k.phat, nullptr, 0, ks, c->ctr, s);
-        enq_psolve<T>(c, S, k.p, k.phat, ks, G_RUNNING, s);
-    } else {
-        launch_bi_p<T>(n, k.r, k.v, k.p, k.phat, S.jacobi ? k.diag : nullptr, S.ident || !S.jacobi, ks, c->ctr, s);
-    }
-    enq_matvec<T>(c, S, T(1), k.phat, T(0), k.v, k.rtld, 0, 0, ks, G_RUNNING, s);
-    launch_bi_alpha(ks, d, c->ctr, s);
-    launch_bi_s<T>(n, k.v, k.r, d, ks, c->ctr, s);
-    launch_bi_snorm(ks, d, c->ctr, s);
-    enq_psolve<T>(c, S, k.r, k.shat, ks, G_RUNNING, s);
-    enq_matvec<T>(c, S, T(1), k.shat, T(0), k.t, k.r, 1, 1, ks, G_RUNNING, s);
-    launch_bi_omega(ks, d, c->ctr, s);
-    launch_bi_xr<T>(n, k.phat, k.shat, k.t, k.rtld, k.x, k.r, d, ks, c->ctr, s);
-    launch_bi_end(ks, d, h, use_graph, c->ctr, s);
+    enq_bicg_body<T>(c, S, k, ks, s);
+    launch_bi_end(ks, dots(c), h, use_graph, c->ctr, s);
 }
 
 // Start of the solve with the guess already in k.x (:229-255).
@@ -356,9 +359,10 @@ void enq_bicg_setup(drd_ctx* c, const Sys& S, KVecs<T>& k, KState* ks, double to
     launch_bi_init4<T>(S.n, k.r, k.rtld, d, ks, c->ctr, s);
 }
 
-// Appends a WHILE conditional node to the graph being captured on `s` and captures
-// body(stream, handle) into its body graph on `sb`.
-int capture_while(drd_ctx* c, cudaStream_t s, cudaStream_t sb,
+// Appends a WHILE conditional node looping on state `ks` to the graph being captured on `s`
+// (preceded by a kernel that arms its condition from ks) and captures body(stream, handle)
+// into its body graph on `sb`.
+int capture_while(drd_ctx* c, cudaStream_t s, cudaStream_t sb, const KState* ks,
                   const std::function<void(cudaStream_t, cudaGraphConditionalHandle)>& body) {
     cudaStreamCaptureStatus st;
     cudaGraph_t g = nullptr;
@@ -367,7 +371,9 @@ int capture_while(drd_ctx* c, cudaStream_t s, cudaStream_t sb,
     CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
     if (st != cudaStreamCaptureStatusActive) { c->err = "capture_while: stream not capturing"; return DRD_ERR_CUDA; }
     cudaGraphConditionalHandle h;
-    CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+    launch_arm_while(ks, h, c->ctr, s);
+    CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
     cudaGraphNodeParams p{};
     p.type = cudaGraphNodeTypeConditional;
     p.conditional.handle = h;
@@ -384,6 +390,40 @@ int capture_while(drd_ctx* c, cudaStream_t s, cudaStream_t sb,
     return DRD_OK;
 }
 
+// Creates an IF conditional handle in the graph being captured on `s`.
+int make_if_handle(drd_ctx* c, cudaStream_t s, cudaGraphConditionalHandle* h) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, nullptr, nullptr, nullptr));
+    CK(cudaGraphConditionalHandleCreate(h, g, 0, 0));
+    return DRD_OK;
+}
+
+// Appends an IF conditional node on handle h (set by an already captured kernel) to the graph
+// being captured on `s`, and captures body(stream) into its body graph on `sb`.
+int capture_if(drd_ctx* c, cudaStream_t s, cudaStream_t sb, cudaGraphConditionalHandle h,
+               const std::function<void(cudaStream_t)>& body) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphNodeParams p{};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+    CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraph_t bg = p.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(sb, bg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    body(sb);
+    cudaGraph_t out;
+    CK(cudaStreamEndCapture(sb, &out));
+    return DRD_OK;
+}
+
 // A whole Krylov solve of system S for k64.b with guess k64.x (FP64 result in k64.x).
 // FP64 mode: the reference's BiCGSTAB.  Mixed mode: FP64 iterative refinement around an FP32
 // BiCGSTAB with the same preconditioner.  `ks_slot` receives the status.
@@ -395,31 +435,34 @@ int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int 
     if (!mixed) {
         enq_sys_setup<double>(c, S, s);
         enq_bicg_setup<double>(c, S, k, ks, tol, maxit, nullptr, s);
-        rc = capture_while(c, s, c->s2, [&](cudaStream_t sb, cudaGraphConditionalHandle h) {
+        rc = capture_while(c, s, c->s2, ks, [&](cudaStream_t sb, cudaGraphConditionalHandle h) {
             enq_bicg_iter<double>(c, S, k, ks, h, 1, sb);
         });
         if (rc) return rc;
     } else {
+        // FP32 BiCGSTAB (FP64 inner products) with FP64 reliable updates
         KVecs<float>& f = c->k32;
-        KState* in = c->ks + KS_INNER;
         enq_sys_setup<float>(c, S, s);
+        CK(cudaMemsetAsync(f.x, 0, sizeof(float) * S.n, s));
         launch_copy<double>(S.n, k.b, k.r, c->ctr, s);
         enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.r, nullptr, 1, -1, nullptr, G_ALWAYS, s);
         launch_norm2_partial<double>(S.n, k.b, d, 3, c->ctr, s);
-        launch_mx_init(ks, d, tol, c->P.mixed_max_refine, c->ctr, s);
-        const double itol = c->P.mixed_inner_tol;
-        const int imax = maxit;
-        rc = capture_while(c, s, c->s2, [&](cudaStream_t sb, cudaGraphConditionalHandle ho) {
-            launch_mx_scale<float>(S.n, k.r, ks, f.b, f.x, c->ctr, sb);
-            enq_bicg_setup<float>(c, S, f, in, itol, imax, ks, sb);
-            int rc2 = capture_while(c, sb, c->s3, [&](cudaStream_t si, cudaGraphConditionalHandle hi) {
-                enq_bicg_iter<float>(c, S, f, in, hi, 1, si);
+        launch_mr_init(ks, d, tol, maxit, c->ctr, s);
+        launch_mr_reset<float>(S.n, k.r, f.r, f.rtld, d, ks, c->ctr, s);
+        rc = capture_while(c, s, c->s2, ks, [&](cudaStream_t sb, cudaGraphConditionalHandle hw) {
+            enq_bicg_body<float>(c, S, f, ks, sb);
+            cudaGraphConditionalHandle hif;
+            int rc2 = make_if_handle(c, sb, &hif);
+            if (rc2) { rc = rc2; return; }
+            launch_mr_end(ks, d, hw, hif, c->ctr, sb);
+            rc2 = capture_if(c, sb, c->s3, hif, [&](cudaStream_t su) {
+                launch_mr_fold<float>(S.n, f.x, k.x, c->ctr, su);
+                launch_copy<double>(S.n, k.b, k.r, c->ctr, su);
+                enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.r, nullptr, 1, -1, nullptr, G_ALWAYS, su);
+                launch_mr_check(ks, d, hw, c->ctr, su);
+                launch_mr_reset<float>(S.n, k.r, f.r, f.rtld, d, ks, c->ctr, su);
             });
             if (rc2) rc = rc2;
-            launch_axpy_f2d(S.n, ks, f.x, k.x, c->ctr, sb);
-            launch_copy<double>(S.n, k.b, k.r, c->ctr, sb);
-            enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.r, nullptr, 1, -1, nullptr, G_ALWAYS, sb);
-            launch_mx_check(ks, in, d, ho, 1, c->ctr, sb);
         });
         if (rc) return rc;
     }
@@ -574,12 +617,12 @@ int tune_pass(drd_ctx* c, int zpass) {
                        : gargs<T>(c, nz, nr, nr, t1, nr, mx, nr, t2, nr, nullptr, G_ALWAYS);
         a.ctr = nullptr;
         launch_gemm<T>(cfg, EPI_STORE, a, c->s);  // warm-up
-        cudaEventRecord(c->ev0, c->s);
+        cudaEventRecord(c->tev0, c->s);
         for (int r = 0; r < 5; ++r) launch_gemm<T>(cfg, EPI_STORE, a, c->s);
-        cudaEventRecord(c->ev1, c->s);
-        cudaEventSynchronize(c->ev1);
+        cudaEventRecord(c->tev1, c->s);
+        cudaEventSynchronize(c->tev1);
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        cudaEventElapsedTime(&ms, c->tev0, c->tev1);
         if (cudaGetLastError() != cudaSuccess) continue;
         if (ms < best_ms) { best_ms = ms; best = cfg; }
     }
@@ -665,6 +708,8 @@ int setup_context(drd_ctx* c) {
     CK(cudaStreamCreateWithFlags(&c->s3, cudaStreamNonBlocking));
     CK(cudaEventCreate(&c->ev0));
     CK(cudaEventCreate(&c->ev1));
+    CK(cudaEventCreate(&c->tev0));
+    CK(cudaEventCreate(&c->tev1));
     c->arena_bytes = arena_need(c->cs, c->us, c->vs, c->nc, nr, nz, c->nmax);
     CK(cudaMalloc(&c->arena, c->arena_bytes));
     CK(cudaMemset(c->arena, 0, c->arena_bytes));
@@ -817,6 +862,8 @@ int drd_destroy(drd_ctx* c) {
     if (c->h_mass) cudaFreeHost(c->h_mass);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->tev0) cudaEventDestroy(c->tev0);
+    if (c->tev1) cudaEventDestroy(c->tev1);
     if (c->s) cudaStreamDestroy(c->s);
     if (c->s2) cudaStreamDestroy(c->s2);
     if (c->s3) cudaStreamDestroy(c->s3);
@@ -1103,6 +1150,101 @@ int drd_op_apply(drd_ctx* c, int op, int bdf, int precision, const double* x, do
     CK(cudaMemcpyAsync(y, k.v, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
     CK(cudaStreamSynchronize(c->s));
     CK(cudaGetLastError());
+    return DRD_OK;
+}
+
+int drd_kernel_bench(drd_ctx* c, int which, int reps, double* us, double* bytes, double* flops) {
+    if (!c || which < 0 || which >= DRD_KB_COUNT || reps <= 0 || !us) return DRD_ERR_BADARG;
+    int rc = ensure_tuned(c);
+    if (rc) return rc;
+    const int nr = c->nr, nz = c->nz;
+    Sys S = sys_of(c, SYS_UV, 2);
+    double by = 0.0, fl = 0.0;
+    auto enqueue = [&](cudaStream_t s) {
+        switch (which) {
+            case DRD_KB_UV_MATVEC_FP64:
+                launch_uv_matvec<double>(make_op<double>(c, 2), c->rho, c->eta, c->pen, 1.0, c->k64.p, 0.0, c->k64.v,
+                                         nullptr, 0, dots(c), 0, nullptr, G_ALWAYS, nullptr, s);
+                break;
+            case DRD_KB_UV_MATVEC_FP32:
+                launch_uv_matvec<float>(make_op<float>(c, 2), c->rho32, c->eta32, c->pen32, 1.0f, c->k32.p, 0.0f,
+                                        c->k32.v, nullptr, 0, dots(c), 0, nullptr, G_ALWAYS, nullptr, s);
+                break;
+            case DRD_KB_DCT_X_FP64: {
+                auto a = gargs<double>(c, nz, nr, nr, c->k64.p, nr, c->m1xT, nr, c->t1, nr, nullptr, G_ALWAYS);
+                a.ctr = nullptr;
+                launch_gemm<double>(gcfg<double>(c, 0), EPI_STORE, a, s);
+                break;
+            }
+            case DRD_KB_DCT_X_FP32: {
+                auto a = gargs<float>(c, nz, nr, nr, c->k32.p, nr, c->m1xT32, nr, c->t1f, nr, nullptr, G_ALWAYS);
+                a.ctr = nullptr;
+                launch_gemm<float>(gcfg<float>(c, 0), EPI_STORE, a, s);
+                break;
+            }
+            case DRD_KB_DCT_Z_FP64: {
+                auto a = gargs<double>(c, nz, nr, nz, c->m1z, nz, c->k64.p, nr, c->t1, nr, nullptr, G_ALWAYS);
+                a.ctr = nullptr;
+                launch_gemm<double>(gcfg<double>(c, 1), EPI_STORE, a, s);
+                break;
+            }
+            case DRD_KB_DCT_Z_FP32: {
+                auto a = gargs<float>(c, nz, nr, nz, c->m1z32, nz, c->k32.p, nr, c->t1f, nr, nullptr, G_ALWAYS);
+                a.ctr = nullptr;
+                launch_gemm<float>(gcfg<float>(c, 1), EPI_STORE, a, s);
+                break;
+            }
+            default:
+                launch_ch_matvec<float>(make_op<float>(c, 0), c->M032, c->Mi32, 1.0f, c->k32.p, 0.0f, c->k32.v,
+                                        c->k32.ff1, nullptr, 0, dots(c), 0, nullptr, G_ALWAYS, nullptr, s);
+                break;
+        }
+    };
+    switch (which) {
+        case DRD_KB_UV_MATVEC_FP64: by = 8.0 * (2.0 * S.n + 3.0 * c->cs); fl = 45.0 * S.n; break;
+        case DRD_KB_UV_MATVEC_FP32: by = 4.0 * (2.0 * S.n + 3.0 * c->cs); fl = 45.0 * S.n; break;
+        case DRD_KB_DCT_X_FP64: by = 8.0 * (2.0 * c->nc + (double)nr * nr); fl = 2.0 * nz * (double)nr * nr; break;
+        case DRD_KB_DCT_X_FP32: by = 4.0 * (2.0 * c->nc + (double)nr * nr); fl = 2.0 * nz * (double)nr * nr; break;
+        case DRD_KB_DCT_Z_FP64: by = 8.0 * (2.0 * c->nc + (double)nz * nz); fl = 2.0 * nr * (double)nz * nz; break;
+        case DRD_KB_DCT_Z_FP32: by = 4.0 * (2.0 * c->nc + (double)nz * nz); fl = 2.0 * nr * (double)nz * nz; break;
+        default: by = 4.0 * (3.0 * c->nc + 2.0 * c->cs); fl = 40.0 * c->nc; break;
+    }
+    CK(cudaMemsetAsync(c->k64.p, 0, sizeof(double) * c->nmax, c->s));
+    CK(cudaMemsetAsync(c->k32.p, 0, sizeof(float) * c->nmax, c->s));
+    enqueue(c->s);  // warm-up
+    CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
+    for (int r = 0; r < reps; ++r) enqueue(c->s);
+    cudaGraph_t g;
+    CK(cudaStreamEndCapture(c->s, &g));
+    cudaGraphExec_t ex;
+    CK(cudaGraphInstantiate(&ex, g, 0));
+    cudaGraphDestroy(g);
+    CK(cudaGraphLaunch(ex, c->s));  // warm-up of the graph
+    CK(cudaEventRecord(c->ev0, c->s));
+    CK(cudaGraphLaunch(ex, c->s));
+    CK(cudaEventRecord(c->ev1, c->s));
+    CK(cudaEventSynchronize(c->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    cudaGraphExecDestroy(ex);
+    *us = 1e3 * ms / reps;
+    if (bytes) *bytes = by;
+    if (flops) *flops = fl;
+    return DRD_OK;
+}
+
+int drd_flush_l2(drd_ctx* c, int64_t bytes) {
+    if (!c || bytes < 0) return DRD_ERR_BADARG;
+    static thread_local void* buf = nullptr;
+    static thread_local int64_t have = 0;
+    if (have < bytes) {
+        if (buf) cudaFree(buf);
+        buf = nullptr;
+        have = 0;
+        CK(cudaMalloc(&buf, (size_t)bytes));
+        have = bytes;
+    }
+    CK(cudaMemsetAsync(buf, have & 0xff, (size_t)bytes, c->s));
     return DRD_OK;
 }
 

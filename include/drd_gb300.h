@@ -243,6 +243,23 @@ long drd_op_length(drd_ctx* ctx, int op);
 
 /* ---- performance instrumentation ------------------------------------------------------- */
 
+/* Kernels that drd_kernel_bench can time in isolation on the context's current data. */
+#define DRD_KB_UV_MATVEC_FP64 0   /* MatrixVector_uv_2_CG stencil, FP64                    */
+#define DRD_KB_UV_MATVEC_FP32 1   /* the same in FP32 (mixed mode inner solves)            */
+#define DRD_KB_DCT_X_FP64 2       /* one x-axis DCT-I pass of PSolve_CG (GEMM form), FP64  */
+#define DRD_KB_DCT_X_FP32 3       /* the same in FP32                                       */
+#define DRD_KB_DCT_Z_FP64 4       /* one z-axis DCT-I pass, FP64                            */
+#define DRD_KB_DCT_Z_FP32 5       /* the same in FP32                                       */
+#define DRD_KB_CH_MATVEC_FP32 6   /* MATRIX_VECTOR_CG second stencil pass, FP32             */
+#define DRD_KB_COUNT 7
+/* Launches kernel `which` `reps` times back to back (one captured graph) between CUDA events
+ * on the context stream.  Returns the average device time per launch and the algorithmic
+ * bytes and flops one launch moves / performs (compulsory inputs and outputs only). */
+int drd_kernel_bench(drd_ctx* ctx, int which, int reps, double* us_per_launch, double* bytes_per_launch,
+                     double* flops_per_launch);
+/* Writes `bytes` of scratch memory on the context stream (evicts L2 between timed steps). */
+int drd_flush_l2(drd_ctx* ctx, int64_t bytes);
+
 /* Number of kernels this library has launched on the context (graph nodes counted per
  * execution), cumulative. */
 int64_t drd_kernel_launches(drd_ctx* ctx);

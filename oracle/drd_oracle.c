@@ -32,6 +32,17 @@ static long uv_len(int nr, int nz) { return (long)(nr + 1) * nz + (long)nr * (nz
 
 static double* dalloc(long n) { return (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double)); }
 
+/* The OpenMP build (-DORC_OPENMP, used for the all-cores CPU timing) splits the independent
+ * sequences of a transform across threads; every output is still summed by one thread in
+ * the serial order, so both builds give identical results. */
+#ifdef ORC_OPENMP
+#define ORC_PARALLEL _Pragma("omp parallel")
+#define ORC_FOR _Pragma("omp for schedule(static)")
+#else
+#define ORC_PARALLEL
+#define ORC_FOR
+#endif
+
 /* ---------------------------------------------------------------------------------------
  * BLAS-1 (the MKL routines BiCGSTABREVCOM calls), sequential order.
  * ------------------------------------------------------------------------------------- */
@@ -90,22 +101,28 @@ void orc_vcost(int n, int m, double* x, long seq_stride, long elem_stride) {
     double* in = dalloc(n);
     for (long q = 0; q < period; ++q) tab[q] = cos((double)q * kPimach / (double)(n - 1));
     const double scale = sqrt(2.0 * (n - 1));
-    for (int s = 0; s < m; ++s) {
-        double* xs = x + (long)s * seq_stride;
-        for (int j = 0; j < n; ++j) in[j] = xs[j * elem_stride];
-        for (int i = 0; i < n; ++i) {
-            double acc = in[0] + ((i & 1) ? -in[n - 1] : in[n - 1]);
-            long idx = 0;
-            for (int k = 1; k < n - 1; ++k) {
-                idx += i;
-                if (idx >= period) idx -= period * (idx / period);
-                acc += 2.0 * in[k] * tab[idx];
+    free(in);
+    ORC_PARALLEL
+    {
+        double* buf = dalloc(n);
+        ORC_FOR
+        for (int s = 0; s < m; ++s) {
+            double* xs = x + (long)s * seq_stride;
+            for (int j = 0; j < n; ++j) buf[j] = xs[j * elem_stride];
+            for (int i = 0; i < n; ++i) {
+                double acc = buf[0] + ((i & 1) ? -buf[n - 1] : buf[n - 1]);
+                long idx = 0;
+                for (int k = 1; k < n - 1; ++k) {
+                    idx += i;
+                    if (idx >= period) idx -= period * (idx / period);
+                    acc += 2.0 * buf[k] * tab[idx];
+                }
+                xs[i * elem_stride] = acc / scale;
             }
-            xs[i * elem_stride] = acc / scale;
         }
+        free(buf);
     }
     free(tab);
-    free(in);
 }
 
 /* REDFT10 (DCT-II, FFTW manual): Y_k = 2 sum_{j=0}^{n-1} X_j cos(pi (j+1/2) k / n). */
@@ -115,17 +132,23 @@ void orc_redft10(int n, int m, double* x, long seq_stride, long elem_stride) {
     double* tab = dalloc(period);
     double* in = dalloc(n);
     for (long q = 0; q < period; ++q) tab[q] = cos(kPi * (double)q / (2.0 * n));
-    for (int s = 0; s < m; ++s) {
-        double* xs = x + (long)s * seq_stride;
-        for (int j = 0; j < n; ++j) in[j] = xs[j * elem_stride];
-        for (int k = 0; k < n; ++k) {
-            double acc = 0.0;
-            for (int j = 0; j < n; ++j) acc += in[j] * tab[((long)(2 * j + 1) * k) % period];
-            xs[k * elem_stride] = 2.0 * acc;
+    free(in);
+    ORC_PARALLEL
+    {
+        double* buf = dalloc(n);
+        ORC_FOR
+        for (int s = 0; s < m; ++s) {
+            double* xs = x + (long)s * seq_stride;
+            for (int j = 0; j < n; ++j) buf[j] = xs[j * elem_stride];
+            for (int k = 0; k < n; ++k) {
+                double acc = 0.0;
+                for (int j = 0; j < n; ++j) acc += buf[j] * tab[((long)(2 * j + 1) * k) % period];
+                xs[k * elem_stride] = 2.0 * acc;
+            }
         }
+        free(buf);
     }
     free(tab);
-    free(in);
 }
 
 /* REDFT01 (DCT-III, FFTW manual): Y_k = X_0 + 2 sum_{j=1}^{n-1} X_j cos(pi j (k+1/2) / n). */
@@ -135,17 +158,23 @@ void orc_redft01(int n, int m, double* x, long seq_stride, long elem_stride) {
     double* tab = dalloc(period);
     double* in = dalloc(n);
     for (long q = 0; q < period; ++q) tab[q] = cos(kPi * (double)q / (2.0 * n));
-    for (int s = 0; s < m; ++s) {
-        double* xs = x + (long)s * seq_stride;
-        for (int j = 0; j < n; ++j) in[j] = xs[j * elem_stride];
-        for (int k = 0; k < n; ++k) {
-            double acc = 0.0;
-            for (int j = 1; j < n; ++j) acc += in[j] * tab[((long)j * (2 * k + 1)) % period];
-            xs[k * elem_stride] = in[0] + 2.0 * acc;
+    free(in);
+    ORC_PARALLEL
+    {
+        double* buf = dalloc(n);
+        ORC_FOR
+        for (int s = 0; s < m; ++s) {
+            double* xs = x + (long)s * seq_stride;
+            for (int j = 0; j < n; ++j) buf[j] = xs[j * elem_stride];
+            for (int k = 0; k < n; ++k) {
+                double acc = 0.0;
+                for (int j = 1; j < n; ++j) acc += buf[j] * tab[((long)j * (2 * k + 1)) % period];
+                xs[k * elem_stride] = buf[0] + 2.0 * acc;
+            }
         }
+        free(buf);
     }
     free(tab);
-    free(in);
 }
 
 /* ---------------------------------------------------------------------------------------
@@ -399,19 +428,17 @@ static double bulk_mf(double phi, double psi) {
     return 0.5 * phi * (1.0 - phi) * (1.0 - 2.0 * phi) * aa;
 }
 
-/* PhSolve: microfluidics_complex_domain/PhSolve.f90:1-126. */
-int orc_phsolve(const drd_params* P, const double* ph_lcc, const double* u, const double* v,
-                const double* ph, const double* rmu, const double* bdr_ph, const double* bdr_ph_grad,
-                const double* M0, const double* Mi, double* rmu_after, double* ph_after, drd_status* st) {
+/* RHS of PhSolve (microfluidics_complex_domain/PhSolve.f90:26-63): f2 (CELL), the packed
+ * rhs -f1 + s f2/eps - eps L_Mi(f2) and the packed initial guess rmu. */
+void orc_ch_system(const drd_params* P, const double* u, const double* v, const double* ph, const double* rmu,
+                   const double* bdr_ph, const double* bdr_ph_grad, const double* Mi, double* f2, double* rhs,
+                   double* x0) {
     const int nr = P->nr, nz = P->nz;
     const double dr = P->dr, dz = P->dz, dt = P->dt, eps = P->I_thickness, s = P->s_implicit;
     const double dr2 = dr * dr, dz2 = dz * dz;
-    const long cs = cell_size(nr, nz), n = (long)nr * nz;
+    const long cs = cell_size(nr, nz);
     double* f1 = dalloc(cs);
-    double* f2 = dalloc(cs);
     double* ff = dalloc(cs);
-    double* rhs = dalloc(n);
-    double* x = dalloc(n);
     memcpy(f2, ph, sizeof(double) * cs); /* :26 */
     for (int k = 0; k < nz; ++k)        /* :29-34 */
         for (int i = 0; i < nr; ++i)
@@ -432,7 +459,23 @@ int orc_phsolve(const drd_params* P, const double* ph_lcc, const double* u, cons
             f1[c] = -f1[c] + s * f2[c] / eps - eps * ff[c];
         }
     atob_cell(nr, nz, f1, rhs); /* :62-63 */
-    atob_cell(nr, nz, rmu, x);
+    atob_cell(nr, nz, rmu, x0);
+    free(f1);
+    free(ff);
+}
+
+/* PhSolve: microfluidics_complex_domain/PhSolve.f90:1-126. */
+int orc_phsolve(const drd_params* P, const double* ph_lcc, const double* u, const double* v,
+                const double* ph, const double* rmu, const double* bdr_ph, const double* bdr_ph_grad,
+                const double* M0, const double* Mi, double* rmu_after, double* ph_after, drd_status* st) {
+    const int nr = P->nr, nz = P->nz;
+    const double dr2 = P->dr * P->dr, dz2 = P->dz * P->dz, dt = P->dt;
+    const long cs = cell_size(nr, nz), n = (long)nr * nz;
+    double* f2 = dalloc(cs);
+    double* ff = dalloc(cs);
+    double* rhs = dalloc(n);
+    double* x = dalloc(n);
+    orc_ch_system(P, u, v, ph, rmu, bdr_ph, bdr_ph_grad, Mi, f2, rhs, x);
     ch_ctx C = {P, M0, Mi, ph_lcc};
     int info = orc_bicgstab(n, rhs, x, P->ch_maxit, P->tol, ch_mv_cb, ch_ps_cb, &C, st); /* :72-74 */
     memcpy(rmu_after, rmu, sizeof(double) * cs);
@@ -455,7 +498,7 @@ int orc_phsolve(const drd_params* P, const double* ph_lcc, const double* u, cons
         ph_after[CI(-1, k)] = ph_after[CI(0, k)];
         ph_after[CI(nr, k)] = ph_after[CI(nr - 1, k)];
     }
-    free(f1); free(f2); free(ff); free(rhs); free(x);
+    free(f2); free(ff); free(rhs); free(x);
     return info;
 }
 
@@ -537,21 +580,19 @@ static void phmu_ps_cb(void* c, const double* x, double* y) {
     orc_phmu_psolve(C->P, x, y);
 }
 
-int orc_ph_mu_solve(const drd_params* P, const double* u, const double* v, const double* ph,
-                    const double* rmu, const double* bdr_ph, const double* bdr_ph_used,
-                    const double* bdr_ph_grad, const double* Mi, const double* angleB,
-                    const double* angleT, double* M0, double* ph_after, double* rmu_after,
-                    double* coef_bot_top, drd_status* st) {
+/* RHS of ph_mu_solve (two_phase_flow_complex_domain/ph_mu_solve.f90:31-153): M0 (CELL,
+ * recomputed from phi), packed rhs [f1; f2], packed guess [phi; mu], wall values pnb/pnt and
+ * coef_bot/top. */
+void orc_phmu_system(const drd_params* P, const double* u, const double* v, const double* ph, const double* rmu,
+                     const double* bdr_ph, const double* bdr_ph_used, const double* bdr_ph_grad, const double* angleB,
+                     const double* angleT, double* M0, double* rhs, double* x0, double* pnb, double* pnt,
+                     double* coef_bot_top) {
     const int nr = P->nr, nz = P->nz, mode = P->phi_mode;
     const double dr = P->dr, dz = P->dz, dt = P->dt, eps = P->I_thickness, s = P->s_implicit;
     const double dz2 = dz * dz;
-    const long cs = cell_size(nr, nz), n = 2L * nr * nz;
+    const long cs = cell_size(nr, nz);
     double* f1 = dalloc(cs);
     double* f2 = dalloc(cs);
-    double* rhs = dalloc(n);
-    double* x = dalloc(n);
-    double* pnb = dalloc(nr);
-    double* pnt = dalloc(nr);
     for (long q = 0; q < cs; ++q) { /* :31-35 */
         double p0 = ph[q];
         if (mode == 1) M0[q] = (1.0 - bdr_ph[q]) * (p0 * p0) * ((p0 - 1.0) * (p0 - 1.0));
@@ -595,18 +636,36 @@ int orc_ph_mu_solve(const drd_params* P, const double* u, const double* v, const
         f1[CI(i, nz - 1)] = f1[CI(i, nz - 1)] + pnt[i] * eps / dz2;
     }
     atob_ph_mu(nr, nz, f1, f2, rhs); /* :152-153 */
-    atob_ph_mu(nr, nz, ph, rmu, x);
-    phmu_ctx C = {P, M0, Mi, bdr_ph_used, coef_bot, coef_top};
+    atob_ph_mu(nr, nz, ph, rmu, x0);
+    if (coef_bot_top) { coef_bot_top[0] = coef_bot; coef_bot_top[1] = coef_top; }
+    free(f1);
+    free(f2);
+}
+
+int orc_ph_mu_solve(const drd_params* P, const double* u, const double* v, const double* ph,
+                    const double* rmu, const double* bdr_ph, const double* bdr_ph_used,
+                    const double* bdr_ph_grad, const double* Mi, const double* angleB,
+                    const double* angleT, double* M0, double* ph_after, double* rmu_after,
+                    double* coef_bot_top, drd_status* st) {
+    const int nr = P->nr, nz = P->nz;
+    const long cs = cell_size(nr, nz), n = 2L * nr * nz;
+    double* rhs = dalloc(n);
+    double* x = dalloc(n);
+    double* pnb = dalloc(nr);
+    double* pnt = dalloc(nr);
+    double cbt[2];
+    orc_phmu_system(P, u, v, ph, rmu, bdr_ph, bdr_ph_used, bdr_ph_grad, angleB, angleT, M0, rhs, x, pnb, pnt, cbt);
+    phmu_ctx C = {P, M0, Mi, bdr_ph_used, cbt[0], cbt[1]};
     int info = orc_bicgstab(n, rhs, x, P->phmu_maxit, P->tol, phmu_mv_cb, phmu_ps_cb, &C, st);
     memcpy(ph_after, ph, sizeof(double) * cs);
     memcpy(rmu_after, rmu, sizeof(double) * cs);
     btoa_ph_mu(nr, nz, ph_after, rmu_after, x); /* :173-177 */
     for (int i = 0; i < nr; ++i) {
-        ph_after[CI(i, -1)] = ph_after[CI(i, 0)] * coef_bot + pnb[i];
-        ph_after[CI(i, nz)] = ph_after[CI(i, nz - 1)] * coef_top + pnt[i];
+        ph_after[CI(i, -1)] = ph_after[CI(i, 0)] * cbt[0] + pnb[i];
+        ph_after[CI(i, nz)] = ph_after[CI(i, nz - 1)] * cbt[1] + pnt[i];
     }
-    if (coef_bot_top) { coef_bot_top[0] = coef_bot; coef_bot_top[1] = coef_top; }
-    free(f1); free(f2); free(rhs); free(x); free(pnb); free(pnt);
+    if (coef_bot_top) { coef_bot_top[0] = cbt[0]; coef_bot_top[1] = cbt[1]; }
+    free(rhs); free(x); free(pnb); free(pnt);
     return info;
 }
 

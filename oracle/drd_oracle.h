@@ -53,6 +53,15 @@ void orc_phmu_matvec(const drd_params* P, const double* M0, const double* Mi, co
                      double* y);
 void orc_phmu_psolve(const drd_params* P, const double* x, double* y);
 
+/* RHS builders of the three Krylov systems (packed rhs and initial guess). */
+void orc_ch_system(const drd_params* P, const double* u, const double* v, const double* ph, const double* rmu,
+                   const double* bdr_ph, const double* bdr_ph_grad, const double* Mi, double* f2, double* rhs,
+                   double* x0);
+void orc_phmu_system(const drd_params* P, const double* u, const double* v, const double* ph, const double* rmu,
+                     const double* bdr_ph, const double* bdr_ph_used, const double* bdr_ph_grad, const double* angleB,
+                     const double* angleT, double* M0, double* rhs, double* x0, double* pnb, double* pnt,
+                     double* coef_bot_top);
+
 /* BiCGSTAB of lib/BiCGSTAB.f + lib/BiCGSTABREVCOM.f + lib/STOPTEST2.f. */
 typedef void (*orc_matvec_fn)(void* ctx, double alpha, const double* x, double beta, double* y);
 typedef void (*orc_psolve_fn)(void* ctx, const double* x, double* y);

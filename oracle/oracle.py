@@ -55,6 +55,8 @@ def lib(openmp=False):
         L.orc_uv_psolve.argtypes = [P, C.c_int, dp, dp, dp, dp]
         L.orc_phmu_matvec.argtypes = [P, dp, dp, dp, C.c_double, C.c_double, C.c_double, dp, C.c_double, dp]
         L.orc_phmu_psolve.argtypes = [P, dp, dp]
+        L.orc_ch_system.argtypes = [P, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.orc_phmu_system.argtypes = [P, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_phsolve.argtypes = [P, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, S]
         L.orc_phsolve.restype = C.c_int
         L.orc_ph_mu_solve.argtypes = [P, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, S]
@@ -144,6 +146,42 @@ class Oracle:
         y = np.zeros_like(x)
         self.L.orc_phmu_psolve(C.byref(self.P), ptr(np.ascontiguousarray(x)), ptr(y))
         return y
+
+    # -- systems and residuals -----------------------------------------------------------------
+    def ch_system(self, u, v, ph, rmu, bdr_ph, bdr_ph_grad, Mi):
+        n = self.P.nr * self.P.nz
+        f2, b, x0 = np.zeros_like(ph), np.zeros(n), np.zeros(n)
+        self.L.orc_ch_system(C.byref(self.P), ptr(u), ptr(v), ptr(ph), ptr(rmu), ptr(bdr_ph), ptr(bdr_ph_grad),
+                             ptr(Mi), ptr(f2), ptr(b), ptr(x0))
+        return b, x0, f2
+
+    def ch_residual(self, inputs, coefs, rmu_after):
+        """||b - A x|| / ||b|| of the PhSolve system for a solution field rmu_after (CELL)."""
+        u, v, ph, rmu = inputs
+        b, _, _ = self.ch_system(u, v, ph, rmu, coefs["bdr_ph"], coefs["bdr_ph_grad"], coefs["Mi"])
+        x = np.ascontiguousarray(rmu_after[1:-1, 1:-1]).reshape(-1)
+        r = b - self.ch_matvec(coefs["M0"], coefs["Mi"], x)
+        return float(np.linalg.norm(r) / np.linalg.norm(b))
+
+    def phmu_system(self, u, v, ph, rmu, bdr_ph, bdr_used, bdr_grad, angleB, angleT):
+        nr, nz = self.P.nr, self.P.nz
+        M0 = np.zeros_like(ph)
+        b, x0 = np.zeros(2 * nr * nz), np.zeros(2 * nr * nz)
+        pnb, pnt, cbt = np.zeros(nr), np.zeros(nr), np.zeros(2)
+        self.L.orc_phmu_system(C.byref(self.P), ptr(u), ptr(v), ptr(ph), ptr(rmu), ptr(bdr_ph), ptr(bdr_used),
+                               ptr(bdr_grad), ptr(np.ascontiguousarray(angleB, dtype=np.float64)),
+                               ptr(np.ascontiguousarray(angleT, dtype=np.float64)), ptr(M0), ptr(b), ptr(x0),
+                               ptr(pnb), ptr(pnt), ptr(cbt))
+        return b, x0, M0, cbt
+
+    def phmu_residual(self, inputs, coefs, angleB, angleT, ph_after, rmu_after):
+        """||b - A x|| / ||b|| of the ph_mu_solve system for solution fields (CELL)."""
+        u, v, ph, rmu = inputs
+        b, _, M0, cbt = self.phmu_system(u, v, ph, rmu, coefs["bdr_ph"], coefs["bdr_used"], coefs["bdr_ph_grad"],
+                                         angleB, angleT)
+        x = np.concatenate([ph_after[1:-1, 1:-1].reshape(-1), rmu_after[1:-1, 1:-1].reshape(-1)])
+        r = b - self.phmu_matvec(M0, coefs["Mi"], coefs["bdr_used"], x, cbt[0], cbt[1])
+        return float(np.linalg.norm(r) / np.linalg.norm(b))
 
     # -- per-step routines -------------------------------------------------------------------
     def phsolve(self, u, v, ph, rmu, bdr_ph, bdr_ph_grad, M0, Mi):

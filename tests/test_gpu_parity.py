@@ -197,16 +197,35 @@ def test_velosolve_tight(mf_case, bdf):
 
 
 def test_ph_mu_solve_tight(tp_case):
+    """The Jacobi-preconditioned coupled system is ill-conditioned (about 1400 iterations for a
+    relative residual of 1e-10 and 3200 for 1e-11), so two iterates at residual 1e-10 can differ
+    by cond * 1e-10 in the fields.  Parity is therefore checked on the system itself: the GPU's
+    fields must satisfy the oracle's own discretisation (rhs and operator rebuilt by the
+    oracle from the same inputs) to the tolerance."""
     case, st, t = tp_case
-    ctx, orc = _ctx(case, tol=1e-11)
+    ctx, orc = _ctx(case, tol=1e-10)
     k = case.coefs
     ang = np.full(case.nr + 1, case.params.angle)
-    g = ctx.ph_mu_solve(st[F.F_U], st[F.F_V], st[F.F_PH], st[F.F_RMU], t)
-    o = orc.ph_mu_solve(st[F.F_U], st[F.F_V], st[F.F_PH], st[F.F_RMU], k["bdr_ph"], k["bdr_used"], k["bdr_ph_grad"],
-                        k["Mi"], ang, ang)
+    inputs = (st[F.F_U], st[F.F_V], st[F.F_PH], st[F.F_RMU])
+    g = ctx.ph_mu_solve(*inputs, t)
+    o = orc.ph_mu_solve(*inputs, k["bdr_ph"], k["bdr_used"], k["bdr_ph_grad"], k["Mi"], ang, ang)
     assert g[4].info == 0 and o[4].info == 0
-    assert rel_err(g[0], o[0]) < 1e-8
-    assert rel_err(g[1], o[1]) < 1e-8
+    assert g[4].true_resid <= 1.01e-10
+    assert orc.phmu_residual(inputs, k, ang, ang, g[0], g[1]) <= 1.01e-10
+    assert orc.phmu_residual(inputs, k, ang, ang, o[0], o[1]) <= 1.01e-10
+    assert rel_err(g[2], o[2]) < 1e-14  # ph_M_0 recomputed from phi, no solve involved
+    # ghost rows of phi follow the wall condition from the interior (ph_mu_solve.f90:174-177)
+    assert rel_err(g[0][0, 1:-1] - g[0][1, 1:-1], o[0][0, 1:-1] - o[0][1, 1:-1]) < 1e-3
+    ctx.close()
+
+
+def test_phsolve_solution_satisfies_oracle_system(mf_case):
+    """Residual-based parity at the deck tolerance: the GPU's mu satisfies the oracle's CH system."""
+    case, st, t = mf_case
+    ctx, orc = _ctx(case)
+    inputs = (st[F.F_U], st[F.F_V], st[F.F_PH], st[F.F_RMU])
+    r_g, p_g, s_g = ctx.PhSolve(*inputs, t)
+    assert orc.ch_residual(inputs, case.coefs, r_g) <= 1.01 * case.params.tol
     ctx.close()
 
 
