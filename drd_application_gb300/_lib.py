@@ -38,6 +38,8 @@ SIGNATURES = {
     "drd_step": (C.c_int, [_ctx, C.c_int, C.c_double, C.POINTER(abi.drd_step_stats)]),
     "drd_steps_async": (C.c_int, [_ctx, C.c_int, C.c_double, C.c_int]),
     "drd_synchronize": (C.c_int, [_ctx]),
+    "drd_presolve_2_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_void_p, C.c_void_p,
+                                         C.c_double, C.c_void_p, C.c_void_p]),
     "drd_op_apply": (C.c_int, [_ctx, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     "drd_op_length": (C.c_long, [_ctx, C.c_int]),
     "drd_kernel_bench": (C.c_int, [_ctx, C.c_int, C.c_int, _dp, _dp, _dp]),

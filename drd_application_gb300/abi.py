@@ -19,6 +19,7 @@ DRD_ERR_TIMEOUT = -102
 DRD_ERR_UNSUPPORTED = -103
 DRD_ERR_NONFINITE = -104
 DRD_ERR_NOMEM = -105
+DRD_ERR_TOO_LARGE = -106
 
 DRD_FLAG_EARLY_S = 1
 DRD_FLAG_EARLY_X0 = 2

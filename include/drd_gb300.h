@@ -55,6 +55,7 @@ extern "C" {
 #define DRD_ERR_UNSUPPORTED (-103)
 #define DRD_ERR_NONFINITE (-104)
 #define DRD_ERR_NOMEM (-105)
+#define DRD_ERR_TOO_LARGE (-106)
 
 /* Status flags. */
 #define DRD_FLAG_EARLY_S 1u      /* stopped at the absolute ||s|| <= tol test (BiCGSTABREVCOM.f:313) */
@@ -219,6 +220,27 @@ int drd_step(drd_ctx* ctx, int first, double t, drd_step_stats* stats);
 /* Enqueue `nsteps` steps without host synchronisation (stats are not collected). */
 int drd_steps_async(drd_ctx* ctx, int first, double t, int nsteps);
 int drd_synchronize(drd_ctx* ctx);
+
+/* ---- pressure step without device allocation ------------------------------------------- */
+
+/* Largest grid drd_presolve_2_noalloc accepts. */
+#define DRD_NOALLOC_MAX_CELLS (512 * 256) /* nr * nz */
+#define DRD_NOALLOC_MAX_LINE 1024         /* nr and nz each */
+
+/* The pressure step of drd_presolve_2 for callers that cannot let the library call
+ * cudaMalloc (an application whose device memory all belongs to its own pool allocator, or a
+ * driver issuing the step from code where allocation is not allowed).  No context: u (UFACE),
+ * v (VFACE) and psi (CELL) are device pointers owned by the caller, and the kernels run on
+ * `stream` (a cudaStream_t, NULL for the default stream).  All intermediates live in one
+ * fixed __device__ array of about 3.2 MB, held by every GPU that loads the library until the
+ * process exits; grids beyond DRD_NOALLOC_MAX_* return DRD_ERR_TOO_LARGE.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress) and should therefore
+ * come before any stream capture on that device.  Calls share the array: each call writes
+ * every intermediate before reading it, but calls that overlap on the GPU race on it.
+ * No counterpart in the reference (its PreSolve_2 allocates nothing on a device because it has
+ * none). */
+int drd_presolve_2_noalloc(int nr, int nz, double dr, double dz, const double* u, const double* v, double coef,
+                           double* psi, void* stream);
 
 /* ---- operator access (verification) ---------------------------------------------------- */
 
