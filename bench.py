@@ -324,9 +324,9 @@ def run_gpu(args, ws, rank, local):
         kb[kid] = (us, by, fl)
 
     # e2e through the drop-in C-ABI routines (host arrays)
-    e2e = time_e2e(ctx, case, 1, max(3, K // 4), flush)
+    e2e = time_e2e(ctx, case, W, K, flush)
     e2e_sec = max_over_ranks(dist, e2e["seconds"])
-    e2e_steps = max(3, K // 4)
+    e2e_steps = K
     ctx.close()
 
     # plain FP64 path, resident state

@@ -24,6 +24,15 @@ SIGNATURES = {
     "drd_set_coefs": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, _dp]),
     "drd_set_tp_fields": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
     "drd_interpolate_coef": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
+    "drd_phsolve_ori": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp, _st]),
+    "drd_finit_wall": (C.c_int, [_ctx, _dp, C.c_int, _dp, _dp, _dp]),
+    "drd_particle_params_default": (C.c_int, [C.POINTER(abi.drd_particle_params), C.c_double, C.c_double]),
+    "drd_particle_initialize": (C.c_int, [C.POINTER(abi.drd_particle_params), C.c_double, C.c_double, _dp]),
+    "drd_particles_set": (C.c_int, [_ctx, C.POINTER(abi.drd_particle_params), _dp, _dp]),
+    "drd_particles_get": (C.c_int, [_ctx, _dp, _dp]),
+    "drd_force_caculation_vel": (C.c_int, [_ctx, C.c_double, C.c_double, _dp, _dp]),
+    "drd_update_position_vel": (C.c_int, [_ctx, _dp, _dp, C.c_double]),
+    "drd_interpolate_coef_particles": (C.c_int, [_ctx, _dp, _dp, _dp]),
     "drd_phsolve": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp, _st]),
     "drd_ph_mu_solve": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp, _dp, _dp, _st]),
     "drd_velosolve_combined": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp, _dp, _dp, _dp,
@@ -38,6 +47,15 @@ SIGNATURES = {
     "drd_step": (C.c_int, [_ctx, C.c_int, C.c_double, C.POINTER(abi.drd_step_stats)]),
     "drd_steps_async": (C.c_int, [_ctx, C.c_int, C.c_double, C.c_int]),
     "drd_synchronize": (C.c_int, [_ctx]),
+    "drd_read_deck": (C.c_int, [C.c_char_p, C.POINTER(abi.drd_deck), C.c_char_p, C.c_int]),
+    "drd_params_from_deck": (C.c_int, [C.POINTER(abi.drd_deck), C.c_int, C.c_int, C.c_int,
+                                       C.POINTER(abi.drd_params)]),
+    "drd_output": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double] + [_dp] * 7 + [C.c_double]),
+    "drd_input": (C.c_int, [C.c_char_p, C.c_int, C.c_int] + [_dp] * 7),
+    "drd_read_time": (C.c_int, [C.c_char_p, C.c_int, C.c_int, _dp]),
+    "drd_output_particles": (C.c_int, [C.c_char_p, C.c_int, _dp]),
+    "drd_checkpoint_async": (C.c_int, [_ctx, C.c_char_p, C.c_double]),
+    "drd_checkpoint_wait": (C.c_int, [_ctx]),
     "drd_presolve_2_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_void_p, C.c_void_p,
                                          C.c_double, C.c_void_p, C.c_void_p]),
     "drd_op_apply": (C.c_int, [_ctx, C.c_int, C.c_int, C.c_int, _dp, _dp]),

@@ -53,7 +53,7 @@ class drd_params(C.Structure):
     _fields_ = [
         ("nr", C.c_int32), ("nz", C.c_int32), ("variant", C.c_int32), ("precision", C.c_int32),
         ("phi_mode", C.c_int32), ("lr_bd_type", C.c_int32), ("ch_maxit", C.c_int32),
-        ("uv_maxit", C.c_int32), ("phmu_maxit", C.c_int32), ("reserved0", C.c_int32),
+        ("uv_maxit", C.c_int32), ("phmu_maxit", C.c_int32), ("guess_mode", C.c_int32),
         ("dr", C.c_double), ("dz", C.c_double), ("dt", C.c_double),
         ("xld", C.c_double), ("re", C.c_double), ("ca", C.c_double),
         ("I_thickness", C.c_double), ("s_implicit", C.c_double), ("tol", C.c_double),
@@ -71,6 +71,68 @@ class drd_params(C.Structure):
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_ if not name.startswith("reserved")}
+
+
+PARTICLES_MAX = 64
+
+
+class drd_particle_params(C.Structure):
+    """module particles_params (microfluidics_complex_domain/particles_params.f90)."""
+    _fields_ = [
+        ("np", C.c_int32), ("reserved0", C.c_int32), ("lx", C.c_double), ("ly", C.c_double),
+        ("fpd_radius", C.c_double), ("l0", C.c_double), ("ks", C.c_double), ("kb", C.c_double),
+        ("theta0", C.c_double), ("k0_inter", C.c_double), ("k0_inter_bdr", C.c_double),
+        ("fpd_fpd_dist", C.c_double), ("fpd_bdr_dist", C.c_double),
+    ]
+
+    def copy(self):
+        out = drd_particle_params()
+        C.memmove(C.byref(out), C.byref(self), C.sizeof(drd_particle_params))
+        return out
+
+
+def default_particle_params(lx, ly, np_beads=9):
+    """The reference's fiber parameters (particles_params.f90:74-98), same arithmetic as
+    drd_particle_params_default in the C library."""
+    pp = drd_particle_params()
+    pp.np = np_beads
+    pp.lx, pp.ly = lx, ly
+    pp.fpd_radius = 0.05 / 2.0
+    pp.l0 = 2 * (pp.fpd_radius + 0.00)
+    pp.ks = 5.0
+    pp.kb = 0.0025 * 100
+    pp.theta0 = 0.0
+    pp.k0_inter = 2.5
+    pp.k0_inter_bdr = 2.5 * 10
+    pp.fpd_fpd_dist = pp.fpd_radius + pp.fpd_radius + 0.01
+    pp.fpd_bdr_dist = pp.fpd_radius + 0.02
+    return pp
+
+
+def particle_chain(pp, xc, yc):
+    """particle_initialize's straight vertical chain (particles_move.f90:50-68) as a POINTS
+    array: Np x 2 column-major, returned as shape (2, Np)."""
+    np_ = pp.np
+    pts = [[0.0] * np_, [0.0] * np_]
+    if np_ > 2:
+        mid = np_ // 2
+        pts[0][mid], pts[1][mid] = xc, yc
+        for i in range(mid):
+            pts[0][i], pts[1][i] = xc, yc + (mid - i) * pp.l0
+            pts[0][np_ - i - 1], pts[1][np_ - i - 1] = xc, yc - (mid - i) * pp.l0
+    return pts
+
+
+class drd_deck(C.Structure):
+    """The `input` deck (microfluidics_complex_domain/mcl6.f90:68-99)."""
+    _fields_ = [(n, C.c_double) for n in ("xld", "re", "ca", "vs", "xlsT", "xlsB", "xlsL", "xlsR", "uwT", "uwB",
+                                          "slen", "shig", "angle", "slipratio")] + [
+        ("iflag", C.c_int32), ("istep", C.c_int32)] + [
+        (n, C.c_double) for n in ("tf", "I_thickness", "s_implicit", "tol", "ggz", "ggx", "time_step_change",
+                                  "lambda_rho", "lambda_eta", "UU")] + [
+        (n, C.c_char) for n in ("lr_bd_type", "top_type_ph", "bot_type_ph", "top_type_u", "bot_type_u",
+                                "is_complex_domain")] + [
+        ("pad", C.c_char * 2), ("entries", C.c_int32), ("reserved", C.c_int32)]
 
 
 class drd_status(C.Structure):
@@ -111,8 +173,8 @@ def default_params(nr, nz, **kw):
     p.lambda_rho, p.lambda_eta = 1.0, 100.0
     p.bdr_ph_used_adjust = 1.0e-6
     p.dt = min(p.dr, p.dz) * 0.1
-    p.mixed_inner_tol = 1.0e-4
-    p.mixed_max_refine = 12
+    p.mixed_inner_tol = 3.0e-3
+    p.mixed_max_refine = 16
     for k, v in kw.items():
         if not hasattr(p, k):
             raise AttributeError(f"drd_params has no field {k!r}")

@@ -103,6 +103,72 @@ class DRDContext:
         self._rc(self.L.drd_interpolate_coef(self.h, ptr(dist), ptr(fpd), ptr(rho), ptr(eta)), "interpolate_coef", False)
         return fpd, rho, eta
 
+    # ---- initialisation (finit.f90) -------------------------------------------------------
+    def PhSolve_ori(self, u, v, ph, angleB=None, angleT=None, alpha_s=0.0):
+        """PhSolve_ori(rmu_after, ph_after, t) -> (rmu_after, ph_after, status)."""
+        u, v = _check_shape(u, self.us, "u"), _check_shape(v, self.vs, "v")
+        ph = _check_shape(ph, self.cs, "ph")
+        ang = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (angleB, angleT)]
+        for a in ang:
+            if a is not None and a.shape != (self.nr + 1,):
+                raise ValueError("angle arrays have nr+1 entries")
+        rmu_after, ph_after = np.zeros(self.cs), np.zeros(self.cs)
+        st = abi.drd_status()
+        rc = self.L.drd_phsolve_ori(self.h, ptr(u), ptr(v), ptr(ph), ptr(ang[0]), ptr(ang[1]), alpha_s,
+                                    ptr(rmu_after), ptr(ph_after), C.byref(st))
+        self._rc(rc, "PhSolve_ori")
+        return rmu_after, ph_after, st
+
+    def finit_wall(self, bdr_ph, nsteps=51):
+        """finit's wall smoothing -> (bdr_ph, ph, rmu, info)."""
+        bdr_ph = _check_shape(bdr_ph, self.cs, "bdr_ph")
+        out = [np.zeros(self.cs) for _ in range(3)]
+        rc = self.L.drd_finit_wall(self.h, ptr(bdr_ph), nsteps, *[ptr(a) for a in out])
+        self._rc(rc, "finit_wall")
+        return out[0], out[1], out[2], rc
+
+    # ---- fiber particles (particles_move.f90) --------------------------------------------
+    def particles_set(self, pp, points=None, bdr_dist=None):
+        """Make a bead chain resident (drd_particles_set); points is a (2, Np) array (x row, y
+        row: the column-major Fortran points(0:Np-1,0:1)), bdr_dist a CELL array."""
+        self.pp = pp.copy()
+        pts = None if points is None else np.ascontiguousarray(points, dtype=np.float64)
+        if pts is not None and pts.shape != (2, pp.np):
+            raise ValueError("points has shape (2, np)")
+        bd = _check_shape(bdr_dist, self.cs, "bdr_dist")
+        self._rc(self.L.drd_particles_set(self.h, C.byref(self.pp), ptr(pts), ptr(bd)), "drd_particles_set", False)
+
+    def particles_get(self):
+        """(points, tot_F), both (2, Np)."""
+        n = self.pp.np if getattr(self, "pp", None) is not None else 0
+        pts, tot = np.zeros((2, n)), np.zeros((2, n))
+        self._rc(self.L.drd_particles_get(self.h, ptr(pts), ptr(tot)), "drd_particles_get", False)
+        return pts, tot
+
+    def force_caculation_vel(self, dt, t):
+        """force_caculation_vel -> (particle_force1, particle_force2) CELL arrays."""
+        pf1, pf2 = np.zeros(self.cs), np.zeros(self.cs)
+        self._rc(self.L.drd_force_caculation_vel(self.h, dt, t, ptr(pf1), ptr(pf2)), "force_caculation_vel", False)
+        return pf1, pf2
+
+    def update_position_vel(self, u, v, dt):
+        u, v = _check_shape(u, self.us, "u"), _check_shape(v, self.vs, "v")
+        self._rc(self.L.drd_update_position_vel(self.h, ptr(u), ptr(v), dt), "update_position_vel", False)
+
+    def interpolate_coef_particles(self):
+        """interpolate_coef with fpd_dist of the resident beads -> (fpd_ph, rho, eta)."""
+        fpd, rho, eta = (np.zeros(self.cs) for _ in range(3))
+        self._rc(self.L.drd_interpolate_coef_particles(self.h, ptr(fpd), ptr(rho), ptr(eta)),
+                 "interpolate_coef_particles", False)
+        return fpd, rho, eta
+
+    # ---- checkpoint of the resident state (inout.f90 output) -------------------------------
+    def checkpoint_async(self, path, t):
+        self._rc(self.L.drd_checkpoint_async(self.h, str(path).encode(), t), "drd_checkpoint_async", False)
+
+    def checkpoint_wait(self):
+        self._rc(self.L.drd_checkpoint_wait(self.h), "drd_checkpoint_wait", False)
+
     def PhSolve(self, u, v, ph, rmu, t):
         """PhSolve(rmu_after, ph_after, t) -> (rmu_after, ph_after, status)."""
         u, v = _check_shape(u, self.us, "u"), _check_shape(v, self.vs, "v")

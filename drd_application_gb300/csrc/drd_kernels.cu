@@ -141,10 +141,11 @@ __device__ __forceinline__ double bulk_mf(double phi, double psi) {
 }
 
 // rhs = -f1 + s f2/eps - eps L_Mi(f2) (:37-48) packed by Atob; x0 = Atob(rmu) (:62-63).
+// With rmu_pre non-NULL the guess is extrapolated: 2 rmu - rmu_pre.
 __global__ void k_ch_rhs(DevParams P, const double* __restrict__ ph, const double* __restrict__ rmu,
-                         const double* __restrict__ bdr, const double* __restrict__ grad,
-                         const double* __restrict__ Mi, const double* __restrict__ f2, double* __restrict__ b,
-                         double* __restrict__ x, ull* ctr) {
+                         const double* __restrict__ rmu_pre, const double* __restrict__ bdr,
+                         const double* __restrict__ grad, const double* __restrict__ Mi,
+                         const double* __restrict__ f2, double* __restrict__ b, double* __restrict__ x, ull* ctr) {
     count_launch(ctr);
     const int nr = P.nr, nz = P.nz;
     const long n = (long)nr * nz;
@@ -157,7 +158,7 @@ __global__ void k_ch_rhs(DevParams P, const double* __restrict__ ph, const doubl
         double f1 = P.s * p0 / P.eps - bulk_mf(p0, bdr[c]) / P.eps - p0 * (p0 - 1.0) * grad[c] * P.cang / sq2;
         const double ff = op_dgn<double>(i, k, nr, nz, P.idr2, P.idz2, F, M);
         b[q] = -f1 + P.s * f2[c] / P.eps - P.eps * ff;
-        x[q] = rmu[c];
+        x[q] = rmu_pre ? 2.0 * rmu[c] - rmu_pre[c] : rmu[c];
     }
 }
 
@@ -217,6 +218,163 @@ __global__ void k_ch_fin(DevParams P, const double* __restrict__ x, const double
         const long c = cidx(nr, i, k);
         rmu_after[c] = x[q];
         ph_after[c] = f2[c] + dtxld * op_dgn<double>(i, k, nr, nz, P.idr2, P.idz2, X, M);
+    }
+}
+
+// ======================================================================================
+// PhSolve_ori (microfluidics_complex_domain/PhSolve_ori.f90): phi in [-1,1], unit mobility,
+// wall-energy rows at k = 0 and nz-1; finit repeats it to smooth the wall indicator.  Neumann
+// left/right (laplace_nn, :463-487) and the non-dynamic wall branch (:71-78, :110-118).
+// ======================================================================================
+
+// laplace_nn at (i,k) of a field read through `a` with Neumann ghosts (clamped neighbours).
+// FP64: the reference's (a+ + a- - 2 a0)/h^2; FP32: ((a+ - a0) - (a0 - a-))/h^2.
+template <typename T, class A>
+__device__ __forceinline__ T lap_nn(int i, int k, int nr, int nz, T dr2, T dz2, const A& a) {
+    const T a0 = a(i, k);
+    const T xl = a(i > 0 ? i - 1 : 0, k), xr = a(i < nr - 1 ? i + 1 : nr - 1, k);
+    const T zl = a(i, k > 0 ? k - 1 : 0), zr = a(i, k < nz - 1 ? k + 1 : nz - 1);
+    if constexpr (sizeof(T) == 4) return ((xr - a0) - (a0 - xl)) / dr2 + ((zr - a0) - (a0 - zl)) / dz2;
+    return (xr + xl - 2 * a0) / dr2 + (zr + zl - 2 * a0) / dz2;
+}
+
+// pnb(i) / pnt(i) of the non-dynamic wall branch: (cf cos(tmp pi/2) + alpha_s tmp) / tmp1,
+// tmp the wall-face mean of ph (:44-49, :71-78; :84-89, :110-118).
+__device__ __forceinline__ double ori_wall(double cf, double p_in, double p_gh, double alpha_s, double tmp1) {
+    const double tmp = (p_gh + p_in) / 2.0;
+    double pn = cf * cos(tmp * 3.14159265358979323846264338327950288 / 2) + alpha_s * tmp;
+    return pn / tmp1;
+}
+
+struct OriF1 {  // f1 of :35-39 plus the wall rows, read with Neumann ghosts
+    const double* ph; const double* cfb; const double* cft; int nr, nz; double s, eps, dz2, alpha_s, tmp1;
+    __device__ __forceinline__ double operator()(int i, int k) const {
+        const double p0 = ph[cidx(nr, i, k)];
+        double f = ((1. + s) * p0 - p0 * p0 * p0) / eps;
+        if (k == 0) f = f + ori_wall(cfb[i], p0, ph[cidx(nr, i, -1)], alpha_s, tmp1) * eps / dz2;
+        if (k == nz - 1) f = f + ori_wall(cft[i], p0, ph[cidx(nr, i, nz)], alpha_s, tmp1) * eps / dz2;
+        return f;
+    }
+};
+
+// rhs = Atob(f2 - dt xld laplace_nn(f1)) and x0 = Atob(ph) (:126-138); pnb / pnt stored for
+// the ghost rows of the result.
+__global__ void k_ori_rhs(DevParams P, const double* __restrict__ ph, const double* __restrict__ f2,
+                          const double* __restrict__ cfb, const double* __restrict__ cft, double alpha_s,
+                          double* __restrict__ b, double* __restrict__ x, double* __restrict__ pnb,
+                          double* __restrict__ pnt, ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz;
+    const long n = (long)nr * nz;
+    const double tmp1 = P.eps / P.dz + 0.5 * alpha_s;
+    const OriF1 F{ph, cfb, cft, nr, nz, P.s, P.eps, P.dz2, alpha_s, tmp1};
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        const long c = cidx(nr, i, k);
+        const double ff = lap_nn<double>(i, k, nr, nz, P.dr2, P.dz2, F);
+        b[q] = f2[c] - P.dt * P.xld * ff;
+        x[q] = ph[c];
+        if (k == 0) pnb[i] = ori_wall(cfb[i], ph[c], ph[cidx(nr, i, -1)], alpha_s, tmp1);
+        if (k == nz - 1) pnt[i] = ori_wall(cft[i], ph[c], ph[cidx(nr, i, nz)], alpha_s, tmp1);
+    }
+}
+
+// MATRIX_VECTOR_CG_ori (:368-421), first half: ff1 = -eps laplace_nn(x) + wall rows + s x/eps.
+template <typename T>
+__global__ void k_ori_mv1(OpScal<T> o, const T* __restrict__ x, T* __restrict__ ff1, const KState* ks, int gate,
+                          ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, gate)) return;
+    const int nr = o.nr, nz = o.nz;
+    const long n = (long)nr * nz;
+    PackedA<T> X{x, nr};
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        const T x0 = x[q];
+        T f = -o.eps * lap_nn<T>(i, k, nr, nz, o.dr2, o.dz2, X);
+        if (k == 0) f = f + o.eps / o.dz2 * (x0 - o.cb * x0);       // the ghost equals x(i,0) here
+        if (k == nz - 1) f = f + o.eps / o.dz2 * (x0 - o.ct * x0);
+        ff1[q] = f + x0 * o.s / o.eps;
+    }
+}
+
+// Second half: y = alpha (x - dt xld laplace_nn(ff1)) + beta y, with optional partial dots.
+template <typename T>
+__global__ void k_ori_mv2(OpScal<T> o, const T* __restrict__ x, const T* __restrict__ ff1, T alpha, T beta, T* y,
+                          const T* dot1, int self2, Dots d, int slot1, const KState* ks, int gate, ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, gate)) return;
+    const int nr = o.nr, nz = o.nz;
+    const long n = (long)nr * nz;
+    PackedA<T> F{ff1, nr};
+    double a1 = 0.0, a2 = 0.0;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        const T ff2 = -(o.dtxld * lap_nn<T>(i, k, nr, nz, o.dr2, o.dz2, F));
+        const T av = x[q] + ff2;
+        const T yn = (beta == T(0)) ? alpha * av : alpha * av + beta * y[q];
+        y[q] = yn;
+        if (dot1) a1 += (double)dot1[q] * (double)yn;
+        if (self2) a2 += (double)yn * (double)yn;
+    }
+    if (dot1 != nullptr || self2) emit_partials<DRD_TPB>(a1, a2, dot1 != nullptr, self2, d, slot1);
+}
+
+// ph_after with its ghost rows (:156-173) and rmu_after (:178-201) on the whole CELL array.
+struct OriPh {
+    const double* x; const double* pnb; const double* pnt; int nr, nz; double cb, ct;
+    __device__ __forceinline__ double operator()(int i, int k) const {
+        i = i < 0 ? 0 : (i > nr - 1 ? nr - 1 : i);  // left/right ghost columns copy columns 0 / nr-1
+        if (k < 0) return x[i] * cb + pnb[i];
+        if (k > nz - 1) return x[i + (long)nr * (nz - 1)] * ct + pnt[i];
+        return x[i + (long)nr * k];
+    }
+};
+__global__ void k_ori_fin(DevParams P, const double* __restrict__ x, const double* __restrict__ pnb,
+                          const double* __restrict__ pnt, double cb, double ct, double* __restrict__ ph_after,
+                          double* __restrict__ rmu_after, ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz;
+    const long cs = (long)(nr + 2) * (nz + 2);
+    const OriPh A{x, pnb, pnt, nr, nz, cb, ct};
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < cs; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % (nr + 2)) - 1, k = (int)(q / (nr + 2)) - 1;
+        ph_after[q] = A(i, k);
+        const int si = i < 0 ? 0 : (i > nr - 1 ? nr - 1 : i);
+        const int sk = k < 0 ? 0 : (k > nz - 1 ? nz - 1 : k);
+        const double p0 = A(si, sk);
+        rmu_after[q] = -P.eps * ((A(si + 1, sk) + A(si - 1, sk) - 2 * p0) / P.dr2 +
+                                 (A(si, sk + 1) + A(si, sk - 1) - 2 * p0) / P.dz2) -
+                       p0 / P.eps + p0 * p0 * p0 / P.eps;
+    }
+}
+
+// finit.f90:163-169: rmu from ph and its ghosts on the interior (ghosts left as they are).
+__global__ void k_ori_rmu0(DevParams P, const double* __restrict__ ph, double* __restrict__ rmu, ull* ctr) {
+    count_launch(ctr);
+    const int nr = P.nr, nz = P.nz;
+    const long n = (long)nr * nz;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        const double p0 = ph[cidx(nr, i, k)];
+        rmu[cidx(nr, i, k)] = -P.eps * ((ph[cidx(nr, i + 1, k)] + ph[cidx(nr, i - 1, k)] - 2 * p0) / P.dr2 +
+                                        (ph[cidx(nr, i, k + 1)] + ph[cidx(nr, i, k - 1)] - 2 * p0) / P.dz2) -
+                              p0 / P.eps + p0 * p0 * p0 / P.eps;
+    }
+}
+
+// finit.f90:178-189: bdr_ph = (ph + 1)/2 everywhere, clipped to [0, 1] on the interior.
+__global__ void k_ori_bdr(int nr, int nz, const double* __restrict__ ph, double* __restrict__ bdr, ull* ctr) {
+    count_launch(ctr);
+    const long cs = (long)(nr + 2) * (nz + 2);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < cs; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % (nr + 2)) - 1, k = (int)(q / (nr + 2)) - 1;
+        double b = (ph[q] + 1.0) / 2.0;
+        if (i >= 0 && i < nr && k >= 0 && k < nz) {
+            if (b >= 1.0) b = 1.0;
+            else if (b <= 0.0) b = 0.0;
+        }
+        bdr[q] = b;
     }
 }
 
@@ -282,6 +440,7 @@ __device__ __forceinline__ double bulk_tp(double phi, double psi, int mode) {
 // rhs [f1; f2] (:55-153) with the wall terms of ch_bdr_condition (:108-149); cfB/cfT hold
 // cos(angle pi/180)/sqrt(2) per column.
 __global__ void k_phmu_rhs(DevParams P, const double* __restrict__ ph, const double* __restrict__ rmu,
+                           const double* __restrict__ ph_pre, const double* __restrict__ rmu_pre,
                            const double* __restrict__ bdr, const double* __restrict__ grad,
                            const double* __restrict__ f2, const double* __restrict__ cfB,
                            const double* __restrict__ cfT, double* __restrict__ b, double* __restrict__ x,
@@ -313,8 +472,8 @@ __global__ void k_phmu_rhs(DevParams P, const double* __restrict__ ph, const dou
         }
         b[q] = f1;
         b[q + n] = f2[c];
-        x[q] = p0;
-        x[q + n] = rmu[c];
+        x[q] = ph_pre ? 2.0 * p0 - ph_pre[c] : p0;
+        x[q + n] = rmu_pre ? 2.0 * rmu[c] - rmu_pre[c] : rmu[c];
     }
 }
 
@@ -403,7 +562,7 @@ __global__ void k_uv_rhs(DevParams P, int bdf, const CallArgs* __restrict__ ca, 
                          const double* __restrict__ used, const double* __restrict__ ph,
                          const double* __restrict__ rmu, const double* __restrict__ pf1,
                          const double* __restrict__ pf2, double* __restrict__ b, double* __restrict__ x,
-                         double* __restrict__ uL, ull* ctr) {
+                         double* __restrict__ uL, int extrap, ull* ctr) {
     count_launch(ctr);
     const int nr = P.nr, nz = P.nz;
     const long mn = (long)(nr + 1) * nz, N = mn + (long)nr * (nz - 1);
@@ -454,7 +613,7 @@ __global__ void k_uv_rhs(DevParams P, int bdf, const CallArgs* __restrict__ ca, 
                 fu = fu + dt * (2.0 * P.uwT / P.dz2 * etay);
             }
             b[q] = fu;
-            x[q] = uu;
+            x[q] = extrap ? 2.0 * uu - u_pre[uidx(nr, i, k)] : uu;
         } else {
             const long qv = q - mn;
             const int i = (int)(qv % nr), k = (int)(qv / nr) + 1;
@@ -475,7 +634,7 @@ __global__ void k_uv_rhs(DevParams P, int bdf, const CallArgs* __restrict__ ca, 
             fv = fv + (C_(pf2, i, k) + C_(pf2, i, k - 1)) / 2.0;
             fv = fv * dt;
             b[q] = fv;
-            x[q] = vv;
+            x[q] = extrap ? 2.0 * vv - v_pre[vidx(nr, i, k)] : vv;
         }
     }
 #undef UT
@@ -714,6 +873,42 @@ __global__ void k_mass_final(Dots d, int slot, double drdz, double* out, ull* ct
 // preconditioner and the pressure solve applied one axis at a time.  Tiles BM x BN x BK,
 // each thread TM x TN outputs strided by the thread grid (coalesced loads and stores).
 // ======================================================================================
+// Operand loads and output placement shared by the transform GEMMs (see GemmArgs::fold).
+template <typename T>
+struct GemmView {
+    const T* A; const T* B; int M, N, par;
+    __device__ __forceinline__ GemmView(const GemmArgs<T>& a, int p) : par(p) {
+        A = (a.fold == FOLD_B && p) ? a.A_odd : a.A;
+        B = (a.fold == FOLD_A && p) ? a.B_odd : a.B;
+        M = (a.fold == FOLD_B && p) ? a.M_odd : a.M;
+        N = (a.fold == FOLD_A && p) ? a.N_odd : a.N;
+    }
+    __device__ __forceinline__ T loadA(const GemmArgs<T>& a, int m, int k, int kend) const {
+        if (m >= M || k >= kend) return T(0);
+        if (a.fold != FOLD_A) return A[(long)m * a.lda + k];
+        const T* row = A + (long)m * a.lda;
+        if (2 * k == a.Lf) return par ? T(0) : row[k];
+        return par ? row[k] - row[a.Lf - k] : row[k] + row[a.Lf - k];
+    }
+    __device__ __forceinline__ T loadB(const GemmArgs<T>& a, int k, int n, int kend) const {
+        if (n >= N || k >= kend) return T(0);
+        if (a.fold != FOLD_B) return B[(long)k * a.ldb + n];
+        if (2 * k == a.Lf) return par ? T(0) : B[(long)k * a.ldb + n];
+        const T x0 = B[(long)k * a.ldb + n], x1 = B[(long)(a.Lf - k) * a.ldb + n];
+        return par ? x0 - x1 : x0 + x1;
+    }
+    __device__ __forceinline__ int orow(const GemmArgs<T>& a, int m) const { return a.fold == FOLD_B ? 2 * m + par : m; }
+    __device__ __forceinline__ int ocol(const GemmArgs<T>& a, int n) const { return a.fold == FOLD_A ? 2 * n + par : n; }
+};
+
+template <typename T, int EPI>
+__device__ __forceinline__ void gemm_store(const GemmArgs<T>& a, int gm, int gn, T v, double coef) {
+    if (EPI == EPI_STORE) a.C[(long)gm * a.ldc + gn] = v;
+    else if (EPI == EPI_DIV_TAB) a.C[(long)gm * a.ldc + gn] = v / a.tab[(long)gm * a.ldt + gn];
+    else if (EPI == EPI_SCALE) a.C[(long)gm * a.ldc + gn] = v * (T)a.scale;
+    else a.C[cidx(a.nr, gn, gm)] = (T)(((double)v / a.scale) * coef);
+}
+
 template <typename T, int BM, int BN, int BK, int TM, int TN, int EPI>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm(GemmArgs<T> a) {
     constexpr int NT = (BM / TM) * (BN / TN);
@@ -722,8 +917,10 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm(GemmArgs<T> a) {
     __shared__ T Bs[BK][BN];
     count_launch(a.ctr);
     if (gate_closed(a.ks, a.gate)) return;
+    const GemmView<T> g(a, a.fold ? (int)blockIdx.z : 0);
     const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    if (m0 >= g.M || n0 >= g.N) return;
     T acc[TM][TN];
 #pragma unroll
     for (int i = 0; i < TM; ++i)
@@ -733,14 +930,12 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm(GemmArgs<T> a) {
 #pragma unroll
         for (int e = tid; e < BM * BK; e += NT) {
             const int r = e / BK, c = e % BK;
-            const int gm = m0 + r, gk = k0 + c;
-            As[c][r] = (gm < a.M && gk < a.K) ? a.A[(long)gm * a.lda + gk] : T(0);
+            As[c][r] = g.loadA(a, m0 + r, k0 + c, a.K);
         }
 #pragma unroll
         for (int e = tid; e < BK * BN; e += NT) {
             const int r = e / BN, c = e % BN;
-            const int gk = k0 + r, gn = n0 + c;
-            Bs[r][c] = (gk < a.K && gn < a.N) ? a.B[(long)gk * a.ldb + gn] : T(0);
+            Bs[r][c] = g.loadB(a, k0 + r, n0 + c, a.K);
         }
         __syncthreads();
 #pragma unroll
@@ -761,16 +956,12 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm(GemmArgs<T> a) {
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
         const int gm = m0 + ty + i * TY;
-        if (gm >= a.M) continue;
+        if (gm >= g.M) continue;
 #pragma unroll
         for (int j = 0; j < TN; ++j) {
             const int gn = n0 + tx + j * TX;
-            if (gn >= a.N) continue;
-            const T v = acc[i][j];
-            if (EPI == EPI_STORE) a.C[(long)gm * a.ldc + gn] = v;
-            else if (EPI == EPI_DIV_TAB) a.C[(long)gm * a.ldc + gn] = v / a.tab[(long)gm * a.ldt + gn];
-            else if (EPI == EPI_SCALE) a.C[(long)gm * a.ldc + gn] = v * (T)a.scale;
-            else a.C[cidx(a.nr, gn, gm)] = (T)(((double)v / a.scale) * coef);
+            if (gn >= g.N) continue;
+            gemm_store<T, EPI>(a, g.orow(a, gm), g.ocol(a, gn), acc[i][j], coef);
         }
     }
 }
@@ -792,8 +983,10 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm_sk(GemmArgs<T> a
     if (gate_closed(a.ks, a.gate)) return;  // uniform over the cluster: the state is not written here
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
+    const GemmView<T> g(a, a.fold ? (int)(blockIdx.z / KS) : 0);
     const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const bool live = m0 < g.M && n0 < g.N;  // uniform over the cluster (same tile, same parity)
     const int kchunk = ((a.K + KS * BK - 1) / (KS * BK)) * BK;
     const int kbeg = rank * kchunk, kend = min(a.K, kbeg + kchunk);
     T acc[TM][TN];
@@ -807,20 +1000,16 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm_sk(GemmArgs<T> a
 #pragma unroll
         for (int l = 0; l < LA; ++l) {
             const int e = tid + l * NT;
-            const int r = e / BK, c = e % BK;
-            const int gm = m0 + r, gk = k0 + c;
-            ra[l] = (e < BM * BK && gm < a.M && gk < kend) ? a.A[(long)gm * a.lda + gk] : T(0);
+            ra[l] = (e < BM * BK) ? g.loadA(a, m0 + e / BK, k0 + e % BK, kend) : T(0);
         }
 #pragma unroll
         for (int l = 0; l < LB; ++l) {
             const int e = tid + l * NT;
-            const int r = e / BN, c = e % BN;
-            const int gk = k0 + r, gn = n0 + c;
-            rb[l] = (e < BK * BN && gk < kend && gn < a.N) ? a.B[(long)gk * a.ldb + gn] : T(0);
+            rb[l] = (e < BK * BN) ? g.loadB(a, k0 + e / BN, n0 + e % BN, kend) : T(0);
         }
     };
-    if (kbeg < kend) gload(kbeg);
-    for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    if (live && kbeg < kend) gload(kbeg);
+    for (int k0 = kbeg; live && k0 < kend; k0 += BK) {
 #pragma unroll
         for (int l = 0; l < LA; ++l) {
             const int e = tid + l * NT;
@@ -854,18 +1043,13 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm_sk(GemmArgs<T> a
     cluster.sync();
     const double coef = (EPI == EPI_PRE_FINAL) ? a.ca->coef : 0.0;
     constexpr int RB = BM / KS;
-    for (int e = tid; e < RB * BN; e += NT) {
+    for (int e = tid; live && e < RB * BN; e += NT) {
         const int r = rank * RB + e / BN, c = e % BN;
         const int gm = m0 + r, gn = n0 + c;
         T v = T(0);
 #pragma unroll
         for (int q = 0; q < KS; ++q) v += cluster.map_shared_rank(&Cs[0][0], q)[r * (BN + 1) + c];
-        if (gm < a.M && gn < a.N) {
-            if (EPI == EPI_STORE) a.C[(long)gm * a.ldc + gn] = v;
-            else if (EPI == EPI_DIV_TAB) a.C[(long)gm * a.ldc + gn] = v / a.tab[(long)gm * a.ldt + gn];
-            else if (EPI == EPI_SCALE) a.C[(long)gm * a.ldc + gn] = v * (T)a.scale;
-            else a.C[cidx(a.nr, gn, gm)] = (T)(((double)v / a.scale) * coef);
-        }
+        if (gm < g.M && gn < g.N) gemm_store<T, EPI>(a, g.orow(a, gm), g.ocol(a, gn), v, coef);
     }
     cluster.sync();  // keep every CTA's partial tile alive until all readers are done
 }
@@ -882,7 +1066,7 @@ template <typename T, int BM, int BN, int TM, int TN, int KS, int EPI>
 static void gemm_sk_launch(const GemmArgs<T>& a, cudaStream_t s) {
     constexpr int NT = (BM / TM) * (BN / TN);
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((a.N + BN - 1) / BN, (a.M + BM - 1) / BM, KS);
+    cfg.gridDim = dim3((a.N + BN - 1) / BN, (a.M + BM - 1) / BM, KS * (a.fold ? 2 : 1));
     cfg.blockDim = dim3(NT, 1, 1);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
@@ -908,7 +1092,7 @@ static void gemm_sk_dispatch(int epi, const GemmArgs<T>& a, cudaStream_t s) {
 
 template <typename T, int BM, int BN, int TM, int TN>
 static void gemm_dispatch_epi(int epi, const GemmArgs<T>& a, cudaStream_t s) {
-    dim3 grid((a.N + BN - 1) / BN, (a.M + BM - 1) / BM);
+    dim3 grid((a.N + BN - 1) / BN, (a.M + BM - 1) / BM, a.fold ? 2 : 1);
     constexpr int NT = (BM / TM) * (BN / TN);
     switch (epi) {
         case EPI_STORE: k_gemm<T, BM, BN, 16, TM, TN, EPI_STORE><<<grid, NT, 0, s>>>(a); break;
@@ -1483,9 +1667,10 @@ void launch_ch_f2(const DevParams& P, const double* u, const double* v, const do
                   cudaStream_t s) {
     k_ch_f2<<<GRID((long)(P.nr + 2) * (P.nz + 2))>>>(P, u, v, ph, f2, ctr);
 }
-void launch_ch_rhs(const DevParams& P, const double* ph, const double* rmu, const double* bdr, const double* grad,
-                   const double* Mi, const double* f2, double* b, double* x, ull* ctr, cudaStream_t s) {
-    k_ch_rhs<<<GRID((long)P.nr * P.nz)>>>(P, ph, rmu, bdr, grad, Mi, f2, b, x, ctr);
+void launch_ch_rhs(const DevParams& P, const double* ph, const double* rmu, const double* rmu_pre, const double* bdr,
+                   const double* grad, const double* Mi, const double* f2, double* b, double* x, ull* ctr,
+                   cudaStream_t s) {
+    k_ch_rhs<<<GRID((long)P.nr * P.nz)>>>(P, ph, rmu, rmu_pre, bdr, grad, Mi, f2, b, x, ctr);
 }
 template <typename T>
 void launch_ch_matvec(const OpScal<T>& o, const T* M0, const T* Mi, T alpha, const T* x, T beta, T* y, T* ff1,
@@ -1504,15 +1689,37 @@ void launch_ch_fin(const DevParams& P, const double* x, const double* f2, const 
 void launch_fill_neumann(int nr, int nz, double* a, double* b, ull* ctr, cudaStream_t s) {
     k_fill_neumann<<<GRID(2L * (nr + 2) + 2L * nz)>>>(nr, nz, a, b, ctr);
 }
+void launch_ori_rhs(const DevParams& P, const double* ph, const double* f2, const double* cfb, const double* cft,
+                    double alpha_s, double* b, double* x, double* pnb, double* pnt, ull* ctr, cudaStream_t s) {
+    k_ori_rhs<<<GRID((long)P.nr * P.nz)>>>(P, ph, f2, cfb, cft, alpha_s, b, x, pnb, pnt, ctr);
+}
+template <typename T>
+void launch_ori_matvec(const OpScal<T>& o, T alpha, const T* x, T beta, T* y, T* ff1, const T* dot1, int self2,
+                       const Dots& d, int slot1, const KState* ks, int gate, ull* ctr, cudaStream_t s) {
+    const long n = (long)o.nr * o.nz;
+    k_ori_mv1<T><<<GRID(n)>>>(o, x, ff1, ks, gate, ctr);
+    const int g = (dot1 || self2) ? d.G : grid_for(n);
+    k_ori_mv2<T><<<g, DRD_TPB, 0, s>>>(o, x, ff1, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);
+}
+void launch_ori_fin(const DevParams& P, const double* x, const double* pnb, const double* pnt, double cb, double ct,
+                    double* ph_after, double* rmu_after, ull* ctr, cudaStream_t s) {
+    k_ori_fin<<<GRID((long)(P.nr + 2) * (P.nz + 2))>>>(P, x, pnb, pnt, cb, ct, ph_after, rmu_after, ctr);
+}
+void launch_ori_rmu0(const DevParams& P, const double* ph, double* rmu, ull* ctr, cudaStream_t s) {
+    k_ori_rmu0<<<GRID((long)P.nr * P.nz)>>>(P, ph, rmu, ctr);
+}
+void launch_ori_bdr(int nr, int nz, const double* ph, double* bdr, ull* ctr, cudaStream_t s) {
+    k_ori_bdr<<<GRID((long)(nr + 2) * (nz + 2))>>>(nr, nz, ph, bdr, ctr);
+}
 
 void launch_phmu_prep(const DevParams& P, const double* u, const double* v, const double* ph, const double* bdr,
                       const double* used, double* M0, double* f2, ull* ctr, cudaStream_t s) {
     k_phmu_prep<<<GRID((long)(P.nr + 2) * (P.nz + 2))>>>(P, u, v, ph, bdr, used, M0, f2, ctr);
 }
-void launch_phmu_rhs(const DevParams& P, const double* ph, const double* rmu, const double* bdr, const double* grad,
-                     const double* f2, const double* cfB, const double* cfT, double* b, double* x, double* pnb,
-                     double* pnt, ull* ctr, cudaStream_t s) {
-    k_phmu_rhs<<<GRID((long)P.nr * P.nz)>>>(P, ph, rmu, bdr, grad, f2, cfB, cfT, b, x, pnb, pnt, ctr);
+void launch_phmu_rhs(const DevParams& P, const double* ph, const double* rmu, const double* ph_pre,
+                     const double* rmu_pre, const double* bdr, const double* grad, const double* f2, const double* cfB,
+                     const double* cfT, double* b, double* x, double* pnb, double* pnt, ull* ctr, cudaStream_t s) {
+    k_phmu_rhs<<<GRID((long)P.nr * P.nz)>>>(P, ph, rmu, ph_pre, rmu_pre, bdr, grad, f2, cfB, cfT, b, x, pnb, pnt, ctr);
 }
 template <typename T>
 void launch_phmu_matvec(const OpScal<T>& o, const T* M0, const T* Mi, const T* used, T alpha, const T* x, T beta, T* y,
@@ -1535,10 +1742,10 @@ void launch_uv_rhs(const DevParams& P, int bdf, const CallArgs* ca, const double
                    const double* u_pre, const double* u, const double* v_pre, const double* v, const double* p,
                    const double* rho, const double* eta, const double* bdr, const double* used, const double* ph_after,
                    const double* rmu_after, const double* pf1, const double* pf2, double* b, double* x, double* uL,
-                   ull* ctr, cudaStream_t s) {
+                   int extrap, ull* ctr, cudaStream_t s) {
     const long N = (long)(P.nr + 1) * P.nz + (long)P.nr * (P.nz - 1);
     k_uv_rhs<<<GRID(N)>>>(P, bdf, ca, psi1, psi2, u_pre, u, v_pre, v, p, rho, eta, bdr, used, ph_after, rmu_after, pf1,
-                          pf2, b, x, uL, ctr);
+                          pf2, b, x, uL, extrap, ctr);
 }
 template <typename T>
 void launch_uv_matvec(const OpScal<T>& o, const T* rho, const T* eta, const T* pen, T alpha, const T* x, T beta, T* y,
@@ -1676,6 +1883,8 @@ template void launch_mx_scale<float>(long, const double*, const KState*, float*,
 #define INST(T)                                                                                                        \
     template void launch_ch_matvec<T>(const OpScal<T>&, const T*, const T*, T, const T*, T, T*, T*, const T*, int,     \
                                       const Dots&, int, const KState*, int, ull*, cudaStream_t);                      \
+    template void launch_ori_matvec<T>(const OpScal<T>&, T, const T*, T, T*, T*, const T*, int, const Dots&, int,      \
+                                       const KState*, int, ull*, cudaStream_t);                                       \
     template void launch_phmu_matvec<T>(const OpScal<T>&, const T*, const T*, const T*, T, const T*, T, T*, const T*,  \
                                         int, const Dots&, int, const KState*, int, ull*, cudaStream_t);               \
     template void launch_phmu_diag<T>(const OpScal<T>&, T*, ull*, cudaStream_t);                                      \

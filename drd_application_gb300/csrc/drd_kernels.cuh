@@ -39,7 +39,15 @@ struct GemmArgs {
     int nr;
     const KState* ks; int gate;
     ull* ctr;
+    // DCT-I even/odd folding (C[o][L-j] = (-1)^o C[o][j]): the output parity is blockIdx.z
+    // (split-K: blockIdx.z / KS).  FOLD_A: A is the data X (lda), loaded as X[m][j] +- X[m][L-j],
+    // B / B_odd the even / odd-column matrices, N / N_odd their widths, output column 2n+p.
+    // FOLD_B: B is the data, loaded as X[j][n] +- X[L-j][n], A / A_odd the even / odd-row
+    // matrices, M / M_odd their heights, output row 2m+p.  K is floor(L/2)+1.
+    int fold; int Lf;
+    const T* A_odd; const T* B_odd; int M_odd, N_odd;
 };
+enum Fold : int { FOLD_NONE = 0, FOLD_A = 1, FOLD_B = 2 };
 int gemm_config_count();
 const char* gemm_config_name(int cfg);
 template <typename T>
@@ -47,8 +55,9 @@ void launch_gemm(int cfg, int epi, const GemmArgs<T>& a, cudaStream_t s);
 
 // ---- CH (microfluidics_complex_domain/PhSolve.f90) -------------------------------------
 void launch_ch_f2(const DevParams& P, const double* u, const double* v, const double* ph, double* f2, ull* ctr, cudaStream_t s);
-void launch_ch_rhs(const DevParams& P, const double* ph, const double* rmu, const double* bdr, const double* grad,
-                   const double* Mi, const double* f2, double* b, double* x, ull* ctr, cudaStream_t s);
+void launch_ch_rhs(const DevParams& P, const double* ph, const double* rmu, const double* rmu_pre, const double* bdr,
+                   const double* grad, const double* Mi, const double* f2, double* b, double* x, ull* ctr,
+                   cudaStream_t s);
 template <typename T>
 void launch_ch_matvec(const OpScal<T>& o, const T* M0, const T* Mi, T alpha, const T* x, T beta, T* y, T* ff1,
                       const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,
@@ -56,12 +65,23 @@ void launch_ch_matvec(const OpScal<T>& o, const T* M0, const T* Mi, T alpha, con
 void launch_ch_fin(const DevParams& P, const double* x, const double* f2, const double* M0, double* rmu_after,
                    double* ph_after, ull* ctr, cudaStream_t s);
 
+// ---- PhSolve_ori (microfluidics_complex_domain/PhSolve_ori.f90), finit's wall smoothing ---
+void launch_ori_rhs(const DevParams& P, const double* ph, const double* f2, const double* cfb, const double* cft,
+                    double alpha_s, double* b, double* x, double* pnb, double* pnt, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_ori_matvec(const OpScal<T>& o, T alpha, const T* x, T beta, T* y, T* ff1, const T* dot1, int self2,
+                       const Dots& d, int slot1, const KState* ks, int gate, ull* ctr, cudaStream_t s);
+void launch_ori_fin(const DevParams& P, const double* x, const double* pnb, const double* pnt, double cb, double ct,
+                    double* ph_after, double* rmu_after, ull* ctr, cudaStream_t s);
+void launch_ori_rmu0(const DevParams& P, const double* ph, double* rmu, ull* ctr, cudaStream_t s);
+void launch_ori_bdr(int nr, int nz, const double* ph, double* bdr, ull* ctr, cudaStream_t s);
+
 // ---- coupled CH (two_phase_flow_complex_domain/ph_mu_solve.f90) -----------------------
 void launch_phmu_prep(const DevParams& P, const double* u, const double* v, const double* ph, const double* bdr,
                       const double* used, double* M0, double* f2, ull* ctr, cudaStream_t s);
-void launch_phmu_rhs(const DevParams& P, const double* ph, const double* rmu, const double* bdr, const double* grad,
-                     const double* f2, const double* cfB, const double* cfT, double* b, double* x, double* pnb,
-                     double* pnt, ull* ctr, cudaStream_t s);
+void launch_phmu_rhs(const DevParams& P, const double* ph, const double* rmu, const double* ph_pre,
+                     const double* rmu_pre, const double* bdr, const double* grad, const double* f2, const double* cfB,
+                     const double* cfT, double* b, double* x, double* pnb, double* pnt, ull* ctr, cudaStream_t s);
 template <typename T>
 void launch_phmu_matvec(const OpScal<T>& o, const T* M0, const T* Mi, const T* used, T alpha, const T* x, T beta, T* y,
                         const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,
@@ -76,7 +96,7 @@ void launch_uv_rhs(const DevParams& P, int bdf, const CallArgs* ca, const double
                    const double* u_pre, const double* u, const double* v_pre, const double* v, const double* p,
                    const double* rho, const double* eta, const double* bdr, const double* used, const double* ph_after,
                    const double* rmu_after, const double* pf1, const double* pf2, double* b, double* x, double* uL,
-                   ull* ctr, cudaStream_t s);
+                   int extrap, ull* ctr, cudaStream_t s);
 template <typename T>
 void launch_uv_matvec(const OpScal<T>& o, const T* rho, const T* eta, const T* pen, T alpha, const T* x, T beta, T* y,
                       const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,
@@ -94,6 +114,24 @@ void launch_cell_add(long n, const double* x, double* y, ull* ctr, cudaStream_t 
 // ---- interpolate_coef / mass ----------------------------------------------------------
 void launch_interp_coef(const DevParams& P, const double* dist, const double* bdr, double* fpd, double* rho, double* eta,
                         ull* ctr, cudaStream_t s);
+
+// ---- fiber particles (microfluidics_complex_domain/particles_move.f90), drd_particles.cu --
+constexpr int PT_GX = 64;  // blocks per bead in the per-bead sums
+struct PartParams {
+    int np, nr, nz, pad;
+    double lx, ly, radius, l0, ks, kb, theta0, k0, k0b, eq_pp, eq_bdr;
+    double dr, dz, eps, dt, lambda_rho, lambda_eta;
+    double skip_d2;  // (radius + 20 sqrt(2) eps)^2: beyond it the bead indicator is < 4.3e-18
+};
+void launch_pt_force(const PartParams& Q, double* pts, double* pts_old, double* totF, const double* bdist, ull* ctr,
+                     cudaStream_t s);
+void launch_pt_sums(const PartParams& Q, const double* pts, const double* u, const double* v, double* part, ull* ctr,
+                    cudaStream_t s);
+void launch_pt_finish(const PartParams& Q, const double* part, double* psum, double* pts, int move, ull* ctr,
+                      cudaStream_t s);
+void launch_pt_spread(const PartParams& Q, int mode, const double* pts_old, const double* pts, const double* totF,
+                      const double* psum, const double* bdr, double* pf1, double* pf2, double* fpd, double* rho,
+                      double* eta, float* rho32, float* eta32, ull* ctr, cudaStream_t s);
 void launch_mass_partial(int nr, int nz, const double* ph, const Dots& d, int slot, ull* ctr, cudaStream_t s);
 void launch_mass_final(const Dots& d, int slot, double drdz, double* out, ull* ctr, cudaStream_t s);
 

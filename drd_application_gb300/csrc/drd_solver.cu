@@ -16,6 +16,7 @@
 #include <functional>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "drd_kernels.cuh"
@@ -24,7 +25,7 @@ using namespace drd;
 
 namespace {
 
-enum SysKind { SYS_CH = 0, SYS_UV = 1, SYS_PHMU = 2 };
+enum SysKind { SYS_CH = 0, SYS_UV = 1, SYS_PHMU = 2, SYS_ORI = 3 };
 enum { KS_CH = 0, KS_UV = 1, KS_PHMU = 2, KS_INNER = 3, KS_PRE = 4, KS_MASS = 5, KS_COUNT = 6 };
 
 template <typename T>
@@ -52,8 +53,12 @@ struct drd_ctx {
     // tables and transform matrices
     double *ph_lcc, *pre_lcc;
     float* ph_lcc32;
-    double *m1xT, *m1z, *m2xT, *m2z, *m3xT, *m3z;
-    float *m1xT32, *m1z32;
+    double *m2xT, *m2z, *m3xT, *m3z;
+    // folded DCT-I (VCOST) matrices of the CH preconditioner: x pass B operands (even / odd
+    // output columns, Kx x Nxe each) and z pass A operands (even / odd output rows, Mze x Kz)
+    double *f1xe, *f1xo, *f1ze, *f1zo;
+    float *f1xe32, *f1xo32, *f1ze32, *f1zo32;
+    int Kx = 0, Kz = 0, Nxe = 0, Nxo = 0, Mze = 0, Mzo = 0;
     double *cfB, *cfT;
     // resident state and scratch
     double* fld[DRD_F_COUNT];
@@ -62,6 +67,12 @@ struct drd_ctx {
     KVecs<double> k64;
     KVecs<float> k32;
     double* part;
+    // fiber particles (particles_move.f90): POINTS arrays (np x 2, column-major) and scratch
+    drd_particle_params pp{};
+    double *pts, *pts_old, *totF, *psum, *ppart, *bdist;
+    // PhSolve_ori: wall-energy prefactors cf of angleB / angleT (XLINE) and alpha_s
+    double *ori_cfb, *ori_cft;
+    double ori_alpha = 0.0;
     KState* ks;      // device, KS_COUNT entries
     CallArgs* ca;    // device
     double* d_mass;  // device
@@ -76,6 +87,12 @@ struct drd_ctx {
     int use_graph = 1;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t tev0 = nullptr, tev1 = nullptr;  // autotuner timing
+    // asynchronous checkpoint: pinned staging, its copy stream and events, the writer thread
+    cudaStream_t sck = nullptr;
+    cudaEvent_t eck0 = nullptr, eck1 = nullptr;
+    double* h_stage = nullptr;
+    std::thread ckpt;
+    int ckpt_rc = 0;
 };
 
 namespace {
@@ -103,8 +120,9 @@ size_t arena_need(long cs, long us, long vs, long nc, long nr, long nz, long nma
     for (int i = 0; i < 8; ++i) add(cs, 8);      // coefficients
     for (int i = 0; i < 6; ++i) add(cs, 4);      // FP32 coefficients
     add(nc, 8); add((nr + 1) * (nz + 1), 8); add(nc, 4);
-    add(nr * nr, 8); add(nz * nz, 8); add(nr * nr, 8); add(nz * nz, 8); add(nr * nr, 8); add(nz * nz, 8);
-    add(nr * nr, 4); add(nz * nz, 4);
+    add(nr * nr, 8); add(nz * nz, 8); add(nr * nr, 8); add(nz * nz, 8);
+    for (int i = 0; i < 4; ++i) { add((nr / 2 + 1) * (nr / 2 + 1), 8); add((nz / 2 + 1) * (nz / 2 + 1), 8); }
+    for (int i = 0; i < 4; ++i) { add((nr / 2 + 1) * (nr / 2 + 1), 4); add((nz / 2 + 1) * (nz / 2 + 1), 4); }
     add(nr + 1, 8); add(nr + 1, 8);
     for (int f = 0; f < DRD_F_COUNT; ++f) add(std::max(us, cs), 8);
     add(us, 8); add(vs, 8); add(cs, 8); add(cs, 8); add(cs, 8); add(nz + 1, 8); add(nr, 8); add(nr, 8);
@@ -113,6 +131,9 @@ size_t arena_need(long cs, long us, long vs, long nc, long nr, long nz, long nma
     for (int i = 0; i < 12; ++i) add(nmax, 4);
     add(DRD_NDOT * DRD_MAXB, 8);
     add(KS_COUNT * sizeof(KState), 1); add(sizeof(CallArgs), 1); add(1, 8); add(1, 8);
+    for (int i = 0; i < 4; ++i) add(2 * DRD_PARTICLES_MAX, 8);  // pts, pts_old, totF, psum
+    add(3 * DRD_PARTICLES_MAX * PT_GX, 8); add(cs, 8);          // ppart, bdist
+    add(nr + 1, 8); add(nr + 1, 8);                            // ori_cfb, ori_cft
     return b + 4096;
 }
 
@@ -143,6 +164,13 @@ OpScal<T> make_op(const drd_ctx* c, int bdf) {
     o.ct = o.cb;
     o.nr = d.nr; o.nz = d.nz; o.variant = d.variant; o.lr_neumann = d.lr_neumann; o.bdf = bdf; o.phi_mode = d.phi_mode;
     return o;
+}
+
+// coef_bot = coef_top of PhSolve_ori's non-dynamic wall branch
+// (microfluidics_complex_domain/PhSolve_ori.f90:71-74, :111-113).
+double ori_coef(const drd_ctx* c) {
+    const double tmp1 = c->P.I_thickness / c->P.dz + 0.5 * c->ori_alpha;
+    return (c->P.I_thickness / c->P.dz - 0.5 * c->ori_alpha) / tmp1;
 }
 
 // setup() tables (microfluidics_complex_domain/setup.f90:106-155), FP64 on the host.
@@ -217,12 +245,19 @@ KVecs<double>& vecs(drd_ctx* c, double*) { return c->k64; }
 KVecs<float>& vecs(drd_ctx* c, float*) { return c->k32; }
 
 // ---- transforms --------------------------------------------------------------------------
+// folded DCT-I operands: 0 x-even, 1 x-odd, 2 z-even, 3 z-odd
 template <typename T>
-const T* mat(const drd_ctx* c, int which);
+const T* fmat(const drd_ctx* c, int which);
 template <>
-const double* mat<double>(const drd_ctx* c, int which) { return which == 0 ? c->m1xT : c->m1z; }
+const double* fmat<double>(const drd_ctx* c, int w) {
+    const double* m[] = {c->f1xe, c->f1xo, c->f1ze, c->f1zo};
+    return m[w];
+}
 template <>
-const float* mat<float>(const drd_ctx* c, int which) { return which == 0 ? c->m1xT32 : c->m1z32; }
+const float* fmat<float>(const drd_ctx* c, int w) {
+    const float* m[] = {c->f1xe32, c->f1xo32, c->f1ze32, c->f1zo32};
+    return m[w];
+}
 
 template <typename T>
 T* tmp1(drd_ctx* c);
@@ -249,22 +284,43 @@ GemmArgs<T> gargs(drd_ctx* c, int M, int N, int K, const T* A, long lda, const T
 template <typename T>
 int gcfg(drd_ctx* c, int zpass) { return c->gcfg[sizeof(T) == 4][zpass]; }
 
+// The folded DCT-I passes of the CH preconditioner.  x pass: out[m][o] = sum_j X[m][j] C_x[o][j]
+// over nr columns; z pass: out[o][n] = sum_j C_z[o][j] X[j][n] over nz rows.  Each pass folds
+// X's j and L-j (C[o][L-j] = (-1)^o C[o][j]) and computes even and odd outputs as the two
+// halves of one launch, halving the multiply-adds.
+template <typename T>
+GemmArgs<T> dct1_xpass(drd_ctx* c, const T* X, T* out, const KState* ks, int gate) {
+    GemmArgs<T> a = gargs<T>(c, c->nz, c->Nxe, c->Kx, X, c->nr, fmat<T>(c, 0), c->Nxe, out, c->nr, ks, gate);
+    a.fold = FOLD_A;
+    a.Lf = c->nr - 1;
+    a.B_odd = fmat<T>(c, 1);
+    a.N_odd = c->Nxo;
+    return a;
+}
+template <typename T>
+GemmArgs<T> dct1_zpass(drd_ctx* c, const T* X, T* out, const KState* ks, int gate) {
+    GemmArgs<T> a = gargs<T>(c, c->Mze, c->nr, c->Kz, fmat<T>(c, 2), c->Kz, X, c->nr, out, c->nr, ks, gate);
+    a.fold = FOLD_B;
+    a.Lf = c->nz - 1;
+    a.A_odd = fmat<T>(c, 3);
+    a.M_odd = c->Mzo;
+    return a;
+}
+
 // PSolve_CG (microfluidics_complex_domain/PhSolve.f90:296-313): y = C (C x ./ Ph_Lcc) with the
-// separable 2-D DCT-I C = VCOST_x VCOST_z, as four GEMM passes (x, z, x, z).
+// separable 2-D DCT-I C = VCOST_x VCOST_z, as four folded GEMM passes (x, z, x, z).
 template <typename T>
 void enq_ch_psolve(drd_ctx* c, const T* x, T* y, const KState* ks, int gate, cudaStream_t s) {
-    const int nr = c->nr, nz = c->nz;
     T* t1 = tmp1<T>(c);
     T* t2 = tmp2<T>(c);
-    const T* mx = mat<T>(c, 0);
-    const T* mz = mat<T>(c, 1);
     const T* tab = (sizeof(T) == 8) ? (const T*)c->ph_lcc : (const T*)c->ph_lcc32;
-    launch_gemm<T>(gcfg<T>(c, 0), EPI_STORE, gargs<T>(c, nz, nr, nr, x, nr, mx, nr, t1, nr, ks, gate), s);
-    auto a2 = gargs<T>(c, nz, nr, nz, mz, nz, t1, nr, t2, nr, ks, gate);
-    a2.tab = tab; a2.ldt = nr;
+    launch_gemm<T>(gcfg<T>(c, 0), EPI_STORE, dct1_xpass<T>(c, x, t1, ks, gate), s);
+    auto a2 = dct1_zpass<T>(c, t1, t2, ks, gate);
+    a2.tab = tab;
+    a2.ldt = c->nr;
     launch_gemm<T>(gcfg<T>(c, 1), EPI_DIV_TAB, a2, s);
-    launch_gemm<T>(gcfg<T>(c, 0), EPI_STORE, gargs<T>(c, nz, nr, nr, t2, nr, mx, nr, t1, nr, ks, gate), s);
-    launch_gemm<T>(gcfg<T>(c, 1), EPI_STORE, gargs<T>(c, nz, nr, nz, mz, nz, t1, nr, y, nr, ks, gate), s);
+    launch_gemm<T>(gcfg<T>(c, 0), EPI_STORE, dct1_xpass<T>(c, t2, t1, ks, gate), s);
+    launch_gemm<T>(gcfg<T>(c, 1), EPI_STORE, dct1_zpass<T>(c, t1, y, ks, gate), s);
 }
 
 // ---- generic system operations -------------------------------------------------------------
@@ -297,6 +353,12 @@ void enq_matvec(drd_ctx* c, const Sys& S, T alpha, const T* x, T beta, T* y, con
     if (S.kind == SYS_CH) {
         launch_ch_matvec<T>(make_op<T>(c, 0), coef<T>(c, 3), coef<T>(c, 4), alpha, x, beta, y, k.ff1, dot1, self2, d,
                             slot1, ks, gate, c->ctr, s);
+    } else if (S.kind == SYS_ORI) {
+        OpScal<T> o = make_op<T>(c, 0);
+        const double cb = ori_coef(c);
+        o.cb = (T)cb;
+        o.ct = (T)cb;
+        launch_ori_matvec<T>(o, alpha, x, beta, y, k.ff1, dot1, self2, d, slot1, ks, gate, c->ctr, s);
     } else if (S.kind == SYS_UV) {
         launch_uv_matvec<T>(make_op<T>(c, S.bdf), coef<T>(c, 0), coef<T>(c, 1), coef<T>(c, 2), alpha, x, beta, y,
                             dot1, self2, d, slot1, ks, gate, c->ctr, s);
@@ -309,7 +371,7 @@ void enq_matvec(drd_ctx* c, const Sys& S, T alpha, const T* x, T beta, T* y, con
 template <typename T>
 void enq_psolve(drd_ctx* c, const Sys& S, const T* x, T* y, const KState* ks, int gate, cudaStream_t s) {
     KVecs<T>& k = vecs(c, (T*)nullptr);
-    if (S.kind == SYS_CH) enq_ch_psolve<T>(c, x, y, ks, gate, s);
+    if (S.kind == SYS_CH || S.kind == SYS_ORI) enq_ch_psolve<T>(c, x, y, ks, gate, s);
     else launch_bi_diag_apply<T>(S.n, x, S.jacobi ? k.diag : nullptr, S.ident, y, ks, gate, c->ctr, s);
 }
 
@@ -326,7 +388,7 @@ template <typename T>
 void enq_bicg_body(drd_ctx* c, const Sys& S, KVecs<T>& k, KState* ks, cudaStream_t s) {
     Dots d = dots(c);
     const long n = S.n;
-    if (S.kind == SYS_CH) {
+    if (S.kind == SYS_CH || S.kind == SYS_ORI) {
         launch_bi_p<T>(n, k.r, k.v, k.p, k.phat, nullptr, 0, ks, d, c->ctr, s);
         enq_psolve<T>(c, S, k.p, k.phat, ks, G_RUNNING, s);
     } else {
@@ -344,7 +406,7 @@ template <typename T>
 void enq_bicg_iter(drd_ctx* c, const Sys& S, KVecs<T>& k, KState* ks, cudaGraphConditionalHandle h, int use_graph,
                    cudaStream_t s) {
     enq_bicg_body<T>(c, S, k, ks, s);
-    launch_bi_end(ks, dots(c), h, use_graph, c->ctr, s);
+    launch_bi_end(ks, dots(c), h, use_graph && c->use_graph, c->ctr, s);
 }
 
 // Start of the solve with the guess already in k.x (:229-255).
@@ -364,6 +426,19 @@ void enq_bicg_setup(drd_ctx* c, const Sys& S, KVecs<T>& k, KState* ks, double to
 // into its body graph on `sb`.
 int capture_while(drd_ctx* c, cudaStream_t s, cudaStream_t sb, const KState* ks,
                   const std::function<void(cudaStream_t, cudaGraphConditionalHandle)>& body) {
+    if (!c->use_graph) {
+        // direct launches (profiling / debugging): the host runs the loop, reading the state's
+        // phase after every body; the body's own cap (MAXIT) still bounds it
+        (void)sb;
+        int* hp = &c->h_ks[KS_COUNT - 1].phase;  // scratch slot of the pinned states
+        for (int guard = 0; guard < (1 << 20); ++guard) {
+            CK(cudaMemcpyAsync(hp, &ks->phase, sizeof(int), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            if (*hp != PH_RUNNING) break;
+            body(s, cudaGraphConditionalHandle{});
+        }
+        return DRD_OK;
+    }
     cudaStreamCaptureStatus st;
     cudaGraph_t g = nullptr;
     const cudaGraphNode_t* deps = nullptr;
@@ -440,29 +515,29 @@ int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int 
         });
         if (rc) return rc;
     } else {
-        // FP32 BiCGSTAB (FP64 inner products) with FP64 reliable updates
+        // FP64 iterative refinement around an FP32 BiCGSTAB: each sweep solves A d = r / ||r||
+        // from a zero guess to mixed_inner_tol, then x += ||r|| d and r = b - A x in FP64.
+        // (A single FP32 sequence with residual replacement is not used: the FP32 transforms'
+        // rounding makes the preconditioner slightly input-dependent and long sequences drift.)
         KVecs<float>& f = c->k32;
+        KState* in = c->ks + KS_INNER;
         enq_sys_setup<float>(c, S, s);
-        CK(cudaMemsetAsync(f.x, 0, sizeof(float) * S.n, s));
         launch_copy<double>(S.n, k.b, k.r, c->ctr, s);
         enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.r, nullptr, 1, -1, nullptr, G_ALWAYS, s);
         launch_norm2_partial<double>(S.n, k.b, d, 3, c->ctr, s);
-        launch_mr_init(ks, d, tol, maxit, c->ctr, s);
-        launch_mr_reset<float>(S.n, k.r, f.r, f.rtld, d, ks, c->ctr, s);
-        rc = capture_while(c, s, c->s2, ks, [&](cudaStream_t sb, cudaGraphConditionalHandle hw) {
-            enq_bicg_body<float>(c, S, f, ks, sb);
-            cudaGraphConditionalHandle hif;
-            int rc2 = make_if_handle(c, sb, &hif);
-            if (rc2) { rc = rc2; return; }
-            launch_mr_end(ks, d, hw, hif, c->ctr, sb);
-            rc2 = capture_if(c, sb, c->s3, hif, [&](cudaStream_t su) {
-                launch_mr_fold<float>(S.n, f.x, k.x, c->ctr, su);
-                launch_copy<double>(S.n, k.b, k.r, c->ctr, su);
-                enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.r, nullptr, 1, -1, nullptr, G_ALWAYS, su);
-                launch_mr_check(ks, d, hw, c->ctr, su);
-                launch_mr_reset<float>(S.n, k.r, f.r, f.rtld, d, ks, c->ctr, su);
+        launch_mx_init(ks, d, tol, c->P.mixed_max_refine, c->ctr, s);
+        const double itol = c->P.mixed_inner_tol;
+        rc = capture_while(c, s, c->s2, ks, [&](cudaStream_t sb, cudaGraphConditionalHandle ho) {
+            launch_mx_scale<float>(S.n, k.r, ks, f.b, f.x, c->ctr, sb);
+            enq_bicg_setup<float>(c, S, f, in, itol, maxit, ks, sb);
+            int rc2 = capture_while(c, sb, c->s3, in, [&](cudaStream_t si, cudaGraphConditionalHandle hi) {
+                enq_bicg_iter<float>(c, S, f, in, hi, 1, si);
             });
             if (rc2) rc = rc2;
+            launch_axpy_f2d(S.n, ks, f.x, k.x, c->ctr, sb);
+            launch_copy<double>(S.n, k.b, k.r, c->ctr, sb);
+            enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.r, nullptr, 1, -1, nullptr, G_ALWAYS, sb);
+            launch_mx_check(ks, in, d, ho, c->use_graph, c->ctr, sb);
         });
         if (rc) return rc;
     }
@@ -478,7 +553,7 @@ Sys sys_of(drd_ctx* c, int kind, int bdf) {
     Sys S{};
     S.kind = kind;
     S.bdf = bdf;
-    if (kind == SYS_CH) S.n = c->nc;
+    if (kind == SYS_CH || kind == SYS_ORI) S.n = c->nc;
     else if (kind == SYS_PHMU) { S.n = c->nphmu; S.jacobi = 1; }
     else {
         S.n = c->nuv;
@@ -492,23 +567,40 @@ Sys sys_of(drd_ctx* c, int kind, int bdf) {
 int mixed_of(drd_ctx* c) { return c->P.precision == DRD_PREC_MIXED; }
 
 // PhSolve (microfluidics_complex_domain/PhSolve.f90:1-126) on fld[U,V,PH,RMU] -> rmu_after, ph_after.
-int enq_ch(drd_ctx* c, cudaStream_t s) {
+// extrap: take 2 rmu - rmu_pre as the initial guess (drd_step with guess_mode 1).
+int enq_ch(drd_ctx* c, cudaStream_t s, int extrap = 0) {
     const DevParams& P = c->dp;
     launch_ch_f2(P, c->fld[DRD_F_U], c->fld[DRD_F_V], c->fld[DRD_F_PH], c->f2, c->ctr, s);
-    launch_ch_rhs(P, c->fld[DRD_F_PH], c->fld[DRD_F_RMU], c->bdr, c->grad, c->Mi, c->f2, c->k64.b, c->k64.x, c->ctr, s);
+    launch_ch_rhs(P, c->fld[DRD_F_PH], c->fld[DRD_F_RMU], extrap ? c->fld[DRD_F_RMU_PRE] : nullptr, c->bdr, c->grad,
+                  c->Mi, c->f2, c->k64.b, c->k64.x, c->ctr, s);
     int rc = enq_solve(c, sys_of(c, SYS_CH, 0), KS_CH, c->P.tol, c->P.ch_maxit, mixed_of(c), s);
     if (rc) return rc;
     launch_ch_fin(P, c->k64.x, c->f2, c->M0, c->rmu_after, c->ph_after, c->ctr, s);
     return DRD_OK;
 }
 
+// PhSolve_ori (microfluidics_complex_domain/PhSolve_ori.f90:1-214) on fld[U,V,PH] ->
+// ph_after, rmu_after, with the wall prefactors and alpha_s last set by set_ori_walls.
+int enq_ori(drd_ctx* c, cudaStream_t s) {
+    const DevParams& P = c->dp;
+    launch_ch_f2(P, c->fld[DRD_F_U], c->fld[DRD_F_V], c->fld[DRD_F_PH], c->f2, c->ctr, s);
+    launch_ori_rhs(P, c->fld[DRD_F_PH], c->f2, c->ori_cfb, c->ori_cft, c->ori_alpha, c->k64.b, c->k64.x, c->pnb, c->pnt,
+                   c->ctr, s);
+    int rc = enq_solve(c, sys_of(c, SYS_ORI, 0), KS_CH, c->P.tol, c->P.ch_maxit, mixed_of(c), s);
+    if (rc) return rc;
+    const double cb = ori_coef(c);
+    launch_ori_fin(P, c->k64.x, c->pnb, c->pnt, cb, cb, c->ph_after, c->rmu_after, c->ctr, s);
+    return DRD_OK;
+}
+
 // ph_mu_solve (two_phase_flow_complex_domain/ph_mu_solve.f90:3-197).
-int enq_phmu(drd_ctx* c, cudaStream_t s) {
+int enq_phmu(drd_ctx* c, cudaStream_t s, int extrap = 0) {
     const DevParams& P = c->dp;
     launch_phmu_prep(P, c->fld[DRD_F_U], c->fld[DRD_F_V], c->fld[DRD_F_PH], c->bdr, c->used, c->M0, c->f2, c->ctr, s);
     launch_convert_scale<float, double>(c->cs, c->M0, 1.0, c->M032, c->ctr, s);
-    launch_phmu_rhs(P, c->fld[DRD_F_PH], c->fld[DRD_F_RMU], c->bdr, c->grad, c->f2, c->cfB, c->cfT, c->k64.b, c->k64.x,
-                    c->pnb, c->pnt, c->ctr, s);
+    launch_phmu_rhs(P, c->fld[DRD_F_PH], c->fld[DRD_F_RMU], extrap ? c->fld[DRD_F_PH_PRE] : nullptr,
+                    extrap ? c->fld[DRD_F_RMU_PRE] : nullptr, c->bdr, c->grad, c->f2, c->cfB, c->cfT, c->k64.b,
+                    c->k64.x, c->pnb, c->pnt, c->ctr, s);
     int rc = enq_solve(c, sys_of(c, SYS_PHMU, 0), KS_PHMU, c->P.tol, c->P.phmu_maxit, mixed_of(c), s);
     if (rc) return rc;
     OpScal<double> o = make_op<double>(c, 0);
@@ -517,12 +609,12 @@ int enq_phmu(drd_ctx* c, cudaStream_t s) {
 }
 
 // VeloSolve_combined (bdf 1) / VeloSolve_2_combined (bdf 2) -> u_after, v_after.
-int enq_uv(drd_ctx* c, int bdf, cudaStream_t s) {
+int enq_uv(drd_ctx* c, int bdf, cudaStream_t s, int extrap = 0) {
     const DevParams& P = c->dp;
     double** f = c->fld;
     launch_uv_rhs(P, bdf, c->ca, f[DRD_F_PSI1], f[DRD_F_PSI2], f[DRD_F_U_PRE], f[DRD_F_U], f[DRD_F_V_PRE], f[DRD_F_V],
                   f[DRD_F_P], c->rho, c->eta, c->bdr, c->used, c->ph_after, c->rmu_after, f[DRD_F_PF1], f[DRD_F_PF2],
-                  c->k64.b, c->k64.x, c->uL, c->ctr, s);
+                  c->k64.b, c->k64.x, c->uL, extrap && bdf == 2, c->ctr, s);
     int rc = enq_solve(c, sys_of(c, SYS_UV, bdf), KS_UV, c->P.tol, c->P.uv_maxit, mixed_of(c), s);
     if (rc) return rc;
     launch_uv_fin(P, c->k64.x, c->uL, c->u_after, c->v_after, c->ctr, s);
@@ -550,13 +642,45 @@ void enq_mass(drd_ctx* c, const double* ph, cudaStream_t s) {
     launch_mass_final(d, 0, c->P.dr * c->P.dz, c->d_mass, c->ctr, s);
 }
 
+PartParams part_params(const drd_ctx* c) {
+    PartParams q{};
+    q.np = c->pp.np; q.nr = c->nr; q.nz = c->nz;
+    q.lx = c->pp.lx; q.ly = c->pp.ly; q.radius = c->pp.fpd_radius; q.l0 = c->pp.l0;
+    q.ks = c->pp.ks; q.kb = c->pp.kb; q.theta0 = c->pp.theta0;
+    q.k0 = c->pp.k0_inter; q.k0b = c->pp.k0_inter_bdr; q.eq_pp = c->pp.fpd_fpd_dist; q.eq_bdr = c->pp.fpd_bdr_dist;
+    q.dr = c->P.dr; q.dz = c->P.dz; q.eps = c->P.I_thickness; q.dt = c->P.dt;
+    q.lambda_rho = c->P.lambda_rho; q.lambda_eta = c->P.lambda_eta;
+    const double cut = c->pp.fpd_radius + 20.0 * std::sqrt(2.0) * c->P.I_thickness;
+    q.skip_d2 = cut * cut;
+    return q;
+}
+
+// The particle block of the mcl6 loop (mcl6.f90:394-402).  PT_FORCE: force_caculation_vel
+// (tot_F, particle_force1/2 at the positions on entry); PT_MOVE: update_position_vel with u, v;
+// PT_COEF: interpolate_coef at the positions after the move.
+enum { PT_FORCE = 1, PT_MOVE = 2, PT_COEF = 4 };
+void enq_particles(drd_ctx* c, int what, const double* u, const double* v, cudaStream_t s) {
+    const PartParams q = part_params(c);
+    if (q.np > 0 && (what & (PT_FORCE | PT_MOVE))) {
+        if (what & PT_FORCE) launch_pt_force(q, c->pts, c->pts_old, c->totF, c->bdist, c->ctr, s);
+        launch_pt_sums(q, c->pts, (what & PT_MOVE) ? u : nullptr, (what & PT_MOVE) ? v : nullptr, c->ppart, c->ctr, s);
+        launch_pt_finish(q, c->ppart, c->psum, c->pts, (what & PT_MOVE) ? 1 : 0, c->ctr, s);
+    }
+    const int mode = ((what & PT_FORCE) && q.np > 0 ? 1 : 0) | ((what & PT_COEF) ? 2 : 0);
+    if (mode)
+        launch_pt_spread(q, mode, c->pts_old, c->pts, c->totF, c->psum, c->bdr, c->fld[DRD_F_PF1], c->fld[DRD_F_PF2],
+                         c->fpd, c->rho, c->eta, c->rho32, c->eta32, c->ctr, s);
+}
+
 // The mcl6 step (microfluidics_complex_domain/mcl6.f90:239-306 first, :378-486 loop).
 int enq_step(drd_ctx* c, int first, cudaStream_t s) {
     double** f = c->fld;
     const size_t cb = sizeof(double) * c->cs, ub = sizeof(double) * c->us, vb = sizeof(double) * c->vs;
-    int rc = (c->P.variant == DRD_VARIANT_TP) ? enq_phmu(c, s) : enq_ch(c, s);
+    const int extrap = (!first && c->P.guess_mode == 1);
+    int rc = (c->P.variant == DRD_VARIANT_TP) ? enq_phmu(c, s, extrap) : enq_ch(c, s, extrap);
     if (rc) return rc;
-    rc = enq_uv(c, first ? 1 : 2, s);
+    if (c->pp.np > 0) enq_particles(c, PT_FORCE | PT_MOVE | PT_COEF, f[DRD_F_U], f[DRD_F_V], s);
+    rc = enq_uv(c, first ? 1 : 2, s, extrap);
     if (rc) return rc;
     CK(cudaMemcpyAsync(f[DRD_F_U_PRE], f[DRD_F_U], ub, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(f[DRD_F_V_PRE], f[DRD_F_V], vb, cudaMemcpyDeviceToDevice, s));
@@ -574,7 +698,7 @@ int enq_step(drd_ctx* c, int first, cudaStream_t s) {
 }
 
 // Graph keys
-enum GraphKind { GK_CH = 1, GK_UV = 2, GK_PHMU = 3, GK_PRE = 4, GK_STEP = 5 };
+enum GraphKind { GK_CH = 1, GK_UV = 2, GK_PHMU = 3, GK_PRE = 4, GK_STEP = 5, GK_ORI = 6 };
 long gkey(int kind, int a, int b) { return (long)kind * 100 + a * 10 + b; }
 
 int get_graph(drd_ctx* c, long key, const std::function<int(cudaStream_t)>& build, cudaGraphExec_t* out) {
@@ -610,11 +734,8 @@ int tune_pass(drd_ctx* c, int zpass) {
     float best_ms = 1e30f;
     T* t1 = tmp1<T>(c);
     T* t2 = tmp2<T>(c);
-    const T* mx = mat<T>(c, 0);
-    const T* mz = mat<T>(c, 1);
     for (int cfg = 0; cfg < gemm_config_count(); ++cfg) {
-        auto a = zpass ? gargs<T>(c, nz, nr, nz, mz, nz, t1, nr, t2, nr, nullptr, G_ALWAYS)
-                       : gargs<T>(c, nz, nr, nr, t1, nr, mx, nr, t2, nr, nullptr, G_ALWAYS);
+        auto a = zpass ? dct1_zpass<T>(c, t1, t2, nullptr, G_ALWAYS) : dct1_xpass<T>(c, t1, t2, nullptr, G_ALWAYS);
         a.ctr = nullptr;
         launch_gemm<T>(cfg, EPI_STORE, a, c->s);  // warm-up
         cudaEventRecord(c->tev0, c->s);
@@ -644,13 +765,14 @@ int ensure_tuned(drd_ctx* c) {
 int run_graph(drd_ctx* c, long key, const std::function<int(cudaStream_t)>& build, double t, double coef) {
     int rc = ensure_tuned(c);
     if (rc) return rc;
-    cudaGraphExec_t ex;
-    rc = get_graph(c, key, build, &ex);
-    if (rc) return rc;
     c->h_ca->t = t;
     c->h_ca->cf = 1.0 - std::exp(-t / c->P.twall);
     c->h_ca->coef = coef;
     CK(cudaMemcpyAsync(c->ca, c->h_ca, sizeof(CallArgs), cudaMemcpyHostToDevice, c->s));
+    if (!c->use_graph) return build(c->s);  // direct launches (DRD_DIRECT_LAUNCH=1)
+    cudaGraphExec_t ex;
+    rc = get_graph(c, key, build, &ex);
+    if (rc) return rc;
     CK(cudaGraphLaunch(ex, c->s));
     return DRD_OK;
 }
@@ -720,10 +842,15 @@ int setup_context(drd_ctx* c) {
     c->ph_lcc = carve<double>(c, c->nc);
     c->pre_lcc = carve<double>(c, (long)(nr + 1) * (nz + 1));
     c->ph_lcc32 = carve<float>(c, c->nc);
-    c->m1xT = carve<double>(c, (long)nr * nr); c->m1z = carve<double>(c, (long)nz * nz);
     c->m2xT = carve<double>(c, (long)nr * nr); c->m2z = carve<double>(c, (long)nz * nz);
     c->m3xT = carve<double>(c, (long)nr * nr); c->m3z = carve<double>(c, (long)nz * nz);
-    c->m1xT32 = carve<float>(c, (long)nr * nr); c->m1z32 = carve<float>(c, (long)nz * nz);
+    c->Kx = (nr - 1) / 2 + 1; c->Nxe = (nr + 1) / 2; c->Nxo = nr / 2;
+    c->Kz = (nz - 1) / 2 + 1; c->Mze = (nz + 1) / 2; c->Mzo = nz / 2;
+    const long fx = (long)c->Kx * c->Nxe, fz = (long)c->Mze * c->Kz;
+    c->f1xe = carve<double>(c, fx); c->f1xo = carve<double>(c, fx);
+    c->f1ze = carve<double>(c, fz); c->f1zo = carve<double>(c, fz);
+    c->f1xe32 = carve<float>(c, fx); c->f1xo32 = carve<float>(c, fx);
+    c->f1ze32 = carve<float>(c, fz); c->f1zo32 = carve<float>(c, fz);
     c->cfB = carve<double>(c, nr + 1); c->cfT = carve<double>(c, nr + 1);
     for (int f = 0; f < DRD_F_COUNT; ++f) c->fld[f] = carve<double>(c, std::max(c->us, c->cs));
     c->u_after = carve<double>(c, c->us); c->v_after = carve<double>(c, c->vs);
@@ -739,6 +866,10 @@ int setup_context(drd_ctx* c) {
     c->ca = (CallArgs*)carve<char>(c, sizeof(CallArgs));
     c->d_mass = carve<double>(c, 1);
     c->ctr = (unsigned long long*)carve<double>(c, 1);
+    c->pts = carve<double>(c, 2 * DRD_PARTICLES_MAX); c->pts_old = carve<double>(c, 2 * DRD_PARTICLES_MAX);
+    c->totF = carve<double>(c, 2 * DRD_PARTICLES_MAX); c->psum = carve<double>(c, 2 * DRD_PARTICLES_MAX);
+    c->ppart = carve<double>(c, 3 * DRD_PARTICLES_MAX * PT_GX); c->bdist = carve<double>(c, c->cs);
+    c->ori_cfb = carve<double>(c, nr + 1); c->ori_cft = carve<double>(c, nr + 1);
     if (c->arena_used > c->arena_bytes) { c->err = "arena overflow"; return DRD_ERR_NOMEM; }
     CK(cudaMallocHost(&c->h_ks, KS_COUNT * sizeof(KState)));
     CK(cudaMallocHost(&c->h_ca, sizeof(CallArgs)));
@@ -759,14 +890,33 @@ int setup_context(drd_ctx* c) {
     auto put = [&](double* dst, const std::vector<double>& v) {
         return cudaMemcpy(dst, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice);
     };
-    CK(put(c->m1xT, transpose(d1, nr)));
     CK(put(c->m2xT, transpose(d2, nr)));
     CK(put(c->m3xT, transpose(d3, nr)));
-    CK(put(c->m1z, e1));
     CK(put(c->m2z, e2));
     CK(put(c->m3z, e3));
-    launch_convert_scale<float, double>((long)nr * nr, c->m1xT, 1.0, c->m1xT32, nullptr, c->s);
-    launch_convert_scale<float, double>((long)nz * nz, c->m1z, 1.0, c->m1z32, nullptr, c->s);
+    {
+        // x pass B operands: B_p[j][n] = D1x[2n+p][j]; z pass A operands: A_p[m][j] = D1z[2m+p][j]
+        std::vector<double> xe((size_t)c->Kx * c->Nxe, 0.0), xo(xe.size(), 0.0);
+        for (int j = 0; j < c->Kx; ++j)
+            for (int n = 0; n < c->Nxe; ++n) {
+                xe[(size_t)j * c->Nxe + n] = d1[(size_t)(2 * n) * nr + j];
+                if (n < c->Nxo) xo[(size_t)j * c->Nxe + n] = d1[(size_t)(2 * n + 1) * nr + j];
+            }
+        std::vector<double> ze((size_t)c->Mze * c->Kz, 0.0), zo(ze.size(), 0.0);
+        for (int m = 0; m < c->Mze; ++m)
+            for (int j = 0; j < c->Kz; ++j) {
+                ze[(size_t)m * c->Kz + j] = e1[(size_t)(2 * m) * nz + j];
+                if (m < c->Mzo) zo[(size_t)m * c->Kz + j] = e1[(size_t)(2 * m + 1) * nz + j];
+            }
+        CK(put(c->f1xe, xe));
+        CK(put(c->f1xo, xo));
+        CK(put(c->f1ze, ze));
+        CK(put(c->f1zo, zo));
+        launch_convert_scale<float, double>((long)xe.size(), c->f1xe, 1.0, c->f1xe32, nullptr, c->s);
+        launch_convert_scale<float, double>((long)xo.size(), c->f1xo, 1.0, c->f1xo32, nullptr, c->s);
+        launch_convert_scale<float, double>((long)ze.size(), c->f1ze, 1.0, c->f1ze32, nullptr, c->s);
+        launch_convert_scale<float, double>((long)zo.size(), c->f1zo, 1.0, c->f1zo32, nullptr, c->s);
+    }
     std::vector<double> cfa(nr + 1, std::cos(c->P.angle * kPi / 180.0) / std::sqrt(2.0));
     CK(put(c->cfB, cfa));
     CK(put(c->cfT, cfa));
@@ -775,7 +925,10 @@ int setup_context(drd_ctx* c) {
     rc = refresh_fp32(c);
     if (rc) return rc;
     CK(cudaStreamSynchronize(c->s));
-    const char* g = std::getenv("DRD_NO_GRAPH");
+    // DRD_DIRECT_LAUNCH=1 launches every kernel directly on the stream with the Krylov loops
+    // run by the host (for per-kernel profilers and debugging); the default is one CUDA graph
+    // per routine or step with device-side WHILE loops.
+    const char* g = std::getenv("DRD_DIRECT_LAUNCH");
     c->use_graph = !(g && g[0] == '1');
     return DRD_OK;
 }
@@ -791,6 +944,7 @@ int validate(const drd_params* p, std::string& why) {
     if (p->variant == DRD_VARIANT_TP && p->phi_mode != 1 && p->phi_mode != 2) { why = "phi_mode must be 1 or 2"; return DRD_ERR_BADARG; }
     if (p->ch_maxit <= 0 || p->uv_maxit <= 0 || p->phmu_maxit <= 0) { why = "maxit must be positive"; return DRD_ERR_BADARG; }
     if (p->xlsB >= 1.e-8) { why = "slip walls (xlsB >= 1e-8) have no solve in the reference"; return DRD_ERR_UNSUPPORTED; }
+    if (p->guess_mode != 0 && p->guess_mode != 1) { why = "guess_mode must be 0 or 1"; return DRD_ERR_BADARG; }
     if (p->precision == DRD_PREC_MIXED && (!(p->mixed_inner_tol > 0) || p->mixed_max_refine <= 0)) {
         why = "mixed precision needs mixed_inner_tol > 0 and mixed_max_refine > 0";
         return DRD_ERR_BADARG;
@@ -854,7 +1008,12 @@ int drd_create(const drd_params* params, drd_ctx** out) {
 
 int drd_destroy(drd_ctx* c) {
     if (!c) return DRD_ERR_BADARG;
+    if (c->ckpt.joinable()) c->ckpt.join();
     if (c->s) cudaStreamSynchronize(c->s);
+    if (c->sck) cudaStreamDestroy(c->sck);
+    if (c->eck0) cudaEventDestroy(c->eck0);
+    if (c->eck1) cudaEventDestroy(c->eck1);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
     clear_graphs(c);
     if (c->arena) cudaFree(c->arena);
     if (c->h_ks) cudaFreeHost(c->h_ks);
@@ -945,6 +1104,223 @@ int drd_interpolate_coef(drd_ctx* c, const double* dist, double* fpd_ph, double*
     rc = down(c, fpd_ph, c->fpd, c->cs) | down(c, rho, c->rho, c->cs) | down(c, eta, c->eta, c->cs);
     if (rc) return DRD_ERR_CUDA;
     return finish_call(c, 0, nullptr, false);
+}
+
+int drd_particle_params_default(drd_particle_params* pp, double lx, double ly) {
+    if (!pp) return DRD_ERR_BADARG;
+    memset(pp, 0, sizeof(*pp));
+    pp->np = 9;                                                 // particles_params.f90:78
+    pp->lx = lx;
+    pp->ly = ly;
+    pp->fpd_radius = 0.05 / 2.0;                                // :80
+    pp->l0 = 2 * (pp->fpd_radius + 0.00);                       // :83 (fpd_inter_dist = 0, :81)
+    pp->ks = 5;                                                 // :74
+    pp->kb = 0.0025 * 100;                                      // :75
+    pp->theta0 = 0.0;                                           // :76
+    pp->k0_inter = 2.5;                                         // :93
+    pp->k0_inter_bdr = 2.5 * 10;                                // :94
+    pp->fpd_fpd_dist = pp->fpd_radius + pp->fpd_radius + 0.01;  // :97
+    pp->fpd_bdr_dist = pp->fpd_radius + 0.02;                   // :98
+    return DRD_OK;
+}
+
+int drd_particle_initialize(const drd_particle_params* pp, double xc, double yc, double* points) {
+    // particle_initialize, fibers: particles_move.f90:50-68
+    if (!pp || !points || pp->np < 0 || pp->np > DRD_PARTICLES_MAX) return DRD_ERR_BADARG;
+    const int np = pp->np;
+    if (np > 2) {
+        const int mid = (int)std::floor(np / 2.0);
+        points[mid] = xc;
+        points[np + mid] = yc;
+        for (int i = 0; i < mid; ++i) {
+            points[i] = xc;
+            points[np + i] = yc + (mid - i) * pp->l0;
+            points[np - i - 1] = xc;
+            points[np + np - i - 1] = yc - (mid - i) * pp->l0;
+        }
+    }
+    return DRD_OK;
+}
+
+int drd_particles_set(drd_ctx* c, const drd_particle_params* pp, const double* points, const double* bdr_dist) {
+    if (!c || !pp) return DRD_ERR_BADARG;
+    if (pp->np != 0 && (pp->np < 3 || pp->np > DRD_PARTICLES_MAX || !points || !bdr_dist || !(pp->lx > 0) ||
+                        !(pp->ly > 0) || !(pp->fpd_radius > 0))) {
+        c->err = "drd_particles_set: np must be 0 or 3..DRD_PARTICLES_MAX with points, bdr_dist and a positive box";
+        return DRD_ERR_BADARG;
+    }
+    const int changed = std::memcmp(pp, &c->pp, sizeof(*pp)) != 0;
+    c->pp = *pp;
+    if (pp->np > 0) {
+        CK(cudaMemcpyAsync(c->pts, points, sizeof(double) * 2 * pp->np, cudaMemcpyHostToDevice, c->s));
+        CK(cudaMemcpyAsync(c->pts_old, points, sizeof(double) * 2 * pp->np, cudaMemcpyHostToDevice, c->s));
+        CK(cudaMemsetAsync(c->totF, 0, sizeof(double) * 2 * DRD_PARTICLES_MAX, c->s));
+        if (up(c, c->bdist, bdr_dist, c->cs)) return DRD_ERR_CUDA;
+    }
+    CK(cudaStreamSynchronize(c->s));
+    if (changed) clear_graphs(c);  // the step graph holds the particle launches and their parameters
+    return DRD_OK;
+}
+
+int drd_particles_get(drd_ctx* c, double* points, double* tot_F) {
+    if (!c) return DRD_ERR_BADARG;
+    const size_t b = sizeof(double) * 2 * c->pp.np;
+    if (b && points) CK(cudaMemcpyAsync(points, c->pts, b, cudaMemcpyDeviceToHost, c->s));
+    if (b && tot_F) CK(cudaMemcpyAsync(tot_F, c->totF, b, cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    return DRD_OK;
+}
+
+int drd_force_caculation_vel(drd_ctx* c, double dt, double t, double* pf1, double* pf2) {
+    (void)t;  // only the swimmers' tumbling clock reads t (particles_move.f90:600), and Np_swm = 0
+    if (!c || !pf1 || !pf2) return DRD_ERR_BADARG;
+    if (c->pp.np <= 0) { c->err = "no resident particles (drd_particles_set)"; return DRD_ERR_BADARG; }
+    CK(cudaEventRecord(c->ev0, c->s));
+    const double dt_keep = c->P.dt;
+    c->P.dt = dt;
+    enq_particles(c, PT_FORCE, nullptr, nullptr, c->s);
+    c->P.dt = dt_keep;
+    CK(cudaGetLastError());
+    if (down(c, pf1, c->fld[DRD_F_PF1], c->cs) | down(c, pf2, c->fld[DRD_F_PF2], c->cs)) return DRD_ERR_CUDA;
+    return finish_call(c, 0, nullptr, false);
+}
+
+int drd_update_position_vel(drd_ctx* c, const double* u, const double* v, double dt) {
+    if (!c || !u || !v) return DRD_ERR_BADARG;
+    if (c->pp.np <= 0) { c->err = "no resident particles (drd_particles_set)"; return DRD_ERR_BADARG; }
+    CK(cudaEventRecord(c->ev0, c->s));
+    if (up(c, c->u_after, u, c->us) | up(c, c->v_after, v, c->vs)) return DRD_ERR_CUDA;
+    const double dt_keep = c->P.dt;
+    c->P.dt = dt;
+    enq_particles(c, PT_MOVE, c->u_after, c->v_after, c->s);
+    c->P.dt = dt_keep;
+    CK(cudaGetLastError());
+    return finish_call(c, 0, nullptr, false);
+}
+
+int drd_interpolate_coef_particles(drd_ctx* c, double* fpd_ph, double* rho, double* eta) {
+    if (!c) return DRD_ERR_BADARG;
+    CK(cudaEventRecord(c->ev0, c->s));
+    enq_particles(c, PT_COEF, nullptr, nullptr, c->s);
+    CK(cudaGetLastError());
+    if (down(c, fpd_ph, c->fpd, c->cs) | down(c, rho, c->rho, c->cs) | down(c, eta, c->eta, c->cs)) return DRD_ERR_CUDA;
+    return finish_call(c, 0, nullptr, false);
+}
+
+// Wall prefactors cf = sqrt(2) cos(angle pi/180)/3 pi/2 of PhSolve_ori (:48, :87) and alpha_s.
+// The captured graphs read cf from device memory but take alpha_s by value, so a new alpha_s
+// drops the PhSolve_ori graphs.
+int set_ori_walls(drd_ctx* c, const double* angleB, const double* angleT, double alpha_s) {
+    std::vector<double> cb(c->nr + 1), ct(c->nr + 1);
+    for (int i = 0; i <= c->nr; ++i) {
+        const double aB = angleB ? angleB[i] : 0.0, aT = angleT ? angleT[i] : 0.0;
+        cb[i] = std::sqrt(2.0) * std::cos(aB * kPi / 180.0) / 3.0 * kPi / 2.;
+        ct[i] = std::sqrt(2.0) * std::cos(aT * kPi / 180.0) / 3.0 * kPi / 2.;
+    }
+    CK(cudaMemcpyAsync(c->ori_cfb, cb.data(), sizeof(double) * cb.size(), cudaMemcpyHostToDevice, c->s));
+    CK(cudaMemcpyAsync(c->ori_cft, ct.data(), sizeof(double) * ct.size(), cudaMemcpyHostToDevice, c->s));
+    CK(cudaStreamSynchronize(c->s));  // the host vectors go out of scope
+    if (alpha_s != c->ori_alpha) {
+        c->ori_alpha = alpha_s;
+        for (int m = 0; m < 2; ++m) {
+            auto it = c->graphs.find(gkey(GK_ORI, m, 0));
+            if (it != c->graphs.end()) { cudaGraphExecDestroy(it->second); c->graphs.erase(it); }
+        }
+    }
+    return DRD_OK;
+}
+
+int drd_phsolve_ori(drd_ctx* c, const double* u, const double* v, const double* ph, const double* angleB,
+                    const double* angleT, double alpha_s, double* rmu_after, double* ph_after, drd_status* st) {
+    if (!c || !u || !v || !ph || !rmu_after || !ph_after) return DRD_ERR_BADARG;
+    if (c->P.variant != DRD_VARIANT_MF) { c->err = "PhSolve_ori belongs to the MF variant"; return DRD_ERR_BADARG; }
+    int rc = set_ori_walls(c, angleB, angleT, alpha_s);
+    if (rc) return rc;
+    CK(cudaEventRecord(c->ev0, c->s));
+    rc = up(c, c->fld[DRD_F_U], u, c->us) | up(c, c->fld[DRD_F_V], v, c->vs) | up(c, c->fld[DRD_F_PH], ph, c->cs);
+    if (rc) return DRD_ERR_CUDA;
+    rc = run_graph(c, gkey(GK_ORI, mixed_of(c), 0), [&](cudaStream_t s) { return enq_ori(c, s); }, 0.0, 0.0);
+    if (rc) return rc;
+    if (down(c, rmu_after, c->rmu_after, c->cs) | down(c, ph_after, c->ph_after, c->cs)) return DRD_ERR_CUDA;
+    return finish_call(c, KS_CH, st, true);
+}
+
+int drd_finit_wall(drd_ctx* c, const double* bdr_in, int nsteps, double* bdr_out, double* ph_out, double* rmu_out) {
+    if (!c || !bdr_in || nsteps < 0) return DRD_ERR_BADARG;
+    if (c->P.variant != DRD_VARIANT_MF) { c->err = "finit's wall smoothing belongs to the MF variant"; return DRD_ERR_BADARG; }
+    int rc = set_ori_walls(c, nullptr, nullptr, 0.0);
+    if (rc) return rc;
+    double* ph = c->fld[DRD_F_PH];
+    double* rmu = c->fld[DRD_F_RMU];
+    const size_t cb = sizeof(double) * c->cs;
+    if (up(c, ph, bdr_in, c->cs)) return DRD_ERR_CUDA;                   // finit.f90:123-133
+    launch_fill_neumann(c->nr, c->nz, ph, nullptr, c->ctr, c->s);
+    CK(cudaMemsetAsync(c->fld[DRD_F_U], 0, sizeof(double) * c->us, c->s));  // u = v = 0 (mcl6.f90:143)
+    CK(cudaMemsetAsync(c->fld[DRD_F_V], 0, sizeof(double) * c->vs, c->s));
+    CK(cudaMemsetAsync(rmu, 0, cb, c->s));
+    launch_ori_rmu0(c->dp, ph, rmu, c->ctr, c->s);                        // finit.f90:163-169
+    int info = 0;
+    for (int it = 0; it < nsteps; ++it) {                                 // finit.f90:172-176
+        rc = run_graph(c, gkey(GK_ORI, mixed_of(c), 0), [&](cudaStream_t s) { return enq_ori(c, s); }, 0.0, 0.0);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(rmu, c->rmu_after, cb, cudaMemcpyDeviceToDevice, c->s));
+        CK(cudaMemcpyAsync(ph, c->ph_after, cb, cudaMemcpyDeviceToDevice, c->s));
+    }
+    launch_ori_bdr(c->nr, c->nz, ph, c->w, c->ctr, c->s);                 // finit.f90:178-189
+    CK(cudaGetLastError());
+    if (down(c, bdr_out, c->w, c->cs) | down(c, ph_out, ph, c->cs) | down(c, rmu_out, rmu, c->cs)) return DRD_ERR_CUDA;
+    CK(cudaMemcpyAsync(c->h_ks + KS_CH, c->ks + KS_CH, sizeof(KState), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    if (nsteps > 0) info = c->h_ks[KS_CH].info;
+    return info;
+}
+
+int drd_checkpoint_wait(drd_ctx* c) {
+    if (!c) return DRD_ERR_BADARG;
+    if (c->ckpt.joinable()) c->ckpt.join();
+    const int rc = c->ckpt_rc;
+    c->ckpt_rc = 0;
+    return rc;
+}
+
+int drd_checkpoint_async(drd_ctx* c, const char* path, double t) {
+    if (!c || !path) return DRD_ERR_BADARG;
+    int rc = drd_checkpoint_wait(c);
+    if (rc) return rc;
+    const long us = c->us, vs = c->vs, cs = c->cs;
+    if (!c->h_stage) {
+        CK(cudaMallocHost(&c->h_stage, sizeof(double) * (us + vs + 3 * cs)));
+        CK(cudaStreamCreateWithFlags(&c->sck, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&c->eck0, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->eck1, cudaEventDisableTiming));
+    }
+    double* hu = c->h_stage;
+    double* hv = hu + us;
+    double* hp = hv + vs;
+    double* hf = hp + cs;
+    double* hph = hf + cs;
+    // the copies start after the work already on the context stream, and later work on that
+    // stream (the next step rewrites these fields) waits for them
+    CK(cudaEventRecord(c->eck0, c->s));
+    CK(cudaStreamWaitEvent(c->sck, c->eck0, 0));
+    CK(cudaMemcpyAsync(hu, c->fld[DRD_F_U], sizeof(double) * us, cudaMemcpyDeviceToHost, c->sck));
+    CK(cudaMemcpyAsync(hv, c->fld[DRD_F_V], sizeof(double) * vs, cudaMemcpyDeviceToHost, c->sck));
+    CK(cudaMemcpyAsync(hp, c->fld[DRD_F_P], sizeof(double) * cs, cudaMemcpyDeviceToHost, c->sck));
+    CK(cudaMemcpyAsync(hf, c->fpd, sizeof(double) * cs, cudaMemcpyDeviceToHost, c->sck));
+    CK(cudaMemcpyAsync(hph, c->fld[DRD_F_PH], sizeof(double) * cs, cudaMemcpyDeviceToHost, c->sck));
+    CK(cudaEventRecord(c->eck1, c->sck));
+    CK(cudaStreamWaitEvent(c->s, c->eck1, 0));
+    const std::string file(path);
+    const int nr = c->nr, nz = c->nz, dev = c->device;
+    const double dr = c->P.dr, dz = c->P.dz;
+    cudaEvent_t done = c->eck1;
+    c->ckpt = std::thread([=]() {
+        int r = DRD_OK;
+        if (cudaSetDevice(dev) != cudaSuccess || cudaEventSynchronize(done) != cudaSuccess) r = DRD_ERR_CUDA;
+        else r = drd_output(file.c_str(), nr, nz, dr, dz, nullptr, nullptr, hu, hv, hp, hf, hph, t);
+        c->ckpt_rc = r;
+    });
+    return DRD_OK;
 }
 
 int drd_phsolve(drd_ctx* c, const double* u, const double* v, const double* ph, const double* rmu, double t,
@@ -1171,25 +1547,25 @@ int drd_kernel_bench(drd_ctx* c, int which, int reps, double* us, double* bytes,
                                         c->k32.v, nullptr, 0, dots(c), 0, nullptr, G_ALWAYS, nullptr, s);
                 break;
             case DRD_KB_DCT_X_FP64: {
-                auto a = gargs<double>(c, nz, nr, nr, c->k64.p, nr, c->m1xT, nr, c->t1, nr, nullptr, G_ALWAYS);
+                auto a = dct1_xpass<double>(c, c->k64.p, c->t1, nullptr, G_ALWAYS);
                 a.ctr = nullptr;
                 launch_gemm<double>(gcfg<double>(c, 0), EPI_STORE, a, s);
                 break;
             }
             case DRD_KB_DCT_X_FP32: {
-                auto a = gargs<float>(c, nz, nr, nr, c->k32.p, nr, c->m1xT32, nr, c->t1f, nr, nullptr, G_ALWAYS);
+                auto a = dct1_xpass<float>(c, c->k32.p, c->t1f, nullptr, G_ALWAYS);
                 a.ctr = nullptr;
                 launch_gemm<float>(gcfg<float>(c, 0), EPI_STORE, a, s);
                 break;
             }
             case DRD_KB_DCT_Z_FP64: {
-                auto a = gargs<double>(c, nz, nr, nz, c->m1z, nz, c->k64.p, nr, c->t1, nr, nullptr, G_ALWAYS);
+                auto a = dct1_zpass<double>(c, c->k64.p, c->t1, nullptr, G_ALWAYS);
                 a.ctr = nullptr;
                 launch_gemm<double>(gcfg<double>(c, 1), EPI_STORE, a, s);
                 break;
             }
             case DRD_KB_DCT_Z_FP32: {
-                auto a = gargs<float>(c, nz, nr, nz, c->m1z32, nz, c->k32.p, nr, c->t1f, nr, nullptr, G_ALWAYS);
+                auto a = dct1_zpass<float>(c, c->k32.p, c->t1f, nullptr, G_ALWAYS);
                 a.ctr = nullptr;
                 launch_gemm<float>(gcfg<float>(c, 1), EPI_STORE, a, s);
                 break;
@@ -1203,10 +1579,11 @@ int drd_kernel_bench(drd_ctx* c, int which, int reps, double* us, double* bytes,
     switch (which) {
         case DRD_KB_UV_MATVEC_FP64: by = 8.0 * (2.0 * S.n + 3.0 * c->cs); fl = 45.0 * S.n; break;
         case DRD_KB_UV_MATVEC_FP32: by = 4.0 * (2.0 * S.n + 3.0 * c->cs); fl = 45.0 * S.n; break;
-        case DRD_KB_DCT_X_FP64: by = 8.0 * (2.0 * c->nc + (double)nr * nr); fl = 2.0 * nz * (double)nr * nr; break;
-        case DRD_KB_DCT_X_FP32: by = 4.0 * (2.0 * c->nc + (double)nr * nr); fl = 2.0 * nz * (double)nr * nr; break;
-        case DRD_KB_DCT_Z_FP64: by = 8.0 * (2.0 * c->nc + (double)nz * nz); fl = 2.0 * nr * (double)nz * nz; break;
-        case DRD_KB_DCT_Z_FP32: by = 4.0 * (2.0 * c->nc + (double)nz * nz); fl = 2.0 * nr * (double)nz * nz; break;
+        // folded passes: K = floor((N-1)/2)+1 multiply-adds per output
+        case DRD_KB_DCT_X_FP64: by = 8.0 * (2.0 * c->nc + 2.0 * c->Kx * c->Nxe); fl = 2.0 * c->nc * c->Kx; break;
+        case DRD_KB_DCT_X_FP32: by = 4.0 * (2.0 * c->nc + 2.0 * c->Kx * c->Nxe); fl = 2.0 * c->nc * c->Kx; break;
+        case DRD_KB_DCT_Z_FP64: by = 8.0 * (2.0 * c->nc + 2.0 * c->Mze * c->Kz); fl = 2.0 * c->nc * c->Kz; break;
+        case DRD_KB_DCT_Z_FP32: by = 4.0 * (2.0 * c->nc + 2.0 * c->Mze * c->Kz); fl = 2.0 * c->nc * c->Kz; break;
         default: by = 4.0 * (3.0 * c->nc + 2.0 * c->cs); fl = 40.0 * c->nc; break;
     }
     CK(cudaMemsetAsync(c->k64.p, 0, sizeof(double) * c->nmax, c->s));

@@ -94,7 +94,17 @@ def _empty_state(nr, nz):
     return st
 
 
-def make_case(name="c2", seed=0, nr=None, nz=None, precision=abi.DRD_PREC_FP64, **overrides):
+def fpd_dist_host(pp, points, nr, nz, dr, dz):
+    """dist(r(i,k), z(i,k)) = fpd_dist of the beads (particles_move.f90:361-391), shape (nz, nr)."""
+    X = ((np.arange(nr) + 0.5) * dr)[None, :]
+    Z = ((np.arange(nz) + 0.5) * dz)[:, None]
+    d = np.full((nz, nr), 1.0e10)
+    for b in range(pp.np):
+        d = np.minimum(d, np.sqrt((X - points[0, b]) ** 2 + (Z - points[1, b]) ** 2) - pp.fpd_radius)
+    return d
+
+
+def make_case(name="c2", seed=0, nr=None, nz=None, precision=abi.DRD_PREC_FP64, particles=False, **overrides):
     rng = np.random.default_rng(seed)
     name = name.lower()
     if name == "c1":
@@ -151,6 +161,27 @@ def make_case(name="c2", seed=0, nr=None, nz=None, precision=abi.DRD_PREC_FP64, 
             sdf = np.minimum(sdf, _rect_sdf(X / dr, Z / dz, cxc, czc, 20.0 * sx, 2.0 * sz, ang))
         dist = sdf * min(dr, dz)
         meta["fibers"] = fibers
+    if particles:
+        # the reference's fiber instead of the rigid fibers: a chain of Np = 9 beads placed by
+        # particle_initialize (particles_move.f90:50-68) at mid-length on the channel centre line
+        # (mcl6.f90:178 places it at (slen/2, 0.42) in its own channel), and bdr_ph_dist = the
+        # distance to the walls inside the channel, 0 in the solid (global.f90:83)
+        lx, ly = nr * dr, nz * dz
+        pp = abi.default_particle_params(lx, ly)
+        if name in ("c2", "tp"):
+            ic = nr // 2
+            ycen = yc[ic] * dz
+            bd_cells = np.maximum(d_cells, 0.0) * min(dr, dz)
+        else:
+            ycen = ly / 2.0
+            bd_cells = np.minimum(Z, ly - Z)
+        points = np.array(abi.particle_chain(pp, lx / 2.0, ycen), dtype=np.float64)
+        bdr_dist = np.zeros(cell_shape(nr, nz))
+        bdr_dist[1:-1, 1:-1] = bd_cells
+        neumann_ghosts_cell(bdr_dist)
+        dist = fpd_dist_host(pp, points, nr, nz, dr, dz)
+        meta["particles"] = {"pp": pp, "points": points, "bdr_dist": bdr_dist}
+        meta.pop("fibers", None)
     fpd, rho, eta = interpolate_coef_host(p, dist, bdr)
     # phase field: drops (phi = 1 inside), clipped by the solid (finit.f90:288)
     ph = np.zeros(cell_shape(nr, nz))

@@ -76,7 +76,8 @@ typedef struct drd_params {
     int32_t ch_maxit;      /* PhSolve ITER, 500 (PhSolve.f90:72)                                   */
     int32_t uv_maxit;      /* VeloSolve ITER, 800 MF (VeloSolve_2_combined.f90:398), 2000 TP       */
     int32_t phmu_maxit;    /* ph_mu_solve ITER, 5000 (TP/ph_mu_solve.f90:156)                      */
-    int32_t reserved0;
+    int32_t guess_mode;    /* initial guess of drd_step's Krylov solves: 0 = the previous step's   */
+                           /* field (the reference), 1 = linear extrapolation 2 x^n - x^(n-1)     */
     double dr, dz, dt;     /* grid spacing and time step (finit.f90:25-28,397)                    */
     double xld, re, ca;    /* 1/Pe, Reynolds, capillary number (input deck lines 1-3)             */
     double I_thickness;    /* interface thickness epsilon (deck line 18)                           */
@@ -138,6 +139,76 @@ int drd_set_tp_fields(drd_ctx* ctx, const double* bdr_ph_used, const double* bdr
  * particle distance dist(r(i,k), z(i,k)) of every interior cell (DIST shape); fpd_ph, rho,
  * eta (CELL) are written and rho/eta also replace the context's coefficients. */
 int drd_interpolate_coef(drd_ctx* ctx, const double* dist, double* fpd_ph, double* rho, double* eta);
+
+/* ---- initialisation: finit's wall smoothing ------------------------------------------- */
+
+/* PhSolve_ori(rmu_after, ph_after, t) (microfluidics_complex_domain/PhSolve_ori.f90:1-214):
+ * the phi in [-1,1] Cahn-Hilliard step with unit mobility and the wall-energy rows at the
+ * bottom and top, solved by BiCGSTAB with the PhSolve DCT-I preconditioner.  Inputs u (UFACE),
+ * v (VFACE), ph (CELL); angleB, angleT (XLINE, degrees; NULL = 0) and alpha_s are the module
+ * globals of its wall terms.  Left/right are Neumann and the wall rows take the non-dynamic
+ * branch: finit forces lr_bd_type = top/bot_type_ph = 'n' around its calls (finit.f90:144-147).
+ * The context's dt, tol and ch_maxit are the solve's (finit runs it with dt = 1e-4). */
+int drd_phsolve_ori(drd_ctx* ctx, const double* u, const double* v, const double* ph, const double* angleB,
+                    const double* angleT, double alpha_s, double* rmu_after, double* ph_after, drd_status* st);
+/* finit's wall smoothing (finit.f90:120-189): ph = bdr_ph (CELL, interior read) with Neumann
+ * ghosts, rmu from ph, then `nsteps` PhSolve_ori steps with u = v = 0 and zero angles and
+ * alpha_s (finit sets those after the loop, finit.f90:364-374), then
+ * bdr_ph = (ph + 1)/2 clipped to [0, 1] on the interior.  The reference runs 51 steps
+ * (finit.f90:172) on a context whose dt is 1e-4 (finit.f90:151).  bdr_ph_out, ph_out, rmu_out
+ * (CELL) may be NULL.  The context's resident u, v, ph and rmu fields are overwritten.
+ * Returns the last solve's INFO. */
+int drd_finit_wall(drd_ctx* ctx, const double* bdr_ph_in, int nsteps, double* bdr_ph_out, double* ph_out,
+                   double* rmu_out);
+
+/* ---- fiber particles coupled to the flow (microfluidics_complex_domain/particles_move.f90) --
+ *
+ * A fiber is a chain of Np beads (module particles: points(0:Np-1,0:1)).  Per step the driver
+ * (mcl6.f90:394-402) computes the chain forces, spreads them onto the grid as
+ * particle_force1/2, moves the beads with the fluid and rebuilds fpd_ph, rho and eta from the
+ * new bead positions.  Point arrays are POINTS shaped: Np x 2, column-major like the Fortran
+ * points(0:Np-1,0:1) (x of bead b at [b], y at [Np + b]).  Swimmers are not modelled: the
+ * reference fixes Np_swm = 0 (particles_params.f90:61). */
+#define DRD_PARTICLES_MAX 64
+
+/* The parameters of module particles_params (microfluidics_complex_domain/particles_params.f90). */
+typedef struct drd_particle_params {
+    int32_t np;            /* beads Np (:78); 0 = no particles, else 3..DRD_PARTICLES_MAX      */
+    int32_t reserved0;
+    double lx, ly;         /* periodic box: slen, shig (mcl6.f90:397)                         */
+    double fpd_radius;     /* bead radius (:80)                                               */
+    double l0;             /* rest length between beads (:83)                                 */
+    double ks, kb;         /* stretching and bending stiffness (:74-75)                       */
+    double theta0;         /* rest bending angle (:76)                                        */
+    double k0_inter;       /* bead-bead repulsion (:93)                                       */
+    double k0_inter_bdr;   /* wall repulsion (:94)                                            */
+    double fpd_fpd_dist;   /* bead-bead repulsion range (:97)                                 */
+    double fpd_bdr_dist;   /* wall repulsion range (:98)                                      */
+} drd_particle_params;
+
+/* Fills `pp` with the reference's values (Np = 9, radius 0.025, ks 5, kb 0.25, ...) for a box
+ * of lx x ly. */
+int drd_particle_params_default(drd_particle_params* pp, double lx, double ly);
+/* particle_initialize's fiber placement (particles_move.f90:50-68): a straight vertical chain
+ * centred on (xc, yc), bead spacing l0.  Host-only; writes POINTS. */
+int drd_particle_initialize(const drd_particle_params* pp, double xc, double yc, double* points);
+/* Makes the chain resident: parameters, POINTS and bdr_ph_dist (CELL; the distance to the
+ * walls that interaction_force_bdr samples, global.f90:83).  pp->np == 0 turns the coupling
+ * off.  While np > 0, drd_step runs the particle coupling of mcl6.f90:394-402 every step. */
+int drd_particles_set(drd_ctx* ctx, const drd_particle_params* pp, const double* points, const double* bdr_dist);
+/* Current bead positions and the last computed total bead forces tot_F (both POINTS; either
+ * may be NULL). */
+int drd_particles_get(drd_ctx* ctx, double* points, double* tot_F);
+/* force_caculation_vel (particles_move.f90:758-868 with force_caculation :421-627): chain,
+ * bead-bead and wall forces, spread onto the grid as particle_force1/2 (CELL, written). */
+int drd_force_caculation_vel(drd_ctx* ctx, double dt, double t, double* particle_force1, double* particle_force2);
+/* update_position_vel (particles_move.f90:872-980): moves every bead by dt times the
+ * indicator-weighted mean of u (UFACE) and v (VFACE), wrapping periodically. */
+int drd_update_position_vel(drd_ctx* ctx, const double* u, const double* v, double dt);
+/* interpolate_coef with dist = fpd_dist of the resident beads (particles_move.f90:361-391,
+ * dist.f90): fpd_ph, rho, eta (CELL) written (each may be NULL); rho/eta also replace the
+ * context's coefficients. */
+int drd_interpolate_coef_particles(drd_ctx* ctx, double* fpd_ph, double* rho, double* eta);
 
 /* PhSolve(rmu_after, ph_after, t) (microfluidics_complex_domain/PhSolve.f90:1-126).
  * Inputs u (UFACE), v (VFACE), ph, rmu (CELL) are the module globals it reads. */
@@ -212,14 +283,65 @@ typedef struct drd_step_stats {
 } drd_step_stats;
 
 /* One pass of the mcl6 time loop body (microfluidics_complex_domain/mcl6.f90:378-486, the
- * first step :239-306 when `first` != 0): CH solve -> momentum -> swaps -> pressure ->
- * p += psi2, on the resident state, with particles held fixed (coefficients as last set).
+ * first step :239-306 when `first` != 0): CH solve -> [particle coupling] -> momentum ->
+ * swaps -> pressure -> p += psi2, on the resident state.  The particle coupling
+ * (force_caculation_vel, update_position_vel, interpolate_coef) runs when drd_particles_set
+ * made a chain resident; otherwise the coefficients stay as last set.
  * t is the time before the step; solves see t + dt as in the reference.  `stats` may be NULL;
  * when non-NULL the call waits for the step and fills it. */
 int drd_step(drd_ctx* ctx, int first, double t, drd_step_stats* stats);
 /* Enqueue `nsteps` steps without host synchronisation (stats are not collected). */
 int drd_steps_async(drd_ctx* ctx, int first, double t, int nsteps);
 int drd_synchronize(drd_ctx* ctx);
+
+/* ---- input deck and checkpoint files --------------------------------------------------- */
+
+/* The `input` deck that mcl6 reads line by line with list-directed READ
+ * (microfluidics_complex_domain/mcl6.f90:68-99; the TP deck adds is_complex_domain,
+ * two_phase_flow_complex_domain/mcl6.f90:100).  Only the first value of each line is read,
+ * as list-directed input does; the rest of the line (the deck's '!' notes) is ignored. */
+typedef struct drd_deck {
+    double xld, re, ca, vs, xlsT, xlsB, xlsL, xlsR, uwT, uwB, slen, shig, angle, slipratio;
+    int32_t iflag, istep;
+    double tf, I_thickness, s_implicit, tol, ggz, ggx, time_step_change, lambda_rho, lambda_eta, UU;
+    char lr_bd_type, top_type_ph, bot_type_ph, top_type_u, bot_type_u, is_complex_domain;
+    char pad[2];
+    int32_t entries;       /* values read: 31 for an MF deck, 32 for a TP deck */
+    int32_t reserved;
+} drd_deck;
+/* Parses a deck file.  Returns DRD_OK, or DRD_ERR_BADARG with a message in `err` (may be NULL,
+ * `err_len` bytes) when the file cannot be read or a value does not parse. */
+int drd_read_deck(const char* path, drd_deck* deck, char* err, int err_len);
+/* drd_params of an nr x nz grid from a deck, as finit and mcl6 derive them: dr = slen/nr,
+ * dz = shig/nz (finit.f90:25-26), dt = min(dr,dz) * time_step_change (finit.f90:395-397),
+ * twall = 0.1 (mcl6.f90:140), penalty_k = 1e5 (global.f90:91), bdr_low/upp = 0.1725/0.6725
+ * (finit.f90:104-105); `variant` selects the application. */
+int drd_params_from_deck(const drd_deck* deck, int nr, int nz, int variant, drd_params* params);
+
+/* output(M,N,x,y,u,v,p,f,f2,t,fname) (microfluidics_complex_domain/inout.f90:1-19): a Fortran
+ * unformatted sequential file (4-byte record markers) with the records
+ * ((a(i,k),k=0,nz),i=0,nr) of x, y, u, v, p, f, f2 and the record t.  x and y are NODE shaped,
+ * (nr+1)*(nz+1) doubles with element (i,k) at [i + k*(nr+1)] (the grids r(0:nr,0:nz),
+ * z(0:nr,0:nz)); u UFACE, v VFACE, p, f, f2 CELL.  mcl6 writes fpd_ph as f and ph as f2
+ * (mcl6.f90:352).  x or y NULL writes the cell-centre grid (i+0.5)dr, (k+0.5)dz. */
+int drd_output(const char* path, int nr, int nz, double dr, double dz, const double* x, const double* y,
+               const double* u, const double* v, const double* p, const double* f, const double* f2, double t);
+/* input(M,N,x,y,u,v,p,f,t,fname) (inout.f90:41-60): reads the six field records and then t
+ * from the NEXT record, which in a file written by output is f2's, so t receives f2(0,0) as
+ * in the reference.  drd_read_time returns the true t of the last record instead.  Any array
+ * may be NULL (skipped). */
+int drd_input(const char* path, int nr, int nz, double* x, double* y, double* u, double* v, double* p, double* f,
+              double* t);
+int drd_read_time(const char* path, int nr, int nz, double* t);
+/* output_particles (particles_move.f90:312-323): one record ((points(i,k),i=0,Np-1),k=0,1). */
+int drd_output_particles(const char* path, int np, const double* points);
+/* The output of the resident state: u, v, p, the context's fpd_ph (from the last
+ * interpolate_coef or particle step) and ph, written as drd_output does.  The device copies
+ * are ordered after the work already enqueued and before any later step, and the file is
+ * written by a host thread while the GPU runs on; drd_checkpoint_wait joins it (and reports
+ * its status).  One checkpoint may be in flight per context. */
+int drd_checkpoint_async(drd_ctx* ctx, const char* path, double t);
+int drd_checkpoint_wait(drd_ctx* ctx);
 
 /* ---- pressure step without device allocation ------------------------------------------- */
 

@@ -503,6 +503,215 @@ int orc_phsolve(const drd_params* P, const double* ph_lcc, const double* u, cons
 }
 
 /* ---------------------------------------------------------------------------------------
+ * PhSolve_ori: microfluidics_complex_domain/PhSolve_ori.f90 (phi in [-1,1], constant
+ * mobility, wall-energy boundary rows), the solve finit repeats to smooth the wall indicator
+ * (finit.f90:120-189).  Neumann left/right (laplace_nn) and the non-dynamic wall branch, which
+ * is what finit selects (finit.f90:144-147).
+ * ------------------------------------------------------------------------------------- */
+/* laplace_nn (PhSolve_ori.f90:463-487): writes a's Neumann ghosts, then the 5-point Laplacian. */
+static void laplace_nn(int nr, int nz, double dr2, double dz2, double* a, double* b) {
+    for (int i = 0; i < nr; ++i) {
+        a[CI(i, -1)] = a[CI(i, 0)];
+        a[CI(i, nz)] = a[CI(i, nz - 1)];
+    }
+    for (int j = -1; j <= nz; ++j) {
+        a[CI(-1, j)] = a[CI(0, j)];
+        a[CI(nr, j)] = a[CI(nr - 1, j)];
+    }
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i < nr; ++i)
+            b[CI(i, j)] = (a[CI(i + 1, j)] + a[CI(i - 1, j)] - 2 * a[CI(i, j)]) / dr2 +
+                          (a[CI(i, j + 1)] + a[CI(i, j - 1)] - 2 * a[CI(i, j)]) / dz2;
+}
+
+/* coef_bot = coef_top of the non-dynamic branch (PhSolve_ori.f90:71-74, :111-113). */
+double orc_ori_coef(const drd_params* P, double alpha_s) {
+    const double tmp1 = P->I_thickness / P->dz + 0.5 * alpha_s;
+    return (P->I_thickness / P->dz - 0.5 * alpha_s) / tmp1;
+}
+
+typedef struct { const drd_params* P; double cb, ct; const double* lcc; } ori_ctx;
+
+/* MATRIX_VECTOR_CG_ori (PhSolve_ori.f90:368-421). */
+void orc_ori_matvec(const drd_params* P, double coef_bot, double coef_top, double alpha, const double* x,
+                    double beta, double* y) {
+    const int nr = P->nr, nz = P->nz;
+    const long cs = cell_size(nr, nz);
+    const double dr2 = P->dr * P->dr, dz2 = P->dz * P->dz, eps = P->I_thickness;
+    double* f1 = dalloc(cs);
+    double* ff1 = dalloc(cs);
+    double* ff2 = dalloc(cs);
+    btoa_cell(nr, nz, f1, x);
+    laplace_nn(nr, nz, dr2, dz2, f1, ff1);
+    for (long q = 0; q < cs; ++q) ff1[q] = -eps * ff1[q];
+    for (int i = 0; i < nr; ++i) {
+        int j = 0;
+        ff1[CI(i, j)] = ff1[CI(i, j)] + eps / dz2 * (f1[CI(i, j - 1)] - coef_bot * f1[CI(i, j)]);
+        j = nz - 1;
+        ff1[CI(i, j)] = ff1[CI(i, j)] + eps / dz2 * (f1[CI(i, j + 1)] - coef_top * f1[CI(i, j)]);
+    }
+    for (long q = 0; q < cs; ++q) ff1[q] = ff1[q] + f1[q] * P->s_implicit / eps;
+    laplace_nn(nr, nz, dr2, dz2, ff1, ff2);
+    for (long q = 0; q < cs; ++q) ff2[q] = -(P->dt * P->xld * ff2[q]);
+    for (long q = 0; q < cs; ++q) ff2[q] = f1[q] + ff2[q];
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i < nr; ++i) {
+            const long q = i + (long)nr * j;
+            y[q] = alpha * ff2[CI(i, j)] + beta * y[q];
+        }
+    free(f1); free(ff1); free(ff2);
+}
+static void ori_mv_cb(void* c, double a, const double* x, double b, double* y) {
+    ori_ctx* C = (ori_ctx*)c;
+    orc_ori_matvec(C->P, C->cb, C->ct, a, x, b, y);
+}
+static void ori_ps_cb(void* c, const double* x, double* y) {
+    ori_ctx* C = (ori_ctx*)c;
+    orc_ch_psolve(C->P, C->lcc, x, y); /* PSolve_CG_ori: the same DCT preconditioner (:426-441) */
+}
+
+/* RHS of PhSolve_ori (:23-139): f2 (CELL), packed rhs and guess Atob(ph), wall terms pnb/pnt. */
+void orc_ori_system(const drd_params* P, const double* u, const double* v, const double* ph, const double* angleB,
+                    const double* angleT, double alpha_s, double* f2, double* rhs, double* x0, double* pnb,
+                    double* pnt) {
+    const int nr = P->nr, nz = P->nz;
+    const double dr = P->dr, dz = P->dz, dt = P->dt, eps = P->I_thickness, s = P->s_implicit;
+    const double dr2 = dr * dr, dz2 = dz * dz;
+    const long cs = cell_size(nr, nz);
+    double* f1 = dalloc(cs);
+    double* ff = dalloc(cs);
+    memcpy(f2, ph, sizeof(double) * cs); /* :23 */
+    for (int k = 0; k < nz; ++k)        /* :26-32 */
+        for (int i = 0; i < nr; ++i)
+            f2[CI(i, k)] = f2[CI(i, k)] -
+                           dt * (u[UI(i + 1, k)] + u[UI(i, k)]) / 2.0 * (ph[CI(i + 1, k)] - ph[CI(i - 1, k)]) / 2.0 / dr -
+                           dt * (v[VI(i, k + 1)] + v[VI(i, k)]) / 2.0 * (ph[CI(i, k + 1)] - ph[CI(i, k - 1)]) / 2.0 / dz;
+    for (int k = 0; k < nz; ++k) /* :35-39 */
+        for (int i = 0; i < nr; ++i) {
+            const double p0 = ph[CI(i, k)];
+            f1[CI(i, k)] = ((1. + s) * p0 - p0 * p0 * p0) / eps;
+        }
+    const double tmp1 = eps / dz + 0.5 * alpha_s;
+    for (int i = 0; i < nr; ++i) { /* :44-49, :71-78 */
+        const int k = 0;
+        const double cf = sqrt(2.0) * cos((angleB ? angleB[i] : 0.0) * kPi / 180.0) / 3.0 * kPi / 2.;
+        const double tmp = (ph[CI(i, k - 1)] + ph[CI(i, k)]) / 2.0;
+        pnb[i] = cf * cos(tmp * kPi / 2) + alpha_s * tmp;
+        pnb[i] = pnb[i] / tmp1;
+        f1[CI(i, k)] = f1[CI(i, k)] + pnb[i] * eps / dz2;
+    }
+    for (int i = 0; i < nr; ++i) { /* :84-89, :110-118 */
+        const int k = nz - 1;
+        const double cf = sqrt(2.0) * cos((angleT ? angleT[i] : 0.0) * kPi / 180.0) / 3.0 * kPi / 2.;
+        const double tmp = (ph[CI(i, k)] + ph[CI(i, k + 1)]) / 2.0;
+        pnt[i] = cf * cos(tmp * kPi / 2) + alpha_s * tmp;
+        pnt[i] = pnt[i] / tmp1;
+        f1[CI(i, k)] = f1[CI(i, k)] + pnt[i] * eps / dz2;
+    }
+    laplace_nn(nr, nz, dr2, dz2, f1, ff); /* :126-130 */
+    for (long q = 0; q < cs; ++q) f2[q] = f2[q] - dt * P->xld * ff[q];
+    atob_cell(nr, nz, f2, rhs); /* :137-138 */
+    atob_cell(nr, nz, ph, x0);
+    free(f1); free(ff);
+}
+
+/* rmu from ph with its ghosts (PhSolve_ori.f90:187-194, finit.f90:163-169), interior. */
+static void ori_rmu(int nr, int nz, double dr2, double dz2, double eps, const double* ph, double* rmu) {
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) {
+            const double p0 = ph[CI(i, k)];
+            rmu[CI(i, k)] = -eps * ((ph[CI(i + 1, k)] + ph[CI(i - 1, k)] - 2 * p0) / dr2 +
+                                    (ph[CI(i, k + 1)] + ph[CI(i, k - 1)] - 2 * p0) / dz2) -
+                            p0 / eps + p0 * p0 * p0 / eps;
+        }
+}
+
+/* PhSolve_ori(rmu_after, ph_after, t) (PhSolve_ori.f90:1-214); t is unused by the routine. */
+int orc_phsolve_ori(const drd_params* P, const double* ph_lcc, const double* u, const double* v, const double* ph,
+                    const double* angleB, const double* angleT, double alpha_s, double* rmu_after, double* ph_after,
+                    drd_status* st) {
+    const int nr = P->nr, nz = P->nz;
+    const double dr2 = P->dr * P->dr, dz2 = P->dz * P->dz;
+    const long cs = cell_size(nr, nz), n = (long)nr * nz;
+    double* f2 = dalloc(cs);
+    double* rhs = dalloc(n);
+    double* x = dalloc(n);
+    double* pnb = dalloc(nr);
+    double* pnt = dalloc(nr);
+    orc_ori_system(P, u, v, ph, angleB, angleT, alpha_s, f2, rhs, x, pnb, pnt);
+    const double cb = orc_ori_coef(P, alpha_s);
+    ori_ctx C = {P, cb, cb, ph_lcc};
+    int info = orc_bicgstab(n, rhs, x, P->ch_maxit, P->tol, ori_mv_cb, ori_ps_cb, &C, st); /* :146-147 */
+    memset(ph_after, 0, sizeof(double) * cs);
+    btoa_cell(nr, nz, ph_after, x); /* :156 */
+    for (int i = 0; i < nr; ++i) {  /* :159-162 */
+        ph_after[CI(i, -1)] = ph_after[CI(i, 0)] * cb + pnb[i];
+        ph_after[CI(i, nz)] = ph_after[CI(i, nz - 1)] * cb + pnt[i];
+    }
+    for (int k = -1; k <= nz; ++k) { /* :169-173 */
+        ph_after[CI(-1, k)] = ph_after[CI(0, k)];
+        ph_after[CI(nr, k)] = ph_after[CI(nr - 1, k)];
+    }
+    memset(rmu_after, 0, sizeof(double) * cs);
+    ori_rmu(nr, nz, dr2, dz2, P->I_thickness, ph_after, rmu_after); /* :178-184 */
+    for (int i = 0; i < nr; ++i) {                                  /* :186-189 */
+        rmu_after[CI(i, -1)] = rmu_after[CI(i, 0)];
+        rmu_after[CI(i, nz)] = rmu_after[CI(i, nz - 1)];
+    }
+    for (int k = -1; k <= nz; ++k) { /* :197-201 */
+        rmu_after[CI(-1, k)] = rmu_after[CI(0, k)];
+        rmu_after[CI(nr, k)] = rmu_after[CI(nr - 1, k)];
+    }
+    free(f2); free(rhs); free(x); free(pnb); free(pnt);
+    return info;
+}
+
+/* finit's wall smoothing (finit.f90:120-189): ph = bdr_ph with Neumann ghosts, rmu from ph,
+ * `nsteps` PhSolve_ori solves with u = v = 0, then bdr_ph = (ph + 1)/2 clipped to [0, 1] on the
+ * interior.  The context's dt is finit's (1e-4, finit.f90:151); angleB/angleT and alpha_s are
+ * zero there (finit.f90:364-374 sets them after this loop). */
+int orc_finit_wall(const drd_params* P, const double* ph_lcc, const double* bdr_in, int nsteps, double* bdr_out,
+                   double* ph_out, double* rmu_out) {
+    const int nr = P->nr, nz = P->nz;
+    const long cs = cell_size(nr, nz);
+    const long us = u_size(nr, nz), vs = v_size(nr, nz);
+    double* u = dalloc(us);
+    double* v = dalloc(vs);
+    double* ph = dalloc(cs);
+    double* rmu = dalloc(cs);
+    double* pa = dalloc(cs);
+    double* ra = dalloc(cs);
+    memcpy(ph, bdr_in, sizeof(double) * cs); /* :123-133 */
+    for (int j = 0; j < nz; ++j) {
+        ph[CI(-1, j)] = ph[CI(0, j)];
+        ph[CI(nr, j)] = ph[CI(nr - 1, j)];
+    }
+    for (int i = -1; i <= nr; ++i) {
+        ph[CI(i, -1)] = ph[CI(i, 0)];
+        ph[CI(i, nz)] = ph[CI(i, nz - 1)];
+    }
+    ori_rmu(nr, nz, P->dr * P->dr, P->dz * P->dz, P->I_thickness, ph, rmu); /* :163-169 */
+    int info = 0;
+    for (int it = 0; it < nsteps; ++it) { /* :172-176 */
+        drd_status st;
+        info = orc_phsolve_ori(P, ph_lcc, u, v, ph, NULL, NULL, 0.0, ra, pa, &st);
+        memcpy(rmu, ra, sizeof(double) * cs);
+        memcpy(ph, pa, sizeof(double) * cs);
+    }
+    for (long q = 0; q < cs; ++q) bdr_out[q] = (ph[q] + 1.0) / 2.0; /* :178 */
+    for (int j = 0; j < nz; ++j)                                     /* :181-189 */
+        for (int i = 0; i < nr; ++i) {
+            double* b = &bdr_out[CI(i, j)];
+            if (*b >= 1.0) *b = 1.0;
+            else if (*b <= 0.0) *b = 0.0;
+        }
+    if (ph_out) memcpy(ph_out, ph, sizeof(double) * cs);
+    if (rmu_out) memcpy(rmu_out, rmu, sizeof(double) * cs);
+    free(u); free(v); free(ph); free(rmu); free(pa); free(ra);
+    return info;
+}
+
+/* ---------------------------------------------------------------------------------------
  * Coupled CH: two_phase_flow_complex_domain/ph_mu_solve.f90:3-380, ch_bulk_energy.f90:32-67,
  * ch_bdr_condition.f90:3-27.
  * ------------------------------------------------------------------------------------- */
@@ -1032,6 +1241,264 @@ double orc_mass(const drd_params* P, const double* ph) {
 }
 
 /* ---------------------------------------------------------------------------------------
+ * Fiber particles: microfluidics_complex_domain/particles_move.f90 (Np_swm = 0, so the
+ * swimmer and phantom loops of those routines are empty and not restated).
+ * POINTS arrays are Np x 2 column-major: x of bead b at [b], y at [np + b].
+ * ------------------------------------------------------------------------------------- */
+int drd_particle_params_default(drd_particle_params* pp, double lx, double ly) {
+    if (!pp) return DRD_ERR_BADARG;
+    memset(pp, 0, sizeof(*pp));
+    pp->np = 9;                                       /* particles_params.f90:78 */
+    pp->lx = lx;
+    pp->ly = ly;
+    pp->fpd_radius = 0.05 / 2.0;                      /* :80 */
+    pp->l0 = 2 * (pp->fpd_radius + 0.00);             /* :83, fpd_inter_dist = 0 (:81) */
+    pp->ks = 5;                                       /* :74 */
+    pp->kb = 0.0025 * 100;                            /* :75 */
+    pp->theta0 = 0.0;                                 /* :76 */
+    pp->k0_inter = 2.5;                               /* :93 */
+    pp->k0_inter_bdr = 2.5 * 10;                      /* :94 */
+    pp->fpd_fpd_dist = pp->fpd_radius + pp->fpd_radius + 0.01; /* :97 */
+    pp->fpd_bdr_dist = pp->fpd_radius + 0.02;         /* :98 */
+    return DRD_OK;
+}
+
+/* particle_initialize, fibers: particles_move.f90:50-68. */
+int drd_particle_initialize(const drd_particle_params* pp, double xc, double yc, double* points) {
+    if (!pp || !points || pp->np < 0 || pp->np > DRD_PARTICLES_MAX) return DRD_ERR_BADARG;
+    const int np = pp->np;
+    if (np > 2) {
+        const int mid = (int)floor(np / 2.0);
+        points[mid] = xc;
+        points[np + mid] = yc;
+        for (int i = 0; i < mid; ++i) {
+            points[i] = xc;
+            points[np + i] = yc + (mid - i) * pp->l0;
+            points[np - i - 1] = xc;
+            points[np + np - i - 1] = yc - (mid - i) * pp->l0;
+        }
+    }
+    return DRD_OK;
+}
+
+/* MirrorDistance: particles_move.f90:1055-1065. */
+static double mirror_distance(double d, double l) {
+    if (d < -0.5 * l) return d + l;
+    if (d > 0.5 * l) return d - l;
+    return d;
+}
+
+/* fpd_dist_periodic: particles_move.f90:326-357. */
+static double fpd_dist_periodic(double x, double y, double lx, double ly, double rx, double ry, double r) {
+    double xd = 0.0, yd = 0.0;
+    if (rx < r) xd = -lx;
+    else if (lx - rx < r) xd = lx;
+    if (ry < r) yd = -ly;
+    else if (ly - ry < r) yd = ly;
+    double d = sqrt((x - rx) * (x - rx) + (y - ry) * (y - ry)) - r;
+    d = fmin(d, sqrt((x + xd - rx) * (x + xd - rx) + (y - ry) * (y - ry)) - r);
+    d = fmin(d, sqrt((x - rx) * (x - rx) + (y + yd - ry) * (y + yd - ry)) - r);
+    d = fmin(d, sqrt((x + xd - rx) * (x + xd - rx) + (y + yd - ry) * (y + yd - ry)) - r);
+    return d;
+}
+
+/* The smoothed bead indicator (tanh(-dd/sqrt(2)/eps) + 1)/2 of particles_move.f90:786-787. */
+static double bead_indicator(double dd, double eps) { return (tanh(-1.0 * dd / sqrt(2.0) / eps) + 1.0) / 2.0; }
+
+/* interaction_force: particles_move.f90:1010-1053. */
+static void interaction_force(double p1x, double p1y, double p2x, double p2y, double eq, double k, double f[2],
+                              double lx, double ly) {
+    double dx = mirror_distance(p1x - p2x, lx);
+    double dy = mirror_distance(p1y - p2y, ly);
+    const double d = sqrt(dx * dx + dy * dy);
+    if (d < eq) {
+        dx = dx / d;
+        dy = dy / d;
+        f[0] = -(k / (eq * eq) * (d - eq) * dx);
+        f[1] = -(k / (eq * eq) * (d - eq) * dy);
+    } else {
+        f[0] = 0.0;
+        f[1] = 0.0;
+    }
+}
+
+/* Flat CELL index of bdr_dist(i,j) as the Fortran column-major array addresses it, clamped to
+ * the array: interaction_force_bdr reads bdr_dist(i-1,j) with i = -1 for a bead within half a
+ * cell of x = 0, which column-major storage maps to bdr_dist(nr, j-1). */
+static long bdr_flat(int nr, int nz, int i, int j) {
+    long q = (long)(i + 1) + (long)(j + 1) * (nr + 2);
+    const long cs = cell_size(nr, nz);
+    return q < 0 ? 0 : (q >= cs ? cs - 1 : q);
+}
+
+/* interaction_force_bdr: particles_move.f90:1069-1103. */
+static void interaction_force_bdr(int nr, int nz, double dr, double dz, const double* bd, double px, double py,
+                                  double eq, double k, double f[2]) {
+    const int i = (int)floor((px - dr * 0.5) / dr);
+    const int j = (int)floor((py - dz * 0.5) / dz);
+    const double d = bd[bdr_flat(nr, nz, i, j)];
+    double dx = (bd[bdr_flat(nr, nz, i + 1, j)] - bd[bdr_flat(nr, nz, i - 1, j)]) / 2.0 / dr;
+    double dy = (bd[bdr_flat(nr, nz, i, j + 1)] - bd[bdr_flat(nr, nz, i, j - 1)]) / 2.0 / dz;
+    const double di = sqrt(dx * dx + dy * dy);
+    dx = dx / di;
+    dy = dy / di;
+    if (d < eq) {
+        f[0] = -(k / (eq * eq) * (d - eq) * dx);
+        f[1] = -(k / (eq * eq) * (d - eq) * dy);
+    } else {
+        f[0] = 0.0;
+        f[1] = 0.0;
+    }
+}
+
+/* force_caculation, fiber part: particles_move.f90:421-549 and :589-594 (tot_F). */
+void orc_particle_forces(const drd_params* P, const drd_particle_params* pp, const double* pts,
+                         const double* bdr_dist, double* tot_F) {
+    const int np = pp->np;
+    const double lx = pp->lx, ly = pp->ly, l0 = pp->l0, ks = pp->ks, kb = pp->kb;
+    const double PI = 4.0 * atan(1.0); /* particles_params.f90:4 */
+    double rdiff[DRD_PARTICLES_MAX] = {0}, tv[DRD_PARTICLES_MAX][2] = {{0}}, nv[DRD_PARTICLES_MAX][2] = {{0}};
+    double theta[DRD_PARTICLES_MAX] = {0}, G[DRD_PARTICLES_MAX] = {0};
+    for (int i = 0; i < np - 1; ++i) {                                  /* :445-459 */
+        const double dX = mirror_distance(pts[i + 1] - pts[i], lx);
+        const double dY = mirror_distance(pts[np + i + 1] - pts[np + i], ly);
+        rdiff[i] = sqrt(dX * dX + dY * dY);
+        tv[i][0] = dX / rdiff[i];
+        tv[i][1] = dY / rdiff[i];
+        nv[i][0] = -dY / rdiff[i];
+        nv[i][1] = dX / rdiff[i];
+        theta[i] = atan2(tv[i][1], tv[i][0]);
+        if (theta[i] < 0) theta[i] = theta[i] + 2 * PI;
+    }
+    for (int i = 0; i < np - 2; ++i) {                                  /* :471-481 */
+        double a = theta[i + 1] - theta[i];
+        a = mirror_distance(a, 2 * PI);
+        G[i] = a - pp->theta0;
+    }
+    const double kl = ks / (l0 * l0);
+    for (int i = 0; i < np; ++i) {                                      /* :483-516 */
+        double Fs[2], Fb[2];
+        for (int c = 0; c < 2; ++c) {
+            if (i == 0) {
+                Fs[c] = kl * (rdiff[i] - l0) * tv[i][c];
+                Fb[c] = -(kb * G[i] / rdiff[i] * nv[i][c]);
+            } else if (i == 1) {
+                Fs[c] = kl * ((rdiff[i] - l0) * tv[i][c] - (rdiff[i - 1] - l0) * tv[i - 1][c]);
+                Fb[c] = kb * (G[i - 1] / rdiff[i - 1] * nv[i - 1][c] - (G[i] - G[i - 1]) / rdiff[i] * nv[i - 1][c]);
+            } else if (i == np - 1) {
+                Fs[c] = -kl * (rdiff[i - 1] - l0) * tv[i - 1][c];
+                Fb[c] = -(kb * (G[i - 2] / rdiff[i - 1] * nv[i - 1][c]));
+            } else if (i == np - 2) {
+                Fs[c] = kl * ((rdiff[i] - l0) * tv[i][c] - (rdiff[i - 1] - l0) * tv[i - 1][c]);
+                Fb[c] = kb * ((G[i - 1] - G[i - 2]) / rdiff[i - 1] * nv[i - 1][c] + G[i - 1] / rdiff[i] * nv[i - 1][c]);
+            } else {
+                Fs[c] = kl * ((rdiff[i] - l0) * tv[i][c] - (rdiff[i - 1] - l0) * tv[i - 1][c]);
+                Fb[c] = kb * ((G[i - 1] - G[i - 2]) / rdiff[i - 1] * nv[i - 1][c] - (G[i] - G[i - 1]) / rdiff[i] * nv[i][c]);
+            }
+            tot_F[i + (long)np * c] = Fs[c] + Fb[c];                    /* :518 */
+        }
+    }
+    double f[2];
+    for (int i = 0; i < np; ++i)                                        /* :532-539 */
+        for (int j = i + 1; j < np; ++j) {
+            interaction_force(pts[i], pts[np + i], pts[j], pts[np + j], pp->fpd_fpd_dist, pp->k0_inter, f, lx, ly);
+            tot_F[i] = tot_F[i] + f[0];
+            tot_F[np + i] = tot_F[np + i] + f[1];
+            tot_F[j] = tot_F[j] - f[0];
+            tot_F[np + j] = tot_F[np + j] - f[1];
+        }
+    for (int i = 0; i < np; ++i) {                                      /* :574-579 */
+        interaction_force_bdr(P->nr, P->nz, P->dr, P->dz, bdr_dist, pts[i], pts[np + i], pp->fpd_bdr_dist,
+                              pp->k0_inter_bdr, f);
+        tot_F[i] = tot_F[i] + f[0];
+        tot_F[np + i] = tot_F[np + i] + f[1];
+    }
+}
+
+/* force_caculation_vel: particles_move.f90:758-815 (fiber beads; grid r = (i+0.5)dr,
+ * z = (k+0.5)dz as finit.f90:34-35 sets it).  pf1/pf2 are CELL with zero ghosts. */
+void orc_force_caculation_vel(const drd_params* P, const drd_particle_params* pp, const double* pts,
+                              const double* bdr_dist, double* tot_F, double* pf1, double* pf2) {
+    const int nr = P->nr, nz = P->nz, np = pp->np;
+    const long cs = cell_size(nr, nz);
+    orc_particle_forces(P, pp, pts, bdr_dist, tot_F);
+    for (long q = 0; q < cs; ++q) { pf1[q] = 0.0; pf2[q] = 0.0; }
+    double* w = dalloc((long)nr * nz);
+    for (int b = 0; b < np; ++b) {
+        double sum = 0.0;
+        for (int k = 0; k < nz; ++k)
+            for (int i = 0; i < nr; ++i) {
+                const double dd = bead_indicator(
+                    fpd_dist_periodic((i + 0.5) * P->dr, (k + 0.5) * P->dz, pp->lx, pp->ly, pts[b], pts[np + b],
+                                      pp->fpd_radius), P->I_thickness);
+                w[i + (long)nr * k] = dd;
+                sum = sum + dd;
+            }
+        sum = sum * P->dr * P->dz;
+        for (int k = 0; k < nz; ++k)
+            for (int i = 0; i < nr; ++i) {
+                const double dd = w[i + (long)nr * k];
+                pf1[CI(i, k)] = pf1[CI(i, k)] + (tot_F[b] * dd) / sum;
+                pf2[CI(i, k)] = pf2[CI(i, k)] + (tot_F[np + b] * dd) / sum;
+            }
+    }
+    free(w);
+}
+
+/* update_position_vel: particles_move.f90:872-924 (fiber beads). */
+void orc_update_position_vel(const drd_params* P, const drd_particle_params* pp, double* pts, const double* u,
+                             const double* v, double dt) {
+    const int nr = P->nr, nz = P->nz, np = pp->np;
+    for (int b = 0; b < np; ++b) {
+        double ua = 0., va = 0., sum = 0.0;
+        for (int k = 0; k < nz; ++k)
+            for (int i = 0; i < nr; ++i) {
+                const double dd = bead_indicator(
+                    fpd_dist_periodic((i + 0.5) * P->dr, (k + 0.5) * P->dz, pp->lx, pp->ly, pts[b], pts[np + b],
+                                      pp->fpd_radius), P->I_thickness);
+                ua = ua + (u[UI(i, k)] + u[UI(i, k + 1)]) / 2.0 * dd; /* u averaged over k, as :902 */
+                va = va + (v[VI(i, k)] + v[VI(i, k + 1)]) / 2.0 * dd;
+                sum = sum + dd;
+            }
+        ua = ua / sum;
+        va = va / sum;
+        pts[b] = pts[b] + ua * dt;
+        pts[np + b] = pts[np + b] + va * dt;
+        if (pts[b] > pp->lx) pts[b] = pts[b] - pp->lx;
+        else if (pts[b] < 0) pts[b] = pts[b] + pp->lx;
+        if (pts[np + b] > pp->ly) pts[np + b] = pts[np + b] - pp->ly;
+        else if (pts[np + b] < 0) pts[np + b] = pts[np + b] + pp->ly;
+    }
+}
+
+/* dist(r(i,k), z(i,k)) = fpd_dist (dist.f90 -> particles_move.f90:361-391): distance to the
+ * nearest bead surface, not periodic, 1e10 without beads.  DIST shaped. */
+void orc_fpd_dist_field(const drd_params* P, const drd_particle_params* pp, const double* pts, double* dist) {
+    const int nr = P->nr, nz = P->nz, np = pp->np;
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) {
+            const double x = (i + 0.5) * P->dr, y = (k + 0.5) * P->dz;
+            double d = 1.0E10;
+            for (int b = 0; b < np; ++b)
+                d = fmin(d, sqrt((x - pts[b]) * (x - pts[b]) + (y - pts[np + b]) * (y - pts[np + b])) - pp->fpd_radius);
+            dist[i + (long)nr * k] = d;
+        }
+}
+
+/* The particle block of the mcl6 loop (mcl6.f90:394-402): forces and spreading with the beads
+ * where they are, then the move with the current u, v, then interpolate_coef at the new
+ * positions. */
+void orc_particles_step(const drd_params* P, orc_particles* X, const double* u, const double* v,
+                        const double* bdr_ph, double* pf1, double* pf2) {
+    orc_force_caculation_vel(P, &X->pp, X->points, X->bdr_dist, X->tot_F, pf1, pf2);
+    orc_update_position_vel(P, &X->pp, X->points, u, v, P->dt);
+    double* dist = dalloc((long)P->nr * P->nz);
+    orc_fpd_dist_field(P, &X->pp, X->points, dist);
+    orc_interpolate_coef(P, dist, bdr_ph, X->fpd_ph, X->rho, X->eta);
+    free(dist);
+}
+
+/* ---------------------------------------------------------------------------------------
  * The mcl6 step: microfluidics_complex_domain/mcl6.f90:239-306 (first) and :378-486 (loop).
  * ------------------------------------------------------------------------------------- */
 int orc_step(const drd_params* P, const double* ph_lcc, const double* pre_lcc, orc_state* S,
@@ -1055,12 +1522,28 @@ int orc_step(const drd_params* P, const double* ph_lcc, const double* pre_lcc, o
                              S->bdr_ph_grad, S->Mi, ang, ang, S->M0, ph_after, rmu_after, NULL, &st[0]);
         free(ang);
     } else {
-        rc = orc_phsolve(P, ph_lcc, f[DRD_F_U], f[DRD_F_V], f[DRD_F_PH], f[DRD_F_RMU], S->bdr_ph, S->bdr_ph_grad,
+        /* guess_mode 1: the Krylov guess is 2 rmu - rmu_pre (the rhs only reads rmu through it) */
+        double* guess = f[DRD_F_RMU];
+        double* ext = NULL;
+        if (!first && P->guess_mode == 1) {
+            ext = dalloc(cs);
+            for (long q = 0; q < cs; ++q) ext[q] = 2.0 * f[DRD_F_RMU][q] - f[DRD_F_RMU_PRE][q];
+            guess = ext;
+        }
+        rc = orc_phsolve(P, ph_lcc, f[DRD_F_U], f[DRD_F_V], f[DRD_F_PH], guess, S->bdr_ph, S->bdr_ph_grad,
                          S->M0, S->Mi, rmu_after, ph_after, &st[0]);
+        free(ext);
     }
     (void)rc;
+    const double* rho = S->rho;
+    const double* eta = S->eta;
+    if (S->parts && S->parts->pp.np > 0) { /* mcl6.f90:394-402 */
+        orc_particles_step(P, S->parts, f[DRD_F_U], f[DRD_F_V], S->bdr_ph, f[DRD_F_PF1], f[DRD_F_PF2]);
+        rho = S->parts->rho;
+        eta = S->parts->eta;
+    }
     orc_velosolve(P, first ? 1 : 2, f[DRD_F_PSI1], f[DRD_F_PSI2], f[DRD_F_U_PRE], f[DRD_F_U], f[DRD_F_V_PRE],
-                  f[DRD_F_V], f[DRD_F_P], S->rho, S->eta, S->bdr_ph, S->bdr_pen, S->bdr_used, ph_after,
+                  f[DRD_F_V], f[DRD_F_P], rho, eta, S->bdr_ph, S->bdr_pen, S->bdr_used, ph_after,
                   rmu_after, t + P->dt, f[DRD_F_PF1], f[DRD_F_PF2], u_after, v_after, NULL, NULL, &st[1]);
     memcpy(f[DRD_F_U_PRE], f[DRD_F_U], sizeof(double) * us);
     memcpy(f[DRD_F_V_PRE], f[DRD_F_V], sizeof(double) * vs);

@@ -95,6 +95,43 @@ void orc_interpolate_coef(const drd_params* P, const double* dist, const double*
 
 double orc_mass(const drd_params* P, const double* ph);
 
+/* PhSolve_ori and finit's wall smoothing (microfluidics_complex_domain/PhSolve_ori.f90,
+ * finit.f90:120-189).  angleB/angleT may be NULL (zeros, as during finit's loop). */
+double orc_ori_coef(const drd_params* P, double alpha_s);
+void orc_ori_matvec(const drd_params* P, double coef_bot, double coef_top, double alpha, const double* x,
+                    double beta, double* y);
+void orc_ori_system(const drd_params* P, const double* u, const double* v, const double* ph, const double* angleB,
+                    const double* angleT, double alpha_s, double* f2, double* rhs, double* x0, double* pnb,
+                    double* pnt);
+int orc_phsolve_ori(const drd_params* P, const double* ph_lcc, const double* u, const double* v, const double* ph,
+                    const double* angleB, const double* angleT, double alpha_s, double* rmu_after, double* ph_after,
+                    drd_status* st);
+int orc_finit_wall(const drd_params* P, const double* ph_lcc, const double* bdr_in, int nsteps, double* bdr_out,
+                   double* ph_out, double* rmu_out);
+
+/* Fiber particles (microfluidics_complex_domain/particles_move.f90; POINTS arrays as in
+ * include/drd_gb300.h).  drd_particle_params_default and drd_particle_initialize are also
+ * defined here with the library's signatures, so the oracle can set up a chain by itself. */
+void orc_particle_forces(const drd_params* P, const drd_particle_params* pp, const double* points,
+                         const double* bdr_dist, double* tot_F);                      /* :421-627 */
+void orc_force_caculation_vel(const drd_params* P, const drd_particle_params* pp, const double* points,
+                              const double* bdr_dist, double* tot_F, double* pf1, double* pf2); /* :758-868 */
+void orc_update_position_vel(const drd_params* P, const drd_particle_params* pp, double* points,
+                             const double* u, const double* v, double dt);            /* :872-980 */
+void orc_fpd_dist_field(const drd_params* P, const drd_particle_params* pp, const double* points,
+                        double* dist);                                                /* :361-391 */
+typedef struct orc_particles {
+    drd_particle_params pp;
+    double* points;          /* POINTS, moved by each step */
+    double* tot_F;           /* POINTS, written */
+    const double* bdr_dist;  /* CELL */
+    double* fpd_ph;          /* CELL, written */
+    double* rho;             /* CELL, written; the step's momentum solve uses these */
+    double* eta;             /* CELL, written */
+} orc_particles;
+void orc_particles_step(const drd_params* P, orc_particles* X, const double* u, const double* v,
+                        const double* bdr_ph, double* pf1, double* pf2);
+
 /* The mcl6 loop body on a state held by the caller (same field order as DRD_F_*); coefficient
  * arrays as in orc_velosolve.  Returns the CH status in st[0], momentum in st[1]. */
 typedef struct orc_state {
@@ -107,6 +144,7 @@ typedef struct orc_state {
     const double* Mi;
     const double* bdr_pen;
     const double* bdr_used;
+    orc_particles* parts;   /* NULL: particles held fixed; else the coupling of mcl6.f90:394-402 */
 } orc_state;
 int orc_step(const drd_params* P, const double* ph_lcc, const double* pre_lcc, orc_state* S,
              int first, double t, drd_status* st2);

@@ -67,14 +67,35 @@ def lib(openmp=False):
         L.orc_interpolate_coef.argtypes = [P, dp, dp, dp, dp, dp]
         L.orc_mass.argtypes = [P, dp]
         L.orc_mass.restype = C.c_double
+        L.orc_ori_coef.argtypes = [P, C.c_double]
+        L.orc_ori_coef.restype = C.c_double
+        L.orc_ori_matvec.argtypes = [P, C.c_double, C.c_double, C.c_double, dp, C.c_double, dp]
+        L.orc_ori_system.argtypes = [P, dp, dp, dp, dp, dp, C.c_double, dp, dp, dp, dp, dp]
+        L.orc_phsolve_ori.argtypes = [P, dp, dp, dp, dp, dp, dp, C.c_double, dp, dp, S]
+        L.orc_phsolve_ori.restype = C.c_int
+        L.orc_finit_wall.argtypes = [P, dp, dp, C.c_int, dp, dp, dp]
+        L.orc_finit_wall.restype = C.c_int
+        PP = C.POINTER(abi.drd_particle_params)
+        L.orc_particle_forces.argtypes = [P, PP, dp, dp, dp]
+        L.orc_force_caculation_vel.argtypes = [P, PP, dp, dp, dp, dp, dp]
+        L.orc_update_position_vel.argtypes = [P, PP, dp, dp, dp, C.c_double]
+        L.orc_fpd_dist_field.argtypes = [P, PP, dp, dp]
+        L.drd_particle_params_default.argtypes = [PP, C.c_double, C.c_double]
+        L.drd_particle_initialize.argtypes = [PP, C.c_double, C.c_double, dp]
         _libs[path] = L
     return _libs[path]
+
+
+class OrcParticles(C.Structure):
+    _fields_ = [("pp", abi.drd_particle_params)] + [
+        (n, C.POINTER(C.c_double)) for n in ("points", "tot_F", "bdr_dist", "fpd_ph", "rho", "eta")
+    ]
 
 
 class OrcState(C.Structure):
     _fields_ = [("f", C.POINTER(C.c_double) * abi.F_COUNT)] + [
         (n, C.POINTER(C.c_double)) for n in ("rho", "eta", "bdr_ph", "bdr_ph_grad", "M0", "Mi", "bdr_pen", "bdr_used")
-    ]
+    ] + [("parts", C.POINTER(OrcParticles))]
 
 
 class Oracle:
@@ -235,13 +256,82 @@ class Oracle:
     def mass(self, ph):
         return self.L.orc_mass(C.byref(self.P), ptr(ph))
 
-    def step(self, state, coefs, first, t):
-        """state: dict field-id -> array (updated in place); coefs: dict of coefficient arrays."""
+    # -- PhSolve_ori and finit's wall smoothing (PhSolve_ori.f90, finit.f90:120-189) ---------
+    def ori_coef(self, alpha_s=0.0):
+        return self.L.orc_ori_coef(C.byref(self.P), alpha_s)
+
+    def ori_matvec(self, x, alpha_s=0.0, alpha=1.0, beta=0.0, y=None):
+        y = np.zeros_like(x) if y is None else y.copy()
+        cb = self.ori_coef(alpha_s)
+        self.L.orc_ori_matvec(C.byref(self.P), cb, cb, alpha, ptr(x), beta, ptr(y))
+        return y
+
+    def ori_system(self, u, v, ph, angleB=None, angleT=None, alpha_s=0.0):
+        nr, nz = self.P.nr, self.P.nz
+        f2 = np.zeros_like(ph)
+        rhs, x0, pnb, pnt = np.zeros(nr * nz), np.zeros(nr * nz), np.zeros(nr), np.zeros(nr)
+        self.L.orc_ori_system(C.byref(self.P), ptr(u), ptr(v), ptr(ph), ptr(angleB), ptr(angleT), alpha_s,
+                              ptr(f2), ptr(rhs), ptr(x0), ptr(pnb), ptr(pnt))
+        return rhs, x0, pnb, pnt
+
+    def phsolve_ori(self, u, v, ph, angleB=None, angleT=None, alpha_s=0.0):
+        rmu_after, ph_after = np.zeros_like(ph), np.zeros_like(ph)
+        st = abi.drd_status()
+        self.L.orc_phsolve_ori(C.byref(self.P), ptr(self.ph_lcc), ptr(u), ptr(v), ptr(ph), ptr(angleB), ptr(angleT),
+                               alpha_s, ptr(rmu_after), ptr(ph_after), C.byref(st))
+        return rmu_after, ph_after, st
+
+    def finit_wall(self, bdr_ph, nsteps=51):
+        out = [np.zeros_like(bdr_ph) for _ in range(3)]
+        info = self.L.orc_finit_wall(C.byref(self.P), ptr(self.ph_lcc), ptr(bdr_ph), nsteps, *[ptr(a) for a in out])
+        return out[0], out[1], out[2], info
+
+    # -- fiber particles (particles_move.f90) -----------------------------------------------
+    def particle_forces(self, pp, points, bdr_dist):
+        tot_f = np.zeros_like(points)
+        self.L.orc_particle_forces(C.byref(self.P), C.byref(pp), ptr(points), ptr(bdr_dist), ptr(tot_f))
+        return tot_f
+
+    def force_caculation_vel(self, pp, points, bdr_dist):
+        tot_f = np.zeros_like(points)
+        pf1 = np.zeros_like(bdr_dist)
+        pf2 = np.zeros_like(bdr_dist)
+        self.L.orc_force_caculation_vel(C.byref(self.P), C.byref(pp), ptr(points), ptr(bdr_dist), ptr(tot_f),
+                                        ptr(pf1), ptr(pf2))
+        return tot_f, pf1, pf2
+
+    def update_position_vel(self, pp, points, u, v, dt):
+        out = np.array(points, dtype=np.float64, copy=True)
+        self.L.orc_update_position_vel(C.byref(self.P), C.byref(pp), ptr(out), ptr(u), ptr(v), dt)
+        return out
+
+    def fpd_dist_field(self, pp, points):
+        dist = np.zeros((self.P.nz, self.P.nr))
+        self.L.orc_fpd_dist_field(C.byref(self.P), C.byref(pp), ptr(points), ptr(dist))
+        return dist
+
+    def step(self, state, coefs, first, t, particles=None):
+        """state: dict field-id -> array (updated in place); coefs: dict of coefficient arrays.
+        particles: None (held fixed) or a dict with "pp", "points" (POINTS array, moved in place)
+        and "bdr_dist"; the step then writes "tot_F", "fpd", "rho" and "eta" into it."""
         S = OrcState()
         for fid in range(abi.F_COUNT):
             S.f[fid] = ptr(state[fid])
         for name in ("rho", "eta", "bdr_ph", "bdr_ph_grad", "M0", "Mi", "bdr_pen", "bdr_used"):
             setattr(S, name, ptr(coefs[name]))
+        X = None
+        if particles is not None:
+            shape = coefs["rho"].shape
+            for key in ("fpd", "rho", "eta"):
+                particles.setdefault(key, np.zeros(shape))
+            particles.setdefault("tot_F", np.zeros_like(particles["points"]))
+            X = OrcParticles()
+            X.pp = particles["pp"]
+            X.points = ptr(particles["points"])
+            X.tot_F = ptr(particles["tot_F"])
+            X.bdr_dist = ptr(particles["bdr_dist"])
+            X.fpd_ph, X.rho, X.eta = ptr(particles["fpd"]), ptr(particles["rho"]), ptr(particles["eta"])
+            S.parts = C.pointer(X)
         st = (abi.drd_status * 2)()
         self.L.orc_step(C.byref(self.P), ptr(self.ph_lcc), ptr(self.pre_lcc), C.byref(S), int(first), t, st)
         return st[0], st[1]

@@ -52,7 +52,9 @@ def _c_layout(struct, fields):
 
 
 @pytest.mark.parametrize("cls,name", [(abi.drd_params, "drd_params"), (abi.drd_status, "drd_status"),
-                                      (abi.drd_step_stats, "drd_step_stats")])
+                                      (abi.drd_step_stats, "drd_step_stats"),
+                                      (abi.drd_particle_params, "drd_particle_params"),
+                                      (abi.drd_deck, "drd_deck")])
 def test_struct_layout_matches_header(cls, name):
     fields = [f for f, _ in cls._fields_]
     got = _c_layout(name, fields)
@@ -69,3 +71,11 @@ def test_bad_arguments_are_rejected_without_a_gpu():
     p = abi.default_params(16, 8, xlsB=0.1)  # slip walls have no solve in the reference
     assert lib.drd_create(C.byref(p), C.byref(h)) == abi.DRD_ERR_UNSUPPORTED
     assert lib.drd_destroy(None) == abi.DRD_ERR_BADARG
+    # the host-only particle helpers need no GPU and match the Python defaults bit for bit
+    pp = abi.drd_particle_params()
+    assert lib.drd_particle_params_default(C.byref(pp), 3.5, 1.5) == 0
+    assert bytes(pp) == bytes(abi.default_particle_params(3.5, 1.5))
+    pts = (C.c_double * 18)()
+    assert lib.drd_particle_initialize(C.byref(pp), 1.75, 0.42, pts) == 0
+    assert list(pts) == [x for row in abi.particle_chain(pp, 1.75, 0.42) for x in row]
+    assert lib.drd_particles_set(None, C.byref(pp), pts, pts) == abi.DRD_ERR_BADARG

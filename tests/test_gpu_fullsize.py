@@ -1,0 +1,89 @@
+"""Full-size (420x180) and odd-size checks of the transform kernels and the solves.
+
+Every tile configuration of the transform GEMMs (the autotuner may pick any of them for a
+given grid) is forced in turn and checked against the oracle's DCT-I preconditioner; the CH
+solve at 420x180 must meet the deck tolerance in both arithmetic modes.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from drd_application_gb300 import abi
+from drd_application_gb300.api import DRDContext
+from drd_application_gb300.workloads import make_case
+from oracle.oracle import Oracle
+from tests.helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+F = abi
+
+
+def _n_cfg(cuda_lib):
+    return 9
+
+
+@pytest.mark.parametrize("nr,nz", [(420, 180), (97, 53)])
+def test_every_gemm_config_matches_oracle(cuda_lib, oracle_build, nr, nz):
+    case = make_case("c2", seed=1, nr=nr, nz=nz)
+    orc = Oracle(case.params)
+    x = np.random.default_rng(nr).standard_normal(nr * nz)
+    ref = orc.ch_psolve(x)
+    bad = []
+    for cfg in range(_n_cfg(cuda_lib)):
+        os.environ["DRD_GEMM_CFG"] = str(cfg)
+        try:
+            ctx = DRDContext(case.params)
+            ctx.set_case(case)
+            e64 = rel_err(ctx.op_apply(F.DRD_OP_CH_PSOLVE, x), ref)
+            e32 = rel_err(ctx.op_apply(F.DRD_OP_CH_PSOLVE, x, precision=F.DRD_PREC_MIXED), ref)
+            ctx.close()
+        finally:
+            del os.environ["DRD_GEMM_CFG"]
+        if not (e64 < 1e-12 and e32 < 5e-5):
+            bad.append((cfg, e64, e32))
+    assert not bad, bad
+
+
+@pytest.mark.parametrize("precision", [abi.DRD_PREC_FP64, abi.DRD_PREC_MIXED])
+def test_fullsize_first_step_solves_meet_tolerance(cuda_lib, oracle_build, precision):
+    case = make_case("c2", seed=0, precision=precision)
+    P = case.params
+    ctx = DRDContext(P)
+    ctx.set_case(case)
+    st = case.state
+    inputs = (st[F.F_U], st[F.F_V], st[F.F_PH], st[F.F_RMU])
+    r, p, s = ctx.PhSolve(*inputs, P.dt)
+    assert s.info == 0, s.as_dict()
+    assert s.true_resid <= P.tol
+    orc = Oracle(P)
+    assert orc.ch_residual(inputs, case.coefs, r) <= 1.01 * P.tol
+    u, v, _, _, s2 = ctx.VeloSolve_combined(None, st[F.F_U], st[F.F_V], st[F.F_P], r, p, P.dt)
+    assert s2.info == 0 and s2.true_resid <= P.tol, s2.as_dict()
+    ctx.close()
+
+
+def test_direct_launch_mode_matches_graph_mode(cuda_lib):
+    """DRD_DIRECT_LAUNCH=1 (per-kernel launches, host-run loops; used for profiling) computes
+    exactly what the captured graphs compute: the reductions are in a fixed order."""
+    case = make_case("c2", seed=4, nr=64, nz=32, precision=abi.DRD_PREC_MIXED)
+    out = []
+    for direct in (False, True):
+        if direct:
+            os.environ["DRD_DIRECT_LAUNCH"] = "1"
+        try:
+            ctx = DRDContext(case.params)
+            ctx.set_case(case)
+            ctx.upload_state(case.state)
+            t = 0.0
+            for s in range(3):
+                st = ctx.step(s == 0, t)
+                t += case.params.dt
+            out.append((ctx.download_state([F.F_U, F.F_PH, F.F_P]), st.ch.iter, st.uv.iter))
+            ctx.close()
+        finally:
+            os.environ.pop("DRD_DIRECT_LAUNCH", None)
+    (a, ia, ja), (b, ib, jb) = out
+    assert (ia, ja) == (ib, jb)
+    for fid in a:
+        assert np.array_equal(a[fid], b[fid]), fid

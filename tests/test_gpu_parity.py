@@ -255,14 +255,17 @@ def test_mixed_velosolve_reaches_fp64_tolerance(mf_case):
 
 
 # ------------------------------------------------------------------------------- step sequence
-@pytest.mark.parametrize("precision", [abi.DRD_PREC_FP64, abi.DRD_PREC_MIXED])
-def test_step_sequence_matches_oracle(cuda_lib, oracle_build, precision):
+@pytest.mark.parametrize("precision,guess", [(abi.DRD_PREC_FP64, 0), (abi.DRD_PREC_MIXED, 0), (abi.DRD_PREC_MIXED, 1)])
+def test_step_sequence_matches_oracle(cuda_lib, oracle_build, precision, guess):
+    """Four mcl6 steps on the resident state against the oracle at tol 1e-12, where the result
+    no longer depends on the Krylov guess (guess_mode 1 extrapolates it)."""
     from drd_application_gb300.workloads import make_case
 
     case = make_case("c2", seed=7, nr=48, nz=24)
     P = case.params.copy()
     P.tol = 1e-12
     P.precision = precision
+    P.guess_mode = guess
     ctx = DRDContext(P)
     ctx.set_case(case)
     ctx.upload_state(case.state)
