@@ -63,6 +63,8 @@ SIGNATURES = {
     "drd_kernel_bench": (C.c_int, [_ctx, C.c_int, C.c_int, _dp, _dp, _dp]),
     "drd_flush_l2": (C.c_int, [_ctx, C.c_int64]),
     "drd_kernel_launches": (C.c_int64, [_ctx]),
+    "drd_persistent_solver": (C.c_int, [_ctx, C.c_char_p, C.c_int]),
+    "drd_persist_profile": (C.c_int, [_ctx, C.POINTER(C.c_int64), C.c_int]),
     "drd_stream": (C.c_void_p, [_ctx]),
 }
 

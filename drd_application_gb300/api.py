@@ -283,6 +283,12 @@ class DRDContext:
     def flush_l2(self, nbytes=512 << 20):
         self._rc(self.L.drd_flush_l2(self.h, int(nbytes)), "drd_flush_l2", False)
 
+    def persistent_solver(self):
+        """(in use, why not) of the persistent cooperative FP32 inner solver."""
+        why = C.create_string_buffer(512)
+        on = self.L.drd_persistent_solver(self.h, why, len(why))
+        return bool(on == 1), why.value.decode()
+
     def kernel_launches(self):
         return int(self.L.drd_kernel_launches(self.h))
 

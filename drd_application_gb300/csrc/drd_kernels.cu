@@ -645,25 +645,85 @@ __global__ void k_uv_rhs(DevParams P, int bdf, const CallArgs* __restrict__ ca, 
 
 // Values of the unknown fields at any index the operator reads, with the ghost values
 // MatrixVector_uv_2_CG assigns (:533-553; TP lr_bd_type 'n': copies instead of reflections).
-template <typename T>
+template <typename T, bool CG = false>
 struct UVFetch {
     const T* x; int nr, nz; long mn; int neumann;
+    __device__ __forceinline__ T ld(long q) const {
+        if constexpr (CG) return __ldcg(x + q);
+        return x[q];
+    }
     __device__ __forceinline__ T U(int i, int k) const {
         if (k < 0) return -Uc(i, 0);
         if (k > nz - 1) return -Uc(i, nz - 1);
         return Uc(i, k);
     }
     __device__ __forceinline__ T Uc(int i, int k) const {  // k in [0, nz-1]
-        if (i < 0) return neumann ? x[1 + (long)(nr + 1) * k] : -x[1 + (long)(nr + 1) * k];
-        if (i > nr) return neumann ? x[(nr - 1) + (long)(nr + 1) * k] : -x[(nr - 1) + (long)(nr + 1) * k];
-        return x[i + (long)(nr + 1) * k];
+        if (i < 0) return neumann ? ld(1 + (long)(nr + 1) * k) : -ld(1 + (long)(nr + 1) * k);
+        if (i > nr) return neumann ? ld((nr - 1) + (long)(nr + 1) * k) : -ld((nr - 1) + (long)(nr + 1) * k);
+        return ld(i + (long)(nr + 1) * k);
     }
     __device__ __forceinline__ T V(int i, int k) const {
         if (k <= 0 || k >= nz) return T(0);
         const int ii = i < 0 ? 0 : (i > nr - 1 ? nr - 1 : i);
-        return x[mn + ii + (long)nr * (k - 1)];
+        return ld(mn + ii + (long)nr * (k - 1));
     }
 };
+
+// Row q of MatrixVector_uv_2_CG (:515-646) / MatrixVector_uv_CG: (A x)_q.
+template <typename T, class FX>
+__device__ __forceinline__ T uv_apply(const OpScal<T>& o, const T* __restrict__ rho, const T* __restrict__ eta,
+                                      const T* __restrict__ pen, const FX& F, long q) {
+    const int nr = o.nr;
+    const long mn = F.mn;
+    const T h = T(0.5), q4 = T(0.25);
+    const T mcoef = (o.bdf == 2) ? T(1.5) * o.re : o.re;
+    T val;
+#define E_(i, k) eta[cidx(nr, i, k)]
+    if (q < mn) {
+        const int i = (int)(q % (nr + 1)), k = (int)(q / (nr + 1));
+        const T f1 = F.ld(q);
+        if (o.bdf == 2)
+            val = f1 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i - 1, k)]) * h +
+                  f1 * o.pk * (pen[cidx(nr, i, k)] + pen[cidx(nr, i - 1, k)]) * h * o.dt;
+        else
+            val = f1 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i - 1, k)]) * h;
+        T cr = E_(i, k), cl = E_(i - 1, k);
+        if constexpr (sizeof(T) == 4)
+            val = val - T(2) * o.dt * (cr * (F.Uc(i + 1, k) - f1) + cl * (F.Uc(i - 1, k) - f1)) / o.dr2;
+        else
+            val = val - T(2) * o.dt * (cr * F.Uc(i + 1, k) + cl * F.Uc(i - 1, k) - (cl + cr) * f1) / o.dr2;
+        cr = (E_(i, k + 1) + E_(i - 1, k + 1) + E_(i, k) + E_(i - 1, k)) * q4;
+        cl = (E_(i, k) + E_(i - 1, k) + E_(i, k - 1) + E_(i - 1, k - 1)) * q4;
+        if constexpr (sizeof(T) == 4)
+            val = val - o.dt * (cr * (F.U(i, k + 1) - f1) + cl * (F.U(i, k - 1) - f1)) / o.dz2;
+        else
+            val = val - o.dt * (cr * F.U(i, k + 1) + cl * F.U(i, k - 1) - (cl + cr) * f1) / o.dz2;
+        val = val - o.dt * (cr * (F.V(i, k + 1) - F.V(i - 1, k + 1)) - cl * (F.V(i, k) - F.V(i - 1, k))) / o.dr / o.dz;
+    } else {
+        const long qv = q - mn;
+        const int i = (int)(qv % nr), k = (int)(qv / nr) + 1;
+        const T f2 = F.ld(q);
+        if (o.bdf == 2)
+            val = f2 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i, k - 1)]) * h +
+                  f2 * o.pk * (pen[cidx(nr, i, k)] + pen[cidx(nr, i, k - 1)]) * h * o.dt;
+        else
+            val = f2 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i, k - 1)]) * h;
+        T cr = E_(i, k), cl = E_(i, k - 1);
+        if constexpr (sizeof(T) == 4)
+            val = val - T(2) * o.dt * (cr * (F.V(i, k + 1) - f2) + cl * (F.V(i, k - 1) - f2)) / o.dz2;
+        else
+            val = val - T(2) * o.dt * (cr * F.V(i, k + 1) + cl * F.V(i, k - 1) - (cl + cr) * f2) / o.dz2;
+        cr = (E_(i + 1, k) + E_(i, k) + E_(i + 1, k - 1) + E_(i, k - 1)) * q4;
+        cl = (E_(i, k) + E_(i - 1, k) + E_(i, k - 1) + E_(i - 1, k - 1)) * q4;
+        if constexpr (sizeof(T) == 4)
+            val = val - o.dt * (cr * (F.V(i + 1, k) - f2) + cl * (F.V(i - 1, k) - f2)) / o.dr2;
+        else
+            val = val - o.dt * (cr * F.V(i + 1, k) + cl * F.V(i - 1, k) - (cl + cr) * f2) / o.dr2;
+        val = val - o.dt * (cr * (F.Uc(i + 1, k) - F.Uc(i + 1, k - 1)) - cl * (F.Uc(i, k) - F.Uc(i, k - 1))) / o.dr / o.dz;
+    }
+#undef E_
+    return val;
+}
 
 // MatrixVector_uv_2_CG (:515-646) / MatrixVector_uv_CG: y = alpha A x + beta y.
 template <typename T>
@@ -675,60 +735,14 @@ __global__ void k_uv_mv(OpScal<T> o, const T* __restrict__ rho, const T* __restr
     const int nr = o.nr, nz = o.nz;
     const long mn = (long)(nr + 1) * nz, N = mn + (long)nr * (nz - 1);
     UVFetch<T> F{x, nr, nz, mn, o.lr_neumann};
-    const T h = T(0.5), q4 = T(0.25);
-    const T mcoef = (o.bdf == 2) ? T(1.5) * o.re : o.re;
     double a1 = 0.0, a2 = 0.0;
-#define E_(i, k) eta[cidx(nr, i, k)]
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < N; q += (long)gridDim.x * blockDim.x) {
-        T val;
-        if (q < mn) {
-            const int i = (int)(q % (nr + 1)), k = (int)(q / (nr + 1));
-            const T f1 = x[q];
-            if (o.bdf == 2)
-                val = f1 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i - 1, k)]) * h +
-                      f1 * o.pk * (pen[cidx(nr, i, k)] + pen[cidx(nr, i - 1, k)]) * h * o.dt;
-            else
-                val = f1 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i - 1, k)]) * h;
-            T cr = E_(i, k), cl = E_(i - 1, k);
-            if constexpr (sizeof(T) == 4)
-                val = val - T(2) * o.dt * (cr * (F.Uc(i + 1, k) - f1) + cl * (F.Uc(i - 1, k) - f1)) / o.dr2;
-            else
-                val = val - T(2) * o.dt * (cr * F.Uc(i + 1, k) + cl * F.Uc(i - 1, k) - (cl + cr) * f1) / o.dr2;
-            cr = (E_(i, k + 1) + E_(i - 1, k + 1) + E_(i, k) + E_(i - 1, k)) * q4;
-            cl = (E_(i, k) + E_(i - 1, k) + E_(i, k - 1) + E_(i - 1, k - 1)) * q4;
-            if constexpr (sizeof(T) == 4)
-                val = val - o.dt * (cr * (F.U(i, k + 1) - f1) + cl * (F.U(i, k - 1) - f1)) / o.dz2;
-            else
-                val = val - o.dt * (cr * F.U(i, k + 1) + cl * F.U(i, k - 1) - (cl + cr) * f1) / o.dz2;
-            val = val - o.dt * (cr * (F.V(i, k + 1) - F.V(i - 1, k + 1)) - cl * (F.V(i, k) - F.V(i - 1, k))) / o.dr / o.dz;
-        } else {
-            const long qv = q - mn;
-            const int i = (int)(qv % nr), k = (int)(qv / nr) + 1;
-            const T f2 = x[q];
-            if (o.bdf == 2)
-                val = f2 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i, k - 1)]) * h +
-                      f2 * o.pk * (pen[cidx(nr, i, k)] + pen[cidx(nr, i, k - 1)]) * h * o.dt;
-            else
-                val = f2 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i, k - 1)]) * h;
-            T cr = E_(i, k), cl = E_(i, k - 1);
-            if constexpr (sizeof(T) == 4)
-                val = val - T(2) * o.dt * (cr * (F.V(i, k + 1) - f2) + cl * (F.V(i, k - 1) - f2)) / o.dz2;
-            else
-                val = val - T(2) * o.dt * (cr * F.V(i, k + 1) + cl * F.V(i, k - 1) - (cl + cr) * f2) / o.dz2;
-            cr = (E_(i + 1, k) + E_(i, k) + E_(i + 1, k - 1) + E_(i, k - 1)) * q4;
-            cl = (E_(i, k) + E_(i - 1, k) + E_(i, k - 1) + E_(i - 1, k - 1)) * q4;
-            if constexpr (sizeof(T) == 4)
-                val = val - o.dt * (cr * (F.V(i + 1, k) - f2) + cl * (F.V(i - 1, k) - f2)) / o.dr2;
-            else
-                val = val - o.dt * (cr * F.V(i + 1, k) + cl * F.V(i - 1, k) - (cl + cr) * f2) / o.dr2;
-            val = val - o.dt * (cr * (F.Uc(i + 1, k) - F.Uc(i + 1, k - 1)) - cl * (F.Uc(i, k) - F.Uc(i, k - 1))) / o.dr / o.dz;
-        }
+        const T val = uv_apply<T>(o, rho, eta, pen, F, q);
         const T yn = (beta == T(0)) ? alpha * val : alpha * val + beta * y[q];
         y[q] = yn;
         if (dot1) a1 += (double)dot1[q] * (double)yn;
         if (self2) a2 += (double)yn * (double)yn;
     }
-#undef E_
     if (dot1 != nullptr || self2) emit_partials<DRD_TPB>(a1, a2, dot1 != nullptr, self2, d, slot1);
 }
 
@@ -1649,7 +1663,8 @@ __global__ void k_mx_check(KState* o, const KState* in, Dots d, cudaGraphConditi
             o->outer += 1;
             o->inner_total += in->iter;
             o->iter = o->inner_total;
-            if (!isfinite(o->resid)) { o->info = DRD_ERR_NONFINITE; o->phase = PH_DONE; }
+            if (in->info == DRD_ERR_TIMEOUT) { o->info = DRD_ERR_TIMEOUT; o->phase = PH_DONE; }
+            else if (!isfinite(o->resid)) { o->info = DRD_ERR_NONFINITE; o->phase = PH_DONE; }
             else if (o->resid <= o->tol) { o->info = 0; o->phase = PH_DONE; }
             else if (o->outer >= o->maxit) { o->info = 1; o->phase = PH_DONE; }
             else if (o->resid > 0.9 * prev) { o->info = 1; o->phase = PH_DONE; }  // stalled refinement
@@ -1659,9 +1674,515 @@ __global__ void k_mx_check(KState* o, const KState* in, Dots d, cudaGraphConditi
 }
 
 // ======================================================================================
+// Persistent cooperative BiCGSTAB for the FP32 inner solves of the mixed mode (CH and
+// momentum systems).
+//
+// One cooperative launch (all blocks co-resident) runs the whole inner solve: setup and every
+// iteration of lib/BiCGSTABREVCOM.f:229-388, with the same steps, tests and INFO codes as the
+// k_bi_* kernels above, but with the phases of an iteration separated by grid-wide barriers
+// instead of kernel boundaries.  Every block reduces the dot-product partials itself in a fixed
+// order, so all blocks take the same decisions.  Data written in one phase by other blocks is
+// read through L2 (ld.global.cg).  Each barrier's wait is bounded: a wait that runs out sets an
+// error flag, the blocks leave the solve, and the state records DRD_ERR_TIMEOUT.
+// ======================================================================================
+namespace {
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Optional phase timing: thread 0 of block 0 records %globaltimer at entry and exit of each
+// barrier while `p` is set (one iteration of a solve), into p[2k], p[2k+1].
+struct PbProf {
+    unsigned long long* p;
+    int k;
+};
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid barrier on one arrival counter, reset to zero before the launch: barrier k completes when
+// the counter reaches k * gridDim.x.  Thread 0 publishes the block's writes with a release add
+// (ordered after the block's writes by the preceding __syncthreads) and waits with acquire
+// loads; `target` is its running count.
+__device__ __noinline__ bool grid_sync(GridBar* gb, unsigned& target, PbProf& pf) {
+    __shared__ int s_ok;
+    __syncthreads();
+    const bool rec = pf.p != nullptr && blockIdx.x == 0 && threadIdx.x == 0 && pf.k < 62;
+    if (rec) pf.p[2 * pf.k] = gtimer();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        target += gridDim.x;
+        red_release_add(&gb->count, 1u);
+        unsigned spins = 0;
+        while ((int)(ld_acquire_u32(&gb->count) - target) < 0) {
+            if (++spins > (1u << 22)) {  // seconds: a co-resident grid never gets here
+                atomicExch(&gb->err, 1);
+                ok = 0;
+                break;
+            }
+        }
+        if (*((volatile int*)&gb->err) != 0) ok = 0;
+        s_ok = ok;
+    }
+    if (rec) pf.p[2 * pf.k++ + 1] = gtimer();
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <typename T>
+struct PackedCG {  // packed vector written by other blocks in an earlier phase
+    const T* p; int nr;
+    __device__ __forceinline__ T operator()(int i, int k) const { return __ldcg(p + i + (long)nr * k); }
+};
+
+// Sum of a partials slot (gridDim.x values) in a fixed order, broadcast to the block.
+template <int NT>
+__device__ __forceinline__ double slot_sum(const double* part, int slot, double* sm) {
+    double v = 0.0;
+    for (int q = threadIdx.x; q < (int)gridDim.x; q += NT) v += __ldcg(part + slot * DRD_MAXB + q);
+    const double r = block_sum<NT>(v, sm);
+    __shared__ double s_b;
+    if (threadIdx.x == 0) s_b = r;
+    __syncthreads();
+    const double out = s_b;
+    __syncthreads();
+    return out;
+}
+
+template <int NT>
+__device__ __forceinline__ void slot_put(double* part, int slot, double v, double* sm) {
+    const double r = block_sum<NT>(v, sm);
+    if (threadIdx.x == 0) part[slot * DRD_MAXB + blockIdx.x] = r;
+}
+
+constexpr int PB_NT = 512;  // threads per block of the persistent solver
+constexpr int PB_BM = 32, PB_BN = 32, PB_KC = 128;  // x-pass tile and K chunk
+constexpr int PB_CW = 4;                            // columns per z work item
+
+// x pass of the folded DCT-I: out[m][2n+p] = sum_k (X[m][k] +- X[m][L-k]) Bp[k][n].
+__device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float* smem) {
+    const int M = a.nz, L = a.nr - 1, K = a.Kx;
+    const int mt = (M + PB_BM - 1) / PB_BM;
+    const int nt0 = (a.Nxe + PB_BN - 1) / PB_BN, nt1 = (a.Nxo + PB_BN - 1) / PB_BN;
+    const int ntiles = mt * (nt0 + nt1);
+    float* As = smem;                  // [PB_BM][PB_KC + 1]
+    float* Bs = smem + PB_BM * (PB_KC + 1);  // [PB_KC][PB_BN]
+    const int tid = threadIdx.x;
+    const int r = tid / (PB_BN / 2), c0 = (tid % (PB_BN / 2)) * 2;  // 32 rows x 16 column pairs
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int mtile = tile % mt, nrest = tile / mt;
+        const int par = nrest >= nt0 ? 1 : 0;
+        const int ntile = par ? nrest - nt0 : nrest;
+        const int N = par ? a.Nxo : a.Nxe;
+        const float* B = par ? a.fxo : a.fxe;
+        const int ldb = a.Nxe;  // both folded operands are stored Kx x Nxe
+        const int m0 = mtile * PB_BM, n0 = ntile * PB_BN;
+        float acc0 = 0.f, acc1 = 0.f;
+        for (int k0 = 0; k0 < K; k0 += PB_KC) {
+            const int kc = min(PB_KC, K - k0);
+            // every load of the panel is issued before the first shared-memory store, so the
+            // whole chunk costs one L2 round trip (PB_BM * PB_KC / PB_NT = 8 loads a thread)
+            constexpr int JA = PB_BM * PB_KC / PB_NT, JB = PB_KC * PB_BN / PB_NT;
+            float x0[JA], x1[JA], bv[JB];
+#pragma unroll
+            for (int j = 0; j < JA; ++j) {
+                const int e = tid + j * PB_NT, rr = e / kc, kk = e % kc, m = m0 + rr, k = k0 + kk;
+                x0[j] = 0.f;
+                x1[j] = 0.f;
+                if (e < PB_BM * kc && m < M) {
+                    const float* row = X + (long)m * a.nr;
+                    x0[j] = __ldcg(row + k);
+                    if (2 * k != L) x1[j] = __ldcg(row + L - k);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < JB; ++j) {
+                const int e = tid + j * PB_NT, kk = e / PB_BN, cc = e % PB_BN, n = n0 + cc;
+                bv[j] = (kk < kc && n < N) ? __ldg(B + (long)(k0 + kk) * ldb + n) : 0.f;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < JA; ++j) {
+                const int e = tid + j * PB_NT, rr = e / kc, kk = e % kc, k = k0 + kk;
+                if (e < PB_BM * kc) {
+                    // folded operand: x(k) + x(L-k) (even outputs) or x(k) - x(L-k) (odd); the
+                    // middle column of an even L counts once and only for even outputs
+                    float v = par ? x0[j] - x1[j] : x0[j] + x1[j];
+                    if (2 * k == L) v = par ? 0.f : x0[j];
+                    As[rr * (PB_KC + 1) + kk] = v;
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < JB; ++j) {
+                const int e = tid + j * PB_NT, kk = e / PB_BN, cc = e % PB_BN;
+                if (kk < kc) Bs[kk * PB_BN + cc] = bv[j];
+            }
+            __syncthreads();
+            const float* ar = As + r * (PB_KC + 1);
+#pragma unroll 8
+            for (int kk = 0; kk < kc; ++kk) {
+                const float av = ar[kk];
+                acc0 = fmaf(av, Bs[kk * PB_BN + c0], acc0);
+                acc1 = fmaf(av, Bs[kk * PB_BN + c0 + 1], acc1);
+            }
+        }
+        const int m = m0 + r;
+        if (m < M) {
+            if (n0 + c0 < N) out[(long)m * a.nr + 2 * (n0 + c0) + par] = acc0;
+            if (n0 + c0 + 1 < N) out[(long)m * a.nr + 2 * (n0 + c0 + 1) + par] = acc1;
+        }
+    }
+}
+
+// One folded DCT-I along z of PB_CW columns held in xs[nz][PB_CW] -> ys[nz][PB_CW].
+__device__ __forceinline__ void pb_zcols(const PersistArgs& a, const float* xs, float* u, float* ys) {
+    const int nz = a.nz, L = nz - 1, K = a.Kz;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < K * PB_CW; e += PB_NT) {  // fold: u[p][j][c]
+        const int j = e / PB_CW, c = e % PB_CW;
+        const float x0 = xs[j * PB_CW + c];
+        if (2 * j == L) {
+            u[j * PB_CW + c] = x0;
+            u[(K + j) * PB_CW + c] = 0.f;
+        } else {
+            const float x1 = xs[(L - j) * PB_CW + c];
+            u[j * PB_CW + c] = x0 + x1;
+            u[(K + j) * PB_CW + c] = x0 - x1;
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < nz * PB_CW; e += PB_NT) {
+        const int row = e / PB_CW, c = e % PB_CW, par = row & 1, m = row >> 1;
+        const float* A = (par ? a.fzo : a.fze) + (long)m * K;
+        const float* up = u + (par ? K : 0) * PB_CW + c;
+        float acc0 = 0.f, acc1 = 0.f;
+        int j = 0;
+#pragma unroll 4
+        for (; j + 1 < K; j += 2) {
+            acc0 = fmaf(__ldg(A + j), up[j * PB_CW], acc0);
+            acc1 = fmaf(__ldg(A + j + 1), up[(j + 1) * PB_CW], acc1);
+        }
+        if (j < K) acc0 = fmaf(__ldg(A + j), up[j * PB_CW], acc0);
+        ys[row * PB_CW + c] = acc0 + acc1;
+    }
+    __syncthreads();
+}
+
+// z pass, divide by Ph_Lcc, z pass (columns are independent along z): out = Cz ((Cz X) / L).
+__device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* smem) {
+    const int nz = a.nz, nr = a.nr, K = a.Kz;
+    float* xs = smem;                 // [nz][CW]
+    float* u = xs + nz * PB_CW;       // [2][K][CW]
+    float* ys = u + 2 * K * PB_CW;    // [nz][CW]
+    const int nchunks = (nr + PB_CW - 1) / PB_CW;
+    for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const int c0 = ch * PB_CW;
+        __syncthreads();
+        for (int e = threadIdx.x; e < nz * PB_CW; e += PB_NT) {
+            const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
+            xs[e] = col < nr ? __ldcg(X + (long)row * nr + col) : 0.f;
+        }
+        __syncthreads();
+        pb_zcols(a, xs, u, ys);
+        for (int e = threadIdx.x; e < nz * PB_CW; e += PB_NT) {
+            const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
+            xs[e] = col < nr ? ys[e] / __ldg(a.lcc + (long)row * nr + col) : 0.f;
+        }
+        __syncthreads();
+        pb_zcols(a, xs, u, ys);
+        for (int e = threadIdx.x; e < nz * PB_CW; e += PB_NT) {
+            const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
+            if (col < nr) out[(long)row * nr + col] = ys[e];
+        }
+    }
+}
+
+// psolve: y = DCT-I preconditioner applied to x (three phases, two internal barriers).
+__device__ bool pb_psolve(const PersistArgs& a, const float* x, float* y, float* smem, unsigned& gen, PbProf& pf) {
+    pb_xpass(a, x, a.w1, smem);
+    if (!grid_sync(a.bar, gen, pf)) return false;
+    pb_zdz(a, a.w1, a.w2, smem);
+    if (!grid_sync(a.bar, gen, pf)) return false;
+    pb_xpass(a, a.w2, y, smem);
+    return true;
+}
+
+// y = A x (MATRIX_VECTOR_CG) in two phases; optional partial dots of y with d1 and with itself.
+__device__ bool pb_matvec_ch(const PersistArgs& a, const float* x, float* y, float alpha, const float* yin,
+                             const float* d1, int slot1, bool self2, int slot2, double* sm, unsigned& gen,
+                             PbProf& pf) {
+    const int nr = a.nr, nz = a.nz;
+    const long n = (long)nr * nz;
+    const long stride = (long)gridDim.x * PB_NT;
+    PackedCG<float> X{x, nr};
+    CellA<float> M0{a.M0, nr}, Mi{a.Mi, nr};
+    for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < n; q += stride) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        a.ff1[q] = -(a.o.dtxld * op_dgn<float>(i, k, nr, nz, a.o.idr2, a.o.idz2, X, M0));
+    }
+    if (!grid_sync(a.bar, gen, pf)) return false;
+    PackedCG<float> F{a.ff1, nr};
+    double s1 = 0.0, s2 = 0.0;
+    for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < n; q += stride) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        const float f = __ldcg(a.ff1 + q);
+        const float av = __ldcg(x + q) + (a.o.s * f / a.o.eps - a.o.eps * op_dgn<float>(i, k, nr, nz, a.o.idr2,
+                                                                                        a.o.idz2, F, Mi));
+        const float yn = yin ? alpha * av + __ldcg(yin + q) : alpha * av;
+        y[q] = yn;
+        if (d1) s1 += (double)__ldcg(d1 + q) * (double)yn;
+        if (self2) s2 += (double)yn * (double)yn;
+    }
+    if (d1) slot_put<PB_NT>(a.part, slot1, s1, sm);
+    if (self2) slot_put<PB_NT>(a.part, slot2, s2, sm);
+    return true;
+}
+
+// y = A x (MatrixVector_uv_2_CG / MatrixVector_uv_CG) in one phase, with the same options.
+__device__ bool pb_matvec_uv(const PersistArgs& a, const float* x, float* y, float alpha, const float* yin,
+                             const float* d1, int slot1, bool self2, int slot2, double* sm) {
+    const long mn = (long)(a.nr + 1) * a.nz;
+    const long stride = (long)gridDim.x * PB_NT;
+    UVFetch<float, true> F{x, a.nr, a.nz, mn, a.o.lr_neumann};
+    double s1 = 0.0, s2 = 0.0;
+    for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < a.n; q += stride) {
+        const float av = uv_apply<float>(a.o, a.rho, a.eta, a.pen, F, q);
+        const float yn = yin ? alpha * av + __ldcg(yin + q) : alpha * av;
+        y[q] = yn;
+        if (d1) s1 += (double)__ldcg(d1 + q) * (double)yn;
+        if (self2) s2 += (double)yn * (double)yn;
+    }
+    if (d1) slot_put<PB_NT>(a.part, slot1, s1, sm);
+    if (self2) slot_put<PB_NT>(a.part, slot2, s2, sm);
+    return true;
+}
+
+template <int KIND>
+__device__ __forceinline__ bool pb_matvec(const PersistArgs& a, const float* x, float* y, float alpha, const float* yin,
+                                          const float* d1, int slot1, bool self2, int slot2, double* sm,
+                                          unsigned& gen, PbProf& pf) {
+    if constexpr (KIND == PK_CH) return pb_matvec_ch(a, x, y, alpha, yin, d1, slot1, self2, slot2, sm, gen, pf);
+    (void)gen;
+    (void)pf;
+    return pb_matvec_uv(a, x, y, alpha, yin, d1, slot1, self2, slot2, sm);
+}
+
+// Element-wise preconditioner of the momentum system: Jacobi (PSolve_uv_2_CG) or the identity.
+__device__ __forceinline__ float pb_pre(const PersistArgs& a, long q, float v) {
+    return a.ident ? v : v / __ldg(a.diag + q);
+}
+
+}  // namespace
+
+template <int KIND>
+__global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
+    extern __shared__ float smem[];
+    __shared__ double sm[32];
+    count_launch(a.ctr);
+    unsigned gen = 0u;  // arrivals counted so far (the counter is zeroed before the launch)
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    const long n = a.n;
+    const long stride = (long)gridDim.x * PB_NT;
+    const long q0 = blockIdx.x * (long)PB_NT + threadIdx.x;
+    KState* ks = a.ks;
+    PbProf pf{nullptr, 0};
+    // the parent (FP64 refinement) state decides whether this inner solve runs at all
+    if (a.parent && *((volatile const int*)&a.parent->phase) != PH_RUNNING) {
+        if (lead) { ks->phase = PH_DONE; ks->iter = 0; ks->info = 0; }
+        return;
+    }
+    // ---- setup (:229-255): r = b, ||x||, ||b||, x0 test, rtld = r, first rho partials
+    double xx = 0.0, bb = 0.0;
+    for (long q = q0; q < n; q += stride) {
+        const float bv = __ldcg(a.b + q), xv = __ldcg(a.x + q);
+        a.r[q] = bv;
+        xx += (double)xv * (double)xv;
+        bb += (double)bv * (double)bv;
+    }
+    slot_put<PB_NT>(a.part, 0, xx, sm);
+    slot_put<PB_NT>(a.part, 3, bb, sm);
+    bool ok = grid_sync(a.bar, gen, pf);
+    const double xnorm = sqrt(slot_sum<PB_NT>(a.part, 0, sm));
+    const double bnorm_raw = sqrt(slot_sum<PB_NT>(a.part, 3, sm));
+    const double bnrm2 = bnorm_raw == 0.0 ? 1.0 : bnorm_raw;
+    const double tol = a.tol;
+    const int maxit = a.maxit;
+    int info = 0, iter = maxit, phase = maxit <= 0 ? PH_DONE : PH_RUNNING;
+    unsigned flags = 0u;
+    double resid = tol, rho = 0.0, rho1 = 0.0, alpha = 0.0, omega = 0.0, beta = 0.0, snorm = 0.0;
+    if (maxit <= 0) info = -3;
+    if (ok && phase == PH_RUNNING && xnorm != 0.0) {  // r = b - A x0 and the absolute x0 test (:248)
+        ok = pb_matvec<KIND>(a, a.x, a.r, -1.f, a.r, nullptr, 0, true, 0, sm, gen, pf) && grid_sync(a.bar, gen, pf);
+        const double rr = sqrt(slot_sum<PB_NT>(a.part, 0, sm));
+        if (rr <= tol) { phase = PH_DONE; info = 0; flags |= DRD_FLAG_EARLY_X0; }
+    }
+    if (phase == PH_RUNNING) iter = 0;
+    if (ok && phase == PH_RUNNING) {
+        double a1 = 0.0;
+        for (long q = q0; q < n; q += stride) {
+            const float rv = __ldcg(a.r + q);
+            a.rtld[q] = rv;
+            a1 += (double)rv * (double)rv;
+        }
+        slot_put<PB_NT>(a.part, 1, a1, sm);
+        ok = grid_sync(a.bar, gen, pf);
+    }
+    bool first = true;
+    // ---- iterations (:257-388)
+    while (ok && phase == PH_RUNNING) {
+        rho = slot_sum<PB_NT>(a.part, 1, sm);  // RHO = (rtld, r)
+        iter += 1;
+        pf.p = (a.prof != nullptr && iter == 3) ? a.prof : nullptr;  // time the third iteration
+        if (fabs(rho) < kBreakTol) { info = -10; phase = PH_DONE; break; }
+        beta = first ? 0.0 : (rho / rho1) * (alpha / omega);
+        {
+            const float bt = (float)beta, nom = (float)(-omega);
+            for (long q = q0; q < n; q += stride) {
+                float pv;
+                if (first) pv = __ldcg(a.r + q);
+                else {
+                    pv = __ldcg(a.p + q) + nom * __ldcg(a.v + q);
+                    pv = bt * pv;
+                    pv = pv + __ldcg(a.r + q);
+                }
+                a.p[q] = pv;
+                if constexpr (KIND == PK_UV) a.phat[q] = pb_pre(a, q, pv);  // PHAT = M^-1 P, fused
+            }
+        }
+        first = false;
+        if (!(ok = grid_sync(a.bar, gen, pf))) break;
+        if constexpr (KIND == PK_CH) {
+            if (!(ok = pb_psolve(a, a.p, a.phat, smem, gen, pf))) break;     // PHAT = M^-1 P
+            if (!(ok = grid_sync(a.bar, gen, pf))) break;
+        }
+        if (!(ok = pb_matvec<KIND>(a, a.phat, a.v, 1.f, nullptr, a.rtld, 4, false, 0, sm, gen, pf))) break;  // V = A PHAT
+        if (!(ok = grid_sync(a.bar, gen, pf))) break;
+        const double rv = slot_sum<PB_NT>(a.part, 4, sm);
+        alpha = rho / rv;  // (:307)
+        {
+            const float na = (float)(-alpha);
+            double s2 = 0.0;
+            for (long q = q0; q < n; q += stride) {
+                const float sv = __ldcg(a.r + q) + na * __ldcg(a.v + q);
+                a.r[q] = sv;
+                s2 += (double)sv * (double)sv;
+                if constexpr (KIND == PK_UV) a.shat[q] = pb_pre(a, q, sv);  // SHAT = M^-1 S, fused
+            }
+            slot_put<PB_NT>(a.part, 5, s2, sm);
+        }
+        if (!(ok = grid_sync(a.bar, gen, pf))) break;
+        snorm = sqrt(slot_sum<PB_NT>(a.part, 5, sm));
+        if (snorm <= tol) {  // early absolute test (:313-316): X = X + ALPHA PHAT
+            resid = snorm / bnrm2;
+            info = 0;
+            flags |= DRD_FLAG_EARLY_S;
+            const float al = (float)alpha;
+            for (long q = q0; q < n; q += stride) a.x[q] = __ldcg(a.x + q) + al * __ldcg(a.phat + q);
+            phase = PH_DONE;
+            break;
+        }
+        if constexpr (KIND == PK_CH) {
+            if (!(ok = pb_psolve(a, a.r, a.shat, smem, gen, pf))) break;     // SHAT = M^-1 S
+            if (!(ok = grid_sync(a.bar, gen, pf))) break;
+        }
+        if (!(ok = pb_matvec<KIND>(a, a.shat, a.t, 1.f, nullptr, a.r, 6, true, 7, sm, gen, pf))) break;  // T = A SHAT
+        if (!(ok = grid_sync(a.bar, gen, pf))) break;
+        const double ts = slot_sum<PB_NT>(a.part, 6, sm), tt = slot_sum<PB_NT>(a.part, 7, sm);
+        omega = ts / tt;  // (:349-350)
+        {
+            const float al = (float)alpha, om = (float)omega, nom = (float)(-omega);
+            double r2 = 0.0, rr = 0.0;
+            for (long q = q0; q < n; q += stride) {
+                float xv = __ldcg(a.x + q) + al * __ldcg(a.phat + q);
+                xv = xv + om * __ldcg(a.shat + q);
+                a.x[q] = xv;
+                const float rvq = __ldcg(a.r + q) + nom * __ldcg(a.t + q);
+                a.r[q] = rvq;
+                r2 += (double)rvq * (double)rvq;
+                rr += (double)__ldcg(a.rtld + q) * (double)rvq;
+            }
+            slot_put<PB_NT>(a.part, 0, r2, sm);
+            slot_put<PB_NT>(a.part, 1, rr, sm);
+        }
+        if (!(ok = grid_sync(a.bar, gen, pf))) break;
+        resid = sqrt(slot_sum<PB_NT>(a.part, 0, sm)) / bnrm2;  // STOPTEST2 (:361-362)
+        if (!isfinite(resid)) { info = DRD_ERR_NONFINITE; phase = PH_DONE; }
+        else if (resid <= tol) { info = 0; phase = PH_DONE; }
+        else if (iter >= maxit) { info = 1; phase = PH_DONE; }
+        else if (fabs(omega) < kBreakTol) { info = (fabs(rho) < kBreakTol) ? -10 : -11; phase = PH_DONE; }
+        else rho1 = rho;
+    }
+    if (!ok) info = DRD_ERR_TIMEOUT;
+    if (lead) {
+        ks->tol = tol;
+        ks->maxit = maxit;
+        ks->xnorm = xnorm;
+        ks->x_nonzero = xnorm != 0.0;
+        ks->bnorm_raw = bnorm_raw;
+        ks->bnrm2 = bnrm2;
+        ks->iter = iter;
+        ks->info = info;
+        ks->resid = resid;
+        ks->snorm = snorm;
+        ks->rho = rho;
+        ks->rho1 = rho1;
+        ks->alpha = alpha;
+        ks->omega = omega;
+        ks->beta = beta;
+        ks->flags = flags;
+        ks->mixed = 0;
+        ks->phase = PH_DONE;
+    }
+}
+
+// ======================================================================================
 // Host launchers
 // ======================================================================================
 #define GRID(n) grid_for(n), DRD_TPB, 0, s
+
+__global__ void k_bar_reset(GridBar* b, ull* ctr) {
+    count_launch(ctr);
+    if (threadIdx.x == 0) {
+        b->count = 0u;
+        b->err = 0;
+    }
+}
+void launch_bar_reset(GridBar* b, ull* ctr, cudaStream_t s) { k_bar_reset<<<1, 32, 0, s>>>(b, ctr); }
+size_t persist_ch_smem(int nr, int nz) {
+    const size_t xp = sizeof(float) * ((size_t)PB_BM * (PB_KC + 1) + (size_t)PB_KC * PB_BN);
+    const int Kz = (nz - 1) / 2 + 1;
+    const size_t zp = sizeof(float) * ((size_t)nz * PB_CW * 2 + (size_t)2 * Kz * PB_CW);
+    (void)nr;
+    return xp > zp ? xp : zp;
+}
+int persist_threads() { return PB_NT; }
+const void* persist_kernel(int kind) {
+    return kind == PK_CH ? (const void*)k_bicg_persist<PK_CH> : (const void*)k_bicg_persist<PK_UV>;
+}
+cudaError_t launch_bicg_persist(const PersistArgs& a, int grid, cudaStream_t s) {
+    const size_t smem = a.kind == PK_CH ? persist_ch_smem(a.nr, a.nz) : 0;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(PB_NT);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (a.kind == PK_CH) return cudaLaunchKernelEx(&cfg, k_bicg_persist<PK_CH>, a);
+    return cudaLaunchKernelEx(&cfg, k_bicg_persist<PK_UV>, a);
+}
 
 void launch_ch_f2(const DevParams& P, const double* u, const double* v, const double* ph, double* f2, ull* ctr,
                   cudaStream_t s) {

@@ -115,6 +115,40 @@ void launch_cell_add(long n, const double* x, double* y, ull* ctr, cudaStream_t 
 void launch_interp_coef(const DevParams& P, const double* dist, const double* bdr, double* fpd, double* rho, double* eta,
                         ull* ctr, cudaStream_t s);
 
+// ---- persistent cooperative BiCGSTAB (FP32 inner solves of the CH and momentum systems) ---
+struct GridBar {
+    unsigned count, gen;
+    int err, pad;
+};
+enum PersistKind : int { PK_CH = 0, PK_UV = 1 };
+struct PersistArgs {
+    int kind;                             // PK_CH or PK_UV
+    int nr, nz;
+    long n;                               // unknowns
+    OpScal<float> o;
+    // CH: mobilities (CELL), packed Ph_Lcc, folded DCT-I operands
+    const float *M0, *Mi, *lcc;
+    const float *fxe, *fxo, *fze, *fzo;
+    int Kx, Nxe, Nxo, Kz, Mze, Mzo;
+    // momentum: rho, eta, penalty mask (CELL), Jacobi diagonal; ident = identity preconditioner
+    const float *rho, *eta, *pen, *diag;
+    int ident;
+    float *x, *b, *r, *rtld, *p, *v, *phat, *shat, *t, *ff1, *w1, *w2;
+    double* part;
+    KState* ks;
+    const KState* parent;
+    GridBar* bar;
+    double tol;
+    int maxit;
+    ull* ctr;
+    unsigned long long* prof;  // optional: barrier entry/exit times (ns) of block 0 in iteration 3
+};
+size_t persist_ch_smem(int nr, int nz);
+int persist_threads();
+const void* persist_kernel(int kind);
+cudaError_t launch_bicg_persist(const PersistArgs& a, int grid, cudaStream_t s);
+void launch_bar_reset(GridBar* b, ull* ctr, cudaStream_t s);
+
 // ---- fiber particles (microfluidics_complex_domain/particles_move.f90), drd_particles.cu --
 constexpr int PT_GX = 64;  // blocks per bead in the per-bead sums
 struct PartParams {

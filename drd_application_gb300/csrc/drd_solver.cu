@@ -73,6 +73,12 @@ struct drd_ctx {
     // PhSolve_ori: wall-energy prefactors cf of angleB / angleT (XLINE) and alpha_s
     double *ori_cfb, *ori_cft;
     double ori_alpha = 0.0;
+    // persistent cooperative inner solver (FP32 CH): grid size, barrier state, on/off
+    int persist = 0, pgrid = 0;
+    GridBar* bar = nullptr;
+    std::string persist_err;
+    unsigned long long* pprof = nullptr;  // DRD_PERSIST_PROF=1: barrier timestamps of block 0
+    int pprof_on = 0;
     KState* ks;      // device, KS_COUNT entries
     CallArgs* ca;    // device
     double* d_mass;  // device
@@ -134,6 +140,8 @@ size_t arena_need(long cs, long us, long vs, long nc, long nr, long nz, long nma
     for (int i = 0; i < 4; ++i) add(2 * DRD_PARTICLES_MAX, 8);  // pts, pts_old, totF, psum
     add(3 * DRD_PARTICLES_MAX * PT_GX, 8); add(cs, 8);          // ppart, bdist
     add(nr + 1, 8); add(nr + 1, 8);                            // ori_cfb, ori_cft
+    add(sizeof(GridBar), 1);                                   // bar
+    add(128, 8);                                               // pprof
     return b + 4096;
 }
 
@@ -499,6 +507,49 @@ int capture_if(drd_ctx* c, cudaStream_t s, cudaStream_t sb, cudaGraphConditional
     return DRD_OK;
 }
 
+// The persistent cooperative inner solver needs cooperative launch support and one resident
+// block per SM; DRD_PERSIST=0 in the environment turns it off (the graph-loop path is used).
+int setup_persist(drd_ctx* c) {
+    c->persist = 0;
+    const char* env = std::getenv("DRD_PERSIST");
+    if (env && std::atoi(env) == 0) return DRD_OK;
+    int coop = 0, sms = 0;
+    CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+    if (!coop || sms < 1) { c->persist_err = "no cooperative launch on this device"; return DRD_OK; }
+    const size_t smem = persist_ch_smem(c->nr, c->nz);
+    for (int kind = PK_CH; kind <= PK_UV; ++kind) {
+        const size_t sm = kind == PK_CH ? smem : 0;
+        int occ = 0;
+        CK(cudaFuncSetAttribute(persist_kernel(kind), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persist_kernel(kind), persist_threads(), sm));
+        if (occ < 1) { c->persist_err = "persistent solver does not fit one block per SM"; return DRD_OK; }
+    }
+    c->pgrid = std::min(sms, DRD_MAXB);
+    c->persist = 1;
+    const char* pe = std::getenv("DRD_PERSIST_PROF");
+    c->pprof_on = pe && std::atoi(pe) != 0;
+    return DRD_OK;
+}
+
+// Arguments of the persistent FP32 inner solve of system S (the k32 vectors, FP32 coefficients).
+PersistArgs persist_args(drd_ctx* c, const Sys& S, KState* in, const KState* parent, double tol, int maxit) {
+    PersistArgs a{};
+    a.kind = (S.kind == SYS_CH) ? PK_CH : PK_UV;
+    a.nr = c->nr; a.nz = c->nz; a.n = S.n;
+    a.o = make_op<float>(c, S.kind == SYS_UV ? S.bdf : 0);
+    a.M0 = c->M032; a.Mi = c->Mi32; a.lcc = c->ph_lcc32;
+    a.fxe = c->f1xe32; a.fxo = c->f1xo32; a.fze = c->f1ze32; a.fzo = c->f1zo32;
+    a.Kx = c->Kx; a.Nxe = c->Nxe; a.Nxo = c->Nxo; a.Kz = c->Kz; a.Mze = c->Mze; a.Mzo = c->Mzo;
+    KVecs<float>& f = c->k32;
+    a.rho = c->rho32; a.eta = c->eta32; a.pen = c->pen32; a.diag = f.diag; a.ident = S.ident || !S.jacobi;
+    a.x = f.x; a.b = f.b; a.r = f.r; a.rtld = f.rtld; a.p = f.p; a.v = f.v; a.phat = f.phat; a.shat = f.shat;
+    a.t = f.t; a.ff1 = f.ff1; a.w1 = c->t1f; a.w2 = c->t2f;
+    a.part = c->part; a.ks = in; a.parent = parent; a.bar = c->bar; a.tol = tol; a.maxit = maxit; a.ctr = c->ctr;
+    a.prof = c->pprof_on ? c->pprof : nullptr;
+    return a;
+}
+
 // A whole Krylov solve of system S for k64.b with guess k64.x (FP64 result in k64.x).
 // FP64 mode: the reference's BiCGSTAB.  Mixed mode: FP64 iterative refinement around an FP32
 // BiCGSTAB with the same preconditioner.  `ks_slot` receives the status.
@@ -529,11 +580,21 @@ int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int 
         const double itol = c->P.mixed_inner_tol;
         rc = capture_while(c, s, c->s2, ks, [&](cudaStream_t sb, cudaGraphConditionalHandle ho) {
             launch_mx_scale<float>(S.n, k.r, ks, f.b, f.x, c->ctr, sb);
-            enq_bicg_setup<float>(c, S, f, in, itol, maxit, ks, sb);
-            int rc2 = capture_while(c, sb, c->s3, in, [&](cudaStream_t si, cudaGraphConditionalHandle hi) {
-                enq_bicg_iter<float>(c, S, f, in, hi, 1, si);
-            });
-            if (rc2) rc = rc2;
+            if (c->persist && (S.kind == SYS_CH || S.kind == SYS_UV)) {
+                // the whole inner solve in one cooperative launch (grid barriers between phases)
+                launch_bar_reset(c->bar, c->ctr, sb);
+                cudaError_t e = launch_bicg_persist(persist_args(c, S, in, ks, itol, maxit), c->pgrid, sb);
+                if (e != cudaSuccess) {
+                    c->err = std::string("persistent solver launch: ") + cudaGetErrorString(e);
+                    rc = DRD_ERR_CUDA;
+                }
+            } else {
+                enq_bicg_setup<float>(c, S, f, in, itol, maxit, ks, sb);
+                int rc2 = capture_while(c, sb, c->s3, in, [&](cudaStream_t si, cudaGraphConditionalHandle hi) {
+                    enq_bicg_iter<float>(c, S, f, in, hi, 1, si);
+                });
+                if (rc2) rc = rc2;
+            }
             launch_axpy_f2d(S.n, ks, f.x, k.x, c->ctr, sb);
             launch_copy<double>(S.n, k.b, k.r, c->ctr, sb);
             enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.r, nullptr, 1, -1, nullptr, G_ALWAYS, sb);
@@ -772,6 +833,14 @@ int run_graph(drd_ctx* c, long key, const std::function<int(cudaStream_t)>& buil
     if (!c->use_graph) return build(c->s);  // direct launches (DRD_DIRECT_LAUNCH=1)
     cudaGraphExec_t ex;
     rc = get_graph(c, key, build, &ex);
+    if (rc == DRD_ERR_CUDA && c->persist) {
+        // a graph that cannot hold the cooperative inner solver: record why, use the graph loop
+        c->persist_err = c->err;
+        c->persist = 0;
+        cudaGetLastError();
+        clear_graphs(c);
+        rc = get_graph(c, key, build, &ex);
+    }
     if (rc) return rc;
     CK(cudaGraphLaunch(ex, c->s));
     return DRD_OK;
@@ -870,6 +939,8 @@ int setup_context(drd_ctx* c) {
     c->totF = carve<double>(c, 2 * DRD_PARTICLES_MAX); c->psum = carve<double>(c, 2 * DRD_PARTICLES_MAX);
     c->ppart = carve<double>(c, 3 * DRD_PARTICLES_MAX * PT_GX); c->bdist = carve<double>(c, c->cs);
     c->ori_cfb = carve<double>(c, nr + 1); c->ori_cft = carve<double>(c, nr + 1);
+    c->bar = (GridBar*)carve<char>(c, sizeof(GridBar));
+    c->pprof = (unsigned long long*)carve<double>(c, 128);
     if (c->arena_used > c->arena_bytes) { c->err = "arena overflow"; return DRD_ERR_NOMEM; }
     CK(cudaMallocHost(&c->h_ks, KS_COUNT * sizeof(KState)));
     CK(cudaMallocHost(&c->h_ca, sizeof(CallArgs)));
@@ -921,6 +992,8 @@ int setup_context(drd_ctx* c) {
     CK(put(c->cfB, cfa));
     CK(put(c->cfT, cfa));
     int rc = upload_tables(c);
+    if (rc) return rc;
+    rc = setup_persist(c);
     if (rc) return rc;
     rc = refresh_fp32(c);
     if (rc) return rc;
@@ -1623,6 +1696,22 @@ int drd_flush_l2(drd_ctx* c, int64_t bytes) {
     }
     CK(cudaMemsetAsync(buf, have & 0xff, (size_t)bytes, c->s));
     return DRD_OK;
+}
+
+int drd_persist_profile(drd_ctx* c, int64_t* ns, int n) {
+    if (!c || !ns || n <= 0) return DRD_ERR_BADARG;
+    const int m = std::min(n, 124);
+    std::vector<unsigned long long> h(m);
+    CK(cudaStreamSynchronize(c->s));
+    CK(cudaMemcpy(h.data(), c->pprof, sizeof(unsigned long long) * m, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < m; ++i) ns[i] = (int64_t)h[i];
+    return m;
+}
+
+int drd_persistent_solver(drd_ctx* c, char* why, int len) {
+    if (!c) return DRD_ERR_BADARG;
+    if (why && len > 0) std::snprintf(why, (size_t)len, "%s", c->persist_err.c_str());
+    return c->persist;
 }
 
 int64_t drd_kernel_launches(drd_ctx* c) {

@@ -404,6 +404,17 @@ int drd_kernel_bench(drd_ctx* ctx, int which, int reps, double* us_per_launch, d
 /* Writes `bytes` of scratch memory on the context stream (evicts L2 between timed steps). */
 int drd_flush_l2(drd_ctx* ctx, int64_t bytes);
 
+/* 1 when the mixed mode runs each FP32 inner CH solve as one persistent cooperative launch
+ * (grid-wide barriers between the phases of an iteration), 0 when it runs the captured
+ * kernel-per-phase loop (no cooperative launch support, DRD_PERSIST=0 in the environment, or a
+ * graph that could not take the cooperative launch: `why` then receives that error). */
+int drd_persistent_solver(drd_ctx* ctx, char* why, int len);
+/* With DRD_PERSIST_PROF=1 in the environment at drd_create, the persistent solver records
+ * %globaltimer (ns) at entry and exit of each grid barrier of its third iteration, as seen by
+ * block 0: ns[2k], ns[2k+1] for barrier k (up to 62 barriers; zero where none ran).  Returns
+ * the number of entries copied. */
+int drd_persist_profile(drd_ctx* ctx, int64_t* ns, int n);
+
 /* Number of kernels this library has launched on the context (graph nodes counted per
  * execution), cumulative. */
 int64_t drd_kernel_launches(drd_ctx* ctx);
