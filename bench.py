@@ -332,13 +332,15 @@ def run_gpu(args, ws, rank, local):
     e2e_steps = K
     ctx.close()
 
-    # plain FP64 path, resident state
-    case64 = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_FP64)
-    ctx64 = DRDContext(case64.params)
-    ctx64.set_case(case64)
-    f64 = time_resident(ctx64, case64, W, K64, flush)
-    f64_sec = max_over_ranks(dist, f64["seconds"])
-    ctx64.close()
+    # plain FP64 path, resident state (--fp64-steps 0 skips it, e.g. for profiler runs)
+    f64, f64_sec = None, None
+    if K64 > 0:
+        case64 = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_FP64)
+        ctx64 = DRDContext(case64.params)
+        ctx64.set_case(case64)
+        f64 = time_resident(ctx64, case64, W, K64, flush)
+        f64_sec = max_over_ranks(dist, f64["seconds"])
+        ctx64.close()
 
     if rank != 0:
         return 0
@@ -378,10 +380,11 @@ def run_gpu(args, ws, rank, local):
             "ch_iters_mean": statistics.mean(mx["ch_iters"]), "uv_iters_mean": statistics.mean(mx["uv_iters"]),
             "refinements_mean": statistics.mean(mx["refinements"]),
             "wall_s_timed_region": wall,
-            "fp64": {"steps_per_s": K64 * ws / f64_sec, "ms_per_step": 1e3 * f64_sec / K64, "steps": K64,
-                     "ch_iters_mean": statistics.mean(f64["ch_iters"]), "uv_iters_mean": statistics.mean(f64["uv_iters"]),
-                     "solves_to_fp64_1e-8": f"{f64['solves_ok']}/{f64['solves']}"},
-            "mixed_over_fp64": (value / (K64 * ws / f64_sec)),
+            "fp64": None if f64 is None else {
+                "steps_per_s": K64 * ws / f64_sec, "ms_per_step": 1e3 * f64_sec / K64, "steps": K64,
+                "ch_iters_mean": statistics.mean(f64["ch_iters"]), "uv_iters_mean": statistics.mean(f64["uv_iters"]),
+                "solves_to_fp64_1e-8": f"{f64['solves_ok']}/{f64['solves']}"},
+            "mixed_over_fp64": None if f64 is None else (value / (K64 * ws / f64_sec)),
             "kernels_us": {abi.KB_NAMES[k]: round(v[0], 3) for k, v in kb.items()},
         },
         "roofline": {"bound": "hbm", "kernel": abi.KB_NAMES[dom], "achieved": achieved, "peak": hbm_peak,

@@ -15,7 +15,7 @@
 
 #define DRD_TPB 256        // threads per block of the element-wise / stencil kernels
 #define DRD_MAXB 1024      // maximum blocks of a reduction grid (= partials per dot product)
-#define DRD_NDOT 8         // dot-product slots in the partials buffer
+#define DRD_NDOT 10        // dot-product slots in the partials buffer
 
 namespace drd {
 

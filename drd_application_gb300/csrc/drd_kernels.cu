@@ -1704,6 +1704,10 @@ __device__ __forceinline__ unsigned long long gtimer() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
+// Sub-phase mark: time at point `i` (0..3) of the first x pass of a timed iteration, p[124 + i].
+__device__ __forceinline__ void pb_mark(const PbProf& pf, int i) {
+    if (pf.p != nullptr && pf.k <= 1 && blockIdx.x == 0 && threadIdx.x == 0) pf.p[124 + i] = gtimer();
+}
 
 __device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
@@ -1758,6 +1762,26 @@ __device__ __forceinline__ double slot_sum(const double* part, int slot, double*
     return out;
 }
 
+// Sums of two partials slots in one pass (one L2 round trip), broadcast to the block.
+template <int NT>
+__device__ __forceinline__ double2 slot_sum2(const double* part, int s1, int s2, double* sm) {
+    double v1 = 0.0, v2 = 0.0;
+    for (int q = threadIdx.x; q < (int)gridDim.x; q += NT) {
+        v1 += __ldcg(part + s1 * DRD_MAXB + q);
+        v2 += __ldcg(part + s2 * DRD_MAXB + q);
+    }
+    const double r1 = block_sum<NT>(v1, sm);
+    __shared__ double s_b1;
+    if (threadIdx.x == 0) s_b1 = r1;
+    const double r2 = block_sum<NT>(v2, sm);  // its barriers also publish s_b1
+    __shared__ double s_b2;
+    if (threadIdx.x == 0) s_b2 = r2;
+    __syncthreads();
+    const double2 out = make_double2(s_b1, s_b2);
+    __syncthreads();
+    return out;
+}
+
 template <int NT>
 __device__ __forceinline__ void slot_put(double* part, int slot, double v, double* sm) {
     const double r = block_sum<NT>(v, sm);
@@ -1765,124 +1789,223 @@ __device__ __forceinline__ void slot_put(double* part, int slot, double v, doubl
 }
 
 constexpr int PB_NT = 512;  // threads per block of the persistent solver
-constexpr int PB_BM = 32, PB_BN = 32, PB_KC = 128;  // x-pass tile and K chunk
+constexpr int PB_BM = 32, PB_BN = 32, PB_KC = 224;  // x-pass tile and K chunk (JA = 14)
 constexpr int PB_CW = 4;                            // columns per z work item
 
-// x pass of the folded DCT-I: out[m][2n+p] = sum_k (X[m][k] +- X[m][L-k]) Bp[k][n].
-__device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float* smem) {
+// Shared-memory plan of the persistent CH solver (floats; see persist_ch_plan): the z-pass
+// operands and the block's own x-pass B panel stay resident for the whole solve when they fit,
+// so each transform phase only moves the vector data.
+__device__ __forceinline__ int pb_xtiles(const PersistArgs& a, int& mt, int& nt0) {
+    mt = (a.nz + PB_BM - 1) / PB_BM;
+    nt0 = (a.Nxe + PB_BN - 1) / PB_BN;
+    const int nt1 = (a.Nxo + PB_BN - 1) / PB_BN;
+    return mt * (nt0 + nt1);
+}
+
+// Loads the resident operands at the start of the solve.
+__device__ void pb_load_resident(const PersistArgs& a, float* smem) {
+    if (a.z_res) {
+        float* zA = smem + a.z_off;  // [2][Mze][Kz4], rows padded with zeros to a multiple of 4
+        const int K = a.Kz, K4 = (K + 3) & ~3, tot = 2 * a.Mze * K4;
+        for (int e = threadIdx.x; e < tot; e += PB_NT) {
+            const int par = e / (a.Mze * K4), rest = e % (a.Mze * K4), m = rest / K4, jj = rest % K4;
+            float v = 0.f;
+            if (jj < K) {
+                if (par == 0) v = __ldg(a.fze + (long)m * K + jj);
+                else if (m < a.Mzo) v = __ldg(a.fzo + (long)m * K + jj);
+            }
+            zA[e] = v;
+        }
+    }
+    if (a.b_res) {
+        int mt, nt0;
+        const int ntiles = pb_xtiles(a, mt, nt0);
+        const int tile = blockIdx.x;
+        if (tile < ntiles) {
+            const int nrest = tile / mt, par = nrest >= nt0 ? 1 : 0, ntile = par ? nrest - nt0 : nrest;
+            const int N = par ? a.Nxo : a.Nxe, n0 = ntile * PB_BN;
+            const float* B = par ? a.fxo : a.fxe;
+            float* Bs = smem + a.b_off;  // [Kx][PB_BN]
+            for (int e = threadIdx.x; e < a.Kx * PB_BN; e += PB_NT) {
+                const int kk = e / PB_BN, cc = e % PB_BN, n = n0 + cc;
+                Bs[e] = n < N ? __ldg(B + (long)kk * a.Nxe + n) : 0.f;  // both stored Kx x Nxe
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// x pass of the folded DCT-I: out[m][2n+p] = sum_k (X[m][k] +- X[m][L-k]) Bp[k][n], one
+// PB_BM x PB_BN tile per block.  The block's 512 threads split K eight ways; each thread keeps
+// a 4 x 4 register tile and reads its operands as float4 (two 16-byte shared loads per 16 FMA),
+// and the eight partial tiles are summed through shared memory in a fixed order.
+constexpr int PB_KG = 8;  // K groups of the x pass
+__device__ __forceinline__ int pb_swz(int k, int m) { return k * PB_BM + ((((m >> 2) ^ (k & 7)) << 2) | (m & 3)); }
+__device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float* smem, const PbProf& pf) {
     const int M = a.nz, L = a.nr - 1, K = a.Kx;
-    const int mt = (M + PB_BM - 1) / PB_BM;
-    const int nt0 = (a.Nxe + PB_BN - 1) / PB_BN, nt1 = (a.Nxo + PB_BN - 1) / PB_BN;
-    const int ntiles = mt * (nt0 + nt1);
-    float* As = smem;                  // [PB_BM][PB_KC + 1]
-    float* Bs = smem + PB_BM * (PB_KC + 1);  // [PB_KC][PB_BN]
-    const int tid = threadIdx.x;
-    const int r = tid / (PB_BN / 2), c0 = (tid % (PB_BN / 2)) * 2;  // 32 rows x 16 column pairs
+    int mt, nt0;
+    const int ntiles = pb_xtiles(a, mt, nt0);
+    float* At = smem + a.work_off;              // [PB_KC][PB_BM], float4 groups swizzled by k
+    float* Bw = At + PB_KC * PB_BM;             // [PB_KC][PB_BN] when B is not resident
+    float* red = Bw + PB_KC * PB_BN;            // [PB_KG][PB_BM * PB_BN]
+    const int tid = threadIdx.x, g = tid >> 6, t = tid & 63, mi = t >> 3, ni = t & 7;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int mtile = tile % mt, nrest = tile / mt;
         const int par = nrest >= nt0 ? 1 : 0;
         const int ntile = par ? nrest - nt0 : nrest;
         const int N = par ? a.Nxo : a.Nxe;
         const float* B = par ? a.fxo : a.fxe;
-        const int ldb = a.Nxe;  // both folded operands are stored Kx x Nxe
         const int m0 = mtile * PB_BM, n0 = ntile * PB_BN;
-        float acc0 = 0.f, acc1 = 0.f;
+        float acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
         for (int k0 = 0; k0 < K; k0 += PB_KC) {
             const int kc = min(PB_KC, K - k0);
-            // every load of the panel is issued before the first shared-memory store, so the
-            // whole chunk costs one L2 round trip (PB_BM * PB_KC / PB_NT = 8 loads a thread)
-            constexpr int JA = PB_BM * PB_KC / PB_NT, JB = PB_KC * PB_BN / PB_NT;
-            float x0[JA], x1[JA], bv[JB];
+            // all loads of the chunk first (one L2 round trip), then the folded stores
+            constexpr int JA = PB_BM * PB_KC / PB_NT;
+            float x0[JA], x1[JA];
+            // element e = tid + j*PB_NT of the chunk is (row rr, column kk) = (e / kc, e % kc);
+            // the quotient and remainder advance by those of PB_NT instead of dividing again
+            const int dq = PB_NT / kc, dr = PB_NT % kc;
+            int rr = tid / kc, kk = tid % kc;
 #pragma unroll
             for (int j = 0; j < JA; ++j) {
-                const int e = tid + j * PB_NT, rr = e / kc, kk = e % kc, m = m0 + rr, k = k0 + kk;
+                const int m = m0 + rr, k = k0 + kk;
                 x0[j] = 0.f;
                 x1[j] = 0.f;
-                if (e < PB_BM * kc && m < M) {
+                if (rr < PB_BM && m < M) {
                     const float* row = X + (long)m * a.nr;
                     x0[j] = __ldcg(row + k);
                     if (2 * k != L) x1[j] = __ldcg(row + L - k);
                 }
-            }
-#pragma unroll
-            for (int j = 0; j < JB; ++j) {
-                const int e = tid + j * PB_NT, kk = e / PB_BN, cc = e % PB_BN, n = n0 + cc;
-                bv[j] = (kk < kc && n < N) ? __ldg(B + (long)(k0 + kk) * ldb + n) : 0.f;
+                rr += dq;
+                kk += dr;
+                if (kk >= kc) { kk -= kc; rr += 1; }
             }
             __syncthreads();
+            rr = tid / kc;
+            kk = tid % kc;
 #pragma unroll
             for (int j = 0; j < JA; ++j) {
-                const int e = tid + j * PB_NT, rr = e / kc, kk = e % kc, k = k0 + kk;
-                if (e < PB_BM * kc) {
+                if (rr < PB_BM) {
                     // folded operand: x(k) + x(L-k) (even outputs) or x(k) - x(L-k) (odd); the
                     // middle column of an even L counts once and only for even outputs
+                    const int k = k0 + kk;
                     float v = par ? x0[j] - x1[j] : x0[j] + x1[j];
                     if (2 * k == L) v = par ? 0.f : x0[j];
-                    As[rr * (PB_KC + 1) + kk] = v;
+                    At[pb_swz(kk, rr)] = v;
                 }
+                rr += dq;
+                kk += dr;
+                if (kk >= kc) { kk -= kc; rr += 1; }
             }
-#pragma unroll
-            for (int j = 0; j < JB; ++j) {
-                const int e = tid + j * PB_NT, kk = e / PB_BN, cc = e % PB_BN;
-                if (kk < kc) Bs[kk * PB_BN + cc] = bv[j];
+            pb_mark(pf, 0);
+            const float* Bk;
+            if (a.b_res) {
+                Bk = smem + a.b_off + (long)k0 * PB_BN;
+            } else {
+                for (int e = tid; e < kc * PB_BN; e += PB_NT) {
+                    const int kk = e / PB_BN, cc = e % PB_BN, n = n0 + cc;
+                    Bw[e] = n < N ? __ldg(B + (long)(k0 + kk) * a.Nxe + n) : 0.f;
+                }
+                Bk = Bw;
             }
             __syncthreads();
-            const float* ar = As + r * (PB_KC + 1);
-#pragma unroll 8
-            for (int kk = 0; kk < kc; ++kk) {
-                const float av = ar[kk];
-                acc0 = fmaf(av, Bs[kk * PB_BN + c0], acc0);
-                acc1 = fmaf(av, Bs[kk * PB_BN + c0 + 1], acc1);
+            const int kgn = (kc + PB_KG - 1) / PB_KG, kb = g * kgn, ke = min(kb + kgn, kc);
+            for (int kk = kb; kk < ke; ++kk) {
+                const float4 av = *reinterpret_cast<const float4*>(At + kk * PB_BM + ((mi ^ (kk & 7)) << 2));
+                const float4 bv = *reinterpret_cast<const float4*>(Bk + kk * PB_BN + (ni << 2));
+                const float ar[4] = {av.x, av.y, av.z, av.w}, br[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(ar[i], br[j], acc[i][j]);
             }
+            pb_mark(pf, 1);
+            __syncthreads();
         }
-        const int m = m0 + r;
-        if (m < M) {
-            if (n0 + c0 < N) out[(long)m * a.nr + 2 * (n0 + c0) + par] = acc0;
-            if (n0 + c0 + 1 < N) out[(long)m * a.nr + 2 * (n0 + c0 + 1) + par] = acc1;
+        // the eight K-group partial tiles, summed in group order
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            *reinterpret_cast<float4*>(red + g * (PB_BM * PB_BN) + (4 * mi + i) * PB_BN + 4 * ni) =
+                make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+        __syncthreads();
+        for (int o = tid; o < PB_BM * PB_BN; o += PB_NT) {
+            float v = 0.f;
+#pragma unroll
+            for (int gg = 0; gg < PB_KG; ++gg) v += red[gg * (PB_BM * PB_BN) + o];
+            const int m = m0 + o / PB_BN, n = n0 + o % PB_BN;
+            if (m < M && n < N) out[(long)m * a.nr + 2 * n + par] = v;
         }
+        pb_mark(pf, 2);
+        __syncthreads();
     }
 }
 
-// One folded DCT-I along z of PB_CW columns held in xs[nz][PB_CW] -> ys[nz][PB_CW].
-__device__ __forceinline__ void pb_zcols(const PersistArgs& a, const float* xs, float* u, float* ys) {
-    const int nz = a.nz, L = nz - 1, K = a.Kz;
+// One folded DCT-I along z of PB_CW columns held in xs[nz][PB_CW] -> ys[nz][PB_CW].  The folded
+// columns are kept transposed, u[p][c][Kz4] (zero-padded), so both operands of the inner
+// product are read as float4 when the z operands are resident in shared memory.
+__device__ __forceinline__ void pb_zcols(const PersistArgs& a, const float* xs, float* u, float* ys,
+                                         const float* zA) {
+    const int nz = a.nz, L = nz - 1, K = a.Kz, K4 = (K + 3) & ~3;
     const int tid = threadIdx.x;
-    for (int e = tid; e < K * PB_CW; e += PB_NT) {  // fold: u[p][j][c]
-        const int j = e / PB_CW, c = e % PB_CW;
-        const float x0 = xs[j * PB_CW + c];
-        if (2 * j == L) {
-            u[j * PB_CW + c] = x0;
-            u[(K + j) * PB_CW + c] = 0.f;
-        } else {
-            const float x1 = xs[(L - j) * PB_CW + c];
-            u[j * PB_CW + c] = x0 + x1;
-            u[(K + j) * PB_CW + c] = x0 - x1;
+    for (int e = tid; e < K4 * PB_CW; e += PB_NT) {  // fold: u[p][c][j]
+        const int c = e / K4, j = e % K4;
+        float u0 = 0.f, u1 = 0.f;
+        if (j < K) {
+            const float x0 = xs[j * PB_CW + c];
+            if (2 * j == L) {
+                u0 = x0;
+            } else {
+                const float x1 = xs[(L - j) * PB_CW + c];
+                u0 = x0 + x1;
+                u1 = x0 - x1;
+            }
         }
+        u[c * K4 + j] = u0;
+        u[(PB_CW + c) * K4 + j] = u1;
     }
     __syncthreads();
     for (int e = tid; e < nz * PB_CW; e += PB_NT) {
         const int row = e / PB_CW, c = e % PB_CW, par = row & 1, m = row >> 1;
-        const float* A = (par ? a.fzo : a.fze) + (long)m * K;
-        const float* up = u + (par ? K : 0) * PB_CW + c;
+        const float* up = u + (par * PB_CW + c) * K4;
         float acc0 = 0.f, acc1 = 0.f;
-        int j = 0;
+        if (zA) {
+            const float4* A4 = reinterpret_cast<const float4*>(zA + ((long)par * a.Mze + m) * K4);
+            const float4* U4 = reinterpret_cast<const float4*>(up);
 #pragma unroll 4
-        for (; j + 1 < K; j += 2) {
-            acc0 = fmaf(__ldg(A + j), up[j * PB_CW], acc0);
-            acc1 = fmaf(__ldg(A + j + 1), up[(j + 1) * PB_CW], acc1);
+            for (int j4 = 0; j4 < K4 / 4; ++j4) {
+                const float4 av = A4[j4], uv = U4[j4];
+                acc0 = fmaf(av.x, uv.x, acc0);
+                acc1 = fmaf(av.y, uv.y, acc1);
+                acc0 = fmaf(av.z, uv.z, acc0);
+                acc1 = fmaf(av.w, uv.w, acc1);
+            }
+        } else {
+            const float* A = (par ? a.fzo : a.fze) + (long)m * K;
+            int j = 0;
+#pragma unroll 4
+            for (; j + 1 < K; j += 2) {
+                acc0 = fmaf(__ldg(A + j), up[j], acc0);
+                acc1 = fmaf(__ldg(A + j + 1), up[j + 1], acc1);
+            }
+            if (j < K) acc0 = fmaf(__ldg(A + j), up[j], acc0);
         }
-        if (j < K) acc0 = fmaf(__ldg(A + j), up[j * PB_CW], acc0);
         ys[row * PB_CW + c] = acc0 + acc1;
     }
     __syncthreads();
 }
 
-// z pass, divide by Ph_Lcc, z pass (columns are independent along z): out = Cz ((Cz X) / L).
-__device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* smem) {
+// Column pass along z (columns are independent along z): what = 0: out = Cz ((Cz X) / L);
+// 1: out = (Cz X) / L; 2: out = Cz X.
+__device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* smem, int what = 0) {
     const int nz = a.nz, nr = a.nr, K = a.Kz;
-    float* xs = smem;                 // [nz][CW]
-    float* u = xs + nz * PB_CW;       // [2][K][CW]
-    float* ys = u + 2 * K * PB_CW;    // [nz][CW]
+    float* xs = smem + a.work_off;    // [nz][CW]
+    float* u = xs + nz * PB_CW;       // [2][CW][Kz4]
+    float* ys = u + 2 * PB_CW * ((K + 3) & ~3);  // [nz][CW]
+    const float* zA = a.z_res ? smem + a.z_off : nullptr;
     const int nchunks = (nr + PB_CW - 1) / PB_CW;
     for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
         const int c0 = ch * PB_CW;
@@ -1892,27 +2015,40 @@ __device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* 
             xs[e] = col < nr ? __ldcg(X + (long)row * nr + col) : 0.f;
         }
         __syncthreads();
-        pb_zcols(a, xs, u, ys);
-        for (int e = threadIdx.x; e < nz * PB_CW; e += PB_NT) {
-            const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
-            xs[e] = col < nr ? ys[e] / __ldg(a.lcc + (long)row * nr + col) : 0.f;
+        pb_zcols(a, xs, u, ys, zA);
+        if (what != 2) {
+            for (int e = threadIdx.x; e < nz * PB_CW; e += PB_NT) {
+                const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
+                xs[e] = col < nr ? ys[e] / __ldg(a.lcc + (long)row * nr + col) : 0.f;
+            }
+            __syncthreads();
+            if (what == 0) pb_zcols(a, xs, u, ys, zA);
         }
-        __syncthreads();
-        pb_zcols(a, xs, u, ys);
+        const float* res = what == 1 ? xs : ys;
         for (int e = threadIdx.x; e < nz * PB_CW; e += PB_NT) {
             const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
-            if (col < nr) out[(long)row * nr + col] = ys[e];
+            if (col < nr) out[(long)row * nr + col] = res[e];
         }
     }
 }
 
 // psolve: y = DCT-I preconditioner applied to x (three phases, two internal barriers).
 __device__ bool pb_psolve(const PersistArgs& a, const float* x, float* y, float* smem, unsigned& gen, PbProf& pf) {
-    pb_xpass(a, x, a.w1, smem);
+    if (a.zorder == 1) {  // x, z / L, x, z: the order of the kernel-per-phase path
+        pb_xpass(a, x, a.w1, smem, pf);
+        if (!grid_sync(a.bar, gen, pf)) return false;
+        pb_zdz(a, a.w1, a.w2, smem, 1);
+        if (!grid_sync(a.bar, gen, pf)) return false;
+        pb_xpass(a, a.w2, a.w1, smem, pf);
+        if (!grid_sync(a.bar, gen, pf)) return false;
+        pb_zdz(a, a.w1, y, smem, 2);
+        return true;
+    }
+    pb_xpass(a, x, a.w1, smem, pf);
     if (!grid_sync(a.bar, gen, pf)) return false;
     pb_zdz(a, a.w1, a.w2, smem);
     if (!grid_sync(a.bar, gen, pf)) return false;
-    pb_xpass(a, a.w2, y, smem);
+    pb_xpass(a, a.w2, y, smem, pf);
     return true;
 }
 
@@ -1981,71 +2117,34 @@ __device__ __forceinline__ float pb_pre(const PersistArgs& a, long q, float v) {
     return a.ident ? v : v / __ldg(a.diag + q);
 }
 
-}  // namespace
+// State of one inner BiCGSTAB run (the local scalars of BICGSTABREVCOM).
+struct PbInner {
+    int info, iter;
+    unsigned flags;
+    double resid, rho, rho1, alpha, omega, beta, snorm;
+};
 
+// The iterations (lib/BiCGSTABREVCOM.f:257-388) from R, RTLD and the first RHO = (rtld, r);
+// X is updated in place.  Every block runs the same scalar steps; returns false when a barrier
+// timed out.
 template <int KIND>
-__global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
-    extern __shared__ float smem[];
-    __shared__ double sm[32];
-    count_launch(a.ctr);
-    unsigned gen = 0u;  // arrivals counted so far (the counter is zeroed before the launch)
-    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+__device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int maxit, double rho_first, PbInner& st,
+                           float* smem, double* sm, unsigned& gen, PbProf& pf) {
     const long n = a.n;
     const long stride = (long)gridDim.x * PB_NT;
     const long q0 = blockIdx.x * (long)PB_NT + threadIdx.x;
-    KState* ks = a.ks;
-    PbProf pf{nullptr, 0};
-    // the parent (FP64 refinement) state decides whether this inner solve runs at all
-    if (a.parent && *((volatile const int*)&a.parent->phase) != PH_RUNNING) {
-        if (lead) { ks->phase = PH_DONE; ks->iter = 0; ks->info = 0; }
-        return;
-    }
-    // ---- setup (:229-255): r = b, ||x||, ||b||, x0 test, rtld = r, first rho partials
-    double xx = 0.0, bb = 0.0;
-    for (long q = q0; q < n; q += stride) {
-        const float bv = __ldcg(a.b + q), xv = __ldcg(a.x + q);
-        a.r[q] = bv;
-        xx += (double)xv * (double)xv;
-        bb += (double)bv * (double)bv;
-    }
-    slot_put<PB_NT>(a.part, 0, xx, sm);
-    slot_put<PB_NT>(a.part, 3, bb, sm);
-    bool ok = grid_sync(a.bar, gen, pf);
-    const double xnorm = sqrt(slot_sum<PB_NT>(a.part, 0, sm));
-    const double bnorm_raw = sqrt(slot_sum<PB_NT>(a.part, 3, sm));
-    const double bnrm2 = bnorm_raw == 0.0 ? 1.0 : bnorm_raw;
-    const double tol = a.tol;
-    const int maxit = a.maxit;
-    int info = 0, iter = maxit, phase = maxit <= 0 ? PH_DONE : PH_RUNNING;
-    unsigned flags = 0u;
-    double resid = tol, rho = 0.0, rho1 = 0.0, alpha = 0.0, omega = 0.0, beta = 0.0, snorm = 0.0;
-    if (maxit <= 0) info = -3;
-    if (ok && phase == PH_RUNNING && xnorm != 0.0) {  // r = b - A x0 and the absolute x0 test (:248)
-        ok = pb_matvec<KIND>(a, a.x, a.r, -1.f, a.r, nullptr, 0, true, 0, sm, gen, pf) && grid_sync(a.bar, gen, pf);
-        const double rr = sqrt(slot_sum<PB_NT>(a.part, 0, sm));
-        if (rr <= tol) { phase = PH_DONE; info = 0; flags |= DRD_FLAG_EARLY_X0; }
-    }
-    if (phase == PH_RUNNING) iter = 0;
-    if (ok && phase == PH_RUNNING) {
-        double a1 = 0.0;
-        for (long q = q0; q < n; q += stride) {
-            const float rv = __ldcg(a.r + q);
-            a.rtld[q] = rv;
-            a1 += (double)rv * (double)rv;
-        }
-        slot_put<PB_NT>(a.part, 1, a1, sm);
-        ok = grid_sync(a.bar, gen, pf);
-    }
-    bool first = true;
-    // ---- iterations (:257-388)
-    while (ok && phase == PH_RUNNING) {
-        rho = slot_sum<PB_NT>(a.part, 1, sm);  // RHO = (rtld, r)
-        iter += 1;
-        pf.p = (a.prof != nullptr && iter == 3) ? a.prof : nullptr;  // time the third iteration
-        if (fabs(rho) < kBreakTol) { info = -10; phase = PH_DONE; break; }
-        beta = first ? 0.0 : (rho / rho1) * (alpha / omega);
+    bool ok = true, first = true;
+    int phase = PH_RUNNING;
+    double rho_next = rho_first;
+    st.iter = 0;
+    while (phase == PH_RUNNING) {
+        st.rho = rho_next;  // RHO = (rtld, r), summed with the previous STOPTEST norm
+        st.iter += 1;
+        pf.p = (a.prof != nullptr && st.iter == 3 && pf.k == 0) ? a.prof : nullptr;  // time iteration 3 once
+        if (fabs(st.rho) < kBreakTol) { st.info = -10; break; }
+        st.beta = first ? 0.0 : (st.rho / st.rho1) * (st.alpha / st.omega);
         {
-            const float bt = (float)beta, nom = (float)(-omega);
+            const float bt = (float)st.beta, nom = (float)(-st.omega);
             for (long q = q0; q < n; q += stride) {
                 float pv;
                 if (first) pv = __ldcg(a.r + q);
@@ -2067,9 +2166,9 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
         if (!(ok = pb_matvec<KIND>(a, a.phat, a.v, 1.f, nullptr, a.rtld, 4, false, 0, sm, gen, pf))) break;  // V = A PHAT
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
         const double rv = slot_sum<PB_NT>(a.part, 4, sm);
-        alpha = rho / rv;  // (:307)
+        st.alpha = st.rho / rv;  // (:307)
         {
-            const float na = (float)(-alpha);
+            const float na = (float)(-st.alpha);
             double s2 = 0.0;
             for (long q = q0; q < n; q += stride) {
                 const float sv = __ldcg(a.r + q) + na * __ldcg(a.v + q);
@@ -2080,14 +2179,13 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
             slot_put<PB_NT>(a.part, 5, s2, sm);
         }
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
-        snorm = sqrt(slot_sum<PB_NT>(a.part, 5, sm));
-        if (snorm <= tol) {  // early absolute test (:313-316): X = X + ALPHA PHAT
-            resid = snorm / bnrm2;
-            info = 0;
-            flags |= DRD_FLAG_EARLY_S;
-            const float al = (float)alpha;
+        st.snorm = sqrt(slot_sum<PB_NT>(a.part, 5, sm));
+        if (st.snorm <= tol) {  // early absolute test (:313-316): X = X + ALPHA PHAT
+            st.resid = st.snorm / bnrm2;
+            st.info = 0;
+            st.flags |= DRD_FLAG_EARLY_S;
+            const float al = (float)st.alpha;
             for (long q = q0; q < n; q += stride) a.x[q] = __ldcg(a.x + q) + al * __ldcg(a.phat + q);
-            phase = PH_DONE;
             break;
         }
         if constexpr (KIND == PK_CH) {
@@ -2096,32 +2194,233 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
         }
         if (!(ok = pb_matvec<KIND>(a, a.shat, a.t, 1.f, nullptr, a.r, 6, true, 7, sm, gen, pf))) break;  // T = A SHAT
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
-        const double ts = slot_sum<PB_NT>(a.part, 6, sm), tt = slot_sum<PB_NT>(a.part, 7, sm);
-        omega = ts / tt;  // (:349-350)
+        const double2 tst = slot_sum2<PB_NT>(a.part, 6, 7, sm);
+        st.omega = tst.x / tst.y;  // (:349-350)
         {
-            const float al = (float)alpha, om = (float)omega, nom = (float)(-omega);
+            const float al = (float)st.alpha, om = (float)st.omega, nom = (float)(-st.omega);
             double r2 = 0.0, rr = 0.0;
             for (long q = q0; q < n; q += stride) {
-                float xv = __ldcg(a.x + q) + al * __ldcg(a.phat + q);
-                xv = xv + om * __ldcg(a.shat + q);
+                // all six loads before either store (the vectors may alias as far as the
+                // compiler knows), so an element costs one L2 round trip
+                const float x0 = __ldcg(a.x + q), ph = __ldcg(a.phat + q), sh = __ldcg(a.shat + q);
+                const float s0 = __ldcg(a.r + q), t0 = __ldcg(a.t + q), rt = __ldcg(a.rtld + q);
+                float xv = x0 + al * ph;
+                xv = xv + om * sh;
+                const float rvq = s0 + nom * t0;
                 a.x[q] = xv;
-                const float rvq = __ldcg(a.r + q) + nom * __ldcg(a.t + q);
                 a.r[q] = rvq;
                 r2 += (double)rvq * (double)rvq;
-                rr += (double)__ldcg(a.rtld + q) * (double)rvq;
+                rr += (double)rt * (double)rvq;
             }
             slot_put<PB_NT>(a.part, 0, r2, sm);
             slot_put<PB_NT>(a.part, 1, rr, sm);
         }
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
-        resid = sqrt(slot_sum<PB_NT>(a.part, 0, sm)) / bnrm2;  // STOPTEST2 (:361-362)
-        if (!isfinite(resid)) { info = DRD_ERR_NONFINITE; phase = PH_DONE; }
-        else if (resid <= tol) { info = 0; phase = PH_DONE; }
-        else if (iter >= maxit) { info = 1; phase = PH_DONE; }
-        else if (fabs(omega) < kBreakTol) { info = (fabs(rho) < kBreakTol) ? -10 : -11; phase = PH_DONE; }
-        else rho1 = rho;
+        const double2 rr01 = slot_sum2<PB_NT>(a.part, 0, 1, sm);
+        st.resid = sqrt(rr01.x) / bnrm2;  // STOPTEST2 (:361-362)
+        rho_next = rr01.y;
+        if (!isfinite(st.resid)) { st.info = DRD_ERR_NONFINITE; phase = PH_DONE; }
+        else if (st.resid <= tol) { st.info = 0; phase = PH_DONE; }
+        else if (st.iter >= maxit) { st.info = 1; phase = PH_DONE; }
+        else if (fabs(st.omega) < kBreakTol) {
+            st.info = (fabs(st.rho) < kBreakTol) ? -10 : -11;
+            phase = PH_DONE;
+        } else st.rho1 = st.rho;
     }
-    if (!ok) info = DRD_ERR_TIMEOUT;
+    pf.p = nullptr;
+    return ok;
+}
+
+// FP64 residual of the refinement: r64 = b64 - A64 x64 (the reference-form FP64 operators),
+// partials ||r64||^2 into slot 8 and, when `with_b`, ||b64||^2 into slot 9.
+template <int KIND>
+__device__ bool pb_residual64(const PersistArgs& a, bool with_b, double* sm, unsigned& gen, PbProf& pf) {
+    const int nr = a.nr, nz = a.nz;
+    const long n = a.n;
+    const long stride = (long)gridDim.x * PB_NT;
+    double r2 = 0.0, b2 = 0.0;
+    if constexpr (KIND == PK_CH) {
+        PackedCG<double> X{a.x64, nr};
+        CellA<double> M0{a.M0d, nr}, Mi{a.Mid, nr};
+        for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < n; q += stride) {
+            const int i = (int)(q % nr), k = (int)(q / nr);
+            a.f64[q] = -(a.od.dtxld * op_dgn<double>(i, k, nr, nz, a.od.idr2, a.od.idz2, X, M0));
+        }
+        if (!grid_sync(a.bar, gen, pf)) return false;
+        PackedCG<double> Fv{a.f64, nr};
+        for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < n; q += stride) {
+            const int i = (int)(q % nr), k = (int)(q / nr);
+            const double f = __ldcg(a.f64 + q), bq = __ldcg(a.b64 + q);
+            const double av = __ldcg(a.x64 + q) + (a.od.s * f / a.od.eps -
+                                                   a.od.eps * op_dgn<double>(i, k, nr, nz, a.od.idr2, a.od.idz2, Fv, Mi));
+            const double rq = -1.0 * av + 1.0 * bq;
+            a.r64[q] = rq;
+            r2 += rq * rq;
+            b2 += bq * bq;
+        }
+    } else {
+        const long mn = (long)(nr + 1) * nz;
+        UVFetch<double, true> F{a.x64, nr, nz, mn, a.od.lr_neumann};
+        for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < n; q += stride) {
+            const double bq = __ldcg(a.b64 + q);
+            const double av = uv_apply<double>(a.od, a.rhod, a.etad, a.pend, F, q);
+            const double rq = -1.0 * av + 1.0 * bq;
+            a.r64[q] = rq;
+            r2 += rq * rq;
+            b2 += bq * bq;
+        }
+    }
+    slot_put<PB_NT>(a.part, 8, r2, sm);
+    if (with_b) slot_put<PB_NT>(a.part, 9, b2, sm);
+    return true;
+}
+
+}  // namespace
+
+template <int KIND>
+__global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ double sm[32];
+    count_launch(a.ctr);
+    unsigned gen = 0u;  // arrivals counted so far (the counter is zeroed before the launch)
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    const long n = a.n;
+    const long stride = (long)gridDim.x * PB_NT;
+    const long q0 = blockIdx.x * (long)PB_NT + threadIdx.x;
+    KState* ks = a.ks;
+    PbProf pf{nullptr, 0};
+    // the parent (FP64 refinement) state decides whether this inner solve runs at all
+    if (a.parent && *((volatile const int*)&a.parent->phase) != PH_RUNNING) {
+        if (lead) { ks->phase = PH_DONE; ks->iter = 0; ks->info = 0; }
+        return;
+    }
+    if constexpr (KIND == PK_CH) pb_load_resident(a, smem);
+    if (a.mode == PM_PSOLVE || a.mode == PM_MATVEC) {  // one application x = op(b), the solver's code
+        bool done = true;
+        if (a.mode == PM_PSOLVE) {
+            if constexpr (KIND == PK_CH) done = pb_psolve(a, a.b, a.x, smem, gen, pf);
+            else
+                for (long q = q0; q < n; q += stride) a.x[q] = pb_pre(a, q, __ldcg(a.b + q));
+        } else {
+            done = pb_matvec<KIND>(a, a.b, a.x, 1.f, nullptr, nullptr, 0, false, 0, sm, gen, pf);
+        }
+        if (lead) ks->info = done ? 0 : DRD_ERR_TIMEOUT;
+        return;
+    }
+    if (a.mode == PM_REFINE) {
+        // ---- the whole mixed solve: FP64 iterative refinement around the FP32 iterations.
+        // Each sweep: r64 = b64 - A64 x64 and its tests, b32 = r64/||r64||, an inner solve of
+        // A d = b32 from d = 0 to the inner tolerance, x64 += ||r64|| d.
+        const double otol = a.outer_tol;
+        int outer = 0, inner_total = 0, oinfo = 0;
+        double bnorm64 = 0.0, bnrm64 = 1.0, rnorm = 0.0, oresid = 0.0, prev = 0.0;
+        bool ok = true, run = true;
+        PbInner in{};
+        while (run) {
+            if (!(ok = pb_residual64<KIND>(a, outer == 0, sm, gen, pf) && grid_sync(a.bar, gen, pf))) break;
+            const double2 rb = slot_sum2<PB_NT>(a.part, 8, 9, sm);
+            rnorm = sqrt(rb.x);
+            if (outer == 0) {  // k_mx_init
+                bnorm64 = sqrt(rb.y);
+                bnrm64 = bnorm64 == 0.0 ? 1.0 : bnorm64;
+                oresid = rnorm / bnrm64;
+                if (!isfinite(oresid)) { oinfo = DRD_ERR_NONFINITE; break; }
+                if (oresid <= otol || rnorm == 0.0) break;
+            } else {  // k_mx_check
+                prev = oresid;
+                oresid = rnorm / bnrm64;
+                inner_total += in.iter;
+                if (in.info == DRD_ERR_TIMEOUT) { oinfo = DRD_ERR_TIMEOUT; break; }
+                if (!isfinite(oresid)) { oinfo = DRD_ERR_NONFINITE; break; }
+                if (oresid <= otol) { oinfo = 0; break; }
+                if (outer >= a.max_refine) { oinfo = 1; break; }
+                if (oresid > 0.9 * prev) { oinfo = 1; break; }  // stalled refinement
+            }
+            // scale and inner setup in one pass: b32 = r = rtld = r64 / ||r64||, x32 = 0
+            {
+                const double sc = 1.0 / rnorm;
+                double bb = 0.0;
+                for (long q = q0; q < n; q += stride) {
+                    const float bv = (float)(__ldcg(a.r64 + q) * sc);
+                    a.b[q] = bv;
+                    a.r[q] = bv;
+                    a.rtld[q] = bv;
+                    a.x[q] = 0.f;
+                    bb += (double)bv * (double)bv;
+                }
+                slot_put<PB_NT>(a.part, 3, bb, sm);
+            }
+            if (!(ok = grid_sync(a.bar, gen, pf))) break;
+            const double bb = slot_sum<PB_NT>(a.part, 3, sm);
+            const double bn = sqrt(bb);
+            in = PbInner{};
+            if (a.maxit <= 0) { in.info = -3; in.iter = a.maxit; }
+            else if (!(ok = pb_iterate<KIND>(a, bn == 0.0 ? 1.0 : bn, a.tol, a.maxit, bb, in, smem, sm, gen, pf)))
+                break;
+            // x64 += ||r64|| d32
+            for (long q = q0; q < n; q += stride) a.x64[q] = __ldcg(a.x64 + q) + rnorm * (double)__ldcg(a.x + q);
+            outer += 1;
+            if (!(ok = grid_sync(a.bar, gen, pf))) break;
+        }
+        if (!ok) oinfo = DRD_ERR_TIMEOUT;
+        if (lead) {
+            ks->tol = otol;
+            ks->maxit = a.max_refine;
+            ks->bnorm_raw = bnorm64;
+            ks->bnrm2 = bnrm64;
+            ks->snorm = rnorm;
+            ks->resid = oresid;
+            ks->true_resid = oresid;  // the residual of the returned x64, recomputed in FP64
+            ks->outer = outer;
+            ks->inner_total = inner_total;
+            ks->iter = inner_total;
+            ks->info = oinfo;
+            ks->flags = DRD_FLAG_REFINED;
+            ks->mixed = 1;
+            ks->phase = PH_DONE;
+        }
+        return;
+    }
+    // ---- one inner solve (:229-255 setup, then the iterations)
+    double xx = 0.0, bb = 0.0;
+    for (long q = q0; q < n; q += stride) {
+        const float bv = __ldcg(a.b + q), xv = __ldcg(a.x + q);
+        a.r[q] = bv;
+        xx += (double)xv * (double)xv;
+        bb += (double)bv * (double)bv;
+    }
+    slot_put<PB_NT>(a.part, 0, xx, sm);
+    slot_put<PB_NT>(a.part, 3, bb, sm);
+    bool ok = grid_sync(a.bar, gen, pf);
+    const double2 xb = slot_sum2<PB_NT>(a.part, 0, 3, sm);
+    const double xnorm = sqrt(xb.x);
+    const double bnorm_raw = sqrt(xb.y);
+    const double bnrm2 = bnorm_raw == 0.0 ? 1.0 : bnorm_raw;
+    const double tol = a.tol;
+    const int maxit = a.maxit;
+    PbInner st{};
+    st.resid = tol;
+    st.iter = maxit;
+    bool run = maxit > 0;
+    if (maxit <= 0) st.info = -3;
+    if (ok && run && xnorm != 0.0) {  // r = b - A x0 and the absolute x0 test (:248)
+        ok = pb_matvec<KIND>(a, a.x, a.r, -1.f, a.r, nullptr, 0, true, 0, sm, gen, pf) && grid_sync(a.bar, gen, pf);
+        const double rr = sqrt(slot_sum<PB_NT>(a.part, 0, sm));
+        if (rr <= tol) { run = false; st.info = 0; st.flags |= DRD_FLAG_EARLY_X0; }
+    }
+    if (ok && run) {
+        double a1 = 0.0;
+        for (long q = q0; q < n; q += stride) {
+            const float rv = __ldcg(a.r + q);
+            a.rtld[q] = rv;
+            a1 += (double)rv * (double)rv;
+        }
+        slot_put<PB_NT>(a.part, 1, a1, sm);
+        ok = grid_sync(a.bar, gen, pf);
+        const double rho_first = slot_sum<PB_NT>(a.part, 1, sm);
+        if (ok) ok = pb_iterate<KIND>(a, bnrm2, tol, maxit, rho_first, st, smem, sm, gen, pf);
+    }
+    if (!ok) st.info = DRD_ERR_TIMEOUT;
     if (lead) {
         ks->tol = tol;
         ks->maxit = maxit;
@@ -2129,16 +2428,16 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
         ks->x_nonzero = xnorm != 0.0;
         ks->bnorm_raw = bnorm_raw;
         ks->bnrm2 = bnrm2;
-        ks->iter = iter;
-        ks->info = info;
-        ks->resid = resid;
-        ks->snorm = snorm;
-        ks->rho = rho;
-        ks->rho1 = rho1;
-        ks->alpha = alpha;
-        ks->omega = omega;
-        ks->beta = beta;
-        ks->flags = flags;
+        ks->iter = st.iter;
+        ks->info = st.info;
+        ks->resid = st.resid;
+        ks->snorm = st.snorm;
+        ks->rho = st.rho;
+        ks->rho1 = st.rho1;
+        ks->alpha = st.alpha;
+        ks->omega = st.omega;
+        ks->beta = st.beta;
+        ks->flags = st.flags;
         ks->mixed = 0;
         ks->phase = PH_DONE;
     }
@@ -2157,19 +2456,42 @@ __global__ void k_bar_reset(GridBar* b, ull* ctr) {
     }
 }
 void launch_bar_reset(GridBar* b, ull* ctr, cudaStream_t s) { k_bar_reset<<<1, 32, 0, s>>>(b, ctr); }
-size_t persist_ch_smem(int nr, int nz) {
-    const size_t xp = sizeof(float) * ((size_t)PB_BM * (PB_KC + 1) + (size_t)PB_KC * PB_BN);
-    const int Kz = (nz - 1) / 2 + 1;
-    const size_t zp = sizeof(float) * ((size_t)nz * PB_CW * 2 + (size_t)2 * Kz * PB_CW);
-    (void)nr;
-    return xp > zp ? xp : zp;
+// Shared-memory plan (offsets in floats) of the persistent CH solver for an nr x nz grid run by
+// `grid` blocks within `budget` bytes: a work area (x-pass panels or z-pass columns), then the
+// resident z-pass operands and the block's x-pass B panel where they fit.
+PbPlan persist_ch_plan(int nr, int nz, int grid, size_t budget) {
+    PbPlan p{};
+    const int Kx = (nr - 1) / 2 + 1, Nxe = (nr + 1) / 2, Nxo = nr / 2;
+    const int Kz = (nz - 1) / 2 + 1, Mze = (nz + 1) / 2;
+    const size_t xwork = (size_t)PB_KC * PB_BM + (size_t)PB_KC * PB_BN + (size_t)PB_KG * PB_BM * PB_BN;
+    const int Kz4 = (Kz + 3) & ~3;
+    const size_t zwork = (size_t)nz * PB_CW * 2 + (size_t)2 * Kz4 * PB_CW;
+    auto up4 = [](size_t v) { return (v + 3) & ~(size_t)3; };  // float4-aligned offsets
+    size_t used = up4(xwork > zwork ? xwork : zwork);
+    p.work_off = 0;
+    const size_t zres = (size_t)2 * Mze * Kz4;
+    if ((used + zres) * sizeof(float) <= budget) {
+        p.z_res = 1;
+        p.z_off = (long)used;
+        used = up4(used + zres);
+    }
+    const int mt = (nz + PB_BM - 1) / PB_BM;
+    const int ntiles = mt * ((Nxe + PB_BN - 1) / PB_BN + (Nxo + PB_BN - 1) / PB_BN);
+    const size_t bres = (size_t)Kx * PB_BN;
+    if (ntiles <= grid && (used + bres) * sizeof(float) <= budget) {
+        p.b_res = 1;
+        p.b_off = (long)used;
+        used += bres;
+    }
+    p.bytes = used * sizeof(float);
+    return p;
 }
 int persist_threads() { return PB_NT; }
 const void* persist_kernel(int kind) {
     return kind == PK_CH ? (const void*)k_bicg_persist<PK_CH> : (const void*)k_bicg_persist<PK_UV>;
 }
 cudaError_t launch_bicg_persist(const PersistArgs& a, int grid, cudaStream_t s) {
-    const size_t smem = a.kind == PK_CH ? persist_ch_smem(a.nr, a.nz) : 0;
+    const size_t smem = a.kind == PK_CH ? a.smem_bytes : 0;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(PB_NT);

@@ -121,8 +121,11 @@ struct GridBar {
     int err, pad;
 };
 enum PersistKind : int { PK_CH = 0, PK_UV = 1 };
+enum PersistMode : int { PM_SOLVE = 0, PM_PSOLVE = 1, PM_MATVEC = 2, PM_REFINE = 3 };
 struct PersistArgs {
     int kind;                             // PK_CH or PK_UV
+    int mode;                             // PM_SOLVE, or one application x = op(b)
+    int zorder;                           // CH transform order: 0 x,z/z,x (3 phases); 1 x,z/,x,z
     int nr, nz;
     long n;                               // unknowns
     OpScal<float> o;
@@ -134,6 +137,14 @@ struct PersistArgs {
     const float *rho, *eta, *pen, *diag;
     int ident;
     float *x, *b, *r, *rtld, *p, *v, *phat, *shat, *t, *ff1, *w1, *w2;
+    // PM_REFINE: the FP64 system (b64, x64 in place), its residual and stencil scratch, the
+    // FP64 operators' scalars and coefficients, the refinement tolerance and sweep limit
+    const double* b64;
+    double *x64, *r64, *f64;
+    OpScal<double> od;
+    const double *M0d, *Mid, *rhod, *etad, *pend;
+    double outer_tol;
+    int max_refine;
     double* part;
     KState* ks;
     const KState* parent;
@@ -142,8 +153,17 @@ struct PersistArgs {
     int maxit;
     ull* ctr;
     unsigned long long* prof;  // optional: barrier entry/exit times (ns) of block 0 in iteration 3
+    // CH shared-memory plan (floats): work area, resident z operands, resident x-pass B panel
+    long work_off, z_off, b_off;
+    int z_res, b_res;
+    size_t smem_bytes;
 };
-size_t persist_ch_smem(int nr, int nz);
+struct PbPlan {
+    long work_off, z_off, b_off;
+    int z_res, b_res;
+    size_t bytes;
+};
+PbPlan persist_ch_plan(int nr, int nz, int grid, size_t budget);
 int persist_threads();
 const void* persist_kernel(int kind);
 cudaError_t launch_bicg_persist(const PersistArgs& a, int grid, cudaStream_t s);

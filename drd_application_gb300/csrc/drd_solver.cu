@@ -75,6 +75,7 @@ struct drd_ctx {
     double ori_alpha = 0.0;
     // persistent cooperative inner solver (FP32 CH): grid size, barrier state, on/off
     int persist = 0, pgrid = 0;
+    PbPlan pplan{};
     GridBar* bar = nullptr;
     std::string persist_err;
     unsigned long long* pprof = nullptr;  // DRD_PERSIST_PROF=1: barrier timestamps of block 0
@@ -517,15 +518,19 @@ int setup_persist(drd_ctx* c) {
     CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
     if (!coop || sms < 1) { c->persist_err = "no cooperative launch on this device"; return DRD_OK; }
-    const size_t smem = persist_ch_smem(c->nr, c->nz);
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    const int grid = std::min(sms, DRD_MAXB);
+    c->pplan = persist_ch_plan(c->nr, c->nz, grid, (size_t)std::max(0, optin - 4096));
     for (int kind = PK_CH; kind <= PK_UV; ++kind) {
-        const size_t sm = kind == PK_CH ? smem : 0;
+        const size_t sm = kind == PK_CH ? c->pplan.bytes : 0;
+        if (sm > (size_t)optin) { c->persist_err = "persistent solver needs more shared memory"; return DRD_OK; }
         int occ = 0;
         CK(cudaFuncSetAttribute(persist_kernel(kind), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persist_kernel(kind), persist_threads(), sm));
         if (occ < 1) { c->persist_err = "persistent solver does not fit one block per SM"; return DRD_OK; }
     }
-    c->pgrid = std::min(sms, DRD_MAXB);
+    c->pgrid = grid;
     c->persist = 1;
     const char* pe = std::getenv("DRD_PERSIST_PROF");
     c->pprof_on = pe && std::atoi(pe) != 0;
@@ -547,6 +552,10 @@ PersistArgs persist_args(drd_ctx* c, const Sys& S, KState* in, const KState* par
     a.t = f.t; a.ff1 = f.ff1; a.w1 = c->t1f; a.w2 = c->t2f;
     a.part = c->part; a.ks = in; a.parent = parent; a.bar = c->bar; a.tol = tol; a.maxit = maxit; a.ctr = c->ctr;
     a.prof = c->pprof_on ? c->pprof : nullptr;
+    const char* zo = std::getenv("DRD_PERSIST_ORDER");
+    a.zorder = (zo && std::atoi(zo) == 1) ? 1 : 0;
+    a.work_off = c->pplan.work_off; a.z_off = c->pplan.z_off; a.b_off = c->pplan.b_off;
+    a.z_res = c->pplan.z_res; a.b_res = c->pplan.b_res; a.smem_bytes = c->pplan.bytes;
     return a;
 }
 
@@ -565,6 +574,28 @@ int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int 
             enq_bicg_iter<double>(c, S, k, ks, h, 1, sb);
         });
         if (rc) return rc;
+    } else if (c->persist && (S.kind == SYS_CH || S.kind == SYS_UV)) {
+        // the whole mixed solve (FP64 refinement and its FP32 inner solves) in one cooperative
+        // launch; it leaves the FP64 true residual of the returned x in the state
+        enq_sys_setup<float>(c, S, s);
+        launch_bar_reset(c->bar, c->ctr, s);
+        PersistArgs a = persist_args(c, S, ks, nullptr, c->P.mixed_inner_tol, maxit);
+        a.mode = PM_REFINE;
+        a.b64 = k.b;
+        a.x64 = k.x;
+        a.r64 = k.r;
+        a.f64 = k.ff1;
+        a.od = make_op<double>(c, S.kind == SYS_UV ? S.bdf : 0);
+        a.M0d = coef<double>(c, 3); a.Mid = coef<double>(c, 4);
+        a.rhod = coef<double>(c, 0); a.etad = coef<double>(c, 1); a.pend = coef<double>(c, 2);
+        a.outer_tol = tol;
+        a.max_refine = c->P.mixed_max_refine;
+        cudaError_t e = launch_bicg_persist(a, c->pgrid, s);
+        if (e != cudaSuccess) {
+            c->err = std::string("persistent solver launch: ") + cudaGetErrorString(e);
+            return DRD_ERR_CUDA;
+        }
+        return DRD_OK;
     } else {
         // FP64 iterative refinement around an FP32 BiCGSTAB: each sweep solves A d = r / ||r||
         // from a zero guess to mixed_inner_tol, then x += ||r|| d and r = b - A x in FP64.
@@ -580,21 +611,11 @@ int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int 
         const double itol = c->P.mixed_inner_tol;
         rc = capture_while(c, s, c->s2, ks, [&](cudaStream_t sb, cudaGraphConditionalHandle ho) {
             launch_mx_scale<float>(S.n, k.r, ks, f.b, f.x, c->ctr, sb);
-            if (c->persist && (S.kind == SYS_CH || S.kind == SYS_UV)) {
-                // the whole inner solve in one cooperative launch (grid barriers between phases)
-                launch_bar_reset(c->bar, c->ctr, sb);
-                cudaError_t e = launch_bicg_persist(persist_args(c, S, in, ks, itol, maxit), c->pgrid, sb);
-                if (e != cudaSuccess) {
-                    c->err = std::string("persistent solver launch: ") + cudaGetErrorString(e);
-                    rc = DRD_ERR_CUDA;
-                }
-            } else {
-                enq_bicg_setup<float>(c, S, f, in, itol, maxit, ks, sb);
-                int rc2 = capture_while(c, sb, c->s3, in, [&](cudaStream_t si, cudaGraphConditionalHandle hi) {
-                    enq_bicg_iter<float>(c, S, f, in, hi, 1, si);
-                });
-                if (rc2) rc = rc2;
-            }
+            enq_bicg_setup<float>(c, S, f, in, itol, maxit, ks, sb);
+            int rc2 = capture_while(c, sb, c->s3, in, [&](cudaStream_t si, cudaGraphConditionalHandle hi) {
+                enq_bicg_iter<float>(c, S, f, in, hi, 1, si);
+            });
+            if (rc2) rc = rc2;
             launch_axpy_f2d(S.n, ks, f.x, k.x, c->ctr, sb);
             launch_copy<double>(S.n, k.b, k.r, c->ctr, sb);
             enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.r, nullptr, 1, -1, nullptr, G_ALWAYS, sb);
@@ -1584,7 +1605,18 @@ int drd_op_apply(drd_ctx* c, int op, int bdf, int precision, const double* x, do
     Sys S = sys_of(c, kind, bdf);
     KVecs<double>& k = c->k64;
     CK(cudaMemcpyAsync(k.tmp, x, sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
-    if (precision == DRD_PREC_FP64) {
+    if (precision == DRD_OP_PERSISTENT && (kind == SYS_CH || kind == SYS_UV)) {
+        // the persistent solver's own operator code: x = op(b) in one cooperative launch
+        if (!c->persist) { c->err = "persistent solver not in use: " + c->persist_err; return DRD_ERR_UNSUPPORTED; }
+        KVecs<float>& f = c->k32;
+        enq_sys_setup<float>(c, S, c->s);
+        launch_convert_scale<float, double>(n, k.tmp, 1.0, f.b, c->ctr, c->s);
+        PersistArgs a = persist_args(c, S, c->ks + KS_INNER, nullptr, 0.0, 0);
+        a.mode = mv ? PM_MATVEC : PM_PSOLVE;
+        launch_bar_reset(c->bar, c->ctr, c->s);
+        CK(launch_bicg_persist(a, c->pgrid, c->s));
+        launch_convert_scale<double, float>(n, f.x, 1.0, k.v, c->ctr, c->s);
+    } else if (precision == DRD_PREC_FP64) {
         enq_sys_setup<double>(c, S, c->s);
         if (mv) enq_matvec<double>(c, S, 1.0, k.tmp, 0.0, k.v, nullptr, 0, 0, nullptr, G_ALWAYS, c->s);
         else enq_psolve<double>(c, S, k.tmp, k.v, nullptr, G_ALWAYS, c->s);
@@ -1700,7 +1732,7 @@ int drd_flush_l2(drd_ctx* c, int64_t bytes) {
 
 int drd_persist_profile(drd_ctx* c, int64_t* ns, int n) {
     if (!c || !ns || n <= 0) return DRD_ERR_BADARG;
-    const int m = std::min(n, 124);
+    const int m = std::min(n, 128);
     std::vector<unsigned long long> h(m);
     CK(cudaStreamSynchronize(c->s));
     CK(cudaMemcpy(h.data(), c->pprof, sizeof(unsigned long long) * m, cudaMemcpyDeviceToHost));

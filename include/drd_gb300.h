@@ -381,6 +381,9 @@ int drd_presolve_2_noalloc(int nr, int nz, double dr, double dz, const double* u
 #define DRD_OP_UV_PSOLVE 3
 #define DRD_OP_PHMU_MATVEC 4
 #define DRD_OP_PHMU_PSOLVE 5
+/* `precision` DRD_OP_PERSISTENT evaluates the FP32 CH / momentum operators with the device code
+ * of the persistent inner solver (one cooperative launch), for checking it against the others. */
+#define DRD_OP_PERSISTENT 2
 int drd_op_apply(drd_ctx* ctx, int op, int bdf, int precision, const double* x, double* y);
 /* Length of the packed vector of operator `op`. */
 long drd_op_length(drd_ctx* ctx, int op);
