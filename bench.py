@@ -35,6 +35,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "time-steps/s and solves/s to FP64 resid 1e-8: learned+FP32 vs plain FP64, 1 GB300"
+# DRAM bytes (read + write) of one launch of the persistent CH solve kernel, from an ncu capture
+# of this workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch)
+TRAFFIC_CH = 4029184 + 477440
 WORKLOAD = ("420x180 serpentine channel (amp 30, period 140 cells, penalty 1e4), 3 rigid fibers 40x4, "
             "2 drops R=15, lambda_eta 5, Re 0.5, Ca 0.05; CH + momentum + pressure per step, tol 1e-8")
 
@@ -212,16 +215,18 @@ def time_resident(ctx, case, warmup, steps, flush_bytes):
         t += dt
     ctx.synchronize()
     launches0 = ctx.kernel_launches()
-    per, ch_it, uv_it, refine, resid, ok = [], [], [], [], [], 0
+    per, ch_it, uv_it, refine, resid, ok, ch_solve, ch_ref = [], [], [], [], [], 0, [], []
     for s in range(steps):
         ctx.flush_l2(flush_bytes)
         ctx.synchronize()
         st = ctx.step(False, t)
         t += dt
-        per.append(st.ch.seconds)
+        per.append(st.seconds)
+        ch_solve.append(st.ch.seconds)
         ch_it.append(st.ch.iter)
         uv_it.append(st.uv.iter)
         refine.append(st.ch.refinements + st.uv.refinements)
+        ch_ref.append(st.ch.refinements)
         resid.append(max(st.ch.true_resid, st.uv.true_resid))
         ok += int(st.ch.info == 0 and st.ch.true_resid <= case.params.tol * 1.0001) + \
             int(st.uv.info == 0 and st.uv.true_resid <= case.params.tol * 1.0001)
@@ -229,7 +234,7 @@ def time_resident(ctx, case, warmup, steps, flush_bytes):
     del abi
     return {"seconds": sum(per), "per_step_ms": [1e3 * x for x in per], "ch_iters": ch_it, "uv_iters": uv_it,
             "refinements": refine, "max_true_resid": max(resid), "solves_ok": ok, "solves": 2 * steps,
-            "launches": launches, "t_end": t}
+            "launches": launches, "t_end": t, "ch_solve_s": ch_solve, "ch_refinements": ch_ref}
 
 
 def time_e2e(ctx, case, warmup, steps, flush_bytes):
@@ -350,9 +355,21 @@ def run_gpu(args, ws, rank, local):
     except Exception:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    dom = abi.DRD_KB_DCT_X_FP32
-    us, by, fl = kb[dom]
-    achieved = by / (us * 1e-6) / 1e9
+    # dominant kernel: the persistent mixed CH solve (one cooperative launch per step), timed by
+    # the CUDA events the step records around it.  Algorithmic bytes of one launch: 29 N_c
+    # FP32 words per BiCGSTAB iteration (the minimum of a fully fused iteration: 23 vector
+    # passes, two mobility reads, one Ph_Lcc read) plus, per refinement sweep, the FP64
+    # residual (x, b, r and the two mobility fields) and the FP32 scale / FP64 update passes.
+    nc = args.nr * args.nz
+    cs = (args.nr + 2) * (args.nz + 2)
+    it_total = sum(mx["ch_iters"])
+    sweeps_total = sum(mx["ch_refinements"])
+    ch_sec = sum(mx["ch_solve_s"])
+    by_total = 29.0 * nc * 4 * it_total + sweeps_total * (8.0 * (4 * nc + 2 * cs) + 4.0 * 4 * nc + 20.0 * nc)
+    achieved = by_total / ch_sec / 1e9 if ch_sec > 0 else 0.0
+    us = 1e6 * ch_sec / max(1, len(mx["ch_solve_s"]))
+    by = by_total / max(1, len(mx["ch_solve_s"]))
+    fl = None
     steps_total = K * ws
     value = steps_total / sec
     line = {
@@ -387,9 +404,10 @@ def run_gpu(args, ws, rank, local):
             "mixed_over_fp64": None if f64 is None else (value / (K64 * ws / f64_sec)),
             "kernels_us": {abi.KB_NAMES[k]: round(v[0], 3) for k, v in kb.items()},
         },
-        "roofline": {"bound": "hbm", "kernel": abi.KB_NAMES[dom], "achieved": achieved, "peak": hbm_peak,
-                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
-                     "flops_per_launch": fl, "bytes_per_launch": by, "us_per_launch": us,
+        "roofline": {"bound": "hbm", "kernel": "k_bicg_persist<CH> (whole mixed CH solve)", "achieved": achieved,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": TRAFFIC_CH,
+                     "bytes_per_launch": by, "us_per_launch": us,
+                     "iterations_per_launch": it_total / max(1, len(mx["ch_solve_s"])),
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst)" if peaks else "fallback 6800 GB/s"},
         "e2e": {"value": e2e_steps * ws / e2e_sec, "unit": "time-steps/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"]},

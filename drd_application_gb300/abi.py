@@ -148,7 +148,7 @@ class drd_status(C.Structure):
 
 class drd_step_stats(C.Structure):
     _fields_ = [("ch", drd_status), ("uv", drd_status), ("pre", drd_status), ("mass", C.c_double),
-                ("t", C.c_double)]
+                ("t", C.c_double), ("seconds", C.c_double)]
 
 
 def default_params(nr, nz, **kw):

@@ -58,6 +58,7 @@ struct KState {
     int do_update;     // mixed mode: this iteration ends with a reliable update
     int mixed;         // mixed mode: no absolute ||s|| exit; convergence on the FP64 residual only
     int restart;       // mixed mode: the update also restarts the Krylov sequence (breakdown)
+    unsigned long long t_begin, t_end;  // persistent solver: %globaltimer (ns) at its start and end
 };
 
 __host__ __device__ __forceinline__ long cidx(int nr, int i, int k) { return (long)(i + 1) + (long)(k + 1) * (nr + 2); }

@@ -2090,12 +2090,19 @@ __device__ bool pb_matvec_uv(const PersistArgs& a, const float* x, float* y, flo
     const long stride = (long)gridDim.x * PB_NT;
     UVFetch<float, true> F{x, a.nr, a.nz, mn, a.o.lr_neumann};
     double s1 = 0.0, s2 = 0.0;
-    for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < a.n; q += stride) {
+    // two rows per pass, both computed before either is stored, so their loads overlap
+    for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < a.n; q += 2 * stride) {
+        const long q2 = q + stride;
+        const bool two = q2 < a.n;
         const float av = uv_apply<float>(a.o, a.rho, a.eta, a.pen, F, q);
-        const float yn = yin ? alpha * av + __ldcg(yin + q) : alpha * av;
-        y[q] = yn;
-        if (d1) s1 += (double)__ldcg(d1 + q) * (double)yn;
-        if (self2) s2 += (double)yn * (double)yn;
+        const float av2 = two ? uv_apply<float>(a.o, a.rho, a.eta, a.pen, F, q2) : 0.f;
+        const float y1 = yin ? alpha * av + __ldcg(yin + q) : alpha * av;
+        const float y2 = two ? (yin ? alpha * av2 + __ldcg(yin + q2) : alpha * av2) : 0.f;
+        const float e1 = d1 ? __ldcg(d1 + q) : 0.f, e2 = (d1 && two) ? __ldcg(d1 + q2) : 0.f;
+        y[q] = y1;
+        if (two) y[q2] = y2;
+        if (d1) s1 += (double)e1 * (double)y1 + (double)e2 * (double)y2;
+        if (self2) s2 += (double)y1 * (double)y1 + (double)y2 * (double)y2;
     }
     if (d1) slot_put<PB_NT>(a.part, slot1, s1, sm);
     if (self2) slot_put<PB_NT>(a.part, slot2, s2, sm);
@@ -2144,17 +2151,29 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         if (fabs(st.rho) < kBreakTol) { st.info = -10; break; }
         st.beta = first ? 0.0 : (st.rho / st.rho1) * (st.alpha / st.omega);
         {
+            // P = R (first) or BETA (P - OMEGA V) + R; two elements per pass, loads before stores
             const float bt = (float)st.beta, nom = (float)(-st.omega);
-            for (long q = q0; q < n; q += stride) {
-                float pv;
-                if (first) pv = __ldcg(a.r + q);
-                else {
-                    pv = __ldcg(a.p + q) + nom * __ldcg(a.v + q);
-                    pv = bt * pv;
-                    pv = pv + __ldcg(a.r + q);
+            for (long q = q0; q < n; q += 2 * stride) {
+                const long q2 = q + stride;
+                const bool two = q2 < n;
+                float r1 = __ldcg(a.r + q), r2 = two ? __ldcg(a.r + q2) : 0.f;
+                float p1 = 0.f, p2 = 0.f, v1 = 0.f, v2 = 0.f;
+                if (!first) {
+                    p1 = __ldcg(a.p + q);
+                    v1 = __ldcg(a.v + q);
+                    if (two) { p2 = __ldcg(a.p + q2); v2 = __ldcg(a.v + q2); }
                 }
-                a.p[q] = pv;
-                if constexpr (KIND == PK_UV) a.phat[q] = pb_pre(a, q, pv);  // PHAT = M^-1 P, fused
+                float pv1 = r1, pv2 = r2;
+                if (!first) {
+                    pv1 = bt * (p1 + nom * v1) + r1;
+                    pv2 = bt * (p2 + nom * v2) + r2;
+                }
+                a.p[q] = pv1;
+                if (two) a.p[q2] = pv2;
+                if constexpr (KIND == PK_UV) {  // PHAT = M^-1 P, fused
+                    a.phat[q] = pb_pre(a, q, pv1);
+                    if (two) a.phat[q2] = pb_pre(a, q2, pv2);
+                }
             }
         }
         first = false;
@@ -2170,11 +2189,19 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         {
             const float na = (float)(-st.alpha);
             double s2 = 0.0;
-            for (long q = q0; q < n; q += stride) {
-                const float sv = __ldcg(a.r + q) + na * __ldcg(a.v + q);
-                a.r[q] = sv;
-                s2 += (double)sv * (double)sv;
-                if constexpr (KIND == PK_UV) a.shat[q] = pb_pre(a, q, sv);  // SHAT = M^-1 S, fused
+            for (long q = q0; q < n; q += 2 * stride) {
+                const long q2 = q + stride;
+                const bool two = q2 < n;
+                const float ra = __ldcg(a.r + q), va = __ldcg(a.v + q);
+                const float rb = two ? __ldcg(a.r + q2) : 0.f, vb = two ? __ldcg(a.v + q2) : 0.f;
+                const float sv1 = ra + na * va, sv2 = rb + na * vb;
+                a.r[q] = sv1;
+                if (two) a.r[q2] = sv2;
+                s2 += (double)sv1 * (double)sv1 + (double)sv2 * (double)sv2;
+                if constexpr (KIND == PK_UV) {  // SHAT = M^-1 S, fused
+                    a.shat[q] = pb_pre(a, q, sv1);
+                    if (two) a.shat[q2] = pb_pre(a, q2, sv2);
+                }
             }
             slot_put<PB_NT>(a.part, 5, s2, sm);
         }
@@ -2199,18 +2226,29 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         {
             const float al = (float)st.alpha, om = (float)st.omega, nom = (float)(-st.omega);
             double r2 = 0.0, rr = 0.0;
-            for (long q = q0; q < n; q += stride) {
-                // all six loads before either store (the vectors may alias as far as the
-                // compiler knows), so an element costs one L2 round trip
+            for (long q = q0; q < n; q += 2 * stride) {
+                // the loads of both elements before any store (the vectors may alias as far as
+                // the compiler knows), so a pass costs one L2 round trip
+                const long q2 = q + stride;
+                const bool two = q2 < n;
                 const float x0 = __ldcg(a.x + q), ph = __ldcg(a.phat + q), sh = __ldcg(a.shat + q);
                 const float s0 = __ldcg(a.r + q), t0 = __ldcg(a.t + q), rt = __ldcg(a.rtld + q);
+                float x0b = 0.f, phb = 0.f, shb = 0.f, s0b = 0.f, t0b = 0.f, rtb = 0.f;
+                if (two) {
+                    x0b = __ldcg(a.x + q2); phb = __ldcg(a.phat + q2); shb = __ldcg(a.shat + q2);
+                    s0b = __ldcg(a.r + q2); t0b = __ldcg(a.t + q2); rtb = __ldcg(a.rtld + q2);
+                }
                 float xv = x0 + al * ph;
                 xv = xv + om * sh;
                 const float rvq = s0 + nom * t0;
+                float xvb = x0b + al * phb;
+                xvb = xvb + om * shb;
+                const float rvb = s0b + nom * t0b;
                 a.x[q] = xv;
                 a.r[q] = rvq;
-                r2 += (double)rvq * (double)rvq;
-                rr += (double)rt * (double)rvq;
+                if (two) { a.x[q2] = xvb; a.r[q2] = rvb; }
+                r2 += (double)rvq * (double)rvq + (double)rvb * (double)rvb;
+                rr += (double)rt * (double)rvq + (double)rtb * (double)rvb;
             }
             slot_put<PB_NT>(a.part, 0, r2, sm);
             slot_put<PB_NT>(a.part, 1, rr, sm);
@@ -2289,6 +2327,7 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
     const long q0 = blockIdx.x * (long)PB_NT + threadIdx.x;
     KState* ks = a.ks;
     PbProf pf{nullptr, 0};
+    const unsigned long long t_begin = lead ? gtimer() : 0ull;
     // the parent (FP64 refinement) state decides whether this inner solve runs at all
     if (a.parent && *((volatile const int*)&a.parent->phase) != PH_RUNNING) {
         if (lead) { ks->phase = PH_DONE; ks->iter = 0; ks->info = 0; }
@@ -2377,6 +2416,8 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
             ks->info = oinfo;
             ks->flags = DRD_FLAG_REFINED;
             ks->mixed = 1;
+            ks->t_begin = t_begin;
+            ks->t_end = gtimer();
             ks->phase = PH_DONE;
         }
         return;
@@ -2439,6 +2480,8 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
         ks->beta = st.beta;
         ks->flags = st.flags;
         ks->mixed = 0;
+        ks->t_begin = t_begin;
+        ks->t_end = gtimer();
         ks->phase = PH_DONE;
     }
 }

@@ -1571,8 +1571,12 @@ int drd_step(drd_ctx* c, int first, double t, drd_step_stats* stats) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     const int mixed = mixed_of(c);
-    fill_status(c->h_ks[c->P.variant == DRD_VARIANT_TP ? KS_PHMU : KS_CH], &stats->ch, mixed, ms * 1e-3);
-    fill_status(c->h_ks[KS_UV], &stats->uv, mixed, ms * 1e-3);
+    // a solve's own device time: the persistent solver stamps %globaltimer at its start and end
+    auto solve_s = [](const KState& k) { return k.t_end > k.t_begin ? 1e-9 * (double)(k.t_end - k.t_begin) : 0.0; };
+    const KState& kch = c->h_ks[c->P.variant == DRD_VARIANT_TP ? KS_PHMU : KS_CH];
+    fill_status(kch, &stats->ch, mixed, solve_s(kch));
+    fill_status(c->h_ks[KS_UV], &stats->uv, mixed, solve_s(c->h_ks[KS_UV]));
+    stats->seconds = ms * 1e-3;
     memset(&stats->pre, 0, sizeof(stats->pre));
     stats->mass = *c->h_mass;
     stats->t = t + c->P.dt;

@@ -275,11 +275,12 @@ int drd_state_download(drd_ctx* ctx, int field, double* host);
 int drd_state_device_ptr(drd_ctx* ctx, int field, double** dptr);
 
 typedef struct drd_step_stats {
-    drd_status ch;   /* PhSolve or ph_mu_solve */
-    drd_status uv;   /* VeloSolve(_2)_combined  */
+    drd_status ch;   /* PhSolve or ph_mu_solve; .seconds = device time of its Krylov solve        */
+    drd_status uv;   /* VeloSolve(_2)_combined; .seconds = device time of its Krylov solve        */
     drd_status pre;  /* PreSolve_2              */
     double mass;     /* sum(ph) dr dz after the step (FP64)  */
     double t;        /* time after the step     */
+    double seconds;  /* device time of the whole step (CUDA events around the step's launch)     */
 } drd_step_stats;
 
 /* One pass of the mcl6 time loop body (microfluidics_complex_domain/mcl6.f90:378-486, the
