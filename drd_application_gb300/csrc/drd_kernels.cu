@@ -2052,44 +2052,57 @@ __device__ bool pb_psolve(const PersistArgs& a, const float* x, float* y, float*
     return true;
 }
 
-// y = A x (MATRIX_VECTOR_CG) in two phases; optional partial dots of y with d1 and with itself.
+// ff1 = -(dt xld) L_M0(x) evaluated where it is needed (the first half of MATRIX_VECTOR_CG).
+template <typename T, class XA>
+struct ChFF1 {
+    XA x; CellA<T> M0; int nr, nz; T dtxld, idr2, idz2;
+    __device__ __forceinline__ T operator()(int i, int k) const {
+        return -(dtxld * op_dgn<T>(i, k, nr, nz, idr2, idz2, x, M0));
+    }
+};
+
+// y = A x (MATRIX_VECTOR_CG) in ONE phase: the outer operator reads ff1 at a cell and its four
+// neighbours, and each of those five values is recomputed from x (a radius-2 stencil) instead
+// of being stored and re-read after a grid barrier.  The arithmetic of every ff1 value is the
+// same as the two-pass form, so the result is too.  Optional partial dots of y with d1 and with
+// itself.
 __device__ bool pb_matvec_ch(const PersistArgs& a, const float* x, float* y, float alpha, const float* yin,
-                             const float* d1, int slot1, bool self2, int slot2, double* sm, unsigned& gen,
-                             PbProf& pf) {
+                             const float* d1, int slot1, bool self2, int slot2, const float* d3, int slot3,
+                             double* sm, unsigned& gen, PbProf& pf) {
+    (void)gen;
+    (void)pf;
     const int nr = a.nr, nz = a.nz;
     const long n = (long)nr * nz;
     const long stride = (long)gridDim.x * PB_NT;
-    PackedCG<float> X{x, nr};
-    CellA<float> M0{a.M0, nr}, Mi{a.Mi, nr};
+    const ChFF1<float, PackedCG<float>> F{PackedCG<float>{x, nr}, CellA<float>{a.M0, nr}, nr, nz, a.o.dtxld,
+                                          a.o.idr2, a.o.idz2};
+    CellA<float> Mi{a.Mi, nr};
+    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
     for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < n; q += stride) {
         const int i = (int)(q % nr), k = (int)(q / nr);
-        a.ff1[q] = -(a.o.dtxld * op_dgn<float>(i, k, nr, nz, a.o.idr2, a.o.idz2, X, M0));
-    }
-    if (!grid_sync(a.bar, gen, pf)) return false;
-    PackedCG<float> F{a.ff1, nr};
-    double s1 = 0.0, s2 = 0.0;
-    for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < n; q += stride) {
-        const int i = (int)(q % nr), k = (int)(q / nr);
-        const float f = __ldcg(a.ff1 + q);
+        const float f = F(i, k);
         const float av = __ldcg(x + q) + (a.o.s * f / a.o.eps - a.o.eps * op_dgn<float>(i, k, nr, nz, a.o.idr2,
                                                                                         a.o.idz2, F, Mi));
         const float yn = yin ? alpha * av + __ldcg(yin + q) : alpha * av;
         y[q] = yn;
         if (d1) s1 += (double)__ldcg(d1 + q) * (double)yn;
         if (self2) s2 += (double)yn * (double)yn;
+        if (d3) s3 += (double)__ldcg(d3 + q) * (double)yn;
     }
     if (d1) slot_put<PB_NT>(a.part, slot1, s1, sm);
     if (self2) slot_put<PB_NT>(a.part, slot2, s2, sm);
+    if (d3) slot_put<PB_NT>(a.part, slot3, s3, sm);
     return true;
 }
 
 // y = A x (MatrixVector_uv_2_CG / MatrixVector_uv_CG) in one phase, with the same options.
 __device__ bool pb_matvec_uv(const PersistArgs& a, const float* x, float* y, float alpha, const float* yin,
-                             const float* d1, int slot1, bool self2, int slot2, double* sm) {
+                             const float* d1, int slot1, bool self2, int slot2, const float* d3, int slot3,
+                             double* sm) {
     const long mn = (long)(a.nr + 1) * a.nz;
     const long stride = (long)gridDim.x * PB_NT;
     UVFetch<float, true> F{x, a.nr, a.nz, mn, a.o.lr_neumann};
-    double s1 = 0.0, s2 = 0.0;
+    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
     // two rows per pass, both computed before either is stored, so their loads overlap
     for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < a.n; q += 2 * stride) {
         const long q2 = q + stride;
@@ -2099,24 +2112,28 @@ __device__ bool pb_matvec_uv(const PersistArgs& a, const float* x, float* y, flo
         const float y1 = yin ? alpha * av + __ldcg(yin + q) : alpha * av;
         const float y2 = two ? (yin ? alpha * av2 + __ldcg(yin + q2) : alpha * av2) : 0.f;
         const float e1 = d1 ? __ldcg(d1 + q) : 0.f, e2 = (d1 && two) ? __ldcg(d1 + q2) : 0.f;
+        const float g1 = d3 ? __ldcg(d3 + q) : 0.f, g2 = (d3 && two) ? __ldcg(d3 + q2) : 0.f;
         y[q] = y1;
         if (two) y[q2] = y2;
         if (d1) s1 += (double)e1 * (double)y1 + (double)e2 * (double)y2;
         if (self2) s2 += (double)y1 * (double)y1 + (double)y2 * (double)y2;
+        if (d3) s3 += (double)g1 * (double)y1 + (double)g2 * (double)y2;
     }
     if (d1) slot_put<PB_NT>(a.part, slot1, s1, sm);
     if (self2) slot_put<PB_NT>(a.part, slot2, s2, sm);
+    if (d3) slot_put<PB_NT>(a.part, slot3, s3, sm);
     return true;
 }
 
 template <int KIND>
 __device__ __forceinline__ bool pb_matvec(const PersistArgs& a, const float* x, float* y, float alpha, const float* yin,
                                           const float* d1, int slot1, bool self2, int slot2, double* sm,
-                                          unsigned& gen, PbProf& pf) {
-    if constexpr (KIND == PK_CH) return pb_matvec_ch(a, x, y, alpha, yin, d1, slot1, self2, slot2, sm, gen, pf);
+                                          unsigned& gen, PbProf& pf, const float* d3 = nullptr, int slot3 = 0) {
+    if constexpr (KIND == PK_CH)
+        return pb_matvec_ch(a, x, y, alpha, yin, d1, slot1, self2, slot2, d3, slot3, sm, gen, pf);
     (void)gen;
     (void)pf;
-    return pb_matvec_uv(a, x, y, alpha, yin, d1, slot1, self2, slot2, sm);
+    return pb_matvec_uv(a, x, y, alpha, yin, d1, slot1, self2, slot2, d3, slot3, sm);
 }
 
 // Element-wise preconditioner of the momentum system: Jacobi (PSolve_uv_2_CG) or the identity.
@@ -2131,53 +2148,30 @@ struct PbInner {
     double resid, rho, rho1, alpha, omega, beta, snorm;
 };
 
-// The iterations (lib/BiCGSTABREVCOM.f:257-388) from R, RTLD and the first RHO = (rtld, r);
-// X is updated in place.  Every block runs the same scalar steps; returns false when a barrier
-// timed out.
+// The iterations (lib/BiCGSTABREVCOM.f:257-388) from R, RTLD, P = R (and, for the momentum
+// system, PHAT = M^-1 P) and the first RHO = (rtld, r); X is updated in place.  Every block runs
+// the same scalar steps; returns false when a barrier timed out.
+//
+// One change of schedule against the reference: the next RHO is formed as (rtld, s) -
+// omega (rtld, t), from partials of the S pass and the T product, instead of (rtld, r) after R
+// is updated.  BETA is then known when X and R are updated, and the next P = BETA (P - OMEGA V)
+// + R is formed in the same pass: one phase and one grid barrier fewer per iteration.  The
+// STOPTEST2 norm of the new R is read after the next barrier, so the transform of the next P is
+// computed before a converged solve stops (its result is then unused).
 template <int KIND>
 __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int maxit, double rho_first, PbInner& st,
                            float* smem, double* sm, unsigned& gen, PbProf& pf) {
     const long n = a.n;
     const long stride = (long)gridDim.x * PB_NT;
     const long q0 = blockIdx.x * (long)PB_NT + threadIdx.x;
-    bool ok = true, first = true;
-    int phase = PH_RUNNING;
-    double rho_next = rho_first;
+    bool ok = true;
+    double rho = rho_first;
     st.iter = 0;
-    while (phase == PH_RUNNING) {
-        st.rho = rho_next;  // RHO = (rtld, r), summed with the previous STOPTEST norm
+    while (true) {
+        st.rho = rho;
         st.iter += 1;
         pf.p = (a.prof != nullptr && st.iter == 3 && pf.k == 0) ? a.prof : nullptr;  // time iteration 3 once
-        if (fabs(st.rho) < kBreakTol) { st.info = -10; break; }
-        st.beta = first ? 0.0 : (st.rho / st.rho1) * (st.alpha / st.omega);
-        {
-            // P = R (first) or BETA (P - OMEGA V) + R; two elements per pass, loads before stores
-            const float bt = (float)st.beta, nom = (float)(-st.omega);
-            for (long q = q0; q < n; q += 2 * stride) {
-                const long q2 = q + stride;
-                const bool two = q2 < n;
-                float r1 = __ldcg(a.r + q), r2 = two ? __ldcg(a.r + q2) : 0.f;
-                float p1 = 0.f, p2 = 0.f, v1 = 0.f, v2 = 0.f;
-                if (!first) {
-                    p1 = __ldcg(a.p + q);
-                    v1 = __ldcg(a.v + q);
-                    if (two) { p2 = __ldcg(a.p + q2); v2 = __ldcg(a.v + q2); }
-                }
-                float pv1 = r1, pv2 = r2;
-                if (!first) {
-                    pv1 = bt * (p1 + nom * v1) + r1;
-                    pv2 = bt * (p2 + nom * v2) + r2;
-                }
-                a.p[q] = pv1;
-                if (two) a.p[q2] = pv2;
-                if constexpr (KIND == PK_UV) {  // PHAT = M^-1 P, fused
-                    a.phat[q] = pb_pre(a, q, pv1);
-                    if (two) a.phat[q2] = pb_pre(a, q2, pv2);
-                }
-            }
-        }
-        first = false;
-        if (!(ok = grid_sync(a.bar, gen, pf))) break;
+        if (fabs(st.rho) < kBreakTol) { st.info = -10; break; }  // (:261-263)
         if constexpr (KIND == PK_CH) {
             if (!(ok = pb_psolve(a, a.p, a.phat, smem, gen, pf))) break;     // PHAT = M^-1 P
             if (!(ok = grid_sync(a.bar, gen, pf))) break;
@@ -2187,23 +2181,27 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         const double rv = slot_sum<PB_NT>(a.part, 4, sm);
         st.alpha = st.rho / rv;  // (:307)
         {
+            // S = R - ALPHA V (:311-312), ||S||^2 and (rtld, S); two elements per pass
             const float na = (float)(-st.alpha);
-            double s2 = 0.0;
+            double s2 = 0.0, rs = 0.0;
             for (long q = q0; q < n; q += 2 * stride) {
                 const long q2 = q + stride;
                 const bool two = q2 < n;
-                const float ra = __ldcg(a.r + q), va = __ldcg(a.v + q);
+                const float ra = __ldcg(a.r + q), va = __ldcg(a.v + q), ta = __ldcg(a.rtld + q);
                 const float rb = two ? __ldcg(a.r + q2) : 0.f, vb = two ? __ldcg(a.v + q2) : 0.f;
+                const float tb = two ? __ldcg(a.rtld + q2) : 0.f;
                 const float sv1 = ra + na * va, sv2 = rb + na * vb;
                 a.r[q] = sv1;
                 if (two) a.r[q2] = sv2;
                 s2 += (double)sv1 * (double)sv1 + (double)sv2 * (double)sv2;
+                rs += (double)ta * (double)sv1 + (double)tb * (double)sv2;
                 if constexpr (KIND == PK_UV) {  // SHAT = M^-1 S, fused
                     a.shat[q] = pb_pre(a, q, sv1);
                     if (two) a.shat[q2] = pb_pre(a, q2, sv2);
                 }
             }
             slot_put<PB_NT>(a.part, 5, s2, sm);
+            slot_put<PB_NT>(a.part, 2, rs, sm);
         }
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
         st.snorm = sqrt(slot_sum<PB_NT>(a.part, 5, sm));
@@ -2219,51 +2217,65 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
             if (!(ok = pb_psolve(a, a.r, a.shat, smem, gen, pf))) break;     // SHAT = M^-1 S
             if (!(ok = grid_sync(a.bar, gen, pf))) break;
         }
-        if (!(ok = pb_matvec<KIND>(a, a.shat, a.t, 1.f, nullptr, a.r, 6, true, 7, sm, gen, pf))) break;  // T = A SHAT
+        // T = A SHAT with (t, s), (t, t) and (rtld, t)
+        if (!(ok = pb_matvec<KIND>(a, a.shat, a.t, 1.f, nullptr, a.r, 6, true, 7, sm, gen, pf, a.rtld, 1))) break;
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
         const double2 tst = slot_sum2<PB_NT>(a.part, 6, 7, sm);
-        st.omega = tst.x / tst.y;  // (:349-350)
+        const double2 rst = slot_sum2<PB_NT>(a.part, 2, 1, sm);
+        st.omega = tst.x / tst.y;                           // (:349-350)
+        const double rho_new = rst.x - st.omega * rst.y;    // (rtld, S - OMEGA T)
+        st.beta = (rho_new / st.rho) * (st.alpha / st.omega);  // (:269) for the next iteration
         {
+            // X = X + ALPHA PHAT + OMEGA SHAT, R = S - OMEGA T (:354-359), ||R||^2, and the next
+            // P = BETA (P - OMEGA V) + R (:273-275); two elements per pass, loads before stores
             const float al = (float)st.alpha, om = (float)st.omega, nom = (float)(-st.omega);
-            double r2 = 0.0, rr = 0.0;
+            const float bt = (float)st.beta;
+            double r2 = 0.0;
             for (long q = q0; q < n; q += 2 * stride) {
-                // the loads of both elements before any store (the vectors may alias as far as
-                // the compiler knows), so a pass costs one L2 round trip
                 const long q2 = q + stride;
                 const bool two = q2 < n;
-                const float x0 = __ldcg(a.x + q), ph = __ldcg(a.phat + q), sh = __ldcg(a.shat + q);
-                const float s0 = __ldcg(a.r + q), t0 = __ldcg(a.t + q), rt = __ldcg(a.rtld + q);
-                float x0b = 0.f, phb = 0.f, shb = 0.f, s0b = 0.f, t0b = 0.f, rtb = 0.f;
+                float xa = __ldcg(a.x + q), pha = __ldcg(a.phat + q), sha = __ldcg(a.shat + q);
+                float sa = __ldcg(a.r + q), tta = __ldcg(a.t + q), pa = __ldcg(a.p + q), vva = __ldcg(a.v + q);
+                float xb = 0.f, phb = 0.f, shb = 0.f, sb = 0.f, ttb = 0.f, pb = 0.f, vvb = 0.f;
                 if (two) {
-                    x0b = __ldcg(a.x + q2); phb = __ldcg(a.phat + q2); shb = __ldcg(a.shat + q2);
-                    s0b = __ldcg(a.r + q2); t0b = __ldcg(a.t + q2); rtb = __ldcg(a.rtld + q2);
+                    xb = __ldcg(a.x + q2); phb = __ldcg(a.phat + q2); shb = __ldcg(a.shat + q2);
+                    sb = __ldcg(a.r + q2); ttb = __ldcg(a.t + q2); pb = __ldcg(a.p + q2); vvb = __ldcg(a.v + q2);
                 }
-                float xv = x0 + al * ph;
-                xv = xv + om * sh;
-                const float rvq = s0 + nom * t0;
-                float xvb = x0b + al * phb;
+                float xv = xa + al * pha;
+                xv = xv + om * sha;
+                const float rva = sa + nom * tta;
+                float pva = pa + nom * vva;
+                pva = bt * pva;
+                pva = pva + rva;
+                float xvb = xb + al * phb;
                 xvb = xvb + om * shb;
-                const float rvb = s0b + nom * t0b;
+                const float rvb = sb + nom * ttb;
+                float pvb = pb + nom * vvb;
+                pvb = bt * pvb;
+                pvb = pvb + rvb;
                 a.x[q] = xv;
-                a.r[q] = rvq;
-                if (two) { a.x[q2] = xvb; a.r[q2] = rvb; }
-                r2 += (double)rvq * (double)rvq + (double)rvb * (double)rvb;
-                rr += (double)rt * (double)rvq + (double)rtb * (double)rvb;
+                a.r[q] = rva;
+                a.p[q] = pva;
+                if (two) { a.x[q2] = xvb; a.r[q2] = rvb; a.p[q2] = pvb; }
+                if constexpr (KIND == PK_UV) {  // PHAT = M^-1 P of the next iteration, fused
+                    a.phat[q] = pb_pre(a, q, pva);
+                    if (two) a.phat[q2] = pb_pre(a, q2, pvb);
+                }
+                r2 += (double)rva * (double)rva + (double)rvb * (double)rvb;
             }
             slot_put<PB_NT>(a.part, 0, r2, sm);
-            slot_put<PB_NT>(a.part, 1, rr, sm);
         }
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
-        const double2 rr01 = slot_sum2<PB_NT>(a.part, 0, 1, sm);
-        st.resid = sqrt(rr01.x) / bnrm2;  // STOPTEST2 (:361-362)
-        rho_next = rr01.y;
-        if (!isfinite(st.resid)) { st.info = DRD_ERR_NONFINITE; phase = PH_DONE; }
-        else if (st.resid <= tol) { st.info = 0; phase = PH_DONE; }
-        else if (st.iter >= maxit) { st.info = 1; phase = PH_DONE; }
-        else if (fabs(st.omega) < kBreakTol) {
+        st.resid = sqrt(slot_sum<PB_NT>(a.part, 0, sm)) / bnrm2;  // STOPTEST2 (:361-362)
+        if (!isfinite(st.resid)) { st.info = DRD_ERR_NONFINITE; break; }
+        if (st.resid <= tol) { st.info = 0; break; }
+        if (st.iter >= maxit) { st.info = 1; break; }
+        if (fabs(st.omega) < kBreakTol) {  // (:383-388)
             st.info = (fabs(st.rho) < kBreakTol) ? -10 : -11;
-            phase = PH_DONE;
-        } else st.rho1 = st.rho;
+            break;
+        }
+        st.rho1 = st.rho;
+        rho = rho_new;
     }
     pf.p = nullptr;
     return ok;
@@ -2278,17 +2290,14 @@ __device__ bool pb_residual64(const PersistArgs& a, bool with_b, double* sm, uns
     const long stride = (long)gridDim.x * PB_NT;
     double r2 = 0.0, b2 = 0.0;
     if constexpr (KIND == PK_CH) {
-        PackedCG<double> X{a.x64, nr};
-        CellA<double> M0{a.M0d, nr}, Mi{a.Mid, nr};
+        const ChFF1<double, PackedCG<double>> Fv{PackedCG<double>{a.x64, nr}, CellA<double>{a.M0d, nr}, nr, nz,
+                                                 a.od.dtxld, a.od.idr2, a.od.idz2};
+        CellA<double> Mi{a.Mid, nr};
+        (void)gen;
+        (void)pf;
         for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < n; q += stride) {
             const int i = (int)(q % nr), k = (int)(q / nr);
-            a.f64[q] = -(a.od.dtxld * op_dgn<double>(i, k, nr, nz, a.od.idr2, a.od.idz2, X, M0));
-        }
-        if (!grid_sync(a.bar, gen, pf)) return false;
-        PackedCG<double> Fv{a.f64, nr};
-        for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < n; q += stride) {
-            const int i = (int)(q % nr), k = (int)(q / nr);
-            const double f = __ldcg(a.f64 + q), bq = __ldcg(a.b64 + q);
+            const double f = Fv(i, k), bq = __ldcg(a.b64 + q);
             const double av = __ldcg(a.x64 + q) + (a.od.s * f / a.od.eps -
                                                    a.od.eps * op_dgn<double>(i, k, nr, nz, a.od.idr2, a.od.idz2, Fv, Mi));
             const double rq = -1.0 * av + 1.0 * bq;
@@ -2384,6 +2393,8 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
                     a.b[q] = bv;
                     a.r[q] = bv;
                     a.rtld[q] = bv;
+                    a.p[q] = bv;  // the first P = R (:268)
+                    if constexpr (KIND == PK_UV) a.phat[q] = pb_pre(a, q, bv);
                     a.x[q] = 0.f;
                     bb += (double)bv * (double)bv;
                 }
@@ -2454,6 +2465,8 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
         for (long q = q0; q < n; q += stride) {
             const float rv = __ldcg(a.r + q);
             a.rtld[q] = rv;
+            a.p[q] = rv;  // the first P = R (:268)
+            if constexpr (KIND == PK_UV) a.phat[q] = pb_pre(a, q, rv);
             a1 += (double)rv * (double)rv;
         }
         slot_put<PB_NT>(a.part, 1, a1, sm);
