@@ -337,6 +337,19 @@ def run_gpu(args, ws, rank, local):
     e2e_steps = K
     ctx.close()
 
+    # the same mixed step with the fiber coupling of the reference loop (a 9-bead chain moved by
+    # the flow, its forces spread onto the grid, rho/eta rebuilt every step) in place of the
+    # rigid fibers: reported beside the headline, not part of it
+    casep = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED, guess_mode=1,
+                      particles=True)
+    ctxp = DRDContext(casep.params)
+    ctxp.set_case(casep)
+    parts = casep.meta["particles"]
+    ctxp.particles_set(parts["pp"], parts["points"], parts["bdr_dist"])
+    pt = time_resident(ctxp, casep, W, K, flush)
+    pt_sec = max_over_ranks(dist, pt["seconds"])
+    ctxp.close()
+
     # plain FP64 path, resident state (--fp64-steps 0 skips it, e.g. for profiler runs)
     f64, f64_sec = None, None
     if K64 > 0:
@@ -403,6 +416,8 @@ def run_gpu(args, ws, rank, local):
                 "solves_to_fp64_1e-8": f"{f64['solves_ok']}/{f64['solves']}"},
             "mixed_over_fp64": None if f64 is None else (value / (K64 * ws / f64_sec)),
             "kernels_us": {abi.KB_NAMES[k]: round(v[0], 3) for k, v in kb.items()},
+            "with_particles": {"steps_per_s": K * ws / pt_sec, "ms_per_step": 1e3 * pt_sec / K, "beads": 9,
+                               "solves_to_fp64_1e-8": f"{pt['solves_ok']}/{pt['solves']}"},
         },
         "roofline": {"bound": "hbm", "kernel": "k_bicg_persist<CH> (whole mixed CH solve)", "achieved": achieved,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": TRAFFIC_CH,
