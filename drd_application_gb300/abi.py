@@ -28,6 +28,7 @@ DRD_FLAG_FALLBACK64 = 8
 
 DRD_OP_CH_MATVEC, DRD_OP_CH_PSOLVE, DRD_OP_UV_MATVEC, DRD_OP_UV_PSOLVE, DRD_OP_PHMU_MATVEC, DRD_OP_PHMU_PSOLVE = range(6)
 DRD_OP_PERSISTENT = 2  # op_apply precision: the persistent solver's FP32 operator code
+DRD_UV_JACOBI, DRD_UV_ESOLP = 0, 1  # drd_params.uv_precond
 
 (DRD_KB_UV_MATVEC_FP64, DRD_KB_UV_MATVEC_FP32, DRD_KB_DCT_X_FP64, DRD_KB_DCT_X_FP32, DRD_KB_DCT_Z_FP64,
  DRD_KB_DCT_Z_FP32, DRD_KB_CH_MATVEC_FP32) = range(7)
@@ -62,7 +63,7 @@ class drd_params(C.Structure):
         ("UU", C.c_double), ("twall", C.c_double), ("bdr_upp", C.c_double), ("bdr_low", C.c_double),
         ("angle", C.c_double), ("xlsB", C.c_double), ("penalty_k", C.c_double),
         ("lambda_rho", C.c_double), ("lambda_eta", C.c_double), ("bdr_ph_used_adjust", C.c_double),
-        ("mixed_inner_tol", C.c_double), ("mixed_max_refine", C.c_int32), ("reserved1", C.c_int32),
+        ("mixed_inner_tol", C.c_double), ("mixed_max_refine", C.c_int32), ("uv_precond", C.c_int32),
     ]
 
     def copy(self):

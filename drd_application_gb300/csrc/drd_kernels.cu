@@ -378,6 +378,63 @@ __global__ void k_ori_bdr(int nr, int nz, const double* __restrict__ ph, double*
     }
 }
 
+// ======================================================================================
+// ESOLP_x tridiagonal stage (Precipitation_dynamics/ESOLP.f90:23-41 with rfords): for every
+// x mode k of a block of `rows` rows of `len` values (row j, mode k at w[k + len*j]), solve
+// the tridiagonal system along j in place.  The elimination multipliers r_j = -a_j/b'_{j-1}
+// and the pivots b'_j depend only on the coefficients and come precomputed, like c_j, at
+// [k + len*j]: thread k's loads are coalesced across the warp.  The two blocks of a momentum
+// vector (u, then v) are one launch.  The sweep is a chain of dependent steps, so each thread
+// loads TRI_CH rows ahead before it runs the chain through them.
+// ======================================================================================
+constexpr int TRI_CH = 16;
+template <typename T>
+__global__ void k_tridiag(TriBlock<T> b0, TriBlock<T> b1, const KState* ks, int gate, ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, gate)) return;
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool second = k >= b0.len;
+    const TriBlock<T>& B = second ? b1 : b0;
+    if (second) k -= b0.len;
+    if (k >= B.len) return;
+    const long L = B.len;
+    T* __restrict__ w = B.w + k;
+    const T* __restrict__ rm = B.rm + k;
+    const T* __restrict__ bp = B.bp + k;
+    const T* __restrict__ cc = B.cc + k;
+    const int R = B.rows;
+    // forward elimination f_j = f_j + r_j f_{j-1} (f_0 = w_0)
+    T f = T(0);
+    for (int j0 = 0; j0 < R; j0 += TRI_CH) {
+        T wv[TRI_CH], rv[TRI_CH];
+#pragma unroll
+        for (int q = 0; q < TRI_CH; ++q)
+            if (j0 + q < R) { wv[q] = w[L * (j0 + q)]; rv[q] = rm[L * (j0 + q)]; }
+#pragma unroll
+        for (int q = 0; q < TRI_CH; ++q)
+            if (j0 + q < R) {
+                f = (j0 + q == 0) ? wv[q] : wv[q] + rv[q] * f;
+                w[L * (j0 + q)] = f;
+            }
+    }
+    // back substitution ff_{R-1} = f/b' (0 when |b'| <= 1e-12), ff_j = (f_j - c_j ff_{j+1}) / b'_j
+    const T bl = bp[L * (R - 1)];
+    T nxt = (fabs((double)bl) <= 1.0E-12) ? T(0) : f / bl;
+    w[L * (R - 1)] = nxt;
+    for (int j1 = R - 2; j1 >= 0; j1 -= TRI_CH) {
+        T fv[TRI_CH], cv[TRI_CH], bv[TRI_CH];
+#pragma unroll
+        for (int q = 0; q < TRI_CH; ++q)
+            if (j1 - q >= 0) { fv[q] = w[L * (j1 - q)]; cv[q] = cc[L * (j1 - q)]; bv[q] = bp[L * (j1 - q)]; }
+#pragma unroll
+        for (int q = 0; q < TRI_CH; ++q)
+            if (j1 - q >= 0) {
+                nxt = (fv[q] - cv[q] * nxt) / bv[q];
+                w[L * (j1 - q)] = nxt;
+            }
+    }
+}
+
 // Neumann ghost copies of CELL fields: the ghost takes the nearest interior value, which is
 // the net effect of the reference's two loops (e.g. PhSolve.f90:88-96, dct_fftw.f90:175-183).
 __global__ void k_fill_neumann(int nr, int nz, double* a, double* b, ull* ctr) {
@@ -2585,6 +2642,15 @@ void launch_ch_fin(const DevParams& P, const double* x, const double* f2, const 
     k_ch_fin<<<GRID((long)P.nr * P.nz)>>>(P, x, f2, M0, rmu_after, ph_after, ctr);
     launch_fill_neumann(P.nr, P.nz, rmu_after, ph_after, ctr, s);
 }
+template <typename T>
+void launch_tridiag(const TriBlock<T>& b0, const TriBlock<T>& b1, const KState* ks, int gate, ull* ctr, cudaStream_t s) {
+    const int n = b0.len + b1.len;
+    k_tridiag<T><<<(n + 63) / 64, 64, 0, s>>>(b0, b1, ks, gate, ctr);
+}
+template void launch_tridiag<double>(const TriBlock<double>&, const TriBlock<double>&, const KState*, int, ull*,
+                                     cudaStream_t);
+template void launch_tridiag<float>(const TriBlock<float>&, const TriBlock<float>&, const KState*, int, ull*,
+                                    cudaStream_t);
 void launch_fill_neumann(int nr, int nz, double* a, double* b, ull* ctr, cudaStream_t s) {
     k_fill_neumann<<<GRID(2L * (nr + 2) + 2L * nz)>>>(nr, nz, a, b, ctr);
 }

@@ -65,6 +65,18 @@ void launch_ch_matvec(const OpScal<T>& o, const T* M0, const T* Mi, T alpha, con
 void launch_ch_fin(const DevParams& P, const double* x, const double* f2, const double* M0, double* rmu_after,
                    double* ph_after, ull* ctr, cudaStream_t s);
 
+// ---- ESOLP_x tridiagonal stage (microfluidics_complex_domain/ESOLP.f90) --------------------
+// One block of an ESOLP_x momentum vector: `rows` rows of `len` values, row j mode k at
+// w[k + len*j]; the precomputed Thomas factors (multiplier, pivot, super-diagonal) likewise.
+template <typename T>
+struct TriBlock {
+    int len, rows;
+    const T *rm, *bp, *cc;
+    T* w;
+};
+template <typename T>
+void launch_tridiag(const TriBlock<T>& b0, const TriBlock<T>& b1, const KState* ks, int gate, ull* ctr, cudaStream_t s);
+
 // ---- PhSolve_ori (microfluidics_complex_domain/PhSolve_ori.f90), finit's wall smoothing ---
 void launch_ori_rhs(const DevParams& P, const double* ph, const double* f2, const double* cfb, const double* cft,
                     double alpha_s, double* b, double* x, double* pnb, double* pnt, ull* ctr, cudaStream_t s);

@@ -59,6 +59,12 @@ struct drd_ctx {
     double *f1xe, *f1xo, *f1ze, *f1zo;
     float *f1xe32, *f1xo32, *f1ze32, *f1zo32;
     int Kx = 0, Kz = 0, Nxe = 0, Nxo = 0, Mze = 0, Mzo = 0;
+    // ESOLP_x momentum preconditioner: folded DCT-I of length nr+1 for the u block (the v
+    // block's length nr reuses f1xe/f1xo), Thomas factors per bdf [rm|bp|c of u, rm|bp|c of v]
+    // and a momentum-length scratch vector
+    double *f1ue, *f1uo, *es64[2], *esw;
+    float *f1ue32, *f1uo32, *es32[2], *esw32;
+    int Ku = 0, Nue = 0, Nuo = 0;
     double *cfB, *cfT;
     // resident state and scratch
     double* fld[DRD_F_COUNT];
@@ -143,6 +149,10 @@ size_t arena_need(long cs, long us, long vs, long nc, long nr, long nz, long nma
     add(nr + 1, 8); add(nr + 1, 8);                            // ori_cfb, ori_cft
     add(sizeof(GridBar), 1);                                   // bar
     add(128, 8);                                               // pprof
+    const long fu = (nr / 2 + 1) * (nr / 2 + 2), nes = 3 * (us + vs);
+    add(fu, 8); add(fu, 8); add(fu, 4); add(fu, 4);            // f1ue, f1uo (+ FP32)
+    for (int i = 0; i < 2; ++i) { add(nes, 8); add(nes, 4); }  // es64, es32
+    add(nmax, 8); add(nmax, 4);                                // esw, esw32
     return b + 4096;
 }
 
@@ -204,6 +214,61 @@ void host_tables(const drd_params& P, std::vector<double>& ph_lcc, std::vector<d
             ph_lcc[i + (size_t)j * nr] =
                 1. + P.xld * P.dt * P.s_implicit * temp / P.I_thickness + P.xld * P.I_thickness * P.dt * (temp * temp);
         }
+    }
+}
+
+// ESOLP_x coefficients of setup (Precipitation_dynamics/setup.f90:157-235), factored for the
+// Thomas sweep (rfords) of k_tridiag.  Per mode k of a block with `rows` rows, the system along
+// j has sub-diagonal a_j, diagonal b_j = t1 m + (2 dt/dz^2 + fmx_k) (m = 1.5 for bdf 2, the
+// *_2 set), super-diagonal c_j; the u block's wall rows carry (2 - xls) dt/dz^2 with xls =
+// (2 xlsB - dz)/(2 xlsB + dz) for both walls (xlsT = xlsB, slip ratio 1 on the no-slip deck).
+// t1 holds pi/2 when these lines run: the fmx loops before them overwrite the Re-based value
+// (:159, :166-169, :202-205).  Output [rm|bp|c of u ((nr+1) x nz), rm|bp|c of v (nr x (nz-1))],
+// row j of mode k at [k + len*j]; rm_j = -a_j / b'_{j-1}, b'_j = b_j + rm_j c_{j-1}, b'_0 = b_0.
+void host_esolp(const drd_params& P, int bdf, std::vector<double>& out) {
+    const int nr = P.nr, nz = P.nz;
+    const double dt = P.dt, dr2 = P.dr * P.dr, dz2 = P.dz * P.dz, dz = P.dz;
+    const double m = (bdf == 2) ? 1.5 : 1.0;
+    double xls = P.xlsB * (1.0 + 1.0) / 2.0;
+    xls = (2.0 * xls - dz) / (2.0 * xls + dz);
+    const long mu = (long)(nr + 1) * nz, mv = (long)nr * (nz - 1);
+    out.assign(3 * (mu + mv), 0.0);
+    auto factor = [&](int len, int rows, double* base, const std::vector<double>& a, const std::vector<double>& b,
+                      const std::vector<double>& cc, int k) {
+        double* rm = base;
+        double* bp = base + (long)len * rows;
+        double* cv = base + 2L * len * rows;
+        double piv = b[0];
+        rm[k] = 0.0;
+        bp[k] = piv;
+        cv[k] = cc[0];
+        for (int j = 1; j < rows; ++j) {
+            const double r = -a[j] / piv;
+            piv = b[j] + r * cc[j - 1];
+            rm[k + (long)len * j] = r;
+            bp[k + (long)len * j] = piv;
+            cv[k + (long)len * j] = cc[j];
+        }
+    };
+    std::vector<double> a, b, cc;
+    // u block: modes 0..nr of VCOST length nr+1, rows 0..nz-1 (:166-199)
+    const double t1u = kPi * nr / nr / 2.;
+    for (int k = 0; k <= nr; ++k) {
+        const double sk = std::sin(kPi * k / nr / 2.), fmx = 4.0 * dt * sk * sk / dr2;
+        a.assign(nz, -dt / dz2); b.assign(nz, t1u * m + (2.0 * dt / dz2 + fmx)); cc.assign(nz, -dt / dz2);
+        a[0] = 0.0; cc[nz - 1] = 0.0;
+        b[0] = t1u * m + ((2.0 - xls) * dt / dz2 + fmx);
+        b[nz - 1] = t1u * m + ((2.0 - xls) * dt / dz2 + fmx);
+        factor(nr + 1, nz, out.data(), a, b, cc, k);
+    }
+    // v block: modes 0..nr-1 of VCOST length nr, rows 1..nz-1 of v (:202-235)
+    const int rv = nz - 1;
+    const double t1v = kPi * (nr - 1) / (nr - 1) / 2.;
+    for (int k = 0; k < nr; ++k) {
+        const double sk = std::sin(kPi * k / (nr - 1) / 2.), fmx = 4.0 * dt * sk * sk / dr2;
+        a.assign(rv, -dt / dz2); b.assign(rv, t1v * m + 2.0 * dt / dz2 + fmx); cc.assign(rv, -dt / dz2);
+        a[0] = 0.0; cc[rv - 1] = 0.0;
+        factor(nr, rv, out.data() + 3 * mu, a, b, cc, k);
     }
 }
 
@@ -332,6 +397,42 @@ void enq_ch_psolve(drd_ctx* c, const T* x, T* y, const KState* ks, int gate, cud
     launch_gemm<T>(gcfg<T>(c, 1), EPI_STORE, dct1_zpass<T>(c, t1, y, ks, gate), s);
 }
 
+// The row pass of ESOLP_x over one block: VCOST of length L along each of M rows (row
+// stride L), folded like the CH x pass.  L = nr+1 (u block) uses f1ue/f1uo, L = nr (v) f1xe/f1xo.
+template <typename T>
+GemmArgs<T> esolp_rows(drd_ctx* c, int M, int L, const T* X, T* out, const KState* ks, int gate) {
+    const bool u = (L == c->nr + 1);
+    const T* be = u ? (sizeof(T) == 8 ? (const T*)c->f1ue : (const T*)c->f1ue32) : fmat<T>(c, 0);
+    const T* bo = u ? (sizeof(T) == 8 ? (const T*)c->f1uo : (const T*)c->f1uo32) : fmat<T>(c, 1);
+    const int K = u ? c->Ku : c->Kx, Ne = u ? c->Nue : c->Nxe, No = u ? c->Nuo : c->Nxo;
+    GemmArgs<T> a = gargs<T>(c, M, Ne, K, X, L, be, Ne, out, L, ks, gate);
+    a.fold = FOLD_A;
+    a.Lf = L - 1;
+    a.B_odd = bo;
+    a.N_odd = No;
+    return a;
+}
+
+// PSolve_CG with ESOLP_x (Precipitation_dynamics/VeloSolve_combined.f90:800-806, ESOLP.f90):
+// per block (u: nr+1 x nz, v: nr x nz-1 of the packed vector) VCOST along x, a tridiagonal
+// solve along y per x mode, VCOST along x.  Five launches: two row passes, one Thomas sweep
+// over both blocks, two row passes.
+template <typename T>
+void enq_esolp(drd_ctx* c, int bdf, const T* x, T* y, const KState* ks, int gate, cudaStream_t s) {
+    const int nr = c->nr, nz = c->nz;
+    const long mu = (long)(nr + 1) * nz, mv = (long)nr * (nz - 1);
+    T* w = (sizeof(T) == 8) ? (T*)c->esw : (T*)c->esw32;
+    const T* f = (sizeof(T) == 8) ? (const T*)c->es64[bdf - 1] : (const T*)c->es32[bdf - 1];
+    launch_gemm<T>(gcfg<T>(c, 0), EPI_STORE, esolp_rows<T>(c, nz, nr + 1, x, w, ks, gate), s);
+    launch_gemm<T>(gcfg<T>(c, 0), EPI_STORE, esolp_rows<T>(c, nz - 1, nr, x + mu, w + mu, ks, gate), s);
+    const T* fv = f + 3 * mu;
+    TriBlock<T> bu{nr + 1, nz, f, f + mu, f + 2 * mu, w};
+    TriBlock<T> bv{nr, nz - 1, fv, fv + mv, fv + 2 * mv, w + mu};
+    launch_tridiag<T>(bu, bv, ks, gate, c->ctr, s);
+    launch_gemm<T>(gcfg<T>(c, 0), EPI_STORE, esolp_rows<T>(c, nz, nr + 1, w, y, ks, gate), s);
+    launch_gemm<T>(gcfg<T>(c, 0), EPI_STORE, esolp_rows<T>(c, nz - 1, nr, w + mu, y + mu, ks, gate), s);
+}
+
 // ---- generic system operations -------------------------------------------------------------
 struct Sys {
     int kind;
@@ -339,6 +440,7 @@ struct Sys {
     long n;
     int jacobi;  // diagonal preconditioner in k.diag
     int ident;   // identity preconditioner
+    int esolp;   // ESOLP_x preconditioner (momentum)
 };
 
 template <typename T>
@@ -381,6 +483,7 @@ template <typename T>
 void enq_psolve(drd_ctx* c, const Sys& S, const T* x, T* y, const KState* ks, int gate, cudaStream_t s) {
     KVecs<T>& k = vecs(c, (T*)nullptr);
     if (S.kind == SYS_CH || S.kind == SYS_ORI) enq_ch_psolve<T>(c, x, y, ks, gate, s);
+    else if (S.esolp) enq_esolp<T>(c, S.bdf, x, y, ks, gate, s);
     else launch_bi_diag_apply<T>(S.n, x, S.jacobi ? k.diag : nullptr, S.ident, y, ks, gate, c->ctr, s);
 }
 
@@ -397,7 +500,7 @@ template <typename T>
 void enq_bicg_body(drd_ctx* c, const Sys& S, KVecs<T>& k, KState* ks, cudaStream_t s) {
     Dots d = dots(c);
     const long n = S.n;
-    if (S.kind == SYS_CH || S.kind == SYS_ORI) {
+    if (S.kind == SYS_CH || S.kind == SYS_ORI || S.esolp) {
         launch_bi_p<T>(n, k.r, k.v, k.p, k.phat, nullptr, 0, ks, d, c->ctr, s);
         enq_psolve<T>(c, S, k.p, k.phat, ks, G_RUNNING, s);
     } else {
@@ -574,7 +677,7 @@ int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int 
             enq_bicg_iter<double>(c, S, k, ks, h, 1, sb);
         });
         if (rc) return rc;
-    } else if (c->persist && (S.kind == SYS_CH || S.kind == SYS_UV)) {
+    } else if (c->persist && (S.kind == SYS_CH || (S.kind == SYS_UV && !S.esolp))) {
         // the whole mixed solve (FP64 refinement and its FP32 inner solves) in one cooperative
         // launch; it leaves the FP64 true residual of the returned x in the state
         enq_sys_setup<float>(c, S, s);
@@ -640,8 +743,9 @@ Sys sys_of(drd_ctx* c, int kind, int bdf) {
     else {
         S.n = c->nuv;
         const bool tp_ident = (c->P.variant == DRD_VARIANT_TP && bdf == 2);
-        S.jacobi = !tp_ident;
-        S.ident = tp_ident;
+        S.esolp = (c->P.uv_precond == DRD_UV_ESOLP);
+        S.jacobi = !tp_ident && !S.esolp;
+        S.ident = tp_ident && !S.esolp;
     }
     return S;
 }
@@ -908,6 +1012,12 @@ int upload_tables(drd_ctx* c) {
     CK(cudaMemcpy(c->ph_lcc, ph.data(), sizeof(double) * ph.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->pre_lcc, pre.data(), sizeof(double) * pre.size(), cudaMemcpyHostToDevice));
     launch_convert_scale<float, double>(c->nc, c->ph_lcc, 1.0, c->ph_lcc32, nullptr, c->s);
+    for (int bdf = 1; bdf <= 2; ++bdf) {
+        std::vector<double> f;
+        host_esolp(c->P, bdf, f);
+        CK(cudaMemcpy(c->es64[bdf - 1], f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice));
+        launch_convert_scale<float, double>((long)f.size(), c->es64[bdf - 1], 1.0, c->es32[bdf - 1], nullptr, c->s);
+    }
     CK(cudaStreamSynchronize(c->s));
     return DRD_OK;
 }
@@ -962,6 +1072,12 @@ int setup_context(drd_ctx* c) {
     c->ori_cfb = carve<double>(c, nr + 1); c->ori_cft = carve<double>(c, nr + 1);
     c->bar = (GridBar*)carve<char>(c, sizeof(GridBar));
     c->pprof = (unsigned long long*)carve<double>(c, 128);
+    c->Ku = nr / 2 + 1; c->Nue = (nr + 2) / 2; c->Nuo = (nr + 1) / 2;
+    const long fu = (long)c->Ku * c->Nue, nes = 3 * ((long)(nr + 1) * nz + (long)nr * (nz - 1));
+    c->f1ue = carve<double>(c, fu); c->f1uo = carve<double>(c, fu);
+    c->f1ue32 = carve<float>(c, fu); c->f1uo32 = carve<float>(c, fu);
+    for (int b = 0; b < 2; ++b) { c->es64[b] = carve<double>(c, nes); c->es32[b] = carve<float>(c, nes); }
+    c->esw = carve<double>(c, c->nmax); c->esw32 = carve<float>(c, c->nmax);
     if (c->arena_used > c->arena_bytes) { c->err = "arena overflow"; return DRD_ERR_NOMEM; }
     CK(cudaMallocHost(&c->h_ks, KS_COUNT * sizeof(KState)));
     CK(cudaMallocHost(&c->h_ca, sizeof(CallArgs)));
@@ -1008,6 +1124,20 @@ int setup_context(drd_ctx* c) {
         launch_convert_scale<float, double>((long)xo.size(), c->f1xo, 1.0, c->f1xo32, nullptr, c->s);
         launch_convert_scale<float, double>((long)ze.size(), c->f1ze, 1.0, c->f1ze32, nullptr, c->s);
         launch_convert_scale<float, double>((long)zo.size(), c->f1zo, 1.0, c->f1zo32, nullptr, c->s);
+        // ESOLP_x u block: VCOST of length nr+1, the same folded x-pass operands
+        const int L = nr + 1;
+        std::vector<double> g1, g2, g3;
+        host_dct_mats(L, g1, g2, g3);
+        std::vector<double> ue((size_t)c->Ku * c->Nue, 0.0), uo(ue.size(), 0.0);
+        for (int j = 0; j < c->Ku; ++j)
+            for (int n = 0; n < c->Nue; ++n) {
+                ue[(size_t)j * c->Nue + n] = g1[(size_t)(2 * n) * L + j];
+                if (n < c->Nuo) uo[(size_t)j * c->Nue + n] = g1[(size_t)(2 * n + 1) * L + j];
+            }
+        CK(put(c->f1ue, ue));
+        CK(put(c->f1uo, uo));
+        launch_convert_scale<float, double>((long)ue.size(), c->f1ue, 1.0, c->f1ue32, nullptr, c->s);
+        launch_convert_scale<float, double>((long)uo.size(), c->f1uo, 1.0, c->f1uo32, nullptr, c->s);
     }
     std::vector<double> cfa(nr + 1, std::cos(c->P.angle * kPi / 180.0) / std::sqrt(2.0));
     CK(put(c->cfB, cfa));
@@ -1039,6 +1169,7 @@ int validate(const drd_params* p, std::string& why) {
     if (p->ch_maxit <= 0 || p->uv_maxit <= 0 || p->phmu_maxit <= 0) { why = "maxit must be positive"; return DRD_ERR_BADARG; }
     if (p->xlsB >= 1.e-8) { why = "slip walls (xlsB >= 1e-8) have no solve in the reference"; return DRD_ERR_UNSUPPORTED; }
     if (p->guess_mode != 0 && p->guess_mode != 1) { why = "guess_mode must be 0 or 1"; return DRD_ERR_BADARG; }
+    if (p->uv_precond != DRD_UV_JACOBI && p->uv_precond != DRD_UV_ESOLP) { why = "unknown uv_precond"; return DRD_ERR_BADARG; }
     if (p->precision == DRD_PREC_MIXED && (!(p->mixed_inner_tol > 0) || p->mixed_max_refine <= 0)) {
         why = "mixed precision needs mixed_inner_tol > 0 and mixed_max_refine > 0";
         return DRD_ERR_BADARG;
@@ -1612,6 +1743,7 @@ int drd_op_apply(drd_ctx* c, int op, int bdf, int precision, const double* x, do
     if (precision == DRD_OP_PERSISTENT && (kind == SYS_CH || kind == SYS_UV)) {
         // the persistent solver's own operator code: x = op(b) in one cooperative launch
         if (!c->persist) { c->err = "persistent solver not in use: " + c->persist_err; return DRD_ERR_UNSUPPORTED; }
+        if (S.esolp) { c->err = "the persistent momentum solver applies Jacobi only"; return DRD_ERR_UNSUPPORTED; }
         KVecs<float>& f = c->k32;
         enq_sys_setup<float>(c, S, c->s);
         launch_convert_scale<float, double>(n, k.tmp, 1.0, f.b, c->ctr, c->s);

@@ -47,6 +47,11 @@ extern "C" {
 #define DRD_PREC_MIXED 1 /* FP32 operators and preconditioners inside FP64 iterative
                             refinement; FP64 inner products and true-residual recompute  */
 
+/* Momentum preconditioners (drd_params.uv_precond). */
+#define DRD_UV_JACOBI 0 /* PSolve_uv_2_CG (microfluidics_complex_domain/VeloSolve_2_combined.f90:649-711) */
+#define DRD_UV_ESOLP 1  /* ESOLP_x: DCT-I along x, tridiagonal along y (microfluidics_complex_domain/
+                           ESOLP.f90:1-82, applied in Precipitation_dynamics/VeloSolve_combined.f90:795-808) */
+
 /* Return codes besides BiCGSTAB INFO values. */
 #define DRD_OK 0
 #define DRD_ERR_BADARG (-100)
@@ -94,7 +99,8 @@ typedef struct drd_params {
     double bdr_ph_used_adjust;     /* TP: 1e-6 (TP/finit.f90:572)                                  */
     double mixed_inner_tol;        /* mixed mode: relative residual reduction per FP32 inner solve */
     int32_t mixed_max_refine;      /* mixed mode: maximum FP64 refinement sweeps                   */
-    int32_t reserved1;
+    int32_t uv_precond;            /* momentum preconditioner: DRD_UV_JACOBI (the MF reference) or  */
+                                   /* DRD_UV_ESOLP (ESOLP_x, used by the PD application)             */
 } drd_params;
 
 typedef struct drd_status {

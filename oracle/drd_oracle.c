@@ -1012,6 +1012,108 @@ void orc_uv_psolve(const drd_params* P, int bdf, const double* rho, const double
         }
 }
 
+/* ---------------------------------------------------------------------------------------
+ * ESOLP_x preconditioner of the momentum system: DCT-I (VCOST) along x, a tridiagonal solve
+ * along y per x mode, DCT-I along x (microfluidics_complex_domain/ESOLP.f90:1-82), with the
+ * coefficients ua..vc of setup (setup.f90:157-235) and the Thomas solver rfords
+ * (Precipitation_dynamics/setup.f90:327-354).  The reference applies it to the u and v blocks
+ * of the momentum vector in Precipitation_dynamics/VeloSolve_combined.f90:795-808.
+ * ------------------------------------------------------------------------------------- */
+/* rfords: forward elimination on copies of b and f, then back substitution into ff. */
+static void rfords(int n, double* ff, const double* a, const double* bb, const double* c) {
+    double* b = dalloc(n);
+    double* f = dalloc(n);
+    memcpy(b, bb, sizeof(double) * n);
+    memcpy(f, ff, sizeof(double) * n);
+    for (int j = 1; j < n; ++j) {
+        const double r = -a[j] / b[j - 1];
+        b[j] = b[j] + r * c[j - 1];
+        f[j] = f[j] + r * f[j - 1];
+    }
+    if (fabs(b[n - 1]) <= 1.0E-12) ff[n - 1] = 0.0;
+    else ff[n - 1] = f[n - 1] / b[n - 1];
+    for (int j = n - 2; j >= 0; --j) ff[j] = (f[j] - c[j] * ff[j + 1]) / b[j];
+    free(b);
+    free(f);
+}
+
+/* setup()'s ua, ub, uc (nz rows x (nr+1) modes) and va, vb, vc ((nz-1) x nr), element
+ * (row j, mode k) at [j + rows*k]; bdf 2 takes the *_2 set (mass term 1.5 t1).  t1 is pi/2:
+ * the fmx loops overwrite it before use (setup.f90:159,166-169,202-205).  The slip lengths
+ * enter through (2 xls_ave - dz)/(2 xls_ave + dz) with xlsT = xlsB (the no-slip deck). */
+void orc_esolp_coefs(const drd_params* P, int bdf, double* ua, double* ub, double* uc, double* va, double* vb,
+                     double* vc) {
+    const int nr = P->nr, nz = P->nz;
+    const double dt = P->dt, dr2 = P->dr * P->dr, dz2 = P->dz * P->dz, dz = P->dz;
+    const double kPiG = kPi; /* global.f90:27 */
+    double t1 = 0.0, xls = P->xlsB * (1.0 + 1.0) / 2.0;
+    xls = (2.0 * xls - dz) / (2.0 * xls + dz);
+    const double m = (bdf == 2) ? 1.5 : 1.0;
+    double* fmx = dalloc(nr + 1);
+    for (int i = 0; i <= nr; ++i) {
+        t1 = kPiG * i / nr / 2.;
+        fmx[i] = 4.0 * dt * sin(t1) * sin(t1) / dr2;
+    }
+    for (int k = 0; k <= nr; ++k) {
+        for (int j = 0; j < nz; ++j) {
+            const long q = j + (long)nz * k;
+            if (j == 0) {
+                ua[q] = 0.0;
+                ub[q] = t1 * m + ((2.0 - xls) * dt / dz2 + fmx[k]);
+                uc[q] = (-1.0 * dt / dz2);
+            } else if (j == nz - 1) {
+                ua[q] = (-1.0 * dt / dz2);
+                ub[q] = t1 * m + ((2.0 - xls) * dt / dz2 + fmx[k]);
+                uc[q] = 0.0;
+            } else {
+                ua[q] = (-dt / dz2);
+                ub[q] = t1 * m + (2.0 * dt / dz2 + fmx[k]);
+                uc[q] = (-dt / dz2);
+            }
+        }
+    }
+    for (int i = 0; i < nr; ++i) {
+        t1 = kPiG * i / (nr - 1) / 2.;
+        fmx[i] = 4.0 * dt * sin(t1) * sin(t1) / dr2;
+    }
+    const int nv = nz - 1;
+    for (int k = 0; k < nr; ++k)
+        for (int j = 0; j < nv; ++j) {
+            const long q = j + (long)nv * k;
+            va[q] = (j == 0) ? 0.0 : -dt / dz2;
+            vb[q] = t1 * m + 2.0 * dt / dz2 + fmx[k];
+            vc[q] = (j == nv - 1) ? 0.0 : -1.0 * dt / dz2;
+        }
+    free(fmx);
+}
+
+/* ESOLP_x on one block: `rows` rows of `len` values (row j, element k at [k + len*j]), in place. */
+static void esolp_block(int len, int rows, double* w, const double* pa, const double* pb, const double* pc) {
+    orc_vcost(len, rows, w, len, 1); /* along x, one sequence per row (ESOLP.f90:21-30) */
+    double* col = dalloc(rows);
+    for (int k = 0; k < len; ++k) { /* tridiagonal along y per mode (:36-57) */
+        for (int j = 0; j < rows; ++j) col[j] = w[k + (long)len * j];
+        rfords(rows, col, pa + (long)rows * k, pb + (long)rows * k, pc + (long)rows * k);
+        for (int j = 0; j < rows; ++j) w[k + (long)len * j] = col[j];
+    }
+    free(col);
+    orc_vcost(len, rows, w, len, 1); /* (:64-73) */
+}
+
+/* The ESOLP_x preconditioner on a packed momentum vector (Atob_uv order). */
+void orc_uv_psolve_esolp(const drd_params* P, int bdf, const double* x, double* y) {
+    const int nr = P->nr, nz = P->nz;
+    const long N = uv_len(nr, nz), mn = (long)(nr + 1) * nz;
+    double* ua = dalloc(mn); double* ub = dalloc(mn); double* uc = dalloc(mn);
+    const long vn = (long)nr * (nz - 1);
+    double* va = dalloc(vn); double* vb = dalloc(vn); double* vc = dalloc(vn);
+    orc_esolp_coefs(P, bdf, ua, ub, uc, va, vb, vc);
+    memcpy(y, x, sizeof(double) * N);
+    esolp_block(nr + 1, nz, y, ua, ub, uc);
+    esolp_block(nr, nz - 1, y + mn, va, vb, vc);
+    free(ua); free(ub); free(uc); free(va); free(vb); free(vc);
+}
+
 typedef struct {
     const drd_params* P; int bdf; const double* rho; const double* eta; const double* pen;
 } uv_ctx;
@@ -1021,7 +1123,8 @@ static void uv_mv_cb(void* c, double a, const double* x, double b, double* y) {
 }
 static void uv_ps_cb(void* c, const double* x, double* y) {
     uv_ctx* C = (uv_ctx*)c;
-    orc_uv_psolve(C->P, C->bdf, C->rho, C->eta, x, y);
+    if (C->P->uv_precond == DRD_UV_ESOLP) orc_uv_psolve_esolp(C->P, C->bdf, x, y);
+    else orc_uv_psolve(C->P, C->bdf, C->rho, C->eta, x, y);
 }
 
 /* VeloSolve_combined (bdf 1) / VeloSolve_2_combined (bdf 2). */

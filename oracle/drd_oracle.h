@@ -95,6 +95,11 @@ void orc_interpolate_coef(const drd_params* P, const double* dist, const double*
 
 double orc_mass(const drd_params* P, const double* ph);
 
+/* ESOLP_x momentum preconditioner (microfluidics_complex_domain/ESOLP.f90, setup.f90:157-235). */
+void orc_esolp_coefs(const drd_params* P, int bdf, double* ua, double* ub, double* uc, double* va, double* vb,
+                     double* vc);
+void orc_uv_psolve_esolp(const drd_params* P, int bdf, const double* x, double* y);
+
 /* PhSolve_ori and finit's wall smoothing (microfluidics_complex_domain/PhSolve_ori.f90,
  * finit.f90:120-189).  angleB/angleT may be NULL (zeros, as during finit's loop). */
 double orc_ori_coef(const drd_params* P, double alpha_s);

@@ -53,6 +53,8 @@ def lib(openmp=False):
         L.orc_ch_psolve.argtypes = [P, dp, dp, dp]
         L.orc_uv_matvec.argtypes = [P, C.c_int, dp, dp, dp, C.c_double, dp, C.c_double, dp]
         L.orc_uv_psolve.argtypes = [P, C.c_int, dp, dp, dp, dp]
+        L.orc_uv_psolve_esolp.argtypes = [P, C.c_int, dp, dp]
+        L.orc_esolp_coefs.argtypes = [P, C.c_int, dp, dp, dp, dp, dp, dp]
         L.orc_phmu_matvec.argtypes = [P, dp, dp, dp, C.c_double, C.c_double, C.c_double, dp, C.c_double, dp]
         L.orc_phmu_psolve.argtypes = [P, dp, dp]
         L.orc_ch_system.argtypes = [P, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp]
@@ -156,6 +158,20 @@ class Oracle:
         y = np.zeros_like(x)
         self.L.orc_uv_psolve(C.byref(self.P), bdf, ptr(rho), ptr(eta), ptr(np.ascontiguousarray(x)), ptr(y))
         return y
+
+    def uv_psolve_esolp(self, bdf, x):
+        """ESOLP_x on a packed momentum vector (Precipitation_dynamics/VeloSolve_combined.f90:800-806)."""
+        y = np.zeros_like(x)
+        self.L.orc_uv_psolve_esolp(C.byref(self.P), bdf, ptr(np.ascontiguousarray(x)), ptr(y))
+        return y
+
+    def esolp_coefs(self, bdf):
+        """(ua, ub, uc) as (nr+1, nz) arrays [mode, row] and (va, vb, vc) as (nr, nz-1)."""
+        nr, nz = self.P.nr, self.P.nz
+        u = [np.zeros((nr + 1) * nz) for _ in range(3)]
+        v = [np.zeros(nr * (nz - 1)) for _ in range(3)]
+        self.L.orc_esolp_coefs(C.byref(self.P), bdf, *[ptr(a) for a in u + v])
+        return [a.reshape(nr + 1, nz) for a in u], [a.reshape(nr, nz - 1) for a in v]
 
     def phmu_matvec(self, M0, Mi, used, x, coef_bot=1.0, coef_top=1.0, alpha=1.0, beta=0.0, y=None):
         y = np.zeros_like(x) if y is None else np.array(y, dtype=np.float64)
