@@ -1845,6 +1845,54 @@ __device__ __forceinline__ void slot_put(double* part, int slot, double v, doubl
     if (threadIdx.x == 0) part[slot * DRD_MAXB + blockIdx.x] = r;
 }
 
+// GB300 issues FP64 at a small fraction of its FP32 rate, so in the hot loop of the persistent
+// solver the FP64 work of the reductions is kept to one warp: each thread accumulates its
+// products in FP32, each warp sums its lanes in FP32, and only the warp sums (and the grid's
+// block partials) are added in FP64.  The scalar steps of an iteration are evaluated by thread 0
+// and broadcast through shared memory instead of by every thread.
+//
+// Grid sum of one partials slot by warp 0 (each lane its strided share in order, then an xor
+// butterfly: every lane of every block gets the same bits).  Call from warp 0 only.
+__device__ __forceinline__ double warp_slot_sum(const double* part, int slot) {
+    const int lane = threadIdx.x & 31;
+    double v = 0.0;
+    for (int q = lane; q < (int)gridDim.x; q += 32) v += __ldcg(part + slot * DRD_MAXB + q);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block partials of up to three per-thread FP32 values into part[slot][block] (slot < 0: none).
+template <int NT>
+__device__ __forceinline__ void slots_put_f(double* part, int sl0, float v0, int sl1, float v1, int sl2, float v2,
+                                            double* sm) {
+    constexpr int NW = NT / 32;
+    static_assert(3 * NW <= 64, "shared scratch");
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int sl[3] = {sl0, sl1, sl2};
+    float v[3] = {v0, v1, v2};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        if (sl[i] >= 0)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    __syncthreads();  // an earlier sum may still read sm
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) sm[i * NW + w] = (double)v[i];
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (sl[i] < 0) continue;
+            double r = lane < NW ? sm[i * NW + lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+            if (lane == 0) part[sl[i] * DRD_MAXB + blockIdx.x] = r;
+        }
+    }
+}
+
 constexpr int PB_NT = 512;  // threads per block of the persistent solver
 constexpr int PB_BM = 32, PB_BN = 32, PB_KC = 224;  // x-pass tile and K chunk (JA = 14)
 constexpr int PB_CW = 4;                            // columns per z work item
@@ -2134,21 +2182,20 @@ __device__ bool pb_matvec_ch(const PersistArgs& a, const float* x, float* y, flo
     const ChFF1<float, PackedCG<float>> F{PackedCG<float>{x, nr}, CellA<float>{a.M0, nr}, nr, nz, a.o.dtxld,
                                           a.o.idr2, a.o.idz2};
     CellA<float> Mi{a.Mi, nr};
-    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    float s1 = 0.f, s2 = 0.f, s3 = 0.f;
     for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < n; q += stride) {
-        const int i = (int)(q % nr), k = (int)(q / nr);
+        const int qi = (int)q, k = qi / nr, i = qi - k * nr;
         const float f = F(i, k);
         const float av = __ldcg(x + q) + (a.o.s * f / a.o.eps - a.o.eps * op_dgn<float>(i, k, nr, nz, a.o.idr2,
                                                                                         a.o.idz2, F, Mi));
         const float yn = yin ? alpha * av + __ldcg(yin + q) : alpha * av;
         y[q] = yn;
-        if (d1) s1 += (double)__ldcg(d1 + q) * (double)yn;
-        if (self2) s2 += (double)yn * (double)yn;
-        if (d3) s3 += (double)__ldcg(d3 + q) * (double)yn;
+        if (d1) s1 = fmaf(__ldcg(d1 + q), yn, s1);
+        if (self2) s2 = fmaf(yn, yn, s2);
+        if (d3) s3 = fmaf(__ldcg(d3 + q), yn, s3);
     }
-    if (d1) slot_put<PB_NT>(a.part, slot1, s1, sm);
-    if (self2) slot_put<PB_NT>(a.part, slot2, s2, sm);
-    if (d3) slot_put<PB_NT>(a.part, slot3, s3, sm);
+    if (d1 || self2 || d3)
+        slots_put_f<PB_NT>(a.part, d1 ? slot1 : -1, s1, self2 ? slot2 : -1, s2, d3 ? slot3 : -1, s3, sm);
     return true;
 }
 
@@ -2159,7 +2206,7 @@ __device__ bool pb_matvec_uv(const PersistArgs& a, const float* x, float* y, flo
     const long mn = (long)(a.nr + 1) * a.nz;
     const long stride = (long)gridDim.x * PB_NT;
     UVFetch<float, true> F{x, a.nr, a.nz, mn, a.o.lr_neumann};
-    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    float s1 = 0.f, s2 = 0.f, s3 = 0.f;
     // two rows per pass, both computed before either is stored, so their loads overlap
     for (long q = blockIdx.x * (long)PB_NT + threadIdx.x; q < a.n; q += 2 * stride) {
         const long q2 = q + stride;
@@ -2172,13 +2219,12 @@ __device__ bool pb_matvec_uv(const PersistArgs& a, const float* x, float* y, flo
         const float g1 = d3 ? __ldcg(d3 + q) : 0.f, g2 = (d3 && two) ? __ldcg(d3 + q2) : 0.f;
         y[q] = y1;
         if (two) y[q2] = y2;
-        if (d1) s1 += (double)e1 * (double)y1 + (double)e2 * (double)y2;
-        if (self2) s2 += (double)y1 * (double)y1 + (double)y2 * (double)y2;
-        if (d3) s3 += (double)g1 * (double)y1 + (double)g2 * (double)y2;
+        if (d1) s1 = fmaf(e2, y2, fmaf(e1, y1, s1));
+        if (self2) s2 = fmaf(y2, y2, fmaf(y1, y1, s2));
+        if (d3) s3 = fmaf(g2, y2, fmaf(g1, y1, s3));
     }
-    if (d1) slot_put<PB_NT>(a.part, slot1, s1, sm);
-    if (self2) slot_put<PB_NT>(a.part, slot2, s2, sm);
-    if (d3) slot_put<PB_NT>(a.part, slot3, s3, sm);
+    if (d1 || self2 || d3)
+        slots_put_f<PB_NT>(a.part, d1 ? slot1 : -1, s1, self2 ? slot2 : -1, s2, d3 ? slot3 : -1, s3, sm);
     return true;
 }
 
@@ -2223,11 +2269,13 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
     const long q0 = blockIdx.x * (long)PB_NT + threadIdx.x;
     bool ok = true;
     double rho = rho_first;
+    __shared__ double s_sc[4];  // scalars evaluated by thread 0, read by the block
     st.iter = 0;
     while (true) {
         st.rho = rho;
         st.iter += 1;
         pf.p = (a.prof != nullptr && st.iter == 3 && pf.k == 0) ? a.prof : nullptr;  // time iteration 3 once
+        if (pf.p != nullptr && blockIdx.x == 0 && threadIdx.x == 0) pf.p[123] = gtimer();
         if (fabs(st.rho) < kBreakTol) { st.info = -10; break; }  // (:261-263)
         if constexpr (KIND == PK_CH) {
             if (!(ok = pb_psolve(a, a.p, a.phat, smem, gen, pf))) break;     // PHAT = M^-1 P
@@ -2235,12 +2283,16 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         }
         if (!(ok = pb_matvec<KIND>(a, a.phat, a.v, 1.f, nullptr, a.rtld, 4, false, 0, sm, gen, pf))) break;  // V = A PHAT
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
-        const double rv = slot_sum<PB_NT>(a.part, 4, sm);
-        st.alpha = st.rho / rv;  // (:307)
+        if (threadIdx.x < 32) {
+            const double rv = warp_slot_sum(a.part, 4);
+            if (threadIdx.x == 0) s_sc[0] = st.rho / rv;  // ALPHA (:307)
+        }
+        __syncthreads();
+        st.alpha = s_sc[0];
         {
             // S = R - ALPHA V (:311-312), ||S||^2 and (rtld, S); two elements per pass
             const float na = (float)(-st.alpha);
-            double s2 = 0.0, rs = 0.0;
+            float s2 = 0.f, rs = 0.f;
             for (long q = q0; q < n; q += 2 * stride) {
                 const long q2 = q + stride;
                 const bool two = q2 < n;
@@ -2250,18 +2302,22 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
                 const float sv1 = ra + na * va, sv2 = rb + na * vb;
                 a.r[q] = sv1;
                 if (two) a.r[q2] = sv2;
-                s2 += (double)sv1 * (double)sv1 + (double)sv2 * (double)sv2;
-                rs += (double)ta * (double)sv1 + (double)tb * (double)sv2;
+                s2 = fmaf(sv2, sv2, fmaf(sv1, sv1, s2));
+                rs = fmaf(tb, sv2, fmaf(ta, sv1, rs));
                 if constexpr (KIND == PK_UV) {  // SHAT = M^-1 S, fused
                     a.shat[q] = pb_pre(a, q, sv1);
                     if (two) a.shat[q2] = pb_pre(a, q2, sv2);
                 }
             }
-            slot_put<PB_NT>(a.part, 5, s2, sm);
-            slot_put<PB_NT>(a.part, 2, rs, sm);
+            slots_put_f<PB_NT>(a.part, 5, s2, 2, rs, -1, 0.f, sm);
         }
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
-        st.snorm = sqrt(slot_sum<PB_NT>(a.part, 5, sm));
+        if (threadIdx.x < 32) {
+            const double ss = warp_slot_sum(a.part, 5);
+            if (threadIdx.x == 0) s_sc[1] = sqrt(ss);
+        }
+        __syncthreads();
+        st.snorm = s_sc[1];
         if (st.snorm <= tol) {  // early absolute test (:313-316): X = X + ALPHA PHAT
             st.resid = st.snorm / bnrm2;
             st.info = 0;
@@ -2277,17 +2333,27 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         // T = A SHAT with (t, s), (t, t) and (rtld, t)
         if (!(ok = pb_matvec<KIND>(a, a.shat, a.t, 1.f, nullptr, a.r, 6, true, 7, sm, gen, pf, a.rtld, 1))) break;
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
-        const double2 tst = slot_sum2<PB_NT>(a.part, 6, 7, sm);
-        const double2 rst = slot_sum2<PB_NT>(a.part, 2, 1, sm);
-        st.omega = tst.x / tst.y;                           // (:349-350)
-        const double rho_new = rst.x - st.omega * rst.y;    // (rtld, S - OMEGA T)
-        st.beta = (rho_new / st.rho) * (st.alpha / st.omega);  // (:269) for the next iteration
+        if (threadIdx.x < 32) {
+            const double ts = warp_slot_sum(a.part, 6), tt = warp_slot_sum(a.part, 7);
+            const double rs = warp_slot_sum(a.part, 2), rt = warp_slot_sum(a.part, 1);
+            if (threadIdx.x == 0) {
+                const double om = ts / tt;                                // (:349-350)
+                const double rn = rs - om * rt;                           // (rtld, S - OMEGA T)
+                s_sc[0] = om;
+                s_sc[1] = rn;
+                s_sc[2] = (rn / st.rho) * (st.alpha / om);                // (:269) for the next iteration
+            }
+        }
+        __syncthreads();
+        st.omega = s_sc[0];
+        const double rho_new = s_sc[1];
+        st.beta = s_sc[2];
         {
             // X = X + ALPHA PHAT + OMEGA SHAT, R = S - OMEGA T (:354-359), ||R||^2, and the next
             // P = BETA (P - OMEGA V) + R (:273-275); two elements per pass, loads before stores
             const float al = (float)st.alpha, om = (float)st.omega, nom = (float)(-st.omega);
             const float bt = (float)st.beta;
-            double r2 = 0.0;
+            float r2 = 0.f;
             for (long q = q0; q < n; q += 2 * stride) {
                 const long q2 = q + stride;
                 const bool two = q2 < n;
@@ -2318,12 +2384,17 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
                     a.phat[q] = pb_pre(a, q, pva);
                     if (two) a.phat[q2] = pb_pre(a, q2, pvb);
                 }
-                r2 += (double)rva * (double)rva + (double)rvb * (double)rvb;
+                r2 = fmaf(rvb, rvb, fmaf(rva, rva, r2));
             }
-            slot_put<PB_NT>(a.part, 0, r2, sm);
+            slots_put_f<PB_NT>(a.part, 0, r2, -1, 0.f, -1, 0.f, sm);
         }
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
-        st.resid = sqrt(slot_sum<PB_NT>(a.part, 0, sm)) / bnrm2;  // STOPTEST2 (:361-362)
+        if (threadIdx.x < 32) {
+            const double r2 = warp_slot_sum(a.part, 0);
+            if (threadIdx.x == 0) s_sc[3] = sqrt(r2) / bnrm2;  // STOPTEST2 (:361-362)
+        }
+        __syncthreads();
+        st.resid = s_sc[3];
         if (!isfinite(st.resid)) { st.info = DRD_ERR_NONFINITE; break; }
         if (st.resid <= tol) { st.info = 0; break; }
         if (st.iter >= maxit) { st.info = 1; break; }
@@ -2384,7 +2455,7 @@ __device__ bool pb_residual64(const PersistArgs& a, bool with_b, double* sm, uns
 template <int KIND>
 __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
     extern __shared__ __align__(16) float smem[];
-    __shared__ double sm[32];
+    __shared__ double sm[64];
     count_launch(a.ctr);
     unsigned gen = 0u;  // arrivals counted so far (the counter is zeroed before the launch)
     const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
@@ -2569,6 +2640,15 @@ __global__ void k_bar_reset(GridBar* b, ull* ctr) {
     }
 }
 void launch_bar_reset(GridBar* b, ull* ctr, cudaStream_t s) { k_bar_reset<<<1, 32, 0, s>>>(b, ctr); }
+// %globaltimer at the start (end = 0) or end (end = 1) of a solve of the kernel-per-phase path
+__global__ void k_stamp(KState* ks, int end, ull* ctr) {
+    count_launch(ctr);
+    if (threadIdx.x == 0) {
+        if (end) ks->t_end = gtimer();
+        else ks->t_begin = gtimer();
+    }
+}
+void launch_stamp(KState* ks, int end, ull* ctr, cudaStream_t s) { k_stamp<<<1, 32, 0, s>>>(ks, end, ctr); }
 // Shared-memory plan (offsets in floats) of the persistent CH solver for an nr x nz grid run by
 // `grid` blocks within `budget` bytes: a work area (x-pass panels or z-pass columns), then the
 // resident z-pass operands and the block's x-pass B panel where they fit.

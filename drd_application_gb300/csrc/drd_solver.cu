@@ -81,6 +81,10 @@ struct drd_ctx {
     double ori_alpha = 0.0;
     // persistent cooperative inner solver (FP32 CH): grid size, barrier state, on/off
     int persist = 0, pgrid = 0;
+    int persist_ch = 0;  // the CH solve too: only when its transform operands stay in shared memory
+    // mixed mode: the CH system is too stiff for FP32 Krylov vectors and is solved in FP64
+    int ch_fp64 = 0;
+    double ch_stiff = 0.0;
     PbPlan pplan{};
     GridBar* bar = nullptr;
     std::string persist_err;
@@ -635,6 +639,11 @@ int setup_persist(drd_ctx* c) {
     }
     c->pgrid = grid;
     c->persist = 1;
+    // Past the resident plan (more x-pass tiles than blocks, streamed operands) the persistent CH
+    // solve is slower than the kernel-per-phase loop's tuned GEMMs: 2048x1024 took about 10 ms
+    // per FP32 iteration against 2 ms.
+    c->persist_ch = c->pplan.b_res && c->pplan.z_res;
+    if (!c->persist_ch) c->persist_err = "CH: the grid exceeds the resident shared-memory plan; the CH solve uses the kernel-per-phase loop";
     const char* pe = std::getenv("DRD_PERSIST_PROF");
     c->pprof_on = pe && std::atoi(pe) != 0;
     return DRD_OK;
@@ -670,6 +679,9 @@ int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int 
     KVecs<double>& k = c->k64;
     Dots d = dots(c);
     int rc = DRD_OK;
+    const bool persistent =
+        mixed && c->persist && ((S.kind == SYS_CH && c->persist_ch) || (S.kind == SYS_UV && !S.esolp));
+    if (!persistent) launch_stamp(ks, 0, c->ctr, s);
     if (!mixed) {
         enq_sys_setup<double>(c, S, s);
         enq_bicg_setup<double>(c, S, k, ks, tol, maxit, nullptr, s);
@@ -677,7 +689,7 @@ int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int 
             enq_bicg_iter<double>(c, S, k, ks, h, 1, sb);
         });
         if (rc) return rc;
-    } else if (c->persist && (S.kind == SYS_CH || (S.kind == SYS_UV && !S.esolp))) {
+    } else if (persistent) {
         // the whole mixed solve (FP64 refinement and its FP32 inner solves) in one cooperative
         // launch; it leaves the FP64 true residual of the returned x in the state
         enq_sys_setup<float>(c, S, s);
@@ -730,6 +742,7 @@ int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int 
     launch_copy<double>(S.n, k.b, k.tmp, c->ctr, s);
     enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.tmp, nullptr, 1, -1, nullptr, G_ALWAYS, s);
     launch_bi_true_resid(ks, d, c->ctr, s);
+    launch_stamp(ks, 1, c->ctr, s);
     return DRD_OK;
 }
 
@@ -751,6 +764,8 @@ Sys sys_of(drd_ctx* c, int kind, int bdf) {
 }
 
 int mixed_of(drd_ctx* c) { return c->P.precision == DRD_PREC_MIXED; }
+// Whether the solve that reports into status slot `slot` runs mixed (the CH slot may not).
+int mixed_for(drd_ctx* c, int slot) { return mixed_of(c) && !(slot == KS_CH && c->ch_fp64); }
 
 // PhSolve (microfluidics_complex_domain/PhSolve.f90:1-126) on fld[U,V,PH,RMU] -> rmu_after, ph_after.
 // extrap: take 2 rmu - rmu_pre as the initial guess (drd_step with guess_mode 1).
@@ -759,7 +774,7 @@ int enq_ch(drd_ctx* c, cudaStream_t s, int extrap = 0) {
     launch_ch_f2(P, c->fld[DRD_F_U], c->fld[DRD_F_V], c->fld[DRD_F_PH], c->f2, c->ctr, s);
     launch_ch_rhs(P, c->fld[DRD_F_PH], c->fld[DRD_F_RMU], extrap ? c->fld[DRD_F_RMU_PRE] : nullptr, c->bdr, c->grad,
                   c->Mi, c->f2, c->k64.b, c->k64.x, c->ctr, s);
-    int rc = enq_solve(c, sys_of(c, SYS_CH, 0), KS_CH, c->P.tol, c->P.ch_maxit, mixed_of(c), s);
+    int rc = enq_solve(c, sys_of(c, SYS_CH, 0), KS_CH, c->P.tol, c->P.ch_maxit, mixed_for(c, KS_CH), s);
     if (rc) return rc;
     launch_ch_fin(P, c->k64.x, c->f2, c->M0, c->rmu_after, c->ph_after, c->ctr, s);
     return DRD_OK;
@@ -772,7 +787,7 @@ int enq_ori(drd_ctx* c, cudaStream_t s) {
     launch_ch_f2(P, c->fld[DRD_F_U], c->fld[DRD_F_V], c->fld[DRD_F_PH], c->f2, c->ctr, s);
     launch_ori_rhs(P, c->fld[DRD_F_PH], c->f2, c->ori_cfb, c->ori_cft, c->ori_alpha, c->k64.b, c->k64.x, c->pnb, c->pnt,
                    c->ctr, s);
-    int rc = enq_solve(c, sys_of(c, SYS_ORI, 0), KS_CH, c->P.tol, c->P.ch_maxit, mixed_of(c), s);
+    int rc = enq_solve(c, sys_of(c, SYS_ORI, 0), KS_CH, c->P.tol, c->P.ch_maxit, mixed_for(c, KS_CH), s);
     if (rc) return rc;
     const double cb = ori_coef(c);
     launch_ori_fin(P, c->k64.x, c->pnb, c->pnt, cb, cb, c->ph_after, c->rmu_after, c->ctr, s);
@@ -971,14 +986,16 @@ int run_graph(drd_ctx* c, long key, const std::function<int(cudaStream_t)>& buil
     return DRD_OK;
 }
 
-void fill_status(const KState& k, drd_status* st, int mixed, double secs) {
+void fill_status(drd_ctx* c, int slot, const KState& k, drd_status* st, double secs) {
     if (!st) return;
+    const int mixed = mixed_for(c, slot);
     st->info = k.info;
     st->iter = mixed ? k.inner_total : k.iter;
     st->resid = k.resid;
     st->true_resid = k.true_resid;
     st->refinements = mixed ? k.outer : 0;
     st->flags = k.flags;
+    if (mixed_of(c) && !mixed) st->flags |= DRD_FLAG_FALLBACK64;
     st->seconds = secs;
 }
 
@@ -1006,9 +1023,24 @@ int refresh_fp32(drd_ctx* c) {
     return DRD_OK;
 }
 
+// FP32 rounding of the preconditioned direction, |z| 2^-24 spread over all modes by the last
+// DCT-I (a length-K sum: about sqrt(K) roundings), comes back multiplied by the CH operator's
+// largest eigenvalue, which the table's largest entry estimates.  Measured on GB300: with this
+// estimate at 0.004 (420x180), 0.031, 0.040 and 0.069 the mixed CH solves reach 1e-8; at 0.169
+// (1400x600) and 0.42 (2048x1024) the FP64 refinement stalls or diverges.  Above 0.1 the mixed
+// mode solves the CH system with the FP64 solver.
+constexpr double kChStiffLimit = 0.1;
+double ch_stiffness(const drd_ctx* c, const std::vector<double>& ph_lcc) {
+    double lmax = 0.0;
+    for (double v : ph_lcc) lmax = std::max(lmax, v);
+    return std::ldexp(1.0, -24) * std::sqrt((double)std::max(c->Kx, c->Kz)) * lmax;
+}
+
 int upload_tables(drd_ctx* c) {
     std::vector<double> ph, pre;
     host_tables(c->P, ph, pre);
+    c->ch_stiff = ch_stiffness(c, ph);
+    c->ch_fp64 = c->ch_stiff > kChStiffLimit;
     CK(cudaMemcpy(c->ph_lcc, ph.data(), sizeof(double) * ph.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->pre_lcc, pre.data(), sizeof(double) * pre.size(), cudaMemcpyHostToDevice));
     launch_convert_scale<float, double>(c->nc, c->ph_lcc, 1.0, c->ph_lcc32, nullptr, c->s);
@@ -1185,7 +1217,7 @@ int finish_call(drd_ctx* c, int slot, drd_status* st, bool has_solve) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     if (has_solve) {
-        fill_status(c->h_ks[slot], st, mixed_of(c), ms * 1e-3);
+        fill_status(c, slot, c->h_ks[slot], st, ms * 1e-3);
         return c->h_ks[slot].info;
     }
     if (st) { memset(st, 0, sizeof(*st)); st->seconds = ms * 1e-3; }
@@ -1701,12 +1733,11 @@ int drd_step(drd_ctx* c, int first, double t, drd_step_stats* stats) {
     CK(cudaGetLastError());
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-    const int mixed = mixed_of(c);
-    // a solve's own device time: the persistent solver stamps %globaltimer at its start and end
+    // a solve's own device time: %globaltimer stamps at its start and end
     auto solve_s = [](const KState& k) { return k.t_end > k.t_begin ? 1e-9 * (double)(k.t_end - k.t_begin) : 0.0; };
-    const KState& kch = c->h_ks[c->P.variant == DRD_VARIANT_TP ? KS_PHMU : KS_CH];
-    fill_status(kch, &stats->ch, mixed, solve_s(kch));
-    fill_status(c->h_ks[KS_UV], &stats->uv, mixed, solve_s(c->h_ks[KS_UV]));
+    const int sch = c->P.variant == DRD_VARIANT_TP ? KS_PHMU : KS_CH;
+    fill_status(c, sch, c->h_ks[sch], &stats->ch, solve_s(c->h_ks[sch]));
+    fill_status(c, KS_UV, c->h_ks[KS_UV], &stats->uv, solve_s(c->h_ks[KS_UV]));
     stats->seconds = ms * 1e-3;
     memset(&stats->pre, 0, sizeof(stats->pre));
     stats->mass = *c->h_mass;

@@ -18,6 +18,9 @@ Workloads:
         3 rigid fibers of 40x4 cells at seeded poses, two drops of radius 15 cells,
         viscosity ratio 5, Re 0.5, Ca 0.05.
   "tp"  the two_phase_flow_complex_domain variant (phi in [-1,1], ph_mu_solve, sharp penalty).
+  "c5"  2048x1024 serpentine channel (amplitude 150, period 680 cells, half-width 0.35 nz),
+        64 rigid fibers of 60x6 cells and 32 drops of radius U(20, 60) cells at seeded
+        positions in the channel, viscosity ratio 10, Re 1, Ca 0.02, dr = dz = 1/512.
 Any workload can be built at another grid size; geometry lengths scale with the grid.
 """
 import math
@@ -54,6 +57,52 @@ def _rect_sdf(x, y, cx, cy, half_l, half_w, ang):
     outside = np.sqrt(np.maximum(qx, 0.0) ** 2 + np.maximum(qy, 0.0) ** 2)
     inside = np.minimum(np.maximum(qx, qy), 0.0)
     return outside + inside
+
+
+def _c5_channel(rng, p, nr, nz, X, Z, bdr, meta):
+    """Serpentine walls (amplitude 150, period 680 cells at 2048x1024, scaled with the grid) and
+    64 rigid 60x6-cell fibers at seeded poses inside the channel."""
+    sx, sz = nr / 2048.0, nz / 1024.0
+    dr, dz = p.dr, p.dz
+    xi = np.arange(nr) + 0.5
+    zk = np.arange(nz) + 0.5
+    phase = rng.uniform(0, 2 * math.pi)
+    amp, period, half = 150.0 * sz, 680.0 * sx, 0.35 * nz
+    yc = nz / 2.0 + amp * np.sin(2 * math.pi * xi / period + phase)
+    slope = amp * 2 * math.pi / period * np.cos(2 * math.pi * xi / period + phase)
+    d_cells = (half - np.abs(zk[:, None] - yc[None, :])) / np.sqrt(1.0 + slope[None, :] ** 2)
+    smooth = max(2.0 * min(sx, sz), 0.75)
+    bdr[1:-1, 1:-1] = 0.5 * (1.0 - np.tanh(d_cells / smooth))
+    neumann_ghosts_cell(bdr)
+    p.bdr_low = (yc[0] - half) * dz
+    p.bdr_upp = (yc[0] + half) * dz
+    sdf = np.full((nz, nr), np.inf)
+    fibers = []
+    for f in range(64):
+        cxc = rng.uniform(0, nr)
+        ic = int(min(max(round(cxc - 0.5), 0), nr - 1))
+        czc = yc[ic] + rng.uniform(-0.7, 0.7) * half
+        ang = rng.uniform(0, math.pi)
+        fibers.append((cxc, czc, ang))
+        sdf = np.minimum(sdf, _rect_sdf(X / dr, Z / dz, cxc, czc, 30.0 * sx, 3.0 * sz, ang))
+    meta.update(phase=phase, amp=amp, period=period, half=half, fibers=fibers)
+    return bdr, sdf * min(dr, dz), yc, half
+
+
+def _c5_drops(rng, ph, nr, nz, dr, dz, eps, X, Z, yc, half, meta):
+    """32 drops of radius U(20, 60) cells (scaled with the grid) inside the channel."""
+    s = min(nr / 2048.0, nz / 1024.0)
+    drops = []
+    h = min(dr, dz)
+    for j in range(32):
+        R = rng.uniform(20.0, 60.0) * s
+        cxd = rng.uniform(0, nr)
+        ic = int(min(max(round(cxd), 0), nr - 1))
+        czd = yc[ic] + rng.uniform(-0.6, 0.6) * half
+        drops.append((cxd, czd, R))
+        d = np.sqrt((X / dr - cxd) ** 2 + (Z / dz - czd) ** 2) * h
+        ph[1:-1, 1:-1] = np.maximum(ph[1:-1, 1:-1], 0.5 * (1.0 + np.tanh((R * h - d) / (math.sqrt(2.0) * eps))))
+    meta["drops"] = drops
 
 
 def interpolate_coef_host(params, dist, bdr_ph):
@@ -116,6 +165,12 @@ def make_case(name="c2", seed=0, nr=None, nz=None, precision=abi.DRD_PREC_FP64, 
         p.dr, p.dz = slen / nr, shig / nz
         p.dt = 1.0e-3
         p.bdr_low, p.bdr_upp = 0.0, shig
+    elif name == "c5":
+        nr = nr or 2048
+        nz = nz or 1024
+        p = abi.default_params(nr, nz, re=1.0, ca=0.02, lambda_rho=1.0, lambda_eta=10.0, penalty_k=1.0e4)
+        p.dr, p.dz = 4.0 / nr, 2.0 / nz
+        p.dt = min(p.dr, p.dz) * 0.1
     elif name in ("c2", "tp"):
         nr = nr or (420 if name == "c2" else 128)
         nz = nz or (180 if name == "c2" else 128)
@@ -137,6 +192,8 @@ def make_case(name="c2", seed=0, nr=None, nz=None, precision=abi.DRD_PREC_FP64, 
     dist = np.full((nz, nr), 10.0)  # no particles: far away
     meta = {"seed": seed, "nr": nr, "nz": nz}
     sx, sz = nr / 420.0, nz / 180.0
+    if name == "c5":
+        bdr, dist, yc, half = _c5_channel(rng, p, nr, nz, X, Z, bdr, meta)
     if name in ("c2", "tp"):
         phase = rng.uniform(0, 2 * math.pi)
         amp, period, half = 30.0 * sz, 140.0 * sx, 45.0 * sz
@@ -185,7 +242,9 @@ def make_case(name="c2", seed=0, nr=None, nz=None, precision=abi.DRD_PREC_FP64, 
     fpd, rho, eta = interpolate_coef_host(p, dist, bdr)
     # phase field: drops (phi = 1 inside), clipped by the solid (finit.f90:288)
     ph = np.zeros(cell_shape(nr, nz))
-    if name == "c1":
+    if name == "c5":
+        _c5_drops(rng, ph, nr, nz, dr, dz, eps, X, Z, yc, half, meta)
+    elif name == "c1":
         R = 12.0 * sz
         cx = nr / 2.0 + rng.uniform(-2, 2)
         cz = nz / 2.0 + rng.uniform(-2, 2)

@@ -66,7 +66,8 @@ extern "C" {
 #define DRD_FLAG_EARLY_S 1u      /* stopped at the absolute ||s|| <= tol test (BiCGSTABREVCOM.f:313) */
 #define DRD_FLAG_EARLY_X0 2u     /* stopped at the absolute ||b - A x0|| <= tol test (:248)          */
 #define DRD_FLAG_REFINED 4u      /* mixed mode: result produced by FP64 iterative refinement         */
-#define DRD_FLAG_FALLBACK64 8u   /* mixed mode: refinement stalled; finished with the FP64 solver   */
+#define DRD_FLAG_FALLBACK64 8u   /* mixed mode: the CH system is too stiff for FP32 vectors (the    */
+                                 /* grid's stiffness estimate); it was solved with the FP64 solver */
 
 /*
  * Scalars that the reference keeps in `module global` and the input deck
