@@ -1765,6 +1765,11 @@ __device__ __forceinline__ unsigned long long gtimer() {
 __device__ __forceinline__ void pb_mark(const PbProf& pf, int i) {
     if (pf.p != nullptr && pf.k <= 1 && blockIdx.x == 0 && threadIdx.x == 0) pf.p[124 + i] = gtimer();
 }
+// Sub-phase mark of the first z pass of a timed iteration, p[100 + i].
+__device__ __forceinline__ void pb_markz(const PbProf* pf, int i) {
+    if (pf != nullptr && pf->p != nullptr && pf->k == 1 && blockIdx.x == 0 && threadIdx.x == 0)
+        pf->p[100 + i] = gtimer();
+}
 
 __device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
@@ -1894,7 +1899,11 @@ __device__ __forceinline__ void slots_put_f(double* part, int sl0, float v0, int
 }
 
 constexpr int PB_NT = 512;  // threads per block of the persistent solver
-constexpr int PB_BM = 32, PB_BN = 32, PB_KC = 224;  // x-pass tile and K chunk (JA = 14)
+// x-pass tile and K chunk (JA = 7 operand loads per thread).  A wide, short tile: every block
+// whose tile covers a row reloads that row, so short tiles cut the operand traffic per SM, which
+// bounds the load phase; 420x180 gives 12 x 8 = 96 tiles.
+constexpr int PB_BM = 16, PB_BN = 64, PB_KC = 224;
+constexpr int PB_AG = PB_BM / 4;  // float4 groups of an A row
 constexpr int PB_CW = 4;                            // columns per z work item
 
 // Shared-memory plan of the persistent CH solver (floats; see persist_ch_plan): the z-pass
@@ -1945,15 +1954,19 @@ __device__ void pb_load_resident(const PersistArgs& a, float* smem) {
 // a 4 x 4 register tile and reads its operands as float4 (two 16-byte shared loads per 16 FMA),
 // and the eight partial tiles are summed through shared memory in a fixed order.
 constexpr int PB_KG = 8;  // K groups of the x pass
-__device__ __forceinline__ int pb_swz(int k, int m) { return k * PB_BM + ((((m >> 2) ^ (k & 7)) << 2) | (m & 3)); }
+__device__ __forceinline__ int pb_swz(int k, int m) {
+    return k * PB_BM + ((((m >> 2) ^ (k & (PB_AG - 1))) << 2) | (m & 3));
+}
+static_assert((PB_BM / 4) * (PB_BN / 4) * PB_KG == PB_NT, "4 x 4 register tiles, PB_KG groups");
 __device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float* smem, const PbProf& pf) {
     const int M = a.nz, L = a.nr - 1, K = a.Kx;
     int mt, nt0;
     const int ntiles = pb_xtiles(a, mt, nt0);
-    float* At = smem + a.work_off;              // [PB_KC][PB_BM], float4 groups swizzled by k
-    float* Bw = At + PB_KC * PB_BM;             // [PB_KC][PB_BN] when B is not resident
-    float* red = Bw + PB_KC * PB_BN;            // [PB_KG][PB_BM * PB_BN]
-    const int tid = threadIdx.x, g = tid >> 6, t = tid & 63, mi = t >> 3, ni = t & 7;
+    float* At = smem + a.work_off;                        // [PB_KC][PB_BM], float4 groups swizzled by k
+    float* Bw = At + PB_KC * PB_BM;                       // [PB_KC][PB_BN] when B is not resident
+    float* red = Bw + (a.b_res ? 0 : PB_KC * PB_BN);      // [PB_KG][PB_BM * PB_BN]
+    constexpr int TN = PB_BN / 4;                         // threads of a K group along n
+    const int tid = threadIdx.x, g = tid >> 6, t = tid & 63, mi = t / TN, ni = t % TN;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int mtile = tile % mt, nrest = tile / mt;
         const int par = nrest >= nt0 ? 1 : 0;
@@ -2020,7 +2033,7 @@ __device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float
             __syncthreads();
             const int kgn = (kc + PB_KG - 1) / PB_KG, kb = g * kgn, ke = min(kb + kgn, kc);
             for (int kk = kb; kk < ke; ++kk) {
-                const float4 av = *reinterpret_cast<const float4*>(At + kk * PB_BM + ((mi ^ (kk & 7)) << 2));
+                const float4 av = *reinterpret_cast<const float4*>(At + kk * PB_BM + ((mi ^ (kk & (PB_AG - 1))) << 2));
                 const float4 bv = *reinterpret_cast<const float4*>(Bk + kk * PB_BN + (ni << 2));
                 const float ar[4] = {av.x, av.y, av.z, av.w}, br[4] = {bv.x, bv.y, bv.z, bv.w};
 #pragma unroll
@@ -2105,7 +2118,8 @@ __device__ __forceinline__ void pb_zcols(const PersistArgs& a, const float* xs, 
 
 // Column pass along z (columns are independent along z): what = 0: out = Cz ((Cz X) / L);
 // 1: out = (Cz X) / L; 2: out = Cz X.
-__device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* smem, int what = 0) {
+__device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* smem, int what = 0,
+                       const PbProf* pf = nullptr) {
     const int nz = a.nz, nr = a.nr, K = a.Kz;
     float* xs = smem + a.work_off;    // [nz][CW]
     float* u = xs + nz * PB_CW;       // [2][CW][Kz4]
@@ -2120,20 +2134,25 @@ __device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* 
             xs[e] = col < nr ? __ldcg(X + (long)row * nr + col) : 0.f;
         }
         __syncthreads();
+        pb_markz(pf, 0);
         pb_zcols(a, xs, u, ys, zA);
+        pb_markz(pf, 1);
         if (what != 2) {
             for (int e = threadIdx.x; e < nz * PB_CW; e += PB_NT) {
                 const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
                 xs[e] = col < nr ? ys[e] / __ldg(a.lcc + (long)row * nr + col) : 0.f;
             }
             __syncthreads();
+            pb_markz(pf, 2);
             if (what == 0) pb_zcols(a, xs, u, ys, zA);
+            pb_markz(pf, 3);
         }
         const float* res = what == 1 ? xs : ys;
         for (int e = threadIdx.x; e < nz * PB_CW; e += PB_NT) {
             const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
             if (col < nr) out[(long)row * nr + col] = res[e];
         }
+        pb_markz(pf, 4);
     }
 }
 
@@ -2151,7 +2170,7 @@ __device__ bool pb_psolve(const PersistArgs& a, const float* x, float* y, float*
     }
     pb_xpass(a, x, a.w1, smem, pf);
     if (!grid_sync(a.bar, gen, pf)) return false;
-    pb_zdz(a, a.w1, a.w2, smem);
+    pb_zdz(a, a.w1, a.w2, smem, 0, &pf);
     if (!grid_sync(a.bar, gen, pf)) return false;
     pb_xpass(a, a.w2, y, smem, pf);
     return true;
@@ -2656,25 +2675,32 @@ PbPlan persist_ch_plan(int nr, int nz, int grid, size_t budget) {
     PbPlan p{};
     const int Kx = (nr - 1) / 2 + 1, Nxe = (nr + 1) / 2, Nxo = nr / 2;
     const int Kz = (nz - 1) / 2 + 1, Mze = (nz + 1) / 2;
-    const size_t xwork = (size_t)PB_KC * PB_BM + (size_t)PB_KC * PB_BN + (size_t)PB_KG * PB_BM * PB_BN;
+    // x-pass work: A chunk and the K-group partial tiles, plus a B chunk when B is streamed
+    const size_t xres = (size_t)PB_KC * PB_BM + (size_t)PB_KG * PB_BM * PB_BN;
+    const size_t xstr = xres + (size_t)PB_KC * PB_BN;
     const int Kz4 = (Kz + 3) & ~3;
     const size_t zwork = (size_t)nz * PB_CW * 2 + (size_t)2 * Kz4 * PB_CW;
     auto up4 = [](size_t v) { return (v + 3) & ~(size_t)3; };  // float4-aligned offsets
-    size_t used = up4(xwork > zwork ? xwork : zwork);
-    p.work_off = 0;
     const size_t zres = (size_t)2 * Mze * Kz4;
+    const int mt = (nz + PB_BM - 1) / PB_BM;
+    const int ntiles = mt * ((Nxe + PB_BN - 1) / PB_BN + (Nxo + PB_BN - 1) / PB_BN);
+    const size_t bres = (size_t)Kx * PB_BN;
+    p.work_off = 0;
+    // preferred: the z operands and the block's own B panel resident for the whole solve
+    const size_t w = up4(xres > zwork ? xres : zwork);
+    if (ntiles <= grid && (up4(w + zres) + bres) * sizeof(float) <= budget) {
+        p.z_res = 1;
+        p.z_off = (long)w;
+        p.b_res = 1;
+        p.b_off = (long)up4(w + zres);
+        p.bytes = ((size_t)p.b_off + bres) * sizeof(float);
+        return p;
+    }
+    size_t used = up4(xstr > zwork ? xstr : zwork);
     if ((used + zres) * sizeof(float) <= budget) {
         p.z_res = 1;
         p.z_off = (long)used;
         used = up4(used + zres);
-    }
-    const int mt = (nz + PB_BM - 1) / PB_BM;
-    const int ntiles = mt * ((Nxe + PB_BN - 1) / PB_BN + (Nxo + PB_BN - 1) / PB_BN);
-    const size_t bres = (size_t)Kx * PB_BN;
-    if (ntiles <= grid && (used + bres) * sizeof(float) <= budget) {
-        p.b_res = 1;
-        p.b_off = (long)used;
-        used += bres;
     }
     p.bytes = used * sizeof(float);
     return p;
