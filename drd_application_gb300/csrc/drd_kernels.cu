@@ -2086,6 +2086,76 @@ __device__ __forceinline__ void pb_zcols(const PersistArgs& a, const float* xs, 
         u[(PB_CW + c) * K4 + j] = u1;
     }
     __syncthreads();
+    if (zA) {
+        // resident operands: a register-tiled product.  Work item = (parity, 4 output rows, one
+        // of ZKS slices of K); each thread forms the 4 x PB_CW partial sums of its slice from
+        // float4 reads (8 shared loads per 64 FMA), and the ZKS slices of a tile, consecutive
+        // lanes of one warp, are summed by a reduce-scatter of shuffles in a fixed order.
+        constexpr int ZKS = 8;
+        static_assert(PB_CW == 4, "4 x 4 register tile");
+        const int NJ4 = K4 / 4, JC = (NJ4 + ZKS - 1) / ZKS;
+        const int G = (a.Mze + 3) / 4, W = 2 * G * ZKS;
+        const int lane = tid & 31, ks = lane & (ZKS - 1);
+        for (int base = 0; base < W; base += PB_NT) {  // uniform trip count: every lane shuffles
+            const int w = base + tid;
+            const bool valid = w < W;
+            const int tile = w / ZKS, par = valid ? tile / G : 0, m0 = (valid ? tile % G : 0) * 4;
+            float v[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[i] = 0.f;
+            if (valid) {
+                const float4* U4 = reinterpret_cast<const float4*>(u + par * PB_CW * K4);
+                const float4* A4 = reinterpret_cast<const float4*>(zA + (long)par * a.Mze * K4);
+                const int jb = ks * JC, je = min(jb + JC, NJ4);
+                for (int j4 = jb; j4 < je; ++j4) {
+                    float4 av[4], uv[4];
+#pragma unroll
+                    for (int r = 0; r < 4; ++r)
+                        av[r] = m0 + r < a.Mze ? A4[(long)(m0 + r) * (K4 / 4) + j4] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) uv[c] = U4[c * (K4 / 4) + j4];
+#pragma unroll
+                    for (int r = 0; r < 4; ++r)
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            float acc = v[r * 4 + c];
+                            acc = fmaf(av[r].x, uv[c].x, acc);
+                            acc = fmaf(av[r].y, uv[c].y, acc);
+                            acc = fmaf(av[r].z, uv[c].z, acc);
+                            acc = fmaf(av[r].w, uv[c].w, acc);
+                            v[r * 4 + c] = acc;
+                        }
+                }
+            }
+            // reduce-scatter over the ZKS lanes: 16 -> 8 -> 4 -> 2 values per lane
+            const bool b2 = ks & 4, b1 = ks & 2, b0 = ks & 1;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const float snd = b2 ? v[i] : v[i + 8], keep = b2 ? v[i + 8] : v[i];
+                v[i] = keep + __shfl_xor_sync(0xffffffffu, snd, 4);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float snd = b1 ? v[i] : v[i + 4], keep = b1 ? v[i + 4] : v[i];
+                v[i] = keep + __shfl_xor_sync(0xffffffffu, snd, 2);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const float snd = b0 ? v[i] : v[i + 2], keep = b0 ? v[i + 2] : v[i];
+                v[i] = keep + __shfl_xor_sync(0xffffffffu, snd, 1);
+            }
+            if (valid) {
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    const int f = (b2 ? 8 : 0) + (b1 ? 4 : 0) + (b0 ? 2 : 0) + i, r = f >> 2, c = f & 3;
+                    const int row = 2 * (m0 + r) + par;
+                    if (row < nz) ys[row * PB_CW + c] = v[i];
+                }
+            }
+        }
+        __syncthreads();
+        return;
+    }
     for (int e = tid; e < nz * PB_CW; e += PB_NT) {
         const int row = e / PB_CW, c = e % PB_CW, par = row & 1, m = row >> 1;
         const float* up = u + (par * PB_CW + c) * K4;
@@ -2129,6 +2199,14 @@ __device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* 
     for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
         const int c0 = ch * PB_CW;
         __syncthreads();
+        // the Ph_Lcc entries of the divide are fetched with the column data (one round trip)
+        constexpr int LP = 4;
+        float lv[LP];
+#pragma unroll
+        for (int i = 0; i < LP; ++i) {
+            const int e = threadIdx.x + i * PB_NT, row = e / PB_CW, col = c0 + e % PB_CW;
+            lv[i] = (what != 2 && e < nz * PB_CW && col < nr) ? __ldg(a.lcc + (long)row * nr + col) : 1.f;
+        }
         for (int e = threadIdx.x; e < nz * PB_CW; e += PB_NT) {
             const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
             xs[e] = col < nr ? __ldcg(X + (long)row * nr + col) : 0.f;
@@ -2138,7 +2216,12 @@ __device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* 
         pb_zcols(a, xs, u, ys, zA);
         pb_markz(pf, 1);
         if (what != 2) {
-            for (int e = threadIdx.x; e < nz * PB_CW; e += PB_NT) {
+#pragma unroll
+            for (int i = 0; i < LP; ++i) {
+                const int e = threadIdx.x + i * PB_NT, col = c0 + e % PB_CW;
+                if (e < nz * PB_CW) xs[e] = col < nr ? ys[e] / lv[i] : 0.f;
+            }
+            for (int e = threadIdx.x + LP * PB_NT; e < nz * PB_CW; e += PB_NT) {
                 const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
                 xs[e] = col < nr ? ys[e] / __ldg(a.lcc + (long)row * nr + col) : 0.f;
             }

@@ -78,6 +78,9 @@ struct drd_ctx {
     double *pts, *pts_old, *totF, *psum, *ppart, *bdist;
     // PhSolve_ori: wall-energy prefactors cf of angleB / angleT (XLINE) and alpha_s
     double *ori_cfb, *ori_cft;
+    // drd_phsolve with guess_mode 1: the rmu of the previous call (the x^(n-1) of the next one)
+    double* rmu_prev;
+    int rmu_prev_ok = 0;
     double ori_alpha = 0.0;
     // persistent cooperative inner solver (FP32 CH): grid size, barrier state, on/off
     int persist = 0, pgrid = 0;
@@ -151,6 +154,7 @@ size_t arena_need(long cs, long us, long vs, long nc, long nr, long nz, long nma
     for (int i = 0; i < 4; ++i) add(2 * DRD_PARTICLES_MAX, 8);  // pts, pts_old, totF, psum
     add(3 * DRD_PARTICLES_MAX * PT_GX, 8); add(cs, 8);          // ppart, bdist
     add(nr + 1, 8); add(nr + 1, 8);                            // ori_cfb, ori_cft
+    add(cs, 8);                                                // rmu_prev
     add(sizeof(GridBar), 1);                                   // bar
     add(128, 8);                                               // pprof
     const long fu = (nr / 2 + 1) * (nr / 2 + 2), nes = 3 * (us + vs);
@@ -1102,6 +1106,7 @@ int setup_context(drd_ctx* c) {
     c->totF = carve<double>(c, 2 * DRD_PARTICLES_MAX); c->psum = carve<double>(c, 2 * DRD_PARTICLES_MAX);
     c->ppart = carve<double>(c, 3 * DRD_PARTICLES_MAX * PT_GX); c->bdist = carve<double>(c, c->cs);
     c->ori_cfb = carve<double>(c, nr + 1); c->ori_cft = carve<double>(c, nr + 1);
+    c->rmu_prev = carve<double>(c, c->cs);
     c->bar = (GridBar*)carve<char>(c, sizeof(GridBar));
     c->pprof = (unsigned long long*)carve<double>(c, 128);
     c->Ku = nr / 2 + 1; c->Nue = (nr + 2) / 2; c->Nuo = (nr + 1) / 2;
@@ -1585,10 +1590,19 @@ int drd_phsolve(drd_ctx* c, const double* u, const double* v, const double* ph, 
     if (!c || !u || !v || !ph || !rmu || !rmu_after || !ph_after) return DRD_ERR_BADARG;
     if (c->P.variant != DRD_VARIANT_MF) { c->err = "PhSolve belongs to the MF variant"; return DRD_ERR_BADARG; }
     CK(cudaEventRecord(c->ev0, c->s));
+    // guess_mode 1: 2 rmu - rmu_prev, rmu_prev being the previous call's rmu (x^(n-1) when the
+    // calls are successive time steps; otherwise only the starting guess is poorer)
+    const int extrap = c->P.guess_mode == 1 && c->rmu_prev_ok;
+    if (extrap)
+        CK(cudaMemcpyAsync(c->fld[DRD_F_RMU_PRE], c->rmu_prev, sizeof(double) * c->cs, cudaMemcpyDeviceToDevice, c->s));
     int rc = up(c, c->fld[DRD_F_U], u, c->us) | up(c, c->fld[DRD_F_V], v, c->vs) | up(c, c->fld[DRD_F_PH], ph, c->cs) |
              up(c, c->fld[DRD_F_RMU], rmu, c->cs);
     if (rc) return DRD_ERR_CUDA;
-    rc = run_graph(c, gkey(GK_CH, mixed_of(c), 0), [&](cudaStream_t s) { return enq_ch(c, s); }, t, 0.0);
+    if (c->P.guess_mode == 1) {
+        CK(cudaMemcpyAsync(c->rmu_prev, c->fld[DRD_F_RMU], sizeof(double) * c->cs, cudaMemcpyDeviceToDevice, c->s));
+        c->rmu_prev_ok = 1;
+    }
+    rc = run_graph(c, gkey(GK_CH, mixed_of(c), extrap), [&](cudaStream_t s) { return enq_ch(c, s, extrap); }, t, 0.0);
     if (rc) return rc;
     rc = down(c, rmu_after, c->rmu_after, c->cs) | down(c, ph_after, c->ph_after, c->cs);
     if (rc) return DRD_ERR_CUDA;
@@ -1633,7 +1647,10 @@ static int velo_common(drd_ctx* c, int bdf, const double* psi1, const double* ps
     if (pf2) rc |= up(c, c->fld[DRD_F_PF2], pf2, c->cs);
     else CK(cudaMemsetAsync(c->fld[DRD_F_PF2], 0, sizeof(double) * c->cs, c->s));
     if (rc) return DRD_ERR_CUDA;
-    rc = run_graph(c, gkey(GK_UV, mixed_of(c), bdf), [&](cudaStream_t s) { return enq_uv(c, bdf, s); }, t, 0.0);
+    // guess_mode 1 (BDF2): the momentum solve starts from 2 u - u_pre, 2 v - v_pre
+    const int extrap = c->P.guess_mode == 1 && bdf == 2;
+    rc = run_graph(c, gkey(GK_UV, mixed_of(c), bdf + 3 * extrap), [&](cudaStream_t s) { return enq_uv(c, bdf, s, extrap); },
+                   t, 0.0);
     if (rc) return rc;
     rc = down(c, u_after, c->u_after, c->us) | down(c, v_after, c->v_after, c->vs);
     const bool dirichlet = !(c->P.variant == DRD_VARIANT_TP && c->P.lr_bd_type == 'n');

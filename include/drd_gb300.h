@@ -82,8 +82,10 @@ typedef struct drd_params {
     int32_t ch_maxit;      /* PhSolve ITER, 500 (PhSolve.f90:72)                                   */
     int32_t uv_maxit;      /* VeloSolve ITER, 800 MF (VeloSolve_2_combined.f90:398), 2000 TP       */
     int32_t phmu_maxit;    /* ph_mu_solve ITER, 5000 (TP/ph_mu_solve.f90:156)                      */
-    int32_t guess_mode;    /* initial guess of drd_step's Krylov solves: 0 = the previous step's   */
-                           /* field (the reference), 1 = linear extrapolation 2 x^n - x^(n-1)     */
+    int32_t guess_mode;    /* initial guess of the CH and momentum solves: 0 = the previous step's */
+                           /* field (the reference), 1 = linear extrapolation 2 x^n - x^(n-1):   */
+                           /* drd_step; drd_velosolve_2_combined from u_pre, v_pre; drd_phsolve  */
+                           /* from the rmu of the context's previous drd_phsolve call            */
     double dr, dz, dt;     /* grid spacing and time step (finit.f90:25-28,397)                    */
     double xld, re, ca;    /* 1/Pe, Reynolds, capillary number (input deck lines 1-3)             */
     double I_thickness;    /* interface thickness epsilon (deck line 18)                           */

@@ -254,6 +254,25 @@ def test_mixed_velosolve_reaches_fp64_tolerance(mf_case):
     ctx.close()
 
 
+def test_drop_in_guess_extrapolation_keeps_the_answer(mf_case):
+    """guess_mode 1 on the per-routine calls: PhSolve starts from 2 rmu - (the previous call's
+    rmu), VeloSolve_2_combined from 2 u - u_pre.  Only the starting guess changes, so at tol
+    1e-12 the answers agree with guess_mode 0 to 1e-9."""
+    case, st, t = mf_case
+    out = []
+    for gm in (0, 1):
+        ctx, _ = _ctx(case, tol=1e-12, guess_mode=gm)
+        ctx.PhSolve(st[F.F_U_PRE], st[F.F_V_PRE], st[F.F_PH_PRE], st[F.F_RMU_PRE], t - case.params.dt)
+        r, p, s1 = ctx.PhSolve(st[F.F_U], st[F.F_V], st[F.F_PH], st[F.F_RMU], t)
+        g = ctx.VeloSolve_2_combined(st[F.F_PSI1], st[F.F_PSI2], st[F.F_U_PRE], st[F.F_U], st[F.F_V_PRE], st[F.F_V],
+                                     st[F.F_P], None, p, None, r, t)
+        assert s1.info == 0 and g[4].info == 0
+        out.append((r, p, g[0], g[1]))
+        ctx.close()
+    for a, b in zip(*out):
+        assert rel_err(b, a) < 1e-9
+
+
 # ------------------------------------------------------------------------------- step sequence
 @pytest.mark.parametrize("precision,guess", [(abi.DRD_PREC_FP64, 0), (abi.DRD_PREC_MIXED, 0), (abi.DRD_PREC_MIXED, 1)])
 def test_step_sequence_matches_oracle(cuda_lib, oracle_build, precision, guess):
