@@ -726,7 +726,9 @@ struct UVFetch {
     }
 };
 
-// Row q of MatrixVector_uv_2_CG (:515-646) / MatrixVector_uv_CG: (A x)_q.
+// Row q of MatrixVector_uv_2_CG (:515-646) / MatrixVector_uv_CG: (A x)_q.  The FP64 form keeps
+// the reference's expression; the FP32 form (the mixed mode's inner operator) takes differences
+// before scaling and multiplies by the reciprocals of dr^2, dz^2 and dr dz instead of dividing.
 template <typename T, class FX>
 __device__ __forceinline__ T uv_apply(const OpScal<T>& o, const T* __restrict__ rho, const T* __restrict__ eta,
                                       const T* __restrict__ pen, const FX& F, long q) {
@@ -737,7 +739,7 @@ __device__ __forceinline__ T uv_apply(const OpScal<T>& o, const T* __restrict__ 
     T val;
 #define E_(i, k) eta[cidx(nr, i, k)]
     if (q < mn) {
-        const int i = (int)(q % (nr + 1)), k = (int)(q / (nr + 1));
+        const int qi = (int)q, k = qi / (nr + 1), i = qi - k * (nr + 1);
         const T f1 = F.ld(q);
         if (o.bdf == 2)
             val = f1 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i - 1, k)]) * h +
@@ -746,19 +748,20 @@ __device__ __forceinline__ T uv_apply(const OpScal<T>& o, const T* __restrict__ 
             val = f1 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i - 1, k)]) * h;
         T cr = E_(i, k), cl = E_(i - 1, k);
         if constexpr (sizeof(T) == 4)
-            val = val - T(2) * o.dt * (cr * (F.Uc(i + 1, k) - f1) + cl * (F.Uc(i - 1, k) - f1)) / o.dr2;
+            val = val - T(2) * o.dt * (cr * (F.Uc(i + 1, k) - f1) + cl * (F.Uc(i - 1, k) - f1)) * o.idr2;
         else
             val = val - T(2) * o.dt * (cr * F.Uc(i + 1, k) + cl * F.Uc(i - 1, k) - (cl + cr) * f1) / o.dr2;
         cr = (E_(i, k + 1) + E_(i - 1, k + 1) + E_(i, k) + E_(i - 1, k)) * q4;
         cl = (E_(i, k) + E_(i - 1, k) + E_(i, k - 1) + E_(i - 1, k - 1)) * q4;
-        if constexpr (sizeof(T) == 4)
-            val = val - o.dt * (cr * (F.U(i, k + 1) - f1) + cl * (F.U(i, k - 1) - f1)) / o.dz2;
-        else
+        if constexpr (sizeof(T) == 4) {
+            val = val - o.dt * (cr * (F.U(i, k + 1) - f1) + cl * (F.U(i, k - 1) - f1)) * o.idz2;
+            val = val - o.dt * (cr * (F.V(i, k + 1) - F.V(i - 1, k + 1)) - cl * (F.V(i, k) - F.V(i - 1, k))) * o.idrdz;
+        } else {
             val = val - o.dt * (cr * F.U(i, k + 1) + cl * F.U(i, k - 1) - (cl + cr) * f1) / o.dz2;
-        val = val - o.dt * (cr * (F.V(i, k + 1) - F.V(i - 1, k + 1)) - cl * (F.V(i, k) - F.V(i - 1, k))) / o.dr / o.dz;
+            val = val - o.dt * (cr * (F.V(i, k + 1) - F.V(i - 1, k + 1)) - cl * (F.V(i, k) - F.V(i - 1, k))) / o.dr / o.dz;
+        }
     } else {
-        const long qv = q - mn;
-        const int i = (int)(qv % nr), k = (int)(qv / nr) + 1;
+        const int qv = (int)(q - mn), kv = qv / nr, i = qv - kv * nr, k = kv + 1;
         const T f2 = F.ld(q);
         if (o.bdf == 2)
             val = f2 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i, k - 1)]) * h +
@@ -767,16 +770,18 @@ __device__ __forceinline__ T uv_apply(const OpScal<T>& o, const T* __restrict__ 
             val = f2 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i, k - 1)]) * h;
         T cr = E_(i, k), cl = E_(i, k - 1);
         if constexpr (sizeof(T) == 4)
-            val = val - T(2) * o.dt * (cr * (F.V(i, k + 1) - f2) + cl * (F.V(i, k - 1) - f2)) / o.dz2;
+            val = val - T(2) * o.dt * (cr * (F.V(i, k + 1) - f2) + cl * (F.V(i, k - 1) - f2)) * o.idz2;
         else
             val = val - T(2) * o.dt * (cr * F.V(i, k + 1) + cl * F.V(i, k - 1) - (cl + cr) * f2) / o.dz2;
         cr = (E_(i + 1, k) + E_(i, k) + E_(i + 1, k - 1) + E_(i, k - 1)) * q4;
         cl = (E_(i, k) + E_(i - 1, k) + E_(i, k - 1) + E_(i - 1, k - 1)) * q4;
-        if constexpr (sizeof(T) == 4)
-            val = val - o.dt * (cr * (F.V(i + 1, k) - f2) + cl * (F.V(i - 1, k) - f2)) / o.dr2;
-        else
+        if constexpr (sizeof(T) == 4) {
+            val = val - o.dt * (cr * (F.V(i + 1, k) - f2) + cl * (F.V(i - 1, k) - f2)) * o.idr2;
+            val = val - o.dt * (cr * (F.Uc(i + 1, k) - F.Uc(i + 1, k - 1)) - cl * (F.Uc(i, k) - F.Uc(i, k - 1))) * o.idrdz;
+        } else {
             val = val - o.dt * (cr * F.V(i + 1, k) + cl * F.V(i - 1, k) - (cl + cr) * f2) / o.dr2;
-        val = val - o.dt * (cr * (F.Uc(i + 1, k) - F.Uc(i + 1, k - 1)) - cl * (F.Uc(i, k) - F.Uc(i, k - 1))) / o.dr / o.dz;
+            val = val - o.dt * (cr * (F.Uc(i + 1, k) - F.Uc(i + 1, k - 1)) - cl * (F.Uc(i, k) - F.Uc(i, k - 1))) / o.dr / o.dz;
+        }
     }
 #undef E_
     return val;
@@ -2385,6 +2390,13 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         }
         if (!(ok = pb_matvec<KIND>(a, a.phat, a.v, 1.f, nullptr, a.rtld, 4, false, 0, sm, gen, pf))) break;  // V = A PHAT
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
+        // S = R - ALPHA V (:311-312), ||S||^2 and (rtld, S).  The loads of this thread's first two
+        // elements do not depend on ALPHA: they are issued before thread 0 evaluates it.
+        const long qa = q0, qb = q0 + stride;
+        const bool ha = qa < n, hb = qb < n;
+        float ra = 0.f, va = 0.f, ta = 0.f, rb = 0.f, vb = 0.f, tb = 0.f;
+        if (ha) { ra = __ldcg(a.r + qa); va = __ldcg(a.v + qa); ta = __ldcg(a.rtld + qa); }
+        if (hb) { rb = __ldcg(a.r + qb); vb = __ldcg(a.v + qb); tb = __ldcg(a.rtld + qb); }
         if (threadIdx.x < 32) {
             const double rv = warp_slot_sum(a.part, 4);
             if (threadIdx.x == 0) s_sc[0] = st.rho / rv;  // ALPHA (:307)
@@ -2392,25 +2404,18 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         __syncthreads();
         st.alpha = s_sc[0];
         {
-            // S = R - ALPHA V (:311-312), ||S||^2 and (rtld, S); two elements per pass
             const float na = (float)(-st.alpha);
             float s2 = 0.f, rs = 0.f;
-            for (long q = q0; q < n; q += 2 * stride) {
-                const long q2 = q + stride;
-                const bool two = q2 < n;
-                const float ra = __ldcg(a.r + q), va = __ldcg(a.v + q), ta = __ldcg(a.rtld + q);
-                const float rb = two ? __ldcg(a.r + q2) : 0.f, vb = two ? __ldcg(a.v + q2) : 0.f;
-                const float tb = two ? __ldcg(a.rtld + q2) : 0.f;
-                const float sv1 = ra + na * va, sv2 = rb + na * vb;
-                a.r[q] = sv1;
-                if (two) a.r[q2] = sv2;
-                s2 = fmaf(sv2, sv2, fmaf(sv1, sv1, s2));
-                rs = fmaf(tb, sv2, fmaf(ta, sv1, rs));
-                if constexpr (KIND == PK_UV) {  // SHAT = M^-1 S, fused
-                    a.shat[q] = pb_pre(a, q, sv1);
-                    if (two) a.shat[q2] = pb_pre(a, q2, sv2);
-                }
-            }
+            auto s_elem = [&](long q, float r, float v, float t) {
+                const float sv = r + na * v;
+                a.r[q] = sv;
+                s2 = fmaf(sv, sv, s2);
+                rs = fmaf(t, sv, rs);
+                if constexpr (KIND == PK_UV) a.shat[q] = pb_pre(a, q, sv);  // SHAT = M^-1 S, fused
+            };
+            if (ha) s_elem(qa, ra, va, ta);
+            if (hb) s_elem(qb, rb, vb, tb);
+            for (long q = q0 + 2 * stride; q < n; q += stride) s_elem(q, __ldcg(a.r + q), __ldcg(a.v + q), __ldcg(a.rtld + q));
             slots_put_f<PB_NT>(a.part, 5, s2, 2, rs, -1, 0.f, sm);
         }
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
@@ -2435,6 +2440,15 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         // T = A SHAT with (t, s), (t, t) and (rtld, t)
         if (!(ok = pb_matvec<KIND>(a, a.shat, a.t, 1.f, nullptr, a.r, 6, true, 7, sm, gen, pf, a.rtld, 1))) break;
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
+        // loads of this thread's first two elements of the X / R / P pass, issued before thread 0
+        // evaluates OMEGA and BETA (they do not depend on them)
+        float ea[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, eb[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        auto xrp_load = [&](long q, float (&e)[7]) {
+            e[0] = __ldcg(a.x + q); e[1] = __ldcg(a.phat + q); e[2] = __ldcg(a.shat + q); e[3] = __ldcg(a.r + q);
+            e[4] = __ldcg(a.t + q); e[5] = __ldcg(a.p + q); e[6] = __ldcg(a.v + q);
+        };
+        if (ha) xrp_load(qa, ea);
+        if (hb) xrp_load(qb, eb);
         if (threadIdx.x < 32) {
             const double ts = warp_slot_sum(a.part, 6), tt = warp_slot_sum(a.part, 7);
             const double rs = warp_slot_sum(a.part, 2), rt = warp_slot_sum(a.part, 1);
@@ -2456,37 +2470,25 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
             const float al = (float)st.alpha, om = (float)st.omega, nom = (float)(-st.omega);
             const float bt = (float)st.beta;
             float r2 = 0.f;
-            for (long q = q0; q < n; q += 2 * stride) {
-                const long q2 = q + stride;
-                const bool two = q2 < n;
-                float xa = __ldcg(a.x + q), pha = __ldcg(a.phat + q), sha = __ldcg(a.shat + q);
-                float sa = __ldcg(a.r + q), tta = __ldcg(a.t + q), pa = __ldcg(a.p + q), vva = __ldcg(a.v + q);
-                float xb = 0.f, phb = 0.f, shb = 0.f, sb = 0.f, ttb = 0.f, pb = 0.f, vvb = 0.f;
-                if (two) {
-                    xb = __ldcg(a.x + q2); phb = __ldcg(a.phat + q2); shb = __ldcg(a.shat + q2);
-                    sb = __ldcg(a.r + q2); ttb = __ldcg(a.t + q2); pb = __ldcg(a.p + q2); vvb = __ldcg(a.v + q2);
-                }
-                float xv = xa + al * pha;
-                xv = xv + om * sha;
-                const float rva = sa + nom * tta;
-                float pva = pa + nom * vva;
-                pva = bt * pva;
-                pva = pva + rva;
-                float xvb = xb + al * phb;
-                xvb = xvb + om * shb;
-                const float rvb = sb + nom * ttb;
-                float pvb = pb + nom * vvb;
-                pvb = bt * pvb;
-                pvb = pvb + rvb;
+            auto xrp = [&](long q, const float (&e)[7]) {
+                float xv = e[0] + al * e[1];
+                xv = xv + om * e[2];
+                const float rv = e[3] + nom * e[4];
+                float pv = e[5] + nom * e[6];
+                pv = bt * pv;
+                pv = pv + rv;
                 a.x[q] = xv;
-                a.r[q] = rva;
-                a.p[q] = pva;
-                if (two) { a.x[q2] = xvb; a.r[q2] = rvb; a.p[q2] = pvb; }
-                if constexpr (KIND == PK_UV) {  // PHAT = M^-1 P of the next iteration, fused
-                    a.phat[q] = pb_pre(a, q, pva);
-                    if (two) a.phat[q2] = pb_pre(a, q2, pvb);
-                }
-                r2 = fmaf(rvb, rvb, fmaf(rva, rva, r2));
+                a.r[q] = rv;
+                a.p[q] = pv;
+                if constexpr (KIND == PK_UV) a.phat[q] = pb_pre(a, q, pv);  // PHAT = M^-1 P of the next iteration
+                r2 = fmaf(rv, rv, r2);
+            };
+            if (ha) xrp(qa, ea);
+            if (hb) xrp(qb, eb);
+            for (long q = q0 + 2 * stride; q < n; q += stride) {
+                float e[7];
+                xrp_load(q, e);
+                xrp(q, e);
             }
             slots_put_f<PB_NT>(a.part, 0, r2, -1, 0.f, -1, 0.f, sm);
         }

@@ -16,6 +16,7 @@ enum Gate : int { G_ALWAYS = 0, G_RUNNING = 1, G_XNZ = 2, G_EARLY_OR_RUNNING = 3
 template <typename T>
 struct OpScal {
     T dt, xld, eps, s, idr2, idz2, dtxld, re, pk, dr, dz, dr2, dz2, adjust;
+    T idrdz;   // 1 / (dr dz): the FP32 momentum operator multiplies where FP64 divides
     T cb, ct;  // ph_mu_solve coef_bot / coef_top
     int nr, nz, variant, lr_neumann, bdf, phi_mode;
 };

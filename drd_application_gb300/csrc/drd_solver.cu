@@ -185,7 +185,7 @@ OpScal<T> make_op(const drd_ctx* c, int bdf) {
     OpScal<T> o{};
     o.dt = (T)d.dt; o.xld = (T)d.xld; o.eps = (T)d.eps; o.s = (T)d.s; o.idr2 = (T)d.idr2; o.idz2 = (T)d.idz2;
     o.dtxld = (T)(d.dt * d.xld); o.re = (T)d.re; o.pk = (T)d.penalty_k; o.dr = (T)d.dr; o.dz = (T)d.dz;
-    o.dr2 = (T)d.dr2; o.dz2 = (T)d.dz2; o.adjust = (T)d.adjust;
+    o.dr2 = (T)d.dr2; o.dz2 = (T)d.dz2; o.adjust = (T)d.adjust; o.idrdz = (T)(1.0 / (d.dr * d.dz));
     const double tmp = d.eps / d.dz;
     o.cb = (T)((d.eps / d.dz) / tmp);  // coef_bot = (I/dz)/tmp (ph_mu_solve.f90:123)
     o.ct = o.cb;
