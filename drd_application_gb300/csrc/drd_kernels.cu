@@ -141,9 +141,11 @@ __device__ __forceinline__ double bulk_mf(double phi, double psi) {
 }
 
 // rhs = -f1 + s f2/eps - eps L_Mi(f2) (:37-48) packed by Atob; x0 = Atob(rmu) (:62-63).
-// With rmu_pre non-NULL the guess is extrapolated: 2 rmu - rmu_pre.
+// With rmu_pre non-NULL the guess is extrapolated: 2 rmu - rmu_pre, and with rmu_pre2 too,
+// quadratically: 3 rmu - 3 rmu_pre + rmu_pre2.
 __global__ void k_ch_rhs(DevParams P, const double* __restrict__ ph, const double* __restrict__ rmu,
-                         const double* __restrict__ rmu_pre, const double* __restrict__ bdr,
+                         const double* __restrict__ rmu_pre, const double* __restrict__ rmu_pre2,
+                         const double* __restrict__ bdr,
                          const double* __restrict__ grad, const double* __restrict__ Mi,
                          const double* __restrict__ f2, double* __restrict__ b, double* __restrict__ x, ull* ctr) {
     count_launch(ctr);
@@ -158,7 +160,7 @@ __global__ void k_ch_rhs(DevParams P, const double* __restrict__ ph, const doubl
         double f1 = P.s * p0 / P.eps - bulk_mf(p0, bdr[c]) / P.eps - p0 * (p0 - 1.0) * grad[c] * P.cang / sq2;
         const double ff = op_dgn<double>(i, k, nr, nz, P.idr2, P.idz2, F, M);
         b[q] = -f1 + P.s * f2[c] / P.eps - P.eps * ff;
-        x[q] = rmu_pre ? 2.0 * rmu[c] - rmu_pre[c] : rmu[c];
+        x[q] = rmu_pre2 ? 3.0 * (rmu[c] - rmu_pre[c]) + rmu_pre2[c] : rmu_pre ? 2.0 * rmu[c] - rmu_pre[c] : rmu[c];
     }
 }
 
@@ -619,7 +621,8 @@ __global__ void k_uv_rhs(DevParams P, int bdf, const CallArgs* __restrict__ ca, 
                          const double* __restrict__ used, const double* __restrict__ ph,
                          const double* __restrict__ rmu, const double* __restrict__ pf1,
                          const double* __restrict__ pf2, double* __restrict__ b, double* __restrict__ x,
-                         double* __restrict__ uL, int extrap, ull* ctr) {
+                         double* __restrict__ uL, int extrap, const double* __restrict__ u_pre2,
+                         const double* __restrict__ v_pre2, ull* ctr) {
     count_launch(ctr);
     const int nr = P.nr, nz = P.nz;
     const long mn = (long)(nr + 1) * nz, N = mn + (long)nr * (nz - 1);
@@ -670,7 +673,8 @@ __global__ void k_uv_rhs(DevParams P, int bdf, const CallArgs* __restrict__ ca, 
                 fu = fu + dt * (2.0 * P.uwT / P.dz2 * etay);
             }
             b[q] = fu;
-            x[q] = extrap ? 2.0 * uu - u_pre[uidx(nr, i, k)] : uu;
+            x[q] = extrap == 2 ? 3.0 * (uu - u_pre[uidx(nr, i, k)]) + u_pre2[uidx(nr, i, k)]
+                   : extrap ? 2.0 * uu - u_pre[uidx(nr, i, k)] : uu;
         } else {
             const long qv = q - mn;
             const int i = (int)(qv % nr), k = (int)(qv / nr) + 1;
@@ -691,7 +695,8 @@ __global__ void k_uv_rhs(DevParams P, int bdf, const CallArgs* __restrict__ ca, 
             fv = fv + (C_(pf2, i, k) + C_(pf2, i, k - 1)) / 2.0;
             fv = fv * dt;
             b[q] = fv;
-            x[q] = extrap ? 2.0 * vv - v_pre[vidx(nr, i, k)] : vv;
+            x[q] = extrap == 2 ? 3.0 * (vv - v_pre[vidx(nr, i, k)]) + v_pre2[vidx(nr, i, k)]
+                   : extrap ? 2.0 * vv - v_pre[vidx(nr, i, k)] : vv;
         }
     }
 #undef UT
@@ -2814,10 +2819,10 @@ void launch_ch_f2(const DevParams& P, const double* u, const double* v, const do
                   cudaStream_t s) {
     k_ch_f2<<<GRID((long)(P.nr + 2) * (P.nz + 2))>>>(P, u, v, ph, f2, ctr);
 }
-void launch_ch_rhs(const DevParams& P, const double* ph, const double* rmu, const double* rmu_pre, const double* bdr,
-                   const double* grad, const double* Mi, const double* f2, double* b, double* x, ull* ctr,
-                   cudaStream_t s) {
-    k_ch_rhs<<<GRID((long)P.nr * P.nz)>>>(P, ph, rmu, rmu_pre, bdr, grad, Mi, f2, b, x, ctr);
+void launch_ch_rhs(const DevParams& P, const double* ph, const double* rmu, const double* rmu_pre,
+                   const double* rmu_pre2, const double* bdr, const double* grad, const double* Mi, const double* f2,
+                   double* b, double* x, ull* ctr, cudaStream_t s) {
+    k_ch_rhs<<<GRID((long)P.nr * P.nz)>>>(P, ph, rmu, rmu_pre, rmu_pre2, bdr, grad, Mi, f2, b, x, ctr);
 }
 template <typename T>
 void launch_ch_matvec(const OpScal<T>& o, const T* M0, const T* Mi, T alpha, const T* x, T beta, T* y, T* ff1,
@@ -2898,10 +2903,10 @@ void launch_uv_rhs(const DevParams& P, int bdf, const CallArgs* ca, const double
                    const double* u_pre, const double* u, const double* v_pre, const double* v, const double* p,
                    const double* rho, const double* eta, const double* bdr, const double* used, const double* ph_after,
                    const double* rmu_after, const double* pf1, const double* pf2, double* b, double* x, double* uL,
-                   int extrap, ull* ctr, cudaStream_t s) {
+                   int extrap, const double* u_pre2, const double* v_pre2, ull* ctr, cudaStream_t s) {
     const long N = (long)(P.nr + 1) * P.nz + (long)P.nr * (P.nz - 1);
     k_uv_rhs<<<GRID(N)>>>(P, bdf, ca, psi1, psi2, u_pre, u, v_pre, v, p, rho, eta, bdr, used, ph_after, rmu_after, pf1,
-                          pf2, b, x, uL, extrap, ctr);
+                          pf2, b, x, uL, extrap, u_pre2, v_pre2, ctr);
 }
 template <typename T>
 void launch_uv_matvec(const OpScal<T>& o, const T* rho, const T* eta, const T* pen, T alpha, const T* x, T beta, T* y,

@@ -79,8 +79,11 @@ struct drd_ctx {
     // PhSolve_ori: wall-energy prefactors cf of angleB / angleT (XLINE) and alpha_s
     double *ori_cfb, *ori_cft;
     // drd_phsolve with guess_mode 1: the rmu of the previous call (the x^(n-1) of the next one)
-    double* rmu_prev;
-    int rmu_prev_ok = 0;
+    double *rmu_prev, *rmu_prev2;
+    int rmu_hist = 0;  // how many of rmu_prev, rmu_prev2 hold earlier calls' rmu
+    // guess_mode 2: the fields two steps back (rmu, u, v), and how many steps of history exist
+    double *rmu_pre2, *u_pre2, *v_pre2;
+    int hist = 0, uv_hist = 0;
     double ori_alpha = 0.0;
     // persistent cooperative inner solver (FP32 CH): grid size, barrier state, on/off
     int persist = 0, pgrid = 0;
@@ -154,7 +157,8 @@ size_t arena_need(long cs, long us, long vs, long nc, long nr, long nz, long nma
     for (int i = 0; i < 4; ++i) add(2 * DRD_PARTICLES_MAX, 8);  // pts, pts_old, totF, psum
     add(3 * DRD_PARTICLES_MAX * PT_GX, 8); add(cs, 8);          // ppart, bdist
     add(nr + 1, 8); add(nr + 1, 8);                            // ori_cfb, ori_cft
-    add(cs, 8);                                                // rmu_prev
+    add(cs, 8); add(cs, 8);                                    // rmu_prev, rmu_prev2
+    add(cs, 8); add(us, 8); add(vs, 8);                        // rmu_pre2, u_pre2, v_pre2
     add(sizeof(GridBar), 1);                                   // bar
     add(128, 8);                                               // pprof
     const long fu = (nr / 2 + 1) * (nr / 2 + 2), nes = 3 * (us + vs);
@@ -772,12 +776,12 @@ int mixed_of(drd_ctx* c) { return c->P.precision == DRD_PREC_MIXED; }
 int mixed_for(drd_ctx* c, int slot) { return mixed_of(c) && !(slot == KS_CH && c->ch_fp64); }
 
 // PhSolve (microfluidics_complex_domain/PhSolve.f90:1-126) on fld[U,V,PH,RMU] -> rmu_after, ph_after.
-// extrap: take 2 rmu - rmu_pre as the initial guess (drd_step with guess_mode 1).
+// extrap: the initial guess is 2 rmu - rmu_pre (1) or 3 rmu - 3 rmu_pre + rmu_pre2 (2).
 int enq_ch(drd_ctx* c, cudaStream_t s, int extrap = 0) {
     const DevParams& P = c->dp;
     launch_ch_f2(P, c->fld[DRD_F_U], c->fld[DRD_F_V], c->fld[DRD_F_PH], c->f2, c->ctr, s);
-    launch_ch_rhs(P, c->fld[DRD_F_PH], c->fld[DRD_F_RMU], extrap ? c->fld[DRD_F_RMU_PRE] : nullptr, c->bdr, c->grad,
-                  c->Mi, c->f2, c->k64.b, c->k64.x, c->ctr, s);
+    launch_ch_rhs(P, c->fld[DRD_F_PH], c->fld[DRD_F_RMU], extrap ? c->fld[DRD_F_RMU_PRE] : nullptr,
+                  extrap == 2 ? c->rmu_pre2 : nullptr, c->bdr, c->grad, c->Mi, c->f2, c->k64.b, c->k64.x, c->ctr, s);
     int rc = enq_solve(c, sys_of(c, SYS_CH, 0), KS_CH, c->P.tol, c->P.ch_maxit, mixed_for(c, KS_CH), s);
     if (rc) return rc;
     launch_ch_fin(P, c->k64.x, c->f2, c->M0, c->rmu_after, c->ph_after, c->ctr, s);
@@ -803,7 +807,7 @@ int enq_phmu(drd_ctx* c, cudaStream_t s, int extrap = 0) {
     const DevParams& P = c->dp;
     launch_phmu_prep(P, c->fld[DRD_F_U], c->fld[DRD_F_V], c->fld[DRD_F_PH], c->bdr, c->used, c->M0, c->f2, c->ctr, s);
     launch_convert_scale<float, double>(c->cs, c->M0, 1.0, c->M032, c->ctr, s);
-    launch_phmu_rhs(P, c->fld[DRD_F_PH], c->fld[DRD_F_RMU], extrap ? c->fld[DRD_F_PH_PRE] : nullptr,
+    launch_phmu_rhs(P, c->fld[DRD_F_PH], c->fld[DRD_F_RMU], extrap ? c->fld[DRD_F_PH_PRE] : nullptr,  // linear only
                     extrap ? c->fld[DRD_F_RMU_PRE] : nullptr, c->bdr, c->grad, c->f2, c->cfB, c->cfT, c->k64.b,
                     c->k64.x, c->pnb, c->pnt, c->ctr, s);
     int rc = enq_solve(c, sys_of(c, SYS_PHMU, 0), KS_PHMU, c->P.tol, c->P.phmu_maxit, mixed_of(c), s);
@@ -814,12 +818,13 @@ int enq_phmu(drd_ctx* c, cudaStream_t s, int extrap = 0) {
 }
 
 // VeloSolve_combined (bdf 1) / VeloSolve_2_combined (bdf 2) -> u_after, v_after.
+// extrap (BDF2 only): the guess is 2 u - u_pre (1) or 3 u - 3 u_pre + u_pre2 (2), v likewise.
 int enq_uv(drd_ctx* c, int bdf, cudaStream_t s, int extrap = 0) {
     const DevParams& P = c->dp;
     double** f = c->fld;
     launch_uv_rhs(P, bdf, c->ca, f[DRD_F_PSI1], f[DRD_F_PSI2], f[DRD_F_U_PRE], f[DRD_F_U], f[DRD_F_V_PRE], f[DRD_F_V],
                   f[DRD_F_P], c->rho, c->eta, c->bdr, c->used, c->ph_after, c->rmu_after, f[DRD_F_PF1], f[DRD_F_PF2],
-                  c->k64.b, c->k64.x, c->uL, extrap && bdf == 2, c->ctr, s);
+                  c->k64.b, c->k64.x, c->uL, bdf == 2 ? extrap : 0, c->u_pre2, c->v_pre2, c->ctr, s);
     int rc = enq_solve(c, sys_of(c, SYS_UV, bdf), KS_UV, c->P.tol, c->P.uv_maxit, mixed_of(c), s);
     if (rc) return rc;
     launch_uv_fin(P, c->k64.x, c->uL, c->u_after, c->v_after, c->ctr, s);
@@ -878,15 +883,20 @@ void enq_particles(drd_ctx* c, int what, const double* u, const double* v, cudaS
 }
 
 // The mcl6 step (microfluidics_complex_domain/mcl6.f90:239-306 first, :378-486 loop).
-int enq_step(drd_ctx* c, int first, cudaStream_t s) {
+// extrap: 0 = x^n, 1 = linear, 2 = quadratic extrapolation of the solves' initial guesses.
+int enq_step(drd_ctx* c, int first, int extrap, cudaStream_t s) {
     double** f = c->fld;
     const size_t cb = sizeof(double) * c->cs, ub = sizeof(double) * c->us, vb = sizeof(double) * c->vs;
-    const int extrap = (!first && c->P.guess_mode == 1);
-    int rc = (c->P.variant == DRD_VARIANT_TP) ? enq_phmu(c, s, extrap) : enq_ch(c, s, extrap);
+    int rc = (c->P.variant == DRD_VARIANT_TP) ? enq_phmu(c, s, extrap != 0) : enq_ch(c, s, extrap);
     if (rc) return rc;
     if (c->pp.np > 0) enq_particles(c, PT_FORCE | PT_MOVE | PT_COEF, f[DRD_F_U], f[DRD_F_V], s);
     rc = enq_uv(c, first ? 1 : 2, s, extrap);
     if (rc) return rc;
+    if (c->P.guess_mode == 2) {  // the fields two steps back, for the next step's guess
+        CK(cudaMemcpyAsync(c->u_pre2, f[DRD_F_U_PRE], ub, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(c->v_pre2, f[DRD_F_V_PRE], vb, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(c->rmu_pre2, f[DRD_F_RMU_PRE], cb, cudaMemcpyDeviceToDevice, s));
+    }
     CK(cudaMemcpyAsync(f[DRD_F_U_PRE], f[DRD_F_U], ub, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(f[DRD_F_V_PRE], f[DRD_F_V], vb, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(f[DRD_F_U], c->u_after, ub, cudaMemcpyDeviceToDevice, s));
@@ -1106,7 +1116,8 @@ int setup_context(drd_ctx* c) {
     c->totF = carve<double>(c, 2 * DRD_PARTICLES_MAX); c->psum = carve<double>(c, 2 * DRD_PARTICLES_MAX);
     c->ppart = carve<double>(c, 3 * DRD_PARTICLES_MAX * PT_GX); c->bdist = carve<double>(c, c->cs);
     c->ori_cfb = carve<double>(c, nr + 1); c->ori_cft = carve<double>(c, nr + 1);
-    c->rmu_prev = carve<double>(c, c->cs);
+    c->rmu_prev = carve<double>(c, c->cs); c->rmu_prev2 = carve<double>(c, c->cs);
+    c->rmu_pre2 = carve<double>(c, c->cs); c->u_pre2 = carve<double>(c, c->us); c->v_pre2 = carve<double>(c, c->vs);
     c->bar = (GridBar*)carve<char>(c, sizeof(GridBar));
     c->pprof = (unsigned long long*)carve<double>(c, 128);
     c->Ku = nr / 2 + 1; c->Nue = (nr + 2) / 2; c->Nuo = (nr + 1) / 2;
@@ -1205,7 +1216,7 @@ int validate(const drd_params* p, std::string& why) {
     if (p->variant == DRD_VARIANT_TP && p->phi_mode != 1 && p->phi_mode != 2) { why = "phi_mode must be 1 or 2"; return DRD_ERR_BADARG; }
     if (p->ch_maxit <= 0 || p->uv_maxit <= 0 || p->phmu_maxit <= 0) { why = "maxit must be positive"; return DRD_ERR_BADARG; }
     if (p->xlsB >= 1.e-8) { why = "slip walls (xlsB >= 1e-8) have no solve in the reference"; return DRD_ERR_UNSUPPORTED; }
-    if (p->guess_mode != 0 && p->guess_mode != 1) { why = "guess_mode must be 0 or 1"; return DRD_ERR_BADARG; }
+    if (p->guess_mode < 0 || p->guess_mode > 2) { why = "guess_mode must be 0, 1 or 2"; return DRD_ERR_BADARG; }
     if (p->uv_precond != DRD_UV_JACOBI && p->uv_precond != DRD_UV_ESOLP) { why = "unknown uv_precond"; return DRD_ERR_BADARG; }
     if (p->precision == DRD_PREC_MIXED && (!(p->mixed_inner_tol > 0) || p->mixed_max_refine <= 0)) {
         why = "mixed precision needs mixed_inner_tol > 0 and mixed_max_refine > 0";
@@ -1590,17 +1601,21 @@ int drd_phsolve(drd_ctx* c, const double* u, const double* v, const double* ph, 
     if (!c || !u || !v || !ph || !rmu || !rmu_after || !ph_after) return DRD_ERR_BADARG;
     if (c->P.variant != DRD_VARIANT_MF) { c->err = "PhSolve belongs to the MF variant"; return DRD_ERR_BADARG; }
     CK(cudaEventRecord(c->ev0, c->s));
-    // guess_mode 1: 2 rmu - rmu_prev, rmu_prev being the previous call's rmu (x^(n-1) when the
-    // calls are successive time steps; otherwise only the starting guess is poorer)
-    const int extrap = c->P.guess_mode == 1 && c->rmu_prev_ok;
-    if (extrap)
-        CK(cudaMemcpyAsync(c->fld[DRD_F_RMU_PRE], c->rmu_prev, sizeof(double) * c->cs, cudaMemcpyDeviceToDevice, c->s));
+    // guess_mode 1 / 2: the guess extrapolates rmu through the rmu of the previous one or two
+    // calls (x^(n-1), x^(n-2) when the calls are successive time steps; otherwise only the
+    // starting guess is poorer)
+    const size_t cb = sizeof(double) * c->cs;
+    const int gm = c->P.guess_mode;
+    const int extrap = std::min(gm, c->rmu_hist);
+    if (extrap >= 1) CK(cudaMemcpyAsync(c->fld[DRD_F_RMU_PRE], c->rmu_prev, cb, cudaMemcpyDeviceToDevice, c->s));
+    if (extrap == 2) CK(cudaMemcpyAsync(c->rmu_pre2, c->rmu_prev2, cb, cudaMemcpyDeviceToDevice, c->s));
     int rc = up(c, c->fld[DRD_F_U], u, c->us) | up(c, c->fld[DRD_F_V], v, c->vs) | up(c, c->fld[DRD_F_PH], ph, c->cs) |
              up(c, c->fld[DRD_F_RMU], rmu, c->cs);
     if (rc) return DRD_ERR_CUDA;
-    if (c->P.guess_mode == 1) {
-        CK(cudaMemcpyAsync(c->rmu_prev, c->fld[DRD_F_RMU], sizeof(double) * c->cs, cudaMemcpyDeviceToDevice, c->s));
-        c->rmu_prev_ok = 1;
+    if (gm >= 1) {
+        if (gm == 2) CK(cudaMemcpyAsync(c->rmu_prev2, c->rmu_prev, cb, cudaMemcpyDeviceToDevice, c->s));
+        CK(cudaMemcpyAsync(c->rmu_prev, c->fld[DRD_F_RMU], cb, cudaMemcpyDeviceToDevice, c->s));
+        c->rmu_hist = std::min(c->rmu_hist + 1, 2);
     }
     rc = run_graph(c, gkey(GK_CH, mixed_of(c), extrap), [&](cudaStream_t s) { return enq_ch(c, s, extrap); }, t, 0.0);
     if (rc) return rc;
@@ -1647,10 +1662,18 @@ static int velo_common(drd_ctx* c, int bdf, const double* psi1, const double* ps
     if (pf2) rc |= up(c, c->fld[DRD_F_PF2], pf2, c->cs);
     else CK(cudaMemsetAsync(c->fld[DRD_F_PF2], 0, sizeof(double) * c->cs, c->s));
     if (rc) return DRD_ERR_CUDA;
-    // guess_mode 1 (BDF2): the momentum solve starts from 2 u - u_pre, 2 v - v_pre
-    const int extrap = c->P.guess_mode == 1 && bdf == 2;
+    // guess_mode 1 / 2 (BDF2): the momentum solve starts from 2 u - u_pre, or from 3 u - 3 u_pre +
+    // u_pre2 with u_pre2 the u_pre of the previous call; v likewise
+    const int gm = c->P.guess_mode;
+    const int extrap = bdf != 2 ? 0 : (gm == 2 && c->uv_hist >= 1) ? 2 : (gm >= 1 ? 1 : 0);
     rc = run_graph(c, gkey(GK_UV, mixed_of(c), bdf + 3 * extrap), [&](cudaStream_t s) { return enq_uv(c, bdf, s, extrap); },
                    t, 0.0);
+    if (rc) return rc;
+    if (gm == 2 && bdf == 2) {
+        CK(cudaMemcpyAsync(c->u_pre2, c->fld[DRD_F_U_PRE], sizeof(double) * c->us, cudaMemcpyDeviceToDevice, c->s));
+        CK(cudaMemcpyAsync(c->v_pre2, c->fld[DRD_F_V_PRE], sizeof(double) * c->vs, cudaMemcpyDeviceToDevice, c->s));
+        c->uv_hist = 1;
+    }
     if (rc) return rc;
     rc = down(c, u_after, c->u_after, c->us) | down(c, v_after, c->v_after, c->vs);
     const bool dirichlet = !(c->P.variant == DRD_VARIANT_TP && c->P.lr_bd_type == 'n');
@@ -1706,6 +1729,7 @@ int drd_state_upload(drd_ctx* c, int field, const double* host) {
     const long n = (field == DRD_F_U || field == DRD_F_U_PRE) ? c->us : (field == DRD_F_V || field == DRD_F_V_PRE) ? c->vs : c->cs;
     CK(cudaMemcpyAsync(c->fld[field], host, sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
     CK(cudaStreamSynchronize(c->s));
+    c->hist = 0;  // a new state: no step history for the quadratic guess
     return DRD_OK;
 }
 
@@ -1730,9 +1754,13 @@ int drd_steps_async(drd_ctx* c, int first, double t, int nsteps) {
         const double gamma1 = std::min(1.0, c->P.lambda_rho);
         const double coef = fst ? c->P.re * gamma1 / c->P.dt : 3 * c->P.re * gamma1 / 2. / c->P.dt;
         const double tt = t + k * c->P.dt + c->P.dt;
-        int rc = run_graph(c, gkey(GK_STEP, mixed_of(c), fst), [&](cudaStream_t s) { return enq_step(c, fst, s); }, tt,
-                           coef);
+        // the guess of this step: quadratic once two earlier steps are held, else linear
+        const int gm = c->P.guess_mode;
+        const int extrap = fst ? 0 : (gm == 2 && c->hist >= 2) ? 2 : (gm >= 1 ? 1 : 0);
+        int rc = run_graph(c, gkey(GK_STEP, mixed_of(c), fst + 2 * extrap),
+                           [&](cudaStream_t s) { return enq_step(c, fst, extrap, s); }, tt, coef);
         if (rc) return rc;
+        c->hist = fst ? 1 : std::min(c->hist + 1, 2);
     }
     return DRD_OK;
 }
