@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=None, help="timed steps of the plain FP64 path")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--c3-solves", type=int, default=512, help="independent momentum solves of the C3 batch (0: skip)")
     ap.add_argument("--nr", type=int, default=420)
     ap.add_argument("--nz", type=int, default=180)
     return ap.parse_args()
@@ -203,6 +204,61 @@ def run_reference(args, ws, rank):
 
 
 # ----------------------------------------------------------------------------------- GPU arm
+def time_c3(n_solves, seed):
+    """The C3 batch: independent mixed-precision momentum solves A x = b (VeloSolve_2_combined's
+    operator, 2 to 6 disks with eta = 1 + 99 mask, Gaussian-random-field b) on grids drawn from
+    five sizes, through the C-ABI (drd_set_coefs + drd_solve with host arrays).  Each solve's
+    coefficients and right-hand side are generated before its timed region."""
+    from drd_application_gb300 import abi
+    from drd_application_gb300.api import DRDContext
+    from drd_application_gb300.workloads import make_c3_solve
+
+    ctxs = {}
+    total, iters, ok = 0.0, 0, 0
+    for i in range(n_solves):
+        P, coefs, b, _ = make_c3_solve(seed, i)
+        key = (P.nr, P.nz)
+        if key not in ctxs:
+            ctxs[key] = DRDContext(P)
+            # one untimed solve per grid size captures its graph and tunes its transforms
+            ctxs[key].set_coefs(coefs["rho"], coefs["eta"], coefs["bdr_ph"], coefs["bdr_ph_grad"], coefs["M0"],
+                                coefs["Mi"])
+            ctxs[key].solve(abi.DRD_SYS_UV, b)
+        ctx = ctxs[key]
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.set_coefs(coefs["rho"], coefs["eta"], coefs["bdr_ph"], coefs["bdr_ph_grad"], coefs["M0"], coefs["Mi"])
+        x, st = ctx.solve(abi.DRD_SYS_UV, b)
+        total += time.perf_counter() - t0
+        iters += st.iter
+        ok += int(st.info == 0 and st.true_resid <= P.tol)
+    for c in ctxs.values():
+        c.close()
+    return {"solves": n_solves, "seconds": total, "solves_per_s": n_solves / total, "iters_mean": iters / n_solves,
+            "solves_to_fp64_1e-8": f"{ok}/{n_solves}", "sizes": sorted(f"{a}x{b}" for a, b in ctxs)}
+
+
+def cpu_c3_sample(seed, n=4, budget_s=20.0):
+    """The FP64 CPU restatement on the first solves of the same C3 batch (host cores, OpenMP
+    over transform lines; the momentum solve is Jacobi-preconditioned), up to budget_s."""
+    from oracle.oracle import Oracle
+    from drd_application_gb300 import abi
+    from drd_application_gb300.workloads import make_c3_solve
+
+    done, elapsed = 0, 0.0
+    for i in range(n):
+        P, coefs, b, _ = make_c3_solve(seed, i, precision=abi.DRD_PREC_FP64)
+        orc = Oracle(P, openmp=True)
+        t0 = time.perf_counter()
+        orc.solve(1, 2, coefs, b)
+        elapsed += time.perf_counter() - t0
+        done += 1
+        if elapsed > budget_s:
+            break
+    return {"value": done / elapsed, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"first {done} solves of the same C3 batch, FP64 oracle, {elapsed:.1f} s"}
+
+
 def time_resident(ctx, case, warmup, steps, flush_bytes):
     """Per-step device time (CUDA events inside drd_step) with the state resident in HBM."""
     from drd_application_gb300 import abi
@@ -351,6 +407,13 @@ def run_gpu(args, ws, rank, local):
     pt_sec = max_over_ranks(dist, pt["seconds"])
     ctxp.close()
 
+    # the C3 batch of independent momentum solves (reported beside the headline)
+    c3 = time_c3(args.c3_solves, rank) if args.c3_solves > 0 else None
+    if c3 is not None:
+        c3["solves_per_s"] = args.c3_solves * ws / max_over_ranks(dist, c3["seconds"])
+        if rank == 0 and not args.no_cpu:
+            c3["cpu_baseline"] = cpu_c3_sample(rank)
+
     # plain FP64 path, resident state (--fp64-steps 0 skips it, e.g. for profiler runs)
     f64, f64_sec = None, None
     if K64 > 0:
@@ -419,6 +482,7 @@ def run_gpu(args, ws, rank, local):
             "kernels_us": {abi.KB_NAMES[k]: round(v[0], 3) for k, v in kb.items()},
             "with_particles": {"steps_per_s": K * ws / pt_sec, "ms_per_step": 1e3 * pt_sec / K, "beads": 9,
                                "solves_to_fp64_1e-8": f"{pt['solves_ok']}/{pt['solves']}"},
+            "c3_batch": c3,
         },
         "roofline": {"bound": "hbm", "kernel": "k_bicg_persist<CH> (whole mixed CH solve)", "achieved": achieved,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": TRAFFIC_CH,

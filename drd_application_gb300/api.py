@@ -263,6 +263,18 @@ class DRDContext:
     def synchronize(self):
         self._rc(self.L.drd_synchronize(self.h), "drd_synchronize", False)
 
+    def solve(self, system, b, x0=None, bdf=2):
+        """A x = b for DRD_SYS_CH or DRD_SYS_UV with the context's coefficients -> (x, status)."""
+        op = abi.DRD_OP_CH_MATVEC if system == abi.DRD_SYS_CH else abi.DRD_OP_UV_MATVEC
+        n = self.L.drd_op_length(self.h, op)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        if b.shape != (n,):
+            raise ValueError(f"system {system} has {n} unknowns")
+        x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+        st = abi.drd_status()
+        self._rc(self.L.drd_solve(self.h, system, bdf, ptr(b), ptr(x), C.byref(st)), "drd_solve")
+        return x, st
+
     def op_apply(self, op, x, bdf=2, precision=abi.DRD_PREC_FP64):
         """y = op(x) for one of the DRD_OP_* operators (verification access)."""
         n = self.L.drd_op_length(self.h, op)

@@ -913,7 +913,7 @@ int enq_step(drd_ctx* c, int first, int extrap, cudaStream_t s) {
 }
 
 // Graph keys
-enum GraphKind { GK_CH = 1, GK_UV = 2, GK_PHMU = 3, GK_PRE = 4, GK_STEP = 5, GK_ORI = 6 };
+enum GraphKind { GK_CH = 1, GK_UV = 2, GK_PHMU = 3, GK_PRE = 4, GK_STEP = 5, GK_ORI = 6, GK_SOLVE = 7 };
 long gkey(int kind, int a, int b) { return (long)kind * 100 + a * 10 + b; }
 
 int get_graph(drd_ctx* c, long key, const std::function<int(cudaStream_t)>& build, cudaGraphExec_t* out) {
@@ -1711,6 +1711,30 @@ int drd_presolve_2(drd_ctx* c, const double* u, const double* v, double coef, do
     if (rc) return rc;
     if (down(c, psi, c->fld[DRD_F_PSI2], c->cs)) return DRD_ERR_CUDA;
     return finish_call(c, 0, st, false);
+}
+
+int drd_solve(drd_ctx* c, int system, int bdf, const double* b, double* x, drd_status* st) {
+    if (!c || !b || !x || (system != DRD_SYS_CH && system != DRD_SYS_UV) || (bdf != 1 && bdf != 2))
+        return DRD_ERR_BADARG;
+    if (system == DRD_SYS_CH && c->P.variant != DRD_VARIANT_MF) {
+        c->err = "the CH system belongs to the MF variant";
+        return DRD_ERR_BADARG;
+    }
+    int rc = ensure_tuned(c);
+    if (rc) return rc;
+    const int slot = system == DRD_SYS_CH ? KS_CH : KS_UV;
+    const long n = system == DRD_SYS_CH ? c->nc : c->nuv;
+    CK(cudaEventRecord(c->ev0, c->s));
+    rc = up(c, c->k64.b, b, n) | up(c, c->k64.x, x, n);
+    if (rc) return DRD_ERR_CUDA;
+    const int mixed = mixed_for(c, slot);
+    rc = run_graph(c, gkey(GK_SOLVE, mixed, 3 * system + bdf), [&](cudaStream_t s) {
+        const Sys S = sys_of(c, system == DRD_SYS_CH ? SYS_CH : SYS_UV, bdf);
+        return enq_solve(c, S, slot, c->P.tol, system == DRD_SYS_CH ? c->P.ch_maxit : c->P.uv_maxit, mixed, s);
+    }, 0.0, 0.0);
+    if (rc) return rc;
+    if (down(c, x, c->k64.x, n)) return DRD_ERR_CUDA;
+    return finish_call(c, slot, st, true);
 }
 
 int drd_mass(drd_ctx* c, const double* ph, double* mass) {

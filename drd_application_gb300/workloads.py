@@ -22,6 +22,11 @@ Workloads:
         64 rigid fibers of 60x6 cells and 32 drops of radius U(20, 60) cells at seeded
         positions in the channel, viscosity ratio 10, Re 1, Ca 0.02, dr = dz = 1/512.
 Any workload can be built at another grid size; geometry lengths scale with the grid.
+
+  C3 (make_c3_solve): independent momentum solves, A x = b with the VeloSolve_2_combined
+        operator, on a grid drawn from {64x32, 128x64, 256x128, 420x180, 512x256}; the solid is
+        2 to 6 disks of radius 5 to 25 cells, eta = 1 + 99 mask; b is a Gaussian random field
+        (white noise filtered by exp(-k^2 l^2 / 2), l = 8 cells, unit variance, rounded to FP32).
 """
 import math
 
@@ -103,6 +108,49 @@ def _c5_drops(rng, ph, nr, nz, dr, dz, eps, X, Z, yc, half, meta):
         d = np.sqrt((X / dr - cxd) ** 2 + (Z / dz - czd) ** 2) * h
         ph[1:-1, 1:-1] = np.maximum(ph[1:-1, 1:-1], 0.5 * (1.0 + np.tanh((R * h - d) / (math.sqrt(2.0) * eps))))
     meta["drops"] = drops
+
+
+C3_SIZES = ((64, 32), (128, 64), (256, 128), (420, 180), (512, 256))
+
+
+def _grf(rng, shape, ell=8.0):
+    """Gaussian random field: white N(0,1) filtered by exp(-k^2 ell^2 / 2) (k in radians per
+    cell), unit variance, rounded to FP32."""
+    w = rng.standard_normal(shape)
+    ky = 2 * np.pi * np.fft.fftfreq(shape[0])[:, None]
+    kx = 2 * np.pi * np.fft.fftfreq(shape[1])[None, :]
+    f = np.real(np.fft.ifft2(np.fft.fft2(w) * np.exp(-(kx ** 2 + ky ** 2) * ell ** 2 / 2.0)))
+    f = (f - f.mean()) / f.std()
+    return f.astype(np.float32).astype(np.float64)
+
+
+def make_c3_solve(seed, index, size=None, precision=abi.DRD_PREC_MIXED, **overrides):
+    """Solve `index` of the seeded C3 batch: (params, coefs, b) for DRDContext.solve(DRD_SYS_UV)."""
+    rng = np.random.default_rng([seed, index])
+    nr, nz = size if size is not None else C3_SIZES[int(rng.integers(len(C3_SIZES)))]
+    p = abi.default_params(nr, nz, re=0.5, ca=0.05, lambda_rho=1.0, lambda_eta=1.0, penalty_k=1.0e4)
+    p.dr, p.dz = 1.0 / nz, 1.0 / nz
+    p.dt = 0.1 * p.dr
+    p.precision = precision
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    X, Z = np.meshgrid(np.arange(nr) + 0.5, np.arange(nz) + 0.5)
+    d = np.full((nz, nr), np.inf)
+    disks = []
+    for _ in range(int(rng.integers(2, 7))):
+        r = rng.uniform(5.0, 25.0)
+        cx, cz = rng.uniform(0, nr), rng.uniform(0, nz)
+        disks.append((cx, cz, r))
+        d = np.minimum(d, np.hypot(X - cx, Z - cz) - r)
+    bdr = np.zeros(cell_shape(nr, nz))
+    bdr[1:-1, 1:-1] = 0.5 * (1.0 - np.tanh(d / 0.75))
+    neumann_ghosts_cell(bdr)
+    M = 1.0 - bdr
+    coefs = {"rho": np.ones(cell_shape(nr, nz)), "eta": 1.0 + 99.0 * bdr, "bdr_ph": bdr,
+             "bdr_ph_grad": _grad_mag(bdr, dr=p.dr, dz=p.dz), "M0": M.copy(), "Mi": M.copy(), "bdr_pen": bdr.copy(),
+             "bdr_used": M.copy()}
+    b = np.concatenate([_grf(rng, (nz, nr + 1)).ravel(), _grf(rng, (nz - 1, nr)).ravel()])
+    return p, coefs, b, {"disks": disks}
 
 
 def interpolate_coef_host(params, dist, bdr_ph):

@@ -400,6 +400,18 @@ int drd_op_apply(drd_ctx* ctx, int op, int bdf, int precision, const double* x, 
 /* Length of the packed vector of operator `op`. */
 long drd_op_length(drd_ctx* ctx, int op);
 
+/* Systems of drd_solve. */
+#define DRD_SYS_CH 0 /* the mu system of PhSolve (MATRIX_VECTOR_CG, PSolve_CG), MF variant      */
+#define DRD_SYS_UV 1 /* the momentum system of VeloSolve_combined (bdf 1) / _2_combined (bdf 2) */
+
+/* A x = b for one of the Krylov systems of the step, with the context's coefficients
+ * (drd_set_coefs) and parameters: the BiCGSTAB solve of PhSolve.f90:62-74 or
+ * VeloSolve_2_combined.f90:398-401 (tol, ch_maxit / uv_maxit, the precision mode, the mixed
+ * mode's stiffness rule) on a caller's packed right-hand side.  x: the initial guess in, the
+ * solution out; both of length drd_op_length of the system's operator.  For batches of
+ * independent solves that do not come from a time step. */
+int drd_solve(drd_ctx* ctx, int system, int bdf, const double* b, double* x, drd_status* st);
+
 /* ---- performance instrumentation ------------------------------------------------------- */
 
 /* Kernels that drd_kernel_bench can time in isolation on the context's current data. */

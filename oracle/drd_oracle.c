@@ -1127,6 +1127,20 @@ static void uv_ps_cb(void* c, const double* x, double* y) {
     else orc_uv_psolve(C->P, C->bdf, C->rho, C->eta, x, y);
 }
 
+/* A x = b for the CH mu system (system 0: MATRIX_VECTOR_CG with PSolve_CG, ph_lcc the
+ * Ph_Lcc table) or the momentum system (system 1, bdf 1/2) with the reference BiCGSTAB
+ * (PhSolve.f90:72-74, VeloSolve_2_combined.f90:398-401); x: guess in, solution out. */
+int orc_solve_system(const drd_params* P, int system, int bdf, const double* ph_lcc, const double* M0,
+                     const double* Mi, const double* rho, const double* eta, const double* pen, const double* b,
+                     double* x, drd_status* st) {
+    if (system == 0) {
+        ch_ctx C = {P, M0, Mi, ph_lcc};
+        return orc_bicgstab((long)P->nr * P->nz, b, x, P->ch_maxit, P->tol, ch_mv_cb, ch_ps_cb, &C, st);
+    }
+    uv_ctx C = {P, bdf, rho, eta, pen};
+    return orc_bicgstab(uv_len(P->nr, P->nz), b, x, P->uv_maxit, P->tol, uv_mv_cb, uv_ps_cb, &C, st);
+}
+
 /* VeloSolve_combined (bdf 1) / VeloSolve_2_combined (bdf 2). */
 int orc_velosolve(const drd_params* P, int bdf, const double* psi1, const double* psi2,
                   const double* u_pre, const double* u, const double* v_pre, const double* v,

@@ -100,6 +100,11 @@ void orc_esolp_coefs(const drd_params* P, int bdf, double* ua, double* ub, doubl
                      double* vc);
 void orc_uv_psolve_esolp(const drd_params* P, int bdf, const double* x, double* y);
 
+/* A x = b for system 0 (CH mu) or 1 (momentum, bdf 1/2) with the reference BiCGSTAB. */
+int orc_solve_system(const drd_params* P, int system, int bdf, const double* ph_lcc, const double* M0,
+                     const double* Mi, const double* rho, const double* eta, const double* pen, const double* b,
+                     double* x, drd_status* st);
+
 /* PhSolve_ori and finit's wall smoothing (microfluidics_complex_domain/PhSolve_ori.f90,
  * finit.f90:120-189).  angleB/angleT may be NULL (zeros, as during finit's loop). */
 double orc_ori_coef(const drd_params* P, double alpha_s);

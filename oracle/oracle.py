@@ -54,6 +54,7 @@ def lib(openmp=False):
         L.orc_uv_matvec.argtypes = [P, C.c_int, dp, dp, dp, C.c_double, dp, C.c_double, dp]
         L.orc_uv_psolve.argtypes = [P, C.c_int, dp, dp, dp, dp]
         L.orc_uv_psolve_esolp.argtypes = [P, C.c_int, dp, dp]
+        L.orc_solve_system.argtypes = [P, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp, dp, dp, S]
         L.orc_esolp_coefs.argtypes = [P, C.c_int, dp, dp, dp, dp, dp, dp]
         L.orc_phmu_matvec.argtypes = [P, dp, dp, dp, C.c_double, C.c_double, C.c_double, dp, C.c_double, dp]
         L.orc_phmu_psolve.argtypes = [P, dp, dp]
@@ -158,6 +159,18 @@ class Oracle:
         y = np.zeros_like(x)
         self.L.orc_uv_psolve(C.byref(self.P), bdf, ptr(rho), ptr(eta), ptr(np.ascontiguousarray(x)), ptr(y))
         return y
+
+    def solve(self, system, bdf, coefs, b, x0=None):
+        """A x = b for system 0 (CH mu) or 1 (momentum) -> (x, status).  coefs: M0, Mi (CH) or
+        rho, eta, bdr_pen (momentum), CELL shaped."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
+        z = np.zeros(1)
+        g = lambda k: ptr(np.ascontiguousarray(coefs[k])) if k in coefs else ptr(z)
+        st = abi.drd_status()
+        self.L.orc_solve_system(C.byref(self.P), system, bdf, ptr(self.ph_lcc), g("M0"), g("Mi"), g("rho"), g("eta"),
+                                g("bdr_pen"), ptr(b), ptr(x), C.byref(st))
+        return x, st
 
     def uv_psolve_esolp(self, bdf, x):
         """ESOLP_x on a packed momentum vector (Precipitation_dynamics/VeloSolve_combined.f90:800-806)."""
