@@ -54,6 +54,7 @@ struct KState {
     int outer;         // mixed mode: reliable updates (FP64 residual recomputes) so far
     int inner_total;   // mixed mode: FP32 iterations summed
     double rmax;       // mixed mode: ||r|| at the last reliable update
+    double itol;       // mixed mode (outer state): the inner solves' tolerance, tightened on a stall
     int first_next;    // the next iteration starts a fresh Krylov sequence (P = R)
     int do_update;     // mixed mode: this iteration ends with a reliable update
     int mixed;         // mixed mode: no absolute ||s|| exit; convergence on the FP64 residual only

@@ -1211,6 +1211,9 @@ template void launch_gemm<float>(int, int, const GemmArgs<float>&, cudaStream_t)
 // fixed order, so all blocks agree and no one-block scalar kernel is launched for them.
 // ======================================================================================
 static __device__ const double kBreakTol = 1.2325951644078309e-32;  // DLAMCH('E')**2 (getbreak.f)
+// Mixed mode: a refinement sweep that reduces the FP64 residual by less than 10 % tightens the
+// inner FP32 solves' tolerance tenfold, down to this floor; a stall at the floor ends the solve.
+static __device__ const double kMixedItolFloor = 1.5e-4;
 
 template <typename T>
 __global__ void k_bi_init1(long n, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r, Dots d,
@@ -1237,12 +1240,12 @@ __global__ void k_bi_init2(KState* ks, Dots d, double tol, int maxit, const KSta
     const double xx = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
     const double bb = reduce_partials<DRD_TPB>(d.part + 3 * DRD_MAXB, d.G, sm);
     if (threadIdx.x == 0) {
-        ks->tol = tol;
+        ks->tol = parent != nullptr ? parent->itol : tol;  // an inner solve takes its parent's tolerance
         ks->maxit = maxit;
         ks->info = 0;
         ks->flags = 0u;
         ks->iter = maxit;   // ITER keeps MAXIT if the x0 test ends the solve (:248)
-        ks->resid = tol;    // RESID keeps TOL in that case
+        ks->resid = ks->tol;  // RESID keeps TOL in that case
         ks->xnorm = sqrt(xx);
         ks->x_nonzero = (ks->xnorm != 0.0);
         ks->bnorm_raw = sqrt(bb);
@@ -1651,13 +1654,14 @@ __global__ void k_mr_check(KState* ks, Dots d, cudaGraphConditionalHandle hw, ul
 
 // ---- mixed-precision refinement ----------------------------------------------------------
 // outer->snorm holds ||r64||; the FP32 system is solved for r64/||r64|| from a zero guess.
-__global__ void k_mx_init(KState* o, Dots d, double tol, int max_refine, ull* ctr) {
+__global__ void k_mx_init(KState* o, Dots d, double tol, int max_refine, double itol, ull* ctr) {
     count_launch(ctr);
     __shared__ double sm[32];
     const double rr = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sm);
     const double bb = reduce_partials<DRD_TPB>(d.part + 3 * DRD_MAXB, d.G, sm);
     if (threadIdx.x == 0) {
         o->tol = tol;
+        o->itol = itol;
         o->maxit = max_refine;
         o->bnorm_raw = sqrt(bb);
         o->bnrm2 = (o->bnorm_raw == 0.0) ? 1.0 : o->bnorm_raw;
@@ -1734,7 +1738,10 @@ __global__ void k_mx_check(KState* o, const KState* in, Dots d, cudaGraphConditi
             else if (!isfinite(o->resid)) { o->info = DRD_ERR_NONFINITE; o->phase = PH_DONE; }
             else if (o->resid <= o->tol) { o->info = 0; o->phase = PH_DONE; }
             else if (o->outer >= o->maxit) { o->info = 1; o->phase = PH_DONE; }
-            else if (o->resid > 0.9 * prev) { o->info = 1; o->phase = PH_DONE; }  // stalled refinement
+            else if (o->resid > 0.9 * prev) {  // a sweep that gained < 10 %: tighten the inner solves
+                if (o->itol > kMixedItolFloor) o->itol *= 0.1;
+                else { o->info = 1; o->phase = PH_DONE; }  // stalled at the tightest inner tolerance
+            }
         }
         if (use_graph) cudaGraphSetConditional(h, o->phase == PH_RUNNING ? 1u : 0u);
     }
@@ -2597,6 +2604,7 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
         // Each sweep: r64 = b64 - A64 x64 and its tests, b32 = r64/||r64||, an inner solve of
         // A d = b32 from d = 0 to the inner tolerance, x64 += ||r64|| d.
         const double otol = a.outer_tol;
+        double itol = a.tol;  // the inner tolerance, tightened tenfold when a sweep stalls
         int outer = 0, inner_total = 0, oinfo = 0;
         double bnorm64 = 0.0, bnrm64 = 1.0, rnorm = 0.0, oresid = 0.0, prev = 0.0;
         bool ok = true, run = true;
@@ -2619,7 +2627,10 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
                 if (!isfinite(oresid)) { oinfo = DRD_ERR_NONFINITE; break; }
                 if (oresid <= otol) { oinfo = 0; break; }
                 if (outer >= a.max_refine) { oinfo = 1; break; }
-                if (oresid > 0.9 * prev) { oinfo = 1; break; }  // stalled refinement
+                if (oresid > 0.9 * prev) {  // a sweep that gained < 10 %: tighten the inner solves
+                    if (itol > kMixedItolFloor) itol *= 0.1;
+                    else { oinfo = 1; break; }  // stalled at the tightest inner tolerance
+                }
             }
             // scale and inner setup in one pass: b32 = r = rtld = r64 / ||r64||, x32 = 0
             {
@@ -2642,7 +2653,7 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
             const double bn = sqrt(bb);
             in = PbInner{};
             if (a.maxit <= 0) { in.info = -3; in.iter = a.maxit; }
-            else if (!(ok = pb_iterate<KIND>(a, bn == 0.0 ? 1.0 : bn, a.tol, a.maxit, bb, in, smem, sm, gen, pf)))
+            else if (!(ok = pb_iterate<KIND>(a, bn == 0.0 ? 1.0 : bn, itol, a.maxit, bb, in, smem, sm, gen, pf)))
                 break;
             // x64 += ||r64|| d32
             for (long q = q0; q < n; q += stride) a.x64[q] = __ldcg(a.x64 + q) + rnorm * (double)__ldcg(a.x + q);
@@ -3024,8 +3035,9 @@ template void launch_convert_scale<double, double>(long, const double*, double, 
 void launch_axpy_f2d(long n, const KState* ks, const float* d, double* x, ull* ctr, cudaStream_t s) {
     k_axpy_f2d<<<GRID(n)>>>(n, ks, d, x, ctr);
 }
-void launch_mx_init(KState* outer, const Dots& d, double tol, int max_refine, ull* ctr, cudaStream_t s) {
-    k_mx_init<<<1, DRD_TPB, 0, s>>>(outer, d, tol, max_refine, ctr);
+void launch_mx_init(KState* outer, const Dots& d, double tol, int max_refine, double itol, ull* ctr,
+                    cudaStream_t s) {
+    k_mx_init<<<1, DRD_TPB, 0, s>>>(outer, d, tol, max_refine, itol, ctr);
 }
 void launch_mx_inner_setup(KState* inner, const KState* outer, double inner_tol, int inner_maxit, ull* ctr,
                            cudaStream_t s) {

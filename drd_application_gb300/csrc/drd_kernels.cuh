@@ -248,7 +248,8 @@ template <typename T>
 void launch_norm2_partial(long n, const T* x, const Dots& d, int slot, ull* ctr, cudaStream_t s);
 
 // ---- mixed-precision refinement control -------------------------------------------------
-void launch_mx_init(KState* outer, const Dots& d, double tol, int max_refine, ull* ctr, cudaStream_t s);
+void launch_mx_init(KState* outer, const Dots& d, double tol, int max_refine, double itol, ull* ctr,
+                    cudaStream_t s);
 void launch_mx_inner_setup(KState* inner, const KState* outer, double inner_tol, int inner_maxit, ull* ctr,
                            cudaStream_t s);
 void launch_mx_check(KState* outer, const KState* inner, const Dots& d, cudaGraphConditionalHandle h, int use_graph,

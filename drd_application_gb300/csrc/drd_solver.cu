@@ -730,8 +730,8 @@ int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int 
         launch_copy<double>(S.n, k.b, k.r, c->ctr, s);
         enq_matvec<double>(c, S, -1.0, k.x, 1.0, k.r, nullptr, 1, -1, nullptr, G_ALWAYS, s);
         launch_norm2_partial<double>(S.n, k.b, d, 3, c->ctr, s);
-        launch_mx_init(ks, d, tol, c->P.mixed_max_refine, c->ctr, s);
         const double itol = c->P.mixed_inner_tol;
+        launch_mx_init(ks, d, tol, c->P.mixed_max_refine, itol, c->ctr, s);
         rc = capture_while(c, s, c->s2, ks, [&](cudaStream_t sb, cudaGraphConditionalHandle ho) {
             launch_mx_scale<float>(S.n, k.r, ks, f.b, f.x, c->ctr, sb);
             enq_bicg_setup<float>(c, S, f, in, itol, maxit, ks, sb);

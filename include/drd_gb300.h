@@ -102,7 +102,8 @@ typedef struct drd_params {
     double penalty_k;      /* DRD resistance coefficient (global.f90:91, 1e5)                      */
     double lambda_rho, lambda_eta; /* density / viscosity ratios (deck lines 24-25)                */
     double bdr_ph_used_adjust;     /* TP: 1e-6 (TP/finit.f90:572)                                  */
-    double mixed_inner_tol;        /* mixed mode: relative residual reduction per FP32 inner solve */
+    double mixed_inner_tol;        /* mixed mode: relative residual reduction per FP32 inner solve; */
+                                   /* a sweep that gains < 10 % tightens it tenfold (to 1.5e-4)     */
     int32_t mixed_max_refine;      /* mixed mode: maximum FP64 refinement sweeps                   */
     int32_t uv_precond;            /* momentum preconditioner: DRD_UV_JACOBI (the MF reference) or  */
                                    /* DRD_UV_ESOLP (ESOLP_x, used by the PD application)             */
