@@ -2203,10 +2203,8 @@ __device__ __forceinline__ void pb_zcols(const PersistArgs& a, const float* xs, 
     __syncthreads();
 }
 
-// Column pass along z (columns are independent along z): what = 0: out = Cz ((Cz X) / L);
-// 1: out = (Cz X) / L; 2: out = Cz X.
-__device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* smem, int what = 0,
-                       const PbProf* pf = nullptr) {
+// Column pass along z (columns are independent along z): out = Cz ((Cz X) / Ph_Lcc).
+__device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* smem, const PbProf* pf = nullptr) {
     const int nz = a.nz, nr = a.nr, K = a.Kz;
     float* xs = smem + a.work_off;    // [nz][CW]
     float* u = xs + nz * PB_CW;       // [2][CW][Kz4]
@@ -2222,7 +2220,7 @@ __device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* 
 #pragma unroll
         for (int i = 0; i < LP; ++i) {
             const int e = threadIdx.x + i * PB_NT, row = e / PB_CW, col = c0 + e % PB_CW;
-            lv[i] = (what != 2 && e < nz * PB_CW && col < nr) ? __ldg(a.lcc + (long)row * nr + col) : 1.f;
+            lv[i] = (e < nz * PB_CW && col < nr) ? __ldg(a.lcc + (long)row * nr + col) : 1.f;
         }
         for (int e = threadIdx.x; e < nz * PB_CW; e += PB_NT) {
             const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
@@ -2232,25 +2230,22 @@ __device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* 
         pb_markz(pf, 0);
         pb_zcols(a, xs, u, ys, zA);
         pb_markz(pf, 1);
-        if (what != 2) {
 #pragma unroll
-            for (int i = 0; i < LP; ++i) {
-                const int e = threadIdx.x + i * PB_NT, col = c0 + e % PB_CW;
-                if (e < nz * PB_CW) xs[e] = col < nr ? ys[e] / lv[i] : 0.f;
-            }
-            for (int e = threadIdx.x + LP * PB_NT; e < nz * PB_CW; e += PB_NT) {
-                const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
-                xs[e] = col < nr ? ys[e] / __ldg(a.lcc + (long)row * nr + col) : 0.f;
-            }
-            __syncthreads();
-            pb_markz(pf, 2);
-            if (what == 0) pb_zcols(a, xs, u, ys, zA);
-            pb_markz(pf, 3);
+        for (int i = 0; i < LP; ++i) {
+            const int e = threadIdx.x + i * PB_NT, col = c0 + e % PB_CW;
+            if (e < nz * PB_CW) xs[e] = col < nr ? ys[e] / lv[i] : 0.f;
         }
-        const float* res = what == 1 ? xs : ys;
+        for (int e = threadIdx.x + LP * PB_NT; e < nz * PB_CW; e += PB_NT) {
+            const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
+            xs[e] = col < nr ? ys[e] / __ldg(a.lcc + (long)row * nr + col) : 0.f;
+        }
+        __syncthreads();
+        pb_markz(pf, 2);
+        pb_zcols(a, xs, u, ys, zA);
+        pb_markz(pf, 3);
         for (int e = threadIdx.x; e < nz * PB_CW; e += PB_NT) {
             const int row = e / PB_CW, c = e % PB_CW, col = c0 + c;
-            if (col < nr) out[(long)row * nr + col] = res[e];
+            if (col < nr) out[(long)row * nr + col] = ys[e];
         }
         pb_markz(pf, 4);
     }
@@ -2258,19 +2253,9 @@ __device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* 
 
 // psolve: y = DCT-I preconditioner applied to x (three phases, two internal barriers).
 __device__ bool pb_psolve(const PersistArgs& a, const float* x, float* y, float* smem, unsigned& gen, PbProf& pf) {
-    if (a.zorder == 1) {  // x, z / L, x, z: the order of the kernel-per-phase path
-        pb_xpass(a, x, a.w1, smem, pf);
-        if (!grid_sync(a.bar, gen, pf)) return false;
-        pb_zdz(a, a.w1, a.w2, smem, 1);
-        if (!grid_sync(a.bar, gen, pf)) return false;
-        pb_xpass(a, a.w2, a.w1, smem, pf);
-        if (!grid_sync(a.bar, gen, pf)) return false;
-        pb_zdz(a, a.w1, y, smem, 2);
-        return true;
-    }
     pb_xpass(a, x, a.w1, smem, pf);
     if (!grid_sync(a.bar, gen, pf)) return false;
-    pb_zdz(a, a.w1, a.w2, smem, 0, &pf);
+    pb_zdz(a, a.w1, a.w2, smem, &pf);
     if (!grid_sync(a.bar, gen, pf)) return false;
     pb_xpass(a, a.w2, y, smem, pf);
     return true;

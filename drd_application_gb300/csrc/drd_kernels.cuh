@@ -139,7 +139,6 @@ enum PersistMode : int { PM_SOLVE = 0, PM_PSOLVE = 1, PM_MATVEC = 2, PM_REFINE =
 struct PersistArgs {
     int kind;                             // PK_CH or PK_UV
     int mode;                             // PM_SOLVE, or one application x = op(b)
-    int zorder;                           // CH transform order: 0 x,z/z,x (3 phases); 1 x,z/,x,z
     int nr, nz;
     long n;                               // unknowns
     OpScal<float> o;

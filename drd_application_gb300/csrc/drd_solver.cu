@@ -672,8 +672,6 @@ PersistArgs persist_args(drd_ctx* c, const Sys& S, KState* in, const KState* par
     a.t = f.t; a.ff1 = f.ff1; a.w1 = c->t1f; a.w2 = c->t2f;
     a.part = c->part; a.ks = in; a.parent = parent; a.bar = c->bar; a.tol = tol; a.maxit = maxit; a.ctr = c->ctr;
     a.prof = c->pprof_on ? c->pprof : nullptr;
-    const char* zo = std::getenv("DRD_PERSIST_ORDER");
-    a.zorder = (zo && std::atoi(zo) == 1) ? 1 : 0;
     a.work_off = c->pplan.work_off; a.z_off = c->pplan.z_off; a.b_off = c->pplan.b_off;
     a.z_res = c->pplan.z_res; a.b_res = c->pplan.b_res; a.smem_bytes = c->pplan.bytes;
     return a;
