@@ -1135,12 +1135,106 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm_sk(GemmArgs<T> a
     cluster.sync();  // keep every CTA's partial tile alive until all readers are done
 }
 
+// FP64 transforms in double-float arithmetic on the FP32 pipes.  GB300 issues FP64 at a small
+// fraction of its FP32 rate, and the FP64 transform GEMMs were the larger part of an FP64 CH
+// iteration.  Each FP64 operand is split into hi + lo FP32 values (hi = fl32(x), lo = fl32(x -
+// hi): 48 significant bits).  A product is hi*hi, taken exactly as p + e with one FMA, plus the
+// cross terms hi*lo + lo*hi (lo*lo, about 2^-48 of the product, is dropped).  The running sum is
+// a double-float (sh, sl): sh += p by an exact two-sum (Knuth), and its error joins e and the
+// cross terms in sl.  The result is sh + sl in FP64: about 2^-44 of sum |a b|, where FP64
+// accumulation gives about 2^-50.  The error-free steps use the _rn intrinsics, which the
+// compiler never contracts into FMAs.
+__device__ __forceinline__ void df_split(double x, float& hi, float& lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+__device__ __forceinline__ void df_mac(float ah, float al, float bh, float bl, float& sh, float& sl) {
+    const float p = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -p);  // ah*bh = p + e exactly
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    const float s = __fadd_rn(sh, p);  // two-sum: sh + p = s + err exactly
+    const float bv = __fsub_rn(s, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bv)), __fsub_rn(p, bv));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
+template <int BM, int BN, int BK, int TM, int TN, int EPI>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN)) k_gemm_df(GemmArgs<double> a) {
+    constexpr int NT = (BM / TM) * (BN / TN);
+    constexpr int TX = BN / TN, TY = BM / TM;
+    __shared__ float Ah[BK][BM + 1], Al[BK][BM + 1];
+    __shared__ float Bh[BK][BN], Bl[BK][BN];
+    count_launch(a.ctr);
+    if (gate_closed(a.ks, a.gate)) return;
+    const GemmView<double> g(a, a.fold ? (int)blockIdx.z : 0);
+    const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    if (m0 >= g.M || n0 >= g.N) return;
+    float sh[TM][TN], sl[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) sh[i][j] = sl[i][j] = 0.f;
+    for (int k0 = 0; k0 < a.K; k0 += BK) {
+        for (int e = tid; e < BM * BK; e += NT) {
+            const int r = e / BK, c = e % BK;
+            df_split(g.loadA(a, m0 + r, k0 + c, a.K), Ah[c][r], Al[c][r]);
+        }
+        for (int e = tid; e < BK * BN; e += NT) {
+            const int r = e / BN, c = e % BN;
+            df_split(g.loadB(a, k0 + r, n0 + c, a.K), Bh[r][c], Bl[r][c]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            float ah[TM], al[TM], bh[TN], bl[TN];
+#pragma unroll
+            for (int i = 0; i < TM; ++i) { ah[i] = Ah[kk][ty + i * TY]; al[i] = Al[kk][ty + i * TY]; }
+#pragma unroll
+            for (int j = 0; j < TN; ++j) { bh[j] = Bh[kk][tx + j * TX]; bl[j] = Bl[kk][tx + j * TX]; }
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TN; ++j) df_mac(ah[i], al[i], bh[j], bl[j], sh[i][j], sl[i][j]);
+        }
+        __syncthreads();
+    }
+    const double coef = (EPI == EPI_PRE_FINAL) ? a.ca->coef : 0.0;
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+        const int gm = m0 + ty + i * TY;
+        if (gm >= g.M) continue;
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            const int gn = n0 + tx + j * TX;
+            if (gn >= g.N) continue;
+            gemm_store<double, EPI>(a, g.orow(a, gm), g.ocol(a, gn), (double)sh[i][j] + (double)sl[i][j], coef);
+        }
+    }
+}
+
+template <int BM, int BN, int TM, int TN>
+static void gemm_df_dispatch(int epi, const GemmArgs<double>& a, cudaStream_t s) {
+    dim3 grid((a.N + BN - 1) / BN, (a.M + BM - 1) / BM, a.fold ? 2 : 1);
+    constexpr int NT = (BM / TM) * (BN / TN);
+    switch (epi) {
+        case EPI_STORE: k_gemm_df<BM, BN, 16, TM, TN, EPI_STORE><<<grid, NT, 0, s>>>(a); break;
+        case EPI_DIV_TAB: k_gemm_df<BM, BN, 16, TM, TN, EPI_DIV_TAB><<<grid, NT, 0, s>>>(a); break;
+        case EPI_SCALE: k_gemm_df<BM, BN, 16, TM, TN, EPI_SCALE><<<grid, NT, 0, s>>>(a); break;
+        default: k_gemm_df<BM, BN, 16, TM, TN, EPI_PRE_FINAL><<<grid, NT, 0, s>>>(a); break;
+    }
+}
+
 struct GemmCfg { const char* name; };
 static const GemmCfg kGemmCfgs[] = {{"64x64x16/4x4"},         {"32x64x16/2x4"},         {"32x32x16/2x2"},
                                     {"16x32x16/1x2"},         {"sk4 32x64x16/4x4"},     {"sk4 32x32x16/4x4"},
-                                    {"sk4 16x64x16/2x4"},     {"sk8 32x32x16/2x2"},     {"sk2 32x64x16/4x4"}};
+                                    {"sk4 16x64x16/2x4"},     {"sk8 32x32x16/2x2"},     {"sk2 32x64x16/4x4"},
+                                    {"df 64x64x16/4x4"},      {"df 32x64x16/2x4"},      {"df 32x32x16/2x2"}};
 
-int gemm_config_count() { return 9; }
+// Configurations 9-11 are the double-float kernels: FP64 only.
+int gemm_config_count(int fp64) { return fp64 ? 12 : 9; }
 const char* gemm_config_name(int cfg) { return kGemmCfgs[cfg].name; }
 
 template <typename T, int BM, int BN, int TM, int TN, int KS, int EPI>
@@ -1194,7 +1288,16 @@ void launch_gemm(int cfg, int epi, const GemmArgs<T>& a, cudaStream_t s) {
         case 5: gemm_sk_dispatch<T, 32, 32, 4, 4, 4>(epi, a, s); break;
         case 6: gemm_sk_dispatch<T, 16, 64, 2, 4, 4>(epi, a, s); break;
         case 7: gemm_sk_dispatch<T, 32, 32, 2, 2, 8>(epi, a, s); break;
-        default: gemm_sk_dispatch<T, 32, 64, 4, 4, 2>(epi, a, s); break;
+        case 8: gemm_sk_dispatch<T, 32, 64, 4, 4, 2>(epi, a, s); break;
+        default:
+            if constexpr (sizeof(T) == 8) {
+                if (cfg == 9) gemm_df_dispatch<64, 64, 4, 4>(epi, a, s);
+                else if (cfg == 10) gemm_df_dispatch<32, 64, 2, 4>(epi, a, s);
+                else gemm_df_dispatch<32, 32, 2, 2>(epi, a, s);
+            } else {
+                gemm_dispatch_epi<T, 64, 64, 4, 4>(epi, a, s);
+            }
+            break;
     }
 }
 template void launch_gemm<double>(int, int, const GemmArgs<double>&, cudaStream_t);

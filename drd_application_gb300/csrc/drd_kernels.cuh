@@ -49,7 +49,7 @@ struct GemmArgs {
     const T* A_odd; const T* B_odd; int M_odd, N_odd;
 };
 enum Fold : int { FOLD_NONE = 0, FOLD_A = 1, FOLD_B = 2 };
-int gemm_config_count();
+int gemm_config_count(int fp64);
 const char* gemm_config_name(int cfg);
 template <typename T>
 void launch_gemm(int cfg, int epi, const GemmArgs<T>& a, cudaStream_t s);

@@ -105,6 +105,8 @@ struct drd_ctx {
     unsigned long long* ctr;
     int G = 1;
     int gcfg[2][2] = {{-1, -1}, {-1, -1}};  // [fp32?][z-pass?]
+    // the mixed mode's FP64 transforms (pressure, a stiff CH system): double-float kernels
+    int gcfg_df[2] = {-1, -1};
     std::map<long, cudaGraphExec_t> graphs;
     std::string err;
     int use_graph = 1;
@@ -368,7 +370,12 @@ GemmArgs<T> gargs(drd_ctx* c, int M, int N, int K, const T* A, long lda, const T
 }
 
 template <typename T>
-int gcfg(drd_ctx* c, int zpass) { return c->gcfg[sizeof(T) == 4][zpass]; }
+int gcfg(drd_ctx* c, int zpass) {
+    // FP64 transforms: true FP64 GEMMs in the FP64 mode (the reference's arithmetic), the
+    // double-float kernels in the mixed mode, where they are never the precision that limits
+    if (sizeof(T) == 8 && c->P.precision == DRD_PREC_MIXED) return c->gcfg_df[zpass];
+    return c->gcfg[sizeof(T) == 4][zpass];
+}
 
 // The folded DCT-I passes of the CH preconditioner.  x pass: out[m][o] = sum_j X[m][j] C_x[o][j]
 // over nr columns; z pass: out[o][n] = sum_j C_z[o][j] X[j][n] over nz rows.  Each pass folds
@@ -939,15 +946,15 @@ void clear_graphs(drd_ctx* c) {
 
 // ---- GEMM tile autotuner: times each tile configuration on the context's transform shapes --
 template <typename T>
-int tune_pass(drd_ctx* c, int zpass) {
+int tune_pass(drd_ctx* c, int zpass, int lo, int hi) {
     const int nr = c->nr, nz = c->nz;
     const char* env = std::getenv("DRD_GEMM_CFG");
-    if (env) { int v = std::atoi(env); if (v >= 0 && v < gemm_config_count()) return v; }
-    int best = 0;
+    if (env) { int v = std::atoi(env); if (v >= lo && v < hi) return v; }
+    int best = lo;
     float best_ms = 1e30f;
     T* t1 = tmp1<T>(c);
     T* t2 = tmp2<T>(c);
-    for (int cfg = 0; cfg < gemm_config_count(); ++cfg) {
+    for (int cfg = lo; cfg < hi; ++cfg) {
         auto a = zpass ? dct1_zpass<T>(c, t1, t2, nullptr, G_ALWAYS) : dct1_xpass<T>(c, t1, t2, nullptr, G_ALWAYS);
         a.ctr = nullptr;
         launch_gemm<T>(cfg, EPI_STORE, a, c->s);  // warm-up
@@ -967,10 +974,13 @@ int ensure_tuned(drd_ctx* c) {
     if (c->gcfg[0][0] >= 0) return DRD_OK;
     CK(cudaMemsetAsync(c->t1, 0, sizeof(double) * c->nc, c->s));
     CK(cudaMemsetAsync(c->t1f, 0, sizeof(float) * c->nc, c->s));
-    c->gcfg[0][0] = tune_pass<double>(c, 0);
-    c->gcfg[0][1] = tune_pass<double>(c, 1);
-    c->gcfg[1][0] = tune_pass<float>(c, 0);
-    c->gcfg[1][1] = tune_pass<float>(c, 1);
+    const int nx = gemm_config_count(0), nd = gemm_config_count(1);  // configs [nx, nd): double-float
+    c->gcfg[0][0] = tune_pass<double>(c, 0, 0, nx);
+    c->gcfg[0][1] = tune_pass<double>(c, 1, 0, nx);
+    c->gcfg_df[0] = tune_pass<double>(c, 0, nx, nd);
+    c->gcfg_df[1] = tune_pass<double>(c, 1, nx, nd);
+    c->gcfg[1][0] = tune_pass<float>(c, 0, 0, nx);
+    c->gcfg[1][1] = tune_pass<float>(c, 1, 0, nx);
     CK(cudaStreamSynchronize(c->s));
     return DRD_OK;
 }

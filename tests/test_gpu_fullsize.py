@@ -19,8 +19,7 @@ pytestmark = pytest.mark.gpu
 F = abi
 
 
-def _n_cfg(cuda_lib):
-    return 9
+N_CFG_FP32, N_CFG_FP64 = 9, 12  # configurations 9-11: the FP64-only double-float kernels
 
 
 @pytest.mark.parametrize("nr,nz", [(420, 180), (97, 53)])
@@ -30,10 +29,15 @@ def test_every_gemm_config_matches_oracle(cuda_lib, oracle_build, nr, nz):
     x = np.random.default_rng(nr).standard_normal(nr * nz)
     ref = orc.ch_psolve(x)
     bad = []
-    for cfg in range(_n_cfg(cuda_lib)):
+    for cfg in range(N_CFG_FP64):
+        # FP64 GEMM configurations serve the FP64 mode; the double-float ones (9-11) serve the
+        # mixed mode's FP64 transforms, so they are checked from a mixed-mode context
         os.environ["DRD_GEMM_CFG"] = str(cfg)
+        P = case.params.copy()
+        if cfg >= N_CFG_FP32:
+            P.precision = F.DRD_PREC_MIXED
         try:
-            ctx = DRDContext(case.params)
+            ctx = DRDContext(P)
             ctx.set_case(case)
             e64 = rel_err(ctx.op_apply(F.DRD_OP_CH_PSOLVE, x), ref)
             e32 = rel_err(ctx.op_apply(F.DRD_OP_CH_PSOLVE, x, precision=F.DRD_PREC_MIXED), ref)
