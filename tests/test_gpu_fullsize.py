@@ -90,6 +90,32 @@ def test_c5_mixed_step_solves_ch_in_fp64_and_conserves_mass(cuda_lib):
     ctx.close()
 
 
+@pytest.mark.parametrize("precision", [abi.DRD_PREC_FP64, abi.DRD_PREC_MIXED])
+def test_c1_steps_match_oracle(cuda_lib, oracle_build, precision):
+    """The C1 configuration at its own size (128x64, one drop, no solid, tol 1e-10): five
+    resident mcl6 steps against the oracle's five steps."""
+    case = make_case("c1", seed=0)
+    P = case.params.copy()
+    P.precision = precision
+    ctx = DRDContext(P)
+    ctx.set_case(case)
+    ctx.upload_state(case.state)
+    orc = Oracle(P)
+    st = case.copy_state()
+    t = 0.0
+    for s in range(5):
+        g = ctx.step(s == 0, t)
+        orc.step(st, case.coefs, s == 0, t)
+        t += P.dt
+        assert g.ch.info == 0 and g.uv.info == 0, (g.ch.as_dict(), g.uv.as_dict())
+        assert g.ch.true_resid <= P.tol and g.uv.true_resid <= P.tol
+    out = ctx.download_state([F.F_U, F.F_V, F.F_PH, F.F_RMU, F.F_P])
+    lim = 1e-6 if precision == abi.DRD_PREC_FP64 else 1e-4
+    for fid, a in out.items():
+        assert rel_err(a, st[fid]) < lim, fid
+    ctx.close()
+
+
 def test_direct_launch_mode_matches_graph_mode(cuda_lib):
     """DRD_DIRECT_LAUNCH=1 (per-kernel launches, host-run loops; used for profiling) computes
     exactly what the captured graphs compute: the reductions are in a fixed order."""
