@@ -1970,29 +1970,33 @@ __device__ __forceinline__ void slot_put(double* part, int slot, double v, doubl
     if (threadIdx.x == 0) part[slot * DRD_MAXB + blockIdx.x] = r;
 }
 
-// GB300 issues FP64 at a small fraction of its FP32 rate, so in the hot loop of the persistent
-// solver the FP64 work of the reductions is kept to one warp: each thread accumulates its
-// products in FP32, each warp sums its lanes in FP32, and only the warp sums (and the grid's
-// block partials) are added in FP64.  The scalar steps of an iteration are evaluated by thread 0
-// and broadcast through shared memory instead of by every thread.
-//
-// Grid sum of one partials slot by warp 0 (each lane its strided share in order, then an xor
+// GB300 issues FP64 at a small fraction of its FP32 rate, so the hot loop of the persistent
+// solver does no FP64 work at all: its dot products, their block and grid sums and the scalar
+// steps of an iteration are FP32, the precision of the inner solve itself (the FP64 work stays
+// in the refinement around it).  A block partial is stored as an FP32 value in its slot of the
+// partials buffer.  The scalar steps are evaluated by thread 0 and broadcast through shared
+// memory.
+__device__ __forceinline__ float* fslot(double* part, int slot, int b) {
+    return reinterpret_cast<float*>(part + slot * DRD_MAXB + b);
+}
+// Grid sum of one FP32 partials slot by warp 0 (each lane its strided share in order, then an xor
 // butterfly: every lane of every block gets the same bits).  Call from warp 0 only.
-__device__ __forceinline__ double warp_slot_sum(const double* part, int slot) {
+__device__ __forceinline__ float warp_slot_sum(double* part, int slot) {
     const int lane = threadIdx.x & 31;
-    double v = 0.0;
-    for (int q = lane; q < (int)gridDim.x; q += 32) v += __ldcg(part + slot * DRD_MAXB + q);
+    float v = 0.f;
+    for (int q = lane; q < (int)gridDim.x; q += 32) v += __ldcg(fslot(part, slot, q));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
-// Block partials of up to three per-thread FP32 values into part[slot][block] (slot < 0: none).
+// Block partials of up to three per-thread FP32 values into their slots (slot < 0: none).
 template <int NT>
 __device__ __forceinline__ void slots_put_f(double* part, int sl0, float v0, int sl1, float v1, int sl2, float v2,
                                             double* sm) {
     constexpr int NW = NT / 32;
-    static_assert(3 * NW <= 64, "shared scratch");
+    static_assert(3 * NW <= 128, "shared scratch");
+    float* smf = reinterpret_cast<float*>(sm);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int sl[3] = {sl0, sl1, sl2};
     float v[3] = {v0, v1, v2};
@@ -2001,19 +2005,19 @@ __device__ __forceinline__ void slots_put_f(double* part, int sl0, float v0, int
         if (sl[i] >= 0)
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
-    __syncthreads();  // an earlier sum may still read sm
+    __syncthreads();  // an earlier sum may still read the scratch
     if (lane == 0)
 #pragma unroll
-        for (int i = 0; i < 3; ++i) sm[i * NW + w] = (double)v[i];
+        for (int i = 0; i < 3; ++i) smf[i * NW + w] = v[i];
     __syncthreads();
     if (w == 0) {
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             if (sl[i] < 0) continue;
-            double r = lane < NW ? sm[i * NW + lane] : 0.0;
+            float r = lane < NW ? smf[i * NW + lane] : 0.f;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-            if (lane == 0) part[sl[i] * DRD_MAXB + blockIdx.x] = r;
+            if (lane == 0) *fslot(part, sl[i], blockIdx.x) = r;
         }
     }
 }
@@ -2452,10 +2456,10 @@ __device__ __forceinline__ float pb_pre(const PersistArgs& a, long q, float v) {
 }
 
 // State of one inner BiCGSTAB run (the local scalars of BICGSTABREVCOM).
-struct PbInner {
+struct PbInner {  // FP32 like the inner iterations themselves
     int info, iter;
     unsigned flags;
-    double resid, rho, rho1, alpha, omega, beta, snorm;
+    float resid, rho, rho1, alpha, omega, beta, snorm;
 };
 
 // The iterations (lib/BiCGSTABREVCOM.f:257-388) from R, RTLD, P = R (and, for the momentum
@@ -2475,15 +2479,16 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
     const long stride = (long)gridDim.x * PB_NT;
     const long q0 = blockIdx.x * (long)PB_NT + threadIdx.x;
     bool ok = true;
-    double rho = rho_first;
-    __shared__ double s_sc[4];  // scalars evaluated by thread 0, read by the block
+    const float bn = (float)bnrm2, tl = (float)tol, kbt = (float)kBreakTol;
+    float rho = (float)rho_first;
+    __shared__ float s_sc[4];  // scalars evaluated by thread 0, read by the block
     st.iter = 0;
     while (true) {
         st.rho = rho;
         st.iter += 1;
         pf.p = (a.prof != nullptr && st.iter == 3 && pf.k == 0) ? a.prof : nullptr;  // time iteration 3 once
         if (pf.p != nullptr && blockIdx.x == 0 && threadIdx.x == 0) pf.p[123] = gtimer();
-        if (fabs(st.rho) < kBreakTol) { st.info = -10; break; }  // (:261-263)
+        if (fabsf(st.rho) < kbt) { st.info = -10; break; }  // (:261-263)
         if constexpr (KIND == PK_CH) {
             if (!(ok = pb_psolve(a, a.p, a.phat, smem, gen, pf))) break;     // PHAT = M^-1 P
             if (!(ok = grid_sync(a.bar, gen, pf))) break;
@@ -2498,13 +2503,13 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         if (ha) { ra = __ldcg(a.r + qa); va = __ldcg(a.v + qa); ta = __ldcg(a.rtld + qa); }
         if (hb) { rb = __ldcg(a.r + qb); vb = __ldcg(a.v + qb); tb = __ldcg(a.rtld + qb); }
         if (threadIdx.x < 32) {
-            const double rv = warp_slot_sum(a.part, 4);
+            const float rv = warp_slot_sum(a.part, 4);
             if (threadIdx.x == 0) s_sc[0] = st.rho / rv;  // ALPHA (:307)
         }
         __syncthreads();
         st.alpha = s_sc[0];
         {
-            const float na = (float)(-st.alpha);
+            const float na = -st.alpha;
             float s2 = 0.f, rs = 0.f;
             auto s_elem = [&](long q, float r, float v, float t) {
                 const float sv = r + na * v;
@@ -2520,16 +2525,16 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         }
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
         if (threadIdx.x < 32) {
-            const double ss = warp_slot_sum(a.part, 5);
-            if (threadIdx.x == 0) s_sc[1] = sqrt(ss);
+            const float ss = warp_slot_sum(a.part, 5);
+            if (threadIdx.x == 0) s_sc[1] = sqrtf(ss);
         }
         __syncthreads();
         st.snorm = s_sc[1];
-        if (st.snorm <= tol) {  // early absolute test (:313-316): X = X + ALPHA PHAT
-            st.resid = st.snorm / bnrm2;
+        if (st.snorm <= tl) {  // early absolute test (:313-316): X = X + ALPHA PHAT
+            st.resid = st.snorm / bn;
             st.info = 0;
             st.flags |= DRD_FLAG_EARLY_S;
-            const float al = (float)st.alpha;
+            const float al = st.alpha;
             for (long q = q0; q < n; q += stride) a.x[q] = __ldcg(a.x + q) + al * __ldcg(a.phat + q);
             break;
         }
@@ -2550,25 +2555,25 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         if (ha) xrp_load(qa, ea);
         if (hb) xrp_load(qb, eb);
         if (threadIdx.x < 32) {
-            const double ts = warp_slot_sum(a.part, 6), tt = warp_slot_sum(a.part, 7);
-            const double rs = warp_slot_sum(a.part, 2), rt = warp_slot_sum(a.part, 1);
+            const float ts = warp_slot_sum(a.part, 6), tt = warp_slot_sum(a.part, 7);
+            const float rs = warp_slot_sum(a.part, 2), rt = warp_slot_sum(a.part, 1);
             if (threadIdx.x == 0) {
-                const double om = ts / tt;                                // (:349-350)
-                const double rn = rs - om * rt;                           // (rtld, S - OMEGA T)
+                const float om = ts / tt;                      // (:349-350)
+                const float rn = rs - om * rt;                 // (rtld, S - OMEGA T)
                 s_sc[0] = om;
                 s_sc[1] = rn;
-                s_sc[2] = (rn / st.rho) * (st.alpha / om);                // (:269) for the next iteration
+                s_sc[2] = (rn / st.rho) * (st.alpha / om);     // (:269) for the next iteration
             }
         }
         __syncthreads();
         st.omega = s_sc[0];
-        const double rho_new = s_sc[1];
+        const float rho_new = s_sc[1];
         st.beta = s_sc[2];
         {
             // X = X + ALPHA PHAT + OMEGA SHAT, R = S - OMEGA T (:354-359), ||R||^2, and the next
             // P = BETA (P - OMEGA V) + R (:273-275); two elements per pass, loads before stores
-            const float al = (float)st.alpha, om = (float)st.omega, nom = (float)(-st.omega);
-            const float bt = (float)st.beta;
+            const float al = st.alpha, om = st.omega, nom = -st.omega;
+            const float bt = st.beta;
             float r2 = 0.f;
             auto xrp = [&](long q, const float (&e)[7]) {
                 float xv = e[0] + al * e[1];
@@ -2594,16 +2599,16 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         }
         if (!(ok = grid_sync(a.bar, gen, pf))) break;
         if (threadIdx.x < 32) {
-            const double r2 = warp_slot_sum(a.part, 0);
-            if (threadIdx.x == 0) s_sc[3] = sqrt(r2) / bnrm2;  // STOPTEST2 (:361-362)
+            const float r2 = warp_slot_sum(a.part, 0);
+            if (threadIdx.x == 0) s_sc[3] = sqrtf(r2) / bn;  // STOPTEST2 (:361-362)
         }
         __syncthreads();
         st.resid = s_sc[3];
         if (!isfinite(st.resid)) { st.info = DRD_ERR_NONFINITE; break; }
-        if (st.resid <= tol) { st.info = 0; break; }
+        if (st.resid <= tl) { st.info = 0; break; }
         if (st.iter >= maxit) { st.info = 1; break; }
-        if (fabs(st.omega) < kBreakTol) {  // (:383-388)
-            st.info = (fabs(st.rho) < kBreakTol) ? -10 : -11;
+        if (fabsf(st.omega) < kbt) {  // (:383-388)
+            st.info = (fabsf(st.rho) < kbt) ? -10 : -11;
             break;
         }
         st.rho1 = st.rho;
