@@ -2654,8 +2654,9 @@ __device__ bool pb_residual64(const PersistArgs& a, bool with_b, double* sm, uns
             b2 += bq * bq;
         }
     }
-    slot_put<PB_NT>(a.part, 8, r2, sm);
-    if (with_b) slot_put<PB_NT>(a.part, 9, b2, sm);
+    // each thread's FP64 sums, then FP32 block and grid sums: the norms decide the sweep's tests
+    // to about 1e-7 relative, far inside any tolerance, and ||r|| itself cancels in the update
+    slots_put_f<PB_NT>(a.part, 8, (float)r2, with_b ? 9 : -1, (float)b2, -1, 0.f, sm);
     return true;
 }
 
@@ -2702,33 +2703,54 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
         double bnorm64 = 0.0, bnrm64 = 1.0, rnorm = 0.0, oresid = 0.0, prev = 0.0;
         bool ok = true, run = true;
         PbInner in{};
+        // the sweep's tests and scalars are evaluated by thread 0 (the other threads would only
+        // repeat its FP64 operations) and broadcast: rnorm, oresid, 1/rnorm, stop, oinfo, itol
+        __shared__ double s_rf[4];
+        __shared__ int s_rs[2];
         while (run) {
             if (!(ok = pb_residual64<KIND>(a, outer == 0, sm, gen, pf) && grid_sync(a.bar, gen, pf))) break;
-            const double2 rb = slot_sum2<PB_NT>(a.part, 8, 9, sm);
-            rnorm = sqrt(rb.x);
-            if (outer == 0) {  // k_mx_init
-                bnorm64 = sqrt(rb.y);
-                bnrm64 = bnorm64 == 0.0 ? 1.0 : bnorm64;
-                oresid = rnorm / bnrm64;
-                if (!isfinite(oresid)) { oinfo = DRD_ERR_NONFINITE; break; }
-                if (oresid <= otol || rnorm == 0.0) break;
-            } else {  // k_mx_check
-                prev = oresid;
-                oresid = rnorm / bnrm64;
-                inner_total += in.iter;
-                if (in.info == DRD_ERR_TIMEOUT) { oinfo = DRD_ERR_TIMEOUT; break; }
-                if (!isfinite(oresid)) { oinfo = DRD_ERR_NONFINITE; break; }
-                if (oresid <= otol) { oinfo = 0; break; }
-                if (outer >= a.max_refine) { oinfo = 1; break; }
-                if (oresid > 0.9 * prev) {  // a sweep that gained < 10 %: tighten the inner solves
-                    if (itol > kMixedItolFloor) itol *= 0.1;
-                    else { oinfo = 1; break; }  // stalled at the tightest inner tolerance
+            if (threadIdx.x < 32) {
+                const float r2 = warp_slot_sum(a.part, 8), b2 = outer == 0 ? warp_slot_sum(a.part, 9) : 0.f;
+                if (threadIdx.x == 0) {
+                    int stop = 0;
+                    rnorm = sqrt((double)r2);
+                    if (outer == 0) {  // k_mx_init
+                        bnorm64 = sqrt((double)b2);
+                        bnrm64 = bnorm64 == 0.0 ? 1.0 : bnorm64;
+                        oresid = rnorm / bnrm64;
+                        if (!isfinite(oresid)) { oinfo = DRD_ERR_NONFINITE; stop = 1; }
+                        else if (oresid <= otol || rnorm == 0.0) stop = 1;
+                    } else {  // k_mx_check
+                        prev = oresid;
+                        oresid = rnorm / bnrm64;
+                        if (in.info == DRD_ERR_TIMEOUT) { oinfo = DRD_ERR_TIMEOUT; stop = 1; }
+                        else if (!isfinite(oresid)) { oinfo = DRD_ERR_NONFINITE; stop = 1; }
+                        else if (oresid <= otol) { oinfo = 0; stop = 1; }
+                        else if (outer >= a.max_refine) { oinfo = 1; stop = 1; }
+                        else if (oresid > 0.9 * prev) {  // a sweep that gained < 10 %: tighten the inner solves
+                            if (itol > kMixedItolFloor) itol *= 0.1;
+                            else { oinfo = 1; stop = 1; }  // stalled at the tightest inner tolerance
+                        }
+                    }
+                    s_rf[0] = rnorm;
+                    s_rf[1] = oresid;
+                    s_rf[2] = rnorm > 0.0 ? 1.0 / rnorm : 0.0;
+                    s_rf[3] = itol;
+                    s_rs[0] = stop;
+                    s_rs[1] = oinfo;
                 }
             }
+            __syncthreads();
+            rnorm = s_rf[0];
+            oresid = s_rf[1];
+            itol = s_rf[3];
+            oinfo = s_rs[1];
+            if (outer > 0) inner_total += in.iter;
+            if (s_rs[0]) break;
             // scale and inner setup in one pass: b32 = r = rtld = r64 / ||r64||, x32 = 0
             {
-                const double sc = 1.0 / rnorm;
-                double bb = 0.0;
+                const double sc = s_rf[2];
+                float bb = 0.f;
                 for (long q = q0; q < n; q += stride) {
                     const float bv = (float)(__ldcg(a.r64 + q) * sc);
                     a.b[q] = bv;
@@ -2737,13 +2759,19 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
                     a.p[q] = bv;  // the first P = R (:268)
                     if constexpr (KIND == PK_UV) a.phat[q] = pb_pre(a, q, bv);
                     a.x[q] = 0.f;
-                    bb += (double)bv * (double)bv;
+                    bb = fmaf(bv, bv, bb);
                 }
-                slot_put<PB_NT>(a.part, 3, bb, sm);
+                slots_put_f<PB_NT>(a.part, 3, bb, -1, 0.f, -1, 0.f, sm);
             }
             if (!(ok = grid_sync(a.bar, gen, pf))) break;
-            const double bb = slot_sum<PB_NT>(a.part, 3, sm);
-            const double bn = sqrt(bb);
+            __shared__ double s_bb[2];
+            if (threadIdx.x < 32) {
+                const float bbs = warp_slot_sum(a.part, 3);
+                if (threadIdx.x == 0) { s_bb[0] = bbs; s_bb[1] = sqrt((double)bbs); }
+            }
+            __syncthreads();
+            const double bb = s_bb[0];
+            const double bn = s_bb[1];
             in = PbInner{};
             if (a.maxit <= 0) { in.info = -3; in.iter = a.maxit; }
             else if (!(ok = pb_iterate<KIND>(a, bn == 0.0 ? 1.0 : bn, itol, a.maxit, bb, in, smem, sm, gen, pf)))
