@@ -37,7 +37,7 @@ sys.path.insert(0, ROOT)
 METRIC = "time-steps/s and solves/s to FP64 resid 1e-8: learned+FP32 vs plain FP64, 1 GB300"
 # DRAM bytes (read + write) of one launch of the persistent CH solve kernel, from an ncu capture
 # of this workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch)
-TRAFFIC_CH = 4045568 + 570624
+TRAFFIC_CH = 4043776 + 558848
 WORKLOAD = ("420x180 serpentine channel (amp 30, period 140 cells, penalty 1e4), 3 rigid fibers 40x4, "
             "2 drops R=15, lambda_eta 5, Re 0.5, Ca 0.05; CH + momentum + pressure per step, tol 1e-8")
 
