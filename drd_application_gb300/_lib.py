@@ -61,6 +61,7 @@ SIGNATURES = {
     "drd_op_apply": (C.c_int, [_ctx, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     "drd_op_length": (C.c_long, [_ctx, C.c_int]),
     "drd_solve": (C.c_int, [_ctx, C.c_int, C.c_int, _dp, _dp, C.POINTER(abi.drd_status)]),
+    "drd_barrier_selftest": (C.c_int, [_ctx, C.c_int, C.POINTER(C.c_int)]),
     "drd_kernel_bench": (C.c_int, [_ctx, C.c_int, C.c_int, _dp, _dp, _dp]),
     "drd_flush_l2": (C.c_int, [_ctx, C.c_int64]),
     "drd_kernel_launches": (C.c_int64, [_ctx]),

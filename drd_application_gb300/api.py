@@ -263,6 +263,12 @@ class DRDContext:
     def synchronize(self):
         self._rc(self.L.drd_synchronize(self.h), "drd_synchronize", False)
 
+    def barrier_selftest(self, absent):
+        """Status of the grid barrier with block `absent` (1) or none (-1) missing: 0 or DRD_ERR_TIMEOUT."""
+        st = C.c_int(0)
+        self._rc(self.L.drd_barrier_selftest(self.h, int(absent), C.byref(st)), "drd_barrier_selftest", False)
+        return st.value
+
     def solve(self, system, b, x0=None, bdf=2):
         """A x = b for DRD_SYS_CH or DRD_SYS_UV with the context's coefficients -> (x, status)."""
         op = abi.DRD_OP_CH_MATVEC if system == abi.DRD_SYS_CH else abi.DRD_OP_UV_MATVEC

@@ -2890,6 +2890,23 @@ __global__ void k_stamp(KState* ks, int end, ull* ctr) {
     }
 }
 void launch_stamp(KState* ks, int end, ull* ctr, cudaStream_t s) { k_stamp<<<1, 32, 0, s>>>(ks, end, ctr); }
+// Two blocks run grid_sync; block `absent` (if any) returns without arriving, so the other's
+// bounded wait runs out: out[b] = 0 or DRD_ERR_TIMEOUT per block that ran the barrier.
+__global__ void k_bar_selftest(GridBar* bar, int absent, int* out, ull* ctr) {
+    count_launch(ctr);
+    if ((int)blockIdx.x == absent) {
+        if (threadIdx.x == 0) out[blockIdx.x] = 1;  // did not take part
+        return;
+    }
+    unsigned gen = 0u;
+    PbProf pf{nullptr, 0};
+    const bool ok = grid_sync(bar, gen, pf);
+    if (threadIdx.x == 0) out[blockIdx.x] = ok ? 0 : DRD_ERR_TIMEOUT;
+}
+void launch_bar_selftest(GridBar* bar, int absent, int* out, ull* ctr, cudaStream_t s) {
+    k_bar_reset<<<1, 32, 0, s>>>(bar, ctr);
+    k_bar_selftest<<<2, 32, 0, s>>>(bar, absent, out, ctr);
+}
 // Shared-memory plan (offsets in floats) of the persistent CH solver for an nr x nz grid run by
 // `grid` blocks within `budget` bytes: a work area (x-pass panels or z-pass columns), then the
 // resident z-pass operands and the block's x-pass B panel where they fit.

@@ -182,6 +182,7 @@ const void* persist_kernel(int kind);
 cudaError_t launch_bicg_persist(const PersistArgs& a, int grid, cudaStream_t s);
 void launch_bar_reset(GridBar* b, ull* ctr, cudaStream_t s);
 void launch_stamp(KState* ks, int end, ull* ctr, cudaStream_t s);
+void launch_bar_selftest(GridBar* bar, int absent, int* out, ull* ctr, cudaStream_t s);
 
 // ---- fiber particles (microfluidics_complex_domain/particles_move.f90), drd_particles.cu --
 constexpr int PT_GX = 64;  // blocks per bead in the per-bead sums

@@ -1984,6 +1984,18 @@ int drd_persist_profile(drd_ctx* c, int64_t* ns, int n) {
     return m;
 }
 
+int drd_barrier_selftest(drd_ctx* c, int absent, int* status) {
+    if (!c || !status || (absent != -1 && absent != 1)) return DRD_ERR_BADARG;
+    int* d_out = reinterpret_cast<int*>(c->pprof + 120);  // scratch: two ints of the profile buffer
+    launch_bar_selftest(c->bar, absent, d_out, c->ctr, c->s);
+    int h[2] = {0, 0};
+    CK(cudaMemcpyAsync(h, d_out, sizeof(h), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    CK(cudaGetLastError());
+    *status = (absent == 1) ? h[0] : (h[0] != 0 ? h[0] : h[1]);
+    return DRD_OK;
+}
+
 int drd_persistent_solver(drd_ctx* c, char* why, int len) {
     if (!c) return DRD_ERR_BADARG;
     if (why && len > 0) std::snprintf(why, (size_t)len, "%s", c->persist_err.c_str());

@@ -442,6 +442,11 @@ int drd_persistent_solver(drd_ctx* ctx, char* why, int len);
  * block 0: ns[2k], ns[2k+1] for barrier k (up to 62 barriers; zero where none ran).  Returns
  * the number of entries copied. */
 int drd_persist_profile(drd_ctx* ctx, int64_t* ns, int n);
+/* Failure detection of the persistent solver's grid barrier, without a fault: two blocks run
+ * the barrier; with absent = 1 the second block never arrives, and the first gives up after
+ * its bounded wait (a few seconds) and reports DRD_ERR_TIMEOUT in *status, as the solver
+ * would.  With absent = -1 both arrive and *status is 0.  The context stays usable. */
+int drd_barrier_selftest(drd_ctx* ctx, int absent, int* status);
 
 /* Number of kernels this library has launched on the context (graph nodes counted per
  * execution), cumulative. */

@@ -87,3 +87,22 @@ def _oracle_op(orc, case, op, x):
     if op == F.DRD_OP_UV_MATVEC:
         return orc.uv_matvec(2, k["rho"], k["eta"], k["bdr_pen"], x)
     return orc.uv_psolve(2, k["rho"], k["eta"], x)
+
+
+def test_grid_barrier_wait_is_bounded(cuda_lib):
+    """Failure detection without a fault: a block that never reaches the persistent solver's grid
+    barrier makes the waiting block give up after its bounded wait and report DRD_ERR_TIMEOUT;
+    the context stays usable afterwards."""
+    import time
+
+    P = abi.default_params(64, 32)
+    ctx = DRDContext(P)
+    assert ctx.barrier_selftest(-1) == 0
+    t0 = time.time()
+    assert ctx.barrier_selftest(1) == abi.DRD_ERR_TIMEOUT
+    assert time.time() - t0 < 60.0
+    x = np.ones(64 * 32)
+    y = ctx.op_apply(abi.DRD_OP_CH_PSOLVE, x)
+    assert np.all(np.isfinite(y))
+    assert ctx.barrier_selftest(-1) == 0
+    ctx.close()
