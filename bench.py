@@ -362,10 +362,10 @@ def run_gpu(args, ws, rank, local):
     flush = 512 << 20  # > 129 MB L2
     K, W = args.steps, max(3, args.warmup)
     K64 = args.fp64_steps if args.fp64_steps is not None else max(3, K // 4)
-    # the mixed leg and the drop-in e2e leg (same context) start each solve from the quadratic
-    # extrapolation 3 x^n - 3 x^(n-1) + x^(n-2) (guess_mode 2); the FP64 leg starts from x^n as the
-    # reference does
-    case = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED, guess_mode=2)
+    # the mixed leg and the drop-in e2e leg (same context) start each solve from the cubic
+    # extrapolation 4 x^n - 6 x^(n-1) + 4 x^(n-2) - x^(n-3) (guess_mode 3); the FP64 leg starts
+    # from x^n as the reference does
+    case = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED, guess_mode=3)
 
     # mixed (headline) path, resident state
     ctx = DRDContext(case.params)
@@ -397,7 +397,7 @@ def run_gpu(args, ws, rank, local):
     # the same mixed step with the fiber coupling of the reference loop (a 9-bead chain moved by
     # the flow, its forces spread onto the grid, rho/eta rebuilt every step) in place of the
     # rigid fibers: reported beside the headline, not part of it
-    casep = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED, guess_mode=2,
+    casep = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED, guess_mode=3,
                       particles=True)
     ctxp = DRDContext(casep.params)
     ctxp.set_case(casep)
@@ -464,7 +464,7 @@ def run_gpu(args, ws, rank, local):
         "data": "synthetic (seeded geometry, fibers and drops per rank)",
         "config": {
             "workload": WORKLOAD, "nr": args.nr, "nz": args.nz, "path": "mixed: FP32 BiCGSTAB in FP64 refinement",
-            "initial_guess": "mixed and e2e legs: quadratic extrapolation 3x^n - 3x^(n-1) + x^(n-2) (guess_mode 2); fp64 leg: x^n",
+            "initial_guess": "mixed and e2e legs: cubic extrapolation 4x^n - 6x^(n-1) + 4x^(n-2) - x^(n-3) (guess_mode 3); fp64 leg: x^n",
             "inner_ch_solver": "persistent cooperative kernel" if persist[0] else
             f"kernel-per-phase graph loop ({persist[1] or 'persistent solver off'})",
             "parallelism": f"replicas x{ws}", "l2": "flushed between timed steps (512 MiB write)",

@@ -141,11 +141,11 @@ __device__ __forceinline__ double bulk_mf(double phi, double psi) {
 }
 
 // rhs = -f1 + s f2/eps - eps L_Mi(f2) (:37-48) packed by Atob; x0 = Atob(rmu) (:62-63).
-// With rmu_pre non-NULL the guess is extrapolated: 2 rmu - rmu_pre, and with rmu_pre2 too,
-// quadratically: 3 rmu - 3 rmu_pre + rmu_pre2.
+// With rmu_pre non-NULL the guess is extrapolated: 2 rmu - rmu_pre; with rmu_pre2 too,
+// quadratically: 3 rmu - 3 rmu_pre + rmu_pre2; with rmu_pre3, cubically.
 __global__ void k_ch_rhs(DevParams P, const double* __restrict__ ph, const double* __restrict__ rmu,
                          const double* __restrict__ rmu_pre, const double* __restrict__ rmu_pre2,
-                         const double* __restrict__ bdr,
+                         const double* __restrict__ rmu_pre3, const double* __restrict__ bdr,
                          const double* __restrict__ grad, const double* __restrict__ Mi,
                          const double* __restrict__ f2, double* __restrict__ b, double* __restrict__ x, ull* ctr) {
     count_launch(ctr);
@@ -160,7 +160,10 @@ __global__ void k_ch_rhs(DevParams P, const double* __restrict__ ph, const doubl
         double f1 = P.s * p0 / P.eps - bulk_mf(p0, bdr[c]) / P.eps - p0 * (p0 - 1.0) * grad[c] * P.cang / sq2;
         const double ff = op_dgn<double>(i, k, nr, nz, P.idr2, P.idz2, F, M);
         b[q] = -f1 + P.s * f2[c] / P.eps - P.eps * ff;
-        x[q] = rmu_pre2 ? 3.0 * (rmu[c] - rmu_pre[c]) + rmu_pre2[c] : rmu_pre ? 2.0 * rmu[c] - rmu_pre[c] : rmu[c];
+        x[q] = rmu_pre3   ? 4.0 * (rmu[c] + rmu_pre2[c]) - 6.0 * rmu_pre[c] - rmu_pre3[c]
+               : rmu_pre2 ? 3.0 * (rmu[c] - rmu_pre[c]) + rmu_pre2[c]
+               : rmu_pre  ? 2.0 * rmu[c] - rmu_pre[c]
+                          : rmu[c];
     }
 }
 
@@ -622,7 +625,8 @@ __global__ void k_uv_rhs(DevParams P, int bdf, const CallArgs* __restrict__ ca, 
                          const double* __restrict__ rmu, const double* __restrict__ pf1,
                          const double* __restrict__ pf2, double* __restrict__ b, double* __restrict__ x,
                          double* __restrict__ uL, int extrap, const double* __restrict__ u_pre2,
-                         const double* __restrict__ v_pre2, ull* ctr) {
+                         const double* __restrict__ v_pre2, const double* __restrict__ u_pre3,
+                         const double* __restrict__ v_pre3, ull* ctr) {
     count_launch(ctr);
     const int nr = P.nr, nz = P.nz;
     const long mn = (long)(nr + 1) * nz, N = mn + (long)nr * (nz - 1);
@@ -673,8 +677,10 @@ __global__ void k_uv_rhs(DevParams P, int bdf, const CallArgs* __restrict__ ca, 
                 fu = fu + dt * (2.0 * P.uwT / P.dz2 * etay);
             }
             b[q] = fu;
-            x[q] = extrap == 2 ? 3.0 * (uu - u_pre[uidx(nr, i, k)]) + u_pre2[uidx(nr, i, k)]
-                   : extrap ? 2.0 * uu - u_pre[uidx(nr, i, k)] : uu;
+            const long ui = uidx(nr, i, k);
+            x[q] = extrap == 3 ? 4.0 * (uu + u_pre2[ui]) - 6.0 * u_pre[ui] - u_pre3[ui]
+                   : extrap == 2 ? 3.0 * (uu - u_pre[ui]) + u_pre2[ui]
+                   : extrap ? 2.0 * uu - u_pre[ui] : uu;
         } else {
             const long qv = q - mn;
             const int i = (int)(qv % nr), k = (int)(qv / nr) + 1;
@@ -695,8 +701,10 @@ __global__ void k_uv_rhs(DevParams P, int bdf, const CallArgs* __restrict__ ca, 
             fv = fv + (C_(pf2, i, k) + C_(pf2, i, k - 1)) / 2.0;
             fv = fv * dt;
             b[q] = fv;
-            x[q] = extrap == 2 ? 3.0 * (vv - v_pre[vidx(nr, i, k)]) + v_pre2[vidx(nr, i, k)]
-                   : extrap ? 2.0 * vv - v_pre[vidx(nr, i, k)] : vv;
+            const long vi = vidx(nr, i, k);
+            x[q] = extrap == 3 ? 4.0 * (vv + v_pre2[vi]) - 6.0 * v_pre[vi] - v_pre3[vi]
+                   : extrap == 2 ? 3.0 * (vv - v_pre[vi]) + v_pre2[vi]
+                   : extrap ? 2.0 * vv - v_pre[vi] : vv;
         }
     }
 #undef UT
@@ -2969,9 +2977,9 @@ void launch_ch_f2(const DevParams& P, const double* u, const double* v, const do
     k_ch_f2<<<GRID((long)(P.nr + 2) * (P.nz + 2))>>>(P, u, v, ph, f2, ctr);
 }
 void launch_ch_rhs(const DevParams& P, const double* ph, const double* rmu, const double* rmu_pre,
-                   const double* rmu_pre2, const double* bdr, const double* grad, const double* Mi, const double* f2,
-                   double* b, double* x, ull* ctr, cudaStream_t s) {
-    k_ch_rhs<<<GRID((long)P.nr * P.nz)>>>(P, ph, rmu, rmu_pre, rmu_pre2, bdr, grad, Mi, f2, b, x, ctr);
+                   const double* rmu_pre2, const double* rmu_pre3, const double* bdr, const double* grad,
+                   const double* Mi, const double* f2, double* b, double* x, ull* ctr, cudaStream_t s) {
+    k_ch_rhs<<<GRID((long)P.nr * P.nz)>>>(P, ph, rmu, rmu_pre, rmu_pre2, rmu_pre3, bdr, grad, Mi, f2, b, x, ctr);
 }
 template <typename T>
 void launch_ch_matvec(const OpScal<T>& o, const T* M0, const T* Mi, T alpha, const T* x, T beta, T* y, T* ff1,
@@ -3052,10 +3060,11 @@ void launch_uv_rhs(const DevParams& P, int bdf, const CallArgs* ca, const double
                    const double* u_pre, const double* u, const double* v_pre, const double* v, const double* p,
                    const double* rho, const double* eta, const double* bdr, const double* used, const double* ph_after,
                    const double* rmu_after, const double* pf1, const double* pf2, double* b, double* x, double* uL,
-                   int extrap, const double* u_pre2, const double* v_pre2, ull* ctr, cudaStream_t s) {
+                   int extrap, const double* u_pre2, const double* v_pre2, const double* u_pre3,
+                   const double* v_pre3, ull* ctr, cudaStream_t s) {
     const long N = (long)(P.nr + 1) * P.nz + (long)P.nr * (P.nz - 1);
     k_uv_rhs<<<GRID(N)>>>(P, bdf, ca, psi1, psi2, u_pre, u, v_pre, v, p, rho, eta, bdr, used, ph_after, rmu_after, pf1,
-                          pf2, b, x, uL, extrap, u_pre2, v_pre2, ctr);
+                          pf2, b, x, uL, extrap, u_pre2, v_pre2, u_pre3, v_pre3, ctr);
 }
 template <typename T>
 void launch_uv_matvec(const OpScal<T>& o, const T* rho, const T* eta, const T* pen, T alpha, const T* x, T beta, T* y,

@@ -57,8 +57,8 @@ void launch_gemm(int cfg, int epi, const GemmArgs<T>& a, cudaStream_t s);
 // ---- CH (microfluidics_complex_domain/PhSolve.f90) -------------------------------------
 void launch_ch_f2(const DevParams& P, const double* u, const double* v, const double* ph, double* f2, ull* ctr, cudaStream_t s);
 void launch_ch_rhs(const DevParams& P, const double* ph, const double* rmu, const double* rmu_pre,
-                   const double* rmu_pre2, const double* bdr, const double* grad, const double* Mi, const double* f2,
-                   double* b, double* x, ull* ctr, cudaStream_t s);
+                   const double* rmu_pre2, const double* rmu_pre3, const double* bdr, const double* grad,
+                   const double* Mi, const double* f2, double* b, double* x, ull* ctr, cudaStream_t s);
 template <typename T>
 void launch_ch_matvec(const OpScal<T>& o, const T* M0, const T* Mi, T alpha, const T* x, T beta, T* y, T* ff1,
                       const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,
@@ -109,8 +109,8 @@ void launch_uv_rhs(const DevParams& P, int bdf, const CallArgs* ca, const double
                    const double* u_pre, const double* u, const double* v_pre, const double* v, const double* p,
                    const double* rho, const double* eta, const double* bdr, const double* used, const double* ph_after,
                    const double* rmu_after, const double* pf1, const double* pf2, double* b, double* x, double* uL,
-                   int extrap, const double* u_pre2, const double* v_pre2, ull* ctr,
-                   cudaStream_t s);
+                   int extrap, const double* u_pre2, const double* v_pre2,
+                   const double* u_pre3, const double* v_pre3, ull* ctr, cudaStream_t s);
 template <typename T>
 void launch_uv_matvec(const OpScal<T>& o, const T* rho, const T* eta, const T* pen, T alpha, const T* x, T beta, T* y,
                       const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,

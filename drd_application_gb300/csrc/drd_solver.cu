@@ -79,10 +79,11 @@ struct drd_ctx {
     // PhSolve_ori: wall-energy prefactors cf of angleB / angleT (XLINE) and alpha_s
     double *ori_cfb, *ori_cft;
     // drd_phsolve with guess_mode 1: the rmu of the previous call (the x^(n-1) of the next one)
-    double *rmu_prev, *rmu_prev2;
-    int rmu_hist = 0;  // how many of rmu_prev, rmu_prev2 hold earlier calls' rmu
-    // guess_mode 2: the fields two steps back (rmu, u, v), and how many steps of history exist
-    double *rmu_pre2, *u_pre2, *v_pre2;
+    double *rmu_prev, *rmu_prev2, *rmu_prev3;
+    int rmu_hist = 0;  // how many of rmu_prev.. hold earlier calls' rmu
+    // guess_mode 2 / 3: the fields two and three steps back (rmu, u, v), and how many steps of
+    // history exist (uv_hist: earlier calls' u_pre held by the per-routine momentum solve)
+    double *rmu_pre2, *u_pre2, *v_pre2, *rmu_pre3, *u_pre3, *v_pre3;
     int hist = 0, uv_hist = 0;
     double ori_alpha = 0.0;
     // persistent cooperative inner solver (FP32 CH): grid size, barrier state, on/off
@@ -159,8 +160,9 @@ size_t arena_need(long cs, long us, long vs, long nc, long nr, long nz, long nma
     for (int i = 0; i < 4; ++i) add(2 * DRD_PARTICLES_MAX, 8);  // pts, pts_old, totF, psum
     add(3 * DRD_PARTICLES_MAX * PT_GX, 8); add(cs, 8);          // ppart, bdist
     add(nr + 1, 8); add(nr + 1, 8);                            // ori_cfb, ori_cft
-    add(cs, 8); add(cs, 8);                                    // rmu_prev, rmu_prev2
+    add(cs, 8); add(cs, 8); add(cs, 8);                        // rmu_prev, rmu_prev2, rmu_prev3
     add(cs, 8); add(us, 8); add(vs, 8);                        // rmu_pre2, u_pre2, v_pre2
+    add(cs, 8); add(us, 8); add(vs, 8);                        // rmu_pre3, u_pre3, v_pre3
     add(sizeof(GridBar), 1);                                   // bar
     add(128, 8);                                               // pprof
     const long fu = (nr / 2 + 1) * (nr / 2 + 2), nes = 3 * (us + vs);
@@ -781,12 +783,14 @@ int mixed_of(drd_ctx* c) { return c->P.precision == DRD_PREC_MIXED; }
 int mixed_for(drd_ctx* c, int slot) { return mixed_of(c) && !(slot == KS_CH && c->ch_fp64); }
 
 // PhSolve (microfluidics_complex_domain/PhSolve.f90:1-126) on fld[U,V,PH,RMU] -> rmu_after, ph_after.
-// extrap: the initial guess is 2 rmu - rmu_pre (1) or 3 rmu - 3 rmu_pre + rmu_pre2 (2).
+// extrap: the initial guess is 2 rmu - rmu_pre (1), 3 rmu - 3 rmu_pre + rmu_pre2 (2) or
+// 4 rmu - 6 rmu_pre + 4 rmu_pre2 - rmu_pre3 (3).
 int enq_ch(drd_ctx* c, cudaStream_t s, int extrap = 0) {
     const DevParams& P = c->dp;
     launch_ch_f2(P, c->fld[DRD_F_U], c->fld[DRD_F_V], c->fld[DRD_F_PH], c->f2, c->ctr, s);
     launch_ch_rhs(P, c->fld[DRD_F_PH], c->fld[DRD_F_RMU], extrap ? c->fld[DRD_F_RMU_PRE] : nullptr,
-                  extrap == 2 ? c->rmu_pre2 : nullptr, c->bdr, c->grad, c->Mi, c->f2, c->k64.b, c->k64.x, c->ctr, s);
+                  extrap >= 2 ? c->rmu_pre2 : nullptr, extrap == 3 ? c->rmu_pre3 : nullptr, c->bdr, c->grad, c->Mi,
+                  c->f2, c->k64.b, c->k64.x, c->ctr, s);
     int rc = enq_solve(c, sys_of(c, SYS_CH, 0), KS_CH, c->P.tol, c->P.ch_maxit, mixed_for(c, KS_CH), s);
     if (rc) return rc;
     launch_ch_fin(P, c->k64.x, c->f2, c->M0, c->rmu_after, c->ph_after, c->ctr, s);
@@ -823,13 +827,15 @@ int enq_phmu(drd_ctx* c, cudaStream_t s, int extrap = 0) {
 }
 
 // VeloSolve_combined (bdf 1) / VeloSolve_2_combined (bdf 2) -> u_after, v_after.
-// extrap (BDF2 only): the guess is 2 u - u_pre (1) or 3 u - 3 u_pre + u_pre2 (2), v likewise.
+// extrap (BDF2 only): the guess extrapolates u through u_pre, u_pre2, u_pre3 linearly (1),
+// quadratically (2) or cubically (3); v likewise.
 int enq_uv(drd_ctx* c, int bdf, cudaStream_t s, int extrap = 0) {
     const DevParams& P = c->dp;
     double** f = c->fld;
     launch_uv_rhs(P, bdf, c->ca, f[DRD_F_PSI1], f[DRD_F_PSI2], f[DRD_F_U_PRE], f[DRD_F_U], f[DRD_F_V_PRE], f[DRD_F_V],
                   f[DRD_F_P], c->rho, c->eta, c->bdr, c->used, c->ph_after, c->rmu_after, f[DRD_F_PF1], f[DRD_F_PF2],
-                  c->k64.b, c->k64.x, c->uL, bdf == 2 ? extrap : 0, c->u_pre2, c->v_pre2, c->ctr, s);
+                  c->k64.b, c->k64.x, c->uL, bdf == 2 ? extrap : 0, c->u_pre2, c->v_pre2, c->u_pre3, c->v_pre3,
+                  c->ctr, s);
     int rc = enq_solve(c, sys_of(c, SYS_UV, bdf), KS_UV, c->P.tol, c->P.uv_maxit, mixed_of(c), s);
     if (rc) return rc;
     launch_uv_fin(P, c->k64.x, c->uL, c->u_after, c->v_after, c->ctr, s);
@@ -897,7 +903,12 @@ int enq_step(drd_ctx* c, int first, int extrap, cudaStream_t s) {
     if (c->pp.np > 0) enq_particles(c, PT_FORCE | PT_MOVE | PT_COEF, f[DRD_F_U], f[DRD_F_V], s);
     rc = enq_uv(c, first ? 1 : 2, s, extrap);
     if (rc) return rc;
-    if (c->P.guess_mode == 2) {  // the fields two steps back, for the next step's guess
+    if (c->P.guess_mode == 3) {  // the fields three steps back, for the next step's guess
+        CK(cudaMemcpyAsync(c->u_pre3, c->u_pre2, ub, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(c->v_pre3, c->v_pre2, vb, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(c->rmu_pre3, c->rmu_pre2, cb, cudaMemcpyDeviceToDevice, s));
+    }
+    if (c->P.guess_mode >= 2) {  // the fields two steps back
         CK(cudaMemcpyAsync(c->u_pre2, f[DRD_F_U_PRE], ub, cudaMemcpyDeviceToDevice, s));
         CK(cudaMemcpyAsync(c->v_pre2, f[DRD_F_V_PRE], vb, cudaMemcpyDeviceToDevice, s));
         CK(cudaMemcpyAsync(c->rmu_pre2, f[DRD_F_RMU_PRE], cb, cudaMemcpyDeviceToDevice, s));
@@ -1124,8 +1135,9 @@ int setup_context(drd_ctx* c) {
     c->totF = carve<double>(c, 2 * DRD_PARTICLES_MAX); c->psum = carve<double>(c, 2 * DRD_PARTICLES_MAX);
     c->ppart = carve<double>(c, 3 * DRD_PARTICLES_MAX * PT_GX); c->bdist = carve<double>(c, c->cs);
     c->ori_cfb = carve<double>(c, nr + 1); c->ori_cft = carve<double>(c, nr + 1);
-    c->rmu_prev = carve<double>(c, c->cs); c->rmu_prev2 = carve<double>(c, c->cs);
+    c->rmu_prev = carve<double>(c, c->cs); c->rmu_prev2 = carve<double>(c, c->cs); c->rmu_prev3 = carve<double>(c, c->cs);
     c->rmu_pre2 = carve<double>(c, c->cs); c->u_pre2 = carve<double>(c, c->us); c->v_pre2 = carve<double>(c, c->vs);
+    c->rmu_pre3 = carve<double>(c, c->cs); c->u_pre3 = carve<double>(c, c->us); c->v_pre3 = carve<double>(c, c->vs);
     c->bar = (GridBar*)carve<char>(c, sizeof(GridBar));
     c->pprof = (unsigned long long*)carve<double>(c, 128);
     c->Ku = nr / 2 + 1; c->Nue = (nr + 2) / 2; c->Nuo = (nr + 1) / 2;
@@ -1224,7 +1236,7 @@ int validate(const drd_params* p, std::string& why) {
     if (p->variant == DRD_VARIANT_TP && p->phi_mode != 1 && p->phi_mode != 2) { why = "phi_mode must be 1 or 2"; return DRD_ERR_BADARG; }
     if (p->ch_maxit <= 0 || p->uv_maxit <= 0 || p->phmu_maxit <= 0) { why = "maxit must be positive"; return DRD_ERR_BADARG; }
     if (p->xlsB >= 1.e-8) { why = "slip walls (xlsB >= 1e-8) have no solve in the reference"; return DRD_ERR_UNSUPPORTED; }
-    if (p->guess_mode < 0 || p->guess_mode > 2) { why = "guess_mode must be 0, 1 or 2"; return DRD_ERR_BADARG; }
+    if (p->guess_mode < 0 || p->guess_mode > 3) { why = "guess_mode must be 0 to 3"; return DRD_ERR_BADARG; }
     if (p->uv_precond != DRD_UV_JACOBI && p->uv_precond != DRD_UV_ESOLP) { why = "unknown uv_precond"; return DRD_ERR_BADARG; }
     if (p->precision == DRD_PREC_MIXED && (!(p->mixed_inner_tol > 0) || p->mixed_max_refine <= 0)) {
         why = "mixed precision needs mixed_inner_tol > 0 and mixed_max_refine > 0";
@@ -1616,14 +1628,16 @@ int drd_phsolve(drd_ctx* c, const double* u, const double* v, const double* ph, 
     const int gm = c->P.guess_mode;
     const int extrap = std::min(gm, c->rmu_hist);
     if (extrap >= 1) CK(cudaMemcpyAsync(c->fld[DRD_F_RMU_PRE], c->rmu_prev, cb, cudaMemcpyDeviceToDevice, c->s));
-    if (extrap == 2) CK(cudaMemcpyAsync(c->rmu_pre2, c->rmu_prev2, cb, cudaMemcpyDeviceToDevice, c->s));
+    if (extrap >= 2) CK(cudaMemcpyAsync(c->rmu_pre2, c->rmu_prev2, cb, cudaMemcpyDeviceToDevice, c->s));
+    if (extrap == 3) CK(cudaMemcpyAsync(c->rmu_pre3, c->rmu_prev3, cb, cudaMemcpyDeviceToDevice, c->s));
     int rc = up(c, c->fld[DRD_F_U], u, c->us) | up(c, c->fld[DRD_F_V], v, c->vs) | up(c, c->fld[DRD_F_PH], ph, c->cs) |
              up(c, c->fld[DRD_F_RMU], rmu, c->cs);
     if (rc) return DRD_ERR_CUDA;
     if (gm >= 1) {
-        if (gm == 2) CK(cudaMemcpyAsync(c->rmu_prev2, c->rmu_prev, cb, cudaMemcpyDeviceToDevice, c->s));
+        if (gm == 3) CK(cudaMemcpyAsync(c->rmu_prev3, c->rmu_prev2, cb, cudaMemcpyDeviceToDevice, c->s));
+        if (gm >= 2) CK(cudaMemcpyAsync(c->rmu_prev2, c->rmu_prev, cb, cudaMemcpyDeviceToDevice, c->s));
         CK(cudaMemcpyAsync(c->rmu_prev, c->fld[DRD_F_RMU], cb, cudaMemcpyDeviceToDevice, c->s));
-        c->rmu_hist = std::min(c->rmu_hist + 1, 2);
+        c->rmu_hist = std::min(c->rmu_hist + 1, 3);
     }
     rc = run_graph(c, gkey(GK_CH, mixed_of(c), extrap), [&](cudaStream_t s) { return enq_ch(c, s, extrap); }, t, 0.0);
     if (rc) return rc;
@@ -1673,14 +1687,19 @@ static int velo_common(drd_ctx* c, int bdf, const double* psi1, const double* ps
     // guess_mode 1 / 2 (BDF2): the momentum solve starts from 2 u - u_pre, or from 3 u - 3 u_pre +
     // u_pre2 with u_pre2 the u_pre of the previous call; v likewise
     const int gm = c->P.guess_mode;
-    const int extrap = bdf != 2 ? 0 : (gm == 2 && c->uv_hist >= 1) ? 2 : (gm >= 1 ? 1 : 0);
-    rc = run_graph(c, gkey(GK_UV, mixed_of(c), bdf + 3 * extrap), [&](cudaStream_t s) { return enq_uv(c, bdf, s, extrap); },
+    const int extrap = (bdf != 2 || gm == 0) ? 0 : std::min(gm, 1 + c->uv_hist);
+    rc = run_graph(c, gkey(GK_UV, mixed_of(c), bdf + 2 * extrap), [&](cudaStream_t s) { return enq_uv(c, bdf, s, extrap); },
                    t, 0.0);
     if (rc) return rc;
-    if (gm == 2 && bdf == 2) {
-        CK(cudaMemcpyAsync(c->u_pre2, c->fld[DRD_F_U_PRE], sizeof(double) * c->us, cudaMemcpyDeviceToDevice, c->s));
-        CK(cudaMemcpyAsync(c->v_pre2, c->fld[DRD_F_V_PRE], sizeof(double) * c->vs, cudaMemcpyDeviceToDevice, c->s));
-        c->uv_hist = 1;
+    if (gm >= 2 && bdf == 2) {  // this call's u_pre is the next call's u_pre2
+        const size_t ub = sizeof(double) * c->us, vb = sizeof(double) * c->vs;
+        if (gm == 3) {
+            CK(cudaMemcpyAsync(c->u_pre3, c->u_pre2, ub, cudaMemcpyDeviceToDevice, c->s));
+            CK(cudaMemcpyAsync(c->v_pre3, c->v_pre2, vb, cudaMemcpyDeviceToDevice, c->s));
+        }
+        CK(cudaMemcpyAsync(c->u_pre2, c->fld[DRD_F_U_PRE], ub, cudaMemcpyDeviceToDevice, c->s));
+        CK(cudaMemcpyAsync(c->v_pre2, c->fld[DRD_F_V_PRE], vb, cudaMemcpyDeviceToDevice, c->s));
+        c->uv_hist = std::min(c->uv_hist + 1, 2);
     }
     if (rc) return rc;
     rc = down(c, u_after, c->u_after, c->us) | down(c, v_after, c->v_after, c->vs);
@@ -1761,7 +1780,7 @@ int drd_state_upload(drd_ctx* c, int field, const double* host) {
     const long n = (field == DRD_F_U || field == DRD_F_U_PRE) ? c->us : (field == DRD_F_V || field == DRD_F_V_PRE) ? c->vs : c->cs;
     CK(cudaMemcpyAsync(c->fld[field], host, sizeof(double) * n, cudaMemcpyHostToDevice, c->s));
     CK(cudaStreamSynchronize(c->s));
-    c->hist = 0;  // a new state: no step history for the quadratic guess
+    c->hist = 0;  // a new state: no step history for the extrapolated guesses
     return DRD_OK;
 }
 
@@ -1786,13 +1805,13 @@ int drd_steps_async(drd_ctx* c, int first, double t, int nsteps) {
         const double gamma1 = std::min(1.0, c->P.lambda_rho);
         const double coef = fst ? c->P.re * gamma1 / c->P.dt : 3 * c->P.re * gamma1 / 2. / c->P.dt;
         const double tt = t + k * c->P.dt + c->P.dt;
-        // the guess of this step: quadratic once two earlier steps are held, else linear
+        // the guess of this step: the polynomial of order guess_mode through the steps held
         const int gm = c->P.guess_mode;
-        const int extrap = fst ? 0 : (gm == 2 && c->hist >= 2) ? 2 : (gm >= 1 ? 1 : 0);
+        const int extrap = (fst || gm == 0) ? 0 : std::min(gm, std::max(c->hist, 1));
         int rc = run_graph(c, gkey(GK_STEP, mixed_of(c), fst + 2 * extrap),
                            [&](cudaStream_t s) { return enq_step(c, fst, extrap, s); }, tt, coef);
         if (rc) return rc;
-        c->hist = fst ? 1 : std::min(c->hist + 1, 2);
+        c->hist = fst ? 1 : std::min(c->hist + 1, 3);
     }
     return DRD_OK;
 }

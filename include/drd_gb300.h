@@ -83,11 +83,12 @@ typedef struct drd_params {
     int32_t uv_maxit;      /* VeloSolve ITER, 800 MF (VeloSolve_2_combined.f90:398), 2000 TP       */
     int32_t phmu_maxit;    /* ph_mu_solve ITER, 5000 (TP/ph_mu_solve.f90:156)                      */
     int32_t guess_mode;    /* initial guess of the CH and momentum solves: 0 = the previous step's */
-                           /* field (the reference), 1 = linear extrapolation 2 x^n - x^(n-1),   */
-                           /* 2 = quadratic 3 x^n - 3 x^(n-1) + x^(n-2) (linear until two earlier */
-                           /* steps are held): drd_step; drd_velosolve_2_combined from u_pre,     */
-                           /* v_pre and the previous call's u_pre, v_pre; drd_phsolve from the    */
-                           /* rmu of the context's previous drd_phsolve calls                    */
+                           /* field (the reference); 1, 2, 3 = the polynomial extrapolation of   */
+                           /* that order through the last 2, 3, 4 steps (lower orders until the  */
+                           /* steps are held): 2 x^n - x^(n-1); 3 x^n - 3 x^(n-1) + x^(n-2);     */
+                           /* 4 x^n - 6 x^(n-1) + 4 x^(n-2) - x^(n-3).  drd_step keeps the      */
+                           /* history on the device; drd_velosolve_2_combined extrapolates from  */
+                           /* u_pre and earlier calls' u_pre, drd_phsolve from earlier calls' rmu */
     double dr, dz, dt;     /* grid spacing and time step (finit.f90:25-28,397)                    */
     double xld, re, ca;    /* 1/Pe, Reynolds, capillary number (input deck lines 1-3)             */
     double I_thickness;    /* interface thickness epsilon (deck line 18)                           */

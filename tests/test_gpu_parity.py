@@ -254,7 +254,7 @@ def test_mixed_velosolve_reaches_fp64_tolerance(mf_case):
     ctx.close()
 
 
-@pytest.mark.parametrize("gm", [1, 2])
+@pytest.mark.parametrize("gm", [1, 2, 3])
 def test_drop_in_guess_extrapolation_keeps_the_answer(mf_case, gm):
     """guess_mode 1 / 2 on the per-routine calls: PhSolve extrapolates rmu through the previous
     calls' rmu, VeloSolve_2_combined u through u_pre (and the previous call's u_pre).  Only the
@@ -263,7 +263,7 @@ def test_drop_in_guess_extrapolation_keeps_the_answer(mf_case, gm):
     out = []
     for g in (0, gm):
         ctx, _ = _ctx(case, tol=1e-12, guess_mode=g)
-        for _ in range(2):  # two earlier calls: the history the quadratic guess reads
+        for _ in range(3):  # earlier calls: the history the quadratic and cubic guesses read
             ctx.PhSolve(st[F.F_U_PRE], st[F.F_V_PRE], st[F.F_PH_PRE], st[F.F_RMU_PRE], t - case.params.dt)
             ctx.VeloSolve_2_combined(st[F.F_PSI1], st[F.F_PSI2], st[F.F_U_PRE], st[F.F_U], st[F.F_V_PRE], st[F.F_V],
                                      st[F.F_P], None, st[F.F_PH], None, st[F.F_RMU], t)
@@ -279,7 +279,8 @@ def test_drop_in_guess_extrapolation_keeps_the_answer(mf_case, gm):
 
 # ------------------------------------------------------------------------------- step sequence
 @pytest.mark.parametrize("precision,guess", [(abi.DRD_PREC_FP64, 0), (abi.DRD_PREC_MIXED, 0), (abi.DRD_PREC_MIXED, 1),
-                                             (abi.DRD_PREC_MIXED, 2), (abi.DRD_PREC_FP64, 2)])
+                                             (abi.DRD_PREC_MIXED, 2), (abi.DRD_PREC_FP64, 2),
+                                             (abi.DRD_PREC_MIXED, 3)])
 def test_step_sequence_matches_oracle(cuda_lib, oracle_build, precision, guess):
     """Four mcl6 steps on the resident state against the oracle at tol 1e-12, where the result
     no longer depends on the Krylov guess (guess_mode 1 extrapolates it)."""
