@@ -176,7 +176,7 @@ def default_params(nr, nz, **kw):
     p.lambda_rho, p.lambda_eta = 1.0, 100.0
     p.bdr_ph_used_adjust = 1.0e-6
     p.dt = min(p.dr, p.dz) * 0.1
-    p.mixed_inner_tol = 0.1
+    p.mixed_inner_tol = 0.2
     p.mixed_max_refine = 30
     for k, v in kw.items():
         if not hasattr(p, k):

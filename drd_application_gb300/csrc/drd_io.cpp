@@ -214,7 +214,7 @@ int drd_params_from_deck(const drd_deck* d, int nr, int nz, int variant, drd_par
     p->lambda_rho = d->lambda_rho;
     p->lambda_eta = d->lambda_eta;
     p->bdr_ph_used_adjust = 1.0e-6;
-    p->mixed_inner_tol = 0.1;
+    p->mixed_inner_tol = 0.2;
     p->mixed_max_refine = 30;
     p->uv_precond = DRD_UV_JACOBI;                    // PSolve_uv_2_CG of the MF application
     return DRD_OK;
