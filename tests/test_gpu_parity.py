@@ -280,7 +280,7 @@ def test_drop_in_guess_extrapolation_keeps_the_answer(mf_case, gm):
 # ------------------------------------------------------------------------------- step sequence
 @pytest.mark.parametrize("precision,guess", [(abi.DRD_PREC_FP64, 0), (abi.DRD_PREC_MIXED, 0), (abi.DRD_PREC_MIXED, 1),
                                              (abi.DRD_PREC_MIXED, 2), (abi.DRD_PREC_FP64, 2),
-                                             (abi.DRD_PREC_MIXED, 3)])
+                                             (abi.DRD_PREC_MIXED, 3), (abi.DRD_PREC_FP64, 3)])
 def test_step_sequence_matches_oracle(cuda_lib, oracle_build, precision, guess):
     """Four mcl6 steps on the resident state against the oracle at tol 1e-12, where the result
     no longer depends on the Krylov guess (guess_mode 1 extrapolates it)."""
