@@ -1239,10 +1239,12 @@ struct GemmCfg { const char* name; };
 static const GemmCfg kGemmCfgs[] = {{"64x64x16/4x4"},         {"32x64x16/2x4"},         {"32x32x16/2x2"},
                                     {"16x32x16/1x2"},         {"sk4 32x64x16/4x4"},     {"sk4 32x32x16/4x4"},
                                     {"sk4 16x64x16/2x4"},     {"sk8 32x32x16/2x2"},     {"sk2 32x64x16/4x4"},
-                                    {"df 64x64x16/4x4"},      {"df 32x64x16/2x4"},      {"df 32x32x16/2x2"}};
+                                    {"df 64x64x16/4x4"},      {"df 32x64x16/2x4"},      {"df 32x32x16/2x2"},
+                                    {"df 16x32x16/1x2"},      {"df 16x16x16/1x1"}};
 
-// Configurations 9-11 are the double-float kernels: FP64 only.
-int gemm_config_count(int fp64) { return fp64 ? 12 : 9; }
+// Configurations 9-13 are the double-float kernels: FP64 only.  The small tiles give the
+// unfolded pressure passes at 420x180 four to eight times the blocks of 32x64 tiles.
+int gemm_config_count(int fp64) { return fp64 ? 14 : 9; }
 const char* gemm_config_name(int cfg) { return kGemmCfgs[cfg].name; }
 
 template <typename T, int BM, int BN, int TM, int TN, int KS, int EPI>
@@ -1301,7 +1303,9 @@ void launch_gemm(int cfg, int epi, const GemmArgs<T>& a, cudaStream_t s) {
             if constexpr (sizeof(T) == 8) {
                 if (cfg == 9) gemm_df_dispatch<64, 64, 4, 4>(epi, a, s);
                 else if (cfg == 10) gemm_df_dispatch<32, 64, 2, 4>(epi, a, s);
-                else gemm_df_dispatch<32, 32, 2, 2>(epi, a, s);
+                else if (cfg == 11) gemm_df_dispatch<32, 32, 2, 2>(epi, a, s);
+                else if (cfg == 12) gemm_df_dispatch<16, 32, 1, 2>(epi, a, s);
+                else gemm_df_dispatch<16, 16, 1, 1>(epi, a, s);
             } else {
                 gemm_dispatch_epi<T, 64, 64, 4, 4>(epi, a, s);
             }

@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 F = abi
 
 
-N_CFG_FP32, N_CFG_FP64 = 9, 12  # configurations 9-11: the FP64-only double-float kernels
+N_CFG_FP32, N_CFG_FP64 = 9, 14  # configurations 9-13: the FP64-only double-float kernels
 
 
 @pytest.mark.parametrize("nr,nz", [(420, 180), (97, 53)])
