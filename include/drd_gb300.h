@@ -433,10 +433,12 @@ int drd_kernel_bench(drd_ctx* ctx, int which, int reps, double* us_per_launch, d
 /* Writes `bytes` of scratch memory on the context stream (evicts L2 between timed steps). */
 int drd_flush_l2(drd_ctx* ctx, int64_t bytes);
 
-/* 1 when the mixed mode runs each FP32 inner CH solve as one persistent cooperative launch
- * (grid-wide barriers between the phases of an iteration), 0 when it runs the captured
- * kernel-per-phase loop (no cooperative launch support, DRD_PERSIST=0 in the environment, or a
- * graph that could not take the cooperative launch: `why` then receives that error). */
+/* 1 when the mixed mode runs each whole CH and momentum solve (the FP64 refinement and its
+ * FP32 iterations) as one persistent cooperative launch with grid-wide barriers between the
+ * phases of an iteration; 0 when it runs the captured kernel-per-phase loop (no cooperative
+ * launch support, DRD_PERSIST=0 in the environment, or a graph that could not take the
+ * cooperative launch).  `why` receives the reason for whatever does not use it, including a
+ * grid past the CH solve's resident shared-memory plan, whose CH solve then uses the loop. */
 int drd_persistent_solver(drd_ctx* ctx, char* why, int len);
 /* With DRD_PERSIST_PROF=1 in the environment at drd_create, the persistent solver records
  * %globaltimer (ns) at entry and exit of each grid barrier of its third iteration, as seen by
