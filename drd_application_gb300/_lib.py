@@ -68,6 +68,16 @@ SIGNATURES = {
     "drd_persistent_solver": (C.c_int, [_ctx, C.c_char_p, C.c_int]),
     "drd_persist_profile": (C.c_int, [_ctx, C.POINTER(C.c_int64), C.c_int]),
     "drd_stream": (C.c_void_p, [_ctx]),
+    "drd_unet_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "drd_unet_destroy": (C.c_int, [C.c_void_p]),
+    "drd_unet_param_count": (C.c_int64, [C.c_void_p]),
+    "drd_unet_last_error": (C.c_char_p, [C.c_void_p]),
+    "drd_unet_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "drd_unet_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "drd_unet_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "drd_unet_gradients": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "drd_unet_train_step": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]),
+    "drd_unet_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
 }
 
 

@@ -1,0 +1,851 @@
+// drd_unet.cu — the learned initial guess of the Krylov solves: a 4-level U-Net (32 base
+// channels, 3x3 convolutions, BF16 weights and activations, FP32 accumulation) with its
+// forward pass, backward pass and Adam update, all as hand-written kernels on the BF16 tensor
+// cores (mma.sync m16n8k16, FP32 accumulators).
+//
+// The network maps (normalised residual, resistance, phase field) on the solver's grid to a
+// normalised correction of the solve's initial guess; the caller scales it back and the
+// solver's FP64 true residual judges the corrected guess against the plain one.
+//
+// Layout on the device:
+//   activations  NHWC BF16, grid padded to Hp x Wp (multiples of 8, zero input outside the
+//                caller's H x W); level l has (Hp >> l) x (Wp >> l) pixels and 32 << l channels.
+//   skip joins   the encoder output of level l is written straight into channels [C_l, 2C_l)
+//                of the decoder's concatenation buffer cat_l; the upsampling convolution
+//                writes channels [0, C_l).  No copy joins them.
+//   parameters   one flat FP32 array (master copy, Adam state alongside); conv weights are
+//                [tap][Cout][Cin], then the bias [Cout].  Two BF16 copies are kept: the same
+//                layout for the forward pass, and [8 - tap][Cin][Cout] (the flipped transpose)
+//                for the data gradient, which then runs through the forward kernel.
+//   caller I/O   FP32 NCHW (batch, channels, H, W) on the caller's H x W grid, host or device.
+//
+// Architecture (conv = 3x3 same-padding + bias + ReLU):
+//   enc l (l = 0..3): conv(C_in_l -> C_l), conv(C_l -> C_l) = e_l;  2x2 average pool between levels
+//   dec l (l = 2..0): conv(up2(d_{l+1}) -> C_l) || e_l  ->  conv(2C_l -> C_l), conv(C_l -> C_l) = d_l
+//   out: 1x1 conv(C_0 -> out_ch), no activation.  d_3 = e_3 (the bottleneck).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/drd_gb300.h"
+
+typedef __nv_bfloat16 bf16;
+
+namespace {
+
+constexpr int kLevels = 4;
+constexpr int kBase = 32;
+constexpr int kCinPad = 16;   // the input's channels, zero-padded to one MMA K step
+constexpr int kMaxOut = 4;
+constexpr int kConvTPB = 128; // 4 warps x 32 pixels per block of the convolution
+constexpr int kWgPix = 2048;  // pixels per block of the weight gradient
+
+// ------------------------------------------------------------------------------------------
+// tensor-core primitive: D(16x8, f32) += A(16x16, bf16, row) * B(16x8, bf16, col)
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t ld_pair(const bf16* p) {
+    return p ? __ldg(reinterpret_cast<const unsigned int*>(p)) : 0u;
+}
+__device__ __forceinline__ uint32_t pack2(const bf16* lo, const bf16* hi) {
+    const unsigned short a = lo ? __ldg(reinterpret_cast<const unsigned short*>(lo)) : 0;
+    const unsigned short b = hi ? __ldg(reinterpret_cast<const unsigned short*>(hi)) : 0;
+    return (uint32_t)a | ((uint32_t)b << 16);
+}
+
+// ------------------------------------------------------------------------------------------
+// 3x3 convolution as an implicit GEMM: M = pixels, N = output channels, K = 9 taps x Cin.
+// A block has 4 warps; a warp computes 32 pixels x 32 output channels (2 x 4 MMA tiles).
+// With `up`, the input is at half resolution and is read through nearest upsampling.  The
+// same kernel computes data gradients (weights = the flipped transpose, no bias/ReLU); `mask`
+// then applies the ReLU derivative of the layer below (zero where mask <= 0).
+struct ConvArgs {
+    const bf16* x; long xbs; int ldx;
+    const bf16* w; const float* bias;
+    bf16* y; float* yf; long ybs; int ldy;
+    const bf16* mask; long mbs; int ldm;
+    int H, W, Cin, Cout, up, relu;
+};
+
+__global__ void __launch_bounds__(kConvTPB) k_conv3(ConvArgs a) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int HW = a.H * a.W, b = blockIdx.z;
+    const int pw = blockIdx.x * kConvTPB + warp * 32;
+    const int co0 = blockIdx.y * 32;
+    const bf16* xb = a.x + (long)b * a.xbs;
+    const int Wl = a.W >> 1;
+    int py[4], px[4];
+    bool pv[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int p = pw + (r >> 1) * 16 + (r & 1) * 8 + g;
+        pv[r] = p < HW;
+        py[r] = pv[r] ? p / a.W : 0;
+        px[r] = pv[r] ? p - py[r] * a.W : 0;
+    }
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
+
+    for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+        const bf16* src[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int sy = py[r] + dy, sx = px[r] + dx;
+            const bool ok = pv[r] && sy >= 0 && sy < a.H && sx >= 0 && sx < a.W;
+            const long sp = a.up ? (long)(sy >> 1) * Wl + (sx >> 1) : (long)sy * a.W + sx;
+            src[r] = ok ? xb + sp * a.ldx + 2 * t : nullptr;
+        }
+        const bf16* wt = a.w + ((long)tap * a.Cout + co0 + g) * a.Cin + 2 * t;
+        for (int c0 = 0; c0 < a.Cin; c0 += 16) {
+            uint32_t af[2][4];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+                const bf16* s0 = src[mt * 2];
+                const bf16* s1 = src[mt * 2 + 1];
+                af[mt][0] = ld_pair(s0 ? s0 + c0 : nullptr);
+                af[mt][1] = ld_pair(s1 ? s1 + c0 : nullptr);
+                af[mt][2] = ld_pair(s0 ? s0 + c0 + 8 : nullptr);
+                af[mt][3] = ld_pair(s1 ? s1 + c0 + 8 : nullptr);
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+                const bf16* wp = wt + (long)nt * 8 * a.Cin + c0;
+                const uint32_t b0 = ld_pair(wp), b1 = ld_pair(wp + 8);
+                mma_bf16(acc[0][nt], af[0], b0, b1);
+                mma_bf16(acc[1][nt], af[1], b0, b1);
+            }
+        }
+    }
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int r = mt * 2 + h;
+            if (!pv[r]) continue;
+            const long p = (long)py[r] * a.W + px[r];
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+                const int co = co0 + nt * 8 + 2 * t;
+                float v0 = acc[mt][nt][2 * h], v1 = acc[mt][nt][2 * h + 1];
+                if (a.bias) { v0 += a.bias[co]; v1 += a.bias[co + 1]; }
+                if (a.relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+                if (a.mask) {
+                    const bf16* m = a.mask + (long)b * a.mbs + p * a.ldm + co;
+                    if (!(__bfloat162float(m[0]) > 0.f)) v0 = 0.f;
+                    if (!(__bfloat162float(m[1]) > 0.f)) v1 = 0.f;
+                }
+                if (a.y) {
+                    *reinterpret_cast<__nv_bfloat162*>(a.y + (long)b * a.ybs + p * a.ldy + co) = __floats2bfloat162_rn(v0, v1);
+                } else {
+                    *reinterpret_cast<float2*>(a.yf + (long)b * a.ybs + p * a.ldy + co) = make_float2(v0, v1);
+                }
+            }
+        }
+}
+
+// ------------------------------------------------------------------------------------------
+// Weight gradient: dW[tap][co][ci] += sum over pixels of G[p][co] * X[p + off(tap)][ci], an MMA
+// with M = output channels, N = input channels, K = pixels (flattened over the batch).  A block
+// takes one tap, a 32 x ci_tile weight tile and kWgPix pixels; its 4 warps split the pixels,
+// then sum through shared memory and add to dW with one atomic per weight.
+struct WgArgs {
+    const bf16* x; long xbs; int ldx;
+    const bf16* g; long gbs; int ldg;
+    float* dw;
+    int H, W, Cin, Cout, up, ci_tile, batch;
+};
+
+__global__ void __launch_bounds__(128) k_wgrad(WgArgs a) {
+    __shared__ float red[4][32][33];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int nco = a.Cout / 32;
+    int tile = blockIdx.y;
+    const int tap = tile % 9;
+    tile /= 9;
+    const int co0 = (tile % nco) * 32, ci0 = (tile / nco) * a.ci_tile;
+    const int nnt = a.ci_tile / 8;
+    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const int HW = a.H * a.W, Wl = a.W >> 1;
+    const long total = (long)a.batch * HW;
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
+
+    for (int ks = warp; ks < kWgPix / 16; ks += 4) {
+        const long q0 = (long)blockIdx.x * kWgPix + ks * 16;
+        if (q0 >= total) break;
+        const bf16* gp[4];
+        const bf16* xp[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const long q = q0 + 2 * t + (j & 1) + (j >> 1) * 8;
+            gp[j] = nullptr;
+            xp[j] = nullptr;
+            if (q < total) {
+                const int b = (int)(q / HW);
+                const int p = (int)(q - (long)b * HW);
+                gp[j] = a.g + (long)b * a.gbs + (long)p * a.ldg + co0 + g;
+                const int y = p / a.W, x = p - y * a.W;
+                const int sy = y + dy, sx = x + dx;
+                if (sy >= 0 && sy < a.H && sx >= 0 && sx < a.W) {
+                    const long sp = a.up ? (long)(sy >> 1) * Wl + (sx >> 1) : (long)sy * a.W + sx;
+                    xp[j] = a.x + (long)b * a.xbs + sp * a.ldx + ci0 + g;
+                }
+            }
+        }
+        uint32_t af[2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            const int o = mt * 16;
+            af[mt][0] = pack2(gp[0] ? gp[0] + o : nullptr, gp[1] ? gp[1] + o : nullptr);
+            af[mt][1] = pack2(gp[0] ? gp[0] + o + 8 : nullptr, gp[1] ? gp[1] + o + 8 : nullptr);
+            af[mt][2] = pack2(gp[2] ? gp[2] + o : nullptr, gp[3] ? gp[3] + o : nullptr);
+            af[mt][3] = pack2(gp[2] ? gp[2] + o + 8 : nullptr, gp[3] ? gp[3] + o + 8 : nullptr);
+        }
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            if (nt >= nnt) break;
+            const int o = nt * 8;
+            const uint32_t b0 = pack2(xp[0] ? xp[0] + o : nullptr, xp[1] ? xp[1] + o : nullptr);
+            const uint32_t b1 = pack2(xp[2] ? xp[2] + o : nullptr, xp[3] ? xp[3] + o : nullptr);
+            mma_bf16(acc[0][nt], af[0], b0, b1);
+            mma_bf16(acc[1][nt], af[1], b0, b1);
+        }
+    }
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                red[warp][mt * 16 + g + (k >> 1) * 8][nt * 8 + 2 * t + (k & 1)] = acc[mt][nt][k];
+    __syncthreads();
+    for (int i = threadIdx.x; i < 32 * a.ci_tile; i += 128) {
+        const int r = i / a.ci_tile, c = i - r * a.ci_tile;
+        const float v = red[0][r][c] + red[1][r][c] + red[2][r][c] + red[3][r][c];
+        atomicAdd(a.dw + ((long)tap * a.Cout + co0 + r) * a.Cin + ci0 + c, v);
+    }
+}
+
+// bias gradient: db[c] += sum over pixels of G[p][c]
+__global__ void k_colsum(const bf16* g, long gbs, int ldg, int HW, int batch, int C, float* db) {
+    const int c = threadIdx.x;
+    if (c >= C) return;
+    const long total = (long)batch * HW;
+    const long q0 = (long)blockIdx.x * 1024;
+    float s = 0.f;
+    for (long q = q0; q < q0 + 1024 && q < total; ++q) {
+        const int b = (int)(q / HW);
+        const long p = q - (long)b * HW;
+        s += __bfloat162float(g[(long)b * gbs + p * ldg + c]);
+    }
+    atomicAdd(db + c, s);
+}
+
+// 2x2 average pool: y (H/2 x W/2) from x (H x W)
+__global__ void k_pool(const bf16* x, long xbs, int ldx, bf16* y, long ybs, int ldy, int H, int W, int C, int batch) {
+    const int Hl = H >> 1, Wl = W >> 1;
+    const long n = (long)batch * Hl * Wl * C;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        long q = i / C;
+        const int xl = (int)(q % Wl);
+        q /= Wl;
+        const int yl = (int)(q % Hl);
+        const int b = (int)(q / Hl);
+        const bf16* s = x + (long)b * xbs + ((long)(2 * yl) * W + 2 * xl) * ldx + c;
+        const float v = __bfloat162float(s[0]) + __bfloat162float(s[ldx]) + __bfloat162float(s[(long)W * ldx]) +
+                        __bfloat162float(s[(long)W * ldx + ldx]);
+        y[(long)b * ybs + ((long)yl * Wl + xl) * ldy + c] = __float2bfloat16_rn(0.25f * v);
+    }
+}
+
+// gradient through nearest upsampling: dl[q] = sum of the 4 children dh[p]
+__global__ void k_up_bwd(const float* dh, long hbs, int ldh, float* dl, long lbs, int ldl, int H, int W, int C, int batch) {
+    const int Hl = H >> 1, Wl = W >> 1;
+    const long n = (long)batch * Hl * Wl * C;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        long q = i / C;
+        const int xl = (int)(q % Wl);
+        q /= Wl;
+        const int yl = (int)(q % Hl);
+        const int b = (int)(q / Hl);
+        const float* s = dh + (long)b * hbs + ((long)(2 * yl) * W + 2 * xl) * ldh + c;
+        dl[(long)b * lbs + ((long)yl * Wl + xl) * ldl + c] = s[0] + s[ldh] + s[(long)W * ldh] + s[(long)W * ldh + ldh];
+    }
+}
+
+// pre-activation gradient of a ReLU layer: G = (mask > 0) * (a + 0.25 * b[parent]) in BF16,
+// with b (optional) the gradient of the 2x2 average pool that also reads this layer.
+__global__ void k_mask_grad(const float* a, long abs_, int lda, const float* bsrc, long bbs, int ldb, const bf16* mask,
+                            long mbs, int ldm, bf16* G, long gbs, int ldg, int H, int W, int C, int batch) {
+    const long n = (long)batch * H * W * C;
+    const int Wl = W >> 1;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        long q = i / C;
+        const int x = (int)(q % W);
+        q /= W;
+        const int y = (int)(q % H);
+        const int b = (int)(q / H);
+        const long p = (long)y * W + x;
+        float v = 0.f;
+        if (__bfloat162float(mask[(long)b * mbs + p * ldm + c]) > 0.f) {
+            v = a[(long)b * abs_ + p * lda + c];
+            if (bsrc) v += 0.25f * bsrc[(long)b * bbs + ((long)(y >> 1) * Wl + (x >> 1)) * ldb + c];
+        }
+        G[(long)b * gbs + p * ldg + c] = __float2bfloat16_rn(v);
+    }
+}
+
+// caller's FP32 NCHW input on H0 x W0 -> NHWC BF16 on Hp x Wp with kCinPad channels
+__global__ void k_pack_in(const float* x, int cin, int H0, int W0, bf16* xin, int Hp, int Wp, int batch) {
+    const long n = (long)batch * Hp * Wp;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int w = (int)(i % Wp);
+        const int h = (int)((i / Wp) % Hp);
+        const int b = (int)(i / ((long)Wp * Hp));
+        alignas(16) bf16 v[kCinPad];
+#pragma unroll
+        for (int c = 0; c < kCinPad; ++c) {
+            float f = 0.f;
+            if (c < cin && h < H0 && w < W0) f = x[(((long)b * cin + c) * H0 + h) * W0 + w];
+            v[c] = __float2bfloat16_rn(f);
+        }
+        uint4* dst = reinterpret_cast<uint4*>(xin + i * kCinPad);
+        dst[0] = *reinterpret_cast<uint4*>(&v[0]);
+        dst[1] = *reinterpret_cast<uint4*>(&v[8]);
+    }
+}
+
+// 1x1 output convolution on the caller's grid: y[b][o][h][w] = bo[o] + sum_c d0[p][c] Wo[o][c]
+__global__ void k_out_fwd(const bf16* d0, const float* wo, const float* bo, int cout, float* y, int H0, int W0, int Hp,
+                          int Wp, int batch) {
+    const long n = (long)batch * H0 * W0;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int w = (int)(i % W0);
+        const int h = (int)((i / W0) % H0);
+        const int b = (int)(i / ((long)W0 * H0));
+        const bf16* s = d0 + ((long)b * Hp * Wp + (long)h * Wp + w) * kBase;
+        float acc[kMaxOut];
+        for (int o = 0; o < cout; ++o) acc[o] = bo[o];
+        for (int c = 0; c < kBase; ++c) {
+            const float v = __bfloat162float(s[c]);
+            for (int o = 0; o < cout; ++o) acc[o] += v * wo[o * kBase + c];
+        }
+        for (int o = 0; o < cout; ++o) y[(((long)b * cout + o) * H0 + h) * W0 + w] = acc[o];
+    }
+}
+
+// mean squared error over the caller's grid; dy = d(loss)/dy
+__global__ void k_loss(const float* y, const float* tg, float* dy, long n, float inv_n, float* loss) {
+    __shared__ float sm[32];
+    float s = 0.f;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const float d = y[i] - tg[i];
+        dy[i] = 2.f * d * inv_n;
+        s += d * d;
+    }
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (blockDim.x >> 5) ? sm[threadIdx.x] : 0.f;
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) atomicAdd(loss, s * inv_n);
+    }
+}
+
+// output layer backward, data part: G0[p][c] = (d0 > 0) * sum_o dy[o][p] Wo[o][c] (dy = 0 off the caller's grid)
+__global__ void k_out_bwd_x(const float* dy, const float* wo, int cout, const bf16* d0, bf16* G, int H0, int W0, int Hp,
+                            int Wp, int batch) {
+    const long n = (long)batch * Hp * Wp;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int w = (int)(i % Wp);
+        const int h = (int)((i / Wp) % Hp);
+        const int b = (int)(i / ((long)Wp * Hp));
+        float dv[kMaxOut];
+        const bool in = h < H0 && w < W0;
+        for (int o = 0; o < cout; ++o) dv[o] = in ? dy[(((long)b * cout + o) * H0 + h) * W0 + w] : 0.f;
+        const bf16* m = d0 + i * kBase;
+        bf16* gp = G + i * kBase;
+        for (int c = 0; c < kBase; ++c) {
+            float v = 0.f;
+            if (__bfloat162float(m[c]) > 0.f)
+                for (int o = 0; o < cout; ++o) v += dv[o] * wo[o * kBase + c];
+            gp[c] = __float2bfloat16_rn(v);
+        }
+    }
+}
+
+// output layer backward, weight part: dWo[o][c] += sum_p dy[o][p] d0[p][c]; dbo[o] += sum_p dy[o][p]
+__global__ void k_out_bwd_w(const float* dy, int cout, const bf16* d0, float* dwo, float* dbo, int H0, int W0, int Hp,
+                            int Wp, int batch) {
+    const int o = threadIdx.x / kBase, c = threadIdx.x % kBase;
+    if (o >= cout) return;
+    const long n = (long)batch * H0 * W0;
+    const long i0 = (long)blockIdx.x * 1024;
+    float s = 0.f, sb = 0.f;
+    for (long i = i0; i < i0 + 1024 && i < n; ++i) {
+        const int w = (int)(i % W0);
+        const int h = (int)((i / W0) % H0);
+        const int b = (int)(i / ((long)W0 * H0));
+        const float d = dy[(((long)b * cout + o) * H0 + h) * W0 + w];
+        s += d * __bfloat162float(d0[((long)b * Hp * Wp + (long)h * Wp + w) * kBase + c]);
+        sb += d;
+    }
+    atomicAdd(dwo + o * kBase + c, s);
+    if (c == 0) atomicAdd(dbo + o, sb);
+}
+
+// Adam step on the FP32 master weights, then the two BF16 copies
+__global__ void k_adam(float* w, const float* gr, float* m, float* v, long n, float lr, float b1, float b2, float eps,
+                       float bc1, float bc2, bf16* wb, bf16* wt, const int* tmap, int update) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        float x = w[i];
+        if (update) {
+            const float gi = gr[i];
+            const float mi = b1 * m[i] + (1.f - b1) * gi;
+            const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+            m[i] = mi;
+            v[i] = vi;
+            x -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+            w[i] = x;
+        }
+        const bf16 xb = __float2bfloat16_rn(x);
+        wb[i] = xb;
+        const int j = tmap[i];
+        if (j >= 0) wt[j] = xb;
+    }
+}
+
+inline int grid_for(long n, int tpb = 256) {
+    long b = (n + tpb - 1) / tpb;
+    if (b > 152 * 32) b = 152 * 32;
+    return (int)(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+struct drd_unet {
+    struct Layer {
+        int cin, cout, level, up;
+        long w_off, b_off;
+    };
+    int H0, W0, Hp, Wp, cin, cout, maxb;
+    cudaStream_t s = nullptr;
+    std::vector<Layer> L;
+    long nparam = 0, wo_off = 0, bo_off = 0, adam_t = 0;
+    float *W32 = nullptr, *G32 = nullptr, *M = nullptr, *V = nullptr;
+    bf16 *Wb = nullptr, *Wt = nullptr;
+    int* tmap = nullptr;
+    // activations (see the header comment)
+    bf16 *xin = nullptr, *ea[kLevels] = {}, *cat[kLevels - 1] = {}, *pool[kLevels] = {}, *b3 = nullptr;
+    bf16 *db[kLevels - 1] = {}, *dd[kLevels - 1] = {};
+    // gradients
+    bf16* Gl[17] = {};
+    float *dcat[kLevels - 1] = {}, *dU = nullptr, *dlow = nullptr, *dpool = nullptr;
+    float *y = nullptr, *dy = nullptr, *tg = nullptr, *xstage = nullptr, *ystage = nullptr, *loss = nullptr;
+    std::vector<void*> allocs;
+    std::string err;
+
+    int HWl(int l) const { return (Hp >> l) * (Wp >> l); }
+    int Hl(int l) const { return Hp >> l; }
+    int Wl(int l) const { return Wp >> l; }
+    static int C(int l) { return kBase << l; }
+};
+
+namespace {
+
+template <class T>
+int dalloc(drd_unet* n, T** p, size_t count) {
+    if (cudaMalloc((void**)p, sizeof(T) * (count ? count : 1)) != cudaSuccess) return DRD_ERR_CUDA;
+    n->allocs.push_back((void*)*p);
+    return cudaMemsetAsync(*p, 0, sizeof(T) * (count ? count : 1), n->s) == cudaSuccess ? DRD_OK : DRD_ERR_CUDA;
+}
+
+void conv(drd_unet* n, int li, const bf16* x, int ldx, long xbs, bf16* y, int ldy, long ybs, int batch) {
+    const auto& Ly = n->L[li];
+    ConvArgs a{};
+    a.x = x; a.xbs = xbs; a.ldx = ldx;
+    a.w = n->Wb + Ly.w_off; a.bias = n->W32 + Ly.b_off;
+    a.y = y; a.yf = nullptr; a.ybs = ybs; a.ldy = ldy;
+    a.mask = nullptr; a.mbs = 0; a.ldm = 0;
+    a.H = n->Hl(Ly.level); a.W = n->Wl(Ly.level); a.Cin = Ly.cin; a.Cout = Ly.cout; a.up = Ly.up; a.relu = 1;
+    dim3 grid((a.H * a.W + kConvTPB - 1) / kConvTPB, a.Cout / 32, batch);
+    k_conv3<<<grid, kConvTPB, 0, n->s>>>(a);
+}
+
+// data gradient of layer li: out (bf16 with mask, or fp32) = conv(G, flipped transpose)
+void dgrad(drd_unet* n, int li, const bf16* G, int batch, bf16* out_b, float* out_f, int ldo, long obs,
+           const bf16* mask, int ldm, long mbs) {
+    const auto& Ly = n->L[li];
+    const int H = n->Hl(Ly.level), W = n->Wl(Ly.level);
+    ConvArgs a{};
+    a.x = G; a.xbs = (long)H * W * Ly.cout; a.ldx = Ly.cout;
+    a.w = n->Wt + Ly.w_off; a.bias = nullptr;
+    a.y = out_b; a.yf = out_f; a.ybs = obs; a.ldy = ldo;
+    a.mask = mask; a.mbs = mbs; a.ldm = ldm;
+    a.H = H; a.W = W; a.Cin = Ly.cout; a.Cout = Ly.cin; a.up = 0; a.relu = 0;
+    dim3 grid((H * W + kConvTPB - 1) / kConvTPB, a.Cout / 32, batch);
+    k_conv3<<<grid, kConvTPB, 0, n->s>>>(a);
+}
+
+void wgrad(drd_unet* n, int li, const bf16* x, int ldx, long xbs, const bf16* G, int batch) {
+    const auto& Ly = n->L[li];
+    const int H = n->Hl(Ly.level), W = n->Wl(Ly.level);
+    WgArgs a{};
+    a.x = x; a.xbs = xbs; a.ldx = ldx;
+    a.g = G; a.gbs = (long)H * W * Ly.cout; a.ldg = Ly.cout;
+    a.dw = n->G32 + Ly.w_off;
+    a.H = H; a.W = W; a.Cin = Ly.cin; a.Cout = Ly.cout; a.up = Ly.up; a.batch = batch;
+    a.ci_tile = Ly.cin < 32 ? Ly.cin : 32;
+    const long total = (long)batch * H * W;
+    dim3 grid((unsigned)((total + kWgPix - 1) / kWgPix), 9 * (Ly.cout / 32) * (Ly.cin / a.ci_tile));
+    k_wgrad<<<grid, 128, 0, n->s>>>(a);
+    k_colsum<<<(unsigned)((total + 1023) / 1024), Ly.cout, 0, n->s>>>(G, a.gbs, Ly.cout, H * W, batch, Ly.cout,
+                                                                     n->G32 + Ly.b_off);
+}
+
+void mask_grad(drd_unet* n, int l, const float* a, int lda, const float* b, int ldb, const bf16* mask, int ldm, bf16* G,
+               int C, int batch) {
+    const long hw = n->HWl(l);
+    const long hwl = l + 1 < kLevels ? n->HWl(l + 1) : 0;
+    k_mask_grad<<<grid_for((long)batch * hw * C), 256, 0, n->s>>>(a, hw * lda, lda, b, hwl * ldb, ldb, mask, hw * ldm, ldm,
+                                                                  G, hw * C, C, n->Hl(l), n->Wl(l), C, batch);
+}
+
+void up_bwd(drd_unet* n, int l, const float* dh, int C, float* dl, int batch) {
+    // dh at level l (C channels), dl at level l+1
+    k_up_bwd<<<grid_for((long)batch * n->HWl(l + 1) * C), 256, 0, n->s>>>(dh, (long)n->HWl(l) * C, C, dl,
+                                                                          (long)n->HWl(l + 1) * C, C, n->Hl(l),
+                                                                          n->Wl(l), C, batch);
+}
+
+void forward(drd_unet* n, const float* x, int batch) {
+    const long n0 = (long)batch * n->Hp * n->Wp;
+    k_pack_in<<<grid_for(n0), 256, 0, n->s>>>(x, n->cin, n->H0, n->W0, n->xin, n->Hp, n->Wp, batch);
+    // encoder
+    for (int l = 0; l < kLevels; ++l) {
+        const int C = drd_unet::C(l);
+        const long hw = n->HWl(l);
+        const bf16* in = l == 0 ? n->xin : n->pool[l];
+        const int ldin = l == 0 ? kCinPad : drd_unet::C(l - 1);
+        conv(n, 2 * l, in, ldin, hw * ldin, n->ea[l], C, hw * C, batch);
+        if (l < kLevels - 1) {
+            conv(n, 2 * l + 1, n->ea[l], C, hw * C, n->cat[l] + C, 2 * C, hw * 2 * C, batch);
+            const long hwl = n->HWl(l + 1);
+            k_pool<<<grid_for((long)batch * hwl * C), 256, 0, n->s>>>(n->cat[l] + C, hw * 2 * C, 2 * C, n->pool[l + 1],
+                                                                      hwl * C, C, n->Hl(l), n->Wl(l), C, batch);
+        } else {
+            conv(n, 2 * l + 1, n->ea[l], C, hw * C, n->b3, C, hw * C, batch);
+        }
+    }
+    // decoder
+    for (int l = kLevels - 2; l >= 0; --l) {
+        const int C = drd_unet::C(l);
+        const long hw = n->HWl(l), hwl = n->HWl(l + 1);
+        const bf16* below = l == kLevels - 2 ? n->b3 : n->dd[l + 1];
+        const int li = 8 + 3 * (kLevels - 2 - l);
+        conv(n, li, below, 2 * C, hwl * 2 * C, n->cat[l], 2 * C, hw * 2 * C, batch);
+        conv(n, li + 1, n->cat[l], 2 * C, hw * 2 * C, n->db[l], C, hw * C, batch);
+        conv(n, li + 2, n->db[l], C, hw * C, n->dd[l], C, hw * C, batch);
+    }
+    k_out_fwd<<<grid_for((long)batch * n->H0 * n->W0), 256, 0, n->s>>>(n->dd[0], n->W32 + n->wo_off, n->W32 + n->bo_off,
+                                                                       n->cout, n->y, n->H0, n->W0, n->Hp, n->Wp, batch);
+}
+
+void backward(drd_unet* n, int batch) {
+    const long hw0 = n->HWl(0);
+    k_out_bwd_w<<<(unsigned)(((long)batch * n->H0 * n->W0 + 1023) / 1024), kMaxOut * kBase, 0, n->s>>>(
+        n->dy, n->cout, n->dd[0], n->G32 + n->wo_off, n->G32 + n->bo_off, n->H0, n->W0, n->Hp, n->Wp, batch);
+    k_out_bwd_x<<<grid_for((long)batch * hw0), 256, 0, n->s>>>(n->dy, n->W32 + n->wo_off, n->cout, n->dd[0], n->Gl[16],
+                                                                n->H0, n->W0, n->Hp, n->Wp, batch);
+    // decoder, top level first
+    for (int l = 0; l <= kLevels - 2; ++l) {
+        const int C = drd_unet::C(l);
+        const long hw = n->HWl(l);
+        const int li = 8 + 3 * (kLevels - 2 - l);  // the level's upsampling conv; li+1, li+2 follow
+        // conv li+2: db[l] -> dd[l]
+        wgrad(n, li + 2, n->db[l], C, hw * C, n->Gl[li + 2], batch);
+        dgrad(n, li + 2, n->Gl[li + 2], batch, n->Gl[li + 1], nullptr, C, hw * C, n->db[l], C, hw * C);
+        // conv li+1: cat[l] -> db[l]; gradient of the concatenation in FP32
+        wgrad(n, li + 1, n->cat[l], 2 * C, hw * 2 * C, n->Gl[li + 1], batch);
+        dgrad(n, li + 1, n->Gl[li + 1], batch, nullptr, n->dcat[l], 2 * C, hw * 2 * C, nullptr, 0, 0);
+        // conv li (upsampling): input up2(d_{l+1}), output channels [0, C) of cat[l]
+        mask_grad(n, l, n->dcat[l], 2 * C, nullptr, 0, n->cat[l], 2 * C, n->Gl[li], C, batch);
+        const bf16* below = l == kLevels - 2 ? n->b3 : n->dd[l + 1];
+        wgrad(n, li, below, 2 * C, n->HWl(l + 1) * 2 * C, n->Gl[li], batch);
+        dgrad(n, li, n->Gl[li], batch, nullptr, n->dU, 2 * C, hw * 2 * C, nullptr, 0, 0);
+        up_bwd(n, l, n->dU, 2 * C, n->dlow, batch);
+        // pre-activation gradient of the layer producing d_{l+1} (or the bottleneck)
+        const int lo = l + 1;
+        const int prod = lo == kLevels - 1 ? 7 : 8 + 3 * (kLevels - 2 - lo) + 2;
+        mask_grad(n, lo, n->dlow, 2 * C, nullptr, 0, below, 2 * C, n->Gl[prod], 2 * C, batch);
+    }
+    // encoder, bottom level first (the bottleneck's G7 is set above)
+    for (int l = kLevels - 1; l >= 0; --l) {
+        const int C = drd_unet::C(l);
+        const long hw = n->HWl(l);
+        // conv 2l+1: ea[l] -> e_l
+        const bf16* ein = n->ea[l];
+        wgrad(n, 2 * l + 1, ein, C, hw * C, n->Gl[2 * l + 1], batch);
+        dgrad(n, 2 * l + 1, n->Gl[2 * l + 1], batch, n->Gl[2 * l], nullptr, C, hw * C, n->ea[l], C, hw * C);
+        // conv 2l: input pool[l] (or the packed input)
+        const bf16* in = l == 0 ? n->xin : n->pool[l];
+        const int ldin = l == 0 ? kCinPad : drd_unet::C(l - 1);
+        wgrad(n, 2 * l, in, ldin, hw * ldin, n->Gl[2 * l], batch);
+        if (l == 0) break;
+        const int Cp = drd_unet::C(l - 1);
+        dgrad(n, 2 * l, n->Gl[2 * l], batch, nullptr, n->dpool, Cp, hw * Cp, nullptr, 0, 0);
+        // e_{l-1}: the decoder's concatenation half plus the pool's share
+        mask_grad(n, l - 1, n->dcat[l - 1] + Cp, 2 * Cp, n->dpool, Cp, n->cat[l - 1] + Cp, 2 * Cp,
+                  n->Gl[2 * (l - 1) + 1], Cp, batch);
+    }
+}
+
+int set_err(drd_unet* n, const char* m) {
+    n->err = m;
+    return DRD_ERR_BADARG;
+}
+
+bool is_device_ptr(const void* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// the caller's FP32 NCHW array (host or device) as a device pointer
+const float* stage_in(drd_unet* n, const float* p, long count, float* stage) {
+    if (is_device_ptr(p)) return p;
+    cudaMemcpyAsync(stage, p, sizeof(float) * count, cudaMemcpyHostToDevice, n->s);
+    return stage;
+}
+
+int finish(drd_unet* n) {
+    cudaError_t e = cudaStreamSynchronize(n->s);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        n->err = cudaGetErrorString(e);
+        return DRD_ERR_CUDA;
+    }
+    return DRD_OK;
+}
+
+int refresh_bf16(drd_unet* n, int update, float lr) {
+    float bc1 = 1.f, bc2 = 1.f;
+    if (update) {
+        ++n->adam_t;
+        bc1 = 1.f - std::pow(0.9f, (float)n->adam_t);
+        bc2 = 1.f - std::pow(0.999f, (float)n->adam_t);
+    }
+    k_adam<<<grid_for(n->nparam), 256, 0, n->s>>>(n->W32, n->G32, n->M, n->V, n->nparam, lr, 0.9f, 0.999f, 1e-8f, bc1,
+                                                  bc2, n->Wb, n->Wt, n->tmap, update);
+    return DRD_OK;
+}
+
+int loss_and_grads(drd_unet* n, int batch, const float* x, const float* target) {
+    const long nin = (long)batch * n->cin * n->H0 * n->W0, nout = (long)batch * n->cout * n->H0 * n->W0;
+    const float* xd = stage_in(n, x, nin, n->xstage);
+    const float* td = stage_in(n, target, nout, n->ystage);
+    forward(n, xd, batch);
+    cudaMemsetAsync(n->loss, 0, sizeof(float), n->s);
+    k_loss<<<grid_for(nout), 256, 0, n->s>>>(n->y, td, n->dy, nout, 1.f / (float)nout, n->loss);
+    cudaMemsetAsync(n->G32, 0, sizeof(float) * n->nparam, n->s);
+    backward(n, batch);
+    return DRD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int drd_unet_create(int H, int W, int in_ch, int out_ch, int max_batch, uint64_t seed, drd_unet** out) {
+    if (!out || H < 8 || W < 8 || in_ch < 1 || in_ch > kCinPad || out_ch < 1 || out_ch > kMaxOut || max_batch < 1)
+        return DRD_ERR_BADARG;
+    *out = nullptr;
+    auto* n = new drd_unet();
+    n->H0 = H; n->W0 = W; n->cin = in_ch; n->cout = out_ch; n->maxb = max_batch;
+    n->Hp = (H + 7) / 8 * 8;
+    n->Wp = (W + 7) / 8 * 8;
+    if (cudaStreamCreateWithFlags(&n->s, cudaStreamNonBlocking) != cudaSuccess) {
+        delete n;
+        return DRD_ERR_CUDA;
+    }
+    // layer table: encoder (2 per level), then 3 per decoder level from the bottom
+    long off = 0;
+    auto add = [&](int ci, int co, int lev, int up) {
+        drd_unet::Layer Ly{ci, co, lev, up, off, 0};
+        off += 9L * ci * co;
+        Ly.b_off = off;
+        off += co;
+        n->L.push_back(Ly);
+    };
+    for (int l = 0; l < kLevels; ++l) {
+        add(l == 0 ? kCinPad : drd_unet::C(l - 1), drd_unet::C(l), l, 0);
+        add(drd_unet::C(l), drd_unet::C(l), l, 0);
+    }
+    for (int l = kLevels - 2; l >= 0; --l) {
+        add(drd_unet::C(l + 1), drd_unet::C(l), l, 1);
+        add(2 * drd_unet::C(l), drd_unet::C(l), l, 0);
+        add(drd_unet::C(l), drd_unet::C(l), l, 0);
+    }
+    n->wo_off = off;
+    off += (long)out_ch * kBase;
+    n->bo_off = off;
+    off += out_ch;
+    n->nparam = off;
+
+    // initial weights: He-normal (std sqrt(2 / fan_in)) from mt19937_64(seed); zero biases and
+    // zero weights on the padded input channels; the output layer at a tenth of the He scale
+    std::vector<float> w(n->nparam, 0.f);
+    std::vector<int> tm(n->nparam, -1);
+    std::mt19937_64 rng(seed);
+    std::normal_distribution<double> nd(0.0, 1.0);
+    for (const auto& Ly : n->L) {
+        const int real_cin = Ly.w_off == 0 ? in_ch : Ly.cin;
+        const double sd = std::sqrt(2.0 / (9.0 * real_cin));
+        for (int tap = 0; tap < 9; ++tap)
+            for (int co = 0; co < Ly.cout; ++co)
+                for (int ci = 0; ci < Ly.cin; ++ci) {
+                    const long i = Ly.w_off + ((long)tap * Ly.cout + co) * Ly.cin + ci;
+                    const double r = nd(rng);
+                    w[i] = ci < real_cin ? (float)(sd * r) : 0.f;
+                    tm[i] = (int)(Ly.w_off + ((long)(8 - tap) * Ly.cin + ci) * Ly.cout + co);
+                }
+    }
+    for (long i = 0; i < (long)out_ch * kBase; ++i) w[n->wo_off + i] = (float)(0.1 * std::sqrt(2.0 / kBase) * nd(rng));
+
+    int rc = dalloc(n, &n->W32, n->nparam) | dalloc(n, &n->G32, n->nparam) | dalloc(n, &n->M, n->nparam) |
+             dalloc(n, &n->V, n->nparam) | dalloc(n, &n->Wb, n->nparam) | dalloc(n, &n->Wt, n->nparam) |
+             dalloc(n, &n->tmap, n->nparam);
+    const int B = max_batch;
+    rc |= dalloc(n, &n->xin, (size_t)B * n->HWl(0) * kCinPad);
+    for (int l = 0; l < kLevels; ++l) {
+        const size_t hw = (size_t)B * n->HWl(l), C = drd_unet::C(l);
+        rc |= dalloc(n, &n->ea[l], hw * C);
+        if (l > 0) rc |= dalloc(n, &n->pool[l], hw * drd_unet::C(l - 1));
+        if (l < kLevels - 1) {
+            rc |= dalloc(n, &n->cat[l], hw * 2 * C) | dalloc(n, &n->db[l], hw * C) | dalloc(n, &n->dd[l], hw * C) |
+                  dalloc(n, &n->dcat[l], hw * 2 * C);
+        } else {
+            rc |= dalloc(n, &n->b3, hw * C);
+        }
+    }
+    for (int li = 0; li < 17; ++li) rc |= dalloc(n, &n->Gl[li], (size_t)B * n->HWl(n->L[li].level) * n->L[li].cout);
+    // the largest temporaries: up-conv input gradient (2C_l at level l) and its low-res sum;
+    // the pool gradient (C_{l-1} at level l)
+    size_t du = 0, dl = 0, dp = 0;
+    for (int l = 0; l < kLevels - 1; ++l) {
+        du = std::max(du, (size_t)n->HWl(l) * 2 * drd_unet::C(l));
+        dl = std::max(dl, (size_t)n->HWl(l + 1) * 2 * drd_unet::C(l));
+        dp = std::max(dp, (size_t)n->HWl(l + 1) * drd_unet::C(l));
+    }
+    rc |= dalloc(n, &n->dU, du * B) | dalloc(n, &n->dlow, dl * B) | dalloc(n, &n->dpool, dp * B);
+    const size_t nio = (size_t)B * n->H0 * n->W0;
+    rc |= dalloc(n, &n->y, nio * out_ch) | dalloc(n, &n->dy, nio * out_ch) | dalloc(n, &n->xstage, nio * in_ch) |
+          dalloc(n, &n->ystage, nio * out_ch) | dalloc(n, &n->loss, 1);
+    if (rc) {
+        drd_unet_destroy(n);
+        return DRD_ERR_CUDA;
+    }
+    cudaMemcpyAsync(n->W32, w.data(), sizeof(float) * n->nparam, cudaMemcpyHostToDevice, n->s);
+    cudaMemcpyAsync(n->tmap, tm.data(), sizeof(int) * n->nparam, cudaMemcpyHostToDevice, n->s);
+    refresh_bf16(n, 0, 0.f);
+    rc = finish(n);
+    if (rc) {
+        drd_unet_destroy(n);
+        return rc;
+    }
+    *out = n;
+    return DRD_OK;
+}
+
+int drd_unet_destroy(drd_unet* n) {
+    if (!n) return DRD_OK;
+    if (n->s) cudaStreamSynchronize(n->s);
+    for (void* p : n->allocs) cudaFree(p);
+    if (n->s) cudaStreamDestroy(n->s);
+    delete n;
+    return DRD_OK;
+}
+
+int64_t drd_unet_param_count(drd_unet* n) { return n ? n->nparam : -1; }
+
+const char* drd_unet_last_error(drd_unet* n) { return n ? n->err.c_str() : "null network"; }
+
+int drd_unet_get_params(drd_unet* n, float* host) {
+    if (!n || !host) return DRD_ERR_BADARG;
+    cudaMemcpyAsync(host, n->W32, sizeof(float) * n->nparam, cudaMemcpyDeviceToHost, n->s);
+    return finish(n);
+}
+
+int drd_unet_set_params(drd_unet* n, const float* host) {
+    if (!n || !host) return DRD_ERR_BADARG;
+    cudaMemcpyAsync(n->W32, host, sizeof(float) * n->nparam, cudaMemcpyHostToDevice, n->s);
+    refresh_bf16(n, 0, 0.f);
+    n->adam_t = 0;
+    cudaMemsetAsync(n->M, 0, sizeof(float) * n->nparam, n->s);
+    cudaMemsetAsync(n->V, 0, sizeof(float) * n->nparam, n->s);
+    return finish(n);
+}
+
+int drd_unet_forward(drd_unet* n, int batch, const float* x, float* y) {
+    if (!n || !x || !y || batch < 1 || batch > n->maxb) return n ? set_err(n, "bad forward arguments") : DRD_ERR_BADARG;
+    const long nin = (long)batch * n->cin * n->H0 * n->W0, nout = (long)batch * n->cout * n->H0 * n->W0;
+    forward(n, stage_in(n, x, nin, n->xstage), batch);
+    cudaMemcpyAsync(y, n->y, sizeof(float) * nout, cudaMemcpyDefault, n->s);
+    return finish(n);
+}
+
+int drd_unet_gradients(drd_unet* n, int batch, const float* x, const float* target, float* loss, float* grads) {
+    if (!n || !x || !target || batch < 1 || batch > n->maxb) return n ? set_err(n, "bad gradient arguments") : DRD_ERR_BADARG;
+    loss_and_grads(n, batch, x, target);
+    if (loss) cudaMemcpyAsync(loss, n->loss, sizeof(float), cudaMemcpyDefault, n->s);
+    if (grads) cudaMemcpyAsync(grads, n->G32, sizeof(float) * n->nparam, cudaMemcpyDefault, n->s);
+    return finish(n);
+}
+
+int drd_unet_train_step(drd_unet* n, int batch, const float* x, const float* target, float lr, float* loss) {
+    if (!n || !x || !target || batch < 1 || batch > n->maxb || !(lr >= 0.f))
+        return n ? set_err(n, "bad train-step arguments") : DRD_ERR_BADARG;
+    loss_and_grads(n, batch, x, target);
+    refresh_bf16(n, 1, lr);
+    if (loss) cudaMemcpyAsync(loss, n->loss, sizeof(float), cudaMemcpyDefault, n->s);
+    return finish(n);
+}
+
+int drd_unet_stream(drd_unet* n, void** stream) {
+    if (!n || !stream) return DRD_ERR_BADARG;
+    *stream = (void*)n->s;
+    return DRD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,243 @@
+"""The learned initial guess of the CH solve: the U-Net of csrc/drd_unet.cu over the C-ABI,
+the training pairs the solver itself emits, the training loop and the guess.
+
+System.  PhSolve solves A mu = rhs (microfluidics_complex_domain/PhSolve.f90:62-74) starting
+from the previous step's mu^n, the plain guess.  Over a run, the error of that guess is
+e_n = mu^{n+1} - mu^n and its residual r_n = A e_n (A is the library's FP64 operator
+DRD_OP_CH_MATVEC; the coefficients do not change within a run without particles).
+
+Pairs.  With s_n = RMS(r_n), the network input is (r_n / s_n, bdr_ph, ph^n) on the nz x nr
+interior (packed CH order: H = nz rows of W = nr) and the target is e_n / s_n.
+
+Guess.  x0 = mu^n + s * net(r / s, bdr_ph, ph^n), r = b - A mu^n.  The plain guess stays the
+fallback: when the learned guess's FP64 residual is not below the plain one's, the plain
+guess is returned.  The solve that follows is unchanged, so the result meets the same FP64
+tolerance either way; what the network changes is the iteration count.
+"""
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import abi, _lib
+from .api import DRDContext
+from .layout import ptr
+
+F = abi
+
+
+class UNetError(RuntimeError):
+    pass
+
+
+def _p(a):
+    """Pointer of a contiguous float32 numpy array or of a CUDA torch tensor."""
+    if isinstance(a, np.ndarray):
+        if a.dtype != np.float32 or not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("expected a C-contiguous float32 array")
+        return C.c_void_p(a.ctypes.data)
+    if hasattr(a, "data_ptr"):
+        if not a.is_contiguous() or str(a.dtype) != "torch.float32":
+            raise ValueError("expected a contiguous float32 tensor")
+        return C.c_void_p(a.data_ptr())
+    raise TypeError(type(a))
+
+
+class UNet:
+    """drd_unet_*: the network on an H x W grid, in_ch -> out_ch fields, batches <= max_batch."""
+
+    def __init__(self, H, W, in_ch=3, out_ch=1, max_batch=8, seed=0, lib=None):
+        self.L = lib or _lib.load()
+        h = C.c_void_p()
+        rc = self.L.drd_unet_create(int(H), int(W), int(in_ch), int(out_ch), int(max_batch), int(seed), C.byref(h))
+        if rc != 0:
+            raise UNetError(f"drd_unet_create failed with {rc}")
+        self.h, self.H, self.W, self.in_ch, self.out_ch, self.max_batch = h, H, W, in_ch, out_ch, max_batch
+        self.nparam = int(self.L.drd_unet_param_count(h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.drd_unet_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _rc(self, rc, what):
+        if rc != 0:
+            msg = self.L.drd_unet_last_error(self.h)
+            raise UNetError(f"{what} failed with {rc}: {msg.decode() if msg else ''}")
+
+    def get_params(self):
+        p = np.zeros(self.nparam, dtype=np.float32)
+        self._rc(self.L.drd_unet_get_params(self.h, _p(p)), "drd_unet_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        if p.shape != (self.nparam,):
+            raise ValueError(f"expected {self.nparam} parameters")
+        self._rc(self.L.drd_unet_set_params(self.h, _p(p)), "drd_unet_set_params")
+
+    def _batch(self, x, ch):
+        b = x.shape[0]
+        if tuple(x.shape[1:]) != (ch, self.H, self.W) or not 1 <= b <= self.max_batch:
+            raise ValueError(f"expected (batch<={self.max_batch}, {ch}, {self.H}, {self.W}), got {tuple(x.shape)}")
+        return b
+
+    def forward(self, x, out=None):
+        b = self._batch(x, self.in_ch)
+        if out is None:
+            out = np.zeros((b, self.out_ch, self.H, self.W), dtype=np.float32)
+        self._rc(self.L.drd_unet_forward(self.h, b, _p(x), _p(out)), "drd_unet_forward")
+        return out
+
+    def gradients(self, x, target):
+        b = self._batch(x, self.in_ch)
+        self._batch(target, self.out_ch)
+        loss = np.zeros(1, dtype=np.float32)
+        g = np.zeros(self.nparam, dtype=np.float32)
+        self._rc(self.L.drd_unet_gradients(self.h, b, _p(x), _p(target), _p(loss), _p(g)), "drd_unet_gradients")
+        return float(loss[0]), g
+
+    def train_step(self, x, target, lr):
+        b = self._batch(x, self.in_ch)
+        self._batch(target, self.out_ch)
+        loss = np.zeros(1, dtype=np.float32)
+        self._rc(self.L.drd_unet_train_step(self.h, b, _p(x), _p(target), C.c_float(lr), _p(loss)),
+                 "drd_unet_train_step")
+        return float(loss[0])
+
+
+# ------------------------------------------------------------------------------------------
+def _interior(a):
+    return np.ascontiguousarray(a[1:-1, 1:-1])
+
+
+def _rms(v):
+    return float(np.sqrt(np.mean(v * v)))
+
+
+def ch_run_pairs(case, nsteps, warmup=0, precision=F.DRD_PREC_MIXED):
+    """Runs warmup + nsteps steps of `case` on the GPU and returns the CH pairs of the last nsteps:
+    dict(x=(n,3,nz,nr) float32 inputs, y=(n,1,nz,nr) float32 targets, s=(n,) scales,
+    mu0=(n, nr*nz) plain guesses, mu1=(n, nr*nz) solutions, b=(n, nr*nz) right-hand sides)."""
+    P = case.params.copy()
+    P.precision = precision
+    nr, nz = P.nr, P.nz
+    ctx = DRDContext(P)
+    try:
+        ctx.set_case(case)
+        ctx.upload_state(case.state)
+        bdr = _interior(case.coefs["bdr_ph"])
+        t = 0.0
+        mus, phs = [], []
+        for s in range(warmup + nsteps + 1):
+            if s >= warmup:
+                st = ctx.download_state([F.F_RMU, F.F_PH])
+                mus.append(_interior(st[F.F_RMU]).reshape(-1))
+                phs.append(_interior(st[F.F_PH]))
+            if s == warmup + nsteps:
+                break
+            stats = ctx.step(s == 0, t)
+            if stats.ch.info != 0:
+                raise UNetError(f"CH solve did not converge at step {s} (info {stats.ch.info})")
+            t += P.dt
+        n = nsteps
+        X = np.zeros((n, 3, nz, nr), dtype=np.float32)
+        Y = np.zeros((n, 1, nz, nr), dtype=np.float32)
+        S = np.zeros(n)
+        B = np.zeros((n, nr * nz))
+        for k in range(n):
+            e = mus[k + 1] - mus[k]
+            r = ctx.op_apply(F.DRD_OP_CH_MATVEC, e, bdf=2)
+            B[k] = ctx.op_apply(F.DRD_OP_CH_MATVEC, mus[k + 1], bdf=2)
+            sc = max(_rms(r), 1e-300)
+            S[k] = sc
+            X[k, 0] = (r / sc).reshape(nz, nr)
+            X[k, 1] = bdr
+            X[k, 2] = phs[k]
+            Y[k, 0] = (e / sc).reshape(nz, nr)
+        return dict(x=X, y=Y, s=S, mu0=np.array(mus[:-1]), mu1=np.array(mus[1:]), b=B)
+    finally:
+        ctx.close()
+
+
+def concat_pairs(parts):
+    return {k: np.concatenate([p[k] for p in parts]) for k in parts[0]}
+
+
+def train(net, data, steps, batch=8, lr=1e-3, lr_final=1e-4, seed=0, log_every=0):
+    """Adam on random minibatches of `data` (dict x, y) with a geometric learning-rate decay.
+    Returns the list of losses."""
+    rng = np.random.default_rng(seed)
+    n = data["x"].shape[0]
+    losses = []
+    batch = min(batch, net.max_batch, n)
+    for it in range(steps):
+        idx = rng.choice(n, size=batch, replace=False)
+        rate = lr * (lr_final / lr) ** (it / max(steps - 1, 1))
+        loss = net.train_step(np.ascontiguousarray(data["x"][idx]), np.ascontiguousarray(data["y"][idx]), rate)
+        losses.append(loss)
+        if log_every and (it % log_every == 0 or it == steps - 1):
+            print(f"  train step {it}: loss {loss:.4e} lr {rate:.2e}", flush=True)
+    return losses
+
+
+def ch_guess(ctx, net, b, mu0, bdr, ph):
+    """The learned guess for A x = b from the plain guess mu0 (packed), or mu0 itself when the
+    learned one's FP64 residual is not smaller.  Returns (x0, used_learned, ||r_plain||, ||r_learned||)."""
+    nr, nz = ctx.nr, ctx.nz
+    r = b - ctx.op_apply(F.DRD_OP_CH_MATVEC, mu0, bdf=2)
+    sc = max(_rms(r), 1e-300)
+    x = np.zeros((1, 3, nz, nr), dtype=np.float32)
+    x[0, 0] = (r / sc).reshape(nz, nr)
+    x[0, 1] = bdr
+    x[0, 2] = ph
+    y = net.forward(x)
+    x0 = mu0 + sc * y[0, 0].reshape(-1).astype(np.float64)
+    r1 = b - ctx.op_apply(F.DRD_OP_CH_MATVEC, x0, bdf=2)
+    n0, n1 = float(np.linalg.norm(r)), float(np.linalg.norm(r1))
+    if not n1 < n0:
+        return mu0.copy(), False, n0, n1
+    return x0, True, n0, n1
+
+
+def evaluate_ch(case, net, pairs, precision=F.DRD_PREC_MIXED, tol=1e-8):
+    """Iterations and wall time of the CH solves of `pairs` (from ch_run_pairs on `case`) to the
+    FP64 relative residual `tol`, from the plain guess and from the learned one."""
+    P = case.params.copy()
+    P.precision = precision
+    P.tol = tol
+    ctx = DRDContext(P)
+    try:
+        ctx.set_case(case)
+        bdr = _interior(case.coefs["bdr_ph"])
+        out = dict(iters_plain=[], iters_learned=[], res_plain=[], res_learned=[], used=[], t_plain=[],
+                   t_learned=[], t_guess=[], true_resid_plain=[], true_resid_learned=[])
+        for k in range(pairs["b"].shape[0]):
+            b, mu0 = pairs["b"][k], pairs["mu0"][k]
+            ph = pairs["x"][k, 2]
+            t0 = time.perf_counter()
+            _, st = ctx.solve(F.DRD_SYS_CH, b, mu0)
+            t1 = time.perf_counter()
+            x0, used, n0, n1 = ch_guess(ctx, net, b, mu0, bdr, ph)
+            t2 = time.perf_counter()
+            _, st2 = ctx.solve(F.DRD_SYS_CH, b, x0)
+            t3 = time.perf_counter()
+            out["iters_plain"].append(st.iter)
+            out["iters_learned"].append(st2.iter)
+            out["res_plain"].append(n0)
+            out["res_learned"].append(n1)
+            out["used"].append(used)
+            out["t_plain"].append(t1 - t0)
+            out["t_guess"].append(t2 - t1)
+            out["t_learned"].append(t3 - t2)
+            out["true_resid_plain"].append(st.true_resid)
+            out["true_resid_learned"].append(st2.true_resid)
+        return {k: np.array(v) for k, v in out.items()}
+    finally:
+        ctx.close()

@@ -414,6 +414,39 @@ long drd_op_length(drd_ctx* ctx, int op);
  * independent solves that do not come from a time step. */
 int drd_solve(drd_ctx* ctx, int system, int bdf, const double* b, double* x, drd_status* st);
 
+/* ---- learned initial guess ---------------------------------------------------------------
+ * A 4-level U-Net (channels 32/64/128/256, 3x3 convolutions with ReLU, 2x2 average pooling,
+ * nearest upsampling, concatenated skips, a 1x1 output convolution) in BF16 weights and
+ * activations with FP32 accumulation, run and trained by the library's own tensor-core
+ * kernels.  It maps in_ch input fields on an H x W grid (for the CH system: the residual of
+ * the plain guess divided by its RMS, the resistance bdr_ph and the phase field, each as the
+ * packed nr x nz interior, H = nz rows of W = nr) to out_ch fields (the correction of the
+ * guess in the same units).  No counterpart exists in the reference: this is the learned
+ * guess its solves (PhSolve.f90:62-74, VeloSolve_2_combined.f90:388-407) can start from, with
+ * the plain guess as the fallback that the FP64 true residual judges.
+ *
+ * Arrays are FP32, (batch, channels, H, W) C order, in host or device memory.  Parameters are
+ * one FP32 vector of drd_unet_param_count floats: per 3x3 layer the weights [tap][Cout][Cin]
+ * then the bias, the 17 layers in the order enc0a enc0b enc1a enc1b enc2a enc2b enc3a enc3b,
+ * then per decoder level 2, 1, 0: upconv, conv(concat), conv; then the output layer's
+ * weights [out_ch][32] and bias.  The first layer's Cin is 16 (inputs zero-padded). */
+typedef struct drd_unet drd_unet;
+int drd_unet_create(int H, int W, int in_ch, int out_ch, int max_batch, uint64_t seed, drd_unet** net);
+int drd_unet_destroy(drd_unet* net);
+int64_t drd_unet_param_count(drd_unet* net);
+const char* drd_unet_last_error(drd_unet* net);
+int drd_unet_get_params(drd_unet* net, float* params);
+/* Sets the parameters and resets the Adam state. */
+int drd_unet_set_params(drd_unet* net, const float* params);
+int drd_unet_forward(drd_unet* net, int batch, const float* x, float* y);
+/* Mean squared error of forward(x) against target over the H x W grid, and its gradient
+ * with respect to every parameter (no update).  loss / grads may be NULL. */
+int drd_unet_gradients(drd_unet* net, int batch, const float* x, const float* target, float* loss, float* grads);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) at learning rate lr on that loss. */
+int drd_unet_train_step(drd_unet* net, int batch, const float* x, const float* target, float lr, float* loss);
+/* The network's CUDA stream (cudaStream_t). */
+int drd_unet_stream(drd_unet* net, void** stream);
+
 /* ---- performance instrumentation ------------------------------------------------------- */
 
 /* Kernels that drd_kernel_bench can time in isolation on the context's current data. */
