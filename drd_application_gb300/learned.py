@@ -12,7 +12,13 @@ interior (packed CH order: H = nz rows of W = nr) and the target is e_n / s_n.
 Guess.  x0 = mu^n + s * net(r / s, bdr_ph, ph^n), r = b - A mu^n.  The plain guess stays the
 fallback: when the learned guess's FP64 residual is not below the plain one's, the plain
 guess is returned.  The solve that follows is unchanged, so the result meets the same FP64
-tolerance either way; what the network changes is the iteration count.
+tolerance either way; what the network changes is the iteration count.  The same holds with
+the cubic extrapolation (guess_mode 3) as the base guess (base="cubic").
+
+    python -m drd_application_gb300.learned [--base plain|cubic] [--train-seeds 24] ...
+
+generates the pairs on the GPU, trains the network and reports, on held-out seeds, the
+relative error of each guess and the mixed-precision CH iterations to the FP64 residual 1e-8.
 """
 import ctypes as C
 import time
@@ -21,7 +27,6 @@ import numpy as np
 
 from . import abi, _lib
 from .api import DRDContext
-from .layout import ptr
 
 F = abi
 
@@ -121,10 +126,18 @@ def _rms(v):
     return float(np.sqrt(np.mean(v * v)))
 
 
-def ch_run_pairs(case, nsteps, warmup=0, precision=F.DRD_PREC_MIXED):
+def cubic_guess(hist):
+    """4 mu^n - 6 mu^{n-1} + 4 mu^{n-2} - mu^{n-3} (guess_mode 3) from [mu^{n-3}, .., mu^n]."""
+    return 4 * hist[-1] - 6 * hist[-2] + 4 * hist[-3] - hist[-4]
+
+
+def ch_run_pairs(case, nsteps, warmup=0, precision=F.DRD_PREC_MIXED, base="plain"):
     """Runs warmup + nsteps steps of `case` on the GPU and returns the CH pairs of the last nsteps:
     dict(x=(n,3,nz,nr) float32 inputs, y=(n,1,nz,nr) float32 targets, s=(n,) scales,
-    mu0=(n, nr*nz) plain guesses, mu1=(n, nr*nz) solutions, b=(n, nr*nz) right-hand sides)."""
+    mu0=(n, nr*nz) base guesses, mu1=(n, nr*nz) solutions, b=(n, nr*nz) right-hand sides).
+    base: "plain" (mu^n) or "cubic" (cubic_guess; needs warmup >= 3)."""
+    if base == "cubic" and warmup < 3:
+        raise ValueError("the cubic guess needs three earlier steps")
     P = case.params.copy()
     P.precision = precision
     nr, nz = P.nr, P.nz
@@ -135,8 +148,9 @@ def ch_run_pairs(case, nsteps, warmup=0, precision=F.DRD_PREC_MIXED):
         bdr = _interior(case.coefs["bdr_ph"])
         t = 0.0
         mus, phs = [], []
+        first = warmup - 3 if base == "cubic" else warmup
         for s in range(warmup + nsteps + 1):
-            if s >= warmup:
+            if s >= first:
                 st = ctx.download_state([F.F_RMU, F.F_PH])
                 mus.append(_interior(st[F.F_RMU]).reshape(-1))
                 phs.append(_interior(st[F.F_PH]))
@@ -146,22 +160,25 @@ def ch_run_pairs(case, nsteps, warmup=0, precision=F.DRD_PREC_MIXED):
             if stats.ch.info != 0:
                 raise UNetError(f"CH solve did not converge at step {s} (info {stats.ch.info})")
             t += P.dt
-        n = nsteps
+        n, o = nsteps, 3 if base == "cubic" else 0
         X = np.zeros((n, 3, nz, nr), dtype=np.float32)
         Y = np.zeros((n, 1, nz, nr), dtype=np.float32)
         S = np.zeros(n)
         B = np.zeros((n, nr * nz))
+        G = np.zeros((n, nr * nz))
         for k in range(n):
-            e = mus[k + 1] - mus[k]
+            j = k + o
+            G[k] = cubic_guess(mus[j - 3:j + 1]) if base == "cubic" else mus[j]
+            e = mus[j + 1] - G[k]
             r = ctx.op_apply(F.DRD_OP_CH_MATVEC, e, bdf=2)
-            B[k] = ctx.op_apply(F.DRD_OP_CH_MATVEC, mus[k + 1], bdf=2)
+            B[k] = ctx.op_apply(F.DRD_OP_CH_MATVEC, mus[j + 1], bdf=2)
             sc = max(_rms(r), 1e-300)
             S[k] = sc
             X[k, 0] = (r / sc).reshape(nz, nr)
             X[k, 1] = bdr
-            X[k, 2] = phs[k]
+            X[k, 2] = phs[j]
             Y[k, 0] = (e / sc).reshape(nz, nr)
-        return dict(x=X, y=Y, s=S, mu0=np.array(mus[:-1]), mu1=np.array(mus[1:]), b=B)
+        return dict(x=X, y=Y, s=S, mu0=G, mu1=np.array(mus[o + 1:o + n + 1]), b=B)
     finally:
         ctx.close()
 
@@ -187,9 +204,12 @@ def train(net, data, steps, batch=8, lr=1e-3, lr_final=1e-4, seed=0, log_every=0
     return losses
 
 
-def ch_guess(ctx, net, b, mu0, bdr, ph):
-    """The learned guess for A x = b from the plain guess mu0 (packed), or mu0 itself when the
-    learned one's FP64 residual is not smaller.  Returns (x0, used_learned, ||r_plain||, ||r_learned||)."""
+def ch_guess(ctx, net, b, mu0, bdr, ph, judge="residual"):
+    """The learned guess for A x = b from the base guess mu0 (packed), or mu0 itself when the
+    learned one is judged worse.  judge: "residual" compares the FP64 residual norms ||b - A x||
+    (the default), "precond" compares ||M^-1 r|| (M^-1 = PSolve_CG, an estimate of the error),
+    "none" always takes the learned guess.  Returns (x0, used_learned, measure_base,
+    measure_learned)."""
     nr, nz = ctx.nr, ctx.nz
     r = b - ctx.op_apply(F.DRD_OP_CH_MATVEC, mu0, bdf=2)
     sc = max(_rms(r), 1e-300)
@@ -199,14 +219,19 @@ def ch_guess(ctx, net, b, mu0, bdr, ph):
     x[0, 2] = ph
     y = net.forward(x)
     x0 = mu0 + sc * y[0, 0].reshape(-1).astype(np.float64)
+    if judge == "none":
+        return x0, True, 0.0, 0.0
     r1 = b - ctx.op_apply(F.DRD_OP_CH_MATVEC, x0, bdf=2)
+    if judge == "precond":
+        r = ctx.op_apply(F.DRD_OP_CH_PSOLVE, r, bdf=2)
+        r1 = ctx.op_apply(F.DRD_OP_CH_PSOLVE, r1, bdf=2)
     n0, n1 = float(np.linalg.norm(r)), float(np.linalg.norm(r1))
     if not n1 < n0:
         return mu0.copy(), False, n0, n1
     return x0, True, n0, n1
 
 
-def evaluate_ch(case, net, pairs, precision=F.DRD_PREC_MIXED, tol=1e-8):
+def evaluate_ch(case, net, pairs, precision=F.DRD_PREC_MIXED, tol=1e-8, judge="residual"):
     """Iterations and wall time of the CH solves of `pairs` (from ch_run_pairs on `case`) to the
     FP64 relative residual `tol`, from the plain guess and from the learned one."""
     P = case.params.copy()
@@ -224,7 +249,7 @@ def evaluate_ch(case, net, pairs, precision=F.DRD_PREC_MIXED, tol=1e-8):
             t0 = time.perf_counter()
             _, st = ctx.solve(F.DRD_SYS_CH, b, mu0)
             t1 = time.perf_counter()
-            x0, used, n0, n1 = ch_guess(ctx, net, b, mu0, bdr, ph)
+            x0, used, n0, n1 = ch_guess(ctx, net, b, mu0, bdr, ph, judge)
             t2 = time.perf_counter()
             _, st2 = ctx.solve(F.DRD_SYS_CH, b, x0)
             t3 = time.perf_counter()
@@ -241,3 +266,75 @@ def evaluate_ch(case, net, pairs, precision=F.DRD_PREC_MIXED, tol=1e-8):
         return {k: np.array(v) for k, v in out.items()}
     finally:
         ctx.close()
+
+
+def _layers():
+    """(cin, cout, level) of the 17 3x3 layers, as drd_unet_create builds them."""
+    L = []
+    for l in range(4):
+        L.append((16 if l == 0 else 32 << (l - 1), 32 << l, l))
+        L.append((32 << l, 32 << l, l))
+    for l in (2, 1, 0):
+        L += [(32 << (l + 1), 32 << l, l), (64 << l, 32 << l, l), (32 << l, 32 << l, l)]
+    return L
+
+
+def conv_flops(Hp, Wp, batch, train=True):
+    """Tensor-core FLOPs (2 per multiply-add) of the 3x3 layers on the padded Hp x Wp grid for
+    one forward pass, or with train=True one training step (forward, data gradient, weight
+    gradient; the first layer has no data gradient)."""
+    total = 0.0
+    for i, (ci, co, l) in enumerate(_layers()):
+        f = 2.0 * 9 * ci * co * (Hp >> l) * (Wp >> l) * batch
+        total += f * ((2 if i == 0 else 3) if train else 1)
+    return total
+
+
+def main(argv=None):
+    import argparse
+
+    from .workloads import make_case
+
+    ap = argparse.ArgumentParser(description="train and evaluate the learned CH guess on C2 runs")
+    ap.add_argument("--base", choices=("plain", "cubic"), default="plain")
+    ap.add_argument("--train-seeds", type=int, default=24, help="C2 geometries 1000.. used for training")
+    ap.add_argument("--per-seed", type=int, default=12, help="pairs per training run")
+    ap.add_argument("--warmup", type=int, default=10, help="steps before the first pair of a run")
+    ap.add_argument("--steps", type=int, default=1500, help="Adam steps (batch 8)")
+    ap.add_argument("--eval-seeds", type=int, default=2, help="held-out geometries 2000..")
+    ap.add_argument("--eval-pairs", type=int, default=8)
+    ap.add_argument("--nr", type=int, default=420)
+    ap.add_argument("--nz", type=int, default=180)
+    ap.add_argument("--save", default=None, help="write the trained parameters (.npy)")
+    a = ap.parse_args(argv)
+    t0 = time.perf_counter()
+    parts = [ch_run_pairs(make_case("c2", seed=1000 + s, nr=a.nr, nz=a.nz), a.per_seed, a.warmup, base=a.base)
+             for s in range(a.train_seeds)]
+    data = concat_pairs(parts)
+    t1 = time.perf_counter()
+    net = UNet(a.nz, a.nr, 3, 1, max_batch=8, seed=0)
+    losses = train(net, data, a.steps, batch=8)
+    t2 = time.perf_counter()
+    fl = conv_flops(-(-a.nz // 8) * 8, -(-a.nr // 8) * 8, 8) * a.steps
+    print(f"pairs {data['x'].shape[0]} in {t1 - t0:.1f} s; {a.steps} Adam steps in {t2 - t1:.1f} s "
+          f"({fl / (t2 - t1) / 1e12:.1f} TFLOP/s in the 3x3 layers); loss {np.mean(losses[:20]):.3e} -> "
+          f"{np.mean(losses[-50:]):.3e}", flush=True)
+    if a.save:
+        np.save(a.save, net.get_params())
+    for s in range(a.eval_seeds):
+        case = make_case("c2", seed=2000 + s, nr=a.nr, nz=a.nz)
+        pr = ch_run_pairs(case, a.eval_pairs, a.warmup, base=a.base)
+        y = np.concatenate([net.forward(np.ascontiguousarray(pr["x"][k:k + 1])) for k in range(pr["x"].shape[0])])
+        rel = np.sqrt(((y - pr["y"]) ** 2).sum(axis=(1, 2, 3)) / (pr["y"] ** 2).sum(axis=(1, 2, 3)))
+        print(f"held-out seed {2000 + s}: error of the learned guess / error of the {a.base} guess: "
+              f"mean {rel.mean():.3f}", flush=True)
+        for judge in ("none", "residual"):
+            ev = evaluate_ch(case, net, pr, judge=judge)
+            print(f"  judge {judge}: mixed CH iterations to 1e-8: {a.base} {ev['iters_plain'].mean():.1f}, "
+                  f"learned {ev['iters_learned'].mean():.1f}; learned guess taken {int(ev['used'].sum())}/"
+                  f"{ev['used'].size}; max true residual {ev['true_resid_learned'].max():.2e}", flush=True)
+    net.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -4,9 +4,12 @@ Adam loop, host and device buffers.
 
 Tolerances: the kernels and the oracle round the same values to BF16, but the kernels sum in
 FP32 in another order, so an element near a rounding boundary can round the other way; such
-flips (2^-8 relative) spread through the 17 layers.  Forward outputs agree to 2e-2 and
-per-layer gradients to 5e-2 in the relative 2-norm, against differences of order 1 for a
-wrong layout, tap or transposition."""
+flips (2^-8 relative) spread through the 17 layers.  Forward outputs agree to 2e-2 in the
+relative 2-norm.  Weight gradients are sums over pixels with heavy cancellation, so BF16
+rounding alone moves them 7-22% from their FP64 values on these random-target cases; the
+check is that every layer's kernel gradient is closer to the rounded oracle than the rounded
+oracle is to FP64 (measured: 0.35-0.6 of it), and within 0.2 of it, against differences of
+order 1 for a wrong layout, tap or transposition."""
 import numpy as np
 import pytest
 
@@ -61,11 +64,13 @@ def test_gradients_match_oracle(cuda_lib, H, W):
     x = rng.standard_normal((2, 3, H, W)).astype(np.float32)
     t = rng.standard_normal((2, 1, H, W)).astype(np.float32)
     loss, g = net.gradients(x, t)
-    lo, go = UNetOracle(H, W, 3, 1).gradients(net.get_params().astype(np.float64), x.astype(np.float64),
-                                              t.astype(np.float64))
+    p, x64, t64 = net.get_params().astype(np.float64), x.astype(np.float64), t.astype(np.float64)
+    lo, go = UNetOracle(H, W, 3, 1).gradients(p, x64, t64)
+    _, g64 = UNetOracle(H, W, 3, 1, rounding=False).gradients(p, x64, t64)
     assert abs(loss - lo) <= 1e-3 * lo
     for li, s in enumerate(_slices(1)):
-        assert _rel(g[s], go[s]) < 5e-2, li
+        noise = _rel(go[s], g64[s])
+        assert _rel(g[s], go[s]) < min(0.8 * noise, 0.2), (li, _rel(g[s], go[s]), noise)
     net.close()
 
 
