@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=None, help="timed steps of the plain FP64 path")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--c3-solves", type=int, default=512, help="independent momentum solves of the C3 batch (0: skip)")
+    ap.add_argument("--learned-steps", type=int, default=600,
+                    help="Adam steps of the learned CH guess leg (0: skip)")
     ap.add_argument("--nr", type=int, default=420)
     ap.add_argument("--nz", type=int, default=180)
     return ap.parse_args()
@@ -259,6 +261,60 @@ def cpu_c3_sample(seed, n=4, budget_s=20.0):
             "sample": f"first {done} solves of the same C3 batch, FP64 oracle, {elapsed:.1f} s"}
 
 
+def time_learned(steps, nr, nz, train_seeds=8, per_seed=12):
+    """The learned CH guess beside the headline: the U-Net trained by the library's kernels on
+    CH pairs from this workload's own runs (geometries 1000..), then evaluated on a held-out
+    geometry (2000): mixed CH iterations to the FP64 residual 1e-8 from the plain guess x^n and
+    from the learned one (taken unconditionally, and under the FP64-residual judge)."""
+    import numpy as np
+
+    from drd_application_gb300 import learned as LN
+    from drd_application_gb300.workloads import make_case
+
+    t0 = time.perf_counter()
+    data = LN.concat_pairs([LN.ch_run_pairs(make_case("c2", seed=1000 + s, nr=nr, nz=nz), per_seed, warmup=10)
+                            for s in range(train_seeds)])
+    t1 = time.perf_counter()
+    net = LN.UNet(nz, nr, 3, 1, max_batch=8, seed=0)
+    rng = np.random.default_rng(0)
+    n = data["x"].shape[0]
+    batches = [rng.choice(n, size=8, replace=False) for _ in range(steps + 3)]
+    xs = [np.ascontiguousarray(data["x"][i]) for i in batches]
+    ys = [np.ascontiguousarray(data["y"][i]) for i in batches]
+    for k in range(3):  # warm-up at learning rate 0
+        net.train_step(xs[k], ys[k], 0.0)
+    losses, step_s = [], []
+    for k in range(steps):
+        lr = 1e-3 * (5e-2) ** (k / max(steps - 1, 1))
+        a = time.perf_counter()
+        losses.append(net.train_step(xs[k + 3], ys[k + 3], lr))
+        step_s.append(time.perf_counter() - a)
+    t2 = time.perf_counter()
+    case = make_case("c2", seed=2000, nr=nr, nz=nz)
+    pr = LN.ch_run_pairs(case, 6, warmup=10)
+    y = np.concatenate([net.forward(np.ascontiguousarray(pr["x"][k:k + 1])) for k in range(6)])
+    rel = np.sqrt(((y - pr["y"]) ** 2).sum(axis=(1, 2, 3)) / (pr["y"] ** 2).sum(axis=(1, 2, 3)))
+    ev = {j: LN.evaluate_ch(case, net, pr, judge=j) for j in ("none", "residual")}
+    net.close()
+    med = statistics.median(step_s)
+    fl = LN.conv_flops(-(-nz // 8) * 8, -(-nr // 8) * 8, 8)
+    return {
+        "network": "U-Net 4 levels, 32 base channels, 3x3, BF16 weights/activations, FP32 accumulate "
+                   "(mma.sync m16n8k16 kernels)",
+        "inputs": "residual of x^n / its RMS, bdr_ph, ph; target (x^(n+1) - x^n) / RMS",
+        "train_pairs": n, "adam_steps": steps, "batch": 8,
+        "data_s": t1 - t0, "train_s": t2 - t1, "loss_first": float(np.mean(losses[:10])),
+        "loss_last": float(np.mean(losses[-20:])),
+        "train_step_ms": 1e3 * med, "conv_tflops": fl / med / 1e12,
+        "held_out_error_ratio": float(rel.mean()),
+        "iters_plain": float(ev["none"]["iters_plain"].mean()),
+        "iters_learned": float(ev["none"]["iters_learned"].mean()),
+        "iters_learned_residual_judge": float(ev["residual"]["iters_learned"].mean()),
+        "learned_taken_residual_judge": f"{int(ev['residual']['used'].sum())}/{ev['residual']['used'].size}",
+        "max_true_resid": float(max(ev["none"]["true_resid_learned"].max(), ev["none"]["true_resid_plain"].max())),
+    }
+
+
 def time_resident(ctx, case, warmup, steps, flush_bytes):
     """Per-step device time (CUDA events inside drd_step) with the state resident in HBM."""
     from drd_application_gb300 import abi
@@ -414,6 +470,9 @@ def run_gpu(args, ws, rank, local):
         if rank == 0 and not args.no_cpu:
             c3["cpu_baseline"] = cpu_c3_sample(rank)
 
+    # the learned CH guess (rank 0 only: it is reported beside the headline)
+    learned = time_learned(args.learned_steps, args.nr, args.nz) if (args.learned_steps > 0 and rank == 0) else None
+
     # plain FP64 path, resident state (--fp64-steps 0 skips it, e.g. for profiler runs)
     f64, f64_sec = None, None
     if K64 > 0:
@@ -483,6 +542,7 @@ def run_gpu(args, ws, rank, local):
             "with_particles": {"steps_per_s": K * ws / pt_sec, "ms_per_step": 1e3 * pt_sec / K, "beads": 9,
                                "solves_to_fp64_1e-8": f"{pt['solves_ok']}/{pt['solves']}"},
             "c3_batch": c3,
+            "learned_guess": learned,
         },
         "roofline": {"bound": "hbm", "kernel": "k_bicg_persist<CH> (whole mixed CH solve)", "achieved": achieved,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": TRAFFIC_CH,

@@ -249,19 +249,34 @@ __global__ void __launch_bounds__(128) k_wgrad(WgArgs a) {
     }
 }
 
-// bias gradient: db[c] += sum over pixels of G[p][c]
-__global__ void k_colsum(const bf16* g, long gbs, int ldg, int HW, int batch, int C, float* db) {
-    const int c = threadIdx.x;
-    if (c >= C) return;
+// bias gradient: db[c] += sum over pixels of G[p][c].  A block sums 256 pixels; its threads
+// are (pixel row, channel pair), the rows reduced through shared memory.
+__global__ void __launch_bounds__(256) k_colsum(const bf16* g, long gbs, int ldg, int HW, int batch, int C, float* db) {
+    __shared__ float2 part[256];
+    const int np = C >> 1;        // channel pairs: 16..128, divides 256
+    const int rows = 256 / np;
+    const int cp = threadIdx.x % np, r = threadIdx.x / np;
     const long total = (long)batch * HW;
-    const long q0 = (long)blockIdx.x * 1024;
-    float s = 0.f;
-    for (long q = q0; q < q0 + 1024 && q < total; ++q) {
+    const long q0 = (long)blockIdx.x * 256;
+    float2 s = make_float2(0.f, 0.f);
+    for (long q = q0 + r; q < q0 + 256 && q < total; q += rows) {
         const int b = (int)(q / HW);
         const long p = q - (long)b * HW;
-        s += __bfloat162float(g[(long)b * gbs + p * ldg + c]);
+        const float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(g + (long)b * gbs + p * ldg + 2 * cp));
+        s.x += v.x;
+        s.y += v.y;
     }
-    atomicAdd(db + c, s);
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < np) {
+        float2 t = make_float2(0.f, 0.f);
+        for (int k = 0; k < rows; ++k) {
+            t.x += part[k * np + threadIdx.x].x;
+            t.y += part[k * np + threadIdx.x].y;
+        }
+        atomicAdd(db + 2 * threadIdx.x, t.x);
+        atomicAdd(db + 2 * threadIdx.x + 1, t.y);
+    }
 }
 
 // 2x2 average pool: y (H/2 x W/2) from x (H x W)
@@ -407,9 +422,9 @@ __global__ void k_out_bwd_w(const float* dy, int cout, const bf16* d0, float* dw
     const int o = threadIdx.x / kBase, c = threadIdx.x % kBase;
     if (o >= cout) return;
     const long n = (long)batch * H0 * W0;
-    const long i0 = (long)blockIdx.x * 1024;
+    const long i0 = (long)blockIdx.x * 256;
     float s = 0.f, sb = 0.f;
-    for (long i = i0; i < i0 + 1024 && i < n; ++i) {
+    for (long i = i0; i < i0 + 256 && i < n; ++i) {
         const int w = (int)(i % W0);
         const int h = (int)((i / W0) % H0);
         const int b = (int)(i / ((long)W0 * H0));
@@ -527,8 +542,8 @@ void wgrad(drd_unet* n, int li, const bf16* x, int ldx, long xbs, const bf16* G,
     const long total = (long)batch * H * W;
     dim3 grid((unsigned)((total + kWgPix - 1) / kWgPix), 9 * (Ly.cout / 32) * (Ly.cin / a.ci_tile));
     k_wgrad<<<grid, 128, 0, n->s>>>(a);
-    k_colsum<<<(unsigned)((total + 1023) / 1024), Ly.cout, 0, n->s>>>(G, a.gbs, Ly.cout, H * W, batch, Ly.cout,
-                                                                     n->G32 + Ly.b_off);
+    k_colsum<<<(unsigned)((total + 255) / 256), 256, 0, n->s>>>(G, a.gbs, Ly.cout, H * W, batch, Ly.cout,
+                                                                 n->G32 + Ly.b_off);
 }
 
 void mask_grad(drd_unet* n, int l, const float* a, int lda, const float* b, int ldb, const bf16* mask, int ldm, bf16* G,
@@ -581,7 +596,7 @@ void forward(drd_unet* n, const float* x, int batch) {
 
 void backward(drd_unet* n, int batch) {
     const long hw0 = n->HWl(0);
-    k_out_bwd_w<<<(unsigned)(((long)batch * n->H0 * n->W0 + 1023) / 1024), kMaxOut * kBase, 0, n->s>>>(
+    k_out_bwd_w<<<(unsigned)(((long)batch * n->H0 * n->W0 + 255) / 256), kMaxOut * kBase, 0, n->s>>>(
         n->dy, n->cout, n->dd[0], n->G32 + n->wo_off, n->G32 + n->bo_off, n->H0, n->W0, n->Hp, n->Wp, batch);
     k_out_bwd_x<<<grid_for((long)batch * hw0), 256, 0, n->s>>>(n->dy, n->W32 + n->wo_off, n->cout, n->dd[0], n->Gl[16],
                                                                 n->H0, n->W0, n->Hp, n->Wp, batch);
