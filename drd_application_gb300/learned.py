@@ -306,6 +306,9 @@ def main(argv=None):
     ap.add_argument("--nr", type=int, default=420)
     ap.add_argument("--nz", type=int, default=180)
     ap.add_argument("--save", default=None, help="write the trained parameters (.npy)")
+    ap.add_argument("--lowpass", type=float, nargs="*", default=[],
+                    help="also evaluate the learned and the exact corrections with only the lowest fraction "
+                         "of their DCT-II modes kept along each axis (evaluation only)")
     a = ap.parse_args(argv)
     t0 = time.perf_counter()
     parts = [ch_run_pairs(make_case("c2", seed=1000 + s, nr=a.nr, nz=a.nz), a.per_seed, a.warmup, base=a.base)
@@ -333,7 +336,46 @@ def main(argv=None):
             print(f"  judge {judge}: mixed CH iterations to 1e-8: {a.base} {ev['iters_plain'].mean():.1f}, "
                   f"learned {ev['iters_learned'].mean():.1f}; learned guess taken {int(ev['used'].sum())}/"
                   f"{ev['used'].size}; max true residual {ev['true_resid_learned'].max():.2e}", flush=True)
+        for frac in a.lowpass:
+            _lowpass_rows(case, net, pr, frac)
     net.close()
+
+
+def _lowpass_rows(case, net, pr, frac):
+    """Mixed CH iterations from the base guess plus the learned, or the exact, correction with
+    only its lowest `frac` of DCT-II modes kept along each axis."""
+    import scipy.fft as sf
+
+    nz, nr = case.nz, case.nr
+
+    def lp(v):
+        c = sf.dctn(v.reshape(nz, nr), type=2, norm="ortho")
+        c[int(nz * frac):, :] = 0.0
+        c[:, int(nr * frac):] = 0.0
+        return sf.idctn(c, type=2, norm="ortho").reshape(-1)
+
+    P = case.params.copy()
+    P.precision = F.DRD_PREC_MIXED
+    P.tol = 1e-8
+    ctx = DRDContext(P)
+    try:
+        ctx.set_case(case)
+        bdr = _interior(case.coefs["bdr_ph"])
+        its = {"learned": [], "exact": []}
+        errs = {"learned": [], "exact": []}
+        for k in range(pr["b"].shape[0]):
+            b, g0, mu1 = pr["b"][k], pr["mu0"][k], pr["mu1"][k]
+            xl, _, _, _ = ch_guess(ctx, net, b, g0, bdr, pr["x"][k, 2], judge="none")
+            for name, corr in (("learned", xl - g0), ("exact", mu1 - g0)):
+                x0 = g0 + lp(corr)
+                _, st = ctx.solve(F.DRD_SYS_CH, b, x0)
+                its[name].append(st.iter)
+                errs[name].append(np.linalg.norm(x0 - mu1) / np.linalg.norm(mu1 - g0))
+        for name in its:
+            print(f"  {name} correction low-passed to {frac}: error ratio {np.mean(errs[name]):.3f}, "
+                  f"iterations {np.mean(its[name]):.1f}", flush=True)
+    finally:
+        ctx.close()
 
 
 if __name__ == "__main__":
