@@ -43,8 +43,7 @@ constexpr int kLevels = 4;
 constexpr int kBase = 32;
 constexpr int kCinPad = 16;   // the input's channels, zero-padded to one MMA K step
 constexpr int kMaxOut = 4;
-constexpr int kConvTPB = 128; // 4 warps x 32 pixels per block of the convolution
-constexpr int kWgPix = 2048;  // pixels per block of the weight gradient
+constexpr int kConvTPB = 128; // 4 warps per block of the convolution, one tile row each
 
 // ------------------------------------------------------------------------------------------
 // tensor-core primitive: D(16x8, f32) += A(16x16, bf16, row) * B(16x8, bf16, col)
@@ -56,21 +55,20 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-__device__ __forceinline__ uint32_t ld_pair(const bf16* p) {
-    return p ? __ldg(reinterpret_cast<const unsigned int*>(p)) : 0u;
-}
-__device__ __forceinline__ uint32_t pack2(const bf16* lo, const bf16* hi) {
-    const unsigned short a = lo ? __ldg(reinterpret_cast<const unsigned short*>(lo)) : 0;
-    const unsigned short b = hi ? __ldg(reinterpret_cast<const unsigned short*>(hi)) : 0;
-    return (uint32_t)a | ((uint32_t)b << 16);
-}
 
 // ------------------------------------------------------------------------------------------
 // 3x3 convolution as an implicit GEMM: M = pixels, N = output channels, K = 9 taps x Cin.
-// A block has 4 warps; a warp computes 32 pixels x 32 output channels (2 x 4 MMA tiles).
-// With `up`, the input is at half resolution and is read through nearest upsampling.  The
-// same kernel computes data gradients (weights = the flipped transpose, no bias/ReLU); `mask`
-// then applies the ReLU derivative of the layer below (zero where mask <= 0).
+// A block computes a tile of kTH x kTW pixels (one image row of kTW pixels per warp, two MMA
+// row tiles) for 32 output channels.  Per chunk of kc input channels it stages the tile's
+// input with its one-pixel halo and the 9 taps' weights in shared memory (rows padded by 8
+// elements, so that the 8 rows an ldmatrix phase reads fall in distinct banks); the MMA
+// fragments then come from shared memory through ldmatrix.  With `up`, the input is at half
+// resolution and is read through nearest upsampling.  The same kernel computes data
+// gradients (weights = the flipped transpose, no bias/ReLU); `mask` then applies the ReLU
+// derivative of the layer below (zero where mask <= 0).
+constexpr int kTH = 4, kTW = 32, kKC = 32;
+constexpr int kHaloPix = (kTH + 2) * (kTW + 2);
+
 struct ConvArgs {
     const bf16* x; long xbs; int ldx;
     const bf16* w; const float* bias;
@@ -79,22 +77,25 @@ struct ConvArgs {
     int H, W, Cin, Cout, up, relu;
 };
 
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const bf16* p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
 __global__ void __launch_bounds__(kConvTPB) k_conv3(ConvArgs a) {
+    __shared__ __align__(16) bf16 s_in[kHaloPix * (kKC + 8)];
+    __shared__ __align__(16) bf16 s_w[9 * 32 * (kKC + 8)];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int HW = a.H * a.W, b = blockIdx.z;
-    const int pw = blockIdx.x * kConvTPB + warp * 32;
-    const int co0 = blockIdx.y * 32;
+    const int nco = a.Cout / 32;
+    const int b = blockIdx.z / nco, co0 = (blockIdx.z % nco) * 32;
+    const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
+    const int kc = (a.Cin % kKC == 0) ? kKC : 16;  // channels per staged chunk
+    const int ps = kc + 8;                          // padded row of one pixel / one weight row
+    const int parts = kc / 8;                       // 16-byte pieces per row
     const bf16* xb = a.x + (long)b * a.xbs;
     const int Wl = a.W >> 1;
-    int py[4], px[4];
-    bool pv[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        const int p = pw + (r >> 1) * 16 + (r & 1) * 8 + g;
-        pv[r] = p < HW;
-        py[r] = pv[r] ? p / a.W : 0;
-        px[r] = pv[r] ? p - py[r] * a.W : 0;
-    }
     float acc[2][4][4];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
@@ -102,45 +103,60 @@ __global__ void __launch_bounds__(kConvTPB) k_conv3(ConvArgs a) {
         for (int j = 0; j < 4; ++j)
 #pragma unroll
             for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
+    // ldmatrix row addresses: A rows are pixels (lane&7) + 8*((lane>>3)&1), k offset 8*(lane>>4);
+    // B rows are output channels 8*(lane>>4) + (lane&7), k offset 8*((lane>>3)&1)
+    const int a_row = (lane & 7) + ((lane >> 3) & 1) * 8, a_k = (lane >> 4) * 8;
+    const int b_row = (lane >> 4) * 8 + (lane & 7), b_k = ((lane >> 3) & 1) * 8;
 
-    for (int tap = 0; tap < 9; ++tap) {
-        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-        const bf16* src[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int sy = py[r] + dy, sx = px[r] + dx;
-            const bool ok = pv[r] && sy >= 0 && sy < a.H && sx >= 0 && sx < a.W;
-            const long sp = a.up ? (long)(sy >> 1) * Wl + (sx >> 1) : (long)sy * a.W + sx;
-            src[r] = ok ? xb + sp * a.ldx + 2 * t : nullptr;
-        }
-        const bf16* wt = a.w + ((long)tap * a.Cout + co0 + g) * a.Cin + 2 * t;
-        for (int c0 = 0; c0 < a.Cin; c0 += 16) {
-            uint32_t af[2][4];
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt) {
-                const bf16* s0 = src[mt * 2];
-                const bf16* s1 = src[mt * 2 + 1];
-                af[mt][0] = ld_pair(s0 ? s0 + c0 : nullptr);
-                af[mt][1] = ld_pair(s1 ? s1 + c0 : nullptr);
-                af[mt][2] = ld_pair(s0 ? s0 + c0 + 8 : nullptr);
-                af[mt][3] = ld_pair(s1 ? s1 + c0 + 8 : nullptr);
+    for (int c0 = 0; c0 < a.Cin; c0 += kc) {
+        for (int i = threadIdx.x; i < kHaloPix * parts; i += kConvTPB) {
+            const int pix = i / parts, part = i - pix * parts;
+            const int ty = pix / (kTW + 2), tx = pix - ty * (kTW + 2);
+            const int gy = y0 + ty - 1, gx = x0 + tx - 1;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) {
+                const long sp = a.up ? (long)(gy >> 1) * Wl + (gx >> 1) : (long)gy * a.W + gx;
+                v = __ldg(reinterpret_cast<const uint4*>(xb + sp * a.ldx + c0 + part * 8));
             }
+            *reinterpret_cast<uint4*>(s_in + pix * ps + part * 8) = v;
+        }
+        for (int i = threadIdx.x; i < 9 * 32 * parts; i += kConvTPB) {
+            const int row = i / parts, part = i - row * parts;  // row = tap * 32 + co
+            const int tap = row >> 5, co = row & 31;
+            *reinterpret_cast<uint4*>(s_w + row * ps + part * 8) =
+                __ldg(reinterpret_cast<const uint4*>(a.w + ((long)tap * a.Cout + co0 + co) * a.Cin + c0 + part * 8));
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int tap = 0; tap < 9; ++tap) {
+            const int dy = tap / 3, dx = tap % 3;  // halo-tile offsets (0..2)
+            for (int ks = 0; ks < kc; ks += 16) {
+                uint32_t af[2][4];
 #pragma unroll
-            for (int nt = 0; nt < 4; ++nt) {
-                const bf16* wp = wt + (long)nt * 8 * a.Cin + c0;
-                const uint32_t b0 = ld_pair(wp), b1 = ld_pair(wp + 8);
-                mma_bf16(acc[0][nt], af[0], b0, b1);
-                mma_bf16(acc[1][nt], af[1], b0, b1);
+                for (int mt = 0; mt < 2; ++mt)
+                    ldsm_x4(af[mt], s_in + ((warp + dy) * (kTW + 2) + mt * 16 + a_row + dx) * ps + ks + a_k);
+#pragma unroll
+                for (int np = 0; np < 2; ++np) {
+                    uint32_t bfr[4];
+                    ldsm_x4(bfr, s_w + (tap * 32 + np * 16 + b_row) * ps + ks + b_k);
+                    mma_bf16(acc[0][2 * np], af[0], bfr[0], bfr[1]);
+                    mma_bf16(acc[1][2 * np], af[1], bfr[0], bfr[1]);
+                    mma_bf16(acc[0][2 * np + 1], af[0], bfr[2], bfr[3]);
+                    mma_bf16(acc[1][2 * np + 1], af[1], bfr[2], bfr[3]);
+                }
             }
         }
+        __syncthreads();
     }
+    const int py = y0 + warp;
+    if (py >= a.H) return;
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            const int r = mt * 2 + h;
-            if (!pv[r]) continue;
-            const long p = (long)py[r] * a.W + px[r];
+            const int px = x0 + mt * 16 + g + 8 * h;
+            if (px >= a.W) continue;
+            const long p = (long)py * a.W + px;
 #pragma unroll
             for (int nt = 0; nt < 4; ++nt) {
                 const int co = co0 + nt * 8 + 2 * t;
@@ -163,9 +179,14 @@ __global__ void __launch_bounds__(kConvTPB) k_conv3(ConvArgs a) {
 
 // ------------------------------------------------------------------------------------------
 // Weight gradient: dW[tap][co][ci] += sum over pixels of G[p][co] * X[p + off(tap)][ci], an MMA
-// with M = output channels, N = input channels, K = pixels (flattened over the batch).  A block
-// takes one tap, a 32 x ci_tile weight tile and kWgPix pixels; its 4 warps split the pixels,
-// then sum through shared memory and add to dW with one atomic per weight.
+// with M = output channels, N = input channels, K = pixels.  A block owns one 32 x ci_tile
+// weight tile for all 9 taps (warp w = tap w) and walks kWgTiles pixel tiles of kTH x kTW:
+// per tile it stages G (the tile) and X (the tile with its halo) in shared memory, and every
+// warp reads its fragments with ldmatrix.trans (both operands are pixel-major there).  The
+// block's sums go to dW with one atomic per weight and tap.
+constexpr int kWgTiles = 8;
+constexpr int kWgThreads = 9 * 32;
+
 struct WgArgs {
     const bf16* x; long xbs; int ldx;
     const bf16* g; long gbs; int ldg;
@@ -173,18 +194,31 @@ struct WgArgs {
     int H, W, Cin, Cout, up, ci_tile, batch;
 };
 
-__global__ void __launch_bounds__(128) k_wgrad(WgArgs a) {
-    __shared__ float red[4][32][33];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const bf16* p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
+__global__ void __launch_bounds__(kWgThreads) k_wgrad(WgArgs a) {
+    constexpr int PS = 32 + 8;  // padded pixel row (32 channels max per tile)
+    __shared__ __align__(16) bf16 s_g[kTH * kTW * PS];
+    __shared__ __align__(16) bf16 s_x[kHaloPix * PS];
+    const int tap = threadIdx.x >> 5, lane = threadIdx.x & 31, t = lane & 3, g = lane >> 2;
     const int nco = a.Cout / 32;
-    int tile = blockIdx.y;
-    const int tap = tile % 9;
-    tile /= 9;
-    const int co0 = (tile % nco) * 32, ci0 = (tile / nco) * a.ci_tile;
-    const int nnt = a.ci_tile / 8;
-    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-    const int HW = a.H * a.W, Wl = a.W >> 1;
-    const long total = (long)a.batch * HW;
+    const int co0 = (blockIdx.y % nco) * 32, ci0 = (blockIdx.y / nco) * a.ci_tile;
+    const int nnt = a.ci_tile / 8;       // 2 or 4 n-tiles
+    const int xparts = a.ci_tile / 8;    // 16-byte pieces of an X row
+    const int dy = tap / 3, dx = tap % 3;
+    const int tx_n = (a.W + kTW - 1) / kTW, ty_n = (a.H + kTH - 1) / kTH;
+    const long ntiles = (long)a.batch * tx_n * ty_n;
+    const int Wl = a.W >> 1;
+    // ldmatrix.trans row addresses: rows are pixels.  A (G^T): matrices (k 0-7, m 0-7),
+    // (k 0-7, m 8-15), (k 8-15, m 0-7), (k 8-15, m 8-15); B (X): (k 0-7, n 0-7), (k 8-15, n 0-7),
+    // (k 0-7, n 8-15), (k 8-15, n 8-15)
+    const int ar = (lane & 7) + (lane >> 4) * 8, am = ((lane >> 3) & 1) * 8;
+    const int br = (lane & 7) + ((lane >> 3) & 1) * 8, bn = (lane >> 4) * 8;
     float acc[2][4][4];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
@@ -193,60 +227,64 @@ __global__ void __launch_bounds__(128) k_wgrad(WgArgs a) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
 
-    for (int ks = warp; ks < kWgPix / 16; ks += 4) {
-        const long q0 = (long)blockIdx.x * kWgPix + ks * 16;
-        if (q0 >= total) break;
-        const bf16* gp[4];
-        const bf16* xp[4];
+    for (int it = 0; it < kWgTiles; ++it) {
+        const long tile = (long)blockIdx.x * kWgTiles + it;
+        if (tile >= ntiles) break;  // uniform over the block
+        const int b = (int)(tile / ((long)tx_n * ty_n));
+        const int rem = (int)(tile - (long)b * tx_n * ty_n);
+        const int y0 = (rem / tx_n) * kTH, x0 = (rem % tx_n) * kTW;
+        for (int i = threadIdx.x; i < kTH * kTW * 4; i += kWgThreads) {
+            const int pix = i >> 2, part = i & 3;
+            const int gy = y0 + pix / kTW, gx = x0 + pix % kTW;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (gy < a.H && gx < a.W)
+                v = __ldg(reinterpret_cast<const uint4*>(a.g + (long)b * a.gbs + ((long)gy * a.W + gx) * a.ldg + co0 +
+                                                         part * 8));
+            *reinterpret_cast<uint4*>(s_g + pix * PS + part * 8) = v;
+        }
+        for (int i = threadIdx.x; i < kHaloPix * xparts; i += kWgThreads) {
+            const int pix = i / xparts, part = i - pix * xparts;
+            const int gy = y0 + pix / (kTW + 2) - 1, gx = x0 + pix % (kTW + 2) - 1;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) {
+                const long sp = a.up ? (long)(gy >> 1) * Wl + (gx >> 1) : (long)gy * a.W + gx;
+                v = __ldg(reinterpret_cast<const uint4*>(a.x + (long)b * a.xbs + sp * a.ldx + ci0 + part * 8));
+            }
+            *reinterpret_cast<uint4*>(s_x + pix * PS + part * 8) = v;
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int ks = 0; ks < kTH * 2; ++ks) {  // 16 pixels: half a tile row
+            const int ry = ks >> 1, cx = (ks & 1) * 16;
+            uint32_t af[2][4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const long q = q0 + 2 * t + (j & 1) + (j >> 1) * 8;
-            gp[j] = nullptr;
-            xp[j] = nullptr;
-            if (q < total) {
-                const int b = (int)(q / HW);
-                const int p = (int)(q - (long)b * HW);
-                gp[j] = a.g + (long)b * a.gbs + (long)p * a.ldg + co0 + g;
-                const int y = p / a.W, x = p - y * a.W;
-                const int sy = y + dy, sx = x + dx;
-                if (sy >= 0 && sy < a.H && sx >= 0 && sx < a.W) {
-                    const long sp = a.up ? (long)(sy >> 1) * Wl + (sx >> 1) : (long)sy * a.W + sx;
-                    xp[j] = a.x + (long)b * a.xbs + sp * a.ldx + ci0 + g;
-                }
+            for (int mt = 0; mt < 2; ++mt) ldsm_x4_t(af[mt], s_g + (ry * kTW + cx + ar) * PS + mt * 16 + am);
+            const bf16* xrow = s_x + ((ry + dy) * (kTW + 2) + cx + dx + br) * PS + bn;
+#pragma unroll
+            for (int np = 0; np < 2; ++np) {
+                if (2 * np >= nnt) break;
+                uint32_t bfr[4];
+                ldsm_x4_t(bfr, xrow + np * 16);
+                mma_bf16(acc[0][2 * np], af[0], bfr[0], bfr[1]);
+                mma_bf16(acc[1][2 * np], af[1], bfr[0], bfr[1]);
+                mma_bf16(acc[0][2 * np + 1], af[0], bfr[2], bfr[3]);
+                mma_bf16(acc[1][2 * np + 1], af[1], bfr[2], bfr[3]);
             }
         }
-        uint32_t af[2][4];
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-            const int o = mt * 16;
-            af[mt][0] = pack2(gp[0] ? gp[0] + o : nullptr, gp[1] ? gp[1] + o : nullptr);
-            af[mt][1] = pack2(gp[0] ? gp[0] + o + 8 : nullptr, gp[1] ? gp[1] + o + 8 : nullptr);
-            af[mt][2] = pack2(gp[2] ? gp[2] + o : nullptr, gp[3] ? gp[3] + o : nullptr);
-            af[mt][3] = pack2(gp[2] ? gp[2] + o + 8 : nullptr, gp[3] ? gp[3] + o + 8 : nullptr);
-        }
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-            if (nt >= nnt) break;
-            const int o = nt * 8;
-            const uint32_t b0 = pack2(xp[0] ? xp[0] + o : nullptr, xp[1] ? xp[1] + o : nullptr);
-            const uint32_t b1 = pack2(xp[2] ? xp[2] + o : nullptr, xp[3] ? xp[3] + o : nullptr);
-            mma_bf16(acc[0][nt], af[0], b0, b1);
-            mma_bf16(acc[1][nt], af[1], b0, b1);
-        }
+        __syncthreads();
     }
+    float* dwt = a.dw + (long)tap * a.Cout * a.Cin;
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-        for (int nt = 0; nt < 4; ++nt)
+        for (int nt = 0; nt < 4; ++nt) {
+            if (nt >= nnt) break;
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
-                red[warp][mt * 16 + g + (k >> 1) * 8][nt * 8 + 2 * t + (k & 1)] = acc[mt][nt][k];
-    __syncthreads();
-    for (int i = threadIdx.x; i < 32 * a.ci_tile; i += 128) {
-        const int r = i / a.ci_tile, c = i - r * a.ci_tile;
-        const float v = red[0][r][c] + red[1][r][c] + red[2][r][c] + red[3][r][c];
-        atomicAdd(a.dw + ((long)tap * a.Cout + co0 + r) * a.Cin + ci0 + c, v);
-    }
+            for (int k = 0; k < 4; ++k) {
+                const int co = co0 + mt * 16 + g + (k >> 1) * 8, ci = ci0 + nt * 8 + 2 * t + (k & 1);
+                atomicAdd(dwt + (long)co * a.Cin + ci, acc[mt][nt][k]);
+            }
+        }
 }
 
 // bias gradient: db[c] += sum over pixels of G[p][c].  A block sums 256 pixels; its threads
@@ -511,7 +549,7 @@ void conv(drd_unet* n, int li, const bf16* x, int ldx, long xbs, bf16* y, int ld
     a.y = y; a.yf = nullptr; a.ybs = ybs; a.ldy = ldy;
     a.mask = nullptr; a.mbs = 0; a.ldm = 0;
     a.H = n->Hl(Ly.level); a.W = n->Wl(Ly.level); a.Cin = Ly.cin; a.Cout = Ly.cout; a.up = Ly.up; a.relu = 1;
-    dim3 grid((a.H * a.W + kConvTPB - 1) / kConvTPB, a.Cout / 32, batch);
+    dim3 grid((a.W + kTW - 1) / kTW, (a.H + kTH - 1) / kTH, batch * (a.Cout / 32));
     k_conv3<<<grid, kConvTPB, 0, n->s>>>(a);
 }
 
@@ -526,7 +564,7 @@ void dgrad(drd_unet* n, int li, const bf16* G, int batch, bf16* out_b, float* ou
     a.y = out_b; a.yf = out_f; a.ybs = obs; a.ldy = ldo;
     a.mask = mask; a.mbs = mbs; a.ldm = ldm;
     a.H = H; a.W = W; a.Cin = Ly.cout; a.Cout = Ly.cin; a.up = 0; a.relu = 0;
-    dim3 grid((H * W + kConvTPB - 1) / kConvTPB, a.Cout / 32, batch);
+    dim3 grid((W + kTW - 1) / kTW, (H + kTH - 1) / kTH, batch * (a.Cout / 32));
     k_conv3<<<grid, kConvTPB, 0, n->s>>>(a);
 }
 
@@ -540,8 +578,9 @@ void wgrad(drd_unet* n, int li, const bf16* x, int ldx, long xbs, const bf16* G,
     a.H = H; a.W = W; a.Cin = Ly.cin; a.Cout = Ly.cout; a.up = Ly.up; a.batch = batch;
     a.ci_tile = Ly.cin < 32 ? Ly.cin : 32;
     const long total = (long)batch * H * W;
-    dim3 grid((unsigned)((total + kWgPix - 1) / kWgPix), 9 * (Ly.cout / 32) * (Ly.cin / a.ci_tile));
-    k_wgrad<<<grid, 128, 0, n->s>>>(a);
+    const long ntiles = (long)batch * ((H + kTH - 1) / kTH) * ((W + kTW - 1) / kTW);
+    dim3 grid((unsigned)((ntiles + kWgTiles - 1) / kWgTiles), (Ly.cout / 32) * (Ly.cin / a.ci_tile));
+    k_wgrad<<<grid, kWgThreads, 0, n->s>>>(a);
     k_colsum<<<(unsigned)((total + 255) / 256), 256, 0, n->s>>>(G, a.gbs, Ly.cout, H * W, batch, Ly.cout,
                                                                  n->G32 + Ly.b_off);
 }
