@@ -79,3 +79,17 @@ def test_bad_arguments_are_rejected_without_a_gpu():
     assert lib.drd_particle_initialize(C.byref(pp), 1.75, 0.42, pts) == 0
     assert list(pts) == [x for row in abi.particle_chain(pp, 1.75, 0.42) for x in row]
     assert lib.drd_particles_set(None, C.byref(pp), pts, pts) == abi.DRD_ERR_BADARG
+
+
+def test_unet_bad_arguments_are_rejected_without_a_gpu():
+    """drd_unet_create validates its arguments before any CUDA call; null handles are rejected."""
+    lib = _lib.load()
+    h = C.c_void_p()
+    for H, W, cin, cout, mb in ((4, 64, 3, 1, 1), (64, 7, 3, 1, 1), (64, 64, 0, 1, 1), (64, 64, 17, 1, 1),
+                                (64, 64, 3, 0, 1), (64, 64, 3, 5, 1), (64, 64, 3, 1, 0)):
+        assert lib.drd_unet_create(H, W, cin, cout, mb, 0, C.byref(h)) == abi.DRD_ERR_BADARG
+    assert lib.drd_unet_create(64, 64, 3, 1, 1, 0, None) == abi.DRD_ERR_BADARG
+    assert lib.drd_unet_param_count(None) == -1
+    assert lib.drd_unet_forward(None, 1, None, None) == abi.DRD_ERR_BADARG
+    assert lib.drd_unet_train_step(None, 1, None, None, C.c_float(1e-3), None) == abi.DRD_ERR_BADARG
+    assert lib.drd_unet_destroy(None) == 0
