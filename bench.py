@@ -138,6 +138,20 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------------------ CPU baseline
+def cpu_model():
+    """The host CPU's model name (lscpu), or the machine type when lscpu has none."""
+    import platform
+
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.machine()
+
+
 def cpu_baseline(steps, budget_s=40.0, nr=420, nz=180):
     """The FP64 CPU restatement (OpenMP over transform lines) on the host cores, on a bounded
     sample of the same workload: the first `steps` steps or as many as fit in budget_s."""
@@ -157,7 +171,7 @@ def cpu_baseline(steps, budget_s=40.0, nr=420, nz=180):
         if elapsed > budget_s:
             break
     cores = os.cpu_count()
-    return {"value": done / elapsed, "unit": "time-steps/s", "cores": cores, "kind": "port",
+    return {"value": done / elapsed, "unit": "time-steps/s", "cores": cores, "kind": "port", "cpu_model": cpu_model(),
             "sample": f"first {done} steps of the same {nr}x{nz} workload, FP64 oracle (oracle/drd_oracle.c, "
                       f"OpenMP over transform lines, {cores} threads), {elapsed:.1f} s"}
 
@@ -197,7 +211,7 @@ def run_reference(args, ws, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "reference_code": "FP64 CPU restatement of the reference routines "
                                                             "(Fortran reference not buildable: no Fortran compiler)"},
-        "cpu_baseline": {"value": v, "unit": "time-steps/s", "cores": cores, "kind": "port",
+        "cpu_baseline": {"value": v, "unit": "time-steps/s", "cores": cores, "kind": "port", "cpu_model": cpu_model(),
                          "sample": f"{timed} timed steps after {w} warm-up, OpenMP over transform lines, {cores} threads"},
         "e2e": {"value": v, "unit": "time-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -257,7 +271,7 @@ def cpu_c3_sample(seed, n=4, budget_s=20.0):
         done += 1
         if elapsed > budget_s:
             break
-    return {"value": done / elapsed, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+    return {"value": done / elapsed, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port", "cpu_model": cpu_model(),
             "sample": f"first {done} solves of the same C3 batch, FP64 oracle, {elapsed:.1f} s"}
 
 
