@@ -821,6 +821,100 @@ __global__ void k_uv_mv(OpScal<T> o, const T* __restrict__ rho, const T* __restr
     if (dot1 != nullptr || self2) emit_partials<DRD_TPB>(a1, a2, dot1 != nullptr, self2, d, slot1);
 }
 
+// The FP32 momentum operator, tiled: a block stages the unknowns (with MatrixVector_uv_2_CG's
+// ghost values, :533-553) and the cell coefficients eta, rho and pen for a tile of
+// kUvTI x kUvTK cells plus a one-cell halo in shared memory, then evaluates the u and v rows
+// of the tile branch-free with the expressions of uv_apply<float>.  Same arguments and
+// partial sums as k_uv_mv; blocks walk the tiles with a grid stride.
+constexpr int kUvTI = 64, kUvTK = 8;
+constexpr int kUvSI = kUvTI + 2, kUvSK = kUvTK + 2;
+
+__global__ void __launch_bounds__(DRD_TPB) k_uv_mv_tile(OpScal<float> o, const float* __restrict__ rho,
+                                                        const float* __restrict__ eta, const float* __restrict__ pen,
+                                                        const float* __restrict__ x, float alpha, float beta, float* y,
+                                                        const float* dot1, int self2, Dots d, int slot1,
+                                                        const KState* ks, int gate, ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, gate)) return;
+    __shared__ float sU[kUvSK][kUvSI], sV[kUvSK][kUvSI], sE[kUvSK][kUvSI], sR[kUvSK][kUvSI], sP[kUvSK][kUvSI];
+    const int nr = o.nr, nz = o.nz;
+    const long mn = (long)(nr + 1) * nz;
+    const int nti = (nr + 1 + kUvTI - 1) / kUvTI, ntk = (nz + kUvTK - 1) / kUvTK;
+    const float h = 0.5f, q4 = 0.25f;
+    const float mcoef = (o.bdf == 2) ? 1.5f * o.re : o.re;
+    const float refl = o.lr_neumann ? 1.f : -1.f;
+    double a1 = 0.0, a2 = 0.0;
+    for (int tile = blockIdx.x; tile < nti * ntk; tile += gridDim.x) {
+        const int i0 = (tile % nti) * kUvTI, k0 = (tile / nti) * kUvTK;
+        __syncthreads();  // the previous tile's reads are done
+        for (int e = threadIdx.x; e < kUvSI * kUvSK; e += DRD_TPB) {
+            const int li = e % kUvSI, lk = e / kUvSI;
+            const int i = i0 - 1 + li, k = k0 - 1 + lk;
+            // U(i, k): k reflected with a sign change, then i by the side rule (UVFetch)
+            const int kc = k < 0 ? 0 : (k > nz - 1 ? nz - 1 : k);
+            const float ks_ = (k < 0 || k > nz - 1) ? -1.f : 1.f;
+            float u;
+            if (i < 0) u = refl * x[1 + (long)(nr + 1) * kc];
+            else if (i > nr) u = refl * x[(nr - 1) + (long)(nr + 1) * kc];
+            else u = x[i + (long)(nr + 1) * kc];
+            sU[lk][li] = ks_ * u;
+            const int ic = i < 0 ? 0 : (i > nr - 1 ? nr - 1 : i);
+            sV[lk][li] = (k <= 0 || k >= nz) ? 0.f : x[mn + ic + (long)nr * (k - 1)];
+            const bool cell = i >= -1 && i <= nr && k >= -1 && k <= nz;
+            const long c = cidx(nr, i, k);
+            sE[lk][li] = cell ? eta[c] : 0.f;
+            sR[lk][li] = cell ? rho[c] : 0.f;
+            sP[lk][li] = cell ? pen[c] : 0.f;
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < kUvTI * kUvTK; r += DRD_TPB) {
+            const int li = r % kUvTI + 1, lk = r / kUvTI + 1;  // staged coordinates of (i, k)
+            const int i = i0 + li - 1, k = k0 + lk - 1;
+#define E_(di, dk) sE[lk + (dk)][li + (di)]
+            if (i <= nr && k <= nz - 1) {  // u row
+                const long q = i + (long)(nr + 1) * k;
+                const float f1 = sU[lk][li];
+                float val;
+                if (o.bdf == 2)
+                    val = f1 * mcoef * (sR[lk][li] + sR[lk][li - 1]) * h + f1 * o.pk * (sP[lk][li] + sP[lk][li - 1]) * h * o.dt;
+                else
+                    val = f1 * mcoef * (sR[lk][li] + sR[lk][li - 1]) * h;
+                float cr = E_(0, 0), cl = E_(-1, 0);
+                val = val - 2.f * o.dt * (cr * (sU[lk][li + 1] - f1) + cl * (sU[lk][li - 1] - f1)) * o.idr2;
+                cr = (E_(0, 1) + E_(-1, 1) + E_(0, 0) + E_(-1, 0)) * q4;
+                cl = (E_(0, 0) + E_(-1, 0) + E_(0, -1) + E_(-1, -1)) * q4;
+                val = val - o.dt * (cr * (sU[lk + 1][li] - f1) + cl * (sU[lk - 1][li] - f1)) * o.idz2;
+                val = val - o.dt * (cr * (sV[lk + 1][li] - sV[lk + 1][li - 1]) - cl * (sV[lk][li] - sV[lk][li - 1])) * o.idrdz;
+                const float yn = (beta == 0.f) ? alpha * val : alpha * val + beta * y[q];
+                y[q] = yn;
+                if (dot1) a1 += (double)dot1[q] * (double)yn;
+                if (self2) a2 += (double)yn * (double)yn;
+            }
+            if (i <= nr - 1 && k >= 1 && k <= nz - 1) {  // v row
+                const long q = mn + i + (long)nr * (k - 1);
+                const float f2 = sV[lk][li];
+                float val;
+                if (o.bdf == 2)
+                    val = f2 * mcoef * (sR[lk][li] + sR[lk - 1][li]) * h + f2 * o.pk * (sP[lk][li] + sP[lk - 1][li]) * h * o.dt;
+                else
+                    val = f2 * mcoef * (sR[lk][li] + sR[lk - 1][li]) * h;
+                float cr = E_(0, 0), cl = E_(0, -1);
+                val = val - 2.f * o.dt * (cr * (sV[lk + 1][li] - f2) + cl * (sV[lk - 1][li] - f2)) * o.idz2;
+                cr = (E_(1, 0) + E_(0, 0) + E_(1, -1) + E_(0, -1)) * q4;
+                cl = (E_(0, 0) + E_(-1, 0) + E_(0, -1) + E_(-1, -1)) * q4;
+                val = val - o.dt * (cr * (sV[lk][li + 1] - f2) + cl * (sV[lk][li - 1] - f2)) * o.idr2;
+                val = val - o.dt * (cr * (sU[lk][li + 1] - sU[lk - 1][li + 1]) - cl * (sU[lk][li] - sU[lk - 1][li])) * o.idrdz;
+                const float yn = (beta == 0.f) ? alpha * val : alpha * val + beta * y[q];
+                y[q] = yn;
+                if (dot1) a1 += (double)dot1[q] * (double)yn;
+                if (self2) a2 += (double)yn * (double)yn;
+            }
+#undef E_
+        }
+    }
+    if (dot1 != nullptr || self2) emit_partials<DRD_TPB>(a1, a2, dot1 != nullptr, self2, d, slot1);
+}
+
 // Jacobi diagonal of PSolve_uv_2_CG (:662-709) / PSolve_uv_CG, including rho(i-1,j) in the
 // v block as written at :690.
 template <typename T>
@@ -3075,8 +3169,14 @@ void launch_uv_matvec(const OpScal<T>& o, const T* rho, const T* eta, const T* p
                       const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,
                       cudaStream_t s) {
     const long N = (long)(o.nr + 1) * o.nz + (long)o.nr * (o.nz - 1);
-    const int g = (dot1 || self2) ? d.G : grid_for(N);
-    k_uv_mv<T><<<g, DRD_TPB, 0, s>>>(o, rho, eta, pen, x, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);
+    if constexpr (sizeof(T) == 4) {
+        const long tiles = (long)((o.nr + 1 + kUvTI - 1) / kUvTI) * ((o.nz + kUvTK - 1) / kUvTK);
+        const int g = (dot1 || self2) ? d.G : (int)std::min<long>(tiles, 152L * 8);
+        k_uv_mv_tile<<<g, DRD_TPB, 0, s>>>(o, rho, eta, pen, x, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);
+    } else {
+        const int g = (dot1 || self2) ? d.G : grid_for(N);
+        k_uv_mv<T><<<g, DRD_TPB, 0, s>>>(o, rho, eta, pen, x, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);
+    }
 }
 template <typename T>
 void launch_uv_diag(const OpScal<T>& o, const T* rho, const T* eta, T* diag, ull* ctr, cudaStream_t s) {
