@@ -826,7 +826,7 @@ __global__ void k_uv_mv(OpScal<T> o, const T* __restrict__ rho, const T* __restr
 // kUvTI x kUvTK cells plus a one-cell halo in shared memory, then evaluates the u and v rows
 // of the tile branch-free with the expressions of uv_apply<float>.  Same arguments and
 // partial sums as k_uv_mv; blocks walk the tiles with a grid stride.
-constexpr int kUvTI = 64, kUvTK = 8;
+constexpr int kUvTI = 64, kUvTK = 16;
 constexpr int kUvSI = kUvTI + 2, kUvSK = kUvTK + 2;
 
 __global__ void __launch_bounds__(DRD_TPB) k_uv_mv_tile(OpScal<float> o, const float* __restrict__ rho,
@@ -847,6 +847,20 @@ __global__ void __launch_bounds__(DRD_TPB) k_uv_mv_tile(OpScal<float> o, const f
     for (int tile = blockIdx.x; tile < nti * ntk; tile += gridDim.x) {
         const int i0 = (tile % nti) * kUvTI, k0 = (tile / nti) * kUvTK;
         __syncthreads();  // the previous tile's reads are done
+        // a tile whose halo lies inside the unknowns' and the cells' ranges needs no ghost rules
+        const bool interior = i0 >= 1 && i0 + kUvTI <= nr - 1 && k0 >= 2 && k0 + kUvTK <= nz - 1;
+        if (interior) {
+            for (int e = threadIdx.x; e < kUvSI * kUvSK; e += DRD_TPB) {
+                const int li = e % kUvSI, lk = e / kUvSI;
+                const int i = i0 - 1 + li, k = k0 - 1 + lk;
+                sU[lk][li] = x[i + (long)(nr + 1) * k];
+                sV[lk][li] = x[mn + i + (long)nr * (k - 1)];
+                const long c = cidx(nr, i, k);
+                sE[lk][li] = eta[c];
+                sR[lk][li] = rho[c];
+                sP[lk][li] = pen[c];
+            }
+        } else
         for (int e = threadIdx.x; e < kUvSI * kUvSK; e += DRD_TPB) {
             const int li = e % kUvSI, lk = e / kUvSI;
             const int i = i0 - 1 + li, k = k0 - 1 + lk;
