@@ -826,14 +826,16 @@ __global__ void k_uv_mv(OpScal<T> o, const T* __restrict__ rho, const T* __restr
 // kUvTI x kUvTK cells plus a one-cell halo in shared memory, then evaluates the u and v rows
 // of the tile branch-free with the expressions of uv_apply<float>.  Same arguments and
 // partial sums as k_uv_mv; blocks walk the tiles with a grid stride.
-constexpr int kUvTI = 64, kUvTK = 16;
-constexpr int kUvSI = kUvTI + 2, kUvSK = kUvTK + 2;
+constexpr int kUvTI = 64;
+constexpr int kUvSI = kUvTI + 2;
 
+template <int kUvTK>
 __global__ void __launch_bounds__(DRD_TPB) k_uv_mv_tile(OpScal<float> o, const float* __restrict__ rho,
                                                         const float* __restrict__ eta, const float* __restrict__ pen,
                                                         const float* __restrict__ x, float alpha, float beta, float* y,
                                                         const float* dot1, int self2, Dots d, int slot1,
                                                         const KState* ks, int gate, ull* ctr) {
+    constexpr int kUvSK = kUvTK + 2;
     count_launch(ctr);
     if (gate_closed(ks, gate)) return;
     __shared__ float sU[kUvSK][kUvSI], sV[kUvSK][kUvSI], sE[kUvSK][kUvSI], sR[kUvSK][kUvSI], sP[kUvSK][kUvSI];
@@ -3184,9 +3186,15 @@ void launch_uv_matvec(const OpScal<T>& o, const T* rho, const T* eta, const T* p
                       cudaStream_t s) {
     const long N = (long)(o.nr + 1) * o.nz + (long)o.nr * (o.nz - 1);
     if constexpr (sizeof(T) == 4) {
-        const long tiles = (long)((o.nr + 1 + kUvTI - 1) / kUvTI) * ((o.nz + kUvTK - 1) / kUvTK);
+        // 16-deep tiles when they give every SM at least 4 tiles, else 8-deep ones
+        const long nti = (o.nr + 1 + kUvTI - 1) / kUvTI;
+        const bool deep = nti * ((o.nz + 15) / 16) >= 4L * 152;
+        const long tiles = deep ? nti * ((o.nz + 15) / 16) : nti * ((o.nz + 7) / 8);
         const int g = (dot1 || self2) ? d.G : (int)std::min<long>(tiles, 152L * 8);
-        k_uv_mv_tile<<<g, DRD_TPB, 0, s>>>(o, rho, eta, pen, x, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);
+        if (deep)
+            k_uv_mv_tile<16><<<g, DRD_TPB, 0, s>>>(o, rho, eta, pen, x, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);
+        else
+            k_uv_mv_tile<8><<<g, DRD_TPB, 0, s>>>(o, rho, eta, pen, x, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);
     } else {
         const int g = (dot1 || self2) ? d.G : grid_for(N);
         k_uv_mv<T><<<g, DRD_TPB, 0, s>>>(o, rho, eta, pen, x, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);
