@@ -64,3 +64,25 @@ def test_backward_matches_finite_differences(H, W):
         fd = (o.loss(p + eps * v, x, t) - o.loss(p - eps * v, x, t)) / (2 * eps)
         an = float(g @ v)
         assert abs(fd - an) <= 1e-4 * max(abs(an), 1e-3), (li, fd, an)
+
+
+def test_harness_layer_table_and_flops_match_the_oracle():
+    """learned.py's FLOP model walks the same 17 layers as the oracle (and drd_unet_create)."""
+    from drd_application_gb300 import learned
+
+    assert learned._layers() == [(ci, co, lev) for ci, co, lev, _ in layer_table()]
+    # one forward pass on an 8 x 16 padded grid: 2 * 9 * cin * cout * pixels of the layer's level
+    want = sum(2.0 * 9 * ci * co * (8 >> lev) * (16 >> lev) for ci, co, lev, _ in layer_table())
+    assert learned.conv_flops(8, 16, 1, train=False) == want
+    # training adds a data gradient (not for the first layer) and a weight gradient
+    first = 2.0 * 9 * 16 * 32 * 8 * 16
+    assert learned.conv_flops(8, 16, 1) == 3 * want - first
+
+
+def test_cubic_guess_is_exact_for_cubics():
+    from drd_application_gb300.learned import cubic_guess
+
+    t = np.arange(4.0)
+    hist = [np.array([1.0 + 2 * s - 0.5 * s ** 2 + 0.25 * s ** 3]) for s in t]
+    s = 4.0
+    assert np.allclose(cubic_guess(hist), 1.0 + 2 * s - 0.5 * s ** 2 + 0.25 * s ** 3)
