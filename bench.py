@@ -338,6 +338,11 @@ def time_learned(steps, nr, nz, train_seeds=8, per_seed=12):
         "held_out_error_ratio": float(rel.mean()),
         "iters_plain": float(ev["none"]["iters_plain"].mean()),
         "iters_learned": float(ev["none"]["iters_learned"].mean()),
+        # wall time per solve through drd_solve with host arrays, and of building the learned
+        # guess (residual, network, update) before it
+        "solve_ms_plain": 1e3 * float(ev["none"]["t_plain"].mean()),
+        "solve_ms_learned": 1e3 * float(ev["none"]["t_learned"].mean()),
+        "guess_ms": 1e3 * float(ev["none"]["t_guess"].mean()),
         "iters_learned_residual_judge": float(ev["residual"]["iters_learned"].mean()),
         "learned_taken_residual_judge": f"{int(ev['residual']['used'].sum())}/{ev['residual']['used'].size}",
         "max_true_resid": float(max(ev["none"]["true_resid_learned"].max(), ev["none"]["true_resid_plain"].max())),
