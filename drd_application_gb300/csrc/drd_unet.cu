@@ -1,7 +1,8 @@
 // drd_unet.cu — the learned initial guess of the Krylov solves: a 4-level U-Net (32 base
 // channels, 3x3 convolutions, BF16 weights and activations, FP32 accumulation) with its
-// forward pass, backward pass and Adam update, all as hand-written kernels on the BF16 tensor
-// cores (mma.sync m16n8k16, FP32 accumulators).
+// forward pass, backward pass and Adam update, all as hand-written kernels.  The convolutions
+// and weight gradients run on the BF16 tensor cores (mma.sync m16n8k16 with FP32 accumulators)
+// from ldmatrix fragments of pixel tiles staged in shared memory with their halo.
 //
 // The network maps (normalised residual, resistance, phase field) on the solver's grid to a
 // normalised correction of the solve's initial guess; the caller scales it back and the
