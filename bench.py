@@ -182,7 +182,6 @@ def run_reference(args, ws, rank):
     from oracle import oracle
 
     oracle.build()
-    w = min(args.warmup, 1)
     from drd_application_gb300.workloads import make_case
     from oracle.oracle import Oracle
 
@@ -190,9 +189,12 @@ def run_reference(args, ws, rank):
     orc = Oracle(case.params, openmp=True)
     st = case.copy_state()
     t = 0.0
-    for s in range(w):
-        orc.step(st, case.coefs, s == 0, t)
+    # the requested warm-up steps, bounded to 60 s of host time; w is the number done
+    w, t_w = 0, time.perf_counter()
+    while w < args.warmup and time.perf_counter() - t_w < 60.0:
+        orc.step(st, case.coefs, w == 0, t)
         t += case.params.dt
+        w += 1
     timed, elapsed = 0, 0.0
     budget = 150.0
     for s in range(args.steps):
