@@ -401,9 +401,14 @@ def time_e2e(ctx, case, warmup, steps, flush_bytes):
     nb_v = st[F.F_V].nbytes
     h2d = (nb_u + nb_v + 2 * nb_cell) + (5 * nb_cell + 2 * nb_u + 2 * nb_v) + (nb_u + nb_v)
     d2h = (2 * nb_cell) + (nb_u + nb_v + 2 * 8 * (P.nz + 1)) + nb_cell
+    if P.two_fluid:  # interpolate_coef's two-fluid rho, eta from ph each step: ph in, rho and eta out
+        h2d += nb_cell
+        d2h += 2 * nb_cell
 
     def one(first, t):
         rmu_after, ph_after, s1 = ctx.PhSolve(st[F.F_U], st[F.F_V], st[F.F_PH], st[F.F_RMU], t + P.dt)
+        if P.two_fluid:
+            ctx.two_phase_coef(None, st[F.F_PH])
         if first:
             u_after, v_after, _, _, s2 = ctx.VeloSolve_combined(None, st[F.F_U], st[F.F_V], st[F.F_P], rmu_after,
                                                                 ph_after, t + P.dt)

@@ -24,6 +24,7 @@ SIGNATURES = {
     "drd_set_coefs": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, _dp]),
     "drd_set_tp_fields": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
     "drd_interpolate_coef": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
+    "drd_two_phase_coef": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
     "drd_phsolve_ori": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp, _st]),
     "drd_finit_wall": (C.c_int, [_ctx, _dp, C.c_int, _dp, _dp, _dp]),
     "drd_particle_params_default": (C.c_int, [C.POINTER(abi.drd_particle_params), C.c_double, C.c_double]),

@@ -65,6 +65,7 @@ class drd_params(C.Structure):
         ("angle", C.c_double), ("xlsB", C.c_double), ("penalty_k", C.c_double),
         ("lambda_rho", C.c_double), ("lambda_eta", C.c_double), ("bdr_ph_used_adjust", C.c_double),
         ("mixed_inner_tol", C.c_double), ("mixed_max_refine", C.c_int32), ("uv_precond", C.c_int32),
+        ("two_fluid", C.c_int32), ("reserved1", C.c_int32),
     ]
 
     def copy(self):

@@ -88,11 +88,25 @@ class DRDContext:
                  "drd_set_tp_fields", False)
 
     def set_case(self, case):
-        """Load the coefficient fields of a workloads.Case."""
+        """Load the coefficient fields of a workloads.Case (with two_fluid, also its indicator
+        fpd_ph, which every step combines with the phase field)."""
         k = case.coefs
         self.set_coefs(k["rho"], k["eta"], k["bdr_ph"], k["bdr_ph_grad"], k["M0"], k["Mi"])
         if self.P.variant == abi.DRD_VARIANT_TP:
             self.set_tp_fields(k["bdr_used"], k["bdr_pen"])
+        if self.P.two_fluid:
+            self.two_phase_coef(k["fpd"], case.state[abi.F_PH])
+
+    def two_phase_coef(self, fpd_ph=None, ph=None):
+        """The two-fluid rho, eta of interpolate_coef (two_phase_flow_complex_domain/
+        interpolate_coef.f90:91-112, commented out there) -> (rho, eta); they also replace the
+        context's coefficients.  fpd_ph None keeps the context's indicator, ph None uses the
+        resident phase field."""
+        f = _check_shape(fpd_ph, self.cs, "fpd_ph")
+        ph = _check_shape(ph, self.cs, "ph")
+        rho, eta = np.zeros(self.cs), np.zeros(self.cs)
+        self._rc(self.L.drd_two_phase_coef(self.h, ptr(f), ptr(ph), ptr(rho), ptr(eta)), "two_phase_coef", False)
+        return rho, eta
 
     # ---- the reference subroutines --------------------------------------------------------
     def interpolate_coef(self, dist):

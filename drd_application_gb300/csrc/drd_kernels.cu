@@ -441,7 +441,7 @@ __global__ void k_tridiag(TriBlock<T> b0, TriBlock<T> b1, const KState* ks, int 
 }
 
 // Neumann ghost copies of CELL fields: the ghost takes the nearest interior value, which is
-// the net effect of the reference's two loops (e.g. PhSolve.f90:88-96, dct_fftw.f90:175-183).
+// the net effect of the reference's two loops (e.g. PhSolve.f90:88-96, dct_fftw.f90:41-51).
 __global__ void k_fill_neumann(int nr, int nz, double* a, double* b, ull* ctr) {
     count_launch(ctr);
     const long ng = 2L * (nr + 2) + 2L * nz;
@@ -1044,6 +1044,35 @@ __global__ void k_interp_coef(DevParams P, const double* __restrict__ dist, cons
         fpd[q] = f;
         rho[q] = 1.0 + (P.lambda_rho - 1.0) * f;
         eta[q] = 1.0 + (P.lambda_eta - 1.0) * f;
+    }
+}
+
+// The two-fluid form of interpolate_coef that two_phase_flow_complex_domain/
+// interpolate_coef.f90:91-112 keeps commented out: rho and eta_ph piecewise linear in ph (1 at
+// ph <= -1, the ratio at ph >= 1), eta = max(eta(fpd), eta_ph).  Products and sums are rounded
+// separately (no contraction), as the host evaluates them.  FP32 copies are written for the
+// mixed mode's operators (may be null).
+__global__ void k_two_phase_coef(DevParams P, long cs, const double* __restrict__ fpd, const double* __restrict__ ph,
+                                 double* __restrict__ rho, double* __restrict__ eta, float* __restrict__ rho32,
+                                 float* __restrict__ eta32, ull* ctr) {
+    count_launch(ctr);
+    const double lr = P.lambda_rho - 1.0, le = P.lambda_eta - 1.0;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < cs; q += (long)gridDim.x * blockDim.x) {
+        const double x = ph[q];
+        double r, e;
+        if (x <= -1.0) {
+            r = 1.0; e = 1.0;
+        } else if (x >= 1.0) {
+            r = P.lambda_rho; e = P.lambda_eta;
+        } else {
+            r = __dadd_rn(1.0, __dmul_rn(lr, x));
+            e = __dadd_rn(1.0, __dmul_rn(le, x));
+        }
+        const double es = __dadd_rn(1.0, __dmul_rn(le, fpd[q]));
+        e = fmax(es, e);
+        rho[q] = r;
+        eta[q] = e;
+        if (rho32) { rho32[q] = (float)r; eta32[q] = (float)e; }
     }
 }
 
@@ -3220,6 +3249,10 @@ void launch_cell_add(long n, const double* x, double* y, ull* ctr, cudaStream_t 
 void launch_interp_coef(const DevParams& P, const double* dist, const double* bdr, double* fpd, double* rho, double* eta,
                         ull* ctr, cudaStream_t s) {
     k_interp_coef<<<GRID((long)(P.nr + 2) * (P.nz + 2))>>>(P, dist, bdr, fpd, rho, eta, ctr);
+}
+void launch_two_phase_coef(const DevParams& P, long cs, const double* fpd, const double* ph, double* rho, double* eta,
+                           float* rho32, float* eta32, ull* ctr, cudaStream_t s) {
+    k_two_phase_coef<<<GRID(cs)>>>(P, cs, fpd, ph, rho, eta, rho32, eta32, ctr);
 }
 void launch_mass_partial(int nr, int nz, const double* ph, const Dots& d, int slot, ull* ctr, cudaStream_t s) {
     k_mass_partial<<<d.G, DRD_TPB, 0, s>>>(nr, nz, ph, d, slot, ctr);

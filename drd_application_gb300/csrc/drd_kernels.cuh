@@ -128,6 +128,8 @@ void launch_cell_add(long n, const double* x, double* y, ull* ctr, cudaStream_t 
 // ---- interpolate_coef / mass ----------------------------------------------------------
 void launch_interp_coef(const DevParams& P, const double* dist, const double* bdr, double* fpd, double* rho, double* eta,
                         ull* ctr, cudaStream_t s);
+void launch_two_phase_coef(const DevParams& P, long cs, const double* fpd, const double* ph, double* rho, double* eta,
+                           float* rho32, float* eta32, ull* ctr, cudaStream_t s);
 
 // ---- persistent cooperative BiCGSTAB (FP32 inner solves of the CH and momentum systems) ---
 struct GridBar {

@@ -116,7 +116,8 @@ __global__ void k_na_zpass(int nr, int nz, int kind, const double* in, double* o
     }
 }
 
-// Neumann ghosts of psi (dct_fftw.f90:175-183).
+// Neumann ghosts of psi (dct_fftw.f90:41-51).  The interior was already scaled by coef, the
+// reference's psi = psi*coef (PreSolve_2.f90:125), so the copies carry the scaled values.
 __global__ void k_na_ghosts(int nr, int nz, double* psi) {
     const long ng = 2L * (nr + 2) + 2L * nz;
     for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < ng; g += (long)gridDim.x * blockDim.x) {
@@ -134,7 +135,9 @@ __global__ void k_na_ghosts(int nr, int nz, double* psi) {
     }
 }
 
-// Device address of g_presolve_scratch, looked up once per device.
+// Device address of g_presolve_scratch, looked up once per device (on the first call made with
+// that device current) and kept for the life of the process.  cudaDeviceReset destroys the
+// module that holds the array, so the cached address is not valid after it.
 std::mutex g_mu;
 double* g_addr[64] = {nullptr};
 

@@ -901,6 +901,10 @@ int enq_step(drd_ctx* c, int first, int extrap, cudaStream_t s) {
     int rc = (c->P.variant == DRD_VARIANT_TP) ? enq_phmu(c, s, extrap != 0) : enq_ch(c, s, extrap);
     if (rc) return rc;
     if (c->pp.np > 0) enq_particles(c, PT_FORCE | PT_MOVE | PT_COEF, f[DRD_F_U], f[DRD_F_V], s);
+    // interpolate_coef's place in the loop (mcl6.f90:401, :254): the two-fluid coefficients
+    // from ph before the swap
+    if (c->P.two_fluid)
+        launch_two_phase_coef(c->dp, c->cs, c->fpd, f[DRD_F_PH], c->rho, c->eta, c->rho32, c->eta32, c->ctr, s);
     rc = enq_uv(c, first ? 1 : 2, s, extrap);
     if (rc) return rc;
     if (c->P.guess_mode == 3) {  // the fields three steps back, for the next step's guess
@@ -1238,6 +1242,7 @@ int validate(const drd_params* p, std::string& why) {
     if (p->xlsB >= 1.e-8) { why = "slip walls (xlsB >= 1e-8) have no solve in the reference"; return DRD_ERR_UNSUPPORTED; }
     if (p->guess_mode < 0 || p->guess_mode > 3) { why = "guess_mode must be 0 to 3"; return DRD_ERR_BADARG; }
     if (p->uv_precond != DRD_UV_JACOBI && p->uv_precond != DRD_UV_ESOLP) { why = "unknown uv_precond"; return DRD_ERR_BADARG; }
+    if (p->two_fluid != 0 && p->two_fluid != 1) { why = "two_fluid must be 0 or 1"; return DRD_ERR_BADARG; }
     if (p->precision == DRD_PREC_MIXED && (!(p->mixed_inner_tol > 0) || p->mixed_max_refine <= 0)) {
         why = "mixed precision needs mixed_inner_tol > 0 and mixed_max_refine > 0";
         return DRD_ERR_BADARG;
@@ -1396,6 +1401,21 @@ int drd_interpolate_coef(drd_ctx* c, const double* dist, double* fpd_ph, double*
     if (rc) return rc;
     rc = down(c, fpd_ph, c->fpd, c->cs) | down(c, rho, c->rho, c->cs) | down(c, eta, c->eta, c->cs);
     if (rc) return DRD_ERR_CUDA;
+    return finish_call(c, 0, nullptr, false);
+}
+
+int drd_two_phase_coef(drd_ctx* c, const double* fpd_ph, const double* ph, double* rho, double* eta) {
+    if (!c) return DRD_ERR_BADARG;
+    CK(cudaEventRecord(c->ev0, c->s));
+    if (up(c, c->fpd, fpd_ph, c->cs)) return DRD_ERR_CUDA;
+    const double* dph = c->fld[DRD_F_PH];
+    if (ph) {
+        if (up(c, c->ph_after, ph, c->cs)) return DRD_ERR_CUDA;  // scratch until the next solve
+        dph = c->ph_after;
+    }
+    launch_two_phase_coef(c->dp, c->cs, c->fpd, dph, c->rho, c->eta, c->rho32, c->eta32, c->ctr, c->s);
+    CK(cudaGetLastError());
+    if (down(c, rho, c->rho, c->cs) | down(c, eta, c->eta, c->cs)) return DRD_ERR_CUDA;
     return finish_call(c, 0, nullptr, false);
 }
 

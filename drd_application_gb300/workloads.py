@@ -16,11 +16,13 @@ Workloads:
   "c2"  420x180 serpentine channel (seeded sinusoidal walls, amplitude 30, period 140 cells,
         half-width 45 cells), resistance penalty 1e4, walls smoothed by tanh(d / 2 cells),
         3 rigid fibers of 40x4 cells at seeded poses, two drops of radius 15 cells,
-        viscosity ratio 5, Re 0.5, Ca 0.05.
+        viscosity ratio 5 between the drops and the matrix fluid (two_fluid = 1: eta =
+        max(1 + 4 fpd_ph, 1 + 4 ph), rebuilt every step from ph), Re 0.5, Ca 0.05.
   "tp"  the two_phase_flow_complex_domain variant (phi in [-1,1], ph_mu_solve, sharp penalty).
   "c5"  2048x1024 serpentine channel (amplitude 150, period 680 cells, half-width 0.35 nz),
         64 rigid fibers of 60x6 cells and 32 drops of radius U(20, 60) cells at seeded
-        positions in the channel, viscosity ratio 10, Re 1, Ca 0.02, dr = dz = 1/512.
+        positions in the channel, viscosity ratio 10 (two-fluid, as c2), Re 1, Ca 0.02,
+        dr = dz = 1/512.
 Any workload can be built at another grid size; geometry lengths scale with the grid.
 
   C3 (make_c3_solve): independent momentum solves, A x = b with the VeloSolve_2_combined
@@ -165,6 +167,16 @@ def interpolate_coef_host(params, dist, bdr_ph):
     return fpd, rho, eta
 
 
+def two_phase_coef_host(params, fpd, ph):
+    """numpy form of the two-fluid coefficients (two_phase_flow_complex_domain/
+    interpolate_coef.f90:91-112, commented out there), evaluated like drd_two_phase_coef."""
+    lr, le = params.lambda_rho - 1.0, params.lambda_eta - 1.0
+    rho = np.where(ph <= -1.0, 1.0, np.where(ph >= 1.0, params.lambda_rho, 1.0 + lr * ph))
+    eta_ph = np.where(ph <= -1.0, 1.0, np.where(ph >= 1.0, params.lambda_eta, 1.0 + le * ph))
+    eta = np.maximum(1.0 + le * fpd, eta_ph)
+    return rho, eta
+
+
 class Case:
     """A workload: parameters, resident-state fields and coefficient fields."""
 
@@ -216,14 +228,16 @@ def make_case(name="c2", seed=0, nr=None, nz=None, precision=abi.DRD_PREC_FP64, 
     elif name == "c5":
         nr = nr or 2048
         nz = nz or 1024
-        p = abi.default_params(nr, nz, re=1.0, ca=0.02, lambda_rho=1.0, lambda_eta=10.0, penalty_k=1.0e4)
+        p = abi.default_params(nr, nz, re=1.0, ca=0.02, lambda_rho=1.0, lambda_eta=10.0, penalty_k=1.0e4,
+                               two_fluid=1)
         p.dr, p.dz = 4.0 / nr, 2.0 / nz
         p.dt = min(p.dr, p.dz) * 0.1
     elif name in ("c2", "tp"):
         nr = nr or (420 if name == "c2" else 128)
         nz = nz or (180 if name == "c2" else 128)
         slen, shig = 3.5, 1.5
-        p = abi.default_params(nr, nz, re=0.5, ca=0.05, lambda_rho=1.0, lambda_eta=5.0, penalty_k=1.0e4)
+        p = abi.default_params(nr, nz, re=0.5, ca=0.05, lambda_rho=1.0, lambda_eta=5.0, penalty_k=1.0e4,
+                               two_fluid=1 if name == "c2" else 0)
         p.dr, p.dz = slen / nr, shig / nz
         p.dt = min(p.dr, p.dz) * 0.1
     else:
@@ -332,7 +346,67 @@ def make_case(name="c2", seed=0, nr=None, nz=None, precision=abi.DRD_PREC_FP64, 
         "rho": rho, "eta": eta, "fpd": fpd, "bdr_ph": bdr, "bdr_ph_grad": _grad_mag(bdr, dr, dz),
         "M0": M.copy(), "Mi": M.copy(), "bdr_pen": bdr.copy(), "bdr_used": 1.0 - bdr,
     }
+    if p.two_fluid:
+        # the drops carry the viscosity ratio (eta = lambda_eta inside them, 1 in the matrix fluid)
+        coefs["rho"], coefs["eta"] = two_phase_coef_host(p, fpd, ph)
     if name == "tp":
         coefs["bdr_pen"] = (bdr > 0.5).astype(np.float64)
         coefs["M0"] = (1.0 - bdr) * (ph ** 2 - 1.0) ** 2
     return Case(name, p, state, coefs, dist, meta)
+
+
+def load_reference_geometry(path):
+    """The reference's serpentine geometry (a domain_snake_420_180.npz fixture holding the raw
+    domain_snake_420_180.bin and _dist.bin values, each a [nr][nz] array as read_var reads
+    them, microfluidics_complex_domain/inout.f90:75-86) -> (mask, dist) as [k][i] arrays."""
+    z = np.load(path)
+    return np.ascontiguousarray(z["mask"].T), np.ascontiguousarray(z["dist"].T)
+
+
+def mask_cell(mask):
+    """finit's ph = bdr_ph from the mask (finit.f90:121-141): interior from the file, Neumann
+    ghosts; the input of drd_finit_wall."""
+    nz, nr = mask.shape
+    a = np.zeros(cell_shape(nr, nz))
+    a[1:-1, 1:-1] = mask
+    return neumann_ghosts_cell(a)
+
+
+def make_reference_snake(bdr_ph, wall_dist, precision=abi.DRD_PREC_FP64, **overrides):
+    """The reference's own microfluidics example on its own geometry: the MF deck
+    (microfluidics_complex_domain/input), bdr_ph = finit's smoothed wall indicator (CELL, the
+    output of drd_finit_wall on the domain_snake mask), bdr_ph_dist = the distance file
+    (interior; the ghosts keep the zero of the module array), the 9-bead fiber at
+    (slen/2, (0.17 + 0.67)/2) (mcl6.f90:178), and the fluid stripe of finit.f90:222-233:
+    ph = min(tanh((r - 0.4 slen - 0.2)/(sqrt2 eps)), tanh(-(r - 0.6 slen - 0.2)/(sqrt2 eps))),
+    rescaled to [0, 1] and clipped by 1 - bdr_ph; rmu, bdr_ph_grad, ph_M_0 = ph_M_inner =
+    1 - bdr_ph as finit.f90:244-278 computes them."""
+    nz, nr = bdr_ph.shape[0] - 2, bdr_ph.shape[1] - 2
+    p = abi.default_params(nr, nz)
+    p.precision = precision
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    dr, dz, eps = p.dr, p.dz, p.I_thickness
+    slen = nr * dr
+    bdr = np.array(bdr_ph, dtype=np.float64, copy=True)
+    pp = abi.default_particle_params(slen, nz * dz)
+    points = np.array(abi.particle_chain(pp, slen / 2.0, (0.17 + 0.67) / 2.0), dtype=np.float64)
+    bdr_dist = np.zeros(cell_shape(nr, nz))
+    bdr_dist[1:-1, 1:-1] = wall_dist
+    dist = fpd_dist_host(pp, points, nr, nz, dr, dz)
+    fpd, rho, eta = interpolate_coef_host(p, dist, bdr)
+    r = ((np.arange(nr) + 0.5) * dr)[None, :] * np.ones((nz, 1))
+    s2 = math.sqrt(2.0) * eps
+    ph = np.zeros(cell_shape(nr, nz))
+    ph[1:-1, 1:-1] = np.minimum(np.tanh((r - 0.4 * slen - 0.2) / s2), np.tanh(-(r - 0.6 * slen - 0.2) / s2))
+    ph = (ph + 1.0) / 2.0
+    ph = np.minimum(1.0 - bdr, ph)
+    neumann_ghosts_cell(ph)
+    state = _empty_state(nr, nz)
+    state[abi.F_PH] = ph
+    state[abi.F_RMU] = _rmu_init(ph, eps, dr, dz)
+    M = 1.0 - bdr
+    coefs = {"rho": rho, "eta": eta, "fpd": fpd, "bdr_ph": bdr, "bdr_ph_grad": _grad_mag(bdr, dr, dz),
+             "M0": M.copy(), "Mi": M.copy(), "bdr_pen": bdr.copy(), "bdr_used": 1.0 - bdr}
+    meta = {"particles": {"pp": pp, "points": points, "bdr_dist": bdr_dist}, "nr": nr, "nz": nz}
+    return Case("reference_snake", p, state, coefs, dist, meta)

@@ -108,6 +108,13 @@ typedef struct drd_params {
     int32_t mixed_max_refine;      /* mixed mode: maximum FP64 refinement sweeps                   */
     int32_t uv_precond;            /* momentum preconditioner: DRD_UV_JACOBI (the MF reference) or  */
                                    /* DRD_UV_ESOLP (ESOLP_x, used by the PD application)             */
+    int32_t two_fluid;             /* 0: rho, eta follow the solid/particle indicator fpd_ph only   */
+                                   /* (interpolate_coef.f90:84-89).  1: the two-fluid form that     */
+                                   /* two_phase_flow_complex_domain/interpolate_coef.f90:91-112     */
+                                   /* keeps commented out: rho = rho(ph), eta = max(eta(fpd_ph),    */
+                                   /* eta(ph)), rebuilt by drd_step after every CH solve from ph    */
+                                   /* before the swap, where mcl6 calls interpolate_coef            */
+    int32_t reserved1;
 } drd_params;
 
 typedef struct drd_status {
@@ -152,6 +159,15 @@ int drd_set_tp_fields(drd_ctx* ctx, const double* bdr_ph_used, const double* bdr
  * particle distance dist(r(i,k), z(i,k)) of every interior cell (DIST shape); fpd_ph, rho,
  * eta (CELL) are written and rho/eta also replace the context's coefficients. */
 int drd_interpolate_coef(drd_ctx* ctx, const double* dist, double* fpd_ph, double* rho, double* eta);
+/* The two-fluid coefficients of interpolate_coef, in the form two_phase_flow_complex_domain/
+ * interpolate_coef.f90:91-112 leaves commented out (its "TODO: two-phase viscosity/density
+ * ratio"): with x = ph, rho = 1 (x <= -1), lambda_rho (x >= 1), else 1 + (lambda_rho - 1) x; the
+ * same for eta_ph with lambda_eta; eta = max(1 + (lambda_eta - 1) fpd_ph, eta_ph).  fpd_ph (CELL)
+ * becomes the context's indicator (NULL keeps the one from the last interpolate_coef, particle
+ * step or call of this routine); ph (CELL, NULL = the resident phase field).  rho, eta (CELL)
+ * are written (each may be NULL) and replace the context's coefficients.  drd_step does the
+ * same on the device after each CH solve when params.two_fluid = 1. */
+int drd_two_phase_coef(drd_ctx* ctx, const double* fpd_ph, const double* ph, double* rho, double* eta);
 
 /* ---- initialisation: finit's wall smoothing ------------------------------------------- */
 
@@ -371,8 +387,10 @@ int drd_checkpoint_wait(drd_ctx* ctx);
  * fixed __device__ array of about 3.2 MB, held by every GPU that loads the library until the
  * process exits; grids beyond DRD_NOALLOC_MAX_* return DRD_ERR_TOO_LARGE.  The first call on a
  * device looks up that array's device address (cudaGetSymbolAddress) and should therefore
- * come before any stream capture on that device.  Calls share the array: each call writes
- * every intermediate before reading it, but calls that overlap on the GPU race on it.
+ * come before any stream capture on that device.  The address is kept for the life of the
+ * process: after cudaDeviceReset on a device, this entry point must not be called on it again.
+ * Calls share the array: each call writes every intermediate before reading it, but calls that
+ * overlap on the GPU race on it.
  * No counterpart in the reference (its PreSolve_2 allocates nothing on a device because it has
  * none). */
 int drd_presolve_2_noalloc(int nr, int nz, double dr, double dz, const double* u, const double* v, double coef,

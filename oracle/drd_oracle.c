@@ -1348,6 +1348,31 @@ void orc_interpolate_coef(const drd_params* P, const double* dist, const double*
     }
 }
 
+/* The two-fluid coefficients that two_phase_flow_complex_domain/interpolate_coef.f90:91-112
+ * keeps commented out: rho and eta_tmp piecewise in ph (1 at ph <= -1, the ratio at ph >= 1,
+ * 1 + (ratio - 1) ph between), then eta = max(eta, eta_tmp) with eta = 1 + (lambda_eta - 1)
+ * fpd_ph as computed above it (:84-89). */
+void orc_two_phase_coef(const drd_params* P, const double* fpd_ph, const double* ph, double* rho, double* eta) {
+    const long cs = cell_size(P->nr, P->nz);
+    for (long q = 0; q < cs; ++q) {
+        const double x = ph[q];
+        double r, e;
+        if (x <= -1.0) {
+            r = 1.0;
+            e = 1.0;
+        } else if (x >= 1.0) {
+            r = P->lambda_rho;
+            e = P->lambda_eta;
+        } else {
+            r = 1.0 + (P->lambda_rho - 1.0) * x;
+            e = 1.0 + (P->lambda_eta - 1.0) * x;
+        }
+        const double es = 1.0 + (P->lambda_eta - 1.0) * fpd_ph[q];
+        rho[q] = r;
+        eta[q] = es > e ? es : e;
+    }
+}
+
 /* Mass sum of dissipation(): microfluidics_complex_domain/dissipation.f90:116-122. */
 double orc_mass(const drd_params* P, const double* ph) {
     const int nr = P->nr, nz = P->nz;
@@ -1659,6 +1684,16 @@ int orc_step(const drd_params* P, const double* ph_lcc, const double* pre_lcc, o
         rho = S->parts->rho;
         eta = S->parts->eta;
     }
+    double *rho2 = NULL, *eta2 = NULL;
+    if (P->two_fluid) { /* interpolate_coef's two-fluid form, from ph before the swap */
+        const double* fpd = (S->parts && S->parts->pp.np > 0) ? S->parts->fpd_ph : S->fpd_ph;
+        if (!fpd) fpd = S->bdr_ph; /* no particles and no indicator given: the solid alone */
+        rho2 = dalloc(cs);
+        eta2 = dalloc(cs);
+        orc_two_phase_coef(P, fpd, f[DRD_F_PH], rho2, eta2);
+        rho = rho2;
+        eta = eta2;
+    }
     orc_velosolve(P, first ? 1 : 2, f[DRD_F_PSI1], f[DRD_F_PSI2], f[DRD_F_U_PRE], f[DRD_F_U], f[DRD_F_V_PRE],
                   f[DRD_F_V], f[DRD_F_P], rho, eta, S->bdr_ph, S->bdr_pen, S->bdr_used, ph_after,
                   rmu_after, t + P->dt, f[DRD_F_PF1], f[DRD_F_PF2], u_after, v_after, NULL, NULL, &st[1]);
@@ -1680,6 +1715,6 @@ int orc_step(const drd_params* P, const double* ph_lcc, const double* pre_lcc, o
     orc_presolve(P, pre_lcc, f[DRD_F_U], f[DRD_F_V], coef, f[DRD_F_PSI2]);
     for (long q = 0; q < cs; ++q) f[DRD_F_P][q] = f[DRD_F_PSI2][q] + f[DRD_F_P][q];
     if (st2) { st2[0] = st[0]; st2[1] = st[1]; }
-    free(rmu_after); free(ph_after); free(u_after); free(v_after);
+    free(rmu_after); free(ph_after); free(u_after); free(v_after); free(rho2); free(eta2);
     return 0;
 }

@@ -93,6 +93,7 @@ void orc_presolve(const drd_params* P, const double* pre_lcc, const double* u, c
 void orc_interpolate_coef(const drd_params* P, const double* dist, const double* bdr_ph,
                           double* fpd_ph, double* rho, double* eta);
 
+void orc_two_phase_coef(const drd_params* P, const double* fpd_ph, const double* ph, double* rho, double* eta);
 double orc_mass(const drd_params* P, const double* ph);
 
 /* ESOLP_x momentum preconditioner (microfluidics_complex_domain/ESOLP.f90, setup.f90:157-235). */
@@ -155,6 +156,7 @@ typedef struct orc_state {
     const double* bdr_pen;
     const double* bdr_used;
     orc_particles* parts;   /* NULL: particles held fixed; else the coupling of mcl6.f90:394-402 */
+    const double* fpd_ph;   /* indicator of interpolate_coef for params.two_fluid (NULL: bdr_ph)  */
 } orc_state;
 int orc_step(const drd_params* P, const double* ph_lcc, const double* pre_lcc, orc_state* S,
              int first, double t, drd_status* st2);

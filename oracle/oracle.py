@@ -68,6 +68,7 @@ def lib(openmp=False):
         L.orc_velosolve.restype = C.c_int
         L.orc_presolve.argtypes = [P, dp, dp, dp, C.c_double, dp]
         L.orc_interpolate_coef.argtypes = [P, dp, dp, dp, dp, dp]
+        L.orc_two_phase_coef.argtypes = [P, dp, dp, dp, dp]
         L.orc_mass.argtypes = [P, dp]
         L.orc_mass.restype = C.c_double
         L.orc_ori_coef.argtypes = [P, C.c_double]
@@ -98,7 +99,7 @@ class OrcParticles(C.Structure):
 class OrcState(C.Structure):
     _fields_ = [("f", C.POINTER(C.c_double) * abi.F_COUNT)] + [
         (n, C.POINTER(C.c_double)) for n in ("rho", "eta", "bdr_ph", "bdr_ph_grad", "M0", "Mi", "bdr_pen", "bdr_used")
-    ] + [("parts", C.POINTER(OrcParticles))]
+    ] + [("parts", C.POINTER(OrcParticles)), ("fpd_ph", C.POINTER(C.c_double))]
 
 
 class Oracle:
@@ -282,6 +283,12 @@ class Oracle:
                                     ptr(rho), ptr(eta))
         return fpd, rho, eta
 
+    def two_phase_coef(self, fpd_ph, ph):
+        """The two-fluid rho, eta (two_phase_flow_complex_domain/interpolate_coef.f90:91-112)."""
+        rho, eta = np.zeros_like(ph), np.zeros_like(ph)
+        self.L.orc_two_phase_coef(C.byref(self.P), ptr(fpd_ph), ptr(ph), ptr(rho), ptr(eta))
+        return rho, eta
+
     def mass(self, ph):
         return self.L.orc_mass(C.byref(self.P), ptr(ph))
 
@@ -348,6 +355,8 @@ class Oracle:
             S.f[fid] = ptr(state[fid])
         for name in ("rho", "eta", "bdr_ph", "bdr_ph_grad", "M0", "Mi", "bdr_pen", "bdr_used"):
             setattr(S, name, ptr(coefs[name]))
+        if "fpd" in coefs:
+            S.fpd_ph = ptr(coefs["fpd"])
         X = None
         if particles is not None:
             shape = coefs["rho"].shape

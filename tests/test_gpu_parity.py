@@ -308,3 +308,24 @@ def test_step_sequence_matches_oracle(cuda_lib, oracle_build, precision, guess):
         assert rel_err(g[fid], st[fid]) < tol, fid
     assert abs(stats.mass - orc.mass(st[F.F_PH])) < 1e-12 * max(1.0, abs(stats.mass))
     ctx.close()
+
+
+def test_interpolate_coef_from_distance(cuda_lib, oracle_build):
+    """drd_interpolate_coef (microfluidics_complex_domain/interpolate_coef.f90:4-92) from a
+    caller's distance field: fpd_ph, rho, eta against the oracle, and they become the
+    coefficients of the momentum operator."""
+    from drd_application_gb300.workloads import make_case
+
+    case = make_case("c2", seed=9, nr=64, nz=32, two_fluid=0, lambda_rho=2.0)
+    ctx = DRDContext(case.params)
+    ctx.set_case(case)
+    rng = np.random.default_rng(5)
+    dist = case.dist + 0.01 * rng.standard_normal(case.dist.shape)
+    fpd, rho, eta = ctx.interpolate_coef(dist)
+    orc = Oracle(case.params)
+    fo, ro, eo = orc.interpolate_coef(dist, case.coefs["bdr_ph"])
+    assert rel_err(fpd, fo) < 1e-14 and rel_err(rho, ro) < 1e-14 and rel_err(eta, eo) < 1e-14
+    x = rng.standard_normal(ctx.L.drd_op_length(ctx.h, F.DRD_OP_UV_MATVEC))
+    y = ctx.op_apply(F.DRD_OP_UV_MATVEC, x, bdf=2)
+    assert rel_err(y, orc.uv_matvec(2, ro, eo, case.coefs["bdr_pen"], x)) < 1e-12
+    ctx.close()

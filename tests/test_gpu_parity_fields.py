@@ -1,0 +1,126 @@
+"""Field parity at 1e-10 in FP64 mode against the oracle, at full size and on the reference's
+own geometry, through the C-ABI.
+
+Two correct BiCGSTABs whose dot products are summed in different orders stop at different
+iterates, so both sides solve to 1e-13 (the FP64 residual floor of these systems), with the
+iteration caps raised where the first step needs more than the reference's 500 / 800, and every
+resident field is compared after each run:
+
+* C2 (420x180 serpentine channel, 3 rigid fibers, 2 drops, viscosity ratio 5 between the
+  fluids): three mcl6 steps;
+* C1 (128x64 channel, one drop, no solid): five steps;
+* the reference's own serpentine geometry (microfluidics_complex_domain/domain_snake_420_180.bin
+  and _dist.bin, stored in tests/golden/): finit's 51 PhSolve_ori wall-smoothing steps
+  (finit.f90:120-189), then one particle-coupled step of the README example (the MF deck, the
+  9-bead fiber of mcl6.f90:178, the fluid stripe of finit.f90:222-233).
+
+The oracle runs with OpenMP over the transform lines (the arithmetic of each line is the
+serial one), so each case costs tens of seconds of host time.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from drd_application_gb300 import abi
+from drd_application_gb300.api import DRDContext
+from drd_application_gb300.workloads import (load_reference_geometry, make_case, make_reference_snake,
+                                             mask_cell)
+from oracle.oracle import Oracle
+from tests.helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+F = abi
+FIELD_TOL = 1e-10
+FIELDS = {"u": F.F_U, "v": F.F_V, "ph": F.F_PH, "rmu": F.F_RMU, "p": F.F_P, "psi2": F.F_PSI2}
+GEOM = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "domain_snake_420_180.npz")
+
+
+def _run_both(case, P, steps, particles=None):
+    ctx = DRDContext(P)
+    ctx.set_case(case)
+    ctx.upload_state(case.state)
+    X = None
+    if particles is not None:
+        X = {"pp": particles["pp"], "points": particles["points"].copy(), "bdr_dist": particles["bdr_dist"]}
+        ctx.particles_set(particles["pp"], particles["points"].copy(), particles["bdr_dist"])
+    orc = Oracle(P, openmp=True)
+    st = case.copy_state()
+    t = 0.0
+    stats = []
+    for s in range(steps):
+        g = ctx.step(s == 0, t)
+        so = orc.step(st, case.coefs, s == 0, t, particles=X)
+        stats.append((g, so))
+        t += P.dt
+    out = ctx.download_state(list(FIELDS.values()))
+    pts = ctx.particles_get()[0] if particles is not None else None
+    ctx.close()
+    return out, st, stats, pts, X
+
+
+def _check(out, st, stats, label):
+    for g, (so_ch, so_uv) in stats:
+        assert g.ch.info == 0 and g.uv.info == 0, (label, g.ch.as_dict(), g.uv.as_dict())
+        assert so_ch.info == 0 and so_uv.info == 0, (label, so_ch.info, so_uv.info)
+    errs = {name: rel_err(out[fid], st[fid]) for name, fid in FIELDS.items()}
+    print(label, {k: f"{v:.2e}" for k, v in errs.items()})
+    for name, e in errs.items():
+        assert e <= FIELD_TOL, (label, name, e)
+    return errs
+
+
+def test_two_phase_coef_matches_oracle(cuda_lib, oracle_build):
+    """drd_two_phase_coef (the two-fluid interpolate_coef) equals the oracle bit for bit."""
+    case = make_case("c2", seed=2, nr=84, nz=36)
+    ctx = DRDContext(case.params)
+    rng = np.random.default_rng(4)
+    ph = case.state[F.F_PH] + 0.3 * rng.standard_normal(case.state[F.F_PH].shape)  # reaches both clipped branches
+    ph[0, :3] = [-1.0, 1.0, 2.0]
+    rho, eta = ctx.two_phase_coef(case.coefs["fpd"], ph)
+    ro, eo = Oracle(case.params).two_phase_coef(case.coefs["fpd"], ph)
+    assert np.array_equal(rho, ro) and np.array_equal(eta, eo)
+    # NULL ph: the resident phase field
+    ctx.upload_state({F.F_PH: ph})
+    r2, e2 = ctx.two_phase_coef(None, None)
+    assert np.array_equal(e2, eo)
+    ctx.close()
+
+
+def test_c2_fullsize_fields_fp64(cuda_lib, oracle_build):
+    case = make_case("c2", seed=1)
+    assert (case.nr, case.nz) == (420, 180) and case.params.two_fluid == 1
+    P = case.params.copy()
+    P.tol, P.ch_maxit, P.uv_maxit = 1e-13, 2000, 2000
+    out, st, stats, _, _ = _run_both(case, P, 3)
+    _check(out, st, stats, "c2 420x180, 3 steps")
+
+
+def test_c1_fields_fp64(cuda_lib, oracle_build):
+    case = make_case("c1", seed=0)
+    P = case.params.copy()
+    P.tol = 1e-13
+    out, st, stats, _, _ = _run_both(case, P, 5)
+    _check(out, st, stats, "c1 128x64, 5 steps")
+
+
+def test_reference_geometry_finit_and_step(cuda_lib, oracle_build):
+    """The reference's own inputs: finit's wall smoothing of domain_snake_420_180.bin, then the
+    first (BDF1) step of its microfluidics example with the fiber coupled."""
+    mask, wall_dist = load_reference_geometry(GEOM)
+    assert mask.shape == (180, 420) and set(np.unique(mask)) == {-1.0, 1.0}
+    P0 = abi.default_params(420, 180, tol=1e-13)
+    P0.dt = 1.0e-4  # finit.f90:151
+    ctx = DRDContext(P0)
+    b_g, ph_g, _, info = ctx.finit_wall(mask_cell(mask), 51)
+    ctx.close()
+    b_o, ph_o, _, info_o = Oracle(P0, openmp=True).finit_wall(mask_cell(mask), 51)
+    assert info == 0 and info_o == 0
+    eb, ep = rel_err(b_g, b_o), rel_err(ph_g, ph_o)
+    print(f"finit 51 steps: bdr_ph {eb:.2e}, ph {ep:.2e}")
+    assert eb <= FIELD_TOL and ep <= FIELD_TOL
+    # the step runs on the oracle's bdr_ph on both sides, so that it is compared on its own
+    case = make_reference_snake(b_o, wall_dist, tol=1e-13, ch_maxit=3000, uv_maxit=6000)
+    out, st, stats, pts, X = _run_both(case, case.params, 1, particles=case.meta["particles"])
+    _check(out, st, stats, "reference geometry, first step with the fiber")
+    assert np.abs(pts - X["points"]).max() < 1e-12

@@ -165,5 +165,24 @@ def test_interpolate_coef_formula(oracle_build):
     o = Oracle(case.params)
     fpd, rho, eta = o.interpolate_coef(case.dist, case.coefs["bdr_ph"])
     assert rel_err(fpd, case.coefs["fpd"]) < 1e-14
-    assert rel_err(eta, case.coefs["eta"]) < 1e-14
+    assert rel_err(eta, 1.0 + (case.params.lambda_eta - 1.0) * fpd) < 1e-14
     assert np.allclose(rho, 1.0 + (case.params.lambda_rho - 1.0) * fpd)
+
+
+def test_two_phase_coef_formula(oracle_build):
+    """The two-fluid coefficients (two_phase_flow_complex_domain/interpolate_coef.f90:91-112):
+    the oracle equals the workload's numpy form bit for bit, the drops carry lambda_eta, the
+    matrix fluid 1, the solid at least 1 + (lambda_eta - 1) fpd_ph, and the clipped branches."""
+    case = make_case("c2", seed=5, nr=84, nz=36)
+    P = case.params
+    assert P.two_fluid == 1 and P.lambda_eta == 5.0
+    o = Oracle(P)
+    ph, fpd = case.state[abi.F_PH], case.coefs["fpd"]
+    rho, eta = o.two_phase_coef(fpd, ph)
+    assert np.array_equal(eta, case.coefs["eta"]) and np.array_equal(rho, case.coefs["rho"])
+    assert np.all(eta >= 1.0 + 4.0 * fpd) and np.all(eta >= 1.0 + 4.0 * np.clip(ph, -1, 1))
+    drop = (ph > 0.5) & (fpd < 1e-6)
+    assert drop.any() and np.allclose(eta[drop], 1.0 + 4.0 * ph[drop])
+    x = np.linspace(-1.5, 1.5, ph.size).reshape(ph.shape)
+    _, e2 = o.two_phase_coef(np.zeros_like(x), x)
+    assert np.all(e2[x >= 1.0] == 5.0) and np.all(e2[x <= -1.0] == 1.0)

@@ -1,4 +1,5 @@
-"""The allocation-free pressure step (drd_presolve_2_noalloc) against drd_presolve_2.
+"""The allocation-free pressure step (drd_presolve_2_noalloc) against drd_presolve_2 and the
+oracle.
 
 drd_presolve_2_noalloc exists for callers that cannot let the library call cudaMalloc: an
 application whose device memory all belongs to its own pool allocator, or a driver issuing
@@ -15,6 +16,7 @@ import pytest
 from drd_application_gb300 import abi
 from drd_application_gb300.api import DRDContext
 from drd_application_gb300.workloads import make_case
+from oracle.oracle import Oracle
 from tests.helpers import advanced_case, rel_err
 
 pytestmark = pytest.mark.gpu
@@ -39,6 +41,7 @@ def test_noalloc_presolve_matches_presolve_2_twice(cuda_lib, oracle_build, nr, n
     case, st, _ = advanced_case("c2", seed=9, nr=nr, nz=nz, steps=1) if nr <= 64 else (make_case("c2", seed=9, nr=nr, nz=nz), None, 0.0)
     P = case.params
     ctx = DRDContext(P)
+    orc = Oracle(P)
     rng = np.random.default_rng(nr)
     for call in range(2):
         if st is not None and call == 0:
@@ -51,6 +54,8 @@ def test_noalloc_presolve_matches_presolve_2_twice(cuda_lib, oracle_build, nr, n
         got = _noalloc(cuda_lib, P, u, v, coef)
         assert np.isfinite(got).all()
         assert rel_err(got, ref) < 1e-12, (call, rel_err(got, ref))
+        # and against the oracle's PreSolve_2 + dct_fftw directly
+        assert rel_err(got, orc.presolve(u, v, coef)) < 1e-12, call
     ctx.close()
 
 
