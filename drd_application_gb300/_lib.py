@@ -25,6 +25,10 @@ SIGNATURES = {
     "drd_set_tp_fields": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
     "drd_interpolate_coef": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
     "drd_two_phase_coef": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
+    "drd_reinint_by_phsolve": (C.c_int, [_ctx, _dp, _dp, _dp]),
+    "drd_dissipation": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.POINTER(abi.drd_diagnostics)]),
+    "drd_write_fort23": (C.c_int, [C.c_char_p, C.c_double, C.POINTER(abi.drd_diagnostics)]),
+    "drd_write_fort22": (C.c_int, [C.c_char_p, C.c_int, C.c_double, C.POINTER(abi.drd_diagnostics)]),
     "drd_phsolve_ori": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp, _st]),
     "drd_finit_wall": (C.c_int, [_ctx, _dp, C.c_int, _dp, _dp, _dp]),
     "drd_particle_params_default": (C.c_int, [C.POINTER(abi.drd_particle_params), C.c_double, C.c_double]),

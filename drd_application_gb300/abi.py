@@ -77,6 +77,14 @@ class drd_params(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_ if not name.startswith("reserved")}
 
 
+class drd_diagnostics(C.Structure):
+    """dissipation()'s diagnostics (microfluidics_complex_domain/dissipation.f90:1-122)."""
+    _fields_ = [(n, C.c_double) for n in ("e1", "e2", "e3", "e4", "dissip", "mass")]
+
+    def as_tuple(self):
+        return (self.e1, self.e2, self.e3, self.e4, self.dissip, self.mass)
+
+
 PARTICLES_MAX = 64
 
 

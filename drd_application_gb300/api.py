@@ -141,6 +141,29 @@ class DRDContext:
         self._rc(rc, "finit_wall")
         return out[0], out[1], out[2], rc
 
+    def reinint_by_PhSolve(self, bdr_ph):
+        """reinint_by_PhSolve (two_phase_flow_complex_domain/reinint_by_PhSolve.f90) ->
+        (bdr_ph, bdr_ph_penalty, info); both also become the context's."""
+        bdr_ph = _check_shape(bdr_ph, self.cs, "bdr_ph")
+        b, pen = np.zeros(self.cs), np.zeros(self.cs)
+        rc = self.L.drd_reinint_by_phsolve(self.h, ptr(bdr_ph), ptr(b), ptr(pen))
+        self._rc(rc, "reinint_by_phsolve")
+        return b, pen, rc
+
+    def dissipation(self, vs, u=None, v=None, ph=None, rmu=None, angleB=None, angleT=None):
+        """dissipation's diagnostics -> abi.drd_diagnostics (e1, e2, e3, e4, dissip, mass).
+        Fields left None are the resident ones."""
+        a = [_check_shape(u, self.us, "u"), _check_shape(v, self.vs, "v"), _check_shape(ph, self.cs, "ph"),
+             _check_shape(rmu, self.cs, "rmu")]
+        ang = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (angleB, angleT)]
+        for x in ang:
+            if x is not None and x.shape[0] < self.nr:
+                raise ValueError("angle arrays need nr entries")
+        out = abi.drd_diagnostics()
+        self._rc(self.L.drd_dissipation(self.h, *[ptr(x) for x in a], ptr(ang[0]), ptr(ang[1]), float(vs),
+                                        C.byref(out)), "dissipation", False)
+        return out
+
     # ---- fiber particles (particles_move.f90) --------------------------------------------
     def particles_set(self, pp, points=None, bdr_dist=None):
         """Make a bead chain resident (drd_particles_set); points is a (2, Np) array (x row, y

@@ -119,9 +119,65 @@ void scatter(Shape s, int nr, int nz, const std::vector<double>& rec, double* a)
         for (int k = 0; k <= nz; ++k) a[at(s, nr, i, k)] = rec[q++];
 }
 
+// Fortran E editing Ew.d with one leading zero digit (the default scale factor): the value as
+// 0.d1d2...dd x 10^e, written in `w` columns right-justified; the exponent takes the form E+ee
+// while |e| <= 99 and +eee without the letter up to 999 (Fortran 2018, 13.7.2.3.3).
+std::string fortran_e(double x, int w, int d) {
+    char buf[64];
+    if (!std::isfinite(x)) {
+        std::snprintf(buf, sizeof(buf), "%*s", w, std::isnan(x) ? "NaN" : (x > 0 ? "Infinity" : "-Infinity"));
+        return buf;
+    }
+    std::string mant;
+    int e = 0;
+    if (x != 0.0) {
+        // d significant digits, rounded to nearest: "D.DDDDDDE+XX" -> mantissa digits and exponent
+        std::snprintf(buf, sizeof(buf), "%.*E", d - 1, std::fabs(x));
+        std::string t(buf);
+        const size_t epos = t.find('E');
+        for (size_t q = 0; q < epos; ++q)
+            if (std::isdigit((unsigned char)t[q])) mant.push_back(t[q]);
+        e = std::atoi(t.c_str() + epos + 1) + 1;
+    } else {
+        mant.assign((size_t)d, '0');
+    }
+    std::string out = (std::signbit(x) && x != 0.0) ? "-0." : "0.";
+    out += mant;
+    if (std::abs(e) <= 99) std::snprintf(buf, sizeof(buf), "E%c%02d", e < 0 ? '-' : '+', std::abs(e));
+    else std::snprintf(buf, sizeof(buf), "%c%03d", e < 0 ? '-' : '+', std::abs(e));
+    out += buf;
+    if ((int)out.size() < w) out.insert(0, (size_t)(w - (int)out.size()), ' ');
+    if ((int)out.size() > w) out.assign((size_t)w, '*');
+    return out;
+}
+
+int append_line(const char* path, const std::string& line) {
+    FILE* f = std::fopen(path, "a");
+    if (!f) return DRD_ERR_BADARG;
+    const bool ok = std::fputs(line.c_str(), f) >= 0 && std::fputc('\n', f) != EOF;
+    return (std::fclose(f) == 0 && ok) ? DRD_OK : DRD_ERR_BADARG;
+}
+
 }  // namespace
 
 extern "C" {
+
+int drd_write_fort23(const char* path, double t, const drd_diagnostics* d) {
+    if (!path || !d) return DRD_ERR_BADARG;
+    std::string line;
+    for (double x : {t, d->e1, d->e2, d->e3, d->e4, d->dissip}) line += fortran_e(x, 14, 7);  // format 6e14.7
+    return append_line(path, line);
+}
+
+int drd_write_fort22(const char* path, int kcount, double dt, const drd_diagnostics* d) {
+    if (!path || !d) return DRD_ERR_BADARG;
+    char buf[32];
+    std::snprintf(buf, sizeof(buf), "%12d", kcount);
+    std::string line(buf);
+    line += " " + fortran_e(dt * d->dissip, 24, 16) + " " + fortran_e(d->mass, 24, 16);
+    return append_line(path, line);
+}
+
 
 int drd_read_deck(const char* path, drd_deck* deck, char* err, int err_len) {
     if (!path || !deck) {

@@ -1047,6 +1047,13 @@ __global__ void k_interp_coef(DevParams P, const double* __restrict__ dist, cons
     }
 }
 
+// y = 1 where x > t, else 0 (reinint_by_PhSolve.f90:78-86's bdr_ph_penalty).
+__global__ void k_threshold(long n, const double* __restrict__ x, double t, double* __restrict__ y, ull* ctr) {
+    count_launch(ctr);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        y[q] = x[q] > t ? 1.0 : 0.0;
+}
+
 // The two-fluid form of interpolate_coef that two_phase_flow_complex_domain/
 // interpolate_coef.f90:91-112 keeps commented out: rho and eta_ph piecewise linear in ph (1 at
 // ph <= -1, the ratio at ph >= 1), eta = max(eta(fpd), eta_ph).  Products and sums are rounded
@@ -1094,6 +1101,94 @@ __global__ void k_mass_final(Dots d, int slot, double drdz, double* out, ull* ct
     __shared__ double sm[32];
     double r = reduce_partials<DRD_TPB>(d.part + slot * DRD_MAXB, d.G, sm);
     if (threadIdx.x == 0) *out = r * drdz;
+}
+
+// dissipation() (microfluidics_complex_domain/dissipation.f90:1-122): per-block partial sums of
+// e1 (|grad rmu|^2 over interior cells), e2 (the wall rows' contact-angle residual), e3 (the
+// velocity-gradient terms at the nodes 0..nr x 0..nz with the trapezoid weights) and the mass.
+// Derivatives use setup's coefficients xa1 = -1/(2dr), xb1 = 0, xc1 = 1/(2dr) in dif1x's
+// expression ua u(i-1) + ub u(i) + uc u(i+1) (setup.f90:9-19, :269-307).  v's derivatives are
+// taken on v's own grid (the reference hands v to dif1x through u's shape), one-sided at i = nr
+// and, like u_z, in the wall rows (:68-77).
+__device__ __forceinline__ double dfdx3(double a, double b, double c, double h) {
+    const double ua = -1.0 / 2.0 / h, ub = 0.0, uc = -ua;
+    return ua * a + ub * b + uc * c;
+}
+__global__ void k_dissip_partial(DissipArgs a, const double* __restrict__ u, const double* __restrict__ v,
+                                 const double* __restrict__ ph, const double* __restrict__ rmu,
+                                 const double* __restrict__ angB, const double* __restrict__ angT, Dots d, ull* ctr) {
+    count_launch(ctr);
+    const int nr = a.nr, nz = a.nz;
+    const long tid = blockIdx.x * (long)blockDim.x + threadIdx.x, nt = (long)gridDim.x * blockDim.x;
+    const double pi = 3.14159265358979323846264338327950288;
+    double s1 = 0.0, s2 = 0.0, s3 = 0.0, sm_ = 0.0;
+    const long nc = (long)nr * nz;
+    for (long q = tid; q < nc; q += nt) {
+        const int i = (int)(q % nr), k = (int)(q / nr);
+        const double gx = (rmu[cidx(nr, i + 1, k)] - rmu[cidx(nr, i - 1, k)]) / 2.0 / a.dr;
+        const double gz = (rmu[cidx(nr, i, k + 1)] - rmu[cidx(nr, i, k - 1)]) / 2.0 / a.dz;
+        s1 += gx * gx + gz * gz;
+        sm_ += ph[cidx(nr, i, k)];
+    }
+    for (long i = tid; i < nr; i += nt) {
+        const double aT = angT ? angT[i] : a.angle, aB = angB ? angB[i] : a.angle;
+        double cf = sqrt(2.0) * cos(aT * pi / 180.0) / 3.0 * pi / 2. / a.eps;
+        const double pt = ph[cidx(nr, (int)i, nz)], pt1 = ph[cidx(nr, (int)i, nz - 1)];
+        const double gt = (pt - pt1) / a.dz - cf * cos(pi * (pt + pt1) / 2.0 / 2.);
+        cf = sqrt(2.0) * cos(aB * pi / 180.0) / 3.0 * pi / 2. / a.eps;
+        const double pb = ph[cidx(nr, (int)i, -1)], pb0 = ph[cidx(nr, (int)i, 0)];
+        const double gb = (pb - pb0) / a.dz - cf * cos(pi * (pb0 + pb) / 2.0 / 2.);
+        s2 += gt * gt + gb * gb;
+    }
+    const long nn = (long)(nr + 1) * (nz + 1);
+    for (long q = tid; q < nn; q += nt) {
+        const int i = (int)(q % (nr + 1)), k = (int)(q / (nr + 1));
+        const double uua = dfdx3(u[uidx(nr, i - 1, k)], u[uidx(nr, i, k)], u[uidx(nr, i + 1, k)], a.dr);
+        double uub, vvb, vva;
+        if (k == 0) {
+            uub = (u[uidx(nr, i, 1)] - u[uidx(nr, i, 0)]) / a.dz;
+            vvb = (v[vidx(nr, i, 1)] - v[vidx(nr, i, 0)]) / a.dz;
+        } else if (k == nz) {
+            uub = (u[uidx(nr, i, nz)] - u[uidx(nr, i, nz - 1)]) / a.dz;
+            vvb = (v[vidx(nr, i, nz)] - v[vidx(nr, i, nz - 1)]) / a.dz;
+        } else {
+            uub = dfdx3(u[uidx(nr, i, k - 1)], u[uidx(nr, i, k)], u[uidx(nr, i, k + 1)], a.dz);
+            vvb = dfdx3(v[vidx(nr, i, k - 1)], v[vidx(nr, i, k)], v[vidx(nr, i, k + 1)], a.dz);
+        }
+        if (i < nr) vva = dfdx3(v[vidx(nr, i - 1, k)], v[vidx(nr, i, k)], v[vidx(nr, i + 1, k)], a.dr);
+        else vva = (v[vidx(nr, nr, k)] - v[vidx(nr, nr - 1, k)]) / a.dr;
+        const double cx = (i == 0 || i == nr) ? 0.5 : 1.0, cz = (k == 0 || k == nz) ? 0.5 : 1.0;
+        s3 += cx * cz * ((uua * uua + vvb * vvb) + uub * uub + vva * vva);
+    }
+    __shared__ double sh[32];
+    double r = block_sum<DRD_TPB>(s1, sh);
+    if (threadIdx.x == 0) d.part[0 * DRD_MAXB + blockIdx.x] = r;
+    r = block_sum<DRD_TPB>(s2, sh);
+    if (threadIdx.x == 0) d.part[1 * DRD_MAXB + blockIdx.x] = r;
+    r = block_sum<DRD_TPB>(s3, sh);
+    if (threadIdx.x == 0) d.part[2 * DRD_MAXB + blockIdx.x] = r;
+    r = block_sum<DRD_TPB>(sm_, sh);
+    if (threadIdx.x == 0) d.part[3 * DRD_MAXB + blockIdx.x] = r;
+}
+
+// Fixed-order sums of the partials and the reference's scalings (dissipation.f90:47, :57, :88,
+// :101, :122): out = e1, e2, e3, e4, dissip, mass.
+__global__ void k_dissip_final(DissipArgs a, Dots d, double* out, ull* ctr) {
+    count_launch(ctr);
+    __shared__ double sh[32];
+    const double s1 = reduce_partials<DRD_TPB>(d.part + 0 * DRD_MAXB, d.G, sh);
+    const double s2 = reduce_partials<DRD_TPB>(d.part + 1 * DRD_MAXB, d.G, sh);
+    const double s3 = reduce_partials<DRD_TPB>(d.part + 2 * DRD_MAXB, d.G, sh);
+    const double sm_ = reduce_partials<DRD_TPB>(d.part + 3 * DRD_MAXB, d.G, sh);
+    if (threadIdx.x == 0) {
+        const double e1 = s1 * a.xld * a.ca * a.dr * a.dz;
+        const double e2 = s2 * a.vs * a.ca * (a.eps * a.eps) * a.dr;
+        const double e3 = s3 * a.dr * a.dz;
+        const double e4 = 0.0;
+        out[0] = e1; out[1] = e2; out[2] = e3; out[3] = e4;
+        out[4] = e1 + e2 + e3 + e4;
+        out[5] = sm_ * a.dr * a.dz;
+    }
 }
 
 // ======================================================================================
@@ -3253,6 +3348,14 @@ void launch_interp_coef(const DevParams& P, const double* dist, const double* bd
 void launch_two_phase_coef(const DevParams& P, long cs, const double* fpd, const double* ph, double* rho, double* eta,
                            float* rho32, float* eta32, ull* ctr, cudaStream_t s) {
     k_two_phase_coef<<<GRID(cs)>>>(P, cs, fpd, ph, rho, eta, rho32, eta32, ctr);
+}
+void launch_dissipation(const DissipArgs& a, const double* u, const double* v, const double* ph, const double* rmu,
+                        const double* angB, const double* angT, const Dots& d, double* out, ull* ctr, cudaStream_t s) {
+    k_dissip_partial<<<d.G, DRD_TPB, 0, s>>>(a, u, v, ph, rmu, angB, angT, d, ctr);
+    k_dissip_final<<<1, DRD_TPB, 0, s>>>(a, d, out, ctr);
+}
+void launch_threshold(long n, const double* x, double t, double* y, ull* ctr, cudaStream_t s) {
+    k_threshold<<<GRID(n)>>>(n, x, t, y, ctr);
 }
 void launch_mass_partial(int nr, int nz, const double* ph, const Dots& d, int slot, ull* ctr, cudaStream_t s) {
     k_mass_partial<<<d.G, DRD_TPB, 0, s>>>(nr, nz, ph, d, slot, ctr);

@@ -128,6 +128,15 @@ void launch_cell_add(long n, const double* x, double* y, ull* ctr, cudaStream_t 
 // ---- interpolate_coef / mass ----------------------------------------------------------
 void launch_interp_coef(const DevParams& P, const double* dist, const double* bdr, double* fpd, double* rho, double* eta,
                         ull* ctr, cudaStream_t s);
+// dissipation() diagnostics (microfluidics_complex_domain/dissipation.f90): out[6] = e1, e2, e3,
+// e4, dissip, mass; uses partial slots 0-3.
+struct DissipArgs {
+    int nr, nz;
+    double dr, dz, xld, ca, eps, vs, angle;
+};
+void launch_dissipation(const DissipArgs& a, const double* u, const double* v, const double* ph, const double* rmu,
+                        const double* angB, const double* angT, const Dots& d, double* out, ull* ctr, cudaStream_t s);
+void launch_threshold(long n, const double* x, double t, double* y, ull* ctr, cudaStream_t s);  // y = x > t
 void launch_two_phase_coef(const DevParams& P, long cs, const double* fpd, const double* ph, double* rho, double* eta,
                            float* rho32, float* eta32, ull* ctr, cudaStream_t s);
 

@@ -100,6 +100,7 @@ struct drd_ctx {
     KState* ks;      // device, KS_COUNT entries
     CallArgs* ca;    // device
     double* d_mass;  // device
+    double* d_diag;  // device: the dissipation diagnostics (e1, e2, e3, e4, dissip, mass)
     KState* h_ks;    // pinned
     CallArgs* h_ca;  // pinned
     double* h_mass;  // pinned
@@ -165,6 +166,7 @@ size_t arena_need(long cs, long us, long vs, long nc, long nr, long nz, long nma
     add(cs, 8); add(us, 8); add(vs, 8);                        // rmu_pre3, u_pre3, v_pre3
     add(sizeof(GridBar), 1);                                   // bar
     add(128, 8);                                               // pprof
+    add(8, 8);                                                 // d_diag
     const long fu = (nr / 2 + 1) * (nr / 2 + 2), nes = 3 * (us + vs);
     add(fu, 8); add(fu, 8); add(fu, 4); add(fu, 4);            // f1ue, f1uo (+ FP32)
     for (int i = 0; i < 2; ++i) { add(nes, 8); add(nes, 4); }  // es64, es32
@@ -1144,6 +1146,7 @@ int setup_context(drd_ctx* c) {
     c->rmu_pre3 = carve<double>(c, c->cs); c->u_pre3 = carve<double>(c, c->us); c->v_pre3 = carve<double>(c, c->vs);
     c->bar = (GridBar*)carve<char>(c, sizeof(GridBar));
     c->pprof = (unsigned long long*)carve<double>(c, 128);
+    c->d_diag = carve<double>(c, 8);
     c->Ku = nr / 2 + 1; c->Nue = (nr + 2) / 2; c->Nuo = (nr + 1) / 2;
     const long fu = (long)c->Ku * c->Nue, nes = 3 * ((long)(nr + 1) * nz + (long)nr * (nz - 1));
     c->f1ue = carve<double>(c, fu); c->f1uo = carve<double>(c, fu);
@@ -1263,6 +1266,39 @@ int finish_call(drd_ctx* c, int slot, drd_status* st, bool has_solve) {
     }
     if (st) { memset(st, 0, sizeof(*st)); st->seconds = ms * 1e-3; }
     return DRD_OK;
+}
+
+extern "C" int set_ori_walls(drd_ctx* c, const double* angleB, const double* angleT, double alpha_s);
+
+// finit's wall smoothing (finit.f90:120-189; reinint_by_PhSolve.f90:12-70 repeats it): ph =
+// bdr_in with Neumann ghosts, rmu from ph, nsteps PhSolve_ori steps, then the clipped
+// (ph + 1)/2 in c->w.
+int wall_smoothing(drd_ctx* c, const double* bdr_in, int nsteps, double* bdr_out, double* ph_out, double* rmu_out) {
+    int rc = set_ori_walls(c, nullptr, nullptr, 0.0);
+    if (rc) return rc;
+    double* ph = c->fld[DRD_F_PH];
+    double* rmu = c->fld[DRD_F_RMU];
+    const size_t cb = sizeof(double) * c->cs;
+    if (up(c, ph, bdr_in, c->cs)) return DRD_ERR_CUDA;                   // finit.f90:123-133
+    launch_fill_neumann(c->nr, c->nz, ph, nullptr, c->ctr, c->s);
+    CK(cudaMemsetAsync(c->fld[DRD_F_U], 0, sizeof(double) * c->us, c->s));  // u = v = 0 (mcl6.f90:143)
+    CK(cudaMemsetAsync(c->fld[DRD_F_V], 0, sizeof(double) * c->vs, c->s));
+    CK(cudaMemsetAsync(rmu, 0, cb, c->s));
+    launch_ori_rmu0(c->dp, ph, rmu, c->ctr, c->s);                        // finit.f90:163-169
+    int info = 0;
+    for (int it = 0; it < nsteps; ++it) {                                 // finit.f90:172-176
+        rc = run_graph(c, gkey(GK_ORI, mixed_of(c), 0), [&](cudaStream_t s) { return enq_ori(c, s); }, 0.0, 0.0);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(rmu, c->rmu_after, cb, cudaMemcpyDeviceToDevice, c->s));
+        CK(cudaMemcpyAsync(ph, c->ph_after, cb, cudaMemcpyDeviceToDevice, c->s));
+    }
+    launch_ori_bdr(c->nr, c->nz, ph, c->w, c->ctr, c->s);                 // finit.f90:178-189
+    CK(cudaGetLastError());
+    if (down(c, bdr_out, c->w, c->cs) | down(c, ph_out, ph, c->cs) | down(c, rmu_out, rmu, c->cs)) return DRD_ERR_CUDA;
+    CK(cudaMemcpyAsync(c->h_ks + KS_CH, c->ks + KS_CH, sizeof(KState), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    if (nsteps > 0) info = c->h_ks[KS_CH].info;
+    return info;
 }
 
 }  // namespace
@@ -1561,32 +1597,51 @@ int drd_phsolve_ori(drd_ctx* c, const double* u, const double* v, const double* 
 int drd_finit_wall(drd_ctx* c, const double* bdr_in, int nsteps, double* bdr_out, double* ph_out, double* rmu_out) {
     if (!c || !bdr_in || nsteps < 0) return DRD_ERR_BADARG;
     if (c->P.variant != DRD_VARIANT_MF) { c->err = "finit's wall smoothing belongs to the MF variant"; return DRD_ERR_BADARG; }
-    int rc = set_ori_walls(c, nullptr, nullptr, 0.0);
-    if (rc) return rc;
-    double* ph = c->fld[DRD_F_PH];
-    double* rmu = c->fld[DRD_F_RMU];
-    const size_t cb = sizeof(double) * c->cs;
-    if (up(c, ph, bdr_in, c->cs)) return DRD_ERR_CUDA;                   // finit.f90:123-133
-    launch_fill_neumann(c->nr, c->nz, ph, nullptr, c->ctr, c->s);
-    CK(cudaMemsetAsync(c->fld[DRD_F_U], 0, sizeof(double) * c->us, c->s));  // u = v = 0 (mcl6.f90:143)
-    CK(cudaMemsetAsync(c->fld[DRD_F_V], 0, sizeof(double) * c->vs, c->s));
-    CK(cudaMemsetAsync(rmu, 0, cb, c->s));
-    launch_ori_rmu0(c->dp, ph, rmu, c->ctr, c->s);                        // finit.f90:163-169
-    int info = 0;
-    for (int it = 0; it < nsteps; ++it) {                                 // finit.f90:172-176
-        rc = run_graph(c, gkey(GK_ORI, mixed_of(c), 0), [&](cudaStream_t s) { return enq_ori(c, s); }, 0.0, 0.0);
-        if (rc) return rc;
-        CK(cudaMemcpyAsync(rmu, c->rmu_after, cb, cudaMemcpyDeviceToDevice, c->s));
-        CK(cudaMemcpyAsync(ph, c->ph_after, cb, cudaMemcpyDeviceToDevice, c->s));
-    }
-    launch_ori_bdr(c->nr, c->nz, ph, c->w, c->ctr, c->s);                 // finit.f90:178-189
+    return wall_smoothing(c, bdr_in, nsteps, bdr_out, ph_out, rmu_out);
+}
+
+int drd_reinint_by_phsolve(drd_ctx* c, const double* bdr_in, double* bdr_out, double* pen_out) {
+    if (!c || !bdr_in) return DRD_ERR_BADARG;
+    // reinint_by_PhSolve.f90:34-70: the wall smoothing of finit, 51 PhSolve_ori steps
+    const int info = wall_smoothing(c, bdr_in, 51, nullptr, nullptr, nullptr);
+    if (info < 0 && info != -10 && info != -11) return info;
+    // the smoothed indicator becomes bdr_ph, and :78-86 the penalty mask over the ghosted array
+    CK(cudaMemcpyAsync(c->bdr, c->w, sizeof(double) * c->cs, cudaMemcpyDeviceToDevice, c->s));
+    launch_threshold(c->cs, c->bdr, 0.5, c->pen, c->ctr, c->s);
     CK(cudaGetLastError());
-    if (down(c, bdr_out, c->w, c->cs) | down(c, ph_out, ph, c->cs) | down(c, rmu_out, rmu, c->cs)) return DRD_ERR_CUDA;
-    CK(cudaMemcpyAsync(c->h_ks + KS_CH, c->ks + KS_CH, sizeof(KState), cudaMemcpyDeviceToHost, c->s));
+    int rc = refresh_fp32(c);
+    if (rc) return rc;
+    if (down(c, bdr_out, c->bdr, c->cs) | down(c, pen_out, c->pen, c->cs)) return DRD_ERR_CUDA;
     CK(cudaStreamSynchronize(c->s));
-    if (nsteps > 0) info = c->h_ks[KS_CH].info;
     return info;
 }
+
+int drd_dissipation(drd_ctx* c, const double* u, const double* v, const double* ph, const double* rmu,
+                    const double* angleB, const double* angleT, double vs, drd_diagnostics* out) {
+    if (!c || !out) return DRD_ERR_BADARG;
+    CK(cudaEventRecord(c->ev0, c->s));
+    // caller arrays go to scratch that the next solve rewrites; NULL keeps the resident field
+    const double* du = u ? c->u_after : c->fld[DRD_F_U];
+    const double* dv = v ? c->v_after : c->fld[DRD_F_V];
+    const double* dph = ph ? c->ph_after : c->fld[DRD_F_PH];
+    const double* drmu = rmu ? c->rmu_after : c->fld[DRD_F_RMU];
+    if (up(c, c->u_after, u, c->us) | up(c, c->v_after, v, c->vs) | up(c, c->ph_after, ph, c->cs) |
+        up(c, c->rmu_after, rmu, c->cs) | up(c, c->pnb, angleB, c->nr) | up(c, c->pnt, angleT, c->nr))
+        return DRD_ERR_CUDA;
+    DissipArgs a{};
+    a.nr = c->nr; a.nz = c->nz; a.dr = c->P.dr; a.dz = c->P.dz; a.xld = c->P.xld; a.ca = c->P.ca;
+    a.eps = c->P.I_thickness; a.vs = vs; a.angle = c->P.angle;
+    launch_dissipation(a, du, dv, dph, drmu, angleB ? c->pnb : nullptr, angleT ? c->pnt : nullptr, dots(c), c->d_diag,
+                       c->ctr, c->s);
+    CK(cudaGetLastError());
+    double h[6];
+    CK(cudaMemcpyAsync(h, c->d_diag, sizeof(h), cudaMemcpyDeviceToHost, c->s));
+    int rc = finish_call(c, 0, nullptr, false);
+    if (rc) return rc;
+    out->e1 = h[0]; out->e2 = h[1]; out->e3 = h[2]; out->e4 = h[3]; out->dissip = h[4]; out->mass = h[5];
+    return DRD_OK;
+}
+
 
 int drd_checkpoint_wait(drd_ctx* c) {
     if (!c) return DRD_ERR_BADARG;

@@ -71,3 +71,17 @@ def output_particles(path, points):
     pts = np.ascontiguousarray(points, dtype=np.float64)
     if L.drd_output_particles(str(path).encode(), pts.shape[1], ptr(pts)) != 0:
         raise OSError(f"drd_output_particles failed for {path}")
+
+
+def write_fort23(path, t, diss, lib=None):
+    """Append dissipation's fort.23 record (t, e1, e2, e3, e4, dissip in format 6e14.7)."""
+    L = lib or _lib.load()
+    if L.drd_write_fort23(str(path).encode(), float(t), C.byref(diss)) != 0:
+        raise OSError(f"drd_write_fort23 failed for {path}")
+
+
+def write_fort22(path, kcount, dt, diss, lib=None):
+    """Append mcl6's fort.22 record (kcount, dt*dissip, mass)."""
+    L = lib or _lib.load()
+    if L.drd_write_fort22(str(path).encode(), int(kcount), float(dt), C.byref(diss)) != 0:
+        raise OSError(f"drd_write_fort22 failed for {path}")

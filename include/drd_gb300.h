@@ -189,6 +189,16 @@ int drd_phsolve_ori(drd_ctx* ctx, const double* u, const double* v, const double
  * Returns the last solve's INFO. */
 int drd_finit_wall(drd_ctx* ctx, const double* bdr_ph_in, int nsteps, double* bdr_ph_out, double* ph_out,
                    double* rmu_out);
+/* reinint_by_PhSolve() (two_phase_flow_complex_domain/reinint_by_PhSolve.f90:1-91): the same
+ * 51 PhSolve_ori steps from ph = bdr_ph (unit mobility, Neumann sides and walls, on a context
+ * whose dt is 1e-4, :34-56), bdr_ph = (ph + 1)/2 clipped to [0, 1] on the interior (:58-70),
+ * then bdr_ph_penalty = 1 where bdr_ph > 0.5, else 0, over the whole ghosted array (:78-86).
+ * bdr_ph_in, bdr_ph_out, bdr_ph_penalty_out are CELL (outputs may be NULL).  Like the
+ * reference, which rewrites these module globals, it makes the results the context's bdr_ph
+ * and penalty mask; the resident u, v, ph and rmu are overwritten.  The mobilities are left as
+ * they are (the reference sets ph_M_0 = ph_M_inner = 1 for its loop): a caller rebuilds them
+ * and bdr_ph_grad from the new bdr_ph with drd_set_coefs.  Any variant. */
+int drd_reinint_by_phsolve(drd_ctx* ctx, const double* bdr_ph_in, double* bdr_ph_out, double* bdr_ph_penalty_out);
 
 /* ---- fiber particles coupled to the flow (microfluidics_complex_domain/particles_move.f90) --
  *
@@ -279,6 +289,34 @@ int drd_presolve_2(drd_ctx* ctx, const double* u, const double* v, double coef, 
 
 /* Mass sum of dissipation() (microfluidics_complex_domain/dissipation.f90:116-122), FP64. */
 int drd_mass(drd_ctx* ctx, const double* ph, double* mass);
+
+/* The diagnostics of dissipation(ph_pre, dissip, mass, t) (microfluidics_complex_domain/
+ * dissipation.f90:1-122), in FP64 on the device with a fixed summation order:
+ *   e1 = xld ca dr dz sum_cells |grad rmu|^2          (central differences over rmu's ghosts, :39-47)
+ *   e2 = vs ca eps^2 dr sum_i (wall residual of the contact-angle condition)^2 at the top and
+ *        bottom rows, with cf = sqrt2 cos(angle pi/180)/3 pi/2/eps (:49-57)
+ *   e3 = dr dz sum_{i=0..nr, k=0..nz} Cx Cz (u_x^2 + v_z^2 + u_z^2 + v_x^2), Cx, Cz = 1/2 at
+ *        the ends (:59-88), u_z and v_z one-sided in the wall rows as :68-77 writes them
+ *   e4 = 0: the slip term (:91-99) runs only for xlsB >= 1e-8, which this library rejects
+ *   dissip = e1 + e2 + e3 + e4; mass = sum ph dr dz (:113-122)
+ * The reference's e3 is not fully defined: it passes v to dif1x through a dummy of u's shape
+ * (leading dimension nr+3 instead of nr+2) and sums vvb where only its two wall rows were
+ * assigned.  Here every derivative is taken on the field's own grid: v_x and v_z by central
+ * differences on v(-1:nr, 0:nz), one-sided at i = nr and in the wall rows.
+ * u (UFACE), v (VFACE), ph, rmu (CELL) may be NULL for the resident fields; angleB, angleT
+ * (XLINE, degrees) NULL for params.angle everywhere; vs is the deck's slip coefficient (line 4). */
+typedef struct drd_diagnostics {
+    double e1, e2, e3, e4, dissip, mass;
+} drd_diagnostics;
+int drd_dissipation(drd_ctx* ctx, const double* u, const double* v, const double* ph, const double* rmu,
+                    const double* angleB, const double* angleT, double vs, drd_diagnostics* out);
+/* The two diagnostic records mcl6 appends per output step: fort.23's `write(23,110) t, e1, e2,
+ * e3, e4, dissip` with format 6e14.7 (dissipation.f90:103-105), and fort.22's
+ * `write(22,*) kcount, dt*dissip, mass` (mcl6.f90:235, :361), written here as one integer and
+ * two values in E format with 16 significant digits (list-directed layout is the compiler's
+ * choice).  Each call appends one line to `path`. */
+int drd_write_fort23(const char* path, double t, const drd_diagnostics* d);
+int drd_write_fort22(const char* path, int kcount, double dt, const drd_diagnostics* d);
 
 /* ---- resident-state time stepping (the mcl6 step sequence on device) ------------------- */
 

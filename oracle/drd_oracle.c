@@ -1348,6 +1348,82 @@ void orc_interpolate_coef(const drd_params* P, const double* dist, const double*
     }
 }
 
+/* reinint_by_PhSolve (two_phase_flow_complex_domain/reinint_by_PhSolve.f90:1-91): finit's wall
+ * smoothing (51 PhSolve_ori steps, :12-70), then bdr_ph_penalty = 1 where bdr_ph > 0.5 over
+ * the whole ghosted array (:78-86). */
+int orc_reinint_by_phsolve(const drd_params* P, const double* ph_lcc, const double* bdr_in, double* bdr_out,
+                           double* pen_out) {
+    const int info = orc_finit_wall(P, ph_lcc, bdr_in, 51, bdr_out, NULL, NULL);
+    const long cs = cell_size(P->nr, P->nz);
+    for (long q = 0; q < cs; ++q) pen_out[q] = bdr_out[q] > 0.5 ? 1.0 : 0.0;
+    return info;
+}
+
+/* dissipation (microfluidics_complex_domain/dissipation.f90:1-122) with setup's derivative
+ * coefficients xa1 = -1/2/dr, xb1 = 0, xc1 = -xa1 (setup.f90:9-19) in dif1x / dif1y's
+ * expression ua u(i-1) + ub u(i) + uc u(i+1) (setup.f90:269-307).  Where the reference is not
+ * defined (v handed to dif1x through a dummy of u's shape, vvb summed where only its wall rows
+ * were assigned), v_x and v_z are taken on v's own grid, one-sided at i = nr and in the wall
+ * rows like u_z (:68-77).  angB/angT NULL: P->angle everywhere.  out: e1 e2 e3 e4 dissip mass. */
+void orc_dissipation(const drd_params* P, const double* u, const double* v, const double* ph, const double* rmu,
+                     const double* angB, const double* angT, double vs, double* out) {
+    const int nr = P->nr, nz = P->nz;
+    const double dr = P->dr, dz = P->dz, eps = P->I_thickness;
+    const double pi = 3.14159265358979323846264338327950288; /* global.f90:27 */
+    const double xa1 = -1.0 / 2.0 / dr, xb1 = 0.0, xc1 = -xa1;
+    const double ya1 = -1.0 / 2.0 / dz, yb1 = 0.0, yc1 = -ya1;
+#define UA(i, k) u[(long)((i) + 1) + (long)((k) + 1) * (nr + 3)]
+#define VA(i, k) v[(long)((i) + 1) + (long)(k) * (nr + 2)]
+    double e1 = 0.;
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) {
+            const double gx = (rmu[CI(i + 1, k)] - rmu[CI(i - 1, k)]) / 2.0 / dr;
+            const double gz = (rmu[CI(i, k + 1)] - rmu[CI(i, k - 1)]) / 2.0 / dz;
+            e1 = e1 + (gx * gx + gz * gz);
+        }
+    e1 = e1 * P->xld * P->ca * dr * dz;
+    double e2 = 0.;
+    for (int i = 0; i < nr; ++i) {
+        double cf = sqrt(2.0) * cos((angT ? angT[i] : P->angle) * pi / 180.0) / 3.0 * pi / 2. / eps;
+        double g = (ph[CI(i, nz)] - ph[CI(i, nz - 1)]) / dz - cf * cos(pi * (ph[CI(i, nz)] + ph[CI(i, nz - 1)]) / 2.0 / 2.);
+        e2 = e2 + g * g;
+        cf = sqrt(2.0) * cos((angB ? angB[i] : P->angle) * pi / 180.0) / 3.0 * pi / 2. / eps;
+        g = (ph[CI(i, -1)] - ph[CI(i, 0)]) / dz - cf * cos(pi * (ph[CI(i, 0)] + ph[CI(i, -1)]) / 2.0 / 2.);
+        e2 = e2 + g * g;
+    }
+    e2 = e2 * vs * P->ca * (eps * eps) * dr;
+    double e3 = 0.;
+    for (int k = 0; k <= nz; ++k)
+        for (int i = 0; i <= nr; ++i) {
+            const double uua = xa1 * UA(i - 1, k) + xb1 * UA(i, k) + xc1 * UA(i + 1, k);
+            double uub, vvb, vva;
+            if (k == 0) {
+                uub = (UA(i, k + 1) - UA(i, k)) / dz;
+                vvb = (VA(i, k + 1) - VA(i, k)) / dz;
+            } else if (k == nz) {
+                uub = (UA(i, k) - UA(i, k - 1)) / dz;
+                vvb = (VA(i, k) - VA(i, k - 1)) / dz;
+            } else {
+                uub = ya1 * UA(i, k - 1) + yb1 * UA(i, k) + yc1 * UA(i, k + 1);
+                vvb = ya1 * VA(i, k - 1) + yb1 * VA(i, k) + yc1 * VA(i, k + 1);
+            }
+            if (i < nr) vva = xa1 * VA(i - 1, k) + xb1 * VA(i, k) + xc1 * VA(i + 1, k);
+            else vva = (VA(nr, k) - VA(nr - 1, k)) / dr;
+            const double cx = (i == 0 || i == nr) ? 0.5 : 1.0, cz = (k == 0 || k == nz) ? 0.5 : 1.0;
+            e3 = e3 + cx * cz * ((uua * uua + vvb * vvb) + uub * uub + vva * vva);
+        }
+    e3 = e3 * dr * dz;
+#undef UA
+#undef VA
+    const double e4 = 0.0; /* :91-99 runs only for xlsB >= 1e-8 */
+    double m = 0.0;
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) m = m + ph[CI(i, k)];
+    out[0] = e1; out[1] = e2; out[2] = e3; out[3] = e4;
+    out[4] = e1 + e2 + e3 + e4;
+    out[5] = m * dr * dz;
+}
+
 /* The two-fluid coefficients that two_phase_flow_complex_domain/interpolate_coef.f90:91-112
  * keeps commented out: rho and eta_tmp piecewise in ph (1 at ph <= -1, the ratio at ph >= 1,
  * 1 + (ratio - 1) ph between), then eta = max(eta, eta_tmp) with eta = 1 + (lambda_eta - 1)

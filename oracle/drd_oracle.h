@@ -93,6 +93,10 @@ void orc_presolve(const drd_params* P, const double* pre_lcc, const double* u, c
 void orc_interpolate_coef(const drd_params* P, const double* dist, const double* bdr_ph,
                           double* fpd_ph, double* rho, double* eta);
 
+int orc_reinint_by_phsolve(const drd_params* P, const double* ph_lcc, const double* bdr_in, double* bdr_out,
+                           double* pen_out);
+void orc_dissipation(const drd_params* P, const double* u, const double* v, const double* ph, const double* rmu,
+                     const double* angB, const double* angT, double vs, double* out);
 void orc_two_phase_coef(const drd_params* P, const double* fpd_ph, const double* ph, double* rho, double* eta);
 double orc_mass(const drd_params* P, const double* ph);
 

@@ -69,6 +69,9 @@ def lib(openmp=False):
         L.orc_presolve.argtypes = [P, dp, dp, dp, C.c_double, dp]
         L.orc_interpolate_coef.argtypes = [P, dp, dp, dp, dp, dp]
         L.orc_two_phase_coef.argtypes = [P, dp, dp, dp, dp]
+        L.orc_reinint_by_phsolve.argtypes = [P, dp, dp, dp, dp]
+        L.orc_reinint_by_phsolve.restype = C.c_int
+        L.orc_dissipation.argtypes = [P, dp, dp, dp, dp, dp, dp, C.c_double, dp]
         L.orc_mass.argtypes = [P, dp]
         L.orc_mass.restype = C.c_double
         L.orc_ori_coef.argtypes = [P, C.c_double]
@@ -288,6 +291,19 @@ class Oracle:
         rho, eta = np.zeros_like(ph), np.zeros_like(ph)
         self.L.orc_two_phase_coef(C.byref(self.P), ptr(fpd_ph), ptr(ph), ptr(rho), ptr(eta))
         return rho, eta
+
+    def reinint_by_phsolve(self, bdr_ph):
+        """reinint_by_PhSolve -> (bdr_ph, bdr_ph_penalty, info)."""
+        b, pen = np.zeros_like(bdr_ph), np.zeros_like(bdr_ph)
+        info = self.L.orc_reinint_by_phsolve(C.byref(self.P), ptr(self.ph_lcc), ptr(bdr_ph), ptr(b), ptr(pen))
+        return b, pen, info
+
+    def dissipation(self, u, v, ph, rmu, vs, angleB=None, angleT=None):
+        """dissipation's (e1, e2, e3, e4, dissip, mass)."""
+        out = np.zeros(6)
+        self.L.orc_dissipation(C.byref(self.P), ptr(u), ptr(v), ptr(ph), ptr(rmu), ptr(angleB), ptr(angleT), vs,
+                               ptr(out))
+        return tuple(float(x) for x in out)
 
     def mass(self, ph):
         return self.L.orc_mass(C.byref(self.P), ptr(ph))

@@ -54,7 +54,7 @@ def _c_layout(struct, fields):
 @pytest.mark.parametrize("cls,name", [(abi.drd_params, "drd_params"), (abi.drd_status, "drd_status"),
                                       (abi.drd_step_stats, "drd_step_stats"),
                                       (abi.drd_particle_params, "drd_particle_params"),
-                                      (abi.drd_deck, "drd_deck")])
+                                      (abi.drd_deck, "drd_deck"), (abi.drd_diagnostics, "drd_diagnostics")])
 def test_struct_layout_matches_header(cls, name):
     fields = [f for f, _ in cls._fields_]
     got = _c_layout(name, fields)
