@@ -53,7 +53,9 @@ def test_reinint_by_phsolve_matches_oracle(cuda_lib, oracle_build):
     b, pen, info = ctx.reinint_by_PhSolve(sharp)
     bo, peno, info_o = Oracle(P).reinint_by_phsolve(sharp)
     assert info == 0 and info_o == 0
-    assert rel_err(b, bo) < 1e-8
+    # 51 smoothing steps from a sharp mask: the oracle against itself, tol 1e-13 against 1e-14,
+    # moves bdr_ph by 1.8e-7 here (its unclipped ghost rows carry the largest values)
+    assert rel_err(b, bo) < 1e-7
     decided = np.abs(bo - 0.5) > 1e-6
     assert np.array_equal(pen[decided], peno[decided])
     # both became the context's: the TP momentum operator now penalises with the new mask
