@@ -25,6 +25,13 @@ SIGNATURES = {
     "drd_set_tp_fields": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
     "drd_interpolate_coef": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
     "drd_two_phase_coef": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
+    "drd_batch_create": (C.c_int, [C.c_int, C.POINTER(abi.drd_batch_problem), C.c_int, C.POINTER(C.c_void_p)]),
+    "drd_batch_run": (C.c_int, [C.c_void_p, _dp]),
+    "drd_batch_result": (C.c_int, [C.c_void_p, C.c_int, _dp, _st]),
+    "drd_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp]),
+    "drd_batch_destroy": (C.c_int, [C.c_void_p]),
+    "drd_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "drd_batch_length": (C.c_long, [C.c_int, C.c_int, C.c_int]),
     "drd_reinint_by_phsolve": (C.c_int, [_ctx, _dp, _dp, _dp]),
     "drd_dissipation": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.POINTER(abi.drd_diagnostics)]),
     "drd_write_fort23": (C.c_int, [C.c_char_p, C.c_double, C.POINTER(abi.drd_diagnostics)]),

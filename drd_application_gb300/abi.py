@@ -85,6 +85,16 @@ class drd_diagnostics(C.Structure):
         return (self.e1, self.e2, self.e3, self.e4, self.dissip, self.mass)
 
 
+DRD_SYS_PRESSURE = 2  # batched variable-coefficient pressure Poisson systems
+DRD_BATCH_MAX_LINE = 2048
+
+
+class drd_batch_problem(C.Structure):
+    """One system of a batch (drd_batch_create)."""
+    _fields_ = [("system", C.c_int32), ("bdf", C.c_int32), ("params", drd_params)] + [
+        (n, C.POINTER(C.c_double)) for n in ("rho", "eta", "bdr_ph", "b", "x0")]
+
+
 PARTICLES_MAX = 64
 
 

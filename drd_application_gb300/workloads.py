@@ -25,10 +25,12 @@ Workloads:
         dr = dz = 1/512.
 Any workload can be built at another grid size; geometry lengths scale with the grid.
 
-  C3 (make_c3_solve): independent momentum solves, A x = b with the VeloSolve_2_combined
-        operator, on a grid drawn from {64x32, 128x64, 256x128, 420x180, 512x256}; the solid is
-        2 to 6 disks of radius 5 to 25 cells, eta = 1 + 99 mask; b is a Gaussian random field
-        (white noise filtered by exp(-k^2 l^2 / 2), l = 8 cells, unit variance, rounded to FP32).
+  C3 (make_c3_solve, make_c3_pressure): independent momentum solves, A x = b with the
+        VeloSolve_2_combined operator, and pressure Poisson solves, div(beta grad psi) = b with
+        beta = 1/(1 + penalty_k dt mask), on a grid drawn from {64x32, 128x64, 256x128, 420x180,
+        512x256}; the solid is 2 to 6 disks of radius 5 to 25 cells, eta = 1 + 99 mask; b is a
+        Gaussian random field (white noise filtered by exp(-k^2 l^2 / 2), l = 8 cells, unit
+        variance, rounded to FP32; zero mean for the pressure systems).
 """
 import math
 
@@ -126,9 +128,9 @@ def _grf(rng, shape, ell=8.0):
     return f.astype(np.float32).astype(np.float64)
 
 
-def make_c3_solve(seed, index, size=None, precision=abi.DRD_PREC_MIXED, **overrides):
-    """Solve `index` of the seeded C3 batch: (params, coefs, b) for DRDContext.solve(DRD_SYS_UV)."""
-    rng = np.random.default_rng([seed, index])
+def _c3_params_mask(rng, size, precision, overrides):
+    """Grid (drawn from C3_SIZES unless given), parameters and the seeded mask of 2 to 6 disks of
+    radius 5 to 25 cells, smoothed by tanh over 0.75 cells."""
     nr, nz = size if size is not None else C3_SIZES[int(rng.integers(len(C3_SIZES)))]
     p = abi.default_params(nr, nz, re=0.5, ca=0.05, lambda_rho=1.0, lambda_eta=1.0, penalty_k=1.0e4)
     p.dr, p.dz = 1.0 / nz, 1.0 / nz
@@ -147,6 +149,25 @@ def make_c3_solve(seed, index, size=None, precision=abi.DRD_PREC_MIXED, **overri
     bdr = np.zeros(cell_shape(nr, nz))
     bdr[1:-1, 1:-1] = 0.5 * (1.0 - np.tanh(d / 0.75))
     neumann_ghosts_cell(bdr)
+    return p, bdr, disks
+
+
+def make_c3_pressure(seed, index, size=None, precision=abi.DRD_PREC_MIXED, **overrides):
+    """Pressure system `index` of the seeded C3 batch: (params, bdr_ph, b) for the batched
+    variable-coefficient Poisson solve (DRD_SYS_PRESSURE).  b is a Gaussian random field rounded to
+    FP32, then its mean is removed in FP64 so that it lies in the operator's range."""
+    rng = np.random.default_rng([seed, index, 2])
+    p, bdr, disks = _c3_params_mask(rng, size, precision, overrides)
+    b = _grf(rng, (p.nz, p.nr)).ravel()
+    b = b - b.mean()
+    return p, bdr, b, {"disks": disks}
+
+
+def make_c3_solve(seed, index, size=None, precision=abi.DRD_PREC_MIXED, **overrides):
+    """Solve `index` of the seeded C3 batch: (params, coefs, b) for DRDContext.solve(DRD_SYS_UV)."""
+    rng = np.random.default_rng([seed, index])
+    p, bdr, disks = _c3_params_mask(rng, size, precision, overrides)
+    nr, nz = p.nr, p.nz
     M = 1.0 - bdr
     coefs = {"rho": np.ones(cell_shape(nr, nz)), "eta": 1.0 + 99.0 * bdr, "bdr_ph": bdr,
              "bdr_ph_grad": _grad_mag(bdr, dr=p.dr, dz=p.dz), "M0": M.copy(), "Mi": M.copy(), "bdr_pen": bdr.copy(),

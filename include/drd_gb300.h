@@ -470,6 +470,57 @@ long drd_op_length(drd_ctx* ctx, int op);
  * independent solves that do not come from a time step. */
 int drd_solve(drd_ctx* ctx, int system, int bdf, const double* b, double* x, drd_status* st);
 
+/* ---- batches of independent solves in one persistent launch --------------------------------
+ *
+ * Many independent systems of uneven grid sizes (no time step between them) are uploaded once
+ * and solved by ONE persistent kernel launch, captured in a CUDA graph: each thread block takes
+ * the next unsolved system from a device-side queue (largest first) and runs its whole
+ * mixed-precision solve (FP64 iterative refinement around FP32 BiCGSTAB, the refinement policy
+ * of the context solves: inner tolerance mixed_inner_tol, tenfold tighter after a sweep that
+ * gains less than 10 %, FP64 true residual judged against tol, at most mixed_max_refine sweeps
+ * and uv_maxit FP32 iterations per sweep).  Systems:
+ *   DRD_SYS_UV        the momentum operator of VeloSolve_2_combined (bdf 2) / VeloSolve_combined
+ *                     (bdf 1), MF variant, from rho, eta and the penalty mask bdr_ph, with the
+ *                     Jacobi preconditioner of PSolve_uv_2_CG (VeloSolve_2_combined.f90:515-711)
+ *   DRD_SYS_PRESSURE  a variable-coefficient pressure Poisson operator that the reference does
+ *                     not have (its PreSolve_2 is a direct DCT solve): A psi = d/dx(beta dpsi/dx)
+ *                     + d/dz(beta dpsi/dz) on the nr x nz cells, beta = 1/(1 + penalty_k dt
+ *                     bdr_ph), face values the mean of the two cells, zero flux through the
+ *                     domain faces; preconditioned by PreSolve_2's DCT solve (dct_fftw.f90:3-54:
+ *                     REDFT10, / Pre_Lcc, REDFT01, / 4 nr nz), in FP32 by FFT.  The constant
+ *                     field is its null space: b must sum to zero.
+ * Packed vectors: DRD_SYS_UV the Atob_uv order (drd_op_length); DRD_SYS_PRESSURE nr*nz, i fastest.
+ * Limits: nr, nz <= DRD_BATCH_MAX_LINE; pressure grids need nr and nz of the form 2^a 3^b 5^c 7^d. */
+#define DRD_SYS_PRESSURE 2
+#define DRD_BATCH_MAX_LINE 2048
+typedef struct drd_batch_problem {
+    int32_t system;     /* DRD_SYS_UV or DRD_SYS_PRESSURE                                           */
+    int32_t bdf;        /* DRD_SYS_UV: 1 or 2                                                       */
+    drd_params params;  /* nr, nz, dr, dz, dt, re, penalty_k, tol, mixed_inner_tol,
+                           mixed_max_refine, uv_maxit; variant MF                                   */
+    const double* rho;    /* CELL; DRD_SYS_UV only                                                  */
+    const double* eta;    /* CELL; DRD_SYS_UV only                                                  */
+    const double* bdr_ph; /* CELL: the penalty mask (DRD_SYS_UV) or the resistance giving beta     */
+    const double* b;      /* packed right-hand side                                                  */
+    const double* x0;     /* packed initial guess, NULL = zero                                       */
+} drd_batch_problem;
+typedef struct drd_batch drd_batch;
+/* Uploads every system (coefficients in FP64 and FP32, right-hand sides, guesses) and builds the
+ * FFT plans and tables; tunes the launch shape (threads per block, blocks per SM) by timing the
+ * candidates on the batch itself when `autotune` is nonzero. */
+int drd_batch_create(int nprob, const drd_batch_problem* probs, int autotune, drd_batch** out);
+/* Solves every system from its x0 in one persistent launch (a captured graph) on the batch's
+ * stream; *seconds receives the device time of the launch (CUDA events). */
+int drd_batch_run(drd_batch* b, double* seconds);
+/* Solution and status of system i after drd_batch_run (x: packed, may be NULL). */
+int drd_batch_result(drd_batch* b, int i, double* x, drd_status* st);
+/* Launch shape in use: threads per block, blocks per SM; algorithmic bytes of the last run. */
+int drd_batch_info(drd_batch* b, int* threads, int* blocks_per_sm, double* bytes_last_run);
+int drd_batch_destroy(drd_batch* b);
+const char* drd_batch_last_error(drd_batch* b);
+/* Packed length of a batch system. */
+long drd_batch_length(int system, int nr, int nz);
+
 /* ---- learned initial guess ---------------------------------------------------------------
  * A 4-level U-Net (channels 32/64/128/256, 3x3 convolutions with ReLU, 2x2 average pooling,
  * nearest upsampling, concatenated skips, a 1x1 output convolution) in BF16 weights and

@@ -1141,6 +1141,68 @@ int orc_solve_system(const drd_params* P, int system, int bdf, const double* ph_
     return orc_bicgstab(uv_len(P->nr, P->nz), b, x, P->uv_maxit, P->tol, uv_mv_cb, uv_ps_cb, &C, st);
 }
 
+/* The variable-coefficient pressure Poisson operator of the batched solves (no reference
+ * counterpart: PreSolve_2 is a direct DCT solve): y = d/dx(beta dx/dx) + d/dz(beta dx/dz) on the
+ * packed nr x nz cells, beta = 1/(1 + penalty_k dt bdr_ph), face values the mean of the two
+ * cells, zero flux through the domain faces. */
+void orc_pressure_matvec(const drd_params* P, const double* bdr_ph, const double* x, double* y) {
+    const int nr = P->nr, nz = P->nz;
+    const double idr2 = 1.0 / (P->dr * P->dr), idz2 = 1.0 / (P->dz * P->dz);
+    double* beta = dalloc((long)nr * nz);
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) beta[i + (long)nr * k] = 1.0 / (1.0 + P->penalty_k * P->dt * bdr_ph[CI(i, k)]);
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) {
+            const long q = i + (long)nr * k;
+            const double c = x[q], bc = beta[q];
+            double fx = 0.0, fz = 0.0;
+            if (i + 1 < nr) fx += (bc + beta[q + 1]) * 0.5 * (x[q + 1] - c);
+            if (i > 0) fx -= (bc + beta[q - 1]) * 0.5 * (c - x[q - 1]);
+            if (k + 1 < nz) fz += (bc + beta[q + nr]) * 0.5 * (x[q + nr] - c);
+            if (k > 0) fz -= (bc + beta[q - nr]) * 0.5 * (c - x[q - nr]);
+            y[q] = fx * idr2 + fz * idz2;
+        }
+    free(beta);
+}
+
+/* PreSolve_2's DCT solve as a preconditioner (dct_fftw.f90:3-54): y = REDFT01(REDFT10(x) /
+ * Pre_Lcc) / (4 nr nz) on the packed cells. */
+void orc_pressure_psolve(const drd_params* P, const double* pre_lcc, const double* x, double* y) {
+    const int nr = P->nr, nz = P->nz;
+    const long n = (long)nr * nz;
+    memcpy(y, x, sizeof(double) * n);
+    orc_redft10(nr, nz, y, nr, 1);
+    orc_redft10(nz, nr, y, 1, nr);
+    for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nr; ++i) y[i + (long)nr * k] = y[i + (long)nr * k] / pre_lcc[i + (long)(nr + 1) * k];
+    orc_redft01(nr, nz, y, nr, 1);
+    orc_redft01(nz, nr, y, 1, nr);
+    const double scale = 4.0 * nr * nz;
+    for (long q = 0; q < n; ++q) y[q] = y[q] / scale;
+}
+
+typedef struct { const drd_params* P; const double* pre_lcc; const double* bdr; double* tmp; } pr_ctx;
+static void pr_mv_cb(void* c, double a, const double* x, double b, double* y) {
+    pr_ctx* C = (pr_ctx*)c;
+    const long n = (long)C->P->nr * C->P->nz;
+    orc_pressure_matvec(C->P, C->bdr, x, C->tmp);
+    for (long q = 0; q < n; ++q) y[q] = a * C->tmp[q] + (b == 0.0 ? 0.0 : b * y[q]);
+}
+static void pr_ps_cb(void* c, const double* x, double* y) {
+    pr_ctx* C = (pr_ctx*)c;
+    orc_pressure_psolve(C->P, C->pre_lcc, x, y);
+}
+
+/* A x = b for the pressure Poisson system with the reference BiCGSTAB (lib/BiCGSTABREVCOM.f),
+ * P->uv_maxit iterations, tolerance P->tol; x: guess in, solution out. */
+int orc_pressure_solve(const drd_params* P, const double* pre_lcc, const double* bdr_ph, const double* b, double* x,
+                       drd_status* st) {
+    pr_ctx C = {P, pre_lcc, bdr_ph, dalloc((long)P->nr * P->nz)};
+    const int info = orc_bicgstab((long)P->nr * P->nz, b, x, P->uv_maxit, P->tol, pr_mv_cb, pr_ps_cb, &C, st);
+    free(C.tmp);
+    return info;
+}
+
 /* VeloSolve_combined (bdf 1) / VeloSolve_2_combined (bdf 2). */
 int orc_velosolve(const drd_params* P, int bdf, const double* psi1, const double* psi2,
                   const double* u_pre, const double* u, const double* v_pre, const double* v,

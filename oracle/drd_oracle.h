@@ -97,6 +97,10 @@ int orc_reinint_by_phsolve(const drd_params* P, const double* ph_lcc, const doub
                            double* pen_out);
 void orc_dissipation(const drd_params* P, const double* u, const double* v, const double* ph, const double* rmu,
                      const double* angB, const double* angT, double vs, double* out);
+void orc_pressure_matvec(const drd_params* P, const double* bdr_ph, const double* x, double* y);
+void orc_pressure_psolve(const drd_params* P, const double* pre_lcc, const double* x, double* y);
+int orc_pressure_solve(const drd_params* P, const double* pre_lcc, const double* bdr_ph, const double* b, double* x,
+                       drd_status* st);
 void orc_two_phase_coef(const drd_params* P, const double* fpd_ph, const double* ph, double* rho, double* eta);
 double orc_mass(const drd_params* P, const double* ph);
 

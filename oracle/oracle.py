@@ -69,6 +69,10 @@ def lib(openmp=False):
         L.orc_presolve.argtypes = [P, dp, dp, dp, C.c_double, dp]
         L.orc_interpolate_coef.argtypes = [P, dp, dp, dp, dp, dp]
         L.orc_two_phase_coef.argtypes = [P, dp, dp, dp, dp]
+        L.orc_pressure_matvec.argtypes = [P, dp, dp, dp]
+        L.orc_pressure_psolve.argtypes = [P, dp, dp, dp]
+        L.orc_pressure_solve.argtypes = [P, dp, dp, dp, dp, S]
+        L.orc_pressure_solve.restype = C.c_int
         L.orc_reinint_by_phsolve.argtypes = [P, dp, dp, dp, dp]
         L.orc_reinint_by_phsolve.restype = C.c_int
         L.orc_dissipation.argtypes = [P, dp, dp, dp, dp, dp, dp, C.c_double, dp]
@@ -285,6 +289,24 @@ class Oracle:
         self.L.orc_interpolate_coef(C.byref(self.P), ptr(np.ascontiguousarray(dist)), ptr(bdr_ph), ptr(fpd),
                                     ptr(rho), ptr(eta))
         return fpd, rho, eta
+
+    def pressure_matvec(self, bdr_ph, x):
+        """The batched solves' variable-coefficient pressure Poisson operator."""
+        y = np.zeros_like(x)
+        self.L.orc_pressure_matvec(C.byref(self.P), ptr(bdr_ph), ptr(np.ascontiguousarray(x)), ptr(y))
+        return y
+
+    def pressure_psolve(self, x):
+        """PreSolve_2's DCT solve on packed cells (the pressure systems' preconditioner)."""
+        y = np.zeros_like(x)
+        self.L.orc_pressure_psolve(C.byref(self.P), ptr(self.pre_lcc), ptr(np.ascontiguousarray(x)), ptr(y))
+        return y
+
+    def pressure_solve(self, bdr_ph, b, x0=None):
+        x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
+        st = abi.drd_status()
+        info = self.L.orc_pressure_solve(C.byref(self.P), ptr(self.pre_lcc), ptr(bdr_ph), ptr(b), ptr(x), C.byref(st))
+        return x, st, info
 
     def two_phase_coef(self, fpd_ph, ph):
         """The two-fluid rho, eta (two_phase_flow_complex_domain/interpolate_coef.f90:91-112)."""
