@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=None, help="timed steps of the plain FP64 path")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--c3-solves", type=int, default=512, help="independent momentum solves of the C3 batch (0: skip)")
+    ap.add_argument("--c3-solves", type=int, default=512,
+                    help="independent momentum and pressure systems of the C3 batch (0: skip)")
     ap.add_argument("--learned-steps", type=int, default=600,
                     help="Adam steps of the learned CH guess leg (0: skip)")
     ap.add_argument("--nr", type=int, default=420)
@@ -229,59 +230,75 @@ def run_reference(args, ws, rank):
 
 
 # ----------------------------------------------------------------------------------- GPU arm
-def time_c3(n_solves, seed):
-    """The C3 batch: independent mixed-precision momentum solves A x = b (VeloSolve_2_combined's
-    operator, 2 to 6 disks with eta = 1 + 99 mask, Gaussian-random-field b) on grids drawn from
-    five sizes, through the C-ABI (drd_set_coefs + drd_solve with host arrays).  Each solve's
-    coefficients and right-hand side are generated before its timed region."""
-    from drd_application_gb300 import abi
-    from drd_application_gb300.api import DRDContext
-    from drd_application_gb300.workloads import make_c3_solve
+def c3_systems(n_solves, seed):
+    """The C3 batch: n_solves independent systems on grids drawn from five sizes, alternately the
+    momentum operator of VeloSolve_2_combined (2 to 6 disks, eta = 1 + 99 mask) and the
+    variable-coefficient pressure Poisson operator (beta = 1/(1 + penalty dt mask)), each with a
+    Gaussian-random-field right-hand side."""
+    from drd_application_gb300.workloads import make_c3_pressure, make_c3_solve
 
-    ctxs = {}
-    total, iters, ok = 0.0, 0, 0
+    systems = []
     for i in range(n_solves):
-        P, coefs, b, _ = make_c3_solve(seed, i)
-        key = (P.nr, P.nz)
-        if key not in ctxs:
-            ctxs[key] = DRDContext(P)
-            # one untimed solve per grid size captures its graph and tunes its transforms
-            ctxs[key].set_coefs(coefs["rho"], coefs["eta"], coefs["bdr_ph"], coefs["bdr_ph_grad"], coefs["M0"],
-                                coefs["Mi"])
-            ctxs[key].solve(abi.DRD_SYS_UV, b)
-        ctx = ctxs[key]
-        ctx.synchronize()
-        t0 = time.perf_counter()
-        ctx.set_coefs(coefs["rho"], coefs["eta"], coefs["bdr_ph"], coefs["bdr_ph_grad"], coefs["M0"], coefs["Mi"])
-        x, st = ctx.solve(abi.DRD_SYS_UV, b)
-        total += time.perf_counter() - t0
-        iters += st.iter
-        ok += int(st.info == 0 and st.true_resid <= P.tol)
-    for c in ctxs.values():
-        c.close()
-    return {"solves": n_solves, "seconds": total, "solves_per_s": n_solves / total, "iters_mean": iters / n_solves,
-            "solves_to_fp64_1e-8": f"{ok}/{n_solves}", "sizes": sorted(f"{a}x{b}" for a, b in ctxs)}
+        if i % 2 == 0:
+            P, c, b, _ = make_c3_solve(seed, i)
+            systems.append(("uv", P, {"rho": c["rho"], "eta": c["eta"], "bdr_ph": c["bdr_ph"]}, b))
+        else:
+            P, bdr, b, _ = make_c3_pressure(seed, i)
+            systems.append(("pressure", P, bdr, b))
+    return systems
+
+
+def time_c3(n_solves, seed, runs=3):
+    """The C3 batch solved by ONE persistent launch under a CUDA graph (drd_batch_run): every
+    system's coefficients and right-hand side are uploaded once at creation (which also tunes the
+    launch shape and team sizes); each timed run solves all systems from a zero guess.  Device
+    time by CUDA events; the roofline uses the algorithmic bytes of the run's iterations."""
+    from drd_application_gb300.batch import Batch
+
+    systems = c3_systems(n_solves, seed)
+    t0 = time.perf_counter()
+    bt = Batch(systems, autotune=True)
+    create_s = time.perf_counter() - t0
+    bt.run()  # warm-up
+    secs = [bt.run() for _ in range(runs)]
+    info = bt.info()
+    st = [bt.status(i) for i in range(n_solves)]
+    ok = sum(int(s.info == 0 and s.true_resid <= systems[i][1].tol) for i, s in enumerate(st))
+    sec = statistics.median(secs)
+    kinds = {}
+    for (kind, P, *_), s in zip(systems, st):
+        kinds.setdefault(kind, []).append(s.iter)
+    bt.close()
+    return {"solves": n_solves, "seconds": sec, "solves_per_s": n_solves / sec, "runs_s": secs,
+            "launch": "one persistent cooperative launch in a CUDA graph",
+            "threads_per_block": info["threads"], "blocks_per_sm": info["blocks_per_sm"],
+            "create_and_tune_s": create_s, "achieved_GBps": info["bytes_last_run"] / secs[-1] / 1e9,
+            "iters_mean": {k: statistics.mean(v) for k, v in kinds.items()},
+            "systems": {k: len(v) for k, v in kinds.items()},
+            "solves_to_fp64_1e-8": f"{ok}/{n_solves}",
+            "sizes": sorted({f"{P.nr}x{P.nz}" for _, P, *_ in systems})}
 
 
 def cpu_c3_sample(seed, n=4, budget_s=20.0):
-    """The FP64 CPU restatement on the first solves of the same C3 batch (host cores, OpenMP
-    over transform lines; the momentum solve is Jacobi-preconditioned), up to budget_s."""
+    """The FP64 CPU restatement on the first systems of the same C3 batch (host cores, OpenMP
+    over transform lines; Jacobi-preconditioned momentum, DCT-preconditioned pressure), up to
+    budget_s."""
     from oracle.oracle import Oracle
-    from drd_application_gb300 import abi
-    from drd_application_gb300.workloads import make_c3_solve
 
     done, elapsed = 0, 0.0
-    for i in range(n):
-        P, coefs, b, _ = make_c3_solve(seed, i, precision=abi.DRD_PREC_FP64)
+    for kind, P, a, b in c3_systems(n, seed):
         orc = Oracle(P, openmp=True)
         t0 = time.perf_counter()
-        orc.solve(1, 2, coefs, b)
+        if kind == "uv":
+            orc.solve(1, 2, {"rho": a["rho"], "eta": a["eta"], "bdr_pen": a["bdr_ph"]}, b)
+        else:
+            orc.pressure_solve(a, b)
         elapsed += time.perf_counter() - t0
         done += 1
         if elapsed > budget_s:
             break
     return {"value": done / elapsed, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port", "cpu_model": cpu_model(),
-            "sample": f"first {done} solves of the same C3 batch, FP64 oracle, {elapsed:.1f} s"}
+            "sample": f"first {done} systems of the same C3 batch, FP64 oracle, {elapsed:.1f} s"}
 
 
 def time_learned(steps, nr, nz, train_seeds=8, per_seed=12):
@@ -515,6 +532,8 @@ def run_gpu(args, ws, rank, local):
     c3 = time_c3(args.c3_solves, rank) if args.c3_solves > 0 else None
     if c3 is not None:
         c3["solves_per_s"] = args.c3_solves * ws / max_over_ranks(dist, c3["seconds"])
+        c3["hbm_frac"] = c3["achieved_GBps"] / float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get(
+            "hbm_gbs", 6800.0)) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
         if rank == 0 and not args.no_cpu:
             c3["cpu_baseline"] = cpu_c3_sample(rank)
 

@@ -37,7 +37,9 @@ struct UVFetch {
 // Row q of MatrixVector_uv_2_CG (:515-646) / MatrixVector_uv_CG: (A x)_q.  The FP64 form keeps
 // the reference's expression; the FP32 form (the mixed mode's inner operator) takes differences
 // before scaling and multiplies by the reciprocals of dr^2, dz^2 and dr dz instead of dividing.
-template <typename T, class FX>
+// DIFF selects the difference form with reciprocal multiplies (the FP32 form) for either T; the
+// default keeps the reference's expression in FP64.
+template <typename T, class FX, bool DIFF = (sizeof(T) == 4)>
 __device__ __forceinline__ T uv_apply(const OpScal<T>& o, const T* __restrict__ rho, const T* __restrict__ eta,
                                       const T* __restrict__ pen, const FX& F, long q) {
     const int nr = o.nr;
@@ -55,13 +57,13 @@ __device__ __forceinline__ T uv_apply(const OpScal<T>& o, const T* __restrict__ 
         else
             val = f1 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i - 1, k)]) * h;
         T cr = E_(i, k), cl = E_(i - 1, k);
-        if constexpr (sizeof(T) == 4)
+        if constexpr (DIFF)
             val = val - T(2) * o.dt * (cr * (F.Uc(i + 1, k) - f1) + cl * (F.Uc(i - 1, k) - f1)) * o.idr2;
         else
             val = val - T(2) * o.dt * (cr * F.Uc(i + 1, k) + cl * F.Uc(i - 1, k) - (cl + cr) * f1) / o.dr2;
         cr = (E_(i, k + 1) + E_(i - 1, k + 1) + E_(i, k) + E_(i - 1, k)) * q4;
         cl = (E_(i, k) + E_(i - 1, k) + E_(i, k - 1) + E_(i - 1, k - 1)) * q4;
-        if constexpr (sizeof(T) == 4) {
+        if constexpr (DIFF) {
             val = val - o.dt * (cr * (F.U(i, k + 1) - f1) + cl * (F.U(i, k - 1) - f1)) * o.idz2;
             val = val - o.dt * (cr * (F.V(i, k + 1) - F.V(i - 1, k + 1)) - cl * (F.V(i, k) - F.V(i - 1, k))) * o.idrdz;
         } else {
@@ -77,13 +79,13 @@ __device__ __forceinline__ T uv_apply(const OpScal<T>& o, const T* __restrict__ 
         else
             val = f2 * mcoef * (rho[cidx(nr, i, k)] + rho[cidx(nr, i, k - 1)]) * h;
         T cr = E_(i, k), cl = E_(i, k - 1);
-        if constexpr (sizeof(T) == 4)
+        if constexpr (DIFF)
             val = val - T(2) * o.dt * (cr * (F.V(i, k + 1) - f2) + cl * (F.V(i, k - 1) - f2)) * o.idz2;
         else
             val = val - T(2) * o.dt * (cr * F.V(i, k + 1) + cl * F.V(i, k - 1) - (cl + cr) * f2) / o.dz2;
         cr = (E_(i + 1, k) + E_(i, k) + E_(i + 1, k - 1) + E_(i, k - 1)) * q4;
         cl = (E_(i, k) + E_(i - 1, k) + E_(i, k - 1) + E_(i - 1, k - 1)) * q4;
-        if constexpr (sizeof(T) == 4) {
+        if constexpr (DIFF) {
             val = val - o.dt * (cr * (F.V(i + 1, k) - f2) + cl * (F.V(i - 1, k) - f2)) * o.idr2;
             val = val - o.dt * (cr * (F.Uc(i + 1, k) - F.Uc(i + 1, k - 1)) - cl * (F.Uc(i, k) - F.Uc(i, k - 1))) * o.idrdz;
         } else {
