@@ -32,7 +32,7 @@ DRD_SYS_CH, DRD_SYS_UV = 0, 1  # drd_solve systems
 DRD_UV_JACOBI, DRD_UV_ESOLP = 0, 1  # drd_params.uv_precond
 
 (DRD_KB_UV_MATVEC_FP64, DRD_KB_UV_MATVEC_FP32, DRD_KB_DCT_X_FP64, DRD_KB_DCT_X_FP32, DRD_KB_DCT_Z_FP64,
- DRD_KB_DCT_Z_FP32, DRD_KB_CH_MATVEC_FP32) = range(7)
+ DRD_KB_DCT_Z_FP32, DRD_KB_CH_MATVEC_FP32, DRD_KB_PRESSURE_FFT64, DRD_KB_DCT2_FFT32) = range(9)
 KB_NAMES = {
     DRD_KB_UV_MATVEC_FP64: "k_uv_mv<double> (momentum stencil)",
     DRD_KB_UV_MATVEC_FP32: "k_uv_mv<float> (momentum stencil)",
@@ -41,6 +41,8 @@ KB_NAMES = {
     DRD_KB_DCT_Z_FP64: "k_gemm<double> DCT-I z pass",
     DRD_KB_DCT_Z_FP32: "k_gemm<float> DCT-I z pass",
     DRD_KB_CH_MATVEC_FP32: "k_ch_mv2<float> (CH stencil)",
+    DRD_KB_PRESSURE_FFT64: "k_pfft_* PreSolve_2 by FFT, FP64 (cold L2)",
+    DRD_KB_DCT2_FFT32: "k_pfft_* REDFT10 / Pre_Lcc / REDFT01, FP32 (cold L2)",
 }
 
 # resident-state fields (DRD_F_*)

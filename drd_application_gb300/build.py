@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIBNAME = "libdrd_gb300.so"
 SOURCES = ["drd_kernels.cu", "drd_solver.cu", "drd_noalloc.cu", "drd_particles.cu", "drd_unet.cu", "drd_batch.cu",
-           "drd_io.cpp"]
+           "drd_pressure_fft.cu", "drd_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr"]
 

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "drd_common.cuh"
+#include "drd_fft.cuh"
 
 namespace drd {
 
@@ -136,6 +137,19 @@ struct DissipArgs {
 };
 void launch_dissipation(const DissipArgs& a, const double* u, const double* v, const double* ph, const double* rmu,
                         const double* angB, const double* angT, const Dots& d, double* out, ull* ctr, cudaStream_t s);
+// PreSolve_2 by FFT (drd_pressure_fft.cu): plans for lengths of the form 2^a 3^b 5^c 7^d;
+// whether a grid fits the passes' shared memory with reals of `real_bytes`; the kernels'
+// shared-memory opt-in (once per context, outside stream capture); the FP64 step (u, v -> psi
+// interior, * ca->coef) and the FP32 2-D pair on plain arrays.
+bool pfft_plan(int n, FftPlan& pl);
+bool pfft_fits(int nr, int nz, int real_bytes);
+cudaError_t pfft_prepare(int nr, int nz);
+cudaError_t launch_pressure_fft(int nr, int nz, double dr, double dz, const FftPlan& px, const FftPlan& pz,
+                                const void* twx, const void* twz, const double* u, const double* v, double* T,
+                                const double* pre_lcc, double* psi, const CallArgs* ca, ull* ctr, cudaStream_t s);
+cudaError_t launch_pressure_fft32(int nr, int nz, const FftPlan& px, const FftPlan& pz, const void* twx,
+                                  const void* twz, const float* x, float* T, const float* lcc, float* out, ull* ctr,
+                                  cudaStream_t s);
 void launch_threshold(long n, const double* x, double t, double* y, ull* ctr, cudaStream_t s);  // y = x > t
 void launch_two_phase_coef(const DevParams& P, long cs, const double* fpd, const double* ph, double* rho, double* eta,
                            float* rho32, float* eta32, ull* ctr, cudaStream_t s);

@@ -66,6 +66,12 @@ struct drd_ctx {
     float *f1ue32, *f1uo32, *es32[2], *esw32;
     int Ku = 0, Nue = 0, Nuo = 0;
     double *cfB, *cfT;
+    // PreSolve_2 by FFT (nr and nz of the form 2^a 3^b 5^c 7^d): plans and twiddle tables in
+    // FP64 (the pressure step) and FP32 (the transform's kernel bench)
+    int pfft = 0, pfft_ok = 0;
+    FftPlan fpx{}, fpz{};
+    double *ftwx, *ftwz;
+    float *ftwx32, *ftwz32;
     // resident state and scratch
     double* fld[DRD_F_COUNT];
     double *u_after, *v_after, *ph_after, *rmu_after, *f2, *uL, *pnb, *pnt, *dist, *fpd, *w, *t1, *t2;
@@ -167,6 +173,7 @@ size_t arena_need(long cs, long us, long vs, long nc, long nr, long nz, long nma
     add(sizeof(GridBar), 1);                                   // bar
     add(128, 8);                                               // pprof
     add(8, 8);                                                 // d_diag
+    add(4 * nr, 8); add(4 * nz, 8); add(4 * nr, 4); add(4 * nz, 4);  // FFT tables (complex, 2n each)
     const long fu = (nr / 2 + 1) * (nr / 2 + 2), nes = 3 * (us + vs);
     add(fu, 8); add(fu, 8); add(fu, 4); add(fu, 4);            // f1ue, f1uo (+ FP32)
     for (int i = 0; i < 2; ++i) { add(nes, 8); add(nes, 4); }  // es64, es32
@@ -847,6 +854,12 @@ int enq_uv(drd_ctx* c, int bdf, cudaStream_t s, int extrap = 0) {
 // PreSolve_2 + dct_fftw (microfluidics_complex_domain/PreSolve_2.f90:1-186) on fld[U,V] -> out.
 void enq_pre(drd_ctx* c, double* out, cudaStream_t s) {
     const int nr = c->nr, nz = c->nz;
+    if (c->pfft) {  // three FFT passes (drd_pressure_fft.cu), then the ghosts
+        launch_pressure_fft(nr, nz, c->P.dr, c->P.dz, c->fpx, c->fpz, c->ftwx, c->ftwz, c->fld[DRD_F_U],
+                            c->fld[DRD_F_V], c->t1, c->pre_lcc, out, c->ca, c->ctr, s);
+        launch_fill_neumann(nr, nz, out, nullptr, c->ctr, s);
+        return;
+    }
     launch_pre_div(c->dp, c->fld[DRD_F_U], c->fld[DRD_F_V], c->w, c->ctr, s);
     launch_gemm<double>(gcfg<double>(c, 0), EPI_STORE, gargs<double>(c, nz, nr, nr, c->w, nr, c->m2xT, nr, c->t1, nr, nullptr, G_ALWAYS), s);
     auto a2 = gargs<double>(c, nz, nr, nz, c->m2z, nz, c->t1, nr, c->t2, nr, nullptr, G_ALWAYS);
@@ -1083,6 +1096,27 @@ int upload_tables(drd_ctx* c) {
     CK(cudaMemcpy(c->ph_lcc, ph.data(), sizeof(double) * ph.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->pre_lcc, pre.data(), sizeof(double) * pre.size(), cudaMemcpyHostToDevice));
     launch_convert_scale<float, double>(c->nc, c->ph_lcc, 1.0, c->ph_lcc32, nullptr, c->s);
+    // FFT twiddles: tw[m] = e^(-2 pi i m/n), then tq[k] = e^(-i pi k/2n) (drd_fft.cuh).
+    // DRD_PRESSURE_FFT=0 in the environment keeps the GEMM-form pressure transforms.
+    const char* pe = std::getenv("DRD_PRESSURE_FFT");
+    c->pfft_ok = pfft_fits(c->nr, c->nz, 8) && pfft_plan(c->nr, c->fpx) && pfft_plan(c->nz, c->fpz);
+    c->pfft = c->pfft_ok && !(pe && pe[0] == '0');
+    if (c->pfft_ok) {
+        CK(pfft_prepare(c->nr, c->nz));
+        for (int ax = 0; ax < 2; ++ax) {
+            const int n = ax ? c->nz : c->nr;
+            std::vector<double> t(4L * n);
+            std::vector<float> t32(4L * n);
+            for (int m = 0; m < n; ++m) {
+                const double a = -2.0 * kPi * m / n, b = -kPi * m / (2.0 * n);
+                t[2 * m] = std::cos(a); t[2 * m + 1] = std::sin(a);
+                t[2 * (n + m)] = std::cos(b); t[2 * (n + m) + 1] = std::sin(b);
+            }
+            for (size_t q = 0; q < t.size(); ++q) t32[q] = (float)t[q];
+            CK(cudaMemcpy(ax ? c->ftwz : c->ftwx, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(ax ? c->ftwz32 : c->ftwx32, t32.data(), sizeof(float) * t32.size(), cudaMemcpyHostToDevice));
+        }
+    }
     for (int bdf = 1; bdf <= 2; ++bdf) {
         std::vector<double> f;
         host_esolp(c->P, bdf, f);
@@ -1147,6 +1181,8 @@ int setup_context(drd_ctx* c) {
     c->bar = (GridBar*)carve<char>(c, sizeof(GridBar));
     c->pprof = (unsigned long long*)carve<double>(c, 128);
     c->d_diag = carve<double>(c, 8);
+    c->ftwx = carve<double>(c, 4L * nr); c->ftwz = carve<double>(c, 4L * nz);
+    c->ftwx32 = carve<float>(c, 4L * nr); c->ftwz32 = carve<float>(c, 4L * nz);
     c->Ku = nr / 2 + 1; c->Nue = (nr + 2) / 2; c->Nuo = (nr + 1) / 2;
     const long fu = (long)c->Ku * c->Nue, nes = 3 * ((long)(nr + 1) * nz + (long)nr * (nz - 1));
     c->f1ue = carve<double>(c, fu); c->f1uo = carve<double>(c, fu);
@@ -2013,12 +2049,22 @@ int drd_kernel_bench(drd_ctx* c, int which, int reps, double* us, double* bytes,
                 launch_gemm<float>(gcfg<float>(c, 1), EPI_STORE, a, s);
                 break;
             }
+            case DRD_KB_PRESSURE_FFT64:
+                launch_pressure_fft(nr, nz, c->P.dr, c->P.dz, c->fpx, c->fpz, c->ftwx, c->ftwz, c->fld[DRD_F_U],
+                                    c->fld[DRD_F_V], c->t1, c->pre_lcc, c->fld[DRD_F_PSI2], c->ca, nullptr, s);
+                break;
+            case DRD_KB_DCT2_FFT32:
+                launch_pressure_fft32(nr, nz, c->fpx, c->fpz, c->ftwx32, c->ftwz32, c->k32.p, c->t1f, c->t2f,
+                                      c->k32.v, nullptr, s);
+                break;
             default:
                 launch_ch_matvec<float>(make_op<float>(c, 0), c->M032, c->Mi32, 1.0f, c->k32.p, 0.0f, c->k32.v,
                                         c->k32.ff1, nullptr, 0, dots(c), 0, nullptr, G_ALWAYS, nullptr, s);
                 break;
         }
     };
+    const bool cold = (which == DRD_KB_PRESSURE_FFT64 || which == DRD_KB_DCT2_FFT32);
+    if (cold && !c->pfft_ok) return DRD_ERR_UNSUPPORTED;
     switch (which) {
         case DRD_KB_UV_MATVEC_FP64: by = 8.0 * (2.0 * S.n + 3.0 * c->cs); fl = 45.0 * S.n; break;
         case DRD_KB_UV_MATVEC_FP32: by = 4.0 * (2.0 * S.n + 3.0 * c->cs); fl = 45.0 * S.n; break;
@@ -2027,7 +2073,43 @@ int drd_kernel_bench(drd_ctx* c, int which, int reps, double* us, double* bytes,
         case DRD_KB_DCT_X_FP32: by = 4.0 * (2.0 * c->nc + 2.0 * c->Kx * c->Nxe); fl = 2.0 * c->nc * c->Kx; break;
         case DRD_KB_DCT_Z_FP64: by = 8.0 * (2.0 * c->nc + 2.0 * c->Mze * c->Kz); fl = 2.0 * c->nc * c->Kz; break;
         case DRD_KB_DCT_Z_FP32: by = 4.0 * (2.0 * c->nc + 2.0 * c->Mze * c->Kz); fl = 2.0 * c->nc * c->Kz; break;
+        // u, v read, psi written; the table and the intermediate round trips are not counted
+        case DRD_KB_PRESSURE_FFT64: by = 8.0 * (c->us + c->vs + c->cs); fl = 0.0; break;
+        case DRD_KB_DCT2_FFT32: by = 4.0 * 3.0 * c->nc; fl = 0.0; break;
         default: by = 4.0 * (3.0 * c->nc + 2.0 * c->cs); fl = 40.0 * c->nc; break;
+    }
+    if (cold) {
+        // an nr x nz Pre_Lcc table in FP32 for the FP32 pair; zero inputs are enough, the
+        // transforms' cost does not depend on the values
+        std::vector<float> l32(c->nc);
+        std::vector<double> ph, pre;
+        host_tables(c->P, ph, pre);
+        for (int k = 0; k < nz; ++k)
+            for (int i = 0; i < nr; ++i) l32[i + (size_t)nr * k] = (float)pre[i + (size_t)(nr + 1) * k];
+        CK(cudaMemcpy(c->t2f, l32.data(), sizeof(float) * l32.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemsetAsync(c->k32.p, 0, sizeof(float) * c->nmax, c->s));
+        const int64_t flush = 512ll << 20;
+        int rc2 = drd_flush_l2(c, flush);
+        if (rc2) return rc2;
+        enqueue(c->s);  // warm-up
+        CK(cudaGetLastError());
+        float total = 0.f;
+        for (int r = 0; r < reps; ++r) {
+            rc2 = drd_flush_l2(c, flush);
+            if (rc2) return rc2;
+            CK(cudaEventRecord(c->ev0, c->s));
+            enqueue(c->s);
+            CK(cudaEventRecord(c->ev1, c->s));
+            CK(cudaEventSynchronize(c->ev1));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+            total += ms;
+        }
+        CK(cudaGetLastError());
+        *us = 1e3 * total / reps;
+        if (bytes) *bytes = by;
+        if (flops) *flops = fl;
+        return DRD_OK;
     }
     CK(cudaMemsetAsync(c->k64.p, 0, sizeof(double) * c->nmax, c->s));
     CK(cudaMemsetAsync(c->k32.p, 0, sizeof(float) * c->nmax, c->s));

@@ -3,7 +3,8 @@
     python -m drd_application_gb300.kernel_bench [--grids 420x180 2048x1024 4096x2048]
 
 Each kernel runs `reps` times back to back in one captured graph between CUDA events on the
-context stream (drd_kernel_bench); the rates use the algorithmic bytes and flops that
+context stream (drd_kernel_bench), except the FFT transforms, which run after a 512 MiB L2 flush
+each and are timed launch by launch; the rates use the algorithmic bytes and flops that
 drd_kernel_bench reports for one launch (compulsory inputs and outputs only), against the
 measured HBM copy rate of MEASURED_PEAKS.json (6.8 TB/s when that file is absent).
 """
@@ -21,7 +22,10 @@ KERNELS = (
     (abi.DRD_KB_DCT_X_FP32, "DCT-I x pass FP32"),
     (abi.DRD_KB_DCT_Z_FP32, "DCT-I z pass FP32"),
     (abi.DRD_KB_DCT_X_FP64, "DCT-I x pass FP64"),
+    (abi.DRD_KB_PRESSURE_FFT64, "PreSolve_2 FFT FP64"),
+    (abi.DRD_KB_DCT2_FFT32, "DCT-II/III FFT FP32"),
 )
+COLD = (abi.DRD_KB_PRESSURE_FFT64, abi.DRD_KB_DCT2_FFT32)  # timed with L2 flushed before each launch
 
 
 def hbm_peak():
@@ -43,7 +47,7 @@ def main(argv=None):
         print(f"{nr}x{nz}", flush=True)
         for kid, name in KERNELS:
             stencil = "stencil" in name
-            reps = 100 if stencil else (20 if nr <= 2048 else 3)
+            reps = 10 if kid in COLD else (100 if stencil else (20 if nr <= 2048 else 3))
             us, by, fl = ctx.kernel_bench(kid, reps=reps)
             gbs = by / us / 1e3
             print(f"  {name:22s} {us:10.2f} us  {gbs:8.1f} GB/s ({100 * gbs / peak:5.1f} % of {peak:.0f})  "

@@ -564,7 +564,12 @@ int drd_unet_stream(drd_unet* net, void** stream);
 #define DRD_KB_DCT_Z_FP64 4       /* one z-axis DCT-I pass, FP64                            */
 #define DRD_KB_DCT_Z_FP32 5       /* the same in FP32                                       */
 #define DRD_KB_CH_MATVEC_FP32 6   /* MATRIX_VECTOR_CG second stencil pass, FP32             */
-#define DRD_KB_COUNT 7
+#define DRD_KB_PRESSURE_FFT64 7   /* PreSolve_2 by FFT, FP64: u, v -> psi (three passes)     */
+#define DRD_KB_DCT2_FFT32 8       /* REDFT10, / Pre_Lcc, REDFT01 of an nr x nz FP32 field    */
+#define DRD_KB_COUNT 9
+/* DRD_KB_PRESSURE_FFT64 and DRD_KB_DCT2_FFT32 write 512 MiB of scratch before every launch (L2
+ * cold, the inputs come from HBM) and report the mean of the per-launch event times; they need
+ * nr and nz of the form 2^a 3^b 5^c 7^d (DRD_ERR_UNSUPPORTED otherwise). */
 /* Launches kernel `which` `reps` times back to back (one captured graph) between CUDA events
  * on the context stream.  Returns the average device time per launch and the algorithmic
  * bytes and flops one launch moves / performs (compulsory inputs and outputs only). */
