@@ -42,9 +42,28 @@ __device__ __forceinline__ Cx<R> csub(Cx<R> a, Cx<R> b) { return {a.x - b.x, a.y
 template <typename R>
 __device__ __forceinline__ Cx<R> conjx(Cx<R> a) { return {a.x, -a.y}; }
 
-// In-place DFT of R points; inverse: sign +1.  w[m] = e^(-2 pi i m / n) with n a multiple of R.
+// cos and sin of 2 pi j / R for j = 0..R-1 (R = 3, 5, 7), to 21 digits; j and R - j mirror.
+__host__ __device__ constexpr double root_c(int r, int j) {
+    const int q = (j <= r / 2) ? j : r - j;
+    return q == 0 ? 1.0
+         : r == 3 ? -0.5
+         : r == 5 ? (q == 1 ? 0.309016994374947424102 : -0.809016994374947424102)
+                  : (q == 1 ? 0.623489801858733530525 : q == 2 ? -0.222520933956314404289 : -0.900968867902419126236);
+}
+__host__ __device__ constexpr double root_s(int r, int j) {
+    const int q = (j <= r / 2) ? j : r - j;
+    const double v = q == 0 ? 0.0
+                   : r == 3 ? 0.866025403784438646764
+                   : r == 5 ? (q == 1 ? 0.951056516295153572116 : 0.587785252292473129169)
+                            : (q == 1 ? 0.781831482468029808708 : q == 2 ? 0.974927912181823607018 : 0.433883739117558120476);
+    return (j <= r / 2) ? v : -v;
+}
+
+// In-place DFT of R points: X_m = sum_t v_t e^(-+2 pi i t m / R) (inverse: +).  Radix 2 and 4 by
+// sums and differences; 3, 5 and 7 by the direct sum with constant roots (the loops unroll, so
+// every root is an immediate).
 template <int RAD, typename R>
-__device__ __forceinline__ void dft_small(Cx<R> (&v)[RAD], const Cx<R>* __restrict__ w, int n, bool inverse) {
+__device__ __forceinline__ void dft_small(Cx<R> (&v)[RAD], bool inverse) {
     if constexpr (RAD == 2) {
         const Cx<R> a = v[0], b = v[1];
         v[0] = cadd(a, b);
@@ -60,14 +79,14 @@ __device__ __forceinline__ void dft_small(Cx<R> (&v)[RAD], const Cx<R>* __restri
         v[3] = csub(a1, jb1);
     } else {
         Cx<R> o[RAD];
-        const int step = n / RAD;
+        const R sg = inverse ? R(1) : R(-1);
 #pragma unroll
         for (int m = 0; m < RAD; ++m) {
             Cx<R> acc = v[0];
 #pragma unroll
             for (int t = 1; t < RAD; ++t) {
-                Cx<R> e = w[((t * m) % RAD) * step];
-                if (inverse) e.y = -e.y;
+                const int j = (t * m) % RAD;
+                const Cx<R> e = {(R)root_c(RAD, j), sg * (R)root_s(RAD, j)};
                 acc = cadd(acc, cmul(v[t], e));
             }
             o[m] = acc;
@@ -97,7 +116,7 @@ __device__ __forceinline__ void fft_stage(const Cx<R>* a, Cx<R>* b, int n, int N
             }
             v[t] = x;
         }
-        dft_small<RAD, R>(v, w, n, inverse);
+        dft_small<RAD, R>(v, inverse);
         const int o = (j / Ns) * Ns * RAD + k;
 #pragma unroll
         for (int t = 0; t < RAD; ++t) b[o + t * Ns] = v[t];

@@ -20,8 +20,13 @@
 namespace drd {
 namespace {
 
-constexpr int kPT = 256;  // threads per block of the passes
-__host__ __device__ __forceinline__ int pgroup(int n) { return n >= 512 ? 128 : (n >= 128 ? 64 : 32); }
+constexpr int kPT = 256;  // most threads per block of the passes
+// Threads per line pair: a stage has n/4 to n/2 butterflies.
+__host__ __device__ __forceinline__ int pgroup(int n) { return n >= 1024 ? 256 : (n >= 256 ? 128 : 64); }
+// Line pairs per block: FP64 takes one, so that the pairs spread over as many SMs as possible (the
+// FP64 pipe of one SM is the limit); FP32 fills 256 threads.
+template <typename R>
+__host__ __device__ __forceinline__ int pgroups(int n) { return sizeof(R) == 8 ? 1 : kPT / pgroup(n); }
 
 template <typename R>
 struct PfftArgs {
@@ -47,7 +52,7 @@ template <typename R>
 __global__ void __launch_bounds__(kPT) k_pfft_rows_fwd(PfftArgs<R> a, ull* ctr) {
     count_launch(ctr);
     extern __shared__ __align__(16) unsigned char smraw[];
-    const int n = a.nr, G = pgroup(n), groups = kPT / G;
+    const int n = a.nr, G = pgroup(n), groups = pgroups<R>(n);
     const int grp = threadIdx.x / G, lane = threadIdx.x - grp * G;
     Cx<R>* A = reinterpret_cast<Cx<R>*>(smraw) + (long)grp * 2 * n;
     Cx<R>* B = A + n;
@@ -85,7 +90,7 @@ template <typename R>
 __global__ void __launch_bounds__(kPT) k_pfft_cols(PfftArgs<R> a, ull* ctr) {
     count_launch(ctr);
     extern __shared__ __align__(16) unsigned char smraw[];
-    const int n = a.nz, G = pgroup(n), groups = kPT / G;
+    const int n = a.nz, G = pgroup(n), groups = pgroups<R>(n);
     const int grp = threadIdx.x / G, lane = threadIdx.x - grp * G;
     Cx<R>* A = reinterpret_cast<Cx<R>*>(smraw) + (long)grp * 2 * n;
     Cx<R>* B = A + n;
@@ -138,7 +143,7 @@ template <typename R>
 __global__ void __launch_bounds__(kPT) k_pfft_rows_inv(PfftArgs<R> a, ull* ctr) {
     count_launch(ctr);
     extern __shared__ __align__(16) unsigned char smraw[];
-    const int n = a.nr, G = pgroup(n), groups = kPT / G;
+    const int n = a.nr, G = pgroup(n), groups = pgroups<R>(n);
     const int grp = threadIdx.x / G, lane = threadIdx.x - grp * G;
     Cx<R>* A = reinterpret_cast<Cx<R>*>(smraw) + (long)grp * 2 * n;
     Cx<R>* B = A + n;
@@ -176,7 +181,7 @@ __global__ void __launch_bounds__(kPT) k_pfft_rows_inv(PfftArgs<R> a, ull* ctr) 
 
 template <typename R>
 size_t pfft_smem(int n) {
-    return (size_t)(kPT / pgroup(n)) * 2 * n * sizeof(Cx<R>);
+    return (size_t)pgroups<R>(n) * 2 * n * sizeof(Cx<R>);
 }
 
 // The passes' shared memory above 48 KB needs an opt-in per kernel; set once per context, outside
@@ -194,11 +199,11 @@ template <typename R>
 cudaError_t pfft_launch(const PfftArgs<R>& a, ull* ctr, cudaStream_t s) {
     const size_t sx = pfft_smem<R>(a.nr), sz = pfft_smem<R>(a.nz);
     const int gx = (a.nz + 1) / 2, gz = (a.nr + 1) / 2;
-    const int bx = (gx + kPT / pgroup(a.nr) - 1) / (kPT / pgroup(a.nr));
-    const int bz = (gz + kPT / pgroup(a.nz) - 1) / (kPT / pgroup(a.nz));
-    k_pfft_rows_fwd<R><<<bx, kPT, sx, s>>>(a, ctr);
-    k_pfft_cols<R><<<bz, kPT, sz, s>>>(a, ctr);
-    k_pfft_rows_inv<R><<<bx, kPT, sx, s>>>(a, ctr);
+    const int px = pgroups<R>(a.nr), pz = pgroups<R>(a.nz);
+    const int tx = px * pgroup(a.nr), tz = pz * pgroup(a.nz);
+    k_pfft_rows_fwd<R><<<(gx + px - 1) / px, tx, sx, s>>>(a, ctr);
+    k_pfft_cols<R><<<(gz + pz - 1) / pz, tz, sz, s>>>(a, ctr);
+    k_pfft_rows_inv<R><<<(gx + px - 1) / px, tx, sx, s>>>(a, ctr);
     return cudaGetLastError();
 }
 
@@ -220,9 +225,12 @@ bool pfft_plan(int n, FftPlan& pl) {
 
 bool pfft_fits(int nr, int nz, int real_bytes) {
     FftPlan p;
-    const size_t cx = 2 * (size_t)real_bytes;
-    return pfft_plan(nr, p) && pfft_plan(nz, p) && (size_t)(kPT / pgroup(nr)) * 2 * nr * cx <= 200 * 1024 &&
-           (size_t)(kPT / pgroup(nz)) * 2 * nz * cx <= 200 * 1024;
+    const size_t lim = 200 * 1024;
+    const bool f64 = real_bytes == 8;
+    auto bytes = [&](int n) {
+        return f64 ? pfft_smem<double>(n) : pfft_smem<float>(n);
+    };
+    return pfft_plan(nr, p) && pfft_plan(nz, p) && bytes(nr) <= lim && bytes(nz) <= lim;
 }
 
 cudaError_t pfft_prepare(int nr, int nz) {
