@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--c3-solves", type=int, default=512,
                     help="independent momentum and pressure systems of the C3 batch (0: skip)")
+    ap.add_argument("--c5-steps", type=int, default=2,
+                    help="steps of the 2048x1024 C5 comparison, mixed against FP64 (0: skip)")
     ap.add_argument("--learned-steps", type=int, default=600,
                     help="Adam steps of the learned CH guess leg (0: skip)")
     ap.add_argument("--nr", type=int, default=420)
@@ -230,6 +232,48 @@ def run_reference(args, ws, rank):
 
 
 # ----------------------------------------------------------------------------------- GPU arm
+def time_c5(steps, seed=0):
+    """C5: the 2048x1024 workload (serpentine channel, 64 rigid fibers, 32 drops, viscosity ratio
+    10 between the fluids), `steps` resident steps in the mixed mode (cubic guess) and in the plain
+    FP64 mode (the reference's arithmetic and guess) from the same state: wall time per step,
+    iterations and convergence of every solve, the phase-field mass drift per step and the
+    velocity and phase fields of the mixed run against the FP64 run."""
+    import numpy as np
+
+    from drd_application_gb300 import abi
+    from drd_application_gb300.api import DRDContext
+    from drd_application_gb300.workloads import make_case
+
+    out, fields = {}, {}
+    for name, prec, gm in (("mixed", abi.DRD_PREC_MIXED, 3), ("fp64", abi.DRD_PREC_FP64, 0)):
+        case = make_case("c5", seed=seed, precision=prec, guess_mode=gm)
+        ctx = DRDContext(case.params)
+        ctx.set_case(case)
+        ctx.upload_state(case.state)
+        m0 = ctx.mass(case.state[abi.F_PH])
+        t, rows = 0.0, []
+        for s_ in range(steps):
+            rows.append(ctx.step(s_ == 0, t))
+            t += case.params.dt
+        g = ctx.download_state([abi.F_U, abi.F_V, abi.F_PH])
+        fields[name] = g
+        ctx.close()
+        out[name] = {
+            "ms_per_step": [1e3 * r.seconds for r in rows],
+            "ch": [{"info": r.ch.info, "iter": r.ch.iter, "true_resid": r.ch.true_resid,
+                    "fp64_fallback": bool(r.ch.flags & abi.DRD_FLAG_FALLBACK64)} for r in rows],
+            "uv": [{"info": r.uv.info, "iter": r.uv.iter, "true_resid": r.uv.true_resid} for r in rows],
+            "mass_drift_per_step": (rows[-1].mass - m0) / abs(m0) / steps,
+        }
+    rel = lambda a, b: float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))  # noqa: E731
+    out["mixed_vs_fp64"] = {"u": rel(fields["mixed"][abi.F_U], fields["fp64"][abi.F_U]),
+                            "v": rel(fields["mixed"][abi.F_V], fields["fp64"][abi.F_V]),
+                            "ph": rel(fields["mixed"][abi.F_PH], fields["fp64"][abi.F_PH])}
+    out["steps"] = steps
+    out["workload"] = "c5 2048x1024: serpentine channel (amp 150, period 680), 64 fibers 60x6, 32 drops, lambda_eta 10"
+    return out
+
+
 def c3_systems(n_solves, seed):
     """The C3 batch: n_solves independent systems on grids drawn from five sizes, alternately the
     momentum operator of VeloSolve_2_combined (2 to 6 disks, eta = 1 + 99 mask) and the
@@ -540,6 +584,9 @@ def run_gpu(args, ws, rank, local):
     # the learned CH guess (rank 0 only: it is reported beside the headline)
     learned = time_learned(args.learned_steps, args.nr, args.nz) if (args.learned_steps > 0 and rank == 0) else None
 
+    # C5 at 2048x1024, mixed against FP64 (rank 0 only, reported beside the headline)
+    c5 = time_c5(args.c5_steps, rank) if (args.c5_steps > 0 and rank == 0) else None
+
     # plain FP64 path, resident state (--fp64-steps 0 skips it, e.g. for profiler runs), and the
     # arms that split mixed_over_fp64 into its factors on the same workload: FP64 with the cubic
     # guess (the guess), mixed with the cubic guess in the kernel-per-phase graph loop that the
@@ -640,6 +687,7 @@ def run_gpu(args, ws, rank, local):
             "with_particles": {"steps_per_s": K * ws / pt_sec, "ms_per_step": 1e3 * pt_sec / K, "beads": 9,
                                "solves_to_fp64_1e-8": f"{pt['solves_ok']}/{pt['solves']}"},
             "c3_batch": c3,
+            "c5": c5,
             "learned_guess": learned,
         },
         "roofline": {"bound": "hbm", "kernel": "k_bicg_persist<CH> (whole mixed CH solve)", "achieved": achieved,

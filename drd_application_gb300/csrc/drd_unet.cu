@@ -29,6 +29,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <random>
 #include <string>
@@ -177,6 +178,198 @@ __global__ void __launch_bounds__(kConvTPB) k_conv3(ConvArgs a) {
             }
         }
 }
+
+// ------------------------------------------------------------------------------------------
+// The same 3x3 convolution on the fifth-generation tensor cores: tcgen05.mma (M = 128 pixels of
+// a 4 x 32 tile, N = up to 256 output channels, K = 16) issued by one thread, operands in shared
+// memory in the K-major, unswizzled core-matrix layout (8 rows x 16 bytes per core matrix), the
+// FP32 accumulator in tensor memory (TMEM), read back by tcgen05.ld for the epilogue.
+//
+// Per chunk of kc input channels a stage holds
+//   A: the tile's input with its halo, three times, shifted by dx = 0, 1, 2 pixels, each
+//      [k-core][6 halo rows][32 columns][8 channels]: the operand of tap (dy, dx) is then copy dx
+//      from halo row dy on, with a uniform 128-byte stride between 8-pixel groups;
+//   B: the 9 taps' weights [tap][k-core][n][8 channels].
+// Two stages alternate: the block fills one while the MMAs of the other run; an mbarrier that
+// tcgen05.commit arrives on tells the block when a stage's MMAs are done.  Waits are bounded:
+// a wait that runs out sets the network's error flag and the block skips the rest.
+constexpr int kTcThreads = 256;   // 8 warps: all load; warps w and w+4 share TMEM lanes 32 (w%4)
+constexpr int kTcSpin = 1 << 22;  // mbarrier polls before a wait gives up
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    // shared-memory matrix descriptor: start >> 4 (bits 0-13), leading-dimension byte offset >> 4
+    // (K-direction core-matrix stride, 16-29), stride byte offset >> 4 (8-row-group stride,
+    // 32-45), descriptor version 1 (46-47), no swizzle (61-63 = 0)
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
+    for (int it = 0; it < kTcSpin; ++it) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+struct TcArgs {
+    ConvArgs c;
+    int nt, kc;   // output channels per block (16..256, multiple of 16), input channels per chunk
+    int* err;     // set when a wait gave up
+};
+
+__global__ void __launch_bounds__(kTcThreads) k_conv3_tc(TcArgs t) {
+    extern __shared__ __align__(1024) unsigned char tsm[];
+    __shared__ uint32_t tmem_base;
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ int bad;
+    const ConvArgs& a = t.c;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nt = t.nt, kc = t.kc, kcores = kc / 8;
+    const int ncot = (a.Cout + nt - 1) / nt;
+    const int b = blockIdx.z / ncot, co0 = (blockIdx.z % ncot) * nt;
+    const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
+    const uint32_t a_bytes = 3u * kcores * 3072u, b_bytes = 9u * kcores * nt * 16u;
+    const uint32_t stage_bytes = a_bytes + b_bytes;
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(tsm);
+    const uint32_t tcols = nt <= 32 ? 32u : (nt <= 64 ? 64u : (nt <= 128 ? 128u : 256u));
+    if (warp == 0) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tmem_base);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(tcols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 2; ++i) {
+            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[i]);
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        bad = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tbase = tmem_base;
+    const bf16* xb = a.x + (long)b * a.xbs;
+    const int Wl = a.W >> 1;
+    const int nchunks = a.Cin / kc;
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nt >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+    for (int c = 0; c < nchunks; ++c) {
+        const int st = c & 1;
+        const int c0 = c * kc;
+        unsigned char* sA = tsm + st * stage_bytes;
+        unsigned char* sB = sA + a_bytes;
+        if (c >= 2) {  // the MMAs of chunk c - 2 read this stage
+            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[st]);
+            if (!bad && !tc_wait(mb, (uint32_t)(((c - 2) >> 1) & 1))) { bad = 1; atomicExch(t.err, 1); }
+            __syncthreads();
+        }
+        if (bad) break;
+        // A: the halo tile (6 x 34 pixels) into the three shifted copies
+        for (int i = tid; i < (kTH + 2) * (kTW + 2) * kcores; i += kTcThreads) {
+            const int ki = i % kcores, pix = i / kcores;
+            const int hr = pix / (kTW + 2), hc = pix - hr * (kTW + 2);
+            const int gy = y0 + hr - 1, gx = x0 + hc - 1;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (gy >= 0 && gy < a.H && gx >= 0 && gx < a.W) {
+                const long sp = a.up ? (long)(gy >> 1) * Wl + (gx >> 1) : (long)gy * a.W + gx;
+                v = __ldg(reinterpret_cast<const uint4*>(xb + sp * a.ldx + c0 + ki * 8));
+            }
+#pragma unroll
+            for (int dx = 0; dx < 3; ++dx) {
+                const int col = hc - dx;
+                if (col >= 0 && col < kTW)
+                    *reinterpret_cast<uint4*>(sA + dx * kcores * 3072 + ki * 3072 + hr * 512 + col * 16) = v;
+            }
+        }
+        // B: the 9 taps' weights of output channels co0 .. co0 + nt - 1
+        for (int i = tid; i < 9 * kcores * nt; i += kTcThreads) {
+            const int n = i % nt, r = i / nt, ki = r % kcores, tap = r / kcores;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (co0 + n < a.Cout)
+                v = __ldg(reinterpret_cast<const uint4*>(a.w + ((long)tap * a.Cout + co0 + n) * a.Cin + c0 + ki * 8));
+            *reinterpret_cast<uint4*>(sB + tap * kcores * nt * 16 + ki * nt * 16 + n * 16) = v;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t aS = sbase + st * stage_bytes, bS = aS + a_bytes;
+            for (int tap = 0; tap < 9; ++tap) {
+                const int dy = tap / 3, dx = tap % 3;
+                for (int j = 0; j < kc / 16; ++j) {
+                    const uint64_t ad = tc_desc(aS + dx * kcores * 3072 + 2 * j * 3072 + dy * 512, 3072, 128);
+                    const uint64_t bd = tc_desc(bS + tap * kcores * nt * 16 + 2 * j * nt * 16, nt * 16, 128);
+                    const uint32_t acc = (c > 0 || tap > 0 || j > 0) ? 1u : 0u;
+                    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                                 ::"r"(tbase), "l"(ad), "l"(bd), "r"(idesc), "r"(acc) : "memory");
+                }
+            }
+            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[st]);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
+        }
+    }
+    // the last chunk's commit covers every MMA of the block
+    if (!bad && nchunks > 0) {
+        const int lc = nchunks - 1;
+        const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[lc & 1]);
+        if (!tc_wait(mb, (uint32_t)((lc >> 1) & 1))) { bad = 1; atomicExch(t.err, 1); }
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. (pixels of tile row w % 4) and half of the
+    // columns (all of them when nt < 32, by warps 0-3)
+    const int q = warp & 3, half = warp >> 2;
+    const int ncol = nt >= 32 ? nt / 2 : nt;
+    const bool ep = !bad && (nt >= 32 || half == 0);
+    const int py = y0 + q, px = x0 + lane;
+    if (ep) {
+        for (int cc = 0; cc < ncol; cc += 16) {
+            const int col = half * ncol + cc;
+            uint32_t r[16];
+            const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)col;
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                         : "r"(ta));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (py < a.H && px < a.W) {
+                const long p = (long)py * a.W + px;
+#pragma unroll
+                for (int e = 0; e < 16; e += 2) {
+                    const int co = co0 + col + e;
+                    if (co >= a.Cout) break;
+                    float v0 = __uint_as_float(r[e]), v1 = __uint_as_float(r[e + 1]);
+                    if (a.bias) { v0 += a.bias[co]; v1 += a.bias[co + 1]; }
+                    if (a.relu) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+                    if (a.mask) {
+                        const bf16* m = a.mask + (long)b * a.mbs + p * a.ldm + co;
+                        if (!(__bfloat162float(m[0]) > 0.f)) v0 = 0.f;
+                        if (!(__bfloat162float(m[1]) > 0.f)) v1 = 0.f;
+                    }
+                    if (a.y)
+                        *reinterpret_cast<__nv_bfloat162*>(a.y + (long)b * a.ybs + p * a.ldy + co) = __floats2bfloat162_rn(v0, v1);
+                    else
+                        *reinterpret_cast<float2*>(a.yf + (long)b * a.ybs + p * a.ldy + co) = make_float2(v0, v1);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(tcols) : "memory");
+}
+
+// Output channels per block and input channels per chunk of the tensor-core convolution, and
+// its shared memory (two stages).
+void tc_shape(int Cin, int Cout, int* nt, int* kc) {
+    *nt = Cout >= 256 ? 256 : Cout;
+    *kc = (*nt >= 128 || Cin % 32 != 0) ? 16 : 32;
+}
+size_t tc_smem(int nt, int kc) { return 2 * (3 * (size_t)(kc / 8) * 3072 + 9 * (size_t)(kc / 8) * nt * 16); }
 
 // ------------------------------------------------------------------------------------------
 // Weight gradient: dW[tap][co][ci] += sum over pixels of G[p][co] * X[p + off(tap)][ci], an MMA
@@ -526,6 +719,8 @@ struct drd_unet {
     float *y = nullptr, *dy = nullptr, *tg = nullptr, *xstage = nullptr, *ystage = nullptr, *loss = nullptr;
     std::vector<void*> allocs;
     std::string err;
+    int tc = 0;            // 3x3 convolutions on tcgen05 (DRD_UNET_TC=1) instead of mma.sync
+    int* dflag = nullptr;  // device: set by a tensor-core wait that gave up
 
     int HWl(int l) const { return (Hp >> l) * (Wp >> l); }
     int Hl(int l) const { return Hp >> l; }
@@ -542,6 +737,23 @@ int dalloc(drd_unet* n, T** p, size_t count) {
     return cudaMemsetAsync(*p, 0, sizeof(T) * (count ? count : 1), n->s) == cudaSuccess ? DRD_OK : DRD_ERR_CUDA;
 }
 
+// One 3x3 convolution: the tensor-core kernel (tcgen05) unless it is switched off, else the
+// mma.sync kernel (which needs Cout % 32 == 0).
+void launch_conv3(drd_unet* n, const ConvArgs& a, int batch) {
+    if (n->tc) {
+        TcArgs t{};
+        t.c = a;
+        tc_shape(a.Cin, a.Cout, &t.nt, &t.kc);
+        t.err = n->dflag;
+        const int ncot = (a.Cout + t.nt - 1) / t.nt;
+        dim3 grid((a.W + kTW - 1) / kTW, (a.H + kTH - 1) / kTH, batch * ncot);
+        k_conv3_tc<<<grid, kTcThreads, tc_smem(t.nt, t.kc), n->s>>>(t);
+        return;
+    }
+    dim3 grid((a.W + kTW - 1) / kTW, (a.H + kTH - 1) / kTH, batch * (a.Cout / 32));
+    k_conv3<<<grid, kConvTPB, 0, n->s>>>(a);
+}
+
 void conv(drd_unet* n, int li, const bf16* x, int ldx, long xbs, bf16* y, int ldy, long ybs, int batch) {
     const auto& Ly = n->L[li];
     ConvArgs a{};
@@ -550,8 +762,7 @@ void conv(drd_unet* n, int li, const bf16* x, int ldx, long xbs, bf16* y, int ld
     a.y = y; a.yf = nullptr; a.ybs = ybs; a.ldy = ldy;
     a.mask = nullptr; a.mbs = 0; a.ldm = 0;
     a.H = n->Hl(Ly.level); a.W = n->Wl(Ly.level); a.Cin = Ly.cin; a.Cout = Ly.cout; a.up = Ly.up; a.relu = 1;
-    dim3 grid((a.W + kTW - 1) / kTW, (a.H + kTH - 1) / kTH, batch * (a.Cout / 32));
-    k_conv3<<<grid, kConvTPB, 0, n->s>>>(a);
+    launch_conv3(n, a, batch);
 }
 
 // data gradient of layer li: out (bf16 with mask, or fp32) = conv(G, flipped transpose)
@@ -565,8 +776,7 @@ void dgrad(drd_unet* n, int li, const bf16* G, int batch, bf16* out_b, float* ou
     a.y = out_b; a.yf = out_f; a.ybs = obs; a.ldy = ldo;
     a.mask = mask; a.mbs = mbs; a.ldm = ldm;
     a.H = H; a.W = W; a.Cin = Ly.cout; a.Cout = Ly.cin; a.up = 0; a.relu = 0;
-    dim3 grid((W + kTW - 1) / kTW, (H + kTH - 1) / kTH, batch * (a.Cout / 32));
-    k_conv3<<<grid, kConvTPB, 0, n->s>>>(a);
+    launch_conv3(n, a, batch);
 }
 
 void wgrad(drd_unet* n, int li, const bf16* x, int ldx, long xbs, const bf16* G, int batch) {
@@ -711,6 +921,14 @@ int finish(drd_unet* n) {
         n->err = cudaGetErrorString(e);
         return DRD_ERR_CUDA;
     }
+    if (n->dflag) {
+        int f = 0;
+        if (cudaMemcpy(&f, n->dflag, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && f) {
+            cudaMemset(n->dflag, 0, sizeof(int));
+            n->err = "a tensor-core convolution gave up waiting for its MMAs";
+            return DRD_ERR_TIMEOUT;
+        }
+    }
     return DRD_OK;
 }
 
@@ -826,7 +1044,15 @@ int drd_unet_create(int H, int W, int in_ch, int out_ch, int max_batch, uint64_t
     rc |= dalloc(n, &n->dU, du * B) | dalloc(n, &n->dlow, dl * B) | dalloc(n, &n->dpool, dp * B);
     const size_t nio = (size_t)B * n->H0 * n->W0;
     rc |= dalloc(n, &n->y, nio * out_ch) | dalloc(n, &n->dy, nio * out_ch) | dalloc(n, &n->xstage, nio * in_ch) |
-          dalloc(n, &n->ystage, nio * out_ch) | dalloc(n, &n->loss, 1);
+          dalloc(n, &n->ystage, nio * out_ch) | dalloc(n, &n->loss, 1) | dalloc(n, &n->dflag, 1);
+    // the tcgen05 convolutions on request (DRD_UNET_TC=1): correct, but their operand staging
+    // (plain loads into shared memory, the weights reloaded for every 128-pixel tile) leaves the
+    // tensor pipe idle most of the time, and the mma.sync kernels are faster on this network
+    const char* tce = std::getenv("DRD_UNET_TC");
+    n->tc = (tce && tce[0] == '1');
+    if (n->tc && cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)tc_smem(256, 16)) != cudaSuccess)
+        n->tc = 0;
     if (rc) {
         drd_unet_destroy(n);
         return DRD_ERR_CUDA;

@@ -105,3 +105,30 @@ def test_training_fits_a_smooth_map(cuda_lib):
         loss = net.train_step(x, t, 1e-3)
     assert loss < 0.05 * l0, (l0, loss)
     net.close()
+
+
+@pytest.mark.parametrize("H,W", [(16, 16), (37, 70), (64, 128)])
+def test_tensor_core_convolutions_match_the_mma_sync_kernels(cuda_lib, H, W):
+    """The tcgen05 convolutions (DRD_UNET_TC=1) against the mma.sync kernels (the default) on
+    the same parameters: forward outputs and gradients.  Both accumulate in FP32 from BF16
+    operands; only the summation order differs, so BF16 rounding flips are the only source of
+    difference."""
+    import os
+
+    rng = np.random.default_rng(H)
+    x = rng.standard_normal((3, 3, H, W)).astype(np.float32)
+    tg = rng.standard_normal((3, 1, H, W)).astype(np.float32)
+    out = []
+    for tc in ("1", "0"):
+        os.environ["DRD_UNET_TC"] = tc
+        try:
+            net = _net(H, W, 3, 1, seed=5)
+        finally:
+            os.environ.pop("DRD_UNET_TC", None)
+        y = net.forward(x)
+        loss, g = net.gradients(x, tg)
+        out.append((y, loss, g))
+        net.close()
+    (y1, l1, g1), (y0, l0, g0) = out
+    assert _rel(y1, y0) < 2e-2 and abs(l1 - l0) <= 2e-2 * abs(l0)
+    assert _rel(g1, g0) < 5e-2
