@@ -23,6 +23,8 @@ SIGNATURES = {
     "drd_last_error": (C.c_char_p, [_ctx]),
     "drd_set_coefs": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, _dp]),
     "drd_set_tp_fields": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
+    "drd_set_ch_blend": (C.c_int, [_ctx, _dp]),
+    "drd_ch_blend_probe": (C.c_int, [_ctx, C.c_int, C.c_uint64, C.c_int, _dp]),
     "drd_interpolate_coef": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
     "drd_two_phase_coef": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
     "drd_batch_create": (C.c_int, [C.c_int, C.POINTER(abi.drd_batch_problem), C.c_int, C.POINTER(C.c_void_p)]),

@@ -87,6 +87,23 @@ class DRDContext:
         self._rc(self.L.drd_set_tp_fields(self.h, ptr(a[0]), ptr(a[1]), ptr(ang[0]), ptr(ang[1])),
                  "drd_set_tp_fields", False)
 
+    def set_ch_blend(self, w):
+        """Install the solid-blend weights of the CH preconditioner (packed nr*nz, in [0, 1]), or
+        remove them (None): drd_set_ch_blend."""
+        if w is not None:
+            w = np.ascontiguousarray(w, dtype=np.float64).reshape(-1)
+            if w.shape != (self.nr * self.nz,):
+                raise ValueError(f"blend weights have nr*nz = {self.nr * self.nz} entries")
+        self._rc(self.L.drd_set_ch_blend(self.h, ptr(w)), "drd_set_ch_blend", False)
+
+    def ch_blend_probe(self, nprobe=32, seed=0, install=True):
+        """Fit the blend weights of the current mobilities with `nprobe` Rademacher probes on the
+        GPU (drd_ch_blend_probe); returns them (packed nr*nz) and installs them if asked."""
+        w = np.zeros(self.nr * self.nz)
+        self._rc(self.L.drd_ch_blend_probe(self.h, int(nprobe), int(seed), int(bool(install)), ptr(w)),
+                 "drd_ch_blend_probe", False)
+        return w
+
     def set_case(self, case):
         """Load the coefficient fields of a workloads.Case (with two_fluid, also its indicator
         fpd_ph, which every step combines with the phase field)."""

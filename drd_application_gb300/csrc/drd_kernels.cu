@@ -1647,6 +1647,58 @@ __global__ void k_bi_diag_apply(long n, const T* __restrict__ x, const T* __rest
         y[q] = ident ? x[q] : x[q] / diag[q];
 }
 
+// The solid-blended CH preconditioner's last step: y = q + w (x - q) with q = PSolve_CG(x)
+// already in y (an extension of PhSolve.f90:296-313, w per packed cell).
+template <typename T>
+__global__ void k_pc_blend(long n, const T* __restrict__ x, const T* __restrict__ w, T* __restrict__ y,
+                           const KState* ks, int gate, ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, gate)) return;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const T v = y[q];
+        y[q] = v + w[q] * (x[q] - v);
+    }
+}
+
+// Entry q of Rademacher probe `probe`: the sign of the top bit of splitmix64(seed + (probe n +
+// q + 1) G), G = 0x9E3779B97F4A7C15.
+__device__ __forceinline__ double probe_sign(unsigned long long seed, long probe, long n, long q) {
+    unsigned long long z = seed + (unsigned long long)(probe * n + q + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z = z ^ (z >> 31);
+    return (z >> 63) ? -1.0 : 1.0;
+}
+__global__ void k_probe_fill(long n, unsigned long long seed, long probe, double* __restrict__ e, ull* ctr) {
+    count_launch(ctr);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        e[q] = probe_sign(seed, probe, n, q);
+}
+// With r = A e and qv = PSolve_CG(r): d = r - qv, t = e - qv; num += t d, den += d d.
+__global__ void k_probe_acc(long n, unsigned long long seed, long probe, const double* __restrict__ r,
+                            const double* __restrict__ qv, double* __restrict__ num, double* __restrict__ den,
+                            int first, ull* ctr) {
+    count_launch(ctr);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const double e = probe_sign(seed, probe, n, q), qq = qv[q];
+        const double d = r[q] - qq, t = e - qq;
+        num[q] = first ? t * d : fma(t, d, num[q]);
+        den[q] = first ? d * d : fma(d, d, den[q]);
+    }
+}
+// w = clamp(num / den, 0, 1), 0 where den = 0; FP64 and FP32 copies.
+__global__ void k_probe_final(long n, const double* __restrict__ num, const double* __restrict__ den,
+                              double* __restrict__ w, float* __restrict__ w32, ull* ctr) {
+    count_launch(ctr);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const double dd = den[q];
+        double v = dd > 0.0 ? num[q] / dd : 0.0;
+        v = v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v);
+        w[q] = v;
+        w32[q] = (float)v;
+    }
+}
+
 // OMEGA = (t, s) / (t, t) (:349-350) from slots 6/7, then X = X + ALPHA PHAT (+ OMEGA SHAT);
 // R = R - OMEGA T (:314, :354-359) with ||R||^2 (slot 0) and (rtld, R) (slot 1) partials for
 // STOPTEST2 and the next RHO.
@@ -2213,7 +2265,10 @@ __device__ __forceinline__ int pb_swz(int k, int m) {
     return k * PB_BM + ((((m >> 2) ^ (k & (PB_AG - 1))) << 2) | (m & 3));
 }
 static_assert((PB_BM / 4) * (PB_BN / 4) * PB_KG == PB_NT, "4 x 4 register tiles, PB_KG groups");
-__device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float* smem, const PbProf& pf) {
+// bx, bw (optional): blend the result with bx as out = v + bw (bx - v) (the solid-blended CH
+// preconditioner's last step; bx is the preconditioner's input, written inside this launch).
+__device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float* smem, const PbProf& pf,
+                         const float* bx = nullptr, const float* bw = nullptr) {
     const int M = a.nz, L = a.nr - 1, K = a.Kx;
     int mt, nt0;
     const int ntiles = pb_xtiles(a, mt, nt0);
@@ -2310,7 +2365,10 @@ __device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float
 #pragma unroll
             for (int gg = 0; gg < PB_KG; ++gg) v += red[gg * (PB_BM * PB_BN) + o];
             const int m = m0 + o / PB_BN, n = n0 + o % PB_BN;
-            if (m < M && n < N) out[(long)m * a.nr + 2 * n + par] = v;
+            if (m < M && n < N) {
+                const long q = (long)m * a.nr + 2 * n + par;
+                out[q] = bw ? v + __ldg(bw + q) * (__ldcg(bx + q) - v) : v;
+            }
         }
         pb_mark(pf, 2);
         __syncthreads();
@@ -2489,13 +2547,14 @@ __device__ void pb_zdz(const PersistArgs& a, const float* X, float* out, float* 
     }
 }
 
-// psolve: y = DCT-I preconditioner applied to x (three phases, two internal barriers).
+// psolve: y = DCT-I preconditioner applied to x (three phases, two internal barriers), blended
+// with x by the per-cell weights a.pcw when they are installed.
 __device__ bool pb_psolve(const PersistArgs& a, const float* x, float* y, float* smem, unsigned& gen, PbProf& pf) {
     pb_xpass(a, x, a.w1, smem, pf);
     if (!grid_sync(a.bar, gen, pf)) return false;
     pb_zdz(a, a.w1, a.w2, smem, &pf);
     if (!grid_sync(a.bar, gen, pf)) return false;
-    pb_xpass(a, a.w2, y, smem, pf);
+    pb_xpass(a, a.w2, y, smem, pf, x, a.pcw);
     return true;
 }
 
@@ -3277,6 +3336,21 @@ void launch_bi_diag_apply(long n, const T* x, const T* diag, int ident, T* y, co
     k_bi_diag_apply<T><<<GRID(n)>>>(n, x, diag, ident, y, ks, gate, ctr);
 }
 template <typename T>
+void launch_pc_blend(long n, const T* x, const T* w, T* y, const KState* ks, int gate, ull* ctr, cudaStream_t s) {
+    k_pc_blend<T><<<GRID(n)>>>(n, x, w, y, ks, gate, ctr);
+}
+void launch_probe_fill(long n, unsigned long long seed, long probe, double* e, ull* ctr, cudaStream_t s) {
+    k_probe_fill<<<GRID(n)>>>(n, seed, probe, e, ctr);
+}
+void launch_probe_acc(long n, unsigned long long seed, long probe, const double* r, const double* qv, double* num,
+                      double* den, int first, ull* ctr, cudaStream_t s) {
+    k_probe_acc<<<GRID(n)>>>(n, seed, probe, r, qv, num, den, first, ctr);
+}
+void launch_probe_final(long n, const double* num, const double* den, double* w, float* w32, ull* ctr,
+                        cudaStream_t s) {
+    k_probe_final<<<GRID(n)>>>(n, num, den, w, w32, ctr);
+}
+template <typename T>
 void launch_bi_xr(long n, const T* phat, const T* shat, const T* t, const T* rtld, T* x, T* r, KState* ks,
                   const Dots& d, ull* ctr, cudaStream_t s) {
     k_bi_xr<T><<<d.G, DRD_TPB, 0, s>>>(n, phat, shat, t, rtld, x, r, ks, d, ctr);
@@ -3364,6 +3438,7 @@ template void launch_mx_scale<float>(long, const double*, const KState*, float*,
                                  cudaStream_t);                                                                       \
     template void launch_bi_s<T>(long, const T*, T*, KState*, const Dots&, ull*, cudaStream_t);                       \
     template void launch_bi_diag_apply<T>(long, const T*, const T*, int, T*, const KState*, int, ull*, cudaStream_t); \
+    template void launch_pc_blend<T>(long, const T*, const T*, T*, const KState*, int, ull*, cudaStream_t);          \
     template void launch_bi_xr<T>(long, const T*, const T*, const T*, const T*, T*, T*, KState*, const Dots&, ull*,   \
                                   cudaStream_t);                                                                      \
     template void launch_copy<T>(long, const T*, T*, ull*, cudaStream_t);                                            \

@@ -169,6 +169,7 @@ struct PersistArgs {
     OpScal<float> o;
     // CH: mobilities (CELL), packed Ph_Lcc, folded DCT-I operands
     const float *M0, *Mi, *lcc;
+    const float* pcw;  // solid-blend weights of the CH preconditioner (packed), or null
     const float *fxe, *fxo, *fze, *fzo;
     int Kx, Nxe, Nxo, Kz, Mze, Mzo;
     // momentum: rho, eta, penalty mask (CELL), Jacobi diagonal; ident = identity preconditioner
@@ -242,6 +243,13 @@ void launch_bi_p(long n, const T* r, const T* v, T* p, T* phat, const T* diag, i
 template <typename T>
 void launch_bi_s(long n, const T* v, T* r, KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
 void launch_bi_snorm(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_pc_blend(long n, const T* x, const T* w, T* y, const KState* ks, int gate, ull* ctr, cudaStream_t s);
+void launch_probe_fill(long n, unsigned long long seed, long probe, double* e, ull* ctr, cudaStream_t s);
+void launch_probe_acc(long n, unsigned long long seed, long probe, const double* r, const double* qv, double* num,
+                      double* den, int first, ull* ctr, cudaStream_t s);
+void launch_probe_final(long n, const double* num, const double* den, double* w, float* w32, ull* ctr,
+                        cudaStream_t s);
 template <typename T>
 void launch_bi_diag_apply(long n, const T* x, const T* diag, int ident, T* y, const KState* ks, int gate, ull* ctr,
                           cudaStream_t s);

@@ -53,6 +53,11 @@ struct drd_ctx {
     // tables and transform matrices
     double *ph_lcc, *pre_lcc;
     float* ph_lcc32;
+    // the solid-blended CH preconditioner: per-cell weights (FP64 and FP32, packed), the probe
+    // accumulators; allocated on first use, pc_on when weights are installed
+    double *pcw = nullptr, *pnum = nullptr, *pden = nullptr;
+    float* pcw32 = nullptr;
+    int pc_on = 0;
     double *m2xT, *m2z, *m3xT, *m3z;
     // folded DCT-I (VCOST) matrices of the CH preconditioner: x pass B operands (even / odd
     // output columns, Kx x Nxe each) and z pass A operands (even / odd output rows, Mze x Kz)
@@ -512,8 +517,11 @@ void enq_matvec(drd_ctx* c, const Sys& S, T alpha, const T* x, T beta, T* y, con
 template <typename T>
 void enq_psolve(drd_ctx* c, const Sys& S, const T* x, T* y, const KState* ks, int gate, cudaStream_t s) {
     KVecs<T>& k = vecs(c, (T*)nullptr);
-    if (S.kind == SYS_CH || S.kind == SYS_ORI) enq_ch_psolve<T>(c, x, y, ks, gate, s);
-    else if (S.esolp) enq_esolp<T>(c, S.bdf, x, y, ks, gate, s);
+    if (S.kind == SYS_CH || S.kind == SYS_ORI) {
+        enq_ch_psolve<T>(c, x, y, ks, gate, s);
+        if (S.kind == SYS_CH && c->pc_on)
+            launch_pc_blend<T>(S.n, x, (sizeof(T) == 8) ? (const T*)c->pcw : (const T*)c->pcw32, y, ks, gate, c->ctr, s);
+    } else if (S.esolp) enq_esolp<T>(c, S.bdf, x, y, ks, gate, s);
     else launch_bi_diag_apply<T>(S.n, x, S.jacobi ? k.diag : nullptr, S.ident, y, ks, gate, c->ctr, s);
 }
 
@@ -682,6 +690,7 @@ PersistArgs persist_args(drd_ctx* c, const Sys& S, KState* in, const KState* par
     a.nr = c->nr; a.nz = c->nz; a.n = S.n;
     a.o = make_op<float>(c, S.kind == SYS_UV ? S.bdf : 0);
     a.M0 = c->M032; a.Mi = c->Mi32; a.lcc = c->ph_lcc32;
+    a.pcw = (S.kind == SYS_CH && c->pc_on) ? c->pcw32 : nullptr;
     a.fxe = c->f1xe32; a.fxo = c->f1xo32; a.fze = c->f1ze32; a.fzo = c->f1zo32;
     a.Kx = c->Kx; a.Nxe = c->Nxe; a.Nxo = c->Nxo; a.Kz = c->Kz; a.Mze = c->Mze; a.Mzo = c->Mzo;
     KVecs<float>& f = c->k32;
@@ -1386,6 +1395,10 @@ int drd_destroy(drd_ctx* c) {
     if (c->h_stage) cudaFreeHost(c->h_stage);
     clear_graphs(c);
     if (c->arena) cudaFree(c->arena);
+    if (c->pcw) cudaFree(c->pcw);
+    if (c->pcw32) cudaFree(c->pcw32);
+    if (c->pnum) cudaFree(c->pnum);
+    if (c->pden) cudaFree(c->pden);
     if (c->h_ks) cudaFreeHost(c->h_ks);
     if (c->h_ca) cudaFreeHost(c->h_ca);
     if (c->h_mass) cudaFreeHost(c->h_mass);
@@ -1431,12 +1444,75 @@ int drd_set_coefs(drd_ctx* c, const double* rho, const double* eta, const double
     rc |= up(c, c->M0, ph_M_0, c->cs);
     rc |= up(c, c->Mi, ph_M_inner, c->cs);
     if (rc) return DRD_ERR_CUDA;
+    // blend weights belong to the mobilities they were fitted for
+    if ((ph_M_0 || ph_M_inner) && c->pc_on) {
+        c->pc_on = 0;
+        clear_graphs(c);
+    }
     // MF penalises with bdr_ph itself (VeloSolve_2_combined.f90:580); TP keeps its own mask
     if (bdr_ph && c->P.variant == DRD_VARIANT_MF)
         CK(cudaMemcpyAsync(c->pen, c->bdr, sizeof(double) * c->cs, cudaMemcpyDeviceToDevice, c->s));
     rc = refresh_fp32(c);
     if (rc) return rc;
     CK(cudaStreamSynchronize(c->s));
+    return DRD_OK;
+}
+
+// ---- the solid-blended CH preconditioner ----------------------------------------------------
+int pc_alloc(drd_ctx* c) {
+    if (c->pcw) return DRD_OK;
+    CK(cudaMalloc(&c->pcw, sizeof(double) * c->nc));
+    CK(cudaMalloc(&c->pcw32, sizeof(float) * c->nc));
+    CK(cudaMalloc(&c->pnum, sizeof(double) * c->nc));
+    CK(cudaMalloc(&c->pden, sizeof(double) * c->nc));
+    return DRD_OK;
+}
+
+// Turns the blend on or off; the step and solve graphs hold the choice, so a change drops them.
+void pc_switch(drd_ctx* c, int on) {
+    if (c->pc_on == on) return;
+    c->pc_on = on;
+    clear_graphs(c);
+}
+
+int drd_set_ch_blend(drd_ctx* c, const double* w) {
+    if (!c) return DRD_ERR_BADARG;
+    if (c->P.variant != DRD_VARIANT_MF) { c->err = "the blended preconditioner belongs to PhSolve (MF)"; return DRD_ERR_UNSUPPORTED; }
+    if (!w) { pc_switch(c, 0); return DRD_OK; }
+    int rc = pc_alloc(c);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->pcw, w, sizeof(double) * c->nc, cudaMemcpyDefault, c->s));
+    launch_convert_scale<float, double>(c->nc, c->pcw, 1.0, c->pcw32, nullptr, c->s);
+    CK(cudaStreamSynchronize(c->s));
+    CK(cudaGetLastError());
+    pc_switch(c, 1);
+    return DRD_OK;
+}
+
+int drd_ch_blend_probe(drd_ctx* c, int nprobe, uint64_t seed, int install, double* w_out) {
+    if (!c || nprobe < 1) return DRD_ERR_BADARG;
+    if (c->P.variant != DRD_VARIANT_MF) { c->err = "the blended preconditioner belongs to PhSolve (MF)"; return DRD_ERR_UNSUPPORTED; }
+    int rc = ensure_tuned(c);
+    if (rc) return rc;
+    rc = pc_alloc(c);
+    if (rc) return rc;
+    const long n = c->nc;
+    Sys S = sys_of(c, SYS_CH, 0);
+    KVecs<double>& k = c->k64;
+    // the probes see the reference preconditioner alone: fit the weights, then install them
+    for (int p = 0; p < nprobe; ++p) {
+        launch_probe_fill(n, seed, p, k.tmp, c->ctr, c->s);
+        enq_matvec<double>(c, S, 1.0, k.tmp, 0.0, k.v, nullptr, 0, 0, nullptr, G_ALWAYS, c->s);
+        enq_ch_psolve<double>(c, k.v, k.phat, nullptr, G_ALWAYS, c->s);
+        launch_probe_acc(n, seed, p, k.v, k.phat, c->pnum, c->pden, p == 0, c->ctr, c->s);
+    }
+    double* wd = install ? c->pcw : k.tmp;  // not installing: the probe vector's buffer holds the fit
+    float* w32 = install ? c->pcw32 : c->k32.tmp;
+    launch_probe_final(n, c->pnum, c->pden, wd, w32, c->ctr, c->s);
+    if (w_out) CK(cudaMemcpyAsync(w_out, wd, sizeof(double) * n, cudaMemcpyDefault, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    CK(cudaGetLastError());
+    if (install) pc_switch(c, 1);
     return DRD_OK;
 }
 

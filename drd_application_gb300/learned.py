@@ -268,6 +268,153 @@ def evaluate_ch(case, net, pairs, precision=F.DRD_PREC_MIXED, tol=1e-8, judge="r
         ctx.close()
 
 
+# ------------------------------------------------------------------------------------------
+# The learned blend inside the CH preconditioner.
+#
+# PSolve_CG (microfluidics_complex_domain/PhSolve.f90:296-313) inverts the CH operator with unit
+# mobility everywhere.  The library's blended form y = q + w (x - q) (drd_set_ch_blend) adds the
+# identity where the mobilities vanish, which is what the operator tends to in the solid.  The
+# best per-cell w of a geometry is fitted on the GPU from Rademacher probes
+# (drd_ch_blend_probe); the network learns the map from the mobility fields to that fit, so a
+# geometry gets its weights from one forward pass, and the network's fit, trained on many
+# geometries, carries less probe noise than a fit from one geometry's probes.
+#
+# Inputs, 3 channels on the nz x nr interior: (log10 M0)/12 + 1, (log10 Mi)/12 + 1 (M clamped to
+# >= 1e-12) and M0.  Target: 1 + ln(w + BLEND_FLOOR) / ln(1/BLEND_FLOOR), so that an error in the
+# output is a relative error in w, and the fluid's w = 0 comes out within a few 1e-5 of zero (a
+# weight of 1e-2 in the fluid would undo most of the gain).
+
+BLEND_FLOOR = 1e-4
+_BLEND_SCALE = float(np.log(1.0 / BLEND_FLOOR))
+
+
+def blend_features(M0, Mi):
+    """(3, nz, nr) float32 network input from the CELL mobility fields."""
+    m0, mi = _interior(M0), _interior(Mi)
+    x = np.empty((3,) + m0.shape, dtype=np.float32)
+    x[0] = np.log10(np.maximum(m0, 1e-12)) / 12.0 + 1.0
+    x[1] = np.log10(np.maximum(mi, 1e-12)) / 12.0 + 1.0
+    x[2] = m0
+    return x
+
+
+def blend_target(w):
+    """Network target of weights w (any shape)."""
+    return (1.0 + np.log(np.asarray(w, dtype=np.float64) + BLEND_FLOOR) / _BLEND_SCALE).astype(np.float32)
+
+
+def blend_weights(y):
+    """Weights in [0, 1] (FP64) from network outputs y."""
+    y = np.asarray(y, dtype=np.float64)
+    return np.clip(np.exp((y - 1.0) * _BLEND_SCALE) - BLEND_FLOOR, 0.0, 1.0)
+
+
+def blend_pairs(cases, nprobe=64, seed=0):
+    """Probe-fitted blend weights of each case's mobilities (one GPU context, the cases share
+    their grid and parameters): dict(x=(n,3,nz,nr) inputs, y=(n,1,nz,nr) targets, w=(n, nr*nz)
+    weights)."""
+    P = cases[0].params.copy()
+    ctx = DRDContext(P)
+    try:
+        X, Y, W = [], [], []
+        for k, case in enumerate(cases):
+            M0, Mi = case.coefs["M0"], case.coefs["Mi"]
+            ctx.set_coefs(ph_M_0=M0, ph_M_inner=Mi)
+            w = ctx.ch_blend_probe(nprobe, seed + k, install=False)
+            X.append(blend_features(M0, Mi))
+            Y.append(blend_target(w).reshape(1, P.nz, P.nr))
+            W.append(w)
+        return dict(x=np.stack(X), y=np.stack(Y), w=np.stack(W))
+    finally:
+        ctx.close()
+
+
+def flip_augment(data):
+    """Adds the mirror images along x, along z and along both (the CH operator, its Neumann
+    sides and the DCT-I preconditioner are symmetric under both reflections)."""
+    xs, ys = [data["x"]], [data["y"]]
+    for ax in ((-1,), (-2,), (-2, -1)):
+        xs.append(np.ascontiguousarray(np.flip(data["x"], ax)))
+        ys.append(np.ascontiguousarray(np.flip(data["y"], ax)))
+    return dict(x=np.concatenate(xs), y=np.concatenate(ys))
+
+
+def learned_blend(net, M0, Mi):
+    """The network's blend weights (packed nr*nz, FP64) for the CELL mobility fields."""
+    x = blend_features(M0, Mi)[None]
+    y = net.forward(np.ascontiguousarray(x))
+    return blend_weights(y[0, 0]).reshape(-1)
+
+
+def train_blend(train_cases, steps=800, nprobe=64, batch=8, lr=1e-3, lr_final=1e-4, seed=0, log_every=0):
+    """Fits the blend weights of `train_cases` on the GPU and trains a network on them (with
+    mirror images).  Returns (net, info)."""
+    t0 = time.perf_counter()
+    data = flip_augment(blend_pairs(train_cases, nprobe, seed=1 << 20))
+    t1 = time.perf_counter()
+    P = train_cases[0].params
+    net = UNet(P.nz, P.nr, 3, 1, max_batch=batch, seed=seed)
+    losses = train(net, data, steps, batch=batch, lr=lr, lr_final=lr_final, seed=seed, log_every=log_every)
+    t2 = time.perf_counter()
+    info = {"geometries": len(train_cases), "samples": int(data["x"].shape[0]), "probes": nprobe,
+            "adam_steps": steps, "data_s": t1 - t0, "train_s": t2 - t1,
+            "loss_first": float(np.mean(losses[:10])), "loss_last": float(np.mean(losses[-20:]))}
+    return net, info
+
+
+def evaluate_blend(case, weights, warmup=4, steps=8):
+    """Steps of `case` (mixed, the case's guess mode) for each entry of `weights` (name -> packed
+    weights, or None for PSolve_CG alone): mean CH iterations and CH solve seconds over the last
+    `steps` steps, and the largest FP64 true residual."""
+    out = {}
+    for name, w in weights.items():
+        P = case.params.copy()
+        P.precision = F.DRD_PREC_MIXED
+        ctx = DRDContext(P)
+        try:
+            ctx.set_case(case)
+            ctx.upload_state(case.state)
+            if w is not None:
+                ctx.set_ch_blend(w)
+            its, secs, tr, ok = [], [], [], 0
+            t = 0.0
+            for k in range(warmup + steps):
+                st = ctx.step(k == 0, t)
+                t += P.dt
+                if k >= warmup:
+                    its.append(st.ch.iter)
+                    secs.append(st.ch.seconds)
+                    tr.append(st.ch.true_resid)
+                    ok += int(st.ch.info == 0 and st.ch.true_resid <= P.tol)
+            out[name] = {"ch_iters": float(np.mean(its)), "ch_solve_ms": 1e3 * float(np.mean(secs)),
+                         "max_true_resid": float(np.max(tr)), "converged": f"{ok}/{steps}"}
+        finally:
+            ctx.close()
+    return out
+
+
+def blend_main(a):
+    from .workloads import make_case
+
+    train_cases = [make_case("c2", seed=1000 + s, nr=a.nr, nz=a.nz, precision=F.DRD_PREC_MIXED, guess_mode=3)
+                   for s in range(a.train_seeds)]
+    net, info = train_blend(train_cases, steps=a.steps, nprobe=a.probes, log_every=max(a.steps // 8, 1))
+    print(f"blend network: {info}", flush=True)
+    if a.save:
+        np.save(a.save, net.get_params())
+    for s in range(a.eval_seeds):
+        case = make_case("c2", seed=2000 + s, nr=a.nr, nz=a.nz, precision=F.DRD_PREC_MIXED, guess_mode=3)
+        ref = blend_pairs([case], a.probes, seed=7)
+        w_net = learned_blend(net, case.coefs["M0"], case.coefs["Mi"])
+        err = float(np.sqrt(np.mean((blend_target(w_net) - blend_target(ref["w"][0])) ** 2)))
+        ev = evaluate_blend(case, {"PSolve_CG": None, "probe fit": ref["w"][0], "learned": w_net})
+        print(f"held-out seed {2000 + s}: target-space RMS error of the learned weights {err:.3f}", flush=True)
+        for name, r in ev.items():
+            print(f"  {name:10s} CH iterations {r['ch_iters']:6.1f}  CH solve {r['ch_solve_ms']:6.2f} ms  "
+                  f"converged {r['converged']}  max true residual {r['max_true_resid']:.2e}", flush=True)
+    net.close()
+
+
 def _layers():
     """(cin, cout, level) of the 17 3x3 layers, as drd_unet_create builds them."""
     L = []
@@ -309,7 +456,12 @@ def main(argv=None):
     ap.add_argument("--lowpass", type=float, nargs="*", default=[],
                     help="also evaluate the learned and the exact corrections with only the lowest fraction "
                          "of their DCT-II modes kept along each axis (evaluation only)")
+    ap.add_argument("--blend", action="store_true",
+                    help="train and evaluate the learned blend of the CH preconditioner instead of the guess")
+    ap.add_argument("--probes", type=int, default=64, help="Rademacher probes per geometry (--blend)")
     a = ap.parse_args(argv)
+    if a.blend:
+        return blend_main(a)
     t0 = time.perf_counter()
     parts = [ch_run_pairs(make_case("c2", seed=1000 + s, nr=a.nr, nz=a.nz), a.per_seed, a.warmup, base=a.base)
              for s in range(a.train_seeds)]

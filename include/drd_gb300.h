@@ -153,6 +153,24 @@ int drd_set_coefs(drd_ctx* ctx, const double* rho, const double* eta, const doub
 int drd_set_tp_fields(drd_ctx* ctx, const double* bdr_ph_used, const double* bdr_ph_penalty,
                       const double* angleB, const double* angleT);
 
+/* ---- the solid-blended CH preconditioner (an extension; the reference has no counterpart) --
+ * PSolve_CG (microfluidics_complex_domain/PhSolve.f90:296-313) inverts the CH operator with
+ * unit mobility everywhere.  In the solid the mobilities ph_M_0, ph_M_inner vanish and the
+ * operator tends to the identity, which that solve resolves worst.  With weights w installed
+ * (packed nr x nz, the CH unknowns' order, values in [0, 1]) every CH preconditioner
+ * application becomes y = q + w (x - q), q = PSolve_CG(x): a fixed linear operator, so
+ * BiCGSTAB is unchanged and the solve still ends on the reference's residual test.  MF only.
+ * The weights belong to the mobilities: drd_set_coefs with new ph_M_0 or ph_M_inner removes them. */
+
+/* Installs w (host or device memory), or removes the weights when w is NULL. */
+int drd_set_ch_blend(drd_ctx* ctx, const double* w);
+/* Fits the weights of the current mobilities with `nprobe` Rademacher probes e (entries +-1, the
+ * sign of the top bit of splitmix64(seed + (probe nr nz + q + 1) 0x9E3779B97F4A7C15)): r = A e,
+ * q = PSolve_CG(r), d = r - q, t = e - q, w = clamp(sum t d / sum d d, 0, 1) per cell (0 where
+ * sum d d = 0), in FP64.  Installs them when `install` is non-zero; writes them to w_out (host or
+ * device, may be NULL). */
+int drd_ch_blend_probe(drd_ctx* ctx, int nprobe, uint64_t seed, int install, double* w_out);
+
 /* ---- the per-step solver core (drop-in for the reference subroutines) ------------------ */
 
 /* interpolate_coef (microfluidics_complex_domain/interpolate_coef.f90:4-92).  `dist` is the

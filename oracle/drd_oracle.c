@@ -1141,6 +1141,76 @@ int orc_solve_system(const drd_params* P, int system, int bdf, const double* ph_
     return orc_bicgstab(uv_len(P->nr, P->nz), b, x, P->uv_maxit, P->tol, uv_mv_cb, uv_ps_cb, &C, st);
 }
 
+/* ---------------------------------------------------------------------------------------
+ * The solid-blended CH preconditioner (an extension of PSolve_CG, PhSolve.f90:296-313; the
+ * reference has no counterpart): y = q + w (x - q) with q = PSolve_CG(x) and a per-cell weight
+ * w in [0, 1] on the packed nr x nz cells.  In the solid the mobilities vanish and the CH
+ * operator tends to the identity, which the constant-mobility DCT-I solve does not resolve;
+ * w blends the identity in there.  The fitted weight of a geometry comes from Rademacher
+ * probes e (entries +-1): r = A e, q = PSolve_CG(r), d = r - q, t = e - q and per cell
+ * w = clamp(sum t d / sum d d, 0, 1) (0 where sum d d = 0), the least-squares weight that maps
+ * the probes' d onto their t.
+ * ------------------------------------------------------------------------------------- */
+void orc_ch_psolve_blend(const drd_params* P, const double* ph_lcc, const double* w, const double* x, double* y) {
+    const long n = (long)P->nr * P->nz;
+    orc_ch_psolve(P, ph_lcc, x, y);
+    if (!w) return;
+    for (long q = 0; q < n; ++q) y[q] = y[q] + w[q] * (x[q] - y[q]);
+}
+
+/* Entry q of probe `probe`: +1 or -1 from the top bit of splitmix64(seed + (probe n + q + 1) G),
+ * G = 0x9E3779B97F4A7C15 (the same integer arithmetic as the device generator). */
+double orc_probe_sign(uint64_t seed, long probe, long n, long q) {
+    uint64_t z = seed + (uint64_t)(probe * n + q + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z = z ^ (z >> 31);
+    return (z >> 63) ? -1.0 : 1.0;
+}
+
+void orc_ch_blend_probe(const drd_params* P, const double* ph_lcc, const double* M0, const double* Mi, int nprobe,
+                        uint64_t seed, double* w) {
+    const long n = (long)P->nr * P->nz;
+    double* e = dalloc(n);
+    double* r = dalloc(n);
+    double* q = dalloc(n);
+    double* num = dalloc(n);
+    double* den = dalloc(n);
+    for (long i = 0; i < n; ++i) num[i] = den[i] = 0.0;
+    for (int p = 0; p < nprobe; ++p) {
+        for (long i = 0; i < n; ++i) e[i] = orc_probe_sign(seed, p, n, i);
+        orc_ch_matvec(P, M0, Mi, 1.0, e, 0.0, r);
+        orc_ch_psolve(P, ph_lcc, r, q);
+        for (long i = 0; i < n; ++i) {
+            const double d = r[i] - q[i], t = e[i] - q[i];
+            num[i] += t * d;
+            den[i] += d * d;
+        }
+    }
+    for (long i = 0; i < n; ++i) {
+        const double v = den[i] > 0.0 ? num[i] / den[i] : 0.0;
+        w[i] = v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v);
+    }
+    free(e); free(r); free(q); free(num); free(den);
+}
+
+typedef struct { const drd_params* P; const double* M0; const double* Mi; const double* lcc; const double* w; } chb_ctx;
+static void chb_mv_cb(void* c, double a, const double* x, double b, double* y) {
+    chb_ctx* C = (chb_ctx*)c;
+    orc_ch_matvec(C->P, C->M0, C->Mi, a, x, b, y);
+}
+static void chb_ps_cb(void* c, const double* x, double* y) {
+    chb_ctx* C = (chb_ctx*)c;
+    orc_ch_psolve_blend(C->P, C->lcc, C->w, x, y);
+}
+
+/* PhSolve's BiCGSTAB (lib/BiCGSTAB.f) with the blended preconditioner. */
+int orc_ch_solve_blend(const drd_params* P, const double* ph_lcc, const double* M0, const double* Mi, const double* w,
+                       const double* b, double* x, drd_status* st) {
+    chb_ctx C = {P, M0, Mi, ph_lcc, w};
+    return orc_bicgstab((long)P->nr * P->nz, b, x, P->ch_maxit, P->tol, chb_mv_cb, chb_ps_cb, &C, st);
+}
+
 /* The variable-coefficient pressure Poisson operator of the batched solves (no reference
  * counterpart: PreSolve_2 is a direct DCT solve): y = d/dx(beta dx/dx) + d/dz(beta dx/dz) on the
  * packed nr x nz cells, beta = 1/(1 + penalty_k dt bdr_ph), face values the mean of the two

@@ -40,6 +40,14 @@ void orc_op_double_gradient_neum(int nr, int nz, double dr2, double dz2, const d
 void orc_ch_matvec(const drd_params* P, const double* M0, const double* Mi, double alpha,
                    const double* x, double beta, double* y);              /* PhSolve.f90:240-292 */
 void orc_ch_psolve(const drd_params* P, const double* ph_lcc, const double* x, double* y); /* :296-313 */
+/* The solid-blended CH preconditioner y = q + w (x - q), q = PSolve_CG(x), its probe fit and
+ * BiCGSTAB with it (an extension; no reference counterpart). */
+void orc_ch_psolve_blend(const drd_params* P, const double* ph_lcc, const double* w, const double* x, double* y);
+double orc_probe_sign(uint64_t seed, long probe, long n, long q);
+void orc_ch_blend_probe(const drd_params* P, const double* ph_lcc, const double* M0, const double* Mi, int nprobe,
+                        uint64_t seed, double* w);
+int orc_ch_solve_blend(const drd_params* P, const double* ph_lcc, const double* M0, const double* Mi, const double* w,
+                       const double* b, double* x, drd_status* st);
 
 /* Operators of the momentum system on packed vectors of length (nr+1)nz + nr(nz-1). */
 void orc_uv_matvec(const drd_params* P, int bdf, const double* rho, const double* eta,

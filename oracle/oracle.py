@@ -51,6 +51,11 @@ def lib(openmp=False):
         L.orc_op_double_gradient_neum.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, dp, dp, dp]
         L.orc_ch_matvec.argtypes = [P, dp, dp, C.c_double, dp, C.c_double, dp]
         L.orc_ch_psolve.argtypes = [P, dp, dp, dp]
+        L.orc_ch_psolve_blend.argtypes = [P, dp, dp, dp, dp]
+        L.orc_probe_sign.argtypes = [C.c_uint64, C.c_long, C.c_long, C.c_long]
+        L.orc_probe_sign.restype = C.c_double
+        L.orc_ch_blend_probe.argtypes = [P, dp, dp, dp, C.c_int, C.c_uint64, dp]
+        L.orc_ch_solve_blend.argtypes = [P, dp, dp, dp, dp, dp, dp, S]
         L.orc_uv_matvec.argtypes = [P, C.c_int, dp, dp, dp, C.c_double, dp, C.c_double, dp]
         L.orc_uv_psolve.argtypes = [P, C.c_int, dp, dp, dp, dp]
         L.orc_uv_psolve_esolp.argtypes = [P, C.c_int, dp, dp]
@@ -156,6 +161,28 @@ class Oracle:
         y = np.zeros_like(x)
         self.L.orc_ch_psolve(C.byref(self.P), ptr(self.ph_lcc), ptr(np.ascontiguousarray(x)), ptr(y))
         return y
+
+    def ch_psolve_blend(self, w, x):
+        """y = q + w (x - q), q = PSolve_CG(x) (w None: PSolve_CG alone)."""
+        y = np.zeros_like(x)
+        self.L.orc_ch_psolve_blend(C.byref(self.P), ptr(self.ph_lcc), None if w is None else ptr(np.ascontiguousarray(w)),
+                                   ptr(np.ascontiguousarray(x)), ptr(y))
+        return y
+
+    def ch_blend_probe(self, M0, Mi, nprobe, seed):
+        """The probe-fitted blend weights (packed nr x nz) of the CH operator with mobilities M0, Mi."""
+        w = np.zeros(self.P.nr * self.P.nz)
+        self.L.orc_ch_blend_probe(C.byref(self.P), ptr(self.ph_lcc), ptr(M0), ptr(Mi), int(nprobe), int(seed), ptr(w))
+        return w
+
+    def ch_solve_blend(self, M0, Mi, w, b, x0=None):
+        """BiCGSTAB on the CH system with the blended preconditioner; returns (x, status)."""
+        x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
+        st = abi.drd_status()
+        self.L.orc_ch_solve_blend(C.byref(self.P), ptr(self.ph_lcc), ptr(M0), ptr(Mi),
+                                  None if w is None else ptr(np.ascontiguousarray(w)), ptr(np.ascontiguousarray(b)),
+                                  ptr(x), C.byref(st))
+        return x, st
 
     def uv_matvec(self, bdf, rho, eta, pen, x, alpha=1.0, beta=0.0, y=None):
         y = np.zeros_like(x) if y is None else np.array(y, dtype=np.float64)
