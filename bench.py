@@ -9,9 +9,12 @@ viscosity ratio 5, Re 0.5, Ca 0.05.  A step is one pass of the reference's time 
 (CH solve -> momentum solve -> pressure solve -> p += psi), every Krylov solve to the deck
 tolerance 1e-8 (relative FP64 residual).  Inputs are synthetic (seeded), as no dataset exists.
 
-value: time-steps/s of the mixed path (FP32 Krylov solves inside FP64 iterative refinement)
-with the state resident in HBM, device-timed with CUDA events per step, L2 flushed between
-steps.  The plain FP64 path is timed the same way and reported beside it.  e2e: the same
+value: time-steps/s of the learned + mixed path (FP32 Krylov solves inside FP64 iterative
+refinement; the CH preconditioner blended per cell by weights that a U-Net, trained before the
+timed region on other seeded geometries, predicts from the mobility fields) with the state
+resident in HBM, device-timed with CUDA events per step, L2 flushed between steps.  The plain
+FP64 path (the reference's arithmetic, guess and preconditioner) is timed the same way and
+reported beside it, with arms that split the ratio into its factors.  e2e: the same
 metric through the drop-in C-ABI routines with host arrays (PhSolve, VeloSolve_2_combined,
 PreSolve_2 each step, host<->device copies inside the timed region).
 
@@ -37,7 +40,9 @@ sys.path.insert(0, ROOT)
 METRIC = "time-steps/s and solves/s to FP64 resid 1e-8: learned+FP32 vs plain FP64, 1 GB300"
 # DRAM bytes (read + write) of one launch of the persistent CH solve kernel, from an ncu capture
 # of this workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch)
-TRAFFIC_CH = 4043776 + 558848
+TRAFFIC_CH = 4353792 + 371712
+# the same for one launch of the persistent momentum solve kernel (the same capture)
+TRAFFIC_UV = 6082048 + 141312
 WORKLOAD = ("420x180 serpentine channel (amp 30, period 140 cells, penalty 1e4), 3 rigid fibers 40x4, "
             "2 drops R=15, lambda_eta 5, Re 0.5, Ca 0.05; CH + momentum + pressure per step, tol 1e-8")
 
@@ -45,7 +50,7 @@ WORKLOAD = ("420x180 serpentine channel (amp 30, period 140 cells, penalty 1e4),
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=None, help="timed steps of the plain FP64 path")
@@ -56,6 +61,9 @@ def parse():
                     help="steps of the 2048x1024 C5 comparison, mixed against FP64 (0: skip)")
     ap.add_argument("--learned-steps", type=int, default=600,
                     help="Adam steps of the learned CH guess leg (0: skip)")
+    ap.add_argument("--blend-steps", type=int, default=800,
+                    help="Adam steps of the blend network that drives the headline (0: PSolve_CG alone)")
+    ap.add_argument("--blend-geometries", type=int, default=16, help="training geometries of the blend network")
     ap.add_argument("--nr", type=int, default=420)
     ap.add_argument("--nz", type=int, default=180)
     return ap.parse_args()
@@ -112,6 +120,10 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once the sampler is delivering (at most 5 s of waiting)
+            t0 = time.perf_counter()
+            while not self.rows and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except FileNotFoundError:
             self.proc = None
 
@@ -245,10 +257,16 @@ def time_c5(steps, seed=0):
     from drd_application_gb300.workloads import make_case
 
     out, fields = {}, {}
-    for name, prec, gm in (("mixed", abi.DRD_PREC_MIXED, 3), ("fp64", abi.DRD_PREC_FP64, 0)):
+    for name, prec, gm, pc in (("mixed", abi.DRD_PREC_MIXED, 3, None), ("mixed_probe_blend", abi.DRD_PREC_MIXED, 3, 64),
+                               ("fp64", abi.DRD_PREC_FP64, 0, None)):
         case = make_case("c5", seed=seed, precision=prec, guess_mode=gm)
         ctx = DRDContext(case.params)
         ctx.set_case(case)
+        fit_s = None
+        if pc:  # this geometry's probe-fitted blend of the CH preconditioner
+            t0 = time.perf_counter()
+            ctx.ch_blend_probe(pc, 11, install=True)
+            fit_s = time.perf_counter() - t0
         ctx.upload_state(case.state)
         m0 = ctx.mass(case.state[abi.F_PH])
         t, rows = 0.0, []
@@ -265,10 +283,13 @@ def time_c5(steps, seed=0):
             "uv": [{"info": r.uv.info, "iter": r.uv.iter, "true_resid": r.uv.true_resid} for r in rows],
             "mass_drift_per_step": (rows[-1].mass - m0) / abs(m0) / steps,
         }
+        if fit_s is not None:
+            out[name]["probe_fit_s"] = fit_s
     rel = lambda a, b: float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))  # noqa: E731
-    out["mixed_vs_fp64"] = {"u": rel(fields["mixed"][abi.F_U], fields["fp64"][abi.F_U]),
-                            "v": rel(fields["mixed"][abi.F_V], fields["fp64"][abi.F_V]),
-                            "ph": rel(fields["mixed"][abi.F_PH], fields["fp64"][abi.F_PH])}
+    for name in ("mixed", "mixed_probe_blend"):
+        out[name + "_vs_fp64"] = {"u": rel(fields[name][abi.F_U], fields["fp64"][abi.F_U]),
+                                  "v": rel(fields[name][abi.F_V], fields["fp64"][abi.F_V]),
+                                  "ph": rel(fields[name][abi.F_PH], fields["fp64"][abi.F_PH])}
     out["steps"] = steps
     out["workload"] = "c5 2048x1024: serpentine channel (amp 150, period 680), 64 fibers 60x6, 32 drops, lambda_eta 10"
     return out
@@ -432,6 +453,7 @@ def time_resident(ctx, case, warmup, steps, flush_bytes):
     ctx.synchronize()
     launches0 = ctx.kernel_launches()
     per, ch_it, uv_it, refine, resid, ok, ch_solve, ch_ref = [], [], [], [], [], 0, [], []
+    uv_solve, uv_ref = [], []
     for s in range(steps):
         ctx.flush_l2(flush_bytes)
         ctx.synchronize()
@@ -443,6 +465,8 @@ def time_resident(ctx, case, warmup, steps, flush_bytes):
         uv_it.append(st.uv.iter)
         refine.append(st.ch.refinements + st.uv.refinements)
         ch_ref.append(st.ch.refinements)
+        uv_solve.append(st.uv.seconds)
+        uv_ref.append(st.uv.refinements)
         resid.append(max(st.ch.true_resid, st.uv.true_resid))
         ok += int(st.ch.info == 0 and st.ch.true_resid <= case.params.tol * 1.0001) + \
             int(st.uv.info == 0 and st.uv.true_resid <= case.params.tol * 1.0001)
@@ -450,7 +474,8 @@ def time_resident(ctx, case, warmup, steps, flush_bytes):
     del abi
     return {"seconds": sum(per), "per_step_ms": [1e3 * x for x in per], "ch_iters": ch_it, "uv_iters": uv_it,
             "refinements": refine, "max_true_resid": max(resid), "solves_ok": ok, "solves": 2 * steps,
-            "launches": launches, "t_end": t, "ch_solve_s": ch_solve, "ch_refinements": ch_ref}
+            "launches": launches, "t_end": t, "ch_solve_s": ch_solve, "ch_refinements": ch_ref,
+            "uv_solve_s": uv_solve, "uv_refinements": uv_ref}
 
 
 def time_e2e(ctx, case, warmup, steps, flush_bytes):
@@ -532,9 +557,31 @@ def run_gpu(args, ws, rank, local):
     # from x^n as the reference does
     case = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED, guess_mode=3)
 
-    # mixed (headline) path, resident state
+    # the learned blend of the CH preconditioner: a U-Net trained, before any timed region, on
+    # the probe fits of other seeded geometries (seeds 1000.., never a rank's own), then asked
+    # for this geometry's weights in one forward pass
+    blend_net, blend = None, None
+    if args.blend_steps > 0:
+        from drd_application_gb300.learned import learned_blend, train_blend
+
+        train_cases = [make_case("c2", seed=1000 + g, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED,
+                                 guess_mode=3) for g in range(args.blend_geometries)]
+        blend_net, blend = train_blend(train_cases, steps=args.blend_steps, nprobe=64)
+        del train_cases
+
+    def install_blend(c, k):
+        if blend_net is None:
+            return None
+        t0 = time.perf_counter()
+        w = learned_blend(blend_net, k.coefs["M0"], k.coefs["Mi"])
+        c.set_ch_blend(w)
+        return time.perf_counter() - t0
+
+    # learned + mixed (headline) path, resident state
     ctx = DRDContext(case.params)
     ctx.set_case(case)
+    if blend is not None:
+        blend["inference_and_install_s"] = install_blend(ctx, case)
     persist = ctx.persistent_solver()
     clocks = ClockSampler(int(local) if ws == 1 else 0)
     barrier(dist)
@@ -566,6 +613,7 @@ def run_gpu(args, ws, rank, local):
                       particles=True)
     ctxp = DRDContext(casep.params)
     ctxp.set_case(casep)
+    install_blend(ctxp, casep)
     parts = casep.meta["particles"]
     ctxp.particles_set(parts["pp"], parts["points"], parts["bdr_dist"])
     pt = time_resident(ctxp, casep, W, K, flush)
@@ -600,8 +648,12 @@ def run_gpu(args, ws, rank, local):
         f64 = time_resident(ctx64, case64, W, K64, flush)
         f64_sec = max_over_ranks(dist, f64["seconds"])
         ctx64.close()
-        for name, prec, persist_env, nsteps in (("fp64_cubic", abi.DRD_PREC_FP64, None, K64),
-                                                ("mixed_cubic_graph_loop", abi.DRD_PREC_MIXED, "0", K)):
+        legs = [("fp64_cubic", abi.DRD_PREC_FP64, None, K64, None),
+                ("mixed_cubic_graph_loop", abi.DRD_PREC_MIXED, "0", K, None)]
+        if blend_net is not None:
+            legs += [("mixed_cubic_persistent_psolve_cg", abi.DRD_PREC_MIXED, None, K, None),
+                     ("mixed_cubic_persistent_probe_blend", abi.DRD_PREC_MIXED, None, K, "probe")]
+        for name, prec, persist_env, nsteps, pc in legs:
             casea = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=prec, guess_mode=3)
             if persist_env is not None:
                 os.environ["DRD_PERSIST"] = persist_env
@@ -610,6 +662,8 @@ def run_gpu(args, ws, rank, local):
             finally:
                 os.environ.pop("DRD_PERSIST", None)
             ctxa.set_case(casea)
+            if pc == "probe":  # this geometry's own probe fit (64 probes) in place of the network's
+                ctxa.ch_blend_probe(64, 7, install=True)
             ra = time_resident(ctxa, casea, W, nsteps, flush)
             ctxa.close()
             sa = max_over_ranks(dist, ra["seconds"])
@@ -617,6 +671,8 @@ def run_gpu(args, ws, rank, local):
                           "ch_iters_mean": statistics.mean(ra["ch_iters"]),
                           "uv_iters_mean": statistics.mean(ra["uv_iters"]),
                           "solves_to_fp64_1e-8": f"{ra['solves_ok']}/{ra['solves']}"}
+    if blend_net is not None:
+        blend_net.close()
 
     if rank != 0:
         return 0
@@ -626,20 +682,46 @@ def run_gpu(args, ws, rank, local):
     except Exception:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    # dominant kernel: the persistent mixed CH solve (one cooperative launch per step), timed by
-    # the CUDA events the step records around it.  Algorithmic bytes of one launch: 29 N_c
-    # FP32 words per BiCGSTAB iteration (the minimum of a fully fused iteration: 23 vector
-    # passes, two mobility reads, one Ph_Lcc read) plus, per refinement sweep, the FP64
-    # residual (x, b, r and the two mobility fields) and the FP32 scale / FP64 update passes.
+    # the roofline line reports the persistent solve kernel with the larger share of the step
+    # (each is one cooperative launch per step, timed by the CUDA events the step records around
+    # it; the other is reported beside it).  Algorithmic bytes of one launch:
+    # CH: 29 N_c FP32 words per BiCGSTAB iteration (the minimum of a fully fused iteration: 23
+    #   vector passes, two mobility reads, one Ph_Lcc read), plus 4 N_c with the blend (the
+    #   weights and the preconditioner's input, read once per preconditioner application), and per
+    #   refinement sweep the FP64 residual (x, b, r and the two mobility fields) and the FP32 scale
+    #   / FP64 update passes.
+    # momentum: 24 n + 6 N_c FP32 words per iteration (n = nuv unknowns: the p update 4 n, the two
+    #   Jacobi applications 3 n each, the two operators 2 n each plus rho, eta and the penalty at
+    #   N_c each, s 3 n, the x update 4 n, r 3 n), and per sweep the FP64 residual (x, b, r and the
+    #   three coefficient fields) and the scale / update passes.
     nc = args.nr * args.nz
     cs = (args.nr + 2) * (args.nz + 2)
-    it_total = sum(mx["ch_iters"])
-    sweeps_total = sum(mx["ch_refinements"])
-    ch_sec = sum(mx["ch_solve_s"])
-    by_total = 29.0 * nc * 4 * it_total + sweeps_total * (8.0 * (4 * nc + 2 * cs) + 4.0 * 4 * nc + 20.0 * nc)
-    achieved = by_total / ch_sec / 1e9 if ch_sec > 0 else 0.0
-    us = 1e6 * ch_sec / max(1, len(mx["ch_solve_s"]))
-    by = by_total / max(1, len(mx["ch_solve_s"]))
+    nuv = (args.nr + 1) * args.nz + args.nr * (args.nz - 1)
+    ch_words = 29.0 + (4.0 if blend_net is not None else 0.0)
+    kernels = {
+        "ch": {"name": "k_bicg_persist<CH> (whole mixed CH solve)", "traffic": TRAFFIC_CH,
+               "iters": sum(mx["ch_iters"]), "sec": sum(mx["ch_solve_s"]), "launches": len(mx["ch_solve_s"]),
+               "bytes": ch_words * nc * 4 * sum(mx["ch_iters"]) +
+               sum(mx["ch_refinements"]) * (8.0 * (4 * nc + 2 * cs) + 4.0 * 4 * nc + 20.0 * nc)},
+        "uv": {"name": "k_bicg_persist<UV> (whole mixed momentum solve)", "traffic": TRAFFIC_UV,
+               "iters": sum(mx["uv_iters"]), "sec": sum(mx["uv_solve_s"]), "launches": len(mx["uv_solve_s"]),
+               "bytes": (24.0 * nuv + 6.0 * nc) * 4 * sum(mx["uv_iters"]) +
+               sum(mx["uv_refinements"]) * (8.0 * (3 * nuv + 3 * cs) + 4.0 * 3 * nuv + 20.0 * nuv)},
+    }
+    for kd in kernels.values():
+        n_l = max(1, kd["launches"])
+        kd["achieved"] = kd["bytes"] / kd["sec"] / 1e9 if kd["sec"] > 0 else 0.0
+        kd["us"] = 1e6 * kd["sec"] / n_l
+        kd["by"] = kd["bytes"] / n_l
+        kd["ipl"] = kd["iters"] / n_l
+    dom = "ch" if kernels["ch"]["sec"] >= kernels["uv"]["sec"] else "uv"
+    other = "uv" if dom == "ch" else "ch"
+
+    def roof(kd):
+        return {"bound": "hbm", "kernel": kd["name"], "achieved": kd["achieved"], "peak": hbm_peak, "unit": "GB/s",
+                "frac": kd["achieved"] / hbm_peak, "traffic": kd["traffic"], "bytes_per_launch": kd["by"],
+                "us_per_launch": kd["us"], "iterations_per_launch": kd["ipl"],
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst)" if peaks else "fallback 6800 GB/s"}
     fl = None
     steps_total = K * ws
     value = steps_total / sec
@@ -658,9 +740,14 @@ def run_gpu(args, ws, rank, local):
         "data": "synthetic (seeded geometry, fibers and drops per rank)",
         "config": {
             "workload": WORKLOAD, "nr": args.nr, "nz": args.nz,
-            "path": "mixed + cubic guess: FP32 BiCGSTAB in FP64 refinement, initial guesses by cubic "
-                    "extrapolation; the learned guess is measured beside it (learned_guess) and does not "
-                    "drive the timed step",
+            "path": ("learned + mixed: FP32 BiCGSTAB in FP64 refinement; the CH preconditioner PSolve_CG "
+                     "blended per cell, y = q + w (x - q), with weights w predicted by the U-Net from the "
+                     "mobility fields (learned_blend); initial guesses by cubic extrapolation. The learned "
+                     "initial guess is measured beside it (learned_guess) and does not drive the timed step")
+            if blend_net is not None else
+            "mixed + cubic guess: FP32 BiCGSTAB in FP64 refinement, PSolve_CG, initial guesses by cubic "
+            "extrapolation",
+            "learned_blend": blend,
             "initial_guess": "mixed and e2e legs: cubic extrapolation 4x^n - 6x^(n-1) + 4x^(n-2) - x^(n-3) (guess_mode 3); fp64 leg: x^n",
             "inner_ch_solver": "persistent cooperative kernel" if persist[0] else
             f"kernel-per-phase graph loop ({persist[1] or 'persistent solver off'})",
@@ -682,7 +769,10 @@ def run_gpu(args, ws, rank, local):
                 "arithmetic (fp64 cubic -> mixed cubic, both graph loops)":
                     arms["mixed_cubic_graph_loop"]["steps_per_s"] / arms["fp64_cubic"]["steps_per_s"],
                 "launch structure (graph loop -> persistent solves)":
-                    value / arms["mixed_cubic_graph_loop"]["steps_per_s"]},
+                    (arms["mixed_cubic_persistent_psolve_cg"]["steps_per_s"] if blend_net is not None else value) /
+                    arms["mixed_cubic_graph_loop"]["steps_per_s"],
+                **({"learned blend (PSolve_CG -> learned blend, persistent)":
+                    value / arms["mixed_cubic_persistent_psolve_cg"]["steps_per_s"]} if blend_net is not None else {})},
             "kernels_us": {abi.KB_NAMES[k]: round(v[0], 3) for k, v in kb.items()},
             "with_particles": {"steps_per_s": K * ws / pt_sec, "ms_per_step": 1e3 * pt_sec / K, "beads": 9,
                                "solves_to_fp64_1e-8": f"{pt['solves_ok']}/{pt['solves']}"},
@@ -690,11 +780,8 @@ def run_gpu(args, ws, rank, local):
             "c5": c5,
             "learned_guess": learned,
         },
-        "roofline": {"bound": "hbm", "kernel": "k_bicg_persist<CH> (whole mixed CH solve)", "achieved": achieved,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": TRAFFIC_CH,
-                     "bytes_per_launch": by, "us_per_launch": us,
-                     "iterations_per_launch": it_total / max(1, len(mx["ch_solve_s"])),
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst)" if peaks else "fallback 6800 GB/s"},
+        "roofline": roof(kernels[dom]),
+        "roofline_other_solve": roof(kernels[other]),
         "e2e": {"value": e2e_steps * ws / e2e_sec, "unit": "time-steps/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"]},
         "clocks": clk,
