@@ -2068,6 +2068,10 @@ __device__ __forceinline__ unsigned long long gtimer() {
 __device__ __forceinline__ void pb_mark(const PbProf& pf, int i) {
     if (pf.p != nullptr && pf.k <= 1 && blockIdx.x == 0 && threadIdx.x == 0) pf.p[124 + i] = gtimer();
 }
+// Sub-phase mark of the first tridiagonal phase (ESOLP_x) of a timed iteration, p[106 + i].
+__device__ __forceinline__ void pb_markt(const PbProf& pf, int i) {
+    if (pf.p != nullptr && pf.k == 1 && blockIdx.x == 0 && threadIdx.x == 0) pf.p[106 + i] = gtimer();
+}
 // Sub-phase mark of the first z pass of a timed iteration, p[100 + i].
 __device__ __forceinline__ void pb_markz(const PbProf* pf, int i) {
     if (pf != nullptr && pf->p != nullptr && pf->k == 1 && blockIdx.x == 0 && threadIdx.x == 0)
@@ -2267,26 +2271,54 @@ __device__ __forceinline__ int pb_swz(int k, int m) {
 static_assert((PB_BM / 4) * (PB_BN / 4) * PB_KG == PB_NT, "4 x 4 register tiles, PB_KG groups");
 // bx, bw (optional): blend the result with bx as out = v + bw (bx - v) (the solid-blended CH
 // preconditioner's last step; bx is the preconditioner's input, written inside this launch).
-__device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float* smem, const PbProf& pf,
-                         const float* bx = nullptr, const float* bw = nullptr) {
-    const int M = a.nz, L = a.nr - 1, K = a.Kx;
-    int mt, nt0;
-    const int ntiles = pb_xtiles(a, mt, nt0);
-    float* At = smem + a.work_off;                        // [PB_KC][PB_BM], float4 groups swizzled by k
-    float* Bw = At + PB_KC * PB_BM;                       // [PB_KC][PB_BN] when B is not resident
-    float* red = Bw + (a.b_res ? 0 : PB_KC * PB_BN);      // [PB_KG][PB_BM * PB_BN]
-    constexpr int TN = PB_BN / 4;                         // threads of a K group along n
-    const int tid = threadIdx.x, g = tid >> 6, t = tid & 63, mi = t / TN, ni = t % TN;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int mtile = tile % mt, nrest = tile / mt;
-        const int par = nrest >= nt0 ? 1 : 0;
-        const int ntile = par ? nrest - nt0 : nrest;
-        const int N = par ? a.Nxo : a.Nxe;
-        const float* B = par ? a.fxo : a.fxe;
-        const int m0 = mtile * PB_BM, n0 = ntile * PB_BN;
-        float acc[4][4];
+// One x-pass problem: the folded DCT-I of length L+1 along each of M rows (row stride ld) of X,
+// out[m][2n+p] = sum_k (X[m][k] +- X[m][L-k]) Bp[k][n], with both Bp stored K x Ne; mt x (nt0 +
+// nt1) tiles of PB_BM x PB_BN.
+struct XProb {
+    const float* X;
+    float* out;
+    int M, ld, L, K, Ne, No;
+    const float *Be, *Bo;
+    int mt, nt0, ntiles;
+};
+template <int BN = PB_BN>
+__device__ __forceinline__ XProb xprob(const float* X, float* out, int M, int ld, int L, int K, int Ne, int No,
+                                       const float* Be, const float* Bo) {
+    XProb d{X, out, M, ld, L, K, Ne, No, Be, Bo, 0, 0, 0};
+    d.mt = (M + PB_BM - 1) / PB_BM;
+    d.nt0 = (Ne + BN - 1) / BN;
+    d.ntiles = d.mt * (d.nt0 + (No + BN - 1) / BN);
+    return d;
+}
+
+// One PB_BM x BN tile of problem d, K split KG ways.  Bres: the block's resident B panel of this
+// tile ([K][BN]), or null (B chunks are then streamed from L2).  bx, bw (optional): blend the
+// result with bx as out = v + bw (bx - v) (the solid-blended CH preconditioner's last step; bx is
+// the preconditioner's input, written inside this launch).
+template <int BN = PB_BN, int KG = PB_KG, int TM = 4>
+__device__ __forceinline__ void pb_xtile(const XProb& d, int tile, const float* Bres, float* work, const PbProf& pf,
+                                         const float* bx, const float* bw) {
+    static_assert((PB_BM / TM) * (BN / 4) * KG == PB_NT, "TM x 4 register tiles, KG groups");
+    static_assert(TM == 4 || TM == 8, "4 or 8 rows per thread");
+    const int M = d.M, L = d.L, K = d.K;
+    const float* X = d.X;
+    float* out = d.out;
+    float* At = work;                                     // [PB_KC][PB_BM], float4 groups swizzled by k
+    float* Bw = At + PB_KC * PB_BM;                       // [PB_KC][BN] when B is not resident
+    float* red = Bw + (Bres ? 0 : PB_KC * BN);         // [KG][PB_BM * BN]
+    constexpr int TN = BN / 4;                         // threads of a K group along n
+    constexpr int GT = (PB_BM / TM) * TN;                 // threads of a K group
+    const int tid = threadIdx.x, g = tid / GT, t = tid % GT, mi = t / TN, ni = t % TN;
+    {
+        const int mtile = tile % d.mt, nrest = tile / d.mt;
+        const int par = nrest >= d.nt0 ? 1 : 0;
+        const int ntile = par ? nrest - d.nt0 : nrest;
+        const int N = par ? d.No : d.Ne;
+        const float* B = par ? d.Bo : d.Be;
+        const int m0 = mtile * PB_BM, n0 = ntile * BN;
+        float acc[TM][4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < TM; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
         for (int k0 = 0; k0 < K; k0 += PB_KC) {
@@ -2304,7 +2336,7 @@ __device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float
                 x0[j] = 0.f;
                 x1[j] = 0.f;
                 if (rr < PB_BM && m < M) {
-                    const float* row = X + (long)m * a.nr;
+                    const float* row = X + (long)m * d.ld;
                     x0[j] = __ldcg(row + k);
                     if (2 * k != L) x1[j] = __ldcg(row + L - k);
                 }
@@ -2331,23 +2363,30 @@ __device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float
             }
             pb_mark(pf, 0);
             const float* Bk;
-            if (a.b_res) {
-                Bk = smem + a.b_off + (long)k0 * PB_BN;
+            if (Bres) {
+                Bk = Bres + (long)k0 * BN;
             } else {
-                for (int e = tid; e < kc * PB_BN; e += PB_NT) {
-                    const int kk = e / PB_BN, cc = e % PB_BN, n = n0 + cc;
-                    Bw[e] = n < N ? __ldg(B + (long)(k0 + kk) * a.Nxe + n) : 0.f;
+                for (int e = tid; e < kc * BN; e += PB_NT) {
+                    const int kk = e / BN, cc = e % BN, n = n0 + cc;
+                    Bw[e] = n < N ? __ldg(B + (long)(k0 + kk) * d.Ne + n) : 0.f;
                 }
                 Bk = Bw;
             }
             __syncthreads();
-            const int kgn = (kc + PB_KG - 1) / PB_KG, kb = g * kgn, ke = min(kb + kgn, kc);
+            const int kgn = (kc + KG - 1) / KG, kb = g * kgn, ke = min(kb + kgn, kc);
+#pragma unroll 2
             for (int kk = kb; kk < ke; ++kk) {
-                const float4 av = *reinterpret_cast<const float4*>(At + kk * PB_BM + ((mi ^ (kk & (PB_AG - 1))) << 2));
-                const float4 bv = *reinterpret_cast<const float4*>(Bk + kk * PB_BN + (ni << 2));
-                const float ar[4] = {av.x, av.y, av.z, av.w}, br[4] = {bv.x, bv.y, bv.z, bv.w};
+                float ar[TM];
 #pragma unroll
-                for (int i = 0; i < 4; ++i)
+                for (int h = 0; h < TM / 4; ++h) {  // the thread's float4 row groups (TM / 4 of them)
+                    const int grp = mi * (TM / 4) + h;
+                    const float4 av = *reinterpret_cast<const float4*>(At + kk * PB_BM + ((grp ^ (kk & (PB_AG - 1))) << 2));
+                    ar[4 * h] = av.x; ar[4 * h + 1] = av.y; ar[4 * h + 2] = av.z; ar[4 * h + 3] = av.w;
+                }
+                const float4 bv = *reinterpret_cast<const float4*>(Bk + kk * BN + (ni << 2));
+                const float br[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+                for (int i = 0; i < TM; ++i)
 #pragma unroll
                     for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(ar[i], br[j], acc[i][j]);
             }
@@ -2356,23 +2395,205 @@ __device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float
         }
         // the eight K-group partial tiles, summed in group order
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-            *reinterpret_cast<float4*>(red + g * (PB_BM * PB_BN) + (4 * mi + i) * PB_BN + 4 * ni) =
+        for (int i = 0; i < TM; ++i)
+            *reinterpret_cast<float4*>(red + g * (PB_BM * BN) + (TM * mi + i) * BN + 4 * ni) =
                 make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
         __syncthreads();
-        for (int o = tid; o < PB_BM * PB_BN; o += PB_NT) {
+        for (int o = tid; o < PB_BM * BN; o += PB_NT) {
             float v = 0.f;
 #pragma unroll
-            for (int gg = 0; gg < PB_KG; ++gg) v += red[gg * (PB_BM * PB_BN) + o];
-            const int m = m0 + o / PB_BN, n = n0 + o % PB_BN;
+            for (int gg = 0; gg < KG; ++gg) v += red[gg * (PB_BM * BN) + o];
+            const int m = m0 + o / BN, n = n0 + o % BN;
             if (m < M && n < N) {
-                const long q = (long)m * a.nr + 2 * n + par;
+                const long q = (long)m * d.ld + 2 * n + par;
                 out[q] = bw ? v + __ldg(bw + q) * (__ldcg(bx + q) - v) : v;
             }
         }
         pb_mark(pf, 2);
         __syncthreads();
     }
+}
+
+
+// x pass of the CH preconditioner over the packed nz x nr cells, one tile per block when the
+// B panels are resident.
+__device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float* smem, const PbProf& pf,
+                         const float* bx = nullptr, const float* bw = nullptr) {
+    const XProb d = xprob(X, out, a.nz, a.nr, a.nr - 1, a.Kx, a.Nxe, a.Nxo, a.fxe, a.fxo);
+    const float* Bres = a.b_res ? smem + a.b_off : nullptr;
+    for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x)
+        pb_xtile(d, tile, Bres, smem + a.work_off, pf, bx, bw);
+}
+
+// ---- ESOLP_x (Precipitation_dynamics/ESOLP.f90:1-54, VeloSolve_combined.f90:800-806) in the
+// persistent momentum solver: per block of the packed vector (u: nz rows of nr+1, v: nz-1 rows of
+// nr) VCOST along x, a tridiagonal solve along y per x mode, VCOST along x; three phases.
+
+// Both blocks' row transforms as one tile space of PB_BM x PB_UBN tiles (8 x 4 register tiles, K
+// split PB_UKG ways: the row operand is a warp broadcast, so each FMA costs half the shared-memory
+// traffic of the 4 x 4 form),
+// at most one tile per block at 420x180 and below; the block's own B panel stays in shared memory
+// for the whole solve when the plan allows (a.b_res).
+constexpr int PB_UBN = 128, PB_UKG = 8, PB_UTM = 8;
+__device__ __forceinline__ void pb_uv_probs(const PersistArgs& a, const float* X, float* out, XProb& du, XProb& dv) {
+    const long mu = (long)(a.nr + 1) * a.nz;
+    du = xprob<PB_UBN>(X, out, a.nz, a.nr + 1, a.nr, a.Ku, a.Nue, a.Nuo, a.fue, a.fuo);
+    dv = xprob<PB_UBN>(X + mu, out + mu, a.nz - 1, a.nr, a.nr - 1, a.Kx, a.Nxe, a.Nxo, a.fxe, a.fxo);
+}
+__device__ void pb_xpass_uv(const PersistArgs& a, const float* X, float* out, float* smem, const PbProf& pf) {
+    XProb du, dv;
+    pb_uv_probs(a, X, out, du, dv);
+    const int tot = du.ntiles + dv.ntiles;
+    const float* Bres = a.b_res ? smem + a.b_off : nullptr;
+    for (int tile = blockIdx.x; tile < tot; tile += gridDim.x) {
+        if (tile < du.ntiles) pb_xtile<PB_UBN, PB_UKG, PB_UTM>(du, tile, Bres, smem, pf, nullptr, nullptr);
+        else pb_xtile<PB_UBN, PB_UKG, PB_UTM>(dv, tile - du.ntiles, Bres, smem, pf, nullptr, nullptr);
+    }
+}
+// The block's resident B panel ([K][PB_UBN]) of its tile, loaded once per launch.
+__device__ void pb_load_resident_uv(const PersistArgs& a, float* smem) {
+    XProb du, dv;
+    pb_uv_probs(a, nullptr, nullptr, du, dv);
+    const int tile = blockIdx.x;
+    if (tile < du.ntiles + dv.ntiles) {
+        const bool ub = tile < du.ntiles;
+        const XProb& d = ub ? du : dv;
+        const int tl = ub ? tile : tile - du.ntiles;
+        const int nrest = tl / d.mt, par = nrest >= d.nt0 ? 1 : 0, ntile = par ? nrest - d.nt0 : nrest;
+        const int N = par ? d.No : d.Ne, n0 = ntile * PB_UBN;
+        const float* B = par ? d.Bo : d.Be;
+        float* Bs = smem + a.b_off;
+        for (int e = threadIdx.x; e < d.K * PB_UBN; e += PB_NT) {
+            const int kk = e / PB_UBN, cc = e % PB_UBN, n = n0 + cc;
+            Bs[e] = n < N ? __ldg(B + (long)kk * d.Ne + n) : 0.f;
+        }
+    }
+    __syncthreads();
+}
+
+constexpr int PB_TRI_MB = 8;  // modes per batch of the tridiagonal phase (one warp each)
+
+// The tridiagonal phase, in place on w: per x mode the forward elimination f_j = w_j + r_j f_{j-1}
+// and the back substitution ff_j = (f_j - c_j ff_{j+1}) / b'_j (ff = 0 at the last row when
+// |b'| <= 1e-12) with the factors of setup (rfords), held as r_j, 1/b'_j and c_j/b'_j.  A batch of PB_TRI_MB modes is staged in
+// shared memory; each mode's warp splits its rows into 32 segments, composes each segment's
+// affine map, scans the maps across the lanes, and then runs its segment from the scanned
+// boundary value with the same recurrence.
+__device__ void pb_tridiag_uv(const PersistArgs& a, float* w, float* smem, const PbProf& pf) {
+    const int nr = a.nr, nz = a.nz;
+    const long mu = (long)(nr + 1) * nz, mv = (long)nr * (nz - 1);
+    const int nmu = nr + 1, total = 2 * nr + 1;
+    // staged [PB_TRI_MB][nz]: a mode's rows are contiguous, so the lanes of its warp, which run
+    // contiguous row segments, fall on distinct banks (2-way at most)
+    float* sw = smem;                      // right-hand sides, then the solution
+    float* sr = sw + nz * PB_TRI_MB;       // elimination factors r_j
+    float* sb = sr + nz * PB_TRI_MB;       // 1 / b'_j
+    float* sc = sb + nz * PB_TRI_MB;       // c_j / b'_j
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    for (int g0 = blockIdx.x * PB_TRI_MB; g0 < total; g0 += gridDim.x * PB_TRI_MB) {
+        __syncthreads();
+        // staging: the loads of up to SU elements per thread are issued before any is stored
+        constexpr int SU = 4;
+        for (int e0 = 0; e0 < nz * PB_TRI_MB; e0 += SU * PB_NT) {
+            float v[SU][4];
+            int at[SU];
+#pragma unroll
+            for (int u = 0; u < SU; ++u) {
+                const int e = e0 + u * PB_NT + threadIdx.x;
+                at[u] = -1;
+                if (e >= nz * PB_TRI_MB) continue;
+                const int sl = e % PB_TRI_MB, j = e / PB_TRI_MB, g = g0 + sl;
+                if (g >= total) continue;
+                const bool ub = g < nmu;
+                const int k = ub ? g : g - nmu, len = ub ? nr + 1 : nr, rows = ub ? nz : nz - 1;
+                if (j >= rows) continue;
+                const float* f = ub ? a.esf : a.esf + 3 * mu;
+                const long rb = ub ? mu : mv;
+                const long q = k + (long)len * j;
+                v[u][0] = __ldcg(w + (ub ? 0 : mu) + q);
+                v[u][1] = __ldg(f + q);
+                v[u][2] = __ldg(f + rb + q);
+                v[u][3] = __ldg(f + 2 * rb + q);
+                at[u] = sl * nz + j;
+            }
+#pragma unroll
+            for (int u = 0; u < SU; ++u)
+                if (at[u] >= 0) {
+                    sw[at[u]] = v[u][0];
+                    sr[at[u]] = v[u][1];
+                    sb[at[u]] = v[u][2];
+                    sc[at[u]] = v[u][3];
+                }
+        }
+        __syncthreads();
+        pb_markt(pf, 0);
+        if (wp < PB_TRI_MB && g0 + wp < total) {
+            const int sl = wp, g = g0 + sl;
+            const int R = g < nmu ? nz : nz - 1;
+            const int cl = (R + 31) / 32, j0 = lane * cl, j1 = min(j0 + cl, R);
+            // forward: f_j = r_j f_{j-1} + w_j as maps (A, B) of f_{j-1}
+            float A = 1.f, B = 0.f;
+            for (int j = j0; j < j1; ++j) {
+                const float r = sr[sl * nz + j];
+                A = r * A;
+                B = fmaf(r, B, sw[sl * nz + j]);
+            }
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {  // inclusive scan: lane l = segments 0..l
+                const float Ap = __shfl_up_sync(0xffffffffu, A, o), Bp = __shfl_up_sync(0xffffffffu, B, o);
+                if (lane >= o) { B = fmaf(A, Bp, B); A = A * Ap; }
+            }
+            float f = __shfl_up_sync(0xffffffffu, B, 1);  // f at the row before the segment (f_{-1} = 0)
+            if (lane == 0) f = 0.f;
+            for (int j = j0; j < j1; ++j) {
+                const float wv = sw[sl * nz + j];
+                f = (j == 0) ? wv : wv + sr[sl * nz + j] * f;
+                sw[sl * nz + j] = f;
+            }
+            __syncwarp();
+            // back substitution as maps of ff_{j+1}: ff_j = (-c_j / b'_j) ff_{j+1} + f_j / b'_j (the last
+            // row's c / b' is 0, and so is its 1 / b' where rfords sets ff = 0)
+            A = 1.f;
+            B = 0.f;
+            for (int j = j1 - 1; j >= j0; --j) {
+                const float Aj = -sc[sl * nz + j], Bj = sw[sl * nz + j] * sb[sl * nz + j];
+                B = fmaf(Aj, B, Bj);
+                A = Aj * A;
+            }
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {  // inclusive suffix scan: lane l = segments l..31
+                const float Ap = __shfl_down_sync(0xffffffffu, A, o), Bp = __shfl_down_sync(0xffffffffu, B, o);
+                if (lane + o < 32) { B = fmaf(A, Bp, B); A = A * Ap; }
+            }
+            float nxt = __shfl_down_sync(0xffffffffu, B, 1);  // ff at the row after the segment
+            if (lane == 31) nxt = 0.f;
+            for (int j = j1 - 1; j >= j0; --j) {
+                nxt = fmaf(-sc[sl * nz + j], nxt, sw[sl * nz + j] * sb[sl * nz + j]);
+                sw[sl * nz + j] = nxt;
+            }
+        }
+        __syncthreads();
+        pb_markt(pf, 1);
+        for (int e = threadIdx.x; e < nz * PB_TRI_MB; e += PB_NT) {
+            const int sl = e % PB_TRI_MB, j = e / PB_TRI_MB, g = g0 + sl;
+            if (g >= total) continue;
+            const bool ub = g < nmu;
+            const int k = ub ? g : g - nmu, len = ub ? nr + 1 : nr, rows = ub ? nz : nz - 1;
+            if (j >= rows) continue;
+            w[(ub ? 0 : mu) + k + (long)len * j] = sw[sl * nz + j];
+        }
+    }
+}
+
+// psolve of the momentum system with ESOLP_x: y = C_x T^-1 C_x x per block (three phases, two
+// internal barriers); a.ff1 holds the intermediate.
+__device__ bool pb_psolve_uv(const PersistArgs& a, const float* x, float* y, float* smem, unsigned& gen, PbProf& pf) {
+    pb_xpass_uv(a, x, a.ff1, smem, pf);
+    if (!grid_sync(a.bar, gen, pf)) return false;
+    pb_tridiag_uv(a, a.ff1, smem, pf);
+    if (!grid_sync(a.bar, gen, pf)) return false;
+    pb_xpass_uv(a, a.ff1, y, smem, pf);
+    return true;
 }
 
 // One folded DCT-I along z of PB_CW columns held in xs[nz][PB_CW] -> ys[nz][PB_CW].  The folded
@@ -2645,6 +2866,15 @@ __device__ __forceinline__ float pb_pre(const PersistArgs& a, long q, float v) {
     return a.ident ? v : v / __ldg(a.diag + q);
 }
 
+// The preconditioner as a phase sequence: the CH DCT-I solve, or ESOLP_x for the momentum system
+// (the momentum system's Jacobi is element-wise and fused into the vector passes instead).
+template <int KIND>
+__device__ __forceinline__ bool pb_psolve_k(const PersistArgs& a, const float* x, float* y, float* smem, unsigned& gen,
+                                            PbProf& pf) {
+    if constexpr (KIND == PK_CH) return pb_psolve(a, x, y, smem, gen, pf);
+    return pb_psolve_uv(a, x, y, smem, gen, pf);
+}
+
 // State of one inner BiCGSTAB run (the local scalars of BICGSTABREVCOM).
 struct PbInner {  // FP32 like the inner iterations themselves
     int info, iter;
@@ -2679,8 +2909,8 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
         pf.p = (a.prof != nullptr && st.iter == 3 && pf.k == 0) ? a.prof : nullptr;  // time iteration 3 once
         if (pf.p != nullptr && blockIdx.x == 0 && threadIdx.x == 0) pf.p[123] = gtimer();
         if (fabsf(st.rho) < kbt) { st.info = -10; break; }  // (:261-263)
-        if constexpr (KIND == PK_CH) {
-            if (!(ok = pb_psolve(a, a.p, a.phat, smem, gen, pf))) break;     // PHAT = M^-1 P
+        if (KIND == PK_CH || a.esolp) {
+            if (!(ok = pb_psolve_k<KIND>(a, a.p, a.phat, smem, gen, pf))) break;     // PHAT = M^-1 P
             if (!(ok = grid_sync(a.bar, gen, pf))) break;
         }
         if (!(ok = pb_matvec<KIND>(a, a.phat, a.v, 1.f, nullptr, a.rtld, 4, false, 0, sm, gen, pf))) break;  // V = A PHAT
@@ -2706,7 +2936,7 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
                 a.r[q] = sv;
                 s2 = fmaf(sv, sv, s2);
                 rs = fmaf(t, sv, rs);
-                if constexpr (KIND == PK_UV) a.shat[q] = pb_pre(a, q, sv);  // SHAT = M^-1 S, fused
+                if (KIND == PK_UV && !a.esolp) a.shat[q] = pb_pre(a, q, sv);  // SHAT = M^-1 S, fused
             };
             if (ha) s_elem(qa, ra, va, ta);
             if (hb) s_elem(qb, rb, vb, tb);
@@ -2728,8 +2958,8 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
             for (long q = q0; q < n; q += stride) a.x[q] = __ldcg(a.x + q) + al * __ldcg(a.phat + q);
             break;
         }
-        if constexpr (KIND == PK_CH) {
-            if (!(ok = pb_psolve(a, a.r, a.shat, smem, gen, pf))) break;     // SHAT = M^-1 S
+        if (KIND == PK_CH || a.esolp) {
+            if (!(ok = pb_psolve_k<KIND>(a, a.r, a.shat, smem, gen, pf))) break;     // SHAT = M^-1 S
             if (!(ok = grid_sync(a.bar, gen, pf))) break;
         }
         // T = A SHAT with (t, s), (t, t) and (rtld, t)
@@ -2775,7 +3005,7 @@ __device__ bool pb_iterate(const PersistArgs& a, double bnrm2, double tol, int m
                 a.x[q] = xv;
                 a.r[q] = rv;
                 a.p[q] = pv;
-                if constexpr (KIND == PK_UV) a.phat[q] = pb_pre(a, q, pv);  // PHAT = M^-1 P of the next iteration
+                if (KIND == PK_UV && !a.esolp) a.phat[q] = pb_pre(a, q, pv);  // PHAT = M^-1 P of the next iteration
                 r2 = fmaf(rv, rv, r2);
             };
             if (ha) xrp(qa, ea);
@@ -2871,10 +3101,11 @@ __global__ void __launch_bounds__(PB_NT, 1) k_bicg_persist(PersistArgs a) {
         return;
     }
     if constexpr (KIND == PK_CH) pb_load_resident(a, smem);
+    else if (a.esolp && a.b_res) pb_load_resident_uv(a, smem);
     if (a.mode == PM_PSOLVE || a.mode == PM_MATVEC) {  // one application x = op(b), the solver's code
         bool done = true;
         if (a.mode == PM_PSOLVE) {
-            if constexpr (KIND == PK_CH) done = pb_psolve(a, a.b, a.x, smem, gen, pf);
+            if (KIND == PK_CH || a.esolp) done = pb_psolve_k<KIND>(a, a.b, a.x, smem, gen, pf);
             else
                 for (long q = q0; q < n; q += stride) a.x[q] = pb_pre(a, q, __ldcg(a.b + q));
         } else {
@@ -3134,12 +3365,38 @@ PbPlan persist_ch_plan(int nr, int nz, int grid, size_t budget) {
     p.bytes = used * sizeof(float);
     return p;
 }
+// Shared-memory plan of the persistent momentum solver with ESOLP_x (floats): a work area for
+// the x pass (A chunk, K-group partial tiles, and a B chunk when B is streamed) that the
+// tridiagonal phase's staged batch reuses, then the block's resident B panel when every tile
+// has its own block and the panel fits.
+PbPlan persist_esolp_plan(int nr, int nz, int grid, size_t budget) {
+    PbPlan p{};
+    auto up4 = [](size_t v) { return (v + 3) & ~(size_t)3; };
+    const int Ku = nr / 2 + 1, Kx = (nr - 1) / 2 + 1, Kmax = Ku > Kx ? Ku : Kx;
+    const int mtu = (nz + PB_BM - 1) / PB_BM, mtv = (nz - 1 + PB_BM - 1) / PB_BM;
+    const int Nue = (nr + 2) / 2, Nuo = (nr + 1) / 2, Nxe = (nr + 1) / 2, Nxo = nr / 2;
+    auto nt = [](int n) { return (n + PB_UBN - 1) / PB_UBN; };
+    const int ntiles = mtu * (nt(Nue) + nt(Nuo)) + mtv * (nt(Nxe) + nt(Nxo));
+    const size_t tri = (size_t)4 * nz * PB_TRI_MB;
+    const size_t xres = (size_t)PB_KC * PB_BM + (size_t)PB_UKG * PB_BM * PB_UBN;
+    const size_t xstr = xres + (size_t)PB_KC * PB_UBN;
+    const size_t wres = up4(xres > tri ? xres : tri);
+    p.work_off = 0;
+    if (ntiles <= grid && (wres + (size_t)Kmax * PB_UBN) * sizeof(float) <= budget) {
+        p.b_res = 1;
+        p.b_off = (long)wres;
+        p.bytes = (wres + (size_t)Kmax * PB_UBN) * sizeof(float);
+        return p;
+    }
+    p.bytes = (xstr > tri ? xstr : tri) * sizeof(float);
+    return p;
+}
 int persist_threads() { return PB_NT; }
 const void* persist_kernel(int kind) {
     return kind == PK_CH ? (const void*)k_bicg_persist<PK_CH> : (const void*)k_bicg_persist<PK_UV>;
 }
 cudaError_t launch_bicg_persist(const PersistArgs& a, int grid, cudaStream_t s) {
-    const size_t smem = a.kind == PK_CH ? a.smem_bytes : 0;
+    const size_t smem = a.smem_bytes;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(PB_NT);

@@ -175,6 +175,12 @@ struct PersistArgs {
     // momentum: rho, eta, penalty mask (CELL), Jacobi diagonal; ident = identity preconditioner
     const float *rho, *eta, *pen, *diag;
     int ident;
+    // momentum with ESOLP_x: the folded VCOST operands of length nr+1 (u block, Ku x Nue; the v
+    // block uses the CH x-pass operands of length nr), the Thomas factors of the bdf (u block
+    // rm, bp, cc, then the v block), the tridiagonal phase's modes per batch
+    int esolp;
+    const float *fue, *fuo, *esf;
+    int Ku, Nue, Nuo;
     float *x, *b, *r, *rtld, *p, *v, *phat, *shat, *t, *ff1, *w1, *w2;
     // PM_REFINE: the FP64 system (b64, x64 in place), its residual and stencil scratch, the
     // FP64 operators' scalars and coefficients, the refinement tolerance and sweep limit
@@ -203,6 +209,7 @@ struct PbPlan {
     size_t bytes;
 };
 PbPlan persist_ch_plan(int nr, int nz, int grid, size_t budget);
+PbPlan persist_esolp_plan(int nr, int nz, int grid, size_t budget);
 int persist_threads();
 const void* persist_kernel(int kind);
 cudaError_t launch_bicg_persist(const PersistArgs& a, int grid, cudaStream_t s);

@@ -69,6 +69,8 @@ struct drd_ctx {
     // and a momentum-length scratch vector
     double *f1ue, *f1uo, *es64[2], *esw;
     float *f1ue32, *f1uo32, *es32[2], *esw32;
+    // the persistent solver's form of the ESOLP_x factors: r_j, 1/b'_j and c_j/b'_j per mode and row
+    float* esq32[2];
     int Ku = 0, Nue = 0, Nuo = 0;
     double *cfB, *cfT;
     // PreSolve_2 by FFT (nr and nz of the form 2^a 3^b 5^c 7^d): plans and twiddle tables in
@@ -100,6 +102,8 @@ struct drd_ctx {
     // persistent cooperative inner solver (FP32 CH): grid size, barrier state, on/off
     int persist = 0, pgrid = 0;
     int persist_ch = 0;  // the CH solve too: only when its transform operands stay in shared memory
+    int persist_esolp = 0;      // the momentum solve with ESOLP_x too (its shared-memory work area fits)
+    PbPlan eplan{};
     // mixed mode: the CH system is too stiff for FP32 Krylov vectors and is solved in FP64
     int ch_fp64 = 0;
     double ch_stiff = 0.0;
@@ -181,7 +185,7 @@ size_t arena_need(long cs, long us, long vs, long nc, long nr, long nz, long nma
     add(4 * nr, 8); add(4 * nz, 8); add(4 * nr, 4); add(4 * nz, 4);  // FFT tables (complex, 2n each)
     const long fu = (nr / 2 + 1) * (nr / 2 + 2), nes = 3 * (us + vs);
     add(fu, 8); add(fu, 8); add(fu, 4); add(fu, 4);            // f1ue, f1uo (+ FP32)
-    for (int i = 0; i < 2; ++i) { add(nes, 8); add(nes, 4); }  // es64, es32
+    for (int i = 0; i < 2; ++i) { add(nes, 8); add(nes, 4); add(nes, 4); }  // es64, es32, esq32
     add(nmax, 8); add(nmax, 4);                                // esw, esw32
     return b + 4096;
 }
@@ -663,6 +667,7 @@ int setup_persist(drd_ctx* c) {
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
     const int grid = std::min(sms, DRD_MAXB);
     c->pplan = persist_ch_plan(c->nr, c->nz, grid, (size_t)std::max(0, optin - 4096));
+    c->eplan = persist_esolp_plan(c->nr, c->nz, grid, (size_t)std::max(0, optin - 4096));
     for (int kind = PK_CH; kind <= PK_UV; ++kind) {
         const size_t sm = kind == PK_CH ? c->pplan.bytes : 0;
         if (sm > (size_t)optin) { c->persist_err = "persistent solver needs more shared memory"; return DRD_OK; }
@@ -673,6 +678,17 @@ int setup_persist(drd_ctx* c) {
     }
     c->pgrid = grid;
     c->persist = 1;
+    // the momentum kernel's ESOLP_x work area (the Jacobi path launches it without one)
+    c->persist_esolp = 0;
+    if (c->eplan.bytes <= (size_t)optin &&
+        cudaFuncSetAttribute(persist_kernel(PK_UV), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->eplan.bytes) ==
+            cudaSuccess) {
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persist_kernel(PK_UV), persist_threads(),
+                                                          c->eplan.bytes) == cudaSuccess && occ >= 1)
+            c->persist_esolp = 1;
+    }
+    cudaGetLastError();
     // Past the resident plan (more x-pass tiles than blocks, streamed operands) the persistent CH
     // solve is slower than the kernel-per-phase loop's tuned GEMMs: 2048x1024 took about 10 ms
     // per FP32 iteration against 2 ms.
@@ -695,12 +711,21 @@ PersistArgs persist_args(drd_ctx* c, const Sys& S, KState* in, const KState* par
     a.Kx = c->Kx; a.Nxe = c->Nxe; a.Nxo = c->Nxo; a.Kz = c->Kz; a.Mze = c->Mze; a.Mzo = c->Mzo;
     KVecs<float>& f = c->k32;
     a.rho = c->rho32; a.eta = c->eta32; a.pen = c->pen32; a.diag = f.diag; a.ident = S.ident || !S.jacobi;
+    a.esolp = (S.kind == SYS_UV && S.esolp) ? 1 : 0;
+    a.fue = c->f1ue32; a.fuo = c->f1uo32; a.Ku = c->Ku; a.Nue = c->Nue; a.Nuo = c->Nuo;
+    a.esf = a.esolp ? c->esq32[S.bdf - 1] : nullptr;
     a.x = f.x; a.b = f.b; a.r = f.r; a.rtld = f.rtld; a.p = f.p; a.v = f.v; a.phat = f.phat; a.shat = f.shat;
     a.t = f.t; a.ff1 = f.ff1; a.w1 = c->t1f; a.w2 = c->t2f;
     a.part = c->part; a.ks = in; a.parent = parent; a.bar = c->bar; a.tol = tol; a.maxit = maxit; a.ctr = c->ctr;
     a.prof = c->pprof_on ? c->pprof : nullptr;
     a.work_off = c->pplan.work_off; a.z_off = c->pplan.z_off; a.b_off = c->pplan.b_off;
-    a.z_res = c->pplan.z_res; a.b_res = c->pplan.b_res; a.smem_bytes = c->pplan.bytes;
+    a.z_res = c->pplan.z_res; a.b_res = c->pplan.b_res;
+    a.smem_bytes = a.kind == PK_CH ? c->pplan.bytes : 0;
+    if (a.esolp) {  // the momentum kernel's own plan
+        a.work_off = c->eplan.work_off; a.b_off = c->eplan.b_off; a.b_res = c->eplan.b_res;
+        a.z_res = 0;
+        a.smem_bytes = c->eplan.bytes;
+    }
     return a;
 }
 
@@ -713,7 +738,7 @@ int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int 
     Dots d = dots(c);
     int rc = DRD_OK;
     const bool persistent =
-        mixed && c->persist && ((S.kind == SYS_CH && c->persist_ch) || (S.kind == SYS_UV && !S.esolp));
+        mixed && c->persist && ((S.kind == SYS_CH && c->persist_ch) || (S.kind == SYS_UV && (!S.esolp || c->persist_esolp)));
     if (!persistent) launch_stamp(ks, 0, c->ctr, s);
     if (!mixed) {
         enq_sys_setup<double>(c, S, s);
@@ -1131,6 +1156,22 @@ int upload_tables(drd_ctx* c) {
         host_esolp(c->P, bdf, f);
         CK(cudaMemcpy(c->es64[bdf - 1], f.data(), sizeof(double) * f.size(), cudaMemcpyHostToDevice));
         launch_convert_scale<float, double>((long)f.size(), c->es64[bdf - 1], 1.0, c->es32[bdf - 1], nullptr, c->s);
+        // r_j, 1/b'_j (0 at the last row when |b'| <= 1e-12, as rfords' back substitution), c_j/b'_j
+        std::vector<float> q(f.size());
+        const long mu = (long)(c->nr + 1) * c->nz, mv = (long)c->nr * (c->nz - 1);
+        for (int blk = 0; blk < 2; ++blk) {
+            const long base = blk ? 3 * mu : 0, rb = blk ? mv : mu;
+            const int len = blk ? c->nr : c->nr + 1, rows = blk ? c->nz - 1 : c->nz;
+            for (long e = 0; e < rb; ++e) {
+                const long j = e / len;
+                const double rm = f[base + e], bp = f[base + rb + e], cc = f[base + 2 * rb + e];
+                const bool last = j == rows - 1;
+                q[base + e] = (float)rm;
+                q[base + rb + e] = (float)((last && std::fabs(bp) <= 1.0E-12) ? 0.0 : 1.0 / bp);
+                q[base + 2 * rb + e] = (float)(last ? 0.0 : cc / bp);
+            }
+        }
+        CK(cudaMemcpy(c->esq32[bdf - 1], q.data(), sizeof(float) * q.size(), cudaMemcpyHostToDevice));
     }
     CK(cudaStreamSynchronize(c->s));
     return DRD_OK;
@@ -1196,7 +1237,11 @@ int setup_context(drd_ctx* c) {
     const long fu = (long)c->Ku * c->Nue, nes = 3 * ((long)(nr + 1) * nz + (long)nr * (nz - 1));
     c->f1ue = carve<double>(c, fu); c->f1uo = carve<double>(c, fu);
     c->f1ue32 = carve<float>(c, fu); c->f1uo32 = carve<float>(c, fu);
-    for (int b = 0; b < 2; ++b) { c->es64[b] = carve<double>(c, nes); c->es32[b] = carve<float>(c, nes); }
+    for (int b = 0; b < 2; ++b) {
+        c->es64[b] = carve<double>(c, nes);
+        c->es32[b] = carve<float>(c, nes);
+        c->esq32[b] = carve<float>(c, nes);
+    }
     c->esw = carve<double>(c, c->nmax); c->esw32 = carve<float>(c, c->nmax);
     if (c->arena_used > c->arena_bytes) { c->err = "arena overflow"; return DRD_ERR_NOMEM; }
     CK(cudaMallocHost(&c->h_ks, KS_COUNT * sizeof(KState)));
@@ -2057,7 +2102,7 @@ int drd_op_apply(drd_ctx* c, int op, int bdf, int precision, const double* x, do
     if (precision == DRD_OP_PERSISTENT && (kind == SYS_CH || kind == SYS_UV)) {
         // the persistent solver's own operator code: x = op(b) in one cooperative launch
         if (!c->persist) { c->err = "persistent solver not in use: " + c->persist_err; return DRD_ERR_UNSUPPORTED; }
-        if (S.esolp) { c->err = "the persistent momentum solver applies Jacobi only"; return DRD_ERR_UNSUPPORTED; }
+        if (S.esolp && !c->persist_esolp) { c->err = "the persistent momentum solver cannot hold ESOLP_x's work area"; return DRD_ERR_UNSUPPORTED; }
         KVecs<float>& f = c->k32;
         enq_sys_setup<float>(c, S, c->s);
         launch_convert_scale<float, double>(n, k.tmp, 1.0, f.b, c->ctr, c->s);
