@@ -40,9 +40,9 @@ sys.path.insert(0, ROOT)
 METRIC = "time-steps/s and solves/s to FP64 resid 1e-8: learned+FP32 vs plain FP64, 1 GB300"
 # DRAM bytes (read + write) of one launch of the persistent CH solve kernel, from an ncu capture
 # of this workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch)
-TRAFFIC_CH = 4353792 + 371712
-# the same for one launch of the persistent momentum solve kernel (the same capture)
-TRAFFIC_UV = 6082048 + 141312
+TRAFFIC_CH = 4347648 + 264704
+# the same for one launch of the persistent momentum solve kernel with ESOLP_x (the same capture)
+TRAFFIC_UV = 8218624 + 1832960
 WORKLOAD = ("420x180 serpentine channel (amp 30, period 140 cells, penalty 1e4), 3 rigid fibers 40x4, "
             "2 drops R=15, lambda_eta 5, Re 0.5, Ca 0.05; CH + momentum + pressure per step, tol 1e-8")
 
@@ -555,7 +555,11 @@ def run_gpu(args, ws, rank, local):
     # the mixed leg and the drop-in e2e leg (same context) start each solve from the cubic
     # extrapolation 4 x^n - 6 x^(n-1) + 4 x^(n-2) - x^(n-3) (guess_mode 3); the FP64 leg starts
     # from x^n as the reference does
-    case = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED, guess_mode=3)
+    # the momentum solves of the headline and of the e2e leg use ESOLP_x (the reference's DCT /
+    # tridiagonal momentum preconditioner, Precipitation_dynamics/ESOLP.f90) in the persistent
+    # solver; the FP64 legs keep VeloSolve_2_combined's Jacobi, and an arm isolates the choice
+    case = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED, guess_mode=3,
+                     uv_precond=abi.DRD_UV_ESOLP)
 
     # the learned blend of the CH preconditioner: a U-Net trained, before any timed region, on
     # the probe fits of other seeded geometries (seeds 1000.., never a rank's own), then asked
@@ -610,7 +614,7 @@ def run_gpu(args, ws, rank, local):
     # the flow, its forces spread onto the grid, rho/eta rebuilt every step) in place of the
     # rigid fibers: reported beside the headline, not part of it
     casep = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED, guess_mode=3,
-                      particles=True)
+                      particles=True, uv_precond=abi.DRD_UV_ESOLP)
     ctxp = DRDContext(casep.params)
     ctxp.set_case(casep)
     install_blend(ctxp, casep)
@@ -648,13 +652,15 @@ def run_gpu(args, ws, rank, local):
         f64 = time_resident(ctx64, case64, W, K64, flush)
         f64_sec = max_over_ranks(dist, f64["seconds"])
         ctx64.close()
-        legs = [("fp64_cubic", abi.DRD_PREC_FP64, None, K64, None),
-                ("mixed_cubic_graph_loop", abi.DRD_PREC_MIXED, "0", K, None)]
+        J, E = abi.DRD_UV_JACOBI, abi.DRD_UV_ESOLP
+        legs = [("fp64_cubic", abi.DRD_PREC_FP64, None, K64, None, J),
+                ("mixed_cubic_graph_loop", abi.DRD_PREC_MIXED, "0", K, None, J),
+                ("mixed_cubic_persistent_psolve_cg", abi.DRD_PREC_MIXED, None, K, None, J)]
         if blend_net is not None:
-            legs += [("mixed_cubic_persistent_psolve_cg", abi.DRD_PREC_MIXED, None, K, None),
-                     ("mixed_cubic_persistent_probe_blend", abi.DRD_PREC_MIXED, None, K, "probe")]
-        for name, prec, persist_env, nsteps, pc in legs:
-            casea = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=prec, guess_mode=3)
+            legs += [("mixed_cubic_persistent_learned_blend_jacobi", abi.DRD_PREC_MIXED, None, K, "learned", J),
+                     ("mixed_cubic_persistent_probe_blend_esolp", abi.DRD_PREC_MIXED, None, K, "probe", E)]
+        for name, prec, persist_env, nsteps, pc, uvp in legs:
+            casea = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=prec, guess_mode=3, uv_precond=uvp)
             if persist_env is not None:
                 os.environ["DRD_PERSIST"] = persist_env
             try:
@@ -664,6 +670,8 @@ def run_gpu(args, ws, rank, local):
             ctxa.set_case(casea)
             if pc == "probe":  # this geometry's own probe fit (64 probes) in place of the network's
                 ctxa.ch_blend_probe(64, 7, install=True)
+            elif pc == "learned":
+                install_blend(ctxa, casea)
             ra = time_resident(ctxa, casea, W, nsteps, flush)
             ctxa.close()
             sa = max_over_ranks(dist, ra["seconds"])
@@ -690,10 +698,11 @@ def run_gpu(args, ws, rank, local):
     #   weights and the preconditioner's input, read once per preconditioner application), and per
     #   refinement sweep the FP64 residual (x, b, r and the two mobility fields) and the FP32 scale
     #   / FP64 update passes.
-    # momentum: 24 n + 6 N_c FP32 words per iteration (n = nuv unknowns: the p update 4 n, the two
-    #   Jacobi applications 3 n each, the two operators 2 n each plus rho, eta and the penalty at
-    #   N_c each, s 3 n, the x update 4 n, r 3 n), and per sweep the FP64 residual (x, b, r and the
-    #   three coefficient fields) and the scale / update passes.
+    # momentum with ESOLP_x: 36 n + 6 N_c FP32 words per iteration (n = nuv unknowns: the two
+    #   preconditioner applications 9 n each -- input read and output written in each of the three
+    #   phases, the three factor arrays read in the tridiagonal one; the two operators 2 n each plus
+    #   rho, eta and the penalty at N_c each; the S pass 4 n; the X / R / P pass 10 n), and per sweep
+    #   the FP64 residual (x, b, r and the three coefficient fields) and the scale / update passes.
     nc = args.nr * args.nz
     cs = (args.nr + 2) * (args.nz + 2)
     nuv = (args.nr + 1) * args.nz + args.nr * (args.nz - 1)
@@ -705,7 +714,7 @@ def run_gpu(args, ws, rank, local):
                sum(mx["ch_refinements"]) * (8.0 * (4 * nc + 2 * cs) + 4.0 * 4 * nc + 20.0 * nc)},
         "uv": {"name": "k_bicg_persist<UV> (whole mixed momentum solve)", "traffic": TRAFFIC_UV,
                "iters": sum(mx["uv_iters"]), "sec": sum(mx["uv_solve_s"]), "launches": len(mx["uv_solve_s"]),
-               "bytes": (24.0 * nuv + 6.0 * nc) * 4 * sum(mx["uv_iters"]) +
+               "bytes": (36.0 * nuv + 6.0 * nc) * 4 * sum(mx["uv_iters"]) +
                sum(mx["uv_refinements"]) * (8.0 * (3 * nuv + 3 * cs) + 4.0 * 3 * nuv + 20.0 * nuv)},
     }
     for kd in kernels.values():
@@ -740,15 +749,17 @@ def run_gpu(args, ws, rank, local):
         "data": "synthetic (seeded geometry, fibers and drops per rank)",
         "config": {
             "workload": WORKLOAD, "nr": args.nr, "nz": args.nz,
-            "path": ("learned + mixed: FP32 BiCGSTAB in FP64 refinement; the CH preconditioner PSolve_CG "
-                     "blended per cell, y = q + w (x - q), with weights w predicted by the U-Net from the "
-                     "mobility fields (learned_blend); initial guesses by cubic extrapolation. The learned "
-                     "initial guess is measured beside it (learned_guess) and does not drive the timed step")
+            "path": ("learned + mixed: FP32 BiCGSTAB in FP64 refinement, one persistent launch per solve; the CH "
+                     "preconditioner PSolve_CG blended per cell, y = q + w (x - q), with weights w predicted by "
+                     "the U-Net from the mobility fields (learned_blend); the momentum preconditioner ESOLP_x; "
+                     "initial guesses by cubic extrapolation. The learned initial guess is measured beside it "
+                     "(learned_guess) and does not drive the timed step")
             if blend_net is not None else
             "mixed + cubic guess: FP32 BiCGSTAB in FP64 refinement, PSolve_CG, initial guesses by cubic "
             "extrapolation",
             "learned_blend": blend,
             "initial_guess": "mixed and e2e legs: cubic extrapolation 4x^n - 6x^(n-1) + 4x^(n-2) - x^(n-3) (guess_mode 3); fp64 leg: x^n",
+            "momentum_preconditioner": "mixed and e2e legs: ESOLP_x (uv_precond 1); fp64 legs: Jacobi (PSolve_uv_2_CG)",
             "inner_ch_solver": "persistent cooperative kernel" if persist[0] else
             f"kernel-per-phase graph loop ({persist[1] or 'persistent solver off'})",
             "parallelism": f"replicas x{ws}", "l2": "flushed between timed steps (512 MiB write)",
@@ -769,10 +780,15 @@ def run_gpu(args, ws, rank, local):
                 "arithmetic (fp64 cubic -> mixed cubic, both graph loops)":
                     arms["mixed_cubic_graph_loop"]["steps_per_s"] / arms["fp64_cubic"]["steps_per_s"],
                 "launch structure (graph loop -> persistent solves)":
-                    (arms["mixed_cubic_persistent_psolve_cg"]["steps_per_s"] if blend_net is not None else value) /
-                    arms["mixed_cubic_graph_loop"]["steps_per_s"],
-                **({"learned blend (PSolve_CG -> learned blend, persistent)":
-                    value / arms["mixed_cubic_persistent_psolve_cg"]["steps_per_s"]} if blend_net is not None else {})},
+                    arms["mixed_cubic_persistent_psolve_cg"]["steps_per_s"] / arms["mixed_cubic_graph_loop"]["steps_per_s"],
+                **({"learned blend (PSolve_CG -> learned blend, persistent, Jacobi)":
+                    arms["mixed_cubic_persistent_learned_blend_jacobi"]["steps_per_s"] /
+                    arms["mixed_cubic_persistent_psolve_cg"]["steps_per_s"],
+                    "momentum preconditioner (Jacobi -> ESOLP_x, persistent, learned blend)":
+                    value / arms["mixed_cubic_persistent_learned_blend_jacobi"]["steps_per_s"]}
+                   if blend_net is not None else
+                   {"momentum preconditioner (Jacobi -> ESOLP_x, persistent)":
+                    value / arms["mixed_cubic_persistent_psolve_cg"]["steps_per_s"]})},
             "kernels_us": {abi.KB_NAMES[k]: round(v[0], 3) for k, v in kb.items()},
             "with_particles": {"steps_per_s": K * ws / pt_sec, "ms_per_step": 1e3 * pt_sec / K, "beads": 9,
                                "solves_to_fp64_1e-8": f"{pt['solves_ok']}/{pt['solves']}"},
