@@ -43,6 +43,9 @@ METRIC = "time-steps/s and solves/s to FP64 resid 1e-8: learned+FP32 vs plain FP
 TRAFFIC_CH = 4347648 + 264704
 # the same for one launch of the persistent momentum solve kernel with ESOLP_x (the same capture)
 TRAFFIC_UV = 8218624 + 1832960
+# relative residual reduction of each FP32 inner solve in the mixed mode's FP64 refinement (every
+# mixed leg of the GPU arm)
+INNER_TOL = 0.1
 WORKLOAD = ("420x180 serpentine channel (amp 30, period 140 cells, penalty 1e4), 3 rigid fibers 40x4, "
             "2 drops R=15, lambda_eta 5, Re 0.5, Ca 0.05; CH + momentum + pressure per step, tol 1e-8")
 
@@ -257,13 +260,15 @@ def time_c5(steps, seed=0):
     from drd_application_gb300.workloads import make_case
 
     out, fields = {}, {}
-    for name, prec, gm, pc in (("mixed", abi.DRD_PREC_MIXED, 3, None), ("mixed_probe_blend", abi.DRD_PREC_MIXED, 3, 64),
-                               ("fp64", abi.DRD_PREC_FP64, 0, None)):
-        case = make_case("c5", seed=seed, precision=prec, guess_mode=gm)
+    J, ES = abi.DRD_UV_JACOBI, abi.DRD_UV_ESOLP_SCALED
+    for name, prec, gm, pc, uvp in (("mixed", abi.DRD_PREC_MIXED, 3, None, J),
+                                    ("mixed_probe_blend_esolp_scaled", abi.DRD_PREC_MIXED, 3, 64, ES),
+                                    ("fp64", abi.DRD_PREC_FP64, 0, None, J)):
+        case = make_case("c5", seed=seed, precision=prec, guess_mode=gm, uv_precond=uvp)
         ctx = DRDContext(case.params)
         ctx.set_case(case)
         fit_s = None
-        if pc:  # this geometry's probe-fitted blend of the CH preconditioner
+        if pc:  # this geometry's probe-fitted blend of the CH preconditioner (the network is per grid)
             t0 = time.perf_counter()
             ctx.ch_blend_probe(pc, 11, install=True)
             fit_s = time.perf_counter() - t0
@@ -286,7 +291,7 @@ def time_c5(steps, seed=0):
         if fit_s is not None:
             out[name]["probe_fit_s"] = fit_s
     rel = lambda a, b: float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))  # noqa: E731
-    for name in ("mixed", "mixed_probe_blend"):
+    for name in ("mixed", "mixed_probe_blend_esolp_scaled"):
         out[name + "_vs_fp64"] = {"u": rel(fields[name][abi.F_U], fields["fp64"][abi.F_U]),
                                   "v": rel(fields[name][abi.F_V], fields["fp64"][abi.F_V]),
                                   "ph": rel(fields[name][abi.F_PH], fields["fp64"][abi.F_PH])}
@@ -556,10 +561,11 @@ def run_gpu(args, ws, rank, local):
     # extrapolation 4 x^n - 6 x^(n-1) + 4 x^(n-2) - x^(n-3) (guess_mode 3); the FP64 leg starts
     # from x^n as the reference does
     # the momentum solves of the headline and of the e2e leg use ESOLP_x (the reference's DCT /
-    # tridiagonal momentum preconditioner, Precipitation_dynamics/ESOLP.f90) in the persistent
-    # solver; the FP64 legs keep VeloSolve_2_combined's Jacobi, and an arm isolates the choice
+    # tridiagonal momentum preconditioner, Precipitation_dynamics/ESOLP.f90) between the diagonal
+    # scalings of the variable coefficients, in the persistent solver; the FP64 legs keep
+    # VeloSolve_2_combined's Jacobi, and arms isolate each choice
     case = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED, guess_mode=3,
-                     uv_precond=abi.DRD_UV_ESOLP)
+                     uv_precond=abi.DRD_UV_ESOLP_SCALED, mixed_inner_tol=INNER_TOL)
 
     # the learned blend of the CH preconditioner: a U-Net trained, before any timed region, on
     # the probe fits of other seeded geometries (seeds 1000.., never a rank's own), then asked
@@ -614,7 +620,7 @@ def run_gpu(args, ws, rank, local):
     # the flow, its forces spread onto the grid, rho/eta rebuilt every step) in place of the
     # rigid fibers: reported beside the headline, not part of it
     casep = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=abi.DRD_PREC_MIXED, guess_mode=3,
-                      particles=True, uv_precond=abi.DRD_UV_ESOLP)
+                      particles=True, uv_precond=abi.DRD_UV_ESOLP_SCALED, mixed_inner_tol=INNER_TOL)
     ctxp = DRDContext(casep.params)
     ctxp.set_case(casep)
     install_blend(ctxp, casep)
@@ -652,15 +658,17 @@ def run_gpu(args, ws, rank, local):
         f64 = time_resident(ctx64, case64, W, K64, flush)
         f64_sec = max_over_ranks(dist, f64["seconds"])
         ctx64.close()
-        J, E = abi.DRD_UV_JACOBI, abi.DRD_UV_ESOLP
+        J, E, ES = abi.DRD_UV_JACOBI, abi.DRD_UV_ESOLP, abi.DRD_UV_ESOLP_SCALED
         legs = [("fp64_cubic", abi.DRD_PREC_FP64, None, K64, None, J),
                 ("mixed_cubic_graph_loop", abi.DRD_PREC_MIXED, "0", K, None, J),
                 ("mixed_cubic_persistent_psolve_cg", abi.DRD_PREC_MIXED, None, K, None, J)]
         if blend_net is not None:
             legs += [("mixed_cubic_persistent_learned_blend_jacobi", abi.DRD_PREC_MIXED, None, K, "learned", J),
-                     ("mixed_cubic_persistent_probe_blend_esolp", abi.DRD_PREC_MIXED, None, K, "probe", E)]
+                     ("mixed_cubic_persistent_learned_blend_esolp", abi.DRD_PREC_MIXED, None, K, "learned", E),
+                     ("mixed_cubic_persistent_probe_blend_esolp_scaled", abi.DRD_PREC_MIXED, None, K, "probe", ES)]
         for name, prec, persist_env, nsteps, pc, uvp in legs:
-            casea = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=prec, guess_mode=3, uv_precond=uvp)
+            casea = make_case("c2", seed=rank, nr=args.nr, nz=args.nz, precision=prec, guess_mode=3, uv_precond=uvp,
+                              **({"mixed_inner_tol": INNER_TOL} if prec == abi.DRD_PREC_MIXED else {}))
             if persist_env is not None:
                 os.environ["DRD_PERSIST"] = persist_env
             try:
@@ -701,8 +709,9 @@ def run_gpu(args, ws, rank, local):
     # momentum with ESOLP_x: 36 n + 6 N_c FP32 words per iteration (n = nuv unknowns: the two
     #   preconditioner applications 9 n each -- input read and output written in each of the three
     #   phases, the three factor arrays read in the tridiagonal one; the two operators 2 n each plus
-    #   rho, eta and the penalty at N_c each; the S pass 4 n; the X / R / P pass 10 n), and per sweep
-    #   the FP64 residual (x, b, r and the three coefficient fields) and the scale / update passes.
+    #   rho, eta and the penalty at N_c each; the S pass 4 n; the X / R / P pass 10 n; 4 n more for
+    #   the diagonal scalings of the scaled form), and per sweep the FP64 residual (x, b, r and the
+    #   three coefficient fields) and the scale / update passes.
     nc = args.nr * args.nz
     cs = (args.nr + 2) * (args.nz + 2)
     nuv = (args.nr + 1) * args.nz + args.nr * (args.nz - 1)
@@ -714,7 +723,7 @@ def run_gpu(args, ws, rank, local):
                sum(mx["ch_refinements"]) * (8.0 * (4 * nc + 2 * cs) + 4.0 * 4 * nc + 20.0 * nc)},
         "uv": {"name": "k_bicg_persist<UV> (whole mixed momentum solve)", "traffic": TRAFFIC_UV,
                "iters": sum(mx["uv_iters"]), "sec": sum(mx["uv_solve_s"]), "launches": len(mx["uv_solve_s"]),
-               "bytes": (36.0 * nuv + 6.0 * nc) * 4 * sum(mx["uv_iters"]) +
+               "bytes": (40.0 * nuv + 6.0 * nc) * 4 * sum(mx["uv_iters"]) +
                sum(mx["uv_refinements"]) * (8.0 * (3 * nuv + 3 * cs) + 4.0 * 3 * nuv + 20.0 * nuv)},
     }
     for kd in kernels.values():
@@ -751,15 +760,17 @@ def run_gpu(args, ws, rank, local):
             "workload": WORKLOAD, "nr": args.nr, "nz": args.nz,
             "path": ("learned + mixed: FP32 BiCGSTAB in FP64 refinement, one persistent launch per solve; the CH "
                      "preconditioner PSolve_CG blended per cell, y = q + w (x - q), with weights w predicted by "
-                     "the U-Net from the mobility fields (learned_blend); the momentum preconditioner ESOLP_x; "
-                     "initial guesses by cubic extrapolation. The learned initial guess is measured beside it "
-                     "(learned_guess) and does not drive the timed step")
+                     "the U-Net from the mobility fields (learned_blend); the momentum preconditioner ESOLP_x "
+                     "between diagonal scalings; initial guesses by cubic extrapolation. The learned initial "
+                     "guess is measured beside it (learned_guess) and does not drive the timed step")
             if blend_net is not None else
             "mixed + cubic guess: FP32 BiCGSTAB in FP64 refinement, PSolve_CG, initial guesses by cubic "
             "extrapolation",
             "learned_blend": blend,
             "initial_guess": "mixed and e2e legs: cubic extrapolation 4x^n - 6x^(n-1) + 4x^(n-2) - x^(n-3) (guess_mode 3); fp64 leg: x^n",
-            "momentum_preconditioner": "mixed and e2e legs: ESOLP_x (uv_precond 1); fp64 legs: Jacobi (PSolve_uv_2_CG)",
+            "momentum_preconditioner": "mixed and e2e legs: ESOLP_x between the diagonal scalings sqrt(D0/D) "
+                                       "(uv_precond 2); fp64 legs: Jacobi (PSolve_uv_2_CG)",
+            "mixed_inner_tol": INNER_TOL,
             "inner_ch_solver": "persistent cooperative kernel" if persist[0] else
             f"kernel-per-phase graph loop ({persist[1] or 'persistent solver off'})",
             "parallelism": f"replicas x{ws}", "l2": "flushed between timed steps (512 MiB write)",
@@ -785,9 +796,12 @@ def run_gpu(args, ws, rank, local):
                     arms["mixed_cubic_persistent_learned_blend_jacobi"]["steps_per_s"] /
                     arms["mixed_cubic_persistent_psolve_cg"]["steps_per_s"],
                     "momentum preconditioner (Jacobi -> ESOLP_x, persistent, learned blend)":
-                    value / arms["mixed_cubic_persistent_learned_blend_jacobi"]["steps_per_s"]}
+                    arms["mixed_cubic_persistent_learned_blend_esolp"]["steps_per_s"] /
+                    arms["mixed_cubic_persistent_learned_blend_jacobi"]["steps_per_s"],
+                    "variable-coefficient scaling (ESOLP_x -> scaled ESOLP_x)":
+                    value / arms["mixed_cubic_persistent_learned_blend_esolp"]["steps_per_s"]}
                    if blend_net is not None else
-                   {"momentum preconditioner (Jacobi -> ESOLP_x, persistent)":
+                   {"momentum preconditioner (Jacobi -> scaled ESOLP_x, persistent)":
                     value / arms["mixed_cubic_persistent_psolve_cg"]["steps_per_s"]})},
             "kernels_us": {abi.KB_NAMES[k]: round(v[0], 3) for k, v in kb.items()},
             "with_particles": {"steps_per_s": K * ws / pt_sec, "ms_per_step": 1e3 * pt_sec / K, "beads": 9,

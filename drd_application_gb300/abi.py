@@ -29,7 +29,7 @@ DRD_FLAG_FALLBACK64 = 8
 DRD_OP_CH_MATVEC, DRD_OP_CH_PSOLVE, DRD_OP_UV_MATVEC, DRD_OP_UV_PSOLVE, DRD_OP_PHMU_MATVEC, DRD_OP_PHMU_PSOLVE = range(6)
 DRD_OP_PERSISTENT = 2  # op_apply precision: the persistent solver's FP32 operator code
 DRD_SYS_CH, DRD_SYS_UV = 0, 1  # drd_solve systems
-DRD_UV_JACOBI, DRD_UV_ESOLP = 0, 1  # drd_params.uv_precond
+DRD_UV_JACOBI, DRD_UV_ESOLP, DRD_UV_ESOLP_SCALED = 0, 1, 2  # drd_params.uv_precond
 
 (DRD_KB_UV_MATVEC_FP64, DRD_KB_UV_MATVEC_FP32, DRD_KB_DCT_X_FP64, DRD_KB_DCT_X_FP32, DRD_KB_DCT_Z_FP64,
  DRD_KB_DCT_Z_FP32, DRD_KB_CH_MATVEC_FP32, DRD_KB_PRESSURE_FFT64, DRD_KB_DCT2_FFT32) = range(9)

@@ -1660,6 +1660,24 @@ __global__ void k_pc_blend(long n, const T* __restrict__ x, const T* __restrict_
     }
 }
 
+// DRD_UV_ESOLP_SCALED's diagonal scaling s = sqrt(D0 / D): D the Jacobi diagonal of PSolve_uv_2_CG
+// with rho and eta, D0 with rho = eta = 1.
+template <typename T>
+__global__ void k_uv_esolp_scale(OpScal<T> o, const T* __restrict__ rho, const T* __restrict__ eta, long n,
+                                 T* __restrict__ s, ull* ctr) {
+    count_launch(ctr);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        s[q] = sqrt(uv_diag<T, true>(o, rho, eta, q) / uv_diag<T>(o, rho, eta, q));
+}
+// out = a s element-wise (out may be a), gated like the solve's other vector passes.
+template <typename T>
+__global__ void k_vmul(long n, const T* a, const T* __restrict__ s, T* out, const KState* ks, int gate, ull* ctr) {
+    count_launch(ctr);
+    if (gate_closed(ks, gate)) return;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        out[q] = a[q] * s[q];
+}
+
 // Entry q of Rademacher probe `probe`: the sign of the top bit of splitmix64(seed + (probe n +
 // q + 1) G), G = 0x9E3779B97F4A7C15.
 __device__ __forceinline__ double probe_sign(unsigned long long seed, long probe, long n, long q) {
@@ -2280,11 +2298,13 @@ struct XProb {
     int M, ld, L, K, Ne, No;
     const float *Be, *Bo;
     int mt, nt0, ntiles;
+    const float* xs;  // optional: X is read as X xs (element-wise, same layout)
+    const float* os;  // optional: out is written as the result times os
 };
 template <int BN = PB_BN>
 __device__ __forceinline__ XProb xprob(const float* X, float* out, int M, int ld, int L, int K, int Ne, int No,
                                        const float* Be, const float* Bo) {
-    XProb d{X, out, M, ld, L, K, Ne, No, Be, Bo, 0, 0, 0};
+    XProb d{X, out, M, ld, L, K, Ne, No, Be, Bo, 0, 0, 0, nullptr, nullptr};
     d.mt = (M + PB_BM - 1) / PB_BM;
     d.nt0 = (Ne + BN - 1) / BN;
     d.ntiles = d.mt * (d.nt0 + (No + BN - 1) / BN);
@@ -2339,6 +2359,11 @@ __device__ __forceinline__ void pb_xtile(const XProb& d, int tile, const float* 
                     const float* row = X + (long)m * d.ld;
                     x0[j] = __ldcg(row + k);
                     if (2 * k != L) x1[j] = __ldcg(row + L - k);
+                    if (d.xs) {
+                        const float* srow = d.xs + (long)m * d.ld;
+                        x0[j] *= __ldg(srow + k);
+                        if (2 * k != L) x1[j] *= __ldg(srow + L - k);
+                    }
                 }
                 rr += dq;
                 kk += dr;
@@ -2406,7 +2431,9 @@ __device__ __forceinline__ void pb_xtile(const XProb& d, int tile, const float* 
             const int m = m0 + o / BN, n = n0 + o % BN;
             if (m < M && n < N) {
                 const long q = (long)m * d.ld + 2 * n + par;
-                out[q] = bw ? v + __ldg(bw + q) * (__ldcg(bx + q) - v) : v;
+                float vo = bw ? v + __ldg(bw + q) * (__ldcg(bx + q) - v) : v;
+                if (d.os) vo *= __ldg(d.os + q);
+                out[q] = vo;
             }
         }
         pb_mark(pf, 2);
@@ -2435,14 +2462,19 @@ __device__ void pb_xpass(const PersistArgs& a, const float* X, float* out, float
 // at most one tile per block at 420x180 and below; the block's own B panel stays in shared memory
 // for the whole solve when the plan allows (a.b_res).
 constexpr int PB_UBN = 128, PB_UKG = 8, PB_UTM = 8;
-__device__ __forceinline__ void pb_uv_probs(const PersistArgs& a, const float* X, float* out, XProb& du, XProb& dv) {
+__device__ __forceinline__ void pb_uv_probs(const PersistArgs& a, const float* X, float* out, XProb& du, XProb& dv,
+                                            const float* xs = nullptr, const float* os = nullptr) {
     const long mu = (long)(a.nr + 1) * a.nz;
     du = xprob<PB_UBN>(X, out, a.nz, a.nr + 1, a.nr, a.Ku, a.Nue, a.Nuo, a.fue, a.fuo);
     dv = xprob<PB_UBN>(X + mu, out + mu, a.nz - 1, a.nr, a.nr - 1, a.Kx, a.Nxe, a.Nxo, a.fxe, a.fxo);
+    du.xs = xs; du.os = os;
+    dv.xs = xs ? xs + mu : nullptr; dv.os = os ? os + mu : nullptr;
 }
-__device__ void pb_xpass_uv(const PersistArgs& a, const float* X, float* out, float* smem, const PbProf& pf) {
+// xs, os (optional): scale the input / the output element-wise (DRD_UV_ESOLP_SCALED)
+__device__ void pb_xpass_uv(const PersistArgs& a, const float* X, float* out, float* smem, const PbProf& pf,
+                            const float* xs = nullptr, const float* os = nullptr) {
     XProb du, dv;
-    pb_uv_probs(a, X, out, du, dv);
+    pb_uv_probs(a, X, out, du, dv, xs, os);
     const int tot = du.ntiles + dv.ntiles;
     const float* Bres = a.b_res ? smem + a.b_off : nullptr;
     for (int tile = blockIdx.x; tile < tot; tile += gridDim.x) {
@@ -2588,11 +2620,12 @@ __device__ void pb_tridiag_uv(const PersistArgs& a, float* w, float* smem, const
 // psolve of the momentum system with ESOLP_x: y = C_x T^-1 C_x x per block (three phases, two
 // internal barriers); a.ff1 holds the intermediate.
 __device__ bool pb_psolve_uv(const PersistArgs& a, const float* x, float* y, float* smem, unsigned& gen, PbProf& pf) {
-    pb_xpass_uv(a, x, a.ff1, smem, pf);
+    const float* sc = a.esolp == 2 ? a.diag : nullptr;  // DRD_UV_ESOLP_SCALED: y = s E(s x), s in a.diag
+    pb_xpass_uv(a, x, a.ff1, smem, pf, sc, nullptr);
     if (!grid_sync(a.bar, gen, pf)) return false;
     pb_tridiag_uv(a, a.ff1, smem, pf);
     if (!grid_sync(a.bar, gen, pf)) return false;
-    pb_xpass_uv(a, a.ff1, y, smem, pf);
+    pb_xpass_uv(a, a.ff1, y, smem, pf, nullptr, sc);
     return true;
 }
 
@@ -3593,6 +3626,14 @@ void launch_bi_diag_apply(long n, const T* x, const T* diag, int ident, T* y, co
     k_bi_diag_apply<T><<<GRID(n)>>>(n, x, diag, ident, y, ks, gate, ctr);
 }
 template <typename T>
+void launch_uv_esolp_scale(const OpScal<T>& o, const T* rho, const T* eta, long n, T* sc, ull* ctr, cudaStream_t s) {
+    k_uv_esolp_scale<T><<<GRID(n)>>>(o, rho, eta, n, sc, ctr);
+}
+template <typename T>
+void launch_vmul(long n, const T* a, const T* sc, T* out, const KState* ks, int gate, ull* ctr, cudaStream_t s) {
+    k_vmul<T><<<GRID(n)>>>(n, a, sc, out, ks, gate, ctr);
+}
+template <typename T>
 void launch_pc_blend(long n, const T* x, const T* w, T* y, const KState* ks, int gate, ull* ctr, cudaStream_t s) {
     k_pc_blend<T><<<GRID(n)>>>(n, x, w, y, ks, gate, ctr);
 }
@@ -3696,6 +3737,8 @@ template void launch_mx_scale<float>(long, const double*, const KState*, float*,
     template void launch_bi_s<T>(long, const T*, T*, KState*, const Dots&, ull*, cudaStream_t);                       \
     template void launch_bi_diag_apply<T>(long, const T*, const T*, int, T*, const KState*, int, ull*, cudaStream_t); \
     template void launch_pc_blend<T>(long, const T*, const T*, T*, const KState*, int, ull*, cudaStream_t);          \
+    template void launch_uv_esolp_scale<T>(const OpScal<T>&, const T*, const T*, long, T*, ull*, cudaStream_t);     \
+    template void launch_vmul<T>(long, const T*, const T*, T*, const KState*, int, ull*, cudaStream_t);              \
     template void launch_bi_xr<T>(long, const T*, const T*, const T*, const T*, T*, T*, KState*, const Dots&, ull*,   \
                                   cudaStream_t);                                                                      \
     template void launch_copy<T>(long, const T*, T*, ull*, cudaStream_t);                                            \

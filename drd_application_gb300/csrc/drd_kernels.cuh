@@ -178,7 +178,7 @@ struct PersistArgs {
     // momentum with ESOLP_x: the folded VCOST operands of length nr+1 (u block, Ku x Nue; the v
     // block uses the CH x-pass operands of length nr), the Thomas factors of the bdf (u block
     // rm, bp, cc, then the v block), the tridiagonal phase's modes per batch
-    int esolp;
+    int esolp;  // 1: ESOLP_x, 2: ESOLP_x between the diagonal scalings held in diag
     const float *fue, *fuo, *esf;
     int Ku, Nue, Nuo;
     float *x, *b, *r, *rtld, *p, *v, *phat, *shat, *t, *ff1, *w1, *w2;
@@ -252,6 +252,10 @@ void launch_bi_s(long n, const T* v, T* r, KState* ks, const Dots& d, ull* ctr, 
 void launch_bi_snorm(KState* ks, const Dots& d, ull* ctr, cudaStream_t s);
 template <typename T>
 void launch_pc_blend(long n, const T* x, const T* w, T* y, const KState* ks, int gate, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_uv_esolp_scale(const OpScal<T>& o, const T* rho, const T* eta, long n, T* sc, ull* ctr, cudaStream_t s);
+template <typename T>
+void launch_vmul(long n, const T* a, const T* sc, T* out, const KState* ks, int gate, ull* ctr, cudaStream_t s);
 void launch_probe_fill(long n, unsigned long long seed, long probe, double* e, ull* ctr, cudaStream_t s);
 void launch_probe_acc(long n, unsigned long long seed, long probe, const double* r, const double* qv, double* num,
                       double* den, int first, ull* ctr, cudaStream_t s);

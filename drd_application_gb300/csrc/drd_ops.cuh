@@ -100,17 +100,18 @@ __device__ __forceinline__ T uv_apply(const OpScal<T>& o, const T* __restrict__ 
 // The Jacobi diagonal of PSolve_uv_2_CG (:649-711) / PSolve_uv_CG for row q: 1.5 re rho-bar (re
 // for bdf 1) plus the eta stencil's diagonal, boundary-aware, without the penalty; the v rows
 // average rho(i,j) and rho(i-1,j) as the reference does (:690).
-template <typename T>
+// UNIT: the same diagonal with rho = eta = 1 (the arrays are not read).
+template <typename T, bool UNIT = false>
 __device__ __forceinline__ T uv_diag(const OpScal<T>& o, const T* __restrict__ rho, const T* __restrict__ eta, long q) {
     const int nr = o.nr, nz = o.nz;
     const long mn = (long)(nr + 1) * nz;
     const T mcoef = (o.bdf == 2) ? T(1.5) * o.re : o.re;
     const T h = T(0.5), q4 = T(0.25);
-#define E_(i, k) eta[cidx(nr, i, k)]
+#define E_(i, k) (UNIT ? T(1) : eta[cidx(nr, i, k)])
     T tmp;
     if (q < mn) {
         const int i = (int)(q % (nr + 1)), j = (int)(q / (nr + 1));
-        tmp = mcoef * (rho[cidx(nr, i, j)] + rho[cidx(nr, i - 1, j)]) * h;
+        tmp = mcoef * (UNIT ? T(2) : rho[cidx(nr, i, j)] + rho[cidx(nr, i - 1, j)]) * h;
         T cr = E_(i, j), cl = E_(i - 1, j);
         tmp = tmp + T(2) * o.dt * (cl + cr) / o.dr2;
         cr = (E_(i, j + 1) + E_(i - 1, j + 1) + E_(i, j) + E_(i - 1, j)) * q4;
@@ -121,7 +122,7 @@ __device__ __forceinline__ T uv_diag(const OpScal<T>& o, const T* __restrict__ r
     } else {
         const long qv = q - mn;
         const int i = (int)(qv % nr), j = (int)(qv / nr) + 1;
-        tmp = mcoef * (rho[cidx(nr, i, j)] + rho[cidx(nr, i - 1, j)]) * h;
+        tmp = mcoef * (UNIT ? T(2) : rho[cidx(nr, i, j)] + rho[cidx(nr, i - 1, j)]) * h;
         T cr = E_(i, j), cl = E_(i, j - 1);
         tmp = tmp + T(2) * o.dt * (cl + cr) / o.dz2;
         cr = (E_(i + 1, j) + E_(i, j) + E_(i + 1, j - 1) + E_(i, j - 1)) * q4;

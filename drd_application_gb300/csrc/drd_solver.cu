@@ -480,6 +480,7 @@ struct Sys {
     int jacobi;  // diagonal preconditioner in k.diag
     int ident;   // identity preconditioner
     int esolp;   // ESOLP_x preconditioner (momentum)
+    int scaled;  // ESOLP_x between the diagonal scalings s = sqrt(D0 / D), held in k.diag
 };
 
 template <typename T>
@@ -525,6 +526,10 @@ void enq_psolve(drd_ctx* c, const Sys& S, const T* x, T* y, const KState* ks, in
         enq_ch_psolve<T>(c, x, y, ks, gate, s);
         if (S.kind == SYS_CH && c->pc_on)
             launch_pc_blend<T>(S.n, x, (sizeof(T) == 8) ? (const T*)c->pcw : (const T*)c->pcw32, y, ks, gate, c->ctr, s);
+    } else if (S.esolp && S.scaled) {  // y = s E(s x)
+        launch_vmul<T>(S.n, x, k.diag, k.ff1, ks, gate, c->ctr, s);
+        enq_esolp<T>(c, S.bdf, k.ff1, y, ks, gate, s);
+        launch_vmul<T>(S.n, y, k.diag, y, ks, gate, c->ctr, s);
     } else if (S.esolp) enq_esolp<T>(c, S.bdf, x, y, ks, gate, s);
     else launch_bi_diag_apply<T>(S.n, x, S.jacobi ? k.diag : nullptr, S.ident, y, ks, gate, c->ctr, s);
 }
@@ -534,6 +539,8 @@ template <typename T>
 void enq_sys_setup(drd_ctx* c, const Sys& S, cudaStream_t s) {
     KVecs<T>& k = vecs(c, (T*)nullptr);
     if (S.kind == SYS_UV && S.jacobi) launch_uv_diag<T>(make_op<T>(c, S.bdf), coef<T>(c, 0), coef<T>(c, 1), k.diag, c->ctr, s);
+    if (S.kind == SYS_UV && S.esolp && S.scaled)
+        launch_uv_esolp_scale<T>(make_op<T>(c, S.bdf), coef<T>(c, 0), coef<T>(c, 1), S.n, k.diag, c->ctr, s);
     if (S.kind == SYS_PHMU) launch_phmu_diag<T>(make_op<T>(c, 0), k.diag, c->ctr, s);
 }
 
@@ -711,7 +718,7 @@ PersistArgs persist_args(drd_ctx* c, const Sys& S, KState* in, const KState* par
     a.Kx = c->Kx; a.Nxe = c->Nxe; a.Nxo = c->Nxo; a.Kz = c->Kz; a.Mze = c->Mze; a.Mzo = c->Mzo;
     KVecs<float>& f = c->k32;
     a.rho = c->rho32; a.eta = c->eta32; a.pen = c->pen32; a.diag = f.diag; a.ident = S.ident || !S.jacobi;
-    a.esolp = (S.kind == SYS_UV && S.esolp) ? 1 : 0;
+    a.esolp = (S.kind == SYS_UV && S.esolp) ? (S.scaled ? 2 : 1) : 0;
     a.fue = c->f1ue32; a.fuo = c->f1uo32; a.Ku = c->Ku; a.Nue = c->Nue; a.Nuo = c->Nuo;
     a.esf = a.esolp ? c->esq32[S.bdf - 1] : nullptr;
     a.x = f.x; a.b = f.b; a.r = f.r; a.rtld = f.rtld; a.p = f.p; a.v = f.v; a.phat = f.phat; a.shat = f.shat;
@@ -814,7 +821,8 @@ Sys sys_of(drd_ctx* c, int kind, int bdf) {
     else {
         S.n = c->nuv;
         const bool tp_ident = (c->P.variant == DRD_VARIANT_TP && bdf == 2);
-        S.esolp = (c->P.uv_precond == DRD_UV_ESOLP);
+        S.esolp = (c->P.uv_precond == DRD_UV_ESOLP || c->P.uv_precond == DRD_UV_ESOLP_SCALED);
+        S.scaled = (c->P.uv_precond == DRD_UV_ESOLP_SCALED);
         S.jacobi = !tp_ident && !S.esolp;
         S.ident = tp_ident && !S.esolp;
     }
@@ -1334,7 +1342,14 @@ int validate(const drd_params* p, std::string& why) {
     if (p->ch_maxit <= 0 || p->uv_maxit <= 0 || p->phmu_maxit <= 0) { why = "maxit must be positive"; return DRD_ERR_BADARG; }
     if (p->xlsB >= 1.e-8) { why = "slip walls (xlsB >= 1e-8) have no solve in the reference"; return DRD_ERR_UNSUPPORTED; }
     if (p->guess_mode < 0 || p->guess_mode > 3) { why = "guess_mode must be 0 to 3"; return DRD_ERR_BADARG; }
-    if (p->uv_precond != DRD_UV_JACOBI && p->uv_precond != DRD_UV_ESOLP) { why = "unknown uv_precond"; return DRD_ERR_BADARG; }
+    if (p->uv_precond != DRD_UV_JACOBI && p->uv_precond != DRD_UV_ESOLP && p->uv_precond != DRD_UV_ESOLP_SCALED) {
+        why = "unknown uv_precond";
+        return DRD_ERR_BADARG;
+    }
+    if (p->uv_precond == DRD_UV_ESOLP_SCALED && p->variant != DRD_VARIANT_MF) {
+        why = "DRD_UV_ESOLP_SCALED scales by VeloSolve_2_combined's (MF) Jacobi diagonal";
+        return DRD_ERR_UNSUPPORTED;
+    }
     if (p->two_fluid != 0 && p->two_fluid != 1) { why = "two_fluid must be 0 or 1"; return DRD_ERR_BADARG; }
     if (p->precision == DRD_PREC_MIXED && (!(p->mixed_inner_tol > 0) || p->mixed_max_refine <= 0)) {
         why = "mixed precision needs mixed_inner_tol > 0 and mixed_max_refine > 0";

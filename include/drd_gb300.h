@@ -51,6 +51,10 @@ extern "C" {
 #define DRD_UV_JACOBI 0 /* PSolve_uv_2_CG (microfluidics_complex_domain/VeloSolve_2_combined.f90:649-711) */
 #define DRD_UV_ESOLP 1  /* ESOLP_x: DCT-I along x, tridiagonal along y (microfluidics_complex_domain/
                            ESOLP.f90:1-82, applied in Precipitation_dynamics/VeloSolve_combined.f90:795-808) */
+#define DRD_UV_ESOLP_SCALED 2 /* ESOLP_x between two diagonal scalings (an extension): y = s E(s x),
+                                 s = sqrt(D0 / D) per unknown, D the Jacobi diagonal of PSolve_uv_2_CG
+                                 with the context's rho and eta, D0 the same with rho = eta = 1 (the
+                                 coefficients ESOLP_x's constant operator has).  MF only. */
 
 /* Return codes besides BiCGSTAB INFO values. */
 #define DRD_OK 0
@@ -106,8 +110,10 @@ typedef struct drd_params {
     double mixed_inner_tol;        /* mixed mode: relative residual reduction per FP32 inner solve; */
                                    /* a sweep that gains < 10 % tightens it tenfold (to 1.5e-4)     */
     int32_t mixed_max_refine;      /* mixed mode: maximum FP64 refinement sweeps                   */
-    int32_t uv_precond;            /* momentum preconditioner: DRD_UV_JACOBI (the MF reference) or  */
-                                   /* DRD_UV_ESOLP (ESOLP_x, used by the PD application)             */
+    int32_t uv_precond;            /* momentum preconditioner: DRD_UV_JACOBI (the MF reference),    */
+                                   /* DRD_UV_ESOLP (ESOLP_x, used by the PD application) or         */
+                                   /* DRD_UV_ESOLP_SCALED (ESOLP_x with the variable-coefficient     */
+                                   /* diagonal scaling)                                             */
     int32_t two_fluid;             /* 0: rho, eta follow the solid/particle indicator fpd_ph only   */
                                    /* (interpolate_coef.f90:84-89).  1: the two-fluid form that     */
                                    /* two_phase_flow_complex_domain/interpolate_coef.f90:91-112     */

@@ -1114,8 +1114,36 @@ void orc_uv_psolve_esolp(const drd_params* P, int bdf, const double* x, double* 
     free(ua); free(ub); free(uc); free(va); free(vb); free(vc);
 }
 
+/* The diagonal scaling of DRD_UV_ESOLP_SCALED (an extension of ESOLP_x): s = sqrt(D0 / D) per
+ * unknown with D the Jacobi diagonal of PSolve_uv_2_CG (orc_uv_psolve's divisor) for rho, eta and
+ * D0 the same for rho = eta = 1, the coefficients of ESOLP_x's constant operator. */
+void orc_uv_esolp_scale(const drd_params* P, int bdf, const double* rho, const double* eta, double* s) {
+    const int nr = P->nr, nz = P->nz;
+    const long N = uv_len(nr, nz), cs = (long)(nr + 2) * (nz + 2);
+    double* one = dalloc(cs);
+    double* e = dalloc(N);
+    double* d = dalloc(N);
+    double* d0 = dalloc(N);
+    for (long q = 0; q < cs; ++q) one[q] = 1.0;
+    for (long q = 0; q < N; ++q) e[q] = 1.0;
+    orc_uv_psolve(P, bdf, rho, eta, e, d);  /* 1 / D */
+    orc_uv_psolve(P, bdf, one, one, e, d0); /* 1 / D0 */
+    for (long q = 0; q < N; ++q) s[q] = sqrt(d[q] / d0[q]);
+    free(one); free(e); free(d); free(d0);
+}
+
+/* y = s ESOLP_x(s x). */
+void orc_uv_psolve_esolp_scaled(const drd_params* P, int bdf, const double* s, const double* x, double* y) {
+    const long N = uv_len(P->nr, P->nz);
+    double* t = dalloc(N);
+    for (long q = 0; q < N; ++q) t[q] = s[q] * x[q];
+    orc_uv_psolve_esolp(P, bdf, t, y);
+    for (long q = 0; q < N; ++q) y[q] = s[q] * y[q];
+    free(t);
+}
+
 typedef struct {
-    const drd_params* P; int bdf; const double* rho; const double* eta; const double* pen;
+    const drd_params* P; int bdf; const double* rho; const double* eta; const double* pen; double* scale;
 } uv_ctx;
 static void uv_mv_cb(void* c, double a, const double* x, double b, double* y) {
     uv_ctx* C = (uv_ctx*)c;
@@ -1124,6 +1152,7 @@ static void uv_mv_cb(void* c, double a, const double* x, double b, double* y) {
 static void uv_ps_cb(void* c, const double* x, double* y) {
     uv_ctx* C = (uv_ctx*)c;
     if (C->P->uv_precond == DRD_UV_ESOLP) orc_uv_psolve_esolp(C->P, C->bdf, x, y);
+    else if (C->P->uv_precond == DRD_UV_ESOLP_SCALED) orc_uv_psolve_esolp_scaled(C->P, C->bdf, C->scale, x, y);
     else orc_uv_psolve(C->P, C->bdf, C->rho, C->eta, x, y);
 }
 
@@ -1137,8 +1166,14 @@ int orc_solve_system(const drd_params* P, int system, int bdf, const double* ph_
         ch_ctx C = {P, M0, Mi, ph_lcc};
         return orc_bicgstab((long)P->nr * P->nz, b, x, P->ch_maxit, P->tol, ch_mv_cb, ch_ps_cb, &C, st);
     }
-    uv_ctx C = {P, bdf, rho, eta, pen};
-    return orc_bicgstab(uv_len(P->nr, P->nz), b, x, P->uv_maxit, P->tol, uv_mv_cb, uv_ps_cb, &C, st);
+    uv_ctx C = {P, bdf, rho, eta, pen, NULL};
+    if (P->uv_precond == DRD_UV_ESOLP_SCALED) {
+        C.scale = dalloc(uv_len(P->nr, P->nz));
+        orc_uv_esolp_scale(P, bdf, rho, eta, C.scale);
+    }
+    const int info = orc_bicgstab(uv_len(P->nr, P->nz), b, x, P->uv_maxit, P->tol, uv_mv_cb, uv_ps_cb, &C, st);
+    free(C.scale);
+    return info;
 }
 
 /* ---------------------------------------------------------------------------------------
@@ -1392,8 +1427,13 @@ int orc_velosolve(const drd_params* P, int bdf, const double* psi1, const double
     }
     atob_uv(nr, nz, fu, fv, rhs); /* :388-389 */
     atob_uv(nr, nz, u, v, x);
-    uv_ctx C = {P, bdf, rho, eta, bdr_pen};
+    uv_ctx C = {P, bdf, rho, eta, bdr_pen, NULL};
+    if (P->uv_precond == DRD_UV_ESOLP_SCALED) {
+        C.scale = dalloc(N);
+        orc_uv_esolp_scale(P, bdf, rho, eta, C.scale);
+    }
     int info = orc_bicgstab(N, rhs, x, P->uv_maxit, P->tol, uv_mv_cb, uv_ps_cb, &C, st); /* :398-401 */
+    free(C.scale);
     btoa_uv(nr, nz, u_after, v_after, x); /* :411 */
     if (dirichlet) {
         for (int k = 0; k < nz; ++k) u_after[UI(-1, k)] = 2.0 * uLl[k] - u_after[UI(1, k)];

@@ -116,6 +116,9 @@ double orc_mass(const drd_params* P, const double* ph);
 void orc_esolp_coefs(const drd_params* P, int bdf, double* ua, double* ub, double* uc, double* va, double* vb,
                      double* vc);
 void orc_uv_psolve_esolp(const drd_params* P, int bdf, const double* x, double* y);
+/* DRD_UV_ESOLP_SCALED (an extension): s = sqrt(D0 / D) and y = s ESOLP_x(s x). */
+void orc_uv_esolp_scale(const drd_params* P, int bdf, const double* rho, const double* eta, double* s);
+void orc_uv_psolve_esolp_scaled(const drd_params* P, int bdf, const double* s, const double* x, double* y);
 
 /* A x = b for system 0 (CH mu) or 1 (momentum, bdf 1/2) with the reference BiCGSTAB. */
 int orc_solve_system(const drd_params* P, int system, int bdf, const double* ph_lcc, const double* M0,

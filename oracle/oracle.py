@@ -59,6 +59,8 @@ def lib(openmp=False):
         L.orc_uv_matvec.argtypes = [P, C.c_int, dp, dp, dp, C.c_double, dp, C.c_double, dp]
         L.orc_uv_psolve.argtypes = [P, C.c_int, dp, dp, dp, dp]
         L.orc_uv_psolve_esolp.argtypes = [P, C.c_int, dp, dp]
+        L.orc_uv_esolp_scale.argtypes = [P, C.c_int, dp, dp, dp]
+        L.orc_uv_psolve_esolp_scaled.argtypes = [P, C.c_int, dp, dp, dp]
         L.orc_solve_system.argtypes = [P, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp, dp, dp, S]
         L.orc_esolp_coefs.argtypes = [P, C.c_int, dp, dp, dp, dp, dp, dp]
         L.orc_phmu_matvec.argtypes = [P, dp, dp, dp, C.c_double, C.c_double, C.c_double, dp, C.c_double, dp]
@@ -112,6 +114,10 @@ class OrcState(C.Structure):
     _fields_ = [("f", C.POINTER(C.c_double) * abi.F_COUNT)] + [
         (n, C.POINTER(C.c_double)) for n in ("rho", "eta", "bdr_ph", "bdr_ph_grad", "M0", "Mi", "bdr_pen", "bdr_used")
     ] + [("parts", C.POINTER(OrcParticles)), ("fpd_ph", C.POINTER(C.c_double))]
+
+
+def abi_uv_len(nr, nz):
+    return (nr + 1) * nz + nr * (nz - 1)
 
 
 class Oracle:
@@ -211,6 +217,18 @@ class Oracle:
         """ESOLP_x on a packed momentum vector (Precipitation_dynamics/VeloSolve_combined.f90:800-806)."""
         y = np.zeros_like(x)
         self.L.orc_uv_psolve_esolp(C.byref(self.P), bdf, ptr(np.ascontiguousarray(x)), ptr(y))
+        return y
+
+    def uv_esolp_scale(self, bdf, rho, eta):
+        """s = sqrt(D0 / D) of DRD_UV_ESOLP_SCALED (packed momentum unknowns)."""
+        s = np.zeros(abi_uv_len(self.P.nr, self.P.nz))
+        self.L.orc_uv_esolp_scale(C.byref(self.P), bdf, ptr(rho), ptr(eta), ptr(s))
+        return s
+
+    def uv_psolve_esolp_scaled(self, bdf, s, x):
+        y = np.zeros_like(x)
+        self.L.orc_uv_psolve_esolp_scaled(C.byref(self.P), bdf, ptr(np.ascontiguousarray(s)),
+                                          ptr(np.ascontiguousarray(x)), ptr(y))
         return y
 
     def esolp_coefs(self, bdf):

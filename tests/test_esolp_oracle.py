@@ -102,3 +102,46 @@ def test_velosolve_esolp_matches_jacobi(oracle_build):
     assert sj.info == 0 and se.info == 0
     assert se.true_resid <= 1e-11
     assert rel_err(ue, uj) < 1e-8 and rel_err(ve, vj) < 1e-8
+
+
+@pytest.mark.parametrize("bdf", [1, 2])
+def test_esolp_scaled_definition(oracle_build, bdf):
+    """DRD_UV_ESOLP_SCALED: s = sqrt(D0 / D) from the Jacobi diagonals (D0 at rho = eta = 1),
+    y = s ESOLP_x(s x); with rho = eta = 1 the scaling is the identity."""
+    case, st, _ = advanced_case("c2", seed=2, nr=48, nz=24, steps=1)
+    P = case.params.copy()
+    orc = Oracle(P)
+    rho, eta = case.coefs["rho"], case.coefs["eta"]
+    one = np.ones_like(rho)
+    n = (P.nr + 1) * P.nz + P.nr * (P.nz - 1)
+    s = orc.uv_esolp_scale(bdf, rho, eta)
+    d = orc.uv_psolve(bdf, rho, eta, np.ones(n))
+    d0 = orc.uv_psolve(bdf, one, one, np.ones(n))
+    assert np.allclose(s, np.sqrt(d / d0), rtol=1e-14, atol=0)
+    assert s.min() > 0 and s.max() <= 1.0 + 1e-12  # rho, eta >= 1 here: D >= D0
+    x = np.random.default_rng(bdf).standard_normal(n)
+    y = orc.uv_psolve_esolp_scaled(bdf, s, x)
+    assert rel_err(y, s * orc.uv_psolve_esolp(bdf, s * x)) <= 1e-15
+    assert np.allclose(orc.uv_esolp_scale(bdf, one, one), 1.0, rtol=1e-15, atol=0)
+
+
+def test_esolp_scaled_fewer_iterations(oracle_build):
+    """With the two-fluid coefficients (viscosity ratio 5) the scaled form needs fewer momentum
+    iterations than ESOLP_x to the same FP64 residual."""
+    case, st, _ = advanced_case("c2", seed=4, nr=84, nz=36, steps=2)
+    c = case.coefs
+    from tests.helpers import pack_uv
+
+    x_true = pack_uv(st[abi.F_U], st[abi.F_V])
+    its = {}
+    for pre in (abi.DRD_UV_ESOLP, abi.DRD_UV_ESOLP_SCALED):
+        P = case.params.copy()
+        P.uv_precond = pre
+        P.tol = 1e-10
+        orc = Oracle(P)
+        b = orc.uv_matvec(2, c["rho"], c["eta"], c["bdr_pen"], x_true)
+        x, stt = orc.solve(1, 2, c, b)
+        assert stt.info == 0
+        assert np.linalg.norm(b - orc.uv_matvec(2, c["rho"], c["eta"], c["bdr_pen"], x)) <= 1.0001e-10 * np.linalg.norm(b)
+        its[pre] = stt.iter
+    assert its[abi.DRD_UV_ESOLP_SCALED] < its[abi.DRD_UV_ESOLP], its
