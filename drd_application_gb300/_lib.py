@@ -24,6 +24,8 @@ SIGNATURES = {
     "drd_set_coefs": (C.c_int, [_ctx, _dp, _dp, _dp, _dp, _dp, _dp]),
     "drd_set_tp_fields": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
     "drd_set_ch_blend": (C.c_int, [_ctx, _dp]),
+    "drd_host_register": (C.c_int, [C.c_void_p, C.c_int64]),
+    "drd_host_unregister": (C.c_int, [C.c_void_p]),
     "drd_ch_blend_probe": (C.c_int, [_ctx, C.c_int, C.c_uint64, C.c_int, _dp]),
     "drd_interpolate_coef": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),
     "drd_two_phase_coef": (C.c_int, [_ctx, _dp, _dp, _dp, _dp]),

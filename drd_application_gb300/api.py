@@ -28,6 +28,34 @@ def _check_shape(a, shape, name):
     return np.ascontiguousarray(a)
 
 
+def _out(a, shape, name):
+    """A caller-supplied output array (written in place), or a new one."""
+    if a is None:
+        return np.zeros(shape)
+    if not isinstance(a, np.ndarray) or a.shape != shape or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+        raise ValueError(f"{name}: expected a C-contiguous float64 array of shape {shape}")
+    return a
+
+
+def pin(a, lib=None):
+    """Page-lock a numpy array's memory (drd_host_register): the per-routine calls then copy it by
+    DMA.  Unpin it (unpin) before it is freed."""
+    L = lib or _lib.load()
+    if not isinstance(a, np.ndarray) or not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("pin: expected a C-contiguous numpy array")
+    rc = L.drd_host_register(C.c_void_p(a.ctypes.data), a.nbytes)
+    if rc != 0:
+        raise DRDError(f"drd_host_register failed with {rc}")
+    return a
+
+
+def unpin(a, lib=None):
+    L = lib or _lib.load()
+    rc = L.drd_host_unregister(C.c_void_p(a.ctypes.data))
+    if rc != 0:
+        raise DRDError(f"drd_host_unregister failed with {rc}")
+
+
 class DRDContext:
     """One GPU context for an nr x nz grid (drd_create / drd_destroy)."""
 
@@ -114,14 +142,15 @@ class DRDContext:
         if self.P.two_fluid:
             self.two_phase_coef(k["fpd"], case.state[abi.F_PH])
 
-    def two_phase_coef(self, fpd_ph=None, ph=None):
+    def two_phase_coef(self, fpd_ph=None, ph=None, out=None):
         """The two-fluid rho, eta of interpolate_coef (two_phase_flow_complex_domain/
         interpolate_coef.f90:91-112, commented out there) -> (rho, eta); they also replace the
         context's coefficients.  fpd_ph None keeps the context's indicator, ph None uses the
         resident phase field."""
         f = _check_shape(fpd_ph, self.cs, "fpd_ph")
         ph = _check_shape(ph, self.cs, "ph")
-        rho, eta = np.zeros(self.cs), np.zeros(self.cs)
+        o = out or (None, None)
+        rho, eta = _out(o[0], self.cs, "rho"), _out(o[1], self.cs, "eta")
         self._rc(self.L.drd_two_phase_coef(self.h, ptr(f), ptr(ph), ptr(rho), ptr(eta)), "two_phase_coef", False)
         return rho, eta
 
@@ -223,11 +252,13 @@ class DRDContext:
     def checkpoint_wait(self):
         self._rc(self.L.drd_checkpoint_wait(self.h), "drd_checkpoint_wait", False)
 
-    def PhSolve(self, u, v, ph, rmu, t):
-        """PhSolve(rmu_after, ph_after, t) -> (rmu_after, ph_after, status)."""
+    def PhSolve(self, u, v, ph, rmu, t, out=None):
+        """PhSolve(rmu_after, ph_after, t) -> (rmu_after, ph_after, status).  out: optional
+        (rmu_after, ph_after) arrays to write."""
         u, v = _check_shape(u, self.us, "u"), _check_shape(v, self.vs, "v")
         ph, rmu = _check_shape(ph, self.cs, "ph"), _check_shape(rmu, self.cs, "rmu")
-        rmu_after, ph_after = np.zeros(self.cs), np.zeros(self.cs)
+        o = out or (None, None)
+        rmu_after, ph_after = _out(o[0], self.cs, "rmu_after"), _out(o[1], self.cs, "ph_after")
         st = abi.drd_status()
         self._rc(self.L.drd_phsolve(self.h, ptr(u), ptr(v), ptr(ph), ptr(rmu), t, ptr(rmu_after), ptr(ph_after),
                                     C.byref(st)), "PhSolve")
@@ -259,27 +290,30 @@ class DRDContext:
         return u_after, v_after, uL, uR, st
 
     def VeloSolve_2_combined(self, psi1, psi2, u_pre, u, v_pre, v, p, ph_pre, ph_after, rmu_pre, rmu_after, t,
-                             particle_force1=None, particle_force2=None):
+                             particle_force1=None, particle_force2=None, out=None):
         """VeloSolve_2_combined(psi1, psi2, u_pre, u_after, v_pre, v_after, ph_pre, ph_after, rmu_pre,
-        rmu_after, t, pf1, pf2) -> (u_after, v_after, uL, uR, status)."""
+        rmu_after, t, pf1, pf2) -> (u_after, v_after, uL, uR, status).  out: optional (u_after,
+        v_after, uL, uR) arrays to write."""
         cs, us, vs = self.cs, self.us, self.vs
         a = [_check_shape(x, s, n) for x, s, n in (
             (psi1, cs, "psi1"), (psi2, cs, "psi2"), (u_pre, us, "u_pre"), (u, us, "u"), (v_pre, vs, "v_pre"),
             (v, vs, "v"), (p, cs, "p"), (ph_pre, cs, "ph_pre"), (ph_after, cs, "ph_after"), (rmu_pre, cs, "rmu_pre"),
             (rmu_after, cs, "rmu_after"))]
         pf = [_check_shape(x, cs, "particle_force") for x in (particle_force1, particle_force2)]
-        u_after, v_after = np.zeros(us), np.zeros(vs)
-        uL, uR = np.zeros(self.nz + 1), np.zeros(self.nz + 1)
+        o = out or (None, None, None, None)
+        u_after, v_after = _out(o[0], us, "u_after"), _out(o[1], vs, "v_after")
+        uL, uR = _out(o[2], (self.nz + 1,), "uL"), _out(o[3], (self.nz + 1,), "uR")
         st = abi.drd_status()
         self._rc(self.L.drd_velosolve_2_combined(self.h, *[ptr(x) for x in a], t, ptr(pf[0]), ptr(pf[1]),
                                                  ptr(u_after), ptr(v_after), ptr(uL), ptr(uR), C.byref(st)),
                  "VeloSolve_2_combined")
         return u_after, v_after, uL, uR, st
 
-    def PreSolve_2(self, u, v, coef):
-        """PreSolve_2(plan, plan_back, psi, coef) -> psi (the FFTW plans live in the context)."""
+    def PreSolve_2(self, u, v, coef, out=None):
+        """PreSolve_2(plan, plan_back, psi, coef) -> psi (the FFTW plans live in the context).
+        out: optional psi array to write."""
         u, v = _check_shape(u, self.us, "u"), _check_shape(v, self.vs, "v")
-        psi = np.zeros(self.cs)
+        psi = _out(out, self.cs, "psi")
         st = abi.drd_status()
         self._rc(self.L.drd_presolve_2(self.h, ptr(u), ptr(v), coef, ptr(psi), C.byref(st)), "PreSolve_2", False)
         return psi

@@ -2271,6 +2271,20 @@ int drd_kernel_bench(drd_ctx* c, int which, int reps, double* us, double* bytes,
     return DRD_OK;
 }
 
+int drd_host_register(void* p, int64_t bytes) {
+    if (!p || bytes <= 0) return DRD_ERR_BADARG;
+    const cudaError_t e = cudaHostRegister(p, (size_t)bytes, cudaHostRegisterDefault);
+    if (e != cudaSuccess) { cudaGetLastError(); return DRD_ERR_CUDA; }
+    return DRD_OK;
+}
+
+int drd_host_unregister(void* p) {
+    if (!p) return DRD_ERR_BADARG;
+    const cudaError_t e = cudaHostUnregister(p);
+    if (e != cudaSuccess) { cudaGetLastError(); return DRD_ERR_CUDA; }
+    return DRD_OK;
+}
+
 int drd_flush_l2(drd_ctx* c, int64_t bytes) {
     if (!c || bytes < 0) return DRD_ERR_BADARG;
     static thread_local void* buf = nullptr;

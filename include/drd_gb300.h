@@ -602,6 +602,12 @@ int drd_kernel_bench(drd_ctx* ctx, int which, int reps, double* us_per_launch, d
 /* Writes `bytes` of scratch memory on the context stream (evicts L2 between timed steps). */
 int drd_flush_l2(drd_ctx* ctx, int64_t bytes);
 
+/* Page-locks `bytes` of the caller's host memory at p (cudaHostRegister) so that the per-routine
+ * calls copy to and from it by DMA; a driver that registers its module arrays once after
+ * allocating them makes every later call's copies faster.  Unregister before freeing. */
+int drd_host_register(void* p, int64_t bytes);
+int drd_host_unregister(void* p);
+
 /* 1 when the mixed mode runs each whole CH and momentum solve (the FP64 refinement and its
  * FP32 iterations) as one persistent cooperative launch with grid-wide barriers between the
  * phases of an iteration; 0 when it runs the captured kernel-per-phase loop (no cooperative
