@@ -1124,6 +1124,19 @@ int refresh_fp32(drd_ctx* c) {
 // (1400x600) and 0.42 (2048x1024) the FP64 refinement stalls or diverges.  Above 0.1 the mixed
 // mode solves the CH system with the FP64 solver.
 constexpr double kChStiffLimit = 0.1;
+// With the solid-blended preconditioner the FP32 inner solves of a stiffer system still converge
+// (2048x1024, estimate 0.42: 269-296 iterations to the FP64 residual 1e-8 where PSolve_CG's
+// diverged), so the limit is raised while weights are installed.
+constexpr double kChStiffLimitBlend = 1.0;
+// Whether the mixed mode solves the CH system with the FP64 solver: the stiffness estimate
+// against the limit for the preconditioner in use (DRD_CH_STIFF_LIMIT in the environment
+// replaces both limits).
+void update_ch_mode(drd_ctx* c) {
+    const char* sl = std::getenv("DRD_CH_STIFF_LIMIT");
+    const double lim = sl ? std::atof(sl) : (c->pc_on ? kChStiffLimitBlend : kChStiffLimit);
+    c->ch_fp64 = c->ch_stiff > lim;
+}
+
 double ch_stiffness(const drd_ctx* c, const std::vector<double>& ph_lcc) {
     double lmax = 0.0;
     for (double v : ph_lcc) lmax = std::max(lmax, v);
@@ -1134,7 +1147,7 @@ int upload_tables(drd_ctx* c) {
     std::vector<double> ph, pre;
     host_tables(c->P, ph, pre);
     c->ch_stiff = ch_stiffness(c, ph);
-    c->ch_fp64 = c->ch_stiff > kChStiffLimit;
+    update_ch_mode(c);
     CK(cudaMemcpy(c->ph_lcc, ph.data(), sizeof(double) * ph.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->pre_lcc, pre.data(), sizeof(double) * pre.size(), cudaMemcpyHostToDevice));
     launch_convert_scale<float, double>(c->nc, c->ph_lcc, 1.0, c->ph_lcc32, nullptr, c->s);
@@ -1507,6 +1520,7 @@ int drd_set_coefs(drd_ctx* c, const double* rho, const double* eta, const double
     // blend weights belong to the mobilities they were fitted for
     if ((ph_M_0 || ph_M_inner) && c->pc_on) {
         c->pc_on = 0;
+        update_ch_mode(c);
         clear_graphs(c);
     }
     // MF penalises with bdr_ph itself (VeloSolve_2_combined.f90:580); TP keeps its own mask
@@ -1532,6 +1546,7 @@ int pc_alloc(drd_ctx* c) {
 void pc_switch(drd_ctx* c, int on) {
     if (c->pc_on == on) return;
     c->pc_on = on;
+    update_ch_mode(c);
     clear_graphs(c);
 }
 

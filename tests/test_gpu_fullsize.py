@@ -90,6 +90,28 @@ def test_c5_mixed_step_solves_ch_in_fp64_and_conserves_mass(cuda_lib):
     ctx.close()
 
 
+def test_c5_mixed_step_with_blend_solves_ch_in_fp32(cuda_lib):
+    """The same step with the probe-fitted blend in the CH preconditioner and the scaled ESOLP_x:
+    with the blend the FP32 inner CH solves converge at this stiffness (the library raises the
+    limit while weights are installed), and both solves reach the FP64 tolerance that PSolve_CG
+    alone does not reach within the reference's 500 iterations."""
+    case = make_case("c5", seed=0, precision=abi.DRD_PREC_MIXED, uv_precond=abi.DRD_UV_ESOLP_SCALED)
+    ctx = DRDContext(case.params)
+    ctx.set_case(case)
+    ctx.ch_blend_probe(64, 11, install=True)
+    ctx.upload_state(case.state)
+    m0 = ctx.mass(case.state[F.F_PH])
+    st = ctx.step(True, 0.0)
+    assert not (st.ch.flags & F.DRD_FLAG_FALLBACK64)
+    assert st.ch.info == 0 and st.ch.true_resid <= case.params.tol, st.ch.as_dict()
+    assert st.uv.info == 0 and st.uv.true_resid <= case.params.tol, st.uv.as_dict()
+    assert abs(st.mass - m0) / m0 < 1e-6
+    ctx.set_ch_blend(None)  # without weights the stiffness rule sends it back to the FP64 solver
+    st2 = ctx.step(False, case.params.dt)
+    assert st2.ch.flags & F.DRD_FLAG_FALLBACK64
+    ctx.close()
+
+
 @pytest.mark.parametrize("precision", [abi.DRD_PREC_FP64, abi.DRD_PREC_MIXED])
 def test_c1_steps_match_oracle(cuda_lib, oracle_build, precision):
     """The C1 configuration at its own size (128x64, one drop, no solid, tol 1e-10): five
