@@ -40,9 +40,10 @@ sys.path.insert(0, ROOT)
 METRIC = "time-steps/s and solves/s to FP64 resid 1e-8: learned+FP32 vs plain FP64, 1 GB300"
 # DRAM bytes (read + write) of one launch of the persistent CH solve kernel, from an ncu capture
 # of this workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch)
-TRAFFIC_CH = 4347648 + 264704
-# the same for one launch of the persistent momentum solve kernel with ESOLP_x (the same capture)
-TRAFFIC_UV = 8218624 + 1832960
+TRAFFIC_CH = 4348160 + 304640
+# the same for one launch of the persistent momentum solve kernel with the scaled ESOLP_x (the
+# same capture)
+TRAFFIC_UV = 8695808 + 1454592
 # relative residual reduction of each FP32 inner solve in the mixed mode's FP64 refinement (every
 # mixed leg of the GPU arm)
 INNER_TOL = 0.1
