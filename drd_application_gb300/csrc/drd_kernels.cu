@@ -1363,6 +1363,259 @@ static const GemmCfg kGemmCfgs[] = {{"64x64x16/4x4"},         {"32x64x16/2x4"}, 
 
 // Configurations 9-13 are the double-float kernels: FP64 only.  The small tiles give the
 // unfolded pressure passes at 420x180 four to eight times the blocks of 32x64 tiles.
+// ---- the transform GEMM on the fifth-generation tensor cores (FP32 data, 3xTF32) -------------
+// C = A B for the folded DCT passes (FOLD_A or FOLD_B, epilogue EPI_STORE or EPI_DIV_TAB): a
+// 128 x 128 output tile per CTA, K in chunks of 32.  Each operand is split into high and low
+// TF32 parts as it is staged (x = hi + lo, both rounded to TF32), and every K step issues
+// tcgen05.mma kind::tf32 three times into one FP32 accumulator in TMEM: lo(A) hi(B),
+// hi(A) lo(B), hi(A) hi(B), the products of FP32 operands up to the lo lo term.  One thread
+// issues the MMAs; the operands are in shared memory in the K-major, unswizzled core-matrix
+// layout (8 rows x 16 bytes, i.e. 4 TF32 values); two stages alternate, tracked by mbarriers
+// that tcgen05.commit arrives on.  Waits are bounded: a wait that gives up sets *err and the
+// tile's outputs are written as NaN, which the solve's FP64 residual then reports.
+constexpr int kGtcThreads = 512;  // 16 warps: all stage; warp w reads TMEM lanes 32 (w % 4), columns 32 (w / 4)
+constexpr int kGtcM = 128, kGtcN = 128, kGtcK = 32;
+constexpr uint32_t kGtcOp = kGtcM * kGtcK * 4;        // bytes of one operand part (hi or lo), 16 KB
+constexpr uint32_t kGtcStage = 4 * kGtcOp;            // A hi, A lo, B hi, B lo
+constexpr int kGtcSmem = 2 * kGtcStage + 1024;        // two stages, 1 KB for alignment
+constexpr int kGtcSpin = 1 << 22;
+
+__device__ __forceinline__ uint64_t gtc_desc(uint32_t addr) {
+    // start >> 4; leading byte offset (K-direction core stride, 16 rows of cores x 128 B = 2048)
+    // >> 4; stride byte offset (8-row group stride, 128) >> 4; descriptor version 1; no swizzle
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((2048u >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((128u >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+__device__ __forceinline__ bool gtc_wait(uint32_t bar, uint32_t parity) {
+    for (int it = 0; it < kGtcSpin; ++it) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ float gtc_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+// byte offset of element (row r, k) of a 128-row K-major operand part
+__device__ __forceinline__ uint32_t gtc_off(int r, int k) {
+    return (uint32_t)((k >> 2) * 2048 + (r >> 3) * 128 + (r & 7) * 16 + (k & 3) * 4);
+}
+__device__ __forceinline__ void gtc_put4(unsigned char* hi, unsigned char* lo, int r, int kg, const float (&v)[4]) {
+    float4 h, l;
+    h.x = gtc_tf32(v[0]); l.x = gtc_tf32(v[0] - h.x);
+    h.y = gtc_tf32(v[1]); l.y = gtc_tf32(v[1] - h.y);
+    h.z = gtc_tf32(v[2]); l.z = gtc_tf32(v[2] - h.z);
+    h.w = gtc_tf32(v[3]); l.w = gtc_tf32(v[3] - h.w);
+    const uint32_t o = gtc_off(r, 4 * kg);
+    *reinterpret_cast<float4*>(hi + o) = h;
+    *reinterpret_cast<float4*>(lo + o) = l;
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(kGtcThreads) k_gemm_tc(GemmArgs<float> a) {
+    extern __shared__ __align__(1024) unsigned char gsm_raw[];
+    __shared__ uint32_t tmem_base;
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ int bad;
+    count_launch(a.ctr);
+    if (gate_closed(a.ks, a.gate)) return;
+    const GemmView<float> g(a, a.fold ? (int)blockIdx.z : 0);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * kGtcM, n0 = blockIdx.x * kGtcN;
+    if (m0 >= g.M || n0 >= g.N) return;
+    unsigned char* gsm = gsm_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(gsm_raw) & 1023u)) & 1023u);
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(gsm);
+    if (warp == 0) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tmem_base);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(128) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 2; ++i) {
+            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[i]);
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        bad = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tbase = tmem_base;
+    // D F32, A TF32, B TF32, both K-major, N = 128, M = 128
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kGtcN >> 3) << 17) | ((uint32_t)(kGtcM >> 4) << 24);
+    const int K = a.K, nchunks = (K + kGtcK - 1) / kGtcK;
+    const int L = a.Lf;
+    // float4 loads of A: 16-byte aligned rows, and for FOLD_A mirrored groups that start on a
+    // multiple of 4 as well (row length L + 1 a multiple of 4)
+    const bool a_vec = (a.lda % 4 == 0) && ((reinterpret_cast<uintptr_t>(g.A) & 15) == 0) &&
+                       (a.fold != FOLD_A || (L + 1) % 4 == 0);
+    for (int c = 0; c < nchunks; ++c) {
+        const int st = c & 1, k0 = c * kGtcK;
+        unsigned char* sA = gsm + st * kGtcStage;
+        unsigned char* sB = sA + 2 * kGtcOp;
+        if (c >= 2) {  // the MMAs of chunk c - 2 read this stage
+            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[st]);
+            if (tid == 0 && !bad && !gtc_wait(mb, (uint32_t)(((c - 2) >> 1) & 1))) {
+                bad = 1;
+                if (a.err) atomicExch(a.err, 1);
+            }
+            __syncthreads();
+        }
+        if (bad) break;
+        // A and B: 128 rows / columns x 8 groups of 4 K values each, two (row, group) items of
+        // each operand per thread (row = item % 128, so a warp's float4 stores are contiguous);
+        // every load of the chunk is issued before any value is split and stored
+        {
+            constexpr int NI = kGtcM * (kGtcK / 4) / kGtcThreads;  // items per operand per thread
+            float va[NI][4], vb[NI][4];
+#pragma unroll
+            for (int it = 0; it < NI; ++it) {
+                const int item = tid + it * kGtcThreads, r = item % kGtcM, kg = item / kGtcM;
+                const int m = m0 + r, n = n0 + r, kb = k0 + 4 * kg;
+                // A as float4 (and its mirrored half, reversed) where a whole group lies before
+                // the middle of the fold and the rows are 16-byte aligned
+                if (a_vec && m < g.M && kb + 3 < K && (a.fold != FOLD_A || 2 * (kb + 3) < L)) {
+                    const float* row = g.A + (long)m * a.lda;
+                    const float4 x0 = *reinterpret_cast<const float4*>(row + kb);
+                    if (a.fold == FOLD_A) {
+                        const float4 x1 = *reinterpret_cast<const float4*>(row + L - kb - 3);
+                        const float sg = g.par ? -1.f : 1.f;
+                        va[it][0] = fmaf(sg, x1.w, x0.x);
+                        va[it][1] = fmaf(sg, x1.z, x0.y);
+                        va[it][2] = fmaf(sg, x1.y, x0.z);
+                        va[it][3] = fmaf(sg, x1.x, x0.w);
+                    } else {
+                        va[it][0] = x0.x; va[it][1] = x0.y; va[it][2] = x0.z; va[it][3] = x0.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int k = kb + j;
+                        float x = 0.f;
+                        if (m < g.M && k < K) {
+                            if (a.fold == FOLD_A) {
+                                const float* row = g.A + (long)m * a.lda;
+                                const float x0 = row[k], x1 = (2 * k == L) ? 0.f : row[L - k];
+                                x = (2 * k == L) ? (g.par ? 0.f : x0) : (g.par ? x0 - x1 : x0 + x1);
+                            } else {
+                                x = g.A[(long)m * a.lda + k];
+                            }
+                        }
+                        va[it][j] = x;
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int k = kb + j;
+                    float y = 0.f;
+                    if (n < g.N && k < K) {
+                        if (a.fold == FOLD_B) {
+                            const float y0 = g.B[(long)k * a.ldb + n];
+                            const float y1 = (2 * k == L) ? 0.f : g.B[(long)(L - k) * a.ldb + n];
+                            y = (2 * k == L) ? (g.par ? 0.f : y0) : (g.par ? y0 - y1 : y0 + y1);
+                        } else {
+                            y = g.B[(long)k * a.ldb + n];
+                        }
+                    }
+                    vb[it][j] = y;
+                }
+            }
+#pragma unroll
+            for (int it = 0; it < NI; ++it) {
+                const int item = tid + it * kGtcThreads, r = item % kGtcM, kg = item / kGtcM;
+                gtc_put4(sA, sA + kGtcOp, r, kg, va[it]);
+                gtc_put4(sB, sB + kGtcOp, r, kg, vb[it]);
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t aH = sbase + st * kGtcStage, aL = aH + kGtcOp, bH = aL + kGtcOp, bL = bH + kGtcOp;
+#pragma unroll
+            for (int t = 0; t < kGtcK / 8; ++t) {  // K = 8 per MMA: two core columns, 4096 bytes
+                const uint32_t off = (uint32_t)t * 4096u;
+                const uint64_t dAH = gtc_desc(aH + off), dAL = gtc_desc(aL + off);
+                const uint64_t dBH = gtc_desc(bH + off), dBL = gtc_desc(bL + off);
+                const uint32_t acc0 = (c > 0 || t > 0) ? 1u : 0u;
+                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+                             ::"r"(tbase), "l"(dAL), "l"(dBH), "r"(idesc), "r"(acc0) : "memory");
+                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+                             ::"r"(tbase), "l"(dAH), "l"(dBL), "r"(idesc), "r"(1u) : "memory");
+                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+                             ::"r"(tbase), "l"(dAH), "l"(dBH), "r"(idesc), "r"(1u) : "memory");
+            }
+            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[st]);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
+        }
+    }
+    // the last chunk's commit covers every MMA of the CTA; after a give-up, wait once more (also
+    // bounded) for what was issued before the TMEM is read or freed
+    if (tid == 0 && nchunks > 0) {
+        const int lc = bad ? -1 : nchunks - 1;
+        if (lc >= 0) {
+            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[lc & 1]);
+            if (!gtc_wait(mb, (uint32_t)((lc >> 1) & 1))) {
+                bad = 1;
+                if (a.err) atomicExch(a.err, 1);
+            }
+        } else {
+            for (int i = 0; i < 2; ++i) {
+                const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[i]);
+                gtc_wait(mb, 0u);
+                gtc_wait(mb, 1u);
+            }
+        }
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool poison = bad != 0;
+    const int q = warp & 3, cq = warp >> 2;  // TMEM lane quarter, column quarter
+    const int m = m0 + 32 * q + lane;
+#pragma unroll 1
+    for (int col = 32 * cq; col < 32 * cq + 32; col += 16) {
+        uint32_t r[16];
+        const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)col;
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                     : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                       "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                     : "r"(ta));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (m < g.M) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int n = n0 + col + j;
+                if (n < g.N) gemm_store<float, EPI>(a, g.orow(a, m), g.ocol(a, n), poison ? __int_as_float(0x7fc00000) : __uint_as_float(r[j]), 0.0);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(128) : "memory");
+}
+
+static void gemm_tc_launch(int epi, const GemmArgs<float>& a, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_gemm_tc<EPI_STORE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtcSmem);
+        cudaFuncSetAttribute(k_gemm_tc<EPI_DIV_TAB>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtcSmem);
+        attr = true;
+    }
+    const int M = a.fold == FOLD_B ? (a.M > a.M_odd ? a.M : a.M_odd) : a.M;
+    const int N = a.fold == FOLD_A ? (a.N > a.N_odd ? a.N : a.N_odd) : a.N;
+    dim3 grid((N + kGtcN - 1) / kGtcN, (M + kGtcM - 1) / kGtcM, a.fold ? 2 : 1);
+    if (epi == EPI_DIV_TAB) k_gemm_tc<EPI_DIV_TAB><<<grid, kGtcThreads, kGtcSmem, s>>>(a);
+    else k_gemm_tc<EPI_STORE><<<grid, kGtcThreads, kGtcSmem, s>>>(a);
+}
+
 int gemm_config_count(int fp64) { return fp64 ? 14 : 9; }
 const char* gemm_config_name(int cfg) { return kGemmCfgs[cfg].name; }
 
@@ -1426,7 +1679,11 @@ void launch_gemm(int cfg, int epi, const GemmArgs<T>& a, cudaStream_t s) {
                 else if (cfg == 12) gemm_df_dispatch<16, 32, 1, 2>(epi, a, s);
                 else gemm_df_dispatch<16, 16, 1, 1>(epi, a, s);
             } else {
-                gemm_dispatch_epi<T, 64, 64, 4, 4>(epi, a, s);
+                // kGemmTcCfg: the tensor-core GEMM for the folded passes it covers
+                if (cfg == kGemmTcCfg && a.fold != FOLD_NONE && (epi == EPI_STORE || epi == EPI_DIV_TAB))
+                    gemm_tc_launch(epi, reinterpret_cast<const GemmArgs<float>&>(a), s);
+                else
+                    gemm_dispatch_epi<T, 64, 64, 4, 4>(epi, a, s);
             }
             break;
     }

@@ -48,9 +48,13 @@ struct GemmArgs {
     // matrices, M / M_odd their heights, output row 2m+p.  K is floor(L/2)+1.
     int fold; int Lf;
     const T* A_odd; const T* B_odd; int M_odd, N_odd;
+    int* err;  // the tensor-core GEMM: set when a wait gave up (may be null)
 };
 enum Fold : int { FOLD_NONE = 0, FOLD_A = 1, FOLD_B = 2 };
 int gemm_config_count(int fp64);
+// FP32 transform GEMM configuration that runs on the tensor cores (3xTF32 tcgen05); the FP32
+// autotuner times it beside the SIMT configurations [0, gemm_config_count(0)).
+constexpr int kGemmTcCfg = 14;
 const char* gemm_config_name(int cfg);
 template <typename T>
 void launch_gemm(int cfg, int epi, const GemmArgs<T>& a, cudaStream_t s);

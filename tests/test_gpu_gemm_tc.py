@@ -1,0 +1,54 @@
+"""The tensor-core transform GEMM (3xTF32 tcgen05, GEMM configuration kGemmTcCfg = 14) in the
+FP32 passes of the kernel-per-phase loop, forced with DRD_GEMM_CFG: the CH preconditioner
+(folded DCT-I passes along x and z, the division by Ph_Lcc in an epilogue) and ESOLP_x's row
+passes, against the oracle's FP64 operators at FP32 accuracy."""
+import os
+
+import numpy as np
+import pytest
+
+from drd_application_gb300 import abi
+from drd_application_gb300.api import DRDContext
+from oracle.oracle import Oracle
+from tests.helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+F = abi
+
+
+def _ctx(P):
+    os.environ["DRD_GEMM_CFG"] = "14"
+    try:
+        return DRDContext(P)
+    finally:
+        del os.environ["DRD_GEMM_CFG"]
+
+
+@pytest.mark.parametrize("nr,nz", [(97, 53), (420, 180), (512, 256)])
+def test_tc_ch_psolve_matches_oracle(cuda_lib, oracle_build, nr, nz):
+    P = abi.default_params(nr, nz)
+    P.dr, P.dz, P.dt = 3.5 / nr, 1.5 / nz, 1e-3
+    P.precision = F.DRD_PREC_MIXED
+    ctx, orc = _ctx(P), Oracle(P)
+    try:
+        x = np.random.default_rng(nr).standard_normal(nr * nz)
+        y = ctx.op_apply(F.DRD_OP_CH_PSOLVE, x, precision=F.DRD_PREC_MIXED)
+        assert np.isfinite(y).all()
+        assert rel_err(y, orc.ch_psolve(x)) < 2e-5, rel_err(y, orc.ch_psolve(x))
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("nr,nz", [(97, 53), (420, 180)])
+def test_tc_esolp_rows_match_oracle(cuda_lib, oracle_build, nr, nz):
+    P = abi.default_params(nr, nz)
+    P.dr, P.dz, P.dt = 3.5 / nr, 1.5 / nz, 1e-3
+    P.precision = F.DRD_PREC_MIXED
+    P.uv_precond = F.DRD_UV_ESOLP
+    ctx, orc = _ctx(P), Oracle(P)
+    try:
+        x = np.random.default_rng(nz).standard_normal(ctx.L.drd_op_length(ctx.h, F.DRD_OP_UV_PSOLVE))
+        y = ctx.op_apply(F.DRD_OP_UV_PSOLVE, x, bdf=2, precision=F.DRD_PREC_MIXED)
+        assert rel_err(y, orc.uv_psolve_esolp(2, x)) < 2e-5
+    finally:
+        ctx.close()
