@@ -7,7 +7,9 @@
 // left the state they belong to, so a fixed launch sequence (a captured CUDA graph) can
 // express BiCGSTAB's early exits.
 #include <cooperative_groups.h>
+#include <cuda.h>  // CUtensorMap and its enums (the encoder is fetched at run time)
 #include <math.h>
+#include <cstdlib>
 
 #include "drd_kernels.cuh"
 #include "drd_ops.cuh"
@@ -1377,7 +1379,8 @@ constexpr int kGtcThreads = 512;  // 16 warps: all stage; warp w reads TMEM lane
 constexpr int kGtcM = 128, kGtcN = 128, kGtcK = 32;
 constexpr uint32_t kGtcOp = kGtcM * kGtcK * 4;        // bytes of one operand part (hi or lo), 16 KB
 constexpr uint32_t kGtcStage = 4 * kGtcOp;            // A hi, A lo, B hi, B lo
-constexpr int kGtcSmem = 2 * kGtcStage + 1024;        // two stages, 1 KB for alignment
+constexpr int kGtcStages = 3;
+constexpr int kGtcSmem = kGtcStages * kGtcStage + 1024;  // three stages, 1 KB for alignment
 constexpr int kGtcSpin = 1 << 22;
 
 __device__ __forceinline__ uint64_t gtc_desc(uint32_t addr) {
@@ -1415,169 +1418,108 @@ __device__ __forceinline__ void gtc_put4(unsigned char* hi, unsigned char* lo, i
     *reinterpret_cast<float4*>(lo + o) = l;
 }
 
-template <int EPI>
-__global__ void __launch_bounds__(kGtcThreads) k_gemm_tc(GemmArgs<float> a) {
-    extern __shared__ __align__(1024) unsigned char gsm_raw[];
-    __shared__ uint32_t tmem_base;
-    __shared__ __align__(8) uint64_t mbar[2];
-    __shared__ int bad;
-    count_launch(a.ctr);
-    if (gate_closed(a.ks, a.gate)) return;
-    const GemmView<float> g(a, a.fold ? (int)blockIdx.z : 0);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int m0 = blockIdx.y * kGtcM, n0 = blockIdx.x * kGtcN;
-    if (m0 >= g.M || n0 >= g.N) return;
-    unsigned char* gsm = gsm_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(gsm_raw) & 1023u)) & 1023u);
-    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(gsm);
-    if (warp == 0) {
-        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tmem_base);
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(128) : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    if (tid == 0) {
-        for (int i = 0; i < 2; ++i) {
-            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[i]);
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
-        }
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        bad = 0;
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t tbase = tmem_base;
-    // D F32, A TF32, B TF32, both K-major, N = 128, M = 128
-    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kGtcN >> 3) << 17) | ((uint32_t)(kGtcM >> 4) << 24);
-    const int K = a.K, nchunks = (K + kGtcK - 1) / kGtcK;
-    const int L = a.Lf;
-    // float4 loads of A: 16-byte aligned rows, and for FOLD_A mirrored groups that start on a
-    // multiple of 4 as well (row length L + 1 a multiple of 4)
-    const bool a_vec = (a.lda % 4 == 0) && ((reinterpret_cast<uintptr_t>(g.A) & 15) == 0) &&
-                       (a.fold != FOLD_A || (L + 1) % 4 == 0);
-    for (int c = 0; c < nchunks; ++c) {
-        const int st = c & 1, k0 = c * kGtcK;
-        unsigned char* sA = gsm + st * kGtcStage;
-        unsigned char* sB = sA + 2 * kGtcOp;
-        if (c >= 2) {  // the MMAs of chunk c - 2 read this stage
-            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[st]);
-            if (tid == 0 && !bad && !gtc_wait(mb, (uint32_t)(((c - 2) >> 1) & 1))) {
-                bad = 1;
-                if (a.err) atomicExch(a.err, 1);
-            }
-            __syncthreads();
-        }
-        if (bad) break;
-        // A and B: 128 rows / columns x 8 groups of 4 K values each, two (row, group) items of
-        // each operand per thread (row = item % 128, so a warp's float4 stores are contiguous);
-        // every load of the chunk is issued before any value is split and stored
-        {
-            constexpr int NI = kGtcM * (kGtcK / 4) / kGtcThreads;  // items per operand per thread
-            float va[NI][4], vb[NI][4];
+// Loads chunk k0 of the data operand(s) of the tensor-core GEMM into registers: 128 rows /
+// columns x 8 groups of 4 K values, GTC_NI (row, group) items of each operand per thread
+// (row = item % 128, so a warp's later float4 stores are contiguous).  The packed constant
+// operand is skipped (its values stay 0).
+constexpr int GTC_NI = kGtcM * (kGtcK / 4) / kGtcThreads;
+__device__ __forceinline__ void gtc_load(const GemmArgs<float>& a, const GemmView<float>& g, bool pk, bool const_b,
+                                         bool a_vec, int m0, int n0, int k0, float (&va)[GTC_NI][4],
+                                         float (&vb)[GTC_NI][4]) {
+    const int tid = threadIdx.x, K = a.K, L = a.Lf;
 #pragma unroll
-            for (int it = 0; it < NI; ++it) {
-                const int item = tid + it * kGtcThreads, r = item % kGtcM, kg = item / kGtcM;
-                const int m = m0 + r, n = n0 + r, kb = k0 + 4 * kg;
-                // A as float4 (and its mirrored half, reversed) where a whole group lies before
-                // the middle of the fold and the rows are 16-byte aligned
-                if (a_vec && m < g.M && kb + 3 < K && (a.fold != FOLD_A || 2 * (kb + 3) < L)) {
-                    const float* row = g.A + (long)m * a.lda;
-                    const float4 x0 = *reinterpret_cast<const float4*>(row + kb);
-                    if (a.fold == FOLD_A) {
-                        const float4 x1 = *reinterpret_cast<const float4*>(row + L - kb - 3);
-                        const float sg = g.par ? -1.f : 1.f;
-                        va[it][0] = fmaf(sg, x1.w, x0.x);
-                        va[it][1] = fmaf(sg, x1.z, x0.y);
-                        va[it][2] = fmaf(sg, x1.y, x0.z);
-                        va[it][3] = fmaf(sg, x1.x, x0.w);
-                    } else {
-                        va[it][0] = x0.x; va[it][1] = x0.y; va[it][2] = x0.z; va[it][3] = x0.w;
-                    }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const int k = kb + j;
-                        float x = 0.f;
-                        if (m < g.M && k < K) {
-                            if (a.fold == FOLD_A) {
-                                const float* row = g.A + (long)m * a.lda;
-                                const float x0 = row[k], x1 = (2 * k == L) ? 0.f : row[L - k];
-                                x = (2 * k == L) ? (g.par ? 0.f : x0) : (g.par ? x0 - x1 : x0 + x1);
-                            } else {
-                                x = g.A[(long)m * a.lda + k];
-                            }
-                        }
-                        va[it][j] = x;
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int k = kb + j;
-                    float y = 0.f;
-                    if (n < g.N && k < K) {
-                        if (a.fold == FOLD_B) {
-                            const float y0 = g.B[(long)k * a.ldb + n];
-                            const float y1 = (2 * k == L) ? 0.f : g.B[(long)(L - k) * a.ldb + n];
-                            y = (2 * k == L) ? (g.par ? 0.f : y0) : (g.par ? y0 - y1 : y0 + y1);
-                        } else {
-                            y = g.B[(long)k * a.ldb + n];
-                        }
-                    }
-                    vb[it][j] = y;
-                }
-            }
-#pragma unroll
-            for (int it = 0; it < NI; ++it) {
-                const int item = tid + it * kGtcThreads, r = item % kGtcM, kg = item / kGtcM;
-                gtc_put4(sA, sA + kGtcOp, r, kg, va[it]);
-                gtc_put4(sB, sB + kGtcOp, r, kg, vb[it]);
-            }
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t aH = sbase + st * kGtcStage, aL = aH + kGtcOp, bH = aL + kGtcOp, bL = bH + kGtcOp;
-#pragma unroll
-            for (int t = 0; t < kGtcK / 8; ++t) {  // K = 8 per MMA: two core columns, 4096 bytes
-                const uint32_t off = (uint32_t)t * 4096u;
-                const uint64_t dAH = gtc_desc(aH + off), dAL = gtc_desc(aL + off);
-                const uint64_t dBH = gtc_desc(bH + off), dBL = gtc_desc(bL + off);
-                const uint32_t acc0 = (c > 0 || t > 0) ? 1u : 0u;
-                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
-                             ::"r"(tbase), "l"(dAL), "l"(dBH), "r"(idesc), "r"(acc0) : "memory");
-                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
-                             ::"r"(tbase), "l"(dAH), "l"(dBL), "r"(idesc), "r"(1u) : "memory");
-                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
-                             ::"r"(tbase), "l"(dAH), "l"(dBH), "r"(idesc), "r"(1u) : "memory");
-            }
-            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[st]);
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
-        }
-    }
-    // the last chunk's commit covers every MMA of the CTA; after a give-up, wait once more (also
-    // bounded) for what was issued before the TMEM is read or freed
-    if (tid == 0 && nchunks > 0) {
-        const int lc = bad ? -1 : nchunks - 1;
-        if (lc >= 0) {
-            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[lc & 1]);
-            if (!gtc_wait(mb, (uint32_t)((lc >> 1) & 1))) {
-                bad = 1;
-                if (a.err) atomicExch(a.err, 1);
+    for (int it = 0; it < GTC_NI; ++it) {
+        const int item = tid + it * kGtcThreads, r = item % kGtcM, kg = item / kGtcM;
+        const int m = m0 + r, n = n0 + r, kb = k0 + 4 * kg, kbb = kb;
+        // A as float4 (and its mirrored half, reversed) where a whole group lies before the
+        // middle of the fold and the rows are 16-byte aligned
+        if (pk && !const_b) {
+            va[it][0] = va[it][1] = va[it][2] = va[it][3] = 0.f;  // A comes packed
+        } else if (a_vec && m < g.M && kb + 3 < K && (a.fold != FOLD_A || 2 * (kb + 3) < L)) {
+            const float* row = g.A + (long)m * a.lda;
+            const float4 x0 = *reinterpret_cast<const float4*>(row + kb);
+            if (a.fold == FOLD_A) {
+                const float4 x1 = *reinterpret_cast<const float4*>(row + L - kb - 3);
+                const float sg = g.par ? -1.f : 1.f;
+                va[it][0] = fmaf(sg, x1.w, x0.x);
+                va[it][1] = fmaf(sg, x1.z, x0.y);
+                va[it][2] = fmaf(sg, x1.y, x0.z);
+                va[it][3] = fmaf(sg, x1.x, x0.w);
+            } else {
+                va[it][0] = x0.x; va[it][1] = x0.y; va[it][2] = x0.z; va[it][3] = x0.w;
             }
         } else {
-            for (int i = 0; i < 2; ++i) {
-                const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[i]);
-                gtc_wait(mb, 0u);
-                gtc_wait(mb, 1u);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int k = kb + j;
+                float x = 0.f;
+                if (m < g.M && k < K) {
+                    if (a.fold == FOLD_A) {
+                        const float* row = g.A + (long)m * a.lda;
+                        const float x0 = row[k], x1 = (2 * k == L) ? 0.f : row[L - k];
+                        x = (2 * k == L) ? (g.par ? 0.f : x0) : (g.par ? x0 - x1 : x0 + x1);
+                    } else {
+                        x = g.A[(long)m * a.lda + k];
+                    }
+                }
+                va[it][j] = x;
             }
         }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int k = kbb + j;
+            float y = 0.f;
+            if (!(pk && const_b) && n < g.N && k < K) {
+                if (a.fold == FOLD_B) {
+                    const float y0 = g.B[(long)k * a.ldb + n];
+                    const float y1 = (2 * k == L) ? 0.f : g.B[(long)(L - k) * a.ldb + n];
+                    y = (2 * k == L) ? (g.par ? 0.f : y0) : (g.par ? y0 - y1 : y0 + y1);
+                } else {
+                    y = g.B[(long)k * a.ldb + n];
+                }
+            }
+            vb[it][j] = y;
+        }
     }
-    __syncthreads();
+}
+
+// One packed block per (parity, 128-row tile, 32-K chunk): hi part then lo part, each in the
+// core-matrix layout of gtc_off, zeros past the matrix.
+__global__ void k_gtc_pack(const float* __restrict__ ev, const float* __restrict__ od, int re, int ro, int K, long ld,
+                           int b_style, int tiles, int chunks, float* __restrict__ out) {
+    const long tot = 2L * tiles * chunks * (kGtcM * kGtcK);
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tot; e += (long)gridDim.x * blockDim.x) {
+        const int kl = (int)(e % kGtcK), rl = (int)((e / kGtcK) % kGtcM);
+        const long blk = e / (kGtcM * kGtcK);
+        const int ch = (int)(blk % chunks), tl = (int)((blk / chunks) % tiles), par = (int)(blk / ((long)chunks * tiles));
+        const int r = tl * kGtcM + rl, k = ch * kGtcK + kl;
+        const float* src = par ? od : ev;
+        const int rows = par ? ro : re;
+        float x = 0.f;
+        if (r < rows && k < K) x = b_style ? src[(long)k * ld + r] : src[(long)r * ld + k];
+        const float hi = gtc_tf32(x), lo = gtc_tf32(x - hi);
+        float* base = out + blk * (2 * kGtcM * kGtcK);
+        const uint32_t o = gtc_off(rl, kl) / 4;
+        base[o] = hi;
+        base[kGtcM * kGtcK + o] = lo;
+    }
+}
+long gemm_tc_pack(const float* even, const float* odd, int rows_e, int rows_o, int K, long ld, int b_style,
+                  float* out, cudaStream_t s) {
+    const int rows = rows_e > rows_o ? rows_e : rows_o;
+    const int tiles = (rows + kGtcM - 1) / kGtcM, chunks = (K + kGtcK - 1) / kGtcK;
+    const long n = 2L * tiles * chunks * 2 * kGtcM * kGtcK;
+    if (out) k_gtc_pack<<<256, 256, 0, s>>>(even, odd, rows_e, rows_o, K, ld, b_style, tiles, chunks, out);
+    return n;
+}
+
+// Epilogue of the tensor-core GEMM: warp w reads TMEM lanes 32 (w % 4) (tile rows) and
+// columns 32 (w / 4) (tile columns), stores them (NaN when the tile gave up) and frees the TMEM.
+template <int EPI>
+__device__ __forceinline__ void gtc_epilogue(const GemmArgs<float>& a, const GemmView<float>& g, uint32_t tbase, int m0,
+                                             int n0, bool poison) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const bool poison = bad != 0;
     const int q = warp & 3, cq = warp >> 2;  // TMEM lane quarter, column quarter
     const int m = m0 + 32 * q + lane;
 #pragma unroll 1
@@ -1602,16 +1544,409 @@ __global__ void __launch_bounds__(kGtcThreads) k_gemm_tc(GemmArgs<float> a) {
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(128) : "memory");
 }
 
+// The twelve MMAs of one 32-K chunk from operand stage `stage` (A hi, A lo, B hi, B lo):
+// per K = 8 step lo(A) hi(B), hi(A) lo(B), hi(A) hi(B); the first of the tile overwrites D.
+__device__ __forceinline__ void gtc_mma_chunk(uint32_t stage, uint32_t tbase, uint32_t idesc, bool first) {
+    const uint32_t aH = stage, aL = aH + kGtcOp, bH = aL + kGtcOp, bL = bH + kGtcOp;
+#pragma unroll
+    for (int t = 0; t < kGtcK / 8; ++t) {  // K = 8 per MMA: two core columns, 4096 bytes
+        const uint32_t off = (uint32_t)t * 4096u;
+        const uint64_t dAH = gtc_desc(aH + off), dAL = gtc_desc(aL + off);
+        const uint64_t dBH = gtc_desc(bH + off), dBL = gtc_desc(bL + off);
+        const uint32_t acc0 = (!first || t > 0) ? 1u : 0u;
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+                     ::"r"(tbase), "l"(dAL), "l"(dBH), "r"(idesc), "r"(acc0) : "memory");
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+                     ::"r"(tbase), "l"(dAH), "l"(dBL), "r"(idesc), "r"(1u) : "memory");
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+                     ::"r"(tbase), "l"(dAH), "l"(dBH), "r"(idesc), "r"(1u) : "memory");
+    }
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(kGtcThreads) k_gemm_tc(GemmArgs<float> a) {
+    extern __shared__ __align__(1024) unsigned char gsm_raw[];
+    __shared__ uint32_t tmem_base;
+    __shared__ __align__(8) uint64_t mbar[kGtcStages];
+    __shared__ __align__(8) uint64_t lbar[kGtcStages];  // bulk copies of the packed constant operand
+    __shared__ int bad;
+    count_launch(a.ctr);
+    if (gate_closed(a.ks, a.gate)) return;
+    const GemmView<float> g(a, a.fold ? (int)blockIdx.z : 0);
+    const bool pk = a.packed != nullptr;  // the constant operand comes packed (B of FOLD_A, A of FOLD_B)
+    const bool const_b = a.fold == FOLD_A;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.y * kGtcM, n0 = blockIdx.x * kGtcN;
+    if (m0 >= g.M || n0 >= g.N) return;
+    unsigned char* gsm = gsm_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(gsm_raw) & 1023u)) & 1023u);
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(gsm);
+    if (warp == 0) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tmem_base);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(128) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < kGtcStages; ++i) {
+            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[i]);
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+            const uint32_t lb = (uint32_t)__cvta_generic_to_shared(&lbar[i]);
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(lb) : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        bad = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tbase = tmem_base;
+    const int ctile = const_b ? (int)blockIdx.x : (int)blockIdx.y;  // the packed operand's row tile
+    // D F32, A TF32, B TF32, both K-major, N = 128, M = 128
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kGtcN >> 3) << 17) | ((uint32_t)(kGtcM >> 4) << 24);
+    const int K = a.K, nchunks = (K + kGtcK - 1) / kGtcK;
+    const int L = a.Lf;
+    // float4 loads of A: 16-byte aligned rows, and for FOLD_A mirrored groups that start on a
+    // multiple of 4 as well (row length L + 1 a multiple of 4)
+    const bool a_vec = (a.lda % 4 == 0) && ((reinterpret_cast<uintptr_t>(g.A) & 15) == 0) &&
+                       (a.fold != FOLD_A || (L + 1) % 4 == 0);
+    // Pipeline over the K chunks, three stages (chunk c in stage c % 3).  Chunk c: store its data
+    // operand (loaded into registers during chunk c - 1) and issue chunk c + 1's loads; after the
+    // barrier thread 0 waits for chunk c's bulk copy (issued two chunks earlier), issues its
+    // MMAs, waits for chunk c - 1's MMAs and issues the bulk copy of chunk c + 2 into the stage
+    // they read.  Use k of stage s completes phase k of lbar[s] and of mbar[s].
+    auto bulk = [&](int cc) {  // thread 0: the packed constant operand of chunk cc
+        const int sc = cc % kGtcStages;
+        const uint32_t lb = (uint32_t)__cvta_generic_to_shared(&lbar[sc]);
+        const uint32_t dst = sbase + sc * kGtcStage + (const_b ? 2 * kGtcOp : 0);
+        const float* src = a.packed + ((long)(g.par * a.pk_tiles + ctile) * a.pk_chunks + cc) * (2 * kGtcM * kGtcK);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(lb), "r"(2u * kGtcOp) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(dst), "l"(src), "r"(2u * kGtcOp), "r"(lb) : "memory");
+    };
+    float cva[GTC_NI][4], cvb[GTC_NI][4];
+    if (nchunks > 0) gtc_load(a, g, pk, const_b, a_vec, m0, n0, 0, cva, cvb);
+    if (pk && tid == 0) {
+        for (int cc = 0; cc < 2 && cc < nchunks; ++cc) bulk(cc);
+    }
+    for (int c = 0; c < nchunks; ++c) {
+        const int st = c % kGtcStages, use = c / kGtcStages;
+        unsigned char* sA = gsm + st * kGtcStage;
+        unsigned char* sB = sA + 2 * kGtcOp;
+        __syncthreads();  // every thread reads the same `bad`; stage st is free (chunk c - 3 done)
+        if (bad) break;
+#pragma unroll
+        for (int it = 0; it < GTC_NI; ++it) {
+            const int item = tid + it * kGtcThreads, r = item % kGtcM, kg = item / kGtcM;
+            if (!(pk && !const_b)) gtc_put4(sA, sA + kGtcOp, r, kg, cva[it]);
+            if (!(pk && const_b)) gtc_put4(sB, sB + kGtcOp, r, kg, cvb[it]);
+        }
+        if (c + 1 < nchunks) gtc_load(a, g, pk, const_b, a_vec, m0, n0, (c + 1) * kGtcK, cva, cvb);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            if (pk) {  // the bulk copy of this chunk has landed
+                const uint32_t lb = (uint32_t)__cvta_generic_to_shared(&lbar[st]);
+                if (!bad && !gtc_wait(lb, (uint32_t)(use & 1))) {
+                    bad = 1;
+                    if (a.err) atomicExch(a.err, 1);
+                }
+            }
+            if (!bad) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                gtc_mma_chunk(sbase + st * kGtcStage, tbase, idesc, c == 0);
+                const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[st]);
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
+            }
+            // chunk c - 1's MMAs done: its stage takes chunk c + 2 (and, with chunk c - 2's, the
+            // next chunk's stores may overwrite stage (c + 1) % 3)
+            if (!bad && c >= 1) {
+                const int pc = c - 1;
+                const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[pc % kGtcStages]);
+                if (!gtc_wait(mb, (uint32_t)((pc / kGtcStages) & 1))) {
+                    bad = 1;
+                    if (a.err) atomicExch(a.err, 1);
+                }
+            }
+            if (!bad && pk && c + 2 < nchunks) bulk(c + 2);
+        }
+    }
+    // the last chunk's commit covers every MMA of the CTA; after a give-up, wait (bounded) for
+    // every stage's MMAs and bulk copy so that nothing still writes or reads the stages or TMEM
+    if (tid == 0 && nchunks > 0) {
+        if (!bad) {
+            const int lc = nchunks - 1;
+            const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[lc % kGtcStages]);
+            if (!gtc_wait(mb, (uint32_t)((lc / kGtcStages) & 1))) {
+                bad = 1;
+                if (a.err) atomicExch(a.err, 1);
+            }
+        }
+        if (bad) {
+            for (int i = 0; i < kGtcStages; ++i) {
+                const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[i]);
+                gtc_wait(mb, 0u);
+                gtc_wait(mb, 1u);
+                if (pk) {
+                    const uint32_t lb = (uint32_t)__cvta_generic_to_shared(&lbar[i]);
+                    gtc_wait(lb, 0u);
+                    gtc_wait(lb, 1u);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    gtc_epilogue<EPI>(a, g, tbase, m0, n0, bad != 0);
+}
+
+// The tensor-core GEMM with TMA staging of the data operand.  Per 32-K chunk the data tile and
+// its fold mirror arrive as two 16 KB boxes of a 2-D tensor map (cp.async.bulk.tensor, one
+// thread issues, an expect-tx mbarrier tracks them), three chunks ahead in a ring of raw
+// stages; the threads fold each (row, 4-K group) from shared memory, split it into TF32 high
+// and low parts and write the MMA operand stage (two stages).  FOLD_A: the boxes are 32 K x 128
+// rows of X at (k0, m0) and (L - k0 - 31, m0), 128-byte swizzled (16-byte chunk j of box row r
+// sits at chunk j ^ (r & 7)); FOLD_B: 128 columns x 32 K rows of X at (n0, k0) and
+// (n0, L - k0 - 31), unswizzled.  The constant operand comes packed (one bulk copy per chunk).
+constexpr int kGtrRaw = 3;                                  // raw stages
+constexpr uint32_t kGtrBox = kGtcM * kGtcK * 4;             // one box, 16 KB
+constexpr uint32_t kGtrRawStage = 2 * kGtrBox;              // the data box and its mirror
+constexpr int kGtrSmem = 2 * kGtcStage + kGtrRaw * kGtrRawStage + 1024;
+
+__device__ __forceinline__ void gtr_box(uint32_t dst, const CUtensorMap* tm, int x, int y, uint32_t bar) {
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+                 ::"r"(dst), "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar) : "memory");
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(kGtcThreads) k_gemm_tc_tma(GemmArgs<float> a, const __grid_constant__ CUtensorMap tm) {
+    extern __shared__ __align__(1024) unsigned char gsm_raw[];
+    __shared__ uint32_t tmem_base;
+    __shared__ __align__(8) uint64_t mbar[2];        // MMAs that read operand stage s are done
+    __shared__ __align__(8) uint64_t lbar[2];        // packed constant operand of stage s landed
+    __shared__ __align__(8) uint64_t rbar[kGtrRaw];  // data boxes of raw stage s landed
+    __shared__ int bad, raw_bad;                     // raw_bad: a wait for data boxes gave up
+    count_launch(a.ctr);
+    if (gate_closed(a.ks, a.gate)) return;
+    const GemmView<float> g(a, a.fold ? (int)blockIdx.z : 0);
+    const bool fa = a.fold == FOLD_A;
+    const int tid = threadIdx.x;
+    const int m0 = blockIdx.y * kGtcM, n0 = blockIdx.x * kGtcN;
+    if (m0 >= g.M || n0 >= g.N) return;
+    unsigned char* gsm = gsm_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(gsm_raw) & 1023u)) & 1023u);
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(gsm);
+    if ((threadIdx.x >> 5) == 0) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tmem_base);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(128) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 2; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&mbar[i])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&lbar[i])) : "memory");
+        }
+        for (int i = 0; i < kGtrRaw; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&rbar[i])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        bad = 0;
+        raw_bad = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tbase = tmem_base;
+    const int ctile = fa ? (int)blockIdx.x : (int)blockIdx.y;  // the packed operand's row tile
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kGtcN >> 3) << 17) | ((uint32_t)(kGtcM >> 4) << 24);
+    const int K = a.K, L = a.Lf, nchunks = (K + kGtcK - 1) / kGtcK;
+    const uint32_t raw0 = sbase + 2 * kGtcStage;
+    unsigned char* rawp = gsm + 2 * kGtcStage;
+    // thread 0's record of what is in flight: chunks [0, n_tma) have their boxes issued,
+    // [0, n_bulk) their packed operand, [0, n_mma) their MMAs committed; [0, w_bulk) and
+    // [0, w_mma) were waited for
+    int n_tma = 0, n_bulk = 0, n_mma = 0, w_bulk = 0, w_mma = 0;
+    auto issue_tma = [&](int cc) {
+        const int rs = cc % kGtrRaw;
+        const uint32_t rb = (uint32_t)__cvta_generic_to_shared(&rbar[rs]);
+        const uint32_t dst = raw0 + rs * kGtrRawStage;
+        const int k0 = cc * kGtcK, k1 = L - k0 - (kGtcK - 1);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(rb), "r"(kGtrRawStage) : "memory");
+        if (fa) {
+            gtr_box(dst, &tm, k0, m0, rb);
+            gtr_box(dst + kGtrBox, &tm, k1, m0, rb);
+        } else {
+            gtr_box(dst, &tm, n0, k0, rb);
+            gtr_box(dst + kGtrBox, &tm, n0, k1, rb);
+        }
+        n_tma = cc + 1;
+    };
+    auto issue_bulk = [&](int cc) {  // the packed constant operand of chunk cc into stage cc & 1
+        const int st = cc & 1;
+        const uint32_t lb = (uint32_t)__cvta_generic_to_shared(&lbar[st]);
+        const uint32_t dst = sbase + st * kGtcStage + (fa ? 2 * kGtcOp : 0);
+        const float* src = a.packed + ((long)(g.par * a.pk_tiles + ctile) * a.pk_chunks + cc) * (2 * kGtcM * kGtcK);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(lb), "r"(2u * kGtcOp) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(dst), "l"(src), "r"(2u * kGtcOp), "r"(lb) : "memory");
+        n_bulk = cc + 1;
+    };
+    auto fail = [&]() {
+        bad = 1;
+        if (a.err) atomicExch(a.err, 1);
+    };
+    if (tid == 0 && nchunks > 0) {
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tm)) : "memory");
+        for (int cc = 0; cc < kGtrRaw && cc < nchunks; ++cc) issue_tma(cc);
+        issue_bulk(0);
+    }
+    const float sg = g.par ? -1.f : 1.f;
+    int c = 0;
+    for (; c < nchunks; ++c) {
+        const int st = c & 1, rs = c % kGtrRaw;
+        __syncthreads();  // `bad` is the same for every thread; stage st's MMAs (chunk c - 2) are done
+        if (bad) break;
+        if (!gtc_wait((uint32_t)__cvta_generic_to_shared(&rbar[rs]), (uint32_t)((c / kGtrRaw) & 1))) {
+            raw_bad = 1;
+            fail();
+        }
+        const unsigned char* r0 = rawp + rs * kGtrRawStage;
+        const unsigned char* r1 = r0 + kGtrBox;
+        unsigned char* op = gsm + st * kGtcStage + (fa ? 0 : 2 * kGtcOp);
+        const int k0 = c * kGtcK;
+#pragma unroll
+        for (int it = 0; it < GTC_NI; ++it) {
+            const int item = tid + it * kGtcThreads, r = item % kGtcM, kg = item / kGtcM;
+            float v[4];
+            if (fa) {
+                const float4 x0 = *reinterpret_cast<const float4*>(r0 + r * 128 + ((kg ^ (r & 7)) << 4));
+                const float4 x1 = *reinterpret_cast<const float4*>(r1 + r * 128 + (((7 - kg) ^ (r & 7)) << 4));
+                const float a0[4] = {x0.x, x0.y, x0.z, x0.w}, a1[4] = {x1.w, x1.z, x1.y, x1.x};
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int k = k0 + 4 * kg + j;
+                    v[j] = (k >= K) ? 0.f : (2 * k == L) ? (g.par ? 0.f : a0[j]) : fmaf(sg, a1[j], a0[j]);
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int k = k0 + 4 * kg + j;
+                    const float y0 = *reinterpret_cast<const float*>(r0 + (4 * kg + j) * 512 + r * 4);
+                    const float y1 = *reinterpret_cast<const float*>(r1 + (kGtcK - 1 - 4 * kg - j) * 512 + r * 4);
+                    v[j] = (k >= K) ? 0.f : (2 * k == L) ? (g.par ? 0.f : y0) : fmaf(sg, y1, y0);
+                }
+            }
+            gtc_put4(op, op + kGtcOp, r, kg, v);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            if (!bad) {
+                if (gtc_wait((uint32_t)__cvta_generic_to_shared(&lbar[st]), (uint32_t)((c >> 1) & 1))) w_bulk = c + 1;
+                else fail();
+            }
+            if (!bad) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                gtc_mma_chunk(sbase + st * kGtcStage, tbase, idesc, c == 0);
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                             ::"r"((uint32_t)__cvta_generic_to_shared(&mbar[st])) : "memory");
+                n_mma = c + 1;
+            }
+            // every thread has read raw stage rs: it takes chunk c + 3
+            if (!bad && c + kGtrRaw < nchunks) issue_tma(c + kGtrRaw);
+            // chunk c - 1's MMAs done: its operand stage takes chunk c + 1
+            if (!bad && c >= 1) {
+                if (gtc_wait((uint32_t)__cvta_generic_to_shared(&mbar[st ^ 1]), (uint32_t)(((c - 1) >> 1) & 1))) w_mma = c;
+                else fail();
+            }
+            if (!bad && c + 1 < nchunks) issue_bulk(c + 1);
+        }
+    }
+    if (tid == 0 && nchunks > 0) {
+        if (!bad) {  // the last commit covers every MMA of the tile
+            const int lc = nchunks - 1;
+            if (gtc_wait((uint32_t)__cvta_generic_to_shared(&mbar[lc & 1]), (uint32_t)((lc >> 1) & 1))) w_mma = nchunks;
+            else fail();
+        }
+        if (bad) {
+            // drain (bounded, in issue order) what is still in flight, so that no copy lands in
+            // and no MMA reads this CTA's shared memory after it has exited: the boxes of the
+            // chunks not yet consumed (from the last one when its wait gave up: then no later
+            // chunk was issued into its stage), the packed operands and the MMAs not yet waited
+            // for.  Each of these is the oldest pending phase of its barrier.
+            const int cl = (raw_bad && c > 0) ? c - 1 : c;
+            for (int cc = cl; cc < n_tma; ++cc)
+                gtc_wait((uint32_t)__cvta_generic_to_shared(&rbar[cc % kGtrRaw]), (uint32_t)((cc / kGtrRaw) & 1));
+            for (int cc = w_bulk; cc < n_bulk; ++cc)
+                gtc_wait((uint32_t)__cvta_generic_to_shared(&lbar[cc & 1]), (uint32_t)((cc >> 1) & 1));
+            for (int cc = w_mma; cc < n_mma; ++cc)
+                gtc_wait((uint32_t)__cvta_generic_to_shared(&mbar[cc & 1]), (uint32_t)((cc >> 1) & 1));
+        }
+    }
+    __syncthreads();
+    gtc_epilogue<EPI>(a, g, tbase, m0, n0, bad != 0);
+}
+
+// cuTensorMapEncodeTiled, fetched from the driver once (no link against libcuda)
+typedef CUresult (*GtrEncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                                const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static GtrEncodeFn gtr_encoder() {
+    static GtrEncodeFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<GtrEncodeFn>(p);
+    }
+    return fn;
+}
+
+// The tensor map of the data operand for k_gemm_tc_tma, or false when the pass does not meet
+// TMA's alignment rules (16-byte base and row stride; for FOLD_A the mirror box's x = L - k0 - 31
+// must be a multiple of 4, i.e. L + 1 a multiple of 4) or has no packed constant operand.
+static bool gtr_map(const GemmArgs<float>& a, CUtensorMap* tm) {
+    if (!a.packed || (a.fold != FOLD_A && a.fold != FOLD_B) || a.Lf < 2 * kGtcK + 1) return false;
+    GtrEncodeFn enc = gtr_encoder();
+    if (!enc) return false;
+    const bool fa = a.fold == FOLD_A;
+    const float* X = fa ? a.A : a.B;
+    const long ld = fa ? a.lda : a.ldb;
+    if ((reinterpret_cast<uintptr_t>(X) & 15) || (ld % 4) || (fa && (a.Lf + 1) % 4)) return false;
+    cuuint64_t dim[2], stride[1] = {(cuuint64_t)ld * 4};
+    cuuint32_t box[2], es[2] = {1, 1};
+    if (fa) {  // X is M rows of L + 1 values
+        dim[0] = (cuuint64_t)a.Lf + 1; dim[1] = (cuuint64_t)a.M;
+        box[0] = kGtcK; box[1] = kGtcM;
+    } else {   // X is L + 1 rows of N values
+        dim[0] = (cuuint64_t)a.N; dim[1] = (cuuint64_t)a.Lf + 1;
+        box[0] = kGtcN; box[1] = kGtcK;
+    }
+    if ((long)dim[0] > ld) return false;
+    return enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(X), dim, stride, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, fa ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 static void gemm_tc_launch(int epi, const GemmArgs<float>& a, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(k_gemm_tc<EPI_STORE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtcSmem);
         cudaFuncSetAttribute(k_gemm_tc<EPI_DIV_TAB>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtcSmem);
+        cudaFuncSetAttribute(k_gemm_tc_tma<EPI_STORE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtrSmem);
+        cudaFuncSetAttribute(k_gemm_tc_tma<EPI_DIV_TAB>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtrSmem);
         attr = true;
     }
     const int M = a.fold == FOLD_B ? (a.M > a.M_odd ? a.M : a.M_odd) : a.M;
     const int N = a.fold == FOLD_A ? (a.N > a.N_odd ? a.N : a.N_odd) : a.N;
     dim3 grid((N + kGtcN - 1) / kGtcN, (M + kGtcM - 1) / kGtcM, a.fold ? 2 : 1);
+    alignas(64) CUtensorMap tm;
+    if (!std::getenv("DRD_GEMM_TC_NOTMA") && gtr_map(a, &tm)) {  // the variable selects the fallback (tests)
+        if (epi == EPI_DIV_TAB) k_gemm_tc_tma<EPI_DIV_TAB><<<grid, kGtcThreads, kGtrSmem, s>>>(a, tm);
+        else k_gemm_tc_tma<EPI_STORE><<<grid, kGtcThreads, kGtrSmem, s>>>(a, tm);
+        return;
+    }
     if (epi == EPI_DIV_TAB) k_gemm_tc<EPI_DIV_TAB><<<grid, kGtcThreads, kGtcSmem, s>>>(a);
     else k_gemm_tc<EPI_STORE><<<grid, kGtcThreads, kGtcSmem, s>>>(a);
 }

@@ -49,7 +49,18 @@ struct GemmArgs {
     int fold; int Lf;
     const T* A_odd; const T* B_odd; int M_odd, N_odd;
     int* err;  // the tensor-core GEMM: set when a wait gave up (may be null)
+    // the tensor-core GEMM: the constant operand (B of FOLD_A, A of FOLD_B) pre-split into TF32
+    // high and low parts and laid out as the CTA's 32 KB shared-memory blocks (gemm_tc_pack),
+    // brought in by one bulk copy per K chunk; null: staged by the threads like the data
+    const float* packed;
+    int pk_tiles, pk_chunks;
 };
+// Packs the constant operand of a folded transform for k_gemm_tc: rows r (its N for FOLD_A, its
+// M for FOLD_B) of the even and odd matrices, K values each; b_style: the matrices are K x rows
+// (B of FOLD_A, row stride ld), else rows x K (A of FOLD_B).  Returns the floats written, or the
+// floats needed when out is null.
+long gemm_tc_pack(const float* even, const float* odd, int rows_e, int rows_o, int K, long ld, int b_style,
+                  float* out, cudaStream_t s);
 enum Fold : int { FOLD_NONE = 0, FOLD_A = 1, FOLD_B = 2 };
 int gemm_config_count(int fp64);
 // FP32 transform GEMM configuration that runs on the tensor cores (3xTF32 tcgen05); the FP32

@@ -12,7 +12,6 @@
 
 #include <cmath>
 #include <cstdio>
-#include <mutex>
 
 #include "drd_common.cuh"
 
@@ -135,26 +134,17 @@ __global__ void k_na_ghosts(int nr, int nz, double* psi) {
     }
 }
 
-// Device address of g_presolve_scratch, looked up once per device (on the first call made with
-// that device current) and kept for the life of the process.  cudaDeviceReset destroys the
-// module that holds the array, so the cached address is not valid after it.
-std::mutex g_mu;
-double* g_addr[64] = {nullptr};
-
+// Device address of g_presolve_scratch in the current context, looked up on every call (a cheap
+// host query): no address is cached, so a cudaDeviceReset, which unloads the module that holds
+// the array, leaves nothing stale behind.
 int scratch_address(double** out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DRD_ERR_CUDA;
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (g_addr[dev] == nullptr) {
-        double* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_presolve_scratch);
-        if (e != cudaSuccess) {
-            std::fprintf(stderr, "drd_presolve_2_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
-            return DRD_ERR_CUDA;
-        }
-        g_addr[dev] = p;
+    double* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_presolve_scratch);
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "drd_presolve_2_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+        return DRD_ERR_CUDA;
     }
-    *out = g_addr[dev];
+    *out = p;
     return DRD_OK;
 }
 

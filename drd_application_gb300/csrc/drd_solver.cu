@@ -111,6 +111,10 @@ struct drd_ctx {
     GridBar* bar = nullptr;
     std::string persist_err;
     int* tcerr = nullptr;  // device: set by the tensor-core transform GEMM when a wait gave up
+    // the tensor-core GEMM's packed constant operands: CH x pass (also ESOLP_x's v rows), CH z
+    // pass, ESOLP_x's u rows; tiles and K chunks of each
+    float *pk_x = nullptr, *pk_z = nullptr, *pk_u = nullptr;
+    int pkx_t = 0, pkx_c = 0, pkz_t = 0, pkz_c = 0, pku_t = 0, pku_c = 0;
     unsigned long long* pprof = nullptr;  // DRD_PERSIST_PROF=1: barrier timestamps of block 0
     int pprof_on = 0;
     KState* ks;      // device, KS_COUNT entries
@@ -411,6 +415,7 @@ GemmArgs<T> dct1_xpass(drd_ctx* c, const T* X, T* out, const KState* ks, int gat
     a.Lf = c->nr - 1;
     a.B_odd = fmat<T>(c, 1);
     a.N_odd = c->Nxo;
+    if (sizeof(T) == 4) { a.packed = c->pk_x; a.pk_tiles = c->pkx_t; a.pk_chunks = c->pkx_c; }
     return a;
 }
 template <typename T>
@@ -420,6 +425,7 @@ GemmArgs<T> dct1_zpass(drd_ctx* c, const T* X, T* out, const KState* ks, int gat
     a.Lf = c->nz - 1;
     a.A_odd = fmat<T>(c, 3);
     a.M_odd = c->Mzo;
+    if (sizeof(T) == 4) { a.packed = c->pk_z; a.pk_tiles = c->pkz_t; a.pk_chunks = c->pkz_c; }
     return a;
 }
 
@@ -452,6 +458,11 @@ GemmArgs<T> esolp_rows(drd_ctx* c, int M, int L, const T* X, T* out, const KStat
     a.Lf = L - 1;
     a.B_odd = bo;
     a.N_odd = No;
+    if (sizeof(T) == 4) {
+        a.packed = u ? c->pk_u : c->pk_x;
+        a.pk_tiles = u ? c->pku_t : c->pkx_t;
+        a.pk_chunks = u ? c->pku_c : c->pkx_c;
+    }
     return a;
 }
 
@@ -1330,6 +1341,23 @@ int setup_context(drd_ctx* c) {
         launch_convert_scale<float, double>((long)ue.size(), c->f1ue, 1.0, c->f1ue32, nullptr, c->s);
         launch_convert_scale<float, double>((long)uo.size(), c->f1uo, 1.0, c->f1uo32, nullptr, c->s);
     }
+    {
+        // the tensor-core GEMM's packed constant operands (TF32 hi / lo, shared-memory block order)
+        auto pack = [&](const float* ev, const float* od, int re, int ro, int K, long ld, int bst, float** out,
+                        int* tiles, int* chunks) -> int {
+            const long n = gemm_tc_pack(ev, od, re, ro, K, ld, bst, nullptr, c->s);
+            CK(cudaMalloc(out, sizeof(float) * n));
+            gemm_tc_pack(ev, od, re, ro, K, ld, bst, *out, c->s);
+            *tiles = ((re > ro ? re : ro) + 127) / 128;
+            *chunks = (K + 31) / 32;
+            return DRD_OK;
+        };
+        int rc = pack(c->f1xe32, c->f1xo32, c->Nxe, c->Nxo, c->Kx, c->Nxe, 1, &c->pk_x, &c->pkx_t, &c->pkx_c);
+        rc |= pack(c->f1ze32, c->f1zo32, c->Mze, c->Mzo, c->Kz, c->Kz, 0, &c->pk_z, &c->pkz_t, &c->pkz_c);
+        rc |= pack(c->f1ue32, c->f1uo32, c->Nue, c->Nuo, c->Ku, c->Nue, 1, &c->pk_u, &c->pku_t, &c->pku_c);
+        if (rc) return DRD_ERR_CUDA;
+        CK(cudaGetLastError());
+    }
     std::vector<double> cfa(nr + 1, std::cos(c->P.angle * kPi / 180.0) / std::sqrt(2.0));
     CK(put(c->cfB, cfa));
     CK(put(c->cfT, cfa));
@@ -1473,6 +1501,9 @@ int drd_destroy(drd_ctx* c) {
     if (c->h_stage) cudaFreeHost(c->h_stage);
     clear_graphs(c);
     if (c->arena) cudaFree(c->arena);
+    if (c->pk_x) cudaFree(c->pk_x);
+    if (c->pk_z) cudaFree(c->pk_z);
+    if (c->pk_u) cudaFree(c->pk_u);
     if (c->pcw) cudaFree(c->pcw);
     if (c->pcw32) cudaFree(c->pcw32);
     if (c->pnum) cudaFree(c->pnum);

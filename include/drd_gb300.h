@@ -447,10 +447,10 @@ int drd_checkpoint_wait(drd_ctx* ctx);
  * v (VFACE) and psi (CELL) are device pointers owned by the caller, and the kernels run on
  * `stream` (a cudaStream_t, NULL for the default stream).  All intermediates live in one
  * fixed __device__ array of about 3.2 MB, held by every GPU that loads the library until the
- * process exits; grids beyond DRD_NOALLOC_MAX_* return DRD_ERR_TOO_LARGE.  The first call on a
- * device looks up that array's device address (cudaGetSymbolAddress) and should therefore
- * come before any stream capture on that device.  The address is kept for the life of the
- * process: after cudaDeviceReset on a device, this entry point must not be called on it again.
+ * process exits; grids beyond DRD_NOALLOC_MAX_* return DRD_ERR_TOO_LARGE.  Every call looks up
+ * that array's device address in the current context (cudaGetSymbolAddress), so the call stays
+ * valid after a cudaDeviceReset; the first call on a device loads the library's module and
+ * should therefore come before any stream capture on that device.
  * Calls share the array: each call writes every intermediate before reading it, but calls that
  * overlap on the GPU race on it.
  * No counterpart in the reference (its PreSolve_2 allocates nothing on a device because it has
