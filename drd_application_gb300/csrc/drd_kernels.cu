@@ -1514,16 +1514,19 @@ long gemm_tc_pack(const float* even, const float* odd, int rows_e, int rows_o, i
 }
 
 // Epilogue of the tensor-core GEMM: warp w reads TMEM lanes 32 (w % 4) (tile rows) and
-// columns 32 (w / 4) (tile columns), stores them (NaN when the tile gave up) and frees the TMEM.
+// columns 32 (w / 4) (tile columns) into a 128 x 129 shared-memory tile (`tile`, 66 KB of the
+// CTA's stages, free once every MMA is done), and the warps then store the tile row by row,
+// lanes along the tile's columns (consecutive output columns for FOLD_B, every other one for
+// FOLD_A); a tile that gave up is stored as NaN.  Frees the TMEM.
 template <int EPI>
 __device__ __forceinline__ void gtc_epilogue(const GemmArgs<float>& a, const GemmView<float>& g, uint32_t tbase, int m0,
-                                             int n0, bool poison) {
+                                             int n0, bool poison, float* tile) {
+    constexpr int TP = kGtcN + 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const int q = warp & 3, cq = warp >> 2;  // TMEM lane quarter, column quarter
-    const int m = m0 + 32 * q + lane;
+    const int q = warp & 3, cq = warp >> 2;  // TMEM lane quarter, column quarter (warps 0-15)
 #pragma unroll 1
-    for (int col = 32 * cq; col < 32 * cq + 32; col += 16) {
+    for (int col = 32 * cq; warp < 16 && col < 32 * cq + 32; col += 16) {
         uint32_t r[16];
         const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)col;
         asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -1531,23 +1534,32 @@ __device__ __forceinline__ void gtc_epilogue(const GemmArgs<float>& a, const Gem
                        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
                      : "r"(ta));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (m < g.M) {
+        float* trow = tile + (32 * q + lane) * TP + col;
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int n = n0 + col + j;
-                if (n < g.N) gemm_store<float, EPI>(a, g.orow(a, m), g.ocol(a, n), poison ? __int_as_float(0x7fc00000) : __uint_as_float(r[j]), 0.0);
-            }
-        }
+        for (int j = 0; j < 16; ++j) trow[j] = __uint_as_float(r[j]);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(128) : "memory");
+    const int nw = blockDim.x >> 5;
+#pragma unroll 1
+    for (int rr = warp; rr < kGtcM; rr += nw) {
+        const int m = m0 + rr;
+        if (m >= g.M) break;
+#pragma unroll
+        for (int i = 0; i < kGtcN / 32; ++i) {
+            const int cl = lane + 32 * i, n = n0 + cl;
+            if (n < g.N)
+                gemm_store<float, EPI>(a, g.orow(a, m), g.ocol(a, n), poison ? __int_as_float(0x7fc00000) : tile[rr * TP + cl], 0.0);
+        }
+    }
 }
 
-// The twelve MMAs of one 32-K chunk from operand stage `stage` (A hi, A lo, B hi, B lo):
-// per K = 8 step lo(A) hi(B), hi(A) lo(B), hi(A) hi(B); the first of the tile overwrites D.
-__device__ __forceinline__ void gtc_mma_chunk(uint32_t stage, uint32_t tbase, uint32_t idesc, bool first) {
-    const uint32_t aH = stage, aL = aH + kGtcOp, bH = aL + kGtcOp, bL = bH + kGtcOp;
+// The twelve MMAs of one 32-K chunk, A and B each given as its hi part followed by its lo part
+// (16 KB each): per K = 8 step lo(A) hi(B), hi(A) lo(B), hi(A) hi(B); the first of the tile
+// overwrites D.
+__device__ __forceinline__ void gtc_mma_chunk(uint32_t opa, uint32_t opb, uint32_t tbase, uint32_t idesc, bool first) {
+    const uint32_t aH = opa, aL = aH + kGtcOp, bH = opb, bL = bH + kGtcOp;
 #pragma unroll
     for (int t = 0; t < kGtcK / 8; ++t) {  // K = 8 per MMA: two core columns, 4096 bytes
         const uint32_t off = (uint32_t)t * 4096u;
@@ -1655,7 +1667,7 @@ __global__ void __launch_bounds__(kGtcThreads) k_gemm_tc(GemmArgs<float> a) {
             }
             if (!bad) {
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                gtc_mma_chunk(sbase + st * kGtcStage, tbase, idesc, c == 0);
+                gtc_mma_chunk(sbase + st * kGtcStage, sbase + st * kGtcStage + 2 * kGtcOp, tbase, idesc, c == 0);
                 const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[st]);
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
             }
@@ -1697,45 +1709,73 @@ __global__ void __launch_bounds__(kGtcThreads) k_gemm_tc(GemmArgs<float> a) {
         }
     }
     __syncthreads();
-    gtc_epilogue<EPI>(a, g, tbase, m0, n0, bad != 0);
+    gtc_epilogue<EPI>(a, g, tbase, m0, n0, bad != 0, reinterpret_cast<float*>(gsm));
 }
 
 // The tensor-core GEMM with TMA staging of the data operand.  Per 32-K chunk the data tile and
 // its fold mirror arrive as two 16 KB boxes of a 2-D tensor map (cp.async.bulk.tensor, one
-// thread issues, an expect-tx mbarrier tracks them), three chunks ahead in a ring of raw
-// stages; the threads fold each (row, 4-K group) from shared memory, split it into TF32 high
-// and low parts and write the MMA operand stage (two stages).  FOLD_A: the boxes are 32 K x 128
+// thread issues, an expect-tx mbarrier tracks them), two chunks ahead in a ring of raw stages;
+// the threads fold each (row, 4-K group) from shared memory, split it into TF32 high and low
+// parts and write the data operand stage (two stages).  The packed constant operand has its
+// own ring of three 32 KB stages, filled two chunks ahead by one bulk copy per chunk.  FOLD_A: the boxes are 32 K x 128
 // rows of X at (k0, m0) and (L - k0 - 31, m0), 128-byte swizzled (16-byte chunk j of box row r
 // sits at chunk j ^ (r & 7)); FOLD_B: 128 columns x 32 K rows of X at (n0, k0) and
-// (n0, L - k0 - 31), unswizzled.  The constant operand comes packed (one bulk copy per chunk).
-constexpr int kGtrRaw = 3;                                  // raw stages
+// (n0, L - k0 - 31), unswizzled.  Shared memory: data stages (2 x 32 KB: hi, lo), constant
+// stages (3 x 32 KB: hi, lo), raw stages (2 x 32 KB: box, mirror box).
+constexpr int kGtrRaw = 2;                                  // raw stages
+constexpr int kGtrCst = 3;                                  // constant operand stages
 constexpr uint32_t kGtrBox = kGtcM * kGtcK * 4;             // one box, 16 KB
 constexpr uint32_t kGtrRawStage = 2 * kGtrBox;              // the data box and its mirror
-constexpr int kGtrSmem = 2 * kGtcStage + kGtrRaw * kGtrRawStage + 1024;
+constexpr uint32_t kGtrOpStage = 2 * kGtcOp;                // hi and lo parts of one operand, 32 KB
+constexpr uint32_t kGtrCst0 = 2 * kGtrOpStage;              // offset of the constant stages
+constexpr uint32_t kGtrRaw0 = kGtrCst0 + kGtrCst * kGtrOpStage;  // offset of the raw stages
+constexpr int kGtrSmem = kGtrRaw0 + kGtrRaw * kGtrRawStage + 1024;
 
 __device__ __forceinline__ void gtr_box(uint32_t dst, const CUtensorMap* tm, int x, int y, uint32_t bar) {
     asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
                  ::"r"(dst), "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar) : "memory");
 }
 
+constexpr int kGtrThreads = kGtcThreads + 32;  // 16 converter warps and the copy / MMA warp
+
+// gtc_wait that also gives up as soon as *flag is set (another thread gave up)
+__device__ __forceinline__ bool gtr_wait(uint32_t bar, uint32_t parity, const volatile int* flag) {
+    for (int it = 0; it < kGtcSpin; ++it) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+        if (ok) return true;
+        if (*flag) return false;
+    }
+    return false;
+}
+
+// Warp roles: warps 0-15 convert (chunk c: wait until the MMAs of chunk c - 2 have released data
+// stage c & 1 and chunk c's boxes have landed, fold and split into the stage, arrive on its
+// `full` barrier); warp 16's first lane issues every copy and MMA (chunk c: wait for `full`,
+// refill the consumed raw stage with chunk c + 2, wait for the constant operand, issue the
+// twelve MMAs and commit them, wait for chunk c - 1's MMAs and refill their constant stage with
+// chunk c + 2).  No block-wide barrier inside the K loop: conversion of chunk c + 1 overlaps
+// the MMAs of chunk c.
 template <int EPI>
-__global__ void __launch_bounds__(kGtcThreads) k_gemm_tc_tma(GemmArgs<float> a, const __grid_constant__ CUtensorMap tm) {
+__global__ void __launch_bounds__(kGtrThreads) k_gemm_tc_tma(GemmArgs<float> a, const __grid_constant__ CUtensorMap tm) {
     extern __shared__ __align__(1024) unsigned char gsm_raw[];
     __shared__ uint32_t tmem_base;
-    __shared__ __align__(8) uint64_t mbar[2];        // MMAs that read operand stage s are done
-    __shared__ __align__(8) uint64_t lbar[2];        // packed constant operand of stage s landed
+    __shared__ __align__(8) uint64_t mbar[2];        // MMAs of chunk c (data stage c & 1) are done
+    __shared__ __align__(8) uint64_t fbar[2];        // data stage s converted (kGtcThreads arrivals)
+    __shared__ __align__(8) uint64_t lbar[kGtrCst];  // packed constant operand of stage s landed
     __shared__ __align__(8) uint64_t rbar[kGtrRaw];  // data boxes of raw stage s landed
-    __shared__ int bad, raw_bad;                     // raw_bad: a wait for data boxes gave up
+    __shared__ volatile int bad;
     count_launch(a.ctr);
     if (gate_closed(a.ks, a.gate)) return;
     const GemmView<float> g(a, a.fold ? (int)blockIdx.z : 0);
     const bool fa = a.fold == FOLD_A;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, warp = tid >> 5;
     const int m0 = blockIdx.y * kGtcM, n0 = blockIdx.x * kGtcN;
     if (m0 >= g.M || n0 >= g.N) return;
     unsigned char* gsm = gsm_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(gsm_raw) & 1023u)) & 1023u);
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(gsm);
-    if ((threadIdx.x >> 5) == 0) {
+    if (warp == 0) {
         const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tmem_base);
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(128) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
@@ -1743,146 +1783,157 @@ __global__ void __launch_bounds__(kGtcThreads) k_gemm_tc_tma(GemmArgs<float> a, 
     if (tid == 0) {
         for (int i = 0; i < 2; ++i) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&mbar[i])) : "memory");
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&lbar[i])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(&fbar[i])),
+                         "r"(kGtcThreads) : "memory");
         }
+        for (int i = 0; i < kGtrCst; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&lbar[i])) : "memory");
         for (int i = 0; i < kGtrRaw; ++i)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&rbar[i])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         bad = 0;
-        raw_bad = 0;
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tbase = tmem_base;
-    const int ctile = fa ? (int)blockIdx.x : (int)blockIdx.y;  // the packed operand's row tile
-    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kGtcN >> 3) << 17) | ((uint32_t)(kGtcM >> 4) << 24);
     const int K = a.K, L = a.Lf, nchunks = (K + kGtcK - 1) / kGtcK;
-    const uint32_t raw0 = sbase + 2 * kGtcStage;
-    unsigned char* rawp = gsm + 2 * kGtcStage;
-    // thread 0's record of what is in flight: chunks [0, n_tma) have their boxes issued,
-    // [0, n_bulk) their packed operand, [0, n_mma) their MMAs committed; [0, w_bulk) and
-    // [0, w_mma) were waited for
-    int n_tma = 0, n_bulk = 0, n_mma = 0, w_bulk = 0, w_mma = 0;
-    auto issue_tma = [&](int cc) {
-        const int rs = cc % kGtrRaw;
-        const uint32_t rb = (uint32_t)__cvta_generic_to_shared(&rbar[rs]);
-        const uint32_t dst = raw0 + rs * kGtrRawStage;
-        const int k0 = cc * kGtcK, k1 = L - k0 - (kGtcK - 1);
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(rb), "r"(kGtrRawStage) : "memory");
-        if (fa) {
-            gtr_box(dst, &tm, k0, m0, rb);
-            gtr_box(dst + kGtrBox, &tm, k1, m0, rb);
-        } else {
-            gtr_box(dst, &tm, n0, k0, rb);
-            gtr_box(dst + kGtrBox, &tm, n0, k1, rb);
-        }
-        n_tma = cc + 1;
-    };
-    auto issue_bulk = [&](int cc) {  // the packed constant operand of chunk cc into stage cc & 1
-        const int st = cc & 1;
-        const uint32_t lb = (uint32_t)__cvta_generic_to_shared(&lbar[st]);
-        const uint32_t dst = sbase + st * kGtcStage + (fa ? 2 * kGtcOp : 0);
-        const float* src = a.packed + ((long)(g.par * a.pk_tiles + ctile) * a.pk_chunks + cc) * (2 * kGtcM * kGtcK);
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(lb), "r"(2u * kGtcOp) : "memory");
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(dst), "l"(src), "r"(2u * kGtcOp), "r"(lb) : "memory");
-        n_bulk = cc + 1;
-    };
     auto fail = [&]() {
         bad = 1;
         if (a.err) atomicExch(a.err, 1);
     };
-    if (tid == 0 && nchunks > 0) {
+    if (warp < kGtcThreads / 32) {
+        // ---- converters ----
+        const float sg = g.par ? -1.f : 1.f;
+        const unsigned char* rawp = gsm + kGtrRaw0;
+        for (int c = 0; c < nchunks; ++c) {
+            if (bad) break;
+            const int st = c & 1, rs = c % kGtrRaw;
+            if (c >= 2 && !gtr_wait((uint32_t)__cvta_generic_to_shared(&mbar[st]), (uint32_t)(((c - 2) >> 1) & 1), &bad)) {
+                fail();
+                break;
+            }
+            if (!gtr_wait((uint32_t)__cvta_generic_to_shared(&rbar[rs]), (uint32_t)((c / kGtrRaw) & 1), &bad)) {
+                fail();
+                break;
+            }
+            const unsigned char* r0 = rawp + rs * kGtrRawStage;
+            const unsigned char* r1 = r0 + kGtrBox;
+            unsigned char* op = gsm + st * kGtrOpStage;
+            const int k0 = c * kGtcK;
+#pragma unroll
+            for (int it = 0; it < GTC_NI; ++it) {
+                const int item = tid + it * kGtcThreads, r = item % kGtcM, kg = item / kGtcM;
+                float v[4];
+                if (fa) {
+                    const float4 x0 = *reinterpret_cast<const float4*>(r0 + r * 128 + ((kg ^ (r & 7)) << 4));
+                    const float4 x1 = *reinterpret_cast<const float4*>(r1 + r * 128 + (((7 - kg) ^ (r & 7)) << 4));
+                    const float a0[4] = {x0.x, x0.y, x0.z, x0.w}, a1[4] = {x1.w, x1.z, x1.y, x1.x};
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int k = k0 + 4 * kg + j;
+                        v[j] = (k >= K) ? 0.f : (2 * k == L) ? (g.par ? 0.f : a0[j]) : fmaf(sg, a1[j], a0[j]);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int k = k0 + 4 * kg + j;
+                        const float y0 = *reinterpret_cast<const float*>(r0 + (4 * kg + j) * 512 + r * 4);
+                        const float y1 = *reinterpret_cast<const float*>(r1 + (kGtcK - 1 - 4 * kg - j) * 512 + r * 4);
+                        v[j] = (k >= K) ? 0.f : (2 * k == L) ? (g.par ? 0.f : y0) : fmaf(sg, y1, y0);
+                    }
+                }
+                gtc_put4(op, op + kGtcOp, r, kg, v);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"((uint32_t)__cvta_generic_to_shared(&fbar[st])) : "memory");
+        }
+    } else if ((tid & 31) == 0) {
+        // ---- copies and MMAs ----
+        const int ctile = fa ? (int)blockIdx.x : (int)blockIdx.y;  // the packed operand's row tile
+        const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kGtcN >> 3) << 17) | ((uint32_t)(kGtcM >> 4) << 24);
+        const uint32_t raw0 = sbase + kGtrRaw0;
+        // chunks [0, n_tma) have their boxes issued, [0, n_bulk) their packed operand, [0, n_mma)
+        // their MMAs committed; [0, w_bulk) and [0, w_mma) were waited for
+        int n_tma = 0, n_bulk = 0, n_mma = 0, w_bulk = 0, w_mma = 0;
+        auto issue_tma = [&](int cc) {
+            const int rs = cc % kGtrRaw;
+            const uint32_t rb = (uint32_t)__cvta_generic_to_shared(&rbar[rs]);
+            const uint32_t dst = raw0 + rs * kGtrRawStage;
+            const int k0 = cc * kGtcK, k1 = L - k0 - (kGtcK - 1);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(rb), "r"(kGtrRawStage) : "memory");
+            if (fa) {
+                gtr_box(dst, &tm, k0, m0, rb);
+                gtr_box(dst + kGtrBox, &tm, k1, m0, rb);
+            } else {
+                gtr_box(dst, &tm, n0, k0, rb);
+                gtr_box(dst + kGtrBox, &tm, n0, k1, rb);
+            }
+            n_tma = cc + 1;
+        };
+        auto issue_bulk = [&](int cc) {  // the packed constant operand of chunk cc into stage cc % 3
+            const int cs = cc % kGtrCst;
+            const uint32_t lb = (uint32_t)__cvta_generic_to_shared(&lbar[cs]);
+            const uint32_t dst = sbase + kGtrCst0 + cs * kGtrOpStage;
+            const float* src = a.packed + ((long)(g.par * a.pk_tiles + ctile) * a.pk_chunks + cc) * (2 * kGtcM * kGtcK);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(lb), "r"(2u * kGtcOp) : "memory");
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         ::"r"(dst), "l"(src), "r"(2u * kGtcOp), "r"(lb) : "memory");
+            n_bulk = cc + 1;
+        };
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tm)) : "memory");
         for (int cc = 0; cc < kGtrRaw && cc < nchunks; ++cc) issue_tma(cc);
-        issue_bulk(0);
-    }
-    const float sg = g.par ? -1.f : 1.f;
-    int c = 0;
-    for (; c < nchunks; ++c) {
-        const int st = c & 1, rs = c % kGtrRaw;
-        __syncthreads();  // `bad` is the same for every thread; stage st's MMAs (chunk c - 2) are done
-        if (bad) break;
-        if (!gtc_wait((uint32_t)__cvta_generic_to_shared(&rbar[rs]), (uint32_t)((c / kGtrRaw) & 1))) {
-            raw_bad = 1;
-            fail();
-        }
-        const unsigned char* r0 = rawp + rs * kGtrRawStage;
-        const unsigned char* r1 = r0 + kGtrBox;
-        unsigned char* op = gsm + st * kGtcStage + (fa ? 0 : 2 * kGtcOp);
-        const int k0 = c * kGtcK;
-#pragma unroll
-        for (int it = 0; it < GTC_NI; ++it) {
-            const int item = tid + it * kGtcThreads, r = item % kGtcM, kg = item / kGtcM;
-            float v[4];
-            if (fa) {
-                const float4 x0 = *reinterpret_cast<const float4*>(r0 + r * 128 + ((kg ^ (r & 7)) << 4));
-                const float4 x1 = *reinterpret_cast<const float4*>(r1 + r * 128 + (((7 - kg) ^ (r & 7)) << 4));
-                const float a0[4] = {x0.x, x0.y, x0.z, x0.w}, a1[4] = {x1.w, x1.z, x1.y, x1.x};
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int k = k0 + 4 * kg + j;
-                    v[j] = (k >= K) ? 0.f : (2 * k == L) ? (g.par ? 0.f : a0[j]) : fmaf(sg, a1[j], a0[j]);
+        for (int cc = 0; cc < kGtrCst - 1 && cc < nchunks; ++cc) issue_bulk(cc);
+        for (int c = 0; c < nchunks; ++c) {
+            const int st = c & 1, cs = c % kGtrCst;
+            // chunk c converted: its raw stage takes chunk c + 2
+            if (!gtr_wait((uint32_t)__cvta_generic_to_shared(&fbar[st]), (uint32_t)((c >> 1) & 1), &bad) || bad) {
+                fail();
+                break;
+            }
+            if (c + kGtrRaw < nchunks) issue_tma(c + kGtrRaw);
+            if (!gtr_wait((uint32_t)__cvta_generic_to_shared(&lbar[cs]), (uint32_t)((c / kGtrCst) & 1), &bad)) {
+                fail();
+                break;
+            }
+            w_bulk = c + 1;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t dop = sbase + st * kGtrOpStage, cop = sbase + kGtrCst0 + cs * kGtrOpStage;
+            gtc_mma_chunk(fa ? dop : cop, fa ? cop : dop, tbase, idesc, c == 0);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         ::"r"((uint32_t)__cvta_generic_to_shared(&mbar[st])) : "memory");
+            n_mma = c + 1;
+            // chunk c - 1's MMAs done: its constant stage takes chunk c + 2
+            if (c >= 1) {
+                if (!gtr_wait((uint32_t)__cvta_generic_to_shared(&mbar[st ^ 1]), (uint32_t)(((c - 1) >> 1) & 1), &bad)) {
+                    fail();
+                    break;
                 }
-            } else {
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int k = k0 + 4 * kg + j;
-                    const float y0 = *reinterpret_cast<const float*>(r0 + (4 * kg + j) * 512 + r * 4);
-                    const float y1 = *reinterpret_cast<const float*>(r1 + (kGtcK - 1 - 4 * kg - j) * 512 + r * 4);
-                    v[j] = (k >= K) ? 0.f : (2 * k == L) ? (g.par ? 0.f : y0) : fmaf(sg, y1, y0);
-                }
+                w_mma = c;
             }
-            gtc_put4(op, op + kGtcOp, r, kg, v);
+            if (c + kGtrCst - 1 < nchunks) issue_bulk(c + kGtrCst - 1);
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            if (!bad) {
-                if (gtc_wait((uint32_t)__cvta_generic_to_shared(&lbar[st]), (uint32_t)((c >> 1) & 1))) w_bulk = c + 1;
-                else fail();
-            }
-            if (!bad) {
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                gtc_mma_chunk(sbase + st * kGtcStage, tbase, idesc, c == 0);
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                             ::"r"((uint32_t)__cvta_generic_to_shared(&mbar[st])) : "memory");
-                n_mma = c + 1;
-            }
-            // every thread has read raw stage rs: it takes chunk c + 3
-            if (!bad && c + kGtrRaw < nchunks) issue_tma(c + kGtrRaw);
-            // chunk c - 1's MMAs done: its operand stage takes chunk c + 1
-            if (!bad && c >= 1) {
-                if (gtc_wait((uint32_t)__cvta_generic_to_shared(&mbar[st ^ 1]), (uint32_t)(((c - 1) >> 1) & 1))) w_mma = c;
-                else fail();
-            }
-            if (!bad && c + 1 < nchunks) issue_bulk(c + 1);
-        }
-    }
-    if (tid == 0 && nchunks > 0) {
         if (!bad) {  // the last commit covers every MMA of the tile
             const int lc = nchunks - 1;
             if (gtc_wait((uint32_t)__cvta_generic_to_shared(&mbar[lc & 1]), (uint32_t)((lc >> 1) & 1))) w_mma = nchunks;
             else fail();
         }
         if (bad) {
-            // drain (bounded, in issue order) what is still in flight, so that no copy lands in
-            // and no MMA reads this CTA's shared memory after it has exited: the boxes of the
-            // chunks not yet consumed (from the last one when its wait gave up: then no later
-            // chunk was issued into its stage), the packed operands and the MMAs not yet waited
-            // for.  Each of these is the oldest pending phase of its barrier.
-            const int cl = (raw_bad && c > 0) ? c - 1 : c;
-            for (int cc = cl; cc < n_tma; ++cc)
+            // drain (bounded, in issue order) what may still be in flight, so that no copy lands
+            // in and no MMA reads this CTA's shared memory after it has exited: the boxes of the
+            // last two chunks issued (a stage is refilled only after every converter has passed
+            // its wait), the packed operands and the MMAs not yet waited for.  Each is the oldest
+            // pending phase of its barrier, or already complete.
+            for (int cc = n_tma > kGtrRaw ? n_tma - kGtrRaw : 0; cc < n_tma; ++cc)
                 gtc_wait((uint32_t)__cvta_generic_to_shared(&rbar[cc % kGtrRaw]), (uint32_t)((cc / kGtrRaw) & 1));
             for (int cc = w_bulk; cc < n_bulk; ++cc)
-                gtc_wait((uint32_t)__cvta_generic_to_shared(&lbar[cc & 1]), (uint32_t)((cc >> 1) & 1));
+                gtc_wait((uint32_t)__cvta_generic_to_shared(&lbar[cc % kGtrCst]), (uint32_t)((cc / kGtrCst) & 1));
             for (int cc = w_mma; cc < n_mma; ++cc)
                 gtc_wait((uint32_t)__cvta_generic_to_shared(&mbar[cc & 1]), (uint32_t)((cc >> 1) & 1));
         }
     }
     __syncthreads();
-    gtc_epilogue<EPI>(a, g, tbase, m0, n0, bad != 0);
+    gtc_epilogue<EPI>(a, g, tbase, m0, n0, bad != 0, reinterpret_cast<float*>(gsm));
 }
 
 // cuTensorMapEncodeTiled, fetched from the driver once (no link against libcuda)
@@ -1943,8 +1994,8 @@ static void gemm_tc_launch(int epi, const GemmArgs<float>& a, cudaStream_t s) {
     dim3 grid((N + kGtcN - 1) / kGtcN, (M + kGtcM - 1) / kGtcM, a.fold ? 2 : 1);
     alignas(64) CUtensorMap tm;
     if (!std::getenv("DRD_GEMM_TC_NOTMA") && gtr_map(a, &tm)) {  // the variable selects the fallback (tests)
-        if (epi == EPI_DIV_TAB) k_gemm_tc_tma<EPI_DIV_TAB><<<grid, kGtcThreads, kGtrSmem, s>>>(a, tm);
-        else k_gemm_tc_tma<EPI_STORE><<<grid, kGtcThreads, kGtrSmem, s>>>(a, tm);
+        if (epi == EPI_DIV_TAB) k_gemm_tc_tma<EPI_DIV_TAB><<<grid, kGtrThreads, kGtrSmem, s>>>(a, tm);
+        else k_gemm_tc_tma<EPI_STORE><<<grid, kGtrThreads, kGtrSmem, s>>>(a, tm);
         return;
     }
     if (epi == EPI_DIV_TAB) k_gemm_tc<EPI_DIV_TAB><<<grid, kGtcThreads, kGtcSmem, s>>>(a);
