@@ -1821,26 +1821,32 @@ __global__ void __launch_bounds__(kGtrThreads) k_gemm_tc_tma(GemmArgs<float> a, 
             const unsigned char* r1 = r0 + kGtrBox;
             unsigned char* op = gsm + st * kGtrOpStage;
             const int k0 = c * kGtcK;
+            // a chunk past K's end or holding the middle point k = L / 2 takes the masked fold
+            const bool edge = (k0 + kGtcK > K) || ((L & 1) == 0 && 2 * k0 <= L && L < 2 * (k0 + kGtcK));
 #pragma unroll
             for (int it = 0; it < GTC_NI; ++it) {
                 const int item = tid + it * kGtcThreads, r = item % kGtcM, kg = item / kGtcM;
-                float v[4];
+                float a0[4], a1[4], v[4];
                 if (fa) {
                     const float4 x0 = *reinterpret_cast<const float4*>(r0 + r * 128 + ((kg ^ (r & 7)) << 4));
                     const float4 x1 = *reinterpret_cast<const float4*>(r1 + r * 128 + (((7 - kg) ^ (r & 7)) << 4));
-                    const float a0[4] = {x0.x, x0.y, x0.z, x0.w}, a1[4] = {x1.w, x1.z, x1.y, x1.x};
+                    a0[0] = x0.x; a0[1] = x0.y; a0[2] = x0.z; a0[3] = x0.w;
+                    a1[0] = x1.w; a1[1] = x1.z; a1[2] = x1.y; a1[3] = x1.x;
+                } else {
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
-                        const int k = k0 + 4 * kg + j;
-                        v[j] = (k >= K) ? 0.f : (2 * k == L) ? (g.par ? 0.f : a0[j]) : fmaf(sg, a1[j], a0[j]);
+                        a0[j] = *reinterpret_cast<const float*>(r0 + (4 * kg + j) * 512 + r * 4);
+                        a1[j] = *reinterpret_cast<const float*>(r1 + (kGtcK - 1 - 4 * kg - j) * 512 + r * 4);
                     }
+                }
+                if (!edge) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) v[j] = fmaf(sg, a1[j], a0[j]);
                 } else {
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
                         const int k = k0 + 4 * kg + j;
-                        const float y0 = *reinterpret_cast<const float*>(r0 + (4 * kg + j) * 512 + r * 4);
-                        const float y1 = *reinterpret_cast<const float*>(r1 + (kGtcK - 1 - 4 * kg - j) * 512 + r * 4);
-                        v[j] = (k >= K) ? 0.f : (2 * k == L) ? (g.par ? 0.f : y0) : fmaf(sg, y1, y0);
+                        v[j] = (k >= K) ? 0.f : (2 * k == L) ? (g.par ? 0.f : a0[j]) : fmaf(sg, a1[j], a0[j]);
                     }
                 }
                 gtc_put4(op, op + kGtcOp, r, kg, v);
