@@ -1942,6 +1942,22 @@ __global__ void __launch_bounds__(kGtrThreads) k_gemm_tc_tma(GemmArgs<float> a, 
     gtc_epilogue<EPI>(a, g, tbase, m0, n0, bad != 0, reinterpret_cast<float*>(gsm));
 }
 
+__global__ void k_host_copies(HostCopies h, ull* ctr) {
+    count_launch(ctr);
+    const int i = blockIdx.y;
+    const double* __restrict__ src = h.src[i];
+    double* __restrict__ dst = h.dst[i];
+    const long n = h.len[i];
+    for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) dst[j] = src[j];
+}
+void launch_host_copies(const HostCopies& h, ull* ctr, cudaStream_t s) {
+    if (h.n <= 0) return;
+    long mx = 0;
+    for (int i = 0; i < h.n; ++i) mx = h.len[i] > mx ? h.len[i] : mx;
+    const int bx = (int)std::min<long>((mx + 255) / 256, 96);  // about 2 MB in flight per copy row
+    k_host_copies<<<dim3(bx, h.n), 256, 0, s>>>(h, ctr);
+}
+
 // cuTensorMapEncodeTiled, fetched from the driver once (no link against libcuda)
 typedef CUresult (*GtrEncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
                                 const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,

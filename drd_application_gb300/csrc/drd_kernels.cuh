@@ -169,6 +169,19 @@ void launch_threshold(long n, const double* x, double t, double* y, ull* ctr, cu
 void launch_two_phase_coef(const DevParams& P, long cs, const double* fpd, const double* ph, double* rho, double* eta,
                            float* rho32, float* eta32, ull* ctr, cudaStream_t s);
 
+// Up to kHostCopyMax copies of FP64 arrays in one launch, each src[i] -> dst[i] of len[i] values
+// (one row of blocks per copy).  The per-routine calls use it for the caller's page-locked host
+// arrays, read or written through their mapped device addresses over the host link, in place of
+// one DMA copy per array.
+constexpr int kHostCopyMax = 16;
+struct HostCopies {
+    int n;
+    const double* src[kHostCopyMax];
+    double* dst[kHostCopyMax];
+    long len[kHostCopyMax];
+};
+void launch_host_copies(const HostCopies& h, ull* ctr, cudaStream_t s);
+
 // ---- persistent cooperative BiCGSTAB (FP32 inner solves of the CH and momentum systems) ---
 struct GridBar {
     unsigned count, gen;

@@ -133,6 +133,8 @@ struct drd_ctx {
     std::string err;
     int use_graph = 1;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // the per-routine calls' copies of page-locked host arrays, gathered into one launch each way
+    HostCopies hq_up{}, hq_down{};
     cudaEvent_t tev0 = nullptr, tev1 = nullptr;  // autotuner timing
     // asynchronous checkpoint: pinned staging, its copy stream and events, the writer thread
     cudaStream_t sck = nullptr;
@@ -1121,6 +1123,58 @@ int down(drd_ctx* c, double* dst, const double* src, long n) {
     return DRD_OK;
 }
 
+// The device address of host array [p, p + n) when the whole range lies in mapped, page-locked
+// host memory (drd_host_register, cudaHostAlloc) with one contiguous device mapping, else null.
+double* mapped_range(const double* p, long n) {
+    cudaPointerAttributes a0{}, a1{};
+    if (n <= 0 || cudaPointerGetAttributes(&a0, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a0.devicePointer == nullptr) return nullptr;
+    if (cudaPointerGetAttributes(&a1, p + (n - 1)) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a1.type != cudaMemoryTypeHost || (double*)a1.devicePointer != (double*)a0.devicePointer + (n - 1)) return nullptr;
+    return (double*)a0.devicePointer;
+}
+
+// Host-to-device copy of a per-routine call's input: queued for the call's one gather launch
+// (flush_up) when the host array is mapped, page-locked memory, else an immediate DMA copy.  The
+// queue must be flushed before any work that reads dst.
+int up_q(drd_ctx* c, double* dst, const double* src, long n) {
+    if (!src) return DRD_OK;
+    HostCopies& h = c->hq_up;
+    const double* m = h.n < kHostCopyMax ? mapped_range(src, n) : nullptr;
+    if (!m) return up(c, dst, src, n);
+    h.src[h.n] = m;
+    h.dst[h.n] = dst;
+    h.len[h.n] = n;
+    ++h.n;
+    return DRD_OK;
+}
+// Device-to-host copy of a call's output, queued likewise (flush_down after the work that
+// writes src).
+int down_q(drd_ctx* c, double* dst, const double* src, long n) {
+    if (!dst) return DRD_OK;
+    HostCopies& h = c->hq_down;
+    double* m = h.n < kHostCopyMax ? mapped_range(dst, n) : nullptr;
+    if (!m) return down(c, dst, src, n);
+    h.src[h.n] = src;
+    h.dst[h.n] = m;
+    h.len[h.n] = n;
+    ++h.n;
+    return DRD_OK;
+}
+int flush_q(drd_ctx* c, HostCopies& h) {
+    launch_host_copies(h, c->ctr, c->s);
+    h.n = 0;
+    CK(cudaGetLastError());
+    return DRD_OK;
+}
+void reset_q(drd_ctx* c) { c->hq_up.n = c->hq_down.n = 0; }
+
 int refresh_fp32(drd_ctx* c) {
     launch_convert_scale<float, double>(c->cs, c->rho, 1.0, c->rho32, nullptr, c->s);
     launch_convert_scale<float, double>(c->cs, c->eta, 1.0, c->eta32, nullptr, c->s);
@@ -1665,16 +1719,18 @@ int drd_interpolate_coef(drd_ctx* c, const double* dist, double* fpd_ph, double*
 
 int drd_two_phase_coef(drd_ctx* c, const double* fpd_ph, const double* ph, double* rho, double* eta) {
     if (!c) return DRD_ERR_BADARG;
+    reset_q(c);
     CK(cudaEventRecord(c->ev0, c->s));
-    if (up(c, c->fpd, fpd_ph, c->cs)) return DRD_ERR_CUDA;
+    if (up_q(c, c->fpd, fpd_ph, c->cs)) return DRD_ERR_CUDA;
     const double* dph = c->fld[DRD_F_PH];
     if (ph) {
-        if (up(c, c->ph_after, ph, c->cs)) return DRD_ERR_CUDA;  // scratch until the next solve
+        if (up_q(c, c->ph_after, ph, c->cs)) return DRD_ERR_CUDA;  // scratch until the next solve
         dph = c->ph_after;
     }
+    if (flush_q(c, c->hq_up)) return DRD_ERR_CUDA;
     launch_two_phase_coef(c->dp, c->cs, c->fpd, dph, c->rho, c->eta, c->rho32, c->eta32, c->ctr, c->s);
     CK(cudaGetLastError());
-    if (down(c, rho, c->rho, c->cs) | down(c, eta, c->eta, c->cs)) return DRD_ERR_CUDA;
+    if (down_q(c, rho, c->rho, c->cs) | down_q(c, eta, c->eta, c->cs) | flush_q(c, c->hq_down)) return DRD_ERR_CUDA;
     return finish_call(c, 0, nullptr, false);
 }
 
@@ -1918,6 +1974,7 @@ int drd_phsolve(drd_ctx* c, const double* u, const double* v, const double* ph, 
                 double* rmu_after, double* ph_after, drd_status* st) {
     if (!c || !u || !v || !ph || !rmu || !rmu_after || !ph_after) return DRD_ERR_BADARG;
     if (c->P.variant != DRD_VARIANT_MF) { c->err = "PhSolve belongs to the MF variant"; return DRD_ERR_BADARG; }
+    reset_q(c);
     CK(cudaEventRecord(c->ev0, c->s));
     // guess_mode 1 / 2: the guess extrapolates rmu through the rmu of the previous one or two
     // calls (x^(n-1), x^(n-2) when the calls are successive time steps; otherwise only the
@@ -1928,8 +1985,9 @@ int drd_phsolve(drd_ctx* c, const double* u, const double* v, const double* ph, 
     if (extrap >= 1) CK(cudaMemcpyAsync(c->fld[DRD_F_RMU_PRE], c->rmu_prev, cb, cudaMemcpyDeviceToDevice, c->s));
     if (extrap >= 2) CK(cudaMemcpyAsync(c->rmu_pre2, c->rmu_prev2, cb, cudaMemcpyDeviceToDevice, c->s));
     if (extrap == 3) CK(cudaMemcpyAsync(c->rmu_pre3, c->rmu_prev3, cb, cudaMemcpyDeviceToDevice, c->s));
-    int rc = up(c, c->fld[DRD_F_U], u, c->us) | up(c, c->fld[DRD_F_V], v, c->vs) | up(c, c->fld[DRD_F_PH], ph, c->cs) |
-             up(c, c->fld[DRD_F_RMU], rmu, c->cs);
+    int rc = up_q(c, c->fld[DRD_F_U], u, c->us) | up_q(c, c->fld[DRD_F_V], v, c->vs) |
+             up_q(c, c->fld[DRD_F_PH], ph, c->cs) | up_q(c, c->fld[DRD_F_RMU], rmu, c->cs);
+    rc |= flush_q(c, c->hq_up);
     if (rc) return DRD_ERR_CUDA;
     if (gm >= 1) {
         if (gm == 3) CK(cudaMemcpyAsync(c->rmu_prev3, c->rmu_prev2, cb, cudaMemcpyDeviceToDevice, c->s));
@@ -1939,7 +1997,8 @@ int drd_phsolve(drd_ctx* c, const double* u, const double* v, const double* ph, 
     }
     rc = run_graph(c, gkey(GK_CH, mixed_of(c), extrap), [&](cudaStream_t s) { return enq_ch(c, s, extrap); }, t, 0.0);
     if (rc) return rc;
-    rc = down(c, rmu_after, c->rmu_after, c->cs) | down(c, ph_after, c->ph_after, c->cs);
+    rc = down_q(c, rmu_after, c->rmu_after, c->cs) | down_q(c, ph_after, c->ph_after, c->cs);
+    rc |= flush_q(c, c->hq_down);
     if (rc) return DRD_ERR_CUDA;
     return finish_call(c, KS_CH, st, true);
 }
@@ -1971,16 +2030,19 @@ static int velo_common(drd_ctx* c, int bdf, const double* psi1, const double* ps
                        double* v_after, double* uL, double* uR, drd_status* st) {
     if (!c || !u || !v || !p || !ph_after || !rmu_after || !u_after || !v_after) return DRD_ERR_BADARG;
     if (bdf == 2 && (!psi1 || !psi2 || !u_pre || !v_pre)) return DRD_ERR_BADARG;
+    reset_q(c);
     CK(cudaEventRecord(c->ev0, c->s));
-    int rc = up(c, c->fld[DRD_F_U], u, c->us) | up(c, c->fld[DRD_F_V], v, c->vs) | up(c, c->fld[DRD_F_P], p, c->cs) |
-             up(c, c->ph_after, ph_after, c->cs) | up(c, c->rmu_after, rmu_after, c->cs);
+    int rc = up_q(c, c->fld[DRD_F_U], u, c->us) | up_q(c, c->fld[DRD_F_V], v, c->vs) |
+             up_q(c, c->fld[DRD_F_P], p, c->cs) | up_q(c, c->ph_after, ph_after, c->cs) |
+             up_q(c, c->rmu_after, rmu_after, c->cs);
     if (bdf == 2)
-        rc |= up(c, c->fld[DRD_F_PSI1], psi1, c->cs) | up(c, c->fld[DRD_F_PSI2], psi2, c->cs) |
-              up(c, c->fld[DRD_F_U_PRE], u_pre, c->us) | up(c, c->fld[DRD_F_V_PRE], v_pre, c->vs);
-    if (pf1) rc |= up(c, c->fld[DRD_F_PF1], pf1, c->cs);
+        rc |= up_q(c, c->fld[DRD_F_PSI1], psi1, c->cs) | up_q(c, c->fld[DRD_F_PSI2], psi2, c->cs) |
+              up_q(c, c->fld[DRD_F_U_PRE], u_pre, c->us) | up_q(c, c->fld[DRD_F_V_PRE], v_pre, c->vs);
+    if (pf1) rc |= up_q(c, c->fld[DRD_F_PF1], pf1, c->cs);
     else CK(cudaMemsetAsync(c->fld[DRD_F_PF1], 0, sizeof(double) * c->cs, c->s));
-    if (pf2) rc |= up(c, c->fld[DRD_F_PF2], pf2, c->cs);
+    if (pf2) rc |= up_q(c, c->fld[DRD_F_PF2], pf2, c->cs);
     else CK(cudaMemsetAsync(c->fld[DRD_F_PF2], 0, sizeof(double) * c->cs, c->s));
+    rc |= flush_q(c, c->hq_up);
     if (rc) return DRD_ERR_CUDA;
     // guess_mode 1 / 2 (BDF2): the momentum solve starts from 2 u - u_pre, or from 3 u - 3 u_pre +
     // u_pre2 with u_pre2 the u_pre of the previous call; v likewise
@@ -2000,9 +2062,10 @@ static int velo_common(drd_ctx* c, int bdf, const double* psi1, const double* ps
         c->uv_hist = std::min(c->uv_hist + 1, 2);
     }
     if (rc) return rc;
-    rc = down(c, u_after, c->u_after, c->us) | down(c, v_after, c->v_after, c->vs);
+    rc = down_q(c, u_after, c->u_after, c->us) | down_q(c, v_after, c->v_after, c->vs);
     const bool dirichlet = !(c->P.variant == DRD_VARIANT_TP && c->P.lr_bd_type == 'n');
-    if (dirichlet) rc |= down(c, uL, c->uL, c->nz) | down(c, uR, c->uL, c->nz);
+    if (dirichlet) rc |= down_q(c, uL, c->uL, c->nz) | down_q(c, uR, c->uL, c->nz);
+    rc |= flush_q(c, c->hq_down);
     if (rc) return DRD_ERR_CUDA;
     return finish_call(c, KS_UV, st, true);
 }
@@ -2028,13 +2091,15 @@ int drd_velosolve_2_combined(drd_ctx* c, const double* psi1, const double* psi2,
 
 int drd_presolve_2(drd_ctx* c, const double* u, const double* v, double coef, double* psi, drd_status* st) {
     if (!c || !u || !v || !psi) return DRD_ERR_BADARG;
+    reset_q(c);
     CK(cudaEventRecord(c->ev0, c->s));
-    int rc = up(c, c->fld[DRD_F_U], u, c->us) | up(c, c->fld[DRD_F_V], v, c->vs);
+    int rc = up_q(c, c->fld[DRD_F_U], u, c->us) | up_q(c, c->fld[DRD_F_V], v, c->vs);
+    rc |= flush_q(c, c->hq_up);
     if (rc) return DRD_ERR_CUDA;
     rc = run_graph(c, gkey(GK_PRE, 0, 0), [&](cudaStream_t s) { enq_pre(c, c->fld[DRD_F_PSI2], s); return DRD_OK; },
                    0.0, coef);
     if (rc) return rc;
-    if (down(c, psi, c->fld[DRD_F_PSI2], c->cs)) return DRD_ERR_CUDA;
+    if (down_q(c, psi, c->fld[DRD_F_PSI2], c->cs) | flush_q(c, c->hq_down)) return DRD_ERR_CUDA;
     return finish_call(c, 0, st, false);
 }
 
@@ -2324,7 +2389,7 @@ int drd_kernel_bench(drd_ctx* c, int which, int reps, double* us, double* bytes,
 
 int drd_host_register(void* p, int64_t bytes) {
     if (!p || bytes <= 0) return DRD_ERR_BADARG;
-    const cudaError_t e = cudaHostRegister(p, (size_t)bytes, cudaHostRegisterDefault);
+    const cudaError_t e = cudaHostRegister(p, (size_t)bytes, cudaHostRegisterMapped);
     if (e != cudaSuccess) { cudaGetLastError(); return DRD_ERR_CUDA; }
     return DRD_OK;
 }
