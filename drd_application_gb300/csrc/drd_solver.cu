@@ -15,6 +15,7 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -1123,21 +1124,26 @@ int down(drd_ctx* c, double* dst, const double* src, long n) {
     return DRD_OK;
 }
 
-// The device address of host array [p, p + n) when the whole range lies in mapped, page-locked
-// host memory (drd_host_register, cudaHostAlloc) with one contiguous device mapping, else null.
+// The host ranges page-locked and mapped through drd_host_register: start -> (bytes, device
+// address of start).  A per-routine call looks its arrays up here, without a driver call.
+struct HostRange {
+    size_t bytes;
+    char* dev;
+};
+std::mutex g_host_mu;
+std::map<uintptr_t, HostRange> g_host_ranges;
+
+// The device address of host array [p, p + n) when the whole range lies in one range
+// registered by drd_host_register, else null.
 double* mapped_range(const double* p, long n) {
-    cudaPointerAttributes a0{}, a1{};
-    if (n <= 0 || cudaPointerGetAttributes(&a0, p) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
-    }
-    if (a0.type != cudaMemoryTypeHost || a0.devicePointer == nullptr) return nullptr;
-    if (cudaPointerGetAttributes(&a1, p + (n - 1)) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
-    }
-    if (a1.type != cudaMemoryTypeHost || (double*)a1.devicePointer != (double*)a0.devicePointer + (n - 1)) return nullptr;
-    return (double*)a0.devicePointer;
+    if (n <= 0) return nullptr;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    std::lock_guard<std::mutex> lock(g_host_mu);
+    auto it = g_host_ranges.upper_bound(a);
+    if (it == g_host_ranges.begin()) return nullptr;
+    --it;
+    if (a + sizeof(double) * (size_t)n > it->first + it->second.bytes) return nullptr;
+    return reinterpret_cast<double*>(it->second.dev + (a - it->first));
 }
 
 // Host-to-device copy of a per-routine call's input: queued for the call's one gather launch
@@ -2389,13 +2395,25 @@ int drd_kernel_bench(drd_ctx* c, int which, int reps, double* us, double* bytes,
 
 int drd_host_register(void* p, int64_t bytes) {
     if (!p || bytes <= 0) return DRD_ERR_BADARG;
-    const cudaError_t e = cudaHostRegister(p, (size_t)bytes, cudaHostRegisterMapped);
+    cudaError_t e = cudaHostRegister(p, (size_t)bytes, cudaHostRegisterMapped);
     if (e != cudaSuccess) { cudaGetLastError(); return DRD_ERR_CUDA; }
+    void* dev = nullptr;
+    e = cudaHostGetDevicePointer(&dev, p, 0);
+    if (e != cudaSuccess || dev == nullptr) {
+        cudaGetLastError();  // page-locked but not mapped: the calls copy it by DMA
+        return DRD_OK;
+    }
+    std::lock_guard<std::mutex> lock(g_host_mu);
+    g_host_ranges[reinterpret_cast<uintptr_t>(p)] = HostRange{(size_t)bytes, static_cast<char*>(dev)};
     return DRD_OK;
 }
 
 int drd_host_unregister(void* p) {
     if (!p) return DRD_ERR_BADARG;
+    {
+        std::lock_guard<std::mutex> lock(g_host_mu);
+        g_host_ranges.erase(reinterpret_cast<uintptr_t>(p));
+    }
     const cudaError_t e = cudaHostUnregister(p);
     if (e != cudaSuccess) { cudaGetLastError(); return DRD_ERR_CUDA; }
     return DRD_OK;
