@@ -38,8 +38,9 @@ def _staging(tma):
 
 
 @pytest.mark.parametrize("tma", [True, False])
-@pytest.mark.parametrize("nr,nz", [(97, 53), (420, 180), (512, 256)])
+@pytest.mark.parametrize("nr,nz", [(97, 53), (420, 180), (512, 256), (128, 97)])
 def test_tc_ch_psolve_matches_oracle(cuda_lib, oracle_build, nr, nz, tma):
+    """(128, 97): the z pass's fold has its middle point k = L / 2 = 48 inside a TMA chunk."""
     P = abi.default_params(nr, nz)
     P.dr, P.dz, P.dt = 3.5 / nr, 1.5 / nz, 1e-3
     P.precision = F.DRD_PREC_MIXED
