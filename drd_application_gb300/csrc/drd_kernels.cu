@@ -1372,9 +1372,11 @@ static const GemmCfg kGemmCfgs[] = {{"64x64x16/4x4"},         {"32x64x16/2x4"}, 
 // tcgen05.mma kind::tf32 three times into one FP32 accumulator in TMEM: lo(A) hi(B),
 // hi(A) lo(B), hi(A) hi(B), the products of FP32 operands up to the lo lo term.  One thread
 // issues the MMAs; the operands are in shared memory in the K-major, unswizzled core-matrix
-// layout (8 rows x 16 bytes, i.e. 4 TF32 values); two stages alternate, tracked by mbarriers
-// that tcgen05.commit arrives on.  Waits are bounded: a wait that gives up sets *err and the
-// tile's outputs are written as NaN, which the solve's FP64 residual then reports.
+// layout (8 rows x 16 bytes, i.e. 4 TF32 values), in stages tracked by mbarriers that
+// tcgen05.commit arrives on.  Two kernels: k_gemm_tc_tma (data operand by TMA boxes,
+// warp-specialised) where the data rows are 16-byte aligned, k_gemm_tc (data operand staged
+// through registers by all threads) otherwise.  Waits are bounded: a wait that gives up sets
+// *err and the tile's outputs are written as NaN, which the solve's FP64 residual then reports.
 constexpr int kGtcThreads = 512;  // 16 warps: all stage; warp w reads TMEM lanes 32 (w % 4), columns 32 (w / 4)
 constexpr int kGtcM = 128, kGtcN = 128, kGtcK = 32;
 constexpr uint32_t kGtcOp = kGtcM * kGtcK * 4;        // bytes of one operand part (hi or lo), 16 KB
@@ -1505,10 +1507,12 @@ __global__ void k_gtc_pack(const float* __restrict__ ev, const float* __restrict
     }
 }
 long gemm_tc_pack(const float* even, const float* odd, int rows_e, int rows_o, int K, long ld, int b_style,
-                  float* out, cudaStream_t s) {
+                  float* out, int* tiles_out, int* chunks_out, cudaStream_t s) {
     const int rows = rows_e > rows_o ? rows_e : rows_o;
     const int tiles = (rows + kGtcM - 1) / kGtcM, chunks = (K + kGtcK - 1) / kGtcK;
     const long n = 2L * tiles * chunks * 2 * kGtcM * kGtcK;
+    if (tiles_out) *tiles_out = tiles;
+    if (chunks_out) *chunks_out = chunks;
     if (out) k_gtc_pack<<<256, 256, 0, s>>>(even, odd, rows_e, rows_o, K, ld, b_style, tiles, chunks, out);
     return n;
 }

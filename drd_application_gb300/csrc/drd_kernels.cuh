@@ -58,9 +58,10 @@ struct GemmArgs {
 // Packs the constant operand of a folded transform for k_gemm_tc: rows r (its N for FOLD_A, its
 // M for FOLD_B) of the even and odd matrices, K values each; b_style: the matrices are K x rows
 // (B of FOLD_A, row stride ld), else rows x K (A of FOLD_B).  Returns the floats written, or the
-// floats needed when out is null.
+// floats needed when out is null; *tiles and *chunks receive the 128-row tiles and 32-K chunks of
+// the layout.
 long gemm_tc_pack(const float* even, const float* odd, int rows_e, int rows_o, int K, long ld, int b_style,
-                  float* out, cudaStream_t s);
+                  float* out, int* tiles, int* chunks, cudaStream_t s);
 enum Fold : int { FOLD_NONE = 0, FOLD_A = 1, FOLD_B = 2 };
 int gemm_config_count(int fp64);
 // FP32 transform GEMM configuration that runs on the tensor cores (3xTF32 tcgen05); the FP32

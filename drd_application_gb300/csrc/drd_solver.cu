@@ -1405,11 +1405,9 @@ int setup_context(drd_ctx* c) {
         // the tensor-core GEMM's packed constant operands (TF32 hi / lo, shared-memory block order)
         auto pack = [&](const float* ev, const float* od, int re, int ro, int K, long ld, int bst, float** out,
                         int* tiles, int* chunks) -> int {
-            const long n = gemm_tc_pack(ev, od, re, ro, K, ld, bst, nullptr, c->s);
+            const long n = gemm_tc_pack(ev, od, re, ro, K, ld, bst, nullptr, tiles, chunks, c->s);
             CK(cudaMalloc(out, sizeof(float) * n));
-            gemm_tc_pack(ev, od, re, ro, K, ld, bst, *out, c->s);
-            *tiles = ((re > ro ? re : ro) + 127) / 128;
-            *chunks = (K + 31) / 32;
+            gemm_tc_pack(ev, od, re, ro, K, ld, bst, *out, nullptr, nullptr, c->s);
             return DRD_OK;
         };
         int rc = pack(c->f1xe32, c->f1xo32, c->Nxe, c->Nxo, c->Kx, c->Nxe, 1, &c->pk_x, &c->pkx_t, &c->pkx_c);
