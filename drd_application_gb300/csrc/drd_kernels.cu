@@ -211,6 +211,70 @@ __global__ void k_ch_mv2(OpScal<T> o, const T* __restrict__ Mi, const T* __restr
     if (dot1 != nullptr || self2) emit_partials<DRD_TPB>(a1, a2, dot1 != nullptr, self2, d, slot1);
 }
 
+// The FP32 CH operator in one pass over 64 x 8 cell tiles (the mixed mode's inner operator):
+// x and M0 for the tile with a halo of two cells, Mi with a halo of one, staged in shared
+// memory; ff1 = -(dt xld) L_M0(x) on the tile and its one-cell halo into shared memory; then
+// y = alpha (x + s ff1/eps - eps L_Mi(ff1)) + beta y on the tile, with the same op_dgn
+// expressions as k_ch_mv1 / k_ch_mv2 (read through shared-memory accessors), so y is the same
+// bit for bit; ff1 never goes to global memory.  Blocks loop over the tiles; each block emits one
+// partial per dot product.
+constexpr int kChTX = 64, kChTY = 8;
+constexpr int kChXW = kChTX + 4, kChXH = kChTY + 4;  // x, M0: tile + 2
+constexpr int kChFW = kChTX + 2, kChFH = kChTY + 2;  // ff1, Mi: tile + 1
+struct ChSm {  // a shared-memory rectangle of a field addressed by global cell (i, k)
+    const float* p; int i0, k0, w;
+    __device__ __forceinline__ float operator()(int i, int k) const { return p[(k - k0) * w + (i - i0)]; }
+};
+__global__ void __launch_bounds__(DRD_TPB) k_ch_mv_tile(OpScal<float> o, const float* __restrict__ M0,
+                                                        const float* __restrict__ Mi, const float* __restrict__ x,
+                                                        float alpha, float beta, float* y, const float* dot1, int self2,
+                                                        Dots d, int slot1, const KState* ks, int gate, ull* ctr) {
+    __shared__ float sx[kChXH * kChXW], sm0[kChXH * kChXW], smi[kChFH * kChFW], sf[kChFH * kChFW];
+    count_launch(ctr);
+    if (gate_closed(ks, gate)) return;
+    const int nr = o.nr, nz = o.nz, tid = threadIdx.x;
+    const int tx = (nr + kChTX - 1) / kChTX, ntiles = tx * ((nz + kChTY - 1) / kChTY);
+    double a1 = 0.0, a2 = 0.0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int i0 = (tile % tx) * kChTX, k0 = (tile / tx) * kChTY;
+        // stage (cells outside the domain are never read by op_dgn: 0)
+        for (int e = tid; e < kChXH * kChXW; e += DRD_TPB) {
+            const int i = i0 - 2 + e % kChXW, k = k0 - 2 + e / kChXW;
+            const bool in = i >= 0 && i < nr && k >= 0 && k < nz;
+            sx[e] = in ? x[i + (long)nr * k] : 0.f;
+            sm0[e] = in ? M0[cidx(nr, i, k)] : 0.f;
+        }
+        for (int e = tid; e < kChFH * kChFW; e += DRD_TPB) {
+            const int i = i0 - 1 + e % kChFW, k = k0 - 1 + e / kChFW;
+            smi[e] = (i >= 0 && i < nr && k >= 0 && k < nz) ? Mi[cidx(nr, i, k)] : 0.f;
+        }
+        __syncthreads();
+        const ChSm X{sx, i0 - 2, k0 - 2, kChXW}, M{sm0, i0 - 2, k0 - 2, kChXW};
+        for (int e = tid; e < kChFH * kChFW; e += DRD_TPB) {
+            const int i = i0 - 1 + e % kChFW, k = k0 - 1 + e / kChFW;
+            sf[e] = (i >= 0 && i < nr && k >= 0 && k < nz)
+                        ? -(o.dtxld * op_dgn<float>(i, k, nr, nz, o.idr2, o.idz2, X, M))
+                        : 0.f;
+        }
+        __syncthreads();
+        const ChSm F{sf, i0 - 1, k0 - 1, kChFW}, MI{smi, i0 - 1, k0 - 1, kChFW};
+        for (int e = tid; e < kChTX * kChTY; e += DRD_TPB) {
+            const int i = i0 + e % kChTX, k = k0 + e / kChTX;
+            if (i >= nr || k >= nz) continue;
+            const long q = i + (long)nr * k;
+            const float f = F(i, k);
+            const float a = o.s * f / o.eps - o.eps * op_dgn<float>(i, k, nr, nz, o.idr2, o.idz2, F, MI);
+            const float av = X(i, k) + a;
+            const float yn = (beta == 0.f) ? alpha * av : alpha * av + beta * y[q];
+            y[q] = yn;
+            if (dot1) a1 += (double)dot1[q] * (double)yn;
+            if (self2) a2 += (double)yn * (double)yn;
+        }
+        __syncthreads();
+    }
+    if (dot1 != nullptr || self2) emit_partials<DRD_TPB>(a1, a2, dot1 != nullptr, self2, d, slot1);
+}
+
 // rmu_after interior (:85) and ph_after = f2 + dt xld L_M0(rmu_after) interior (:100-101).
 __global__ void k_ch_fin(DevParams P, const double* __restrict__ x, const double* __restrict__ f2,
                          const double* __restrict__ M0, double* __restrict__ rmu_after, double* __restrict__ ph_after,
@@ -4127,6 +4191,13 @@ void launch_ch_matvec(const OpScal<T>& o, const T* M0, const T* Mi, T alpha, con
                       const T* dot1, int self2, const Dots& d, int slot1, const KState* ks, int gate, ull* ctr,
                       cudaStream_t s) {
     const long n = (long)o.nr * o.nz;
+    if constexpr (sizeof(T) == 4) {  // FP32: the fused tiled pass
+        const int tiles = ((o.nr + kChTX - 1) / kChTX) * ((o.nz + kChTY - 1) / kChTY);
+        const int g = (dot1 || self2) ? d.G : std::min(tiles, 152 * 8);
+        k_ch_mv_tile<<<g, DRD_TPB, 0, s>>>(o, M0, Mi, x, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);
+        (void)ff1;
+        return;
+    }
     k_ch_mv1<T><<<GRID(n)>>>(o, M0, x, ff1, ks, gate, ctr);
     const int g = (dot1 || self2) ? d.G : grid_for(n);
     k_ch_mv2<T><<<g, DRD_TPB, 0, s>>>(o, Mi, x, ff1, alpha, beta, y, dot1, self2, d, slot1, ks, gate, ctr);

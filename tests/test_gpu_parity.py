@@ -87,6 +87,24 @@ def test_operators_fp32_close(mf_case):
     ctx.close()
 
 
+@pytest.mark.parametrize("nr,nz", [(97, 53), (130, 17), (420, 180)])
+def test_ch_operator_fp32_tiles(cuda_lib, oracle_build, nr, nz):
+    """The FP32 CH operator (one tiled pass over 64 x 8 cells) on grids of several tiles with
+    ragged right and top edges, against the oracle's FP64 operator."""
+    from drd_application_gb300.workloads import make_case
+
+    case = make_case("c2", seed=nr, nr=nr, nz=nz)
+    ctx, orc = _ctx(case)
+    try:
+        k = case.coefs
+        rng = np.random.default_rng(nz)
+        for x in (rng.standard_normal(nr * nz), np.sin(np.arange(nr * nz) * 0.01)):
+            y = ctx.op_apply(F.DRD_OP_CH_MATVEC, x, precision=F.DRD_PREC_MIXED)
+            assert rel_err(y, orc.ch_matvec(k["M0"], k["Mi"], x)) < 2e-6
+    finally:
+        ctx.close()
+
+
 def test_phmu_operators_fp64(tp_case):
     case, st, t = tp_case
     ctx, orc = _ctx(case)
