@@ -103,7 +103,8 @@ struct drd_ctx {
     // persistent cooperative inner solver (FP32 CH): grid size, barrier state, on/off
     int persist = 0, pgrid = 0;
     int persist_ch = 0;  // the CH solve too: only when its transform operands stay in shared memory
-    int persist_esolp = 0;      // the momentum solve with ESOLP_x too (its shared-memory work area fits)
+    int persist_esolp = 0;      // the momentum kernel can run ESOLP_x (its shared-memory work area fits)
+    int persist_esolp_solve = 0;  // ... and the momentum solve with ESOLP_x uses it (resident B panels)
     PbPlan eplan{};
     // mixed mode: the CH system is too stiff for FP32 Krylov vectors and is solved in FP64
     int ch_fp64 = 0;
@@ -718,6 +719,14 @@ int setup_persist(drd_ctx* c) {
     // per FP32 iteration against 2 ms.
     c->persist_ch = c->pplan.b_res && c->pplan.z_res;
     if (!c->persist_ch) c->persist_err = "CH: the grid exceeds the resident shared-memory plan; the CH solve uses the kernel-per-phase loop";
+    // The same for the momentum solve with ESOLP_x: past the resident row-transform panels its
+    // persistent row passes stream their operands, and the kernel-per-phase loop's tuned GEMMs
+    // (the tensor-core passes at large grids) win: at 2048x1024 a solve took 85-92 ms there
+    // against 261-266 ms in the persistent kernel.
+    c->persist_esolp_solve = c->persist_esolp && c->eplan.b_res;
+    if (c->persist_esolp && !c->persist_esolp_solve)
+        c->persist_err += std::string(c->persist_err.empty() ? "" : "; ") +
+                          "momentum: the row-transform panels exceed shared memory; the ESOLP_x solve uses the kernel-per-phase loop";
     const char* pe = std::getenv("DRD_PERSIST_PROF");
     c->pprof_on = pe && std::atoi(pe) != 0;
     return DRD_OK;
@@ -762,7 +771,7 @@ int enq_solve(drd_ctx* c, const Sys& S, int ks_slot, double tol, int maxit, int 
     Dots d = dots(c);
     int rc = DRD_OK;
     const bool persistent =
-        mixed && c->persist && ((S.kind == SYS_CH && c->persist_ch) || (S.kind == SYS_UV && (!S.esolp || c->persist_esolp)));
+        mixed && c->persist && ((S.kind == SYS_CH && c->persist_ch) || (S.kind == SYS_UV && (!S.esolp || c->persist_esolp_solve)));
     if (!persistent) launch_stamp(ks, 0, c->ctr, s);
     if (!mixed) {
         enq_sys_setup<double>(c, S, s);
