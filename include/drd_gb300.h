@@ -615,7 +615,8 @@ int drd_host_unregister(void* p);
  * phases of an iteration; 0 when it runs the captured kernel-per-phase loop (no cooperative
  * launch support, DRD_PERSIST=0 in the environment, or a graph that could not take the
  * cooperative launch).  `why` receives the reason for whatever does not use it, including a
- * grid past the CH solve's resident shared-memory plan, whose CH solve then uses the loop. */
+ * grid past the CH solve's resident shared-memory plan, or past the resident row-transform
+ * panels of the momentum solve with ESOLP_x, whose solve then uses the loop. */
 int drd_persistent_solver(drd_ctx* ctx, char* why, int len);
 /* With DRD_PERSIST_PROF=1 in the environment at drd_create, the persistent solver records
  * %globaltimer (ns) at entry and exit of each grid barrier of its third iteration, as seen by
