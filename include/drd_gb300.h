@@ -602,11 +602,12 @@ int drd_kernel_bench(drd_ctx* ctx, int which, int reps, double* us_per_launch, d
 /* Writes `bytes` of scratch memory on the context stream (evicts L2 between timed steps). */
 int drd_flush_l2(drd_ctx* ctx, int64_t bytes);
 
-/* Page-locks and maps `bytes` of the caller's host memory at p (cudaHostRegister, mapped): the
- * per-routine calls then move every registered array argument in one gather launch in and one
- * scatter launch out through the mapped addresses (other arrays: DMA copies); a driver that
- * registers its module arrays once after allocating them makes every later call's copies
- * faster.  Unregister before freeing. */
+/* Page-locks and maps `bytes` of the caller's host memory at p (cudaHostRegister, mapped) and
+ * records the range with its device address: the per-routine calls then move every array
+ * argument that lies in a recorded range in one gather launch in and one scatter launch out
+ * through the mapped addresses (other arrays, including memory page-locked by other means:
+ * cudaMemcpyAsync); a driver that registers its module arrays once after allocating them makes
+ * every later call's copies faster.  Unregister (which drops the record) before freeing. */
 int drd_host_register(void* p, int64_t bytes);
 int drd_host_unregister(void* p);
 
