@@ -38,8 +38,8 @@ def _out(a, shape, name):
 
 
 def pin(a, lib=None):
-    """Page-lock a numpy array's memory (drd_host_register): the per-routine calls then copy it by
-    DMA.  Unpin it (unpin) before it is freed."""
+    """Page-lock and map a numpy array's memory (drd_host_register): the per-routine calls then
+    read or write it in their one gather / scatter launch.  Unpin it (unpin) before it is freed."""
     L = lib or _lib.load()
     if not isinstance(a, np.ndarray) or not a.flags["C_CONTIGUOUS"]:
         raise ValueError("pin: expected a C-contiguous numpy array")
