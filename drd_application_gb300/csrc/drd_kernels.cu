@@ -1825,7 +1825,9 @@ __device__ __forceinline__ bool gtr_wait(uint32_t bar, uint32_t parity, const vo
 // twelve MMAs and commit them, wait for chunk c - 1's MMAs and refill their constant stage with
 // chunk c + 2).  No block-wide barrier inside the K loop: conversion of chunk c + 1 overlaps
 // the MMAs of chunk c.
-template <int EPI>
+// PF (pre-folded, FOLD_A only): the tensor map addresses the folded even operand in rows
+// [0, M) and the odd one in rows [M, 2M) (gtr_prefold), one box per chunk and no fold here.
+template <int EPI, bool PF>
 __global__ void __launch_bounds__(kGtrThreads) k_gemm_tc_tma(GemmArgs<float> a, const __grid_constant__ CUtensorMap tm) {
     extern __shared__ __align__(1024) unsigned char gsm_raw[];
     __shared__ uint32_t tmem_base;
@@ -1895,6 +1897,12 @@ __global__ void __launch_bounds__(kGtrThreads) k_gemm_tc_tma(GemmArgs<float> a, 
             for (int it = 0; it < GTC_NI; ++it) {
                 const int item = tid + it * kGtcThreads, r = item % kGtcM, kg = item / kGtcM;
                 float a0[4], a1[4], v[4];
+                if (PF) {  // the folded value itself (zeros past K)
+                    const float4 x0 = *reinterpret_cast<const float4*>(r0 + r * 128 + ((kg ^ (r & 7)) << 4));
+                    v[0] = x0.x; v[1] = x0.y; v[2] = x0.z; v[3] = x0.w;
+                    gtc_put4(op, op + kGtcOp, r, kg, v);
+                    continue;
+                }
                 if (fa) {
                     const float4 x0 = *reinterpret_cast<const float4*>(r0 + r * 128 + ((kg ^ (r & 7)) << 4));
                     const float4 x1 = *reinterpret_cast<const float4*>(r1 + r * 128 + (((7 - kg) ^ (r & 7)) << 4));
@@ -1935,8 +1943,11 @@ __global__ void __launch_bounds__(kGtrThreads) k_gemm_tc_tma(GemmArgs<float> a, 
             const uint32_t rb = (uint32_t)__cvta_generic_to_shared(&rbar[rs]);
             const uint32_t dst = raw0 + rs * kGtrRawStage;
             const int k0 = cc * kGtcK, k1 = L - k0 - (kGtcK - 1);
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(rb), "r"(kGtrRawStage) : "memory");
-            if (fa) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(rb),
+                         "r"(PF ? kGtrBox : kGtrRawStage) : "memory");
+            if (PF) {
+                gtr_box(dst, &tm, k0, g.par * a.M + m0, rb);
+            } else if (fa) {
                 gtr_box(dst, &tm, k0, m0, rb);
                 gtr_box(dst + kGtrBox, &tm, k1, m0, rb);
             } else {
@@ -2070,23 +2081,78 @@ static bool gtr_map(const GemmArgs<float>& a, CUtensorMap* tm) {
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Pre-pass of the pre-folded tensor-core GEMM (FOLD_A rows that TMA cannot address): rows
+// [0, M) of `out` receive the even-folded operand x[j] + x[L - j] (x[j] at the middle point
+// j = L / 2), rows [M, 2M) the odd one x[j] - x[L - j] (0 at the middle point), for j < K, and
+// zeros in [K, ld): the values GemmView::loadA and the TMA kernel's fold form.
+__global__ void k_gtr_prefold(const float* __restrict__ X, long lda, int M, int L, int K, int ld,
+                              float* __restrict__ out) {
+    const long tot = (long)M * ld;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tot; e += (long)gridDim.x * blockDim.x) {
+        const int m = (int)(e / ld), j = (int)(e % ld);
+        float ev = 0.f, od = 0.f;
+        if (j < K) {
+            const float* row = X + (long)m * lda;
+            const float x0 = row[j];
+            if (2 * j == L) {
+                ev = x0;
+            } else {
+                const float x1 = row[L - j];
+                ev = x0 + x1;
+                od = x0 - x1;
+            }
+        }
+        out[e] = ev;
+        out[tot + e] = od;
+    }
+}
+
+// The pre-folded form for a FOLD_A pass that gtr_map refuses: runs the pre-pass into a.pad and
+// encodes the tensor map of its 2M rows of ld = K rounded up to 4 values; false when there is no
+// scratch (or too little), no packed operand or no encoder.
+static bool gtr_prefold(const GemmArgs<float>& a, CUtensorMap* tm, cudaStream_t s) {
+    if (a.fold != FOLD_A || !a.packed || !a.pad) return false;
+    GtrEncodeFn enc = gtr_encoder();
+    if (!enc) return false;
+    const int ld = (a.K + 3) & ~3;
+    if (2L * a.M * ld > a.pad_cap || (reinterpret_cast<uintptr_t>(a.pad) & 15)) return false;
+    cuuint64_t dim[2] = {(cuuint64_t)ld, 2 * (cuuint64_t)a.M}, stride[1] = {(cuuint64_t)ld * 4};
+    cuuint32_t box[2] = {kGtcK, kGtcM}, es[2] = {1, 1};
+    if (enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, a.pad, dim, stride, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const long tot = (long)a.M * ld;
+    const int blocks = (int)std::min<long>((tot + 255) / 256, 152L * 8);
+    k_gtr_prefold<<<blocks, 256, 0, s>>>(a.A, a.lda, a.M, a.Lf, a.K, ld, a.pad);
+    return true;
+}
+
 static void gemm_tc_launch(int epi, const GemmArgs<float>& a, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(k_gemm_tc<EPI_STORE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtcSmem);
         cudaFuncSetAttribute(k_gemm_tc<EPI_DIV_TAB>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtcSmem);
-        cudaFuncSetAttribute(k_gemm_tc_tma<EPI_STORE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtrSmem);
-        cudaFuncSetAttribute(k_gemm_tc_tma<EPI_DIV_TAB>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtrSmem);
+        cudaFuncSetAttribute(k_gemm_tc_tma<EPI_STORE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtrSmem);
+        cudaFuncSetAttribute(k_gemm_tc_tma<EPI_DIV_TAB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtrSmem);
+        cudaFuncSetAttribute(k_gemm_tc_tma<EPI_STORE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtrSmem);
+        cudaFuncSetAttribute(k_gemm_tc_tma<EPI_DIV_TAB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGtrSmem);
         attr = true;
     }
     const int M = a.fold == FOLD_B ? (a.M > a.M_odd ? a.M : a.M_odd) : a.M;
     const int N = a.fold == FOLD_A ? (a.N > a.N_odd ? a.N : a.N_odd) : a.N;
     dim3 grid((N + kGtcN - 1) / kGtcN, (M + kGtcM - 1) / kGtcM, a.fold ? 2 : 1);
     alignas(64) CUtensorMap tm;
-    if (!std::getenv("DRD_GEMM_TC_NOTMA") && gtr_map(a, &tm)) {  // the variable selects the fallback (tests)
-        if (epi == EPI_DIV_TAB) k_gemm_tc_tma<EPI_DIV_TAB><<<grid, kGtrThreads, kGtrSmem, s>>>(a, tm);
-        else k_gemm_tc_tma<EPI_STORE><<<grid, kGtrThreads, kGtrSmem, s>>>(a, tm);
-        return;
+    if (!std::getenv("DRD_GEMM_TC_NOTMA")) {  // the variable selects the register-staged fallback (tests)
+        if (gtr_map(a, &tm)) {
+            if (epi == EPI_DIV_TAB) k_gemm_tc_tma<EPI_DIV_TAB, false><<<grid, kGtrThreads, kGtrSmem, s>>>(a, tm);
+            else k_gemm_tc_tma<EPI_STORE, false><<<grid, kGtrThreads, kGtrSmem, s>>>(a, tm);
+            return;
+        }
+        if (gtr_prefold(a, &tm, s)) {
+            if (epi == EPI_DIV_TAB) k_gemm_tc_tma<EPI_DIV_TAB, true><<<grid, kGtrThreads, kGtrSmem, s>>>(a, tm);
+            else k_gemm_tc_tma<EPI_STORE, true><<<grid, kGtrThreads, kGtrSmem, s>>>(a, tm);
+            return;
+        }
     }
     if (epi == EPI_DIV_TAB) k_gemm_tc<EPI_DIV_TAB><<<grid, kGtcThreads, kGtcSmem, s>>>(a);
     else k_gemm_tc<EPI_STORE><<<grid, kGtcThreads, kGtcSmem, s>>>(a);

@@ -54,6 +54,11 @@ struct GemmArgs {
     // brought in by one bulk copy per K chunk; null: staged by the threads like the data
     const float* packed;
     int pk_tiles, pk_chunks;
+    // the tensor-core GEMM, FOLD_A with rows TMA cannot address (a row stride or row length not a
+    // multiple of 16 bytes): scratch of pad_cap floats for the folded even and odd operands, laid
+    // out for TMA by a pre-pass (null: the register-staged kernel runs)
+    float* pad;
+    long pad_cap;
 };
 // Packs the constant operand of a folded transform for k_gemm_tc: rows r (its N for FOLD_A, its
 // M for FOLD_B) of the even and odd matrices, K values each; b_style: the matrices are K x rows

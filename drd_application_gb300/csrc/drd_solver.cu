@@ -117,6 +117,9 @@ struct drd_ctx {
     // pass, ESOLP_x's u rows; tiles and K chunks of each
     float *pk_x = nullptr, *pk_z = nullptr, *pk_u = nullptr;
     int pkx_t = 0, pkx_c = 0, pkz_t = 0, pkz_c = 0, pku_t = 0, pku_c = 0;
+    // its scratch for the pre-folded operand of x passes whose rows TMA cannot address
+    float* tc_pad = nullptr;
+    long tc_pad_cap = 0;
     unsigned long long* pprof = nullptr;  // DRD_PERSIST_PROF=1: barrier timestamps of block 0
     int pprof_on = 0;
     KState* ks;      // device, KS_COUNT entries
@@ -419,7 +422,10 @@ GemmArgs<T> dct1_xpass(drd_ctx* c, const T* X, T* out, const KState* ks, int gat
     a.Lf = c->nr - 1;
     a.B_odd = fmat<T>(c, 1);
     a.N_odd = c->Nxo;
-    if (sizeof(T) == 4) { a.packed = c->pk_x; a.pk_tiles = c->pkx_t; a.pk_chunks = c->pkx_c; }
+    if (sizeof(T) == 4) {
+        a.packed = c->pk_x; a.pk_tiles = c->pkx_t; a.pk_chunks = c->pkx_c;
+        a.pad = (float*)c->tc_pad; a.pad_cap = c->tc_pad_cap;
+    }
     return a;
 }
 template <typename T>
@@ -466,6 +472,8 @@ GemmArgs<T> esolp_rows(drd_ctx* c, int M, int L, const T* X, T* out, const KStat
         a.packed = u ? c->pk_u : c->pk_x;
         a.pk_tiles = u ? c->pku_t : c->pkx_t;
         a.pk_chunks = u ? c->pku_c : c->pkx_c;
+        a.pad = (float*)c->tc_pad;
+        a.pad_cap = c->tc_pad_cap;
     }
     return a;
 }
@@ -1419,6 +1427,11 @@ int setup_context(drd_ctx* c) {
             gemm_tc_pack(ev, od, re, ro, K, ld, bst, *out, nullptr, nullptr, c->s);
             return DRD_OK;
         };
+        // the pre-folded operand: even and odd rows of up to nz + 1 rows (the u block) of the
+        // longest folded row rounded up to 4 values
+        const int kmax = std::max(c->Kx, c->Ku);
+        c->tc_pad_cap = 2L * (nz + 1) * ((kmax + 3) & ~3);
+        CK(cudaMalloc(&c->tc_pad, sizeof(float) * c->tc_pad_cap));
         int rc = pack(c->f1xe32, c->f1xo32, c->Nxe, c->Nxo, c->Kx, c->Nxe, 1, &c->pk_x, &c->pkx_t, &c->pkx_c);
         rc |= pack(c->f1ze32, c->f1zo32, c->Mze, c->Mzo, c->Kz, c->Kz, 0, &c->pk_z, &c->pkz_t, &c->pkz_c);
         rc |= pack(c->f1ue32, c->f1uo32, c->Nue, c->Nuo, c->Ku, c->Nue, 1, &c->pk_u, &c->pku_t, &c->pku_c);
@@ -1571,6 +1584,7 @@ int drd_destroy(drd_ctx* c) {
     if (c->pk_x) cudaFree(c->pk_x);
     if (c->pk_z) cudaFree(c->pk_z);
     if (c->pk_u) cudaFree(c->pk_u);
+    if (c->tc_pad) cudaFree(c->tc_pad);
     if (c->pcw) cudaFree(c->pcw);
     if (c->pcw32) cudaFree(c->pcw32);
     if (c->pnum) cudaFree(c->pnum);
