@@ -2,8 +2,9 @@
 FP32 passes of the kernel-per-phase loop, forced with DRD_GEMM_CFG: the CH preconditioner
 (folded DCT-I passes along x and z, the division by Ph_Lcc in an epilogue) and ESOLP_x's row
 passes, against the oracle's FP64 operators at FP32 accuracy.  Both stagings of the data
-operand run: TMA boxes (k_gemm_tc_tma, taken where rows are 16-byte aligned) and the register
-staging (k_gemm_tc, the fallback; DRD_GEMM_TC_NOTMA forces it)."""
+operand run: TMA boxes (k_gemm_tc_tma: straight from the data where rows are 16-byte aligned,
+else from the operand pre-folded into aligned scratch, as at 97x53 and for ESOLP_x's u rows of
+nr + 1) and the register staging (k_gemm_tc, the fallback; DRD_GEMM_TC_NOTMA forces it)."""
 import contextlib
 import os
 
